@@ -1,0 +1,32 @@
+"""adseismic_gb300 -- GB300 (sm_103a) implementation of ADSeismic's time-stepping
+hot path: acoustic and elastic one-step operators, their adjoints, source
+injection, receiver sampling, misfit and checkpointed multi-shot gradients.
+
+All compute runs in libadseismic_gb300.so (C ABI: include/adseismic_gb300.h).
+This package mirrors the reference's Julia interface on top of it.
+"""
+from . import _lib
+from ._lib import AdsError, ADS_F32, ADS_F64, ADS_VARIANT_U, ADS_VARIANT_W, lib
+from .build import build_library, LIB_PATH
+from .acoustic import (AcousticMisfit, AcousticOneStep, AcousticPlan, AcousticPropagator,
+                       AcousticPropagatorParams, AcousticPropagatorSolver, AcousticReceiver,
+                       AcousticSource, SimulatedObservation, acoustic_one_step,
+                       acoustic_one_step_grad, compute_loss_and_grads_GPU)
+from .acoustic import compute_PML_Params as compute_acoustic_PML_Params
+from .elastic import (ElasticPlan, ElasticPropagator, ElasticPropagatorParams,
+                      ElasticPropagatorSolver, ElasticReceiver, ElasticSource,
+                      elastic_one_step, elastic_one_step_grad)
+from .elastic import SimulatedObservation as ElasticSimulatedObservation
+from .elastic import compute_PML_Params as compute_elastic_PML_Params
+from .utils import (Gauss, Ricker, compute_lame_parameters, compute_properties,
+                    folded_layer_model, gaussian_smooth, layered_gaussian_model,
+                    ricker_width_samples)
+
+
+def version() -> str:
+    return lib().ads_version().decode()
+
+
+def launch_count() -> int:
+    """Number of this library's kernels launched by the process so far."""
+    return int(lib().ads_launch_count())

@@ -1,0 +1,321 @@
+"""Acoustic host API mirroring ADSeismic's src/Struct.jl / src/Core.jl / src/Utils.jl
+on top of the C ABI.
+
+Reference names are kept: AcousticPropagatorParams, AcousticSource,
+AcousticReceiver, AcousticPropagatorSolver, SimulatedObservation (Julia's
+``SimulatedObservation!``) and compute_loss_and_grads_GPU.  Device memory,
+streams and autograd come from PyTorch; every computation runs in
+libadseismic_gb300.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import ADS_F32, ADS_F64, ADS_VARIANT_U, ADS_VARIANT_W, call, lib
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _require_cuda(*ts):
+    for t in ts:
+        if t is not None and not t.is_cuda:
+            raise ValueError("tensors passed to the GPU operators must live on a CUDA device")
+
+
+@dataclass
+class AcousticPropagatorParams:
+    """src/Struct.jl:82-121 (same fields and defaults)."""
+    NX: int = 101
+    NY: int = 641
+    NSTEP: int = 2000 * 2
+    DELTAX: float = 10.0
+    DELTAY: float = 10.0
+    DELTAT: float = 2.0e-3 / 2
+    USE_PML_XMIN: bool = True
+    USE_PML_XMAX: bool = True
+    USE_PML_YMIN: bool = True
+    USE_PML_YMAX: bool = True
+    NPOINTS_PML: int = 12
+    NPOWER: int = 2
+    Rcoef: float = 0.001
+    vp_ref: float = 1000.0
+    IT_DISPLAY: int = 0
+    PropagatorKernel: int = 0
+
+    @property
+    def use_pml(self) -> int:
+        return (int(self.USE_PML_XMIN) | int(self.USE_PML_XMAX) << 1 |
+                int(self.USE_PML_YMIN) << 2 | int(self.USE_PML_YMAX) << 3)
+
+
+@dataclass
+class AcousticSource:
+    """src/Struct.jl:123-127; srci/srcj 1-based into the padded grid, srcv (NSTEP, nsrc)."""
+    srci: np.ndarray
+    srcj: np.ndarray
+    srcv: np.ndarray
+
+
+@dataclass
+class AcousticReceiver:
+    """src/Struct.jl:129-133; rcvv is filled by SimulatedObservation, (NSTEP+1, nrcv)."""
+    rcvi: np.ndarray
+    rcvj: np.ndarray
+    rcvv: object = None
+
+
+def compute_PML_Params(param: AcousticPropagatorParams):
+    """src/Core.jl:622-655: returns (Sigma_x, Sigma_y) as (NX+2, NY+2) arrays."""
+    sx = np.empty(param.NX + 2)
+    ty = np.empty(param.NY + 2)
+    call("ads_acoustic_pml_profiles", param.NX, param.NY, param.DELTAX, param.DELTAY,
+         param.NPOINTS_PML, param.vp_ref, param.Rcoef, param.use_pml,
+         sx.ctypes.data_as(C.c_void_p), ty.ctypes.data_as(C.c_void_p))
+    Sx = np.repeat(sx[:, None], param.NY + 2, axis=1)
+    Sy = np.repeat(ty[None, :], param.NX + 2, axis=0)
+    return Sx, Sy
+
+
+# ------------------------------------------------------------------ single step
+
+def acoustic_one_step(w, wold, phi, psi, sigma, tau, c, dt, hx, hy, NX, NY,
+                      variant=ADS_VARIANT_W):
+    """AcousticOneStep forward (deps/CustomOps/AcousticOneStep/AcousticOneStep.cpp:14-61)
+    on flat CUDA tensors of length (NX+2)(NY+2), float64 or float32."""
+    ts = [w, wold, phi, psi, sigma, tau, c]
+    _require_cuda(*ts)
+    dt_ = w.dtype
+    ts = [t.contiguous().to(dt_) for t in ts]
+    u, po, qo = (torch.empty_like(ts[0]) for _ in range(3))
+    name = "ads_acoustic_step_fwd_f64" if dt_ == torch.float64 else "ads_acoustic_step_fwd_f32"
+    call(name, *[_ptr(t) for t in ts], dt, hx, hy, NX, NY, _ptr(u), _ptr(po), _ptr(qo),
+         int(variant), _stream())
+    return u, po, qo
+
+
+def acoustic_one_step_grad(gu, gphi, gpsi, w, wold, phi, psi, sigma, tau, c, dt, hx, hy,
+                           NX, NY, u, phiout, psiout, variant=ADS_VARIANT_W):
+    """AcousticOneStepGrad (AcousticOneStep.cpp:63-93): returns grad_w, grad_wold,
+    grad_phi, grad_psi, grad_c (grad_sigma/tau/dt/hx/hy are never produced by the
+    reference either)."""
+    dt_ = w.dtype
+    ins = [t.contiguous().to(dt_) for t in (gu, gphi, gpsi, w, wold, phi, psi, sigma, tau, c)]
+    tail = [t.contiguous().to(dt_) for t in (u, phiout, psiout)]
+    _require_cuda(*ins, *tail)
+    outs = [torch.empty_like(ins[3]) for _ in range(5)]
+    name = "ads_acoustic_step_bwd_f64" if dt_ == torch.float64 else "ads_acoustic_step_bwd_f32"
+    call(name, *[_ptr(t) for t in outs], *[_ptr(t) for t in ins], dt, hx, hy, NX, NY,
+         *[_ptr(t) for t in tail], int(variant), _stream())
+    return tuple(outs)
+
+
+class AcousticOneStep(torch.autograd.Function):
+    """The custom operator with its registered gradient (load_op_and_grad in
+    src/Core.jl:483-502): forward and backward both run the CUDA kernels."""
+
+    @staticmethod
+    def forward(ctx, w, wold, phi, psi, sigma, tau, c, dt, hx, hy, NX, NY, variant=0):
+        u, po, qo = acoustic_one_step(w, wold, phi, psi, sigma, tau, c, dt, hx, hy, NX, NY,
+                                      variant)
+        ctx.save_for_backward(w, wold, phi, psi, sigma, tau, c, u, po, qo)
+        ctx.k = (dt, hx, hy, NX, NY, variant)
+        return u, po, qo
+
+    @staticmethod
+    def backward(ctx, gu, gp, gq):
+        w, wold, phi, psi, sigma, tau, c, u, po, qo = ctx.saved_tensors
+        dt, hx, hy, NX, NY, variant = ctx.k
+        z = torch.zeros_like(w)
+        gu = z if gu is None else gu
+        gp = z if gp is None else gp
+        gq = z if gq is None else gq
+        gw, gwo, gph, gps, gc = acoustic_one_step_grad(gu, gp, gq, w, wold, phi, psi, sigma,
+                                                       tau, c, dt, hx, hy, NX, NY, u, po, qo,
+                                                       variant)
+        return gw, gwo, gph, gps, None, None, gc, None, None, None, None, None, None
+
+
+# ------------------------------------------------------------------ whole path
+
+class AcousticPlan:
+    """A persistent multi-shot plan (forward traces, misfit, gradient).
+
+    shots: list of dicts with keys x0, nx, nstep, srci, srcj, srcv, rcvi, rcvj
+    (window-local, 1-based indices).  The model vp is (MX+2, MY+2)."""
+
+    def __init__(self, MX, MY, dx, dy, dt, shots, npml=12, Rcoef=0.001, vp_ref=1000.0,
+                 use_pml=15, precision="f64", use_graph=True, ckpt_every=0,
+                 rows_per_thread=0, stream=None):
+        cfg = _lib.AcousticConfig()
+        cfg.MX, cfg.MY, cfg.dx, cfg.dy, cfg.dt = MX, MY, dx, dy, dt
+        cfg.npml, cfg.Rcoef, cfg.vp_ref, cfg.use_pml = npml, Rcoef, vp_ref, use_pml
+        cfg.precision = ADS_F64 if precision == "f64" else ADS_F32
+        cfg.variant = ADS_VARIANT_W
+        cfg.use_graph = int(bool(use_graph))
+        cfg.ckpt_every = ckpt_every
+        cfg.rows_per_thread = rows_per_thread
+        self.MX, self.MY = MX, MY
+        self.precision = precision
+        self.dtype = torch.float64 if precision == "f64" else torch.float32
+        self._keep = []
+        arr = (_lib.AcousticShot * len(shots))()
+        for k, s in enumerate(shots):
+            srci = np.ascontiguousarray(s["srci"], dtype=np.int64)
+            srcj = np.ascontiguousarray(s["srcj"], dtype=np.int64)
+            srcv = np.ascontiguousarray(s["srcv"], dtype=np.float64)
+            srcv = srcv.reshape(-1, len(srci)) if len(srci) else np.zeros((0, 1))
+            rcvi = np.ascontiguousarray(s["rcvi"], dtype=np.int64)
+            rcvj = np.ascontiguousarray(s["rcvj"], dtype=np.int64)
+            self._keep += [srci, srcj, srcv, rcvi, rcvj]
+            a = arr[k]
+            a.x0, a.nx, a.nstep = s.get("x0", 0), s["nx"], s["nstep"]
+            a.nsrc = len(srci)
+            a.srci, a.srcj = srci.ctypes.data, srcj.ctypes.data
+            a.srcv, a.srcv_rows = srcv.ctypes.data, srcv.shape[0] if len(srci) else 0
+            a.nrcv = len(rcvi)
+            a.rcvi, a.rcvj = rcvi.ctypes.data, rcvj.ctypes.data
+        self.nshots = len(shots)
+        self.shots = shots
+        h = C.c_void_p()
+        st = stream if stream is not None else _stream()
+        call("ads_acoustic_plan_create", C.byref(h), C.byref(cfg), arr, len(shots), st)
+        self._h = h
+        L = lib()
+        self.trace_count = L.ads_acoustic_plan_trace_count(h)
+        self.trace_offsets = [L.ads_acoustic_plan_trace_offset(h, k) for k in range(len(shots))]
+        self.device_bytes = L.ads_acoustic_plan_device_bytes(h)
+        self.launches_forward = L.ads_acoustic_plan_launches(h, 0)
+        self.launches_gradient = L.ads_acoustic_plan_launches(h, 1)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ads_acoustic_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def loop_timing(self):
+        """Device-timed loops of the last forward + gradient calls:
+        {'forward'|'recompute'|'adjoint': (ms, launches, interior cell-steps)}."""
+        out = np.zeros(9)
+        call("ads_acoustic_plan_loop_timing", self._h, out.ctypes.data_as(C.c_void_p))
+        return {k: tuple(out[3 * i:3 * i + 3])
+                for i, k in enumerate(("forward", "recompute", "adjoint"))}
+
+    def split_traces(self, packed):
+        """Packed trace buffer -> list of (nstep+1, nrcv) views per shot."""
+        out = []
+        for k, s in enumerate(self.shots):
+            n = (s["nstep"] + 1) * len(s["rcvi"])
+            o = self.trace_offsets[k]
+            out.append(packed[o:o + n].view(s["nstep"] + 1, len(s["rcvi"])))
+        return out
+
+    def pack(self, per_shot):
+        return torch.cat([t.reshape(-1).to(self.dtype) for t in per_shot])
+
+    def forward(self, vp):
+        _require_cuda(vp)
+        vp = vp.contiguous().to(torch.float64)
+        tr = torch.empty(max(self.trace_count, 1), dtype=self.dtype, device=vp.device)
+        call("ads_acoustic_plan_forward", self._h, _ptr(vp), _ptr(tr), _stream())
+        return tr[:self.trace_count]
+
+    def gradient(self, vp, observed, want_traces=False):
+        _require_cuda(vp, observed)
+        vp = vp.contiguous().to(torch.float64)
+        obs = observed.contiguous().to(self.dtype)
+        loss = torch.empty(1, dtype=torch.float64, device=vp.device)
+        grad = torch.empty_like(vp)
+        tr = (torch.empty(max(self.trace_count, 1), dtype=self.dtype, device=vp.device)
+              if want_traces else None)
+        call("ads_acoustic_plan_gradient", self._h, _ptr(vp), _ptr(obs), _ptr(loss), _ptr(grad),
+             _ptr(tr), _stream())
+        if want_traces:
+            return loss[0], grad, tr[:self.trace_count]
+        return loss[0], grad
+
+
+class AcousticPropagator:
+    """Result handle of AcousticPropagatorSolver (src/Struct.jl:140-147).  The
+    wavefield history is not materialised (the GPU path keeps O(1) steps in
+    memory); receiver traces come from SimulatedObservation."""
+
+    def __init__(self, param, src, vp, precision):
+        self.param, self.src, self.vp, self.precision = param, src, vp, precision
+
+
+def AcousticPropagatorSolver(param: AcousticPropagatorParams, src: AcousticSource, vp,
+                             precision="f64"):
+    """src/Core.jl:562-620 (c = vp^2, PML from param, zero initial slots)."""
+    if param.PropagatorKernel not in (0, 1, 2):
+        raise ValueError("PropagatorKernel must be 0, 1 or 2")
+    return AcousticPropagator(param, src, vp, precision)
+
+
+def _shot_dict(param, src, rcv):
+    return dict(x0=0, nx=param.NX, nstep=param.NSTEP, srci=src.srci, srcj=src.srcj,
+                srcv=src.srcv, rcvi=rcv.rcvi, rcvj=rcv.rcvj)
+
+
+def SimulatedObservation(ap: AcousticPropagator, rcv: AcousticReceiver):
+    """src/Core.jl:726-730: fills rcv.rcvv with the (NSTEP+1, nrcv) traces."""
+    p = ap.param
+    plan = AcousticPlan(p.NX, p.NY, p.DELTAX, p.DELTAY, p.DELTAT, [_shot_dict(p, ap.src, rcv)],
+                        npml=p.NPOINTS_PML, Rcoef=p.Rcoef, vp_ref=p.vp_ref,
+                        use_pml=p.use_pml, precision=ap.precision, use_graph=False)
+    vp = torch.as_tensor(ap.vp, dtype=torch.float64, device="cuda").reshape(p.NX + 2, p.NY + 2)
+    tr = plan.forward(vp)
+    torch.cuda.current_stream().synchronize()
+    plan.close()
+    rcv.rcvv = tr.view(p.NSTEP + 1, len(rcv.rcvi))
+    return rcv.rcvv
+
+
+def compute_loss_and_grads_GPU(param: AcousticPropagatorParams, srcs, rcvs, Rs, vp,
+                               precision="f64", ckpt_every=0):
+    """src/Utils.jl:300-332 for one GPU: loss = sum over shots of sum((rcvv - Rs)^2)
+    and its gradient w.r.t. vp, all shots in one batched plan."""
+    shots = [_shot_dict(param, s, r) for s, r in zip(srcs, rcvs)]
+    plan = AcousticPlan(param.NX, param.NY, param.DELTAX, param.DELTAY, param.DELTAT, shots,
+                        npml=param.NPOINTS_PML, Rcoef=param.Rcoef, vp_ref=param.vp_ref,
+                        use_pml=param.use_pml, precision=precision, use_graph=False,
+                        ckpt_every=ckpt_every)
+    vp = torch.as_tensor(vp, dtype=torch.float64, device="cuda").reshape(param.NX + 2,
+                                                                         param.NY + 2)
+    obs = plan.pack([torch.as_tensor(r, device="cuda") for r in Rs])
+    loss, grad = plan.gradient(vp, obs)
+    torch.cuda.current_stream().synchronize()
+    plan.close()
+    return loss, grad
+
+
+class AcousticMisfit(torch.autograd.Function):
+    """loss = sum((traces(vp) - observed)^2) as an autograd node whose backward is
+    the plan's checkpointed adjoint (the gradient TF builds in src/Utils.jl:312)."""
+
+    @staticmethod
+    def forward(ctx, vp, plan: AcousticPlan, observed):
+        loss, grad = plan.gradient(vp, observed)
+        ctx.save_for_backward(grad)
+        return loss
+
+    @staticmethod
+    def backward(ctx, gl):
+        (grad,) = ctx.saved_tensors
+        return gl * grad, None, None

@@ -1,0 +1,1155 @@
+// elastic.cu -- 2D isotropic elastic velocity-stress step with CPML memory
+// variables (src/Core.jl:96-228, profiles :231-407), its exact transpose, and
+// whole-path multi-shot forward / misfit / gradient w.r.t. lambda, mu, rho.
+//
+// The reference composes one step from ~50 gather/scatter custom ops per step
+// (fw1..fw4 + add_source).  Here a step is two kernels (stresses: fw1+fw2;
+// velocities: fw3+fw4) plus a tiny source/receiver launch; the adjoint is three
+// gather-form kernels.  Per-cell work on the eight memory variables only runs
+// where the 1D CPML profile is active (a != 0 or b != 1); elsewhere the
+// forward memory stays exactly zero and its adjoint never reaches a gradient
+// (it is multiplied by a = 0), so skipping it changes no result.
+//
+// Cell indexing: (i, j) -> i*P + j + OFF (P = NY+2, OFF = 0 for the
+// single-step operators; pitched layout for the plans).
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <numeric>
+#include <vector>
+
+#include "ads_internal.h"
+
+namespace ads {
+namespace {
+
+enum { VX = 0, VY = 1, SXX = 2, SYY = 3, SXY = 4, M1 = 5 };  // mem k at M1 + k - 1
+constexpr int NF = 13;
+// temporaries of the adjoint
+enum { D1 = 0, D2, D3, D4, D5, D6, D7, D8, R4, GL1, GM1, GM2, NTMP };
+// per-step forward store: strains / accelerations the adjoint needs
+enum { E1 = 0, E2, E12, A3, A4, NSTORE };
+
+constexpr int BX = 32, BY = 8;
+
+template <typename T>
+struct ElModel {
+  const T *lam, *mu, *rho;
+  const T *axi, *axh, *bxi, *bxh, *ayi, *ayh, *byi, *byh;  // 1D, index I-1 / J-1
+  T dt, hx24, hy24;
+  int NX, NY, OFF, pad;
+  int64_t P;
+};
+
+template <typename T>
+struct ElShot {
+  const T* fin[NF];  // step input state
+  T* f[NF];          // step output state (== fin in the plans: updated in place)
+  T* g[NF];          // adjoint state (in place)
+  T* tmp[NTMP];
+  T* store;          // K slots x NSTORE fields
+  T* ckpt;           // nseg x NF fields
+  double *glam, *gmu, *grho;
+  T *traces, *resid;            // (nrcv, NSTEP+1)
+  const T* srcv;                // (NSTEP, nsrc)
+  const int64_t* src_cell;      // pitched cell offsets
+  const int* src_type;
+  const int64_t* rcv_cell;
+  const int* rcv_type;
+  int nsrc, nrcv;
+  int64_t fs;                   // elements per field
+};
+
+template <typename T>
+__device__ __forceinline__ T d4(T a0, T am1, T ap1, T am2, T h24) {
+  return (T(27) * a0 - T(27) * am1 - ap1 + am2) / h24;
+}
+
+template <typename T>
+__device__ __forceinline__ bool active(const T* a, const T* b, int k) {
+  return a[k] != T(0) || b[k] != T(1);
+}
+
+#define ELIDX(ii, jj) ((int64_t)(ii) * M.P + (jj) + M.OFF)
+
+// Stress update (fw1: sxx, syy, m1, m2; fw2: sxy, m3, m4).
+// FULL: every cell written (out-of-place operator); else interior boxes only.
+template <typename T, bool FULL, bool STORE>
+__global__ void __launch_bounds__(BX* BY)
+k_el_stress(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
+  const ElShot<T>& sh = shots ? shots[blockIdx.z] : one;
+  const int j = blockIdx.x * BX + threadIdx.x;
+  const int i = blockIdx.y * BY + threadIdx.y;
+  const int NX = M.NX, NY = M.NY;
+  if (i > NX + 1 || j > NY + 1) return;
+  const int64_t x = ELIDX(i, j);
+  const bool b1 = i >= 1 && i <= NX - 1 && j >= 2 && j <= NY;
+  const bool b2 = i >= 2 && i <= NX && j >= 1 && j <= NY - 1;
+  if (!FULL && !b1 && !b2) return;
+  const T* vx = sh.fin[VX];
+  const T* vy = sh.fin[VY];
+  T* st = STORE ? sh.store + (int64_t)store_slot * NSTORE * sh.fs : nullptr;
+  if (b1) {
+    const T lam_ = T(0.5) * (M.lam[ELIDX(i + 1, j)] + M.lam[x]);
+    const T mu_ = T(0.5) * (M.mu[ELIDX(i + 1, j)] + M.mu[x]);
+    const T lm = lam_ + T(2) * mu_;
+    const T dvx = d4<T>(vx[ELIDX(i + 1, j)], vx[x], vx[ELIDX(i + 2, j)], vx[ELIDX(i - 1, j)],
+                        M.hx24);
+    const T dvy = d4<T>(vy[x], vy[ELIDX(i, j - 1)], vy[ELIDX(i, j + 1)], vy[ELIDX(i, j - 2)],
+                        M.hy24);
+    T m1 = T(0), m2 = T(0);
+    if (FULL || active(M.axh, M.bxh, i - 1)) {
+      m1 = M.bxh[i - 1] * sh.fin[M1 + 0][x] + M.axh[i - 1] * dvx;
+      sh.f[M1 + 0][x] = m1;
+    }
+    if (FULL || active(M.ayi, M.byi, j - 1)) {
+      m2 = M.byi[j - 1] * sh.fin[M1 + 1][x] + M.ayi[j - 1] * dvy;
+      sh.f[M1 + 1][x] = m2;
+    }
+    const T e1 = dvx + m1, e2 = dvy + m2;
+    sh.f[SXX][x] = sh.fin[SXX][x] + (lm * e1 + lam_ * e2) * M.dt;
+    sh.f[SYY][x] = sh.fin[SYY][x] + (lm * e2 + lam_ * e1) * M.dt;
+    if (STORE) {
+      st[E1 * sh.fs + x] = e1;
+      st[E2 * sh.fs + x] = e2;
+    }
+  } else if (FULL) {
+    sh.f[SXX][x] = sh.fin[SXX][x];
+    sh.f[SYY][x] = sh.fin[SYY][x];
+    sh.f[M1 + 0][x] = T(0);
+    sh.f[M1 + 1][x] = T(0);
+  }
+  if (b2) {
+    const T mu_ = T(0.5) * (M.mu[x] + M.mu[ELIDX(i, j + 1)]);
+    const T dvydx = d4<T>(vy[x], vy[ELIDX(i - 1, j)], vy[ELIDX(i + 1, j)], vy[ELIDX(i - 2, j)],
+                          M.hx24);
+    const T dvxdy = d4<T>(vx[ELIDX(i, j + 1)], vx[x], vx[ELIDX(i, j + 2)], vx[ELIDX(i, j - 1)],
+                          M.hy24);
+    T m3 = T(0), m4 = T(0);
+    if (FULL || active(M.axi, M.bxi, i - 1)) {
+      m3 = M.bxi[i - 1] * sh.fin[M1 + 2][x] + M.axi[i - 1] * dvydx;
+      sh.f[M1 + 2][x] = m3;
+    }
+    if (FULL || active(M.ayh, M.byh, j - 1)) {
+      m4 = M.byh[j - 1] * sh.fin[M1 + 3][x] + M.ayh[j - 1] * dvxdy;
+      sh.f[M1 + 3][x] = m4;
+    }
+    const T e12 = (dvydx + m3) + (dvxdy + m4);
+    sh.f[SXY][x] = sh.fin[SXY][x] + mu_ * e12 * M.dt;
+    if (STORE) st[E12 * sh.fs + x] = e12;
+  } else if (FULL) {
+    sh.f[SXY][x] = sh.fin[SXY][x];
+    sh.f[M1 + 2][x] = T(0);
+    sh.f[M1 + 3][x] = T(0);
+  }
+}
+
+// Velocity update (fw3: vx, m5, m6 from the new sxx, sxy; fw4: vy, m7, m8
+// from the new sxy, syy).
+template <typename T, bool FULL, bool STORE>
+__global__ void __launch_bounds__(BX* BY)
+k_el_velocity(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
+  const ElShot<T>& sh = shots ? shots[blockIdx.z] : one;
+  const int j = blockIdx.x * BX + threadIdx.x;
+  const int i = blockIdx.y * BY + threadIdx.y;
+  const int NX = M.NX, NY = M.NY;
+  if (i > NX + 1 || j > NY + 1) return;
+  const int64_t x = ELIDX(i, j);
+  const bool b3 = i >= 2 && i <= NX && j >= 2 && j <= NY;
+  const bool b4 = i >= 1 && i <= NX - 1 && j >= 1 && j <= NY - 1;
+  if (!FULL && !b3 && !b4) return;
+  const T* sxx = sh.f[SXX];
+  const T* syy = sh.f[SYY];
+  const T* sxy = sh.f[SXY];
+  T* st = STORE ? sh.store + (int64_t)store_slot * NSTORE * sh.fs : nullptr;
+  if (b3) {
+    const T a = d4<T>(sxx[x], sxx[ELIDX(i - 1, j)], sxx[ELIDX(i + 1, j)], sxx[ELIDX(i - 2, j)],
+                      M.hx24);
+    const T b = d4<T>(sxy[x], sxy[ELIDX(i, j - 1)], sxy[ELIDX(i, j + 1)], sxy[ELIDX(i, j - 2)],
+                      M.hy24);
+    T m5 = T(0), m6 = T(0);
+    if (FULL || active(M.axi, M.bxi, i - 1)) {
+      m5 = M.bxi[i - 1] * sh.fin[M1 + 4][x] + M.axi[i - 1] * a;
+      sh.f[M1 + 4][x] = m5;
+    }
+    if (FULL || active(M.ayi, M.byi, j - 1)) {
+      m6 = M.byi[j - 1] * sh.fin[M1 + 5][x] + M.ayi[j - 1] * b;
+      sh.f[M1 + 5][x] = m6;
+    }
+    const T e3 = (a + m5) + (b + m6);
+    sh.f[VX][x] = sh.fin[VX][x] + e3 * M.dt / M.rho[x];
+    if (STORE) st[A3 * sh.fs + x] = e3;
+  } else if (FULL) {
+    sh.f[VX][x] = sh.fin[VX][x];
+    sh.f[M1 + 4][x] = T(0);
+    sh.f[M1 + 5][x] = T(0);
+  }
+  if (b4) {
+    const T rho_ = T(0.25) * (M.rho[x] + M.rho[ELIDX(i + 1, j)] + M.rho[ELIDX(i + 1, j + 1)] +
+                              M.rho[ELIDX(i, j + 1)]);
+    const T a = d4<T>(sxy[ELIDX(i + 1, j)], sxy[x], sxy[ELIDX(i + 2, j)], sxy[ELIDX(i - 1, j)],
+                      M.hx24);
+    const T b = d4<T>(syy[ELIDX(i, j + 1)], syy[x], syy[ELIDX(i, j + 2)], syy[ELIDX(i, j - 1)],
+                      M.hy24);
+    T m7 = T(0), m8 = T(0);
+    if (FULL || active(M.axh, M.bxh, i - 1)) {
+      m7 = M.bxh[i - 1] * sh.fin[M1 + 6][x] + M.axh[i - 1] * a;
+      sh.f[M1 + 6][x] = m7;
+    }
+    if (FULL || active(M.ayh, M.byh, j - 1)) {
+      m8 = M.byh[j - 1] * sh.fin[M1 + 7][x] + M.ayh[j - 1] * b;
+      sh.f[M1 + 7][x] = m8;
+    }
+    const T e4 = (a + m7) + (b + m8);
+    sh.f[VY][x] = sh.fin[VY][x] + e4 * M.dt / rho_;
+    if (STORE) st[A4 * sh.fs + x] = e4;
+  } else if (FULL) {
+    sh.f[VY][x] = sh.fin[VY][x];
+    sh.f[M1 + 6][x] = T(0);
+    sh.f[M1 + 7][x] = T(0);
+  }
+}
+
+// Adjoint 1 (velocity cells): transposes of fw3 and fw4.  Writes D5..D8 and
+// R4, updates the memory adjoints m5..m8 and grho (fw3 part) in place.
+template <typename T, bool FULL>
+__global__ void __launch_bounds__(BX* BY)
+k_el_adj1(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
+  const ElShot<T>& sh = shots ? shots[blockIdx.z] : one;
+  const int j = blockIdx.x * BX + threadIdx.x;
+  const int i = blockIdx.y * BY + threadIdx.y;
+  const int NX = M.NX, NY = M.NY;
+  if (i > NX + 1 || j > NY + 1) return;
+  const int64_t x = ELIDX(i, j);
+  const bool b3 = i >= 2 && i <= NX && j >= 2 && j <= NY;
+  const bool b4 = i >= 1 && i <= NX - 1 && j >= 1 && j <= NY - 1;
+  const T* st = sh.store + (int64_t)store_slot * NSTORE * sh.fs;
+  if (b3) {
+    const T gv = sh.g[VX][x], r = M.rho[x];
+    const T q = gv * M.dt / r;
+    T gm5 = q, gm6 = q;
+    if (FULL || active(M.axi, M.bxi, i - 1)) {
+      gm5 += sh.g[M1 + 4][x];
+      sh.g[M1 + 4][x] = M.bxi[i - 1] * gm5;
+    }
+    if (FULL || active(M.ayi, M.byi, j - 1)) {
+      gm6 += sh.g[M1 + 5][x];
+      sh.g[M1 + 5][x] = M.byi[j - 1] * gm6;
+    }
+    sh.tmp[D5][x] = (q + M.axi[i - 1] * gm5) / M.hx24;
+    sh.tmp[D6][x] = (q + M.ayi[j - 1] * gm6) / M.hy24;
+    sh.grho[x] += (double)(-gv * st[A3 * sh.fs + x] * M.dt / (r * r));
+  } else if (FULL) {
+    sh.g[M1 + 4][x] = T(0);
+    sh.g[M1 + 5][x] = T(0);
+  }
+  if (b4) {
+    const T gv = sh.g[VY][x];
+    const T rho_ = T(0.25) * (M.rho[x] + M.rho[ELIDX(i + 1, j)] + M.rho[ELIDX(i + 1, j + 1)] +
+                              M.rho[ELIDX(i, j + 1)]);
+    const T q = gv * M.dt / rho_;
+    T gm7 = q, gm8 = q;
+    if (FULL || active(M.axh, M.bxh, i - 1)) {
+      gm7 += sh.g[M1 + 6][x];
+      sh.g[M1 + 6][x] = M.bxh[i - 1] * gm7;
+    }
+    if (FULL || active(M.ayh, M.byh, j - 1)) {
+      gm8 += sh.g[M1 + 7][x];
+      sh.g[M1 + 7][x] = M.byh[j - 1] * gm8;
+    }
+    sh.tmp[D7][x] = (q + M.axh[i - 1] * gm7) / M.hx24;
+    sh.tmp[D8][x] = (q + M.ayh[j - 1] * gm8) / M.hy24;
+    sh.tmp[R4][x] = -gv * st[A4 * sh.fs + x] * M.dt / (rho_ * rho_) * T(0.25);
+  } else if (FULL) {
+    sh.g[M1 + 6][x] = T(0);
+    sh.g[M1 + 7][x] = T(0);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T tld(const T* a, const ElModel<T>& M, int i, int j) {
+  return (i >= 0 && i <= M.NX + 1 && j >= 0 && j <= M.NY + 1) ? a[ELIDX(i, j)] : T(0);
+}
+
+// Adjoint 2 (stress cells): gather D5..D8 into the stress adjoints, then the
+// transposes of fw1 and fw2 (D1..D4, memory adjoints m1..m4, lambda/mu parts).
+template <typename T, bool FULL>
+__global__ void __launch_bounds__(BX* BY)
+k_el_adj2(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
+  const ElShot<T>& sh = shots ? shots[blockIdx.z] : one;
+  const int j = blockIdx.x * BX + threadIdx.x;
+  const int i = blockIdx.y * BY + threadIdx.y;
+  const int NX = M.NX, NY = M.NY;
+  if (i > NX + 1 || j > NY + 1) return;
+  const int64_t x = ELIDX(i, j);
+  const bool b1 = i >= 1 && i <= NX - 1 && j >= 2 && j <= NY;
+  const bool b2 = i >= 2 && i <= NX && j >= 1 && j <= NY - 1;
+  if (!FULL && !b1 && !b2) return;
+  const T* const* D = sh.tmp;
+  const T gsxx = sh.g[SXX][x] + T(27) * D[D5][x] - T(27) * tld(D[D5], M, i + 1, j) -
+                 tld(D[D5], M, i - 1, j) + tld(D[D5], M, i + 2, j);
+  const T gsxy = sh.g[SXY][x] + T(27) * D[D6][x] - T(27) * tld(D[D6], M, i, j + 1) -
+                 tld(D[D6], M, i, j - 1) + tld(D[D6], M, i, j + 2) +
+                 T(27) * tld(D[D7], M, i - 1, j) - T(27) * D[D7][x] -
+                 tld(D[D7], M, i - 2, j) + tld(D[D7], M, i + 1, j);
+  const T gsyy = sh.g[SYY][x] + T(27) * tld(D[D8], M, i, j - 1) - T(27) * D[D8][x] -
+                 tld(D[D8], M, i, j - 2) + tld(D[D8], M, i, j + 1);
+  sh.g[SXX][x] = gsxx;
+  sh.g[SYY][x] = gsyy;
+  sh.g[SXY][x] = gsxy;
+  const T* st = sh.store + (int64_t)store_slot * NSTORE * sh.fs;
+  if (b1) {
+    const T lam_ = T(0.5) * (M.lam[ELIDX(i + 1, j)] + M.lam[x]);
+    const T mu_ = T(0.5) * (M.mu[ELIDX(i + 1, j)] + M.mu[x]);
+    const T lm = lam_ + T(2) * mu_;
+    const T e1 = st[E1 * sh.fs + x], e2 = st[E2 * sh.fs + x];
+    const T gE1 = M.dt * (lm * gsxx + lam_ * gsyy);
+    const T gE2 = M.dt * (lam_ * gsxx + lm * gsyy);
+    const T glm = M.dt * (e1 * gsxx + e2 * gsyy);
+    const T glam = M.dt * (e2 * gsxx + e1 * gsyy) + glm;
+    sh.tmp[GL1][x] = T(0.5) * glam;
+    sh.tmp[GM1][x] = glm;  // 0.5 * (2 glm) to each of mu[i], mu[i+1]
+    T gm1 = gE1, gm2 = gE2;
+    if (FULL || active(M.axh, M.bxh, i - 1)) {
+      gm1 += sh.g[M1 + 0][x];
+      sh.g[M1 + 0][x] = M.bxh[i - 1] * gm1;
+    }
+    if (FULL || active(M.ayi, M.byi, j - 1)) {
+      gm2 += sh.g[M1 + 1][x];
+      sh.g[M1 + 1][x] = M.byi[j - 1] * gm2;
+    }
+    sh.tmp[D1][x] = (gE1 + M.axh[i - 1] * gm1) / M.hx24;
+    sh.tmp[D2][x] = (gE2 + M.ayi[j - 1] * gm2) / M.hy24;
+  } else if (FULL) {
+    sh.g[M1 + 0][x] = T(0);
+    sh.g[M1 + 1][x] = T(0);
+  }
+  if (b2) {
+    const T mu_ = T(0.5) * (M.mu[x] + M.mu[ELIDX(i, j + 1)]);
+    const T q = gsxy * mu_ * M.dt;
+    sh.tmp[GM2][x] = gsxy * st[E12 * sh.fs + x] * M.dt * T(0.5);
+    T gm3 = q, gm4 = q;
+    if (FULL || active(M.axi, M.bxi, i - 1)) {
+      gm3 += sh.g[M1 + 2][x];
+      sh.g[M1 + 2][x] = M.bxi[i - 1] * gm3;
+    }
+    if (FULL || active(M.ayh, M.byh, j - 1)) {
+      gm4 += sh.g[M1 + 3][x];
+      sh.g[M1 + 3][x] = M.byh[j - 1] * gm4;
+    }
+    sh.tmp[D3][x] = (q + M.axi[i - 1] * gm3) / M.hx24;
+    sh.tmp[D4][x] = (q + M.ayh[j - 1] * gm4) / M.hy24;
+  } else if (FULL) {
+    sh.g[M1 + 2][x] = T(0);
+    sh.g[M1 + 3][x] = T(0);
+  }
+}
+
+// Adjoint 3 (velocity cells + parameters): gather D1..D4 into the velocity
+// adjoints and the lambda / mu / rho partials into the FP64 accumulators.
+template <typename T, bool FULL>
+__global__ void __launch_bounds__(BX* BY)
+k_el_adj3(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one) {
+  const ElShot<T>& sh = shots ? shots[blockIdx.z] : one;
+  const int j = blockIdx.x * BX + threadIdx.x;
+  const int i = blockIdx.y * BY + threadIdx.y;
+  const int NX = M.NX, NY = M.NY;
+  if (i > NX + 1 || j > NY + 1) return;
+  const int64_t x = ELIDX(i, j);
+  const bool b3 = i >= 2 && i <= NX && j >= 2 && j <= NY;
+  const bool b4 = i >= 1 && i <= NX - 1 && j >= 1 && j <= NY - 1;
+  const T* const* D = sh.tmp;
+  if (FULL || b3) {
+    sh.g[VX][x] += T(27) * tld(D[D1], M, i - 1, j) - T(27) * D[D1][x] -
+                   tld(D[D1], M, i - 2, j) + tld(D[D1], M, i + 1, j) +
+                   T(27) * tld(D[D4], M, i, j - 1) - T(27) * D[D4][x] -
+                   tld(D[D4], M, i, j - 2) + tld(D[D4], M, i, j + 1);
+  }
+  if (FULL || b4) {
+    sh.g[VY][x] += T(27) * D[D2][x] - T(27) * tld(D[D2], M, i, j + 1) -
+                   tld(D[D2], M, i, j - 1) + tld(D[D2], M, i, j + 2) + T(27) * D[D3][x] -
+                   T(27) * tld(D[D3], M, i + 1, j) - tld(D[D3], M, i - 1, j) +
+                   tld(D[D3], M, i + 2, j);
+  }
+  if (i >= 1 && i <= NX && j >= 1 && j <= NY) {
+    sh.glam[x] += (double)(D[GL1][x] + tld(D[GL1], M, i - 1, j));
+    sh.gmu[x] += (double)(D[GM1][x] + tld(D[GM1], M, i - 1, j) + D[GM2][x] +
+                          tld(D[GM2], M, i, j - 1));
+    sh.grho[x] += (double)(D[R4][x] + tld(D[R4], M, i - 1, j) + tld(D[R4], M, i - 1, j - 1) +
+                           tld(D[R4], M, i, j - 1));
+  }
+}
+
+#undef ELIDX
+
+// Sources of slot n (added in order by one thread), then receivers of slot n.
+template <typename T>
+__global__ void k_el_src_rcv(const ElShot<T>* __restrict__ shots, int n, int nt, int record) {
+  const ElShot<T>& sh = shots[blockIdx.x];
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < sh.nsrc; k++) {
+      const int t = sh.src_type[k];
+      if (t < 0 || t > 4) continue;
+      sh.f[t][sh.src_cell[k]] += sh.srcv[(int64_t)(n - 1) * sh.nsrc + k];
+    }
+  }
+  if (!record) return;
+  __syncthreads();
+  for (int r = threadIdx.x; r < sh.nrcv; r += blockDim.x) {
+    const int t = sh.rcv_type[r];
+    sh.traces[(int64_t)r * nt + n] = (t >= 0 && t <= 4) ? sh.f[t][sh.rcv_cell[r]] : T(0);
+  }
+}
+
+// Adjoint state += residual of slot n at the receivers.
+template <typename T>
+__global__ void k_el_resid(const ElShot<T>* __restrict__ shots, int n, int nt) {
+  const ElShot<T>& sh = shots[blockIdx.x];
+  for (int r = threadIdx.x; r < sh.nrcv; r += blockDim.x) {
+    const int t = sh.rcv_type[r];
+    if (t < 0 || t > 4) continue;
+    atomicAdd(sh.g[t] + sh.rcv_cell[r], sh.resid[(int64_t)r * nt + n]);
+  }
+}
+
+// State <-> checkpoint copies (13 contiguous fields per shot).
+template <typename T>
+__global__ void k_el_ckpt(const ElShot<T>* __restrict__ shots, int slot, int to_ckpt) {
+  const ElShot<T>& sh = shots[blockIdx.y];
+  const int64_t n = NF * sh.fs;
+  T* state = sh.f[0];
+  T* ck = sh.ckpt + (int64_t)slot * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    if (to_ckpt)
+      ck[e] = state[e];
+    else
+      state[e] = ck[e];
+  }
+}
+
+template <typename T>
+__global__ void k_el_cast(T* __restrict__ out, const double* __restrict__ in, int NX, int NY,
+                          int64_t P, int off) {
+  const int64_t n = (int64_t)(NX + 2) * (NY + 2);
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / (NY + 2), j = e % (NY + 2);
+    out[i * P + j + off] = (T)in[e];
+  }
+}
+
+// Sum the shots' FP64 accumulators into the caller's unpitched gradients.
+template <typename T>
+__global__ void k_el_gather_grads(const ElShot<T>* __restrict__ shots, int nshots, int NX,
+                                  int NY, int64_t P, int off, double* __restrict__ gl,
+                                  double* __restrict__ gm, double* __restrict__ gr) {
+  const int64_t n = (int64_t)(NX + 2) * (NY + 2);
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / (NY + 2), j = e % (NY + 2), x = i * P + j + off;
+    double a = 0, b = 0, c = 0;
+    for (int s = 0; s < nshots; s++) {
+      a += shots[s].glam[x];
+      b += shots[s].gmu[x];
+      c += shots[s].grho[x];
+    }
+    gl[e] = a;
+    gm[e] = b;
+    gr[e] = c;
+  }
+}
+
+// Single-step operator sources: 1-based device indices, CPU AddSource order.
+struct Fields5 {
+  double* p[5];
+};
+
+__global__ void k_el_step_src(Fields5 f5, const int64_t* __restrict__ si,
+                              const int64_t* __restrict__ sj, const int64_t* __restrict__ st,
+                              const double* __restrict__ sv, int64_t nsrc, int NX, int NY) {
+  if (threadIdx.x != 0) return;
+  for (int64_t k = 0; k < nsrc; k++) {
+    const int64_t t = st[k], a = si[k] - 1, b = sj[k] - 1;
+    if (t < 0 || t > 4) continue;
+    if (a < 0 || a > NX + 1 || b < 0 || b > NY + 1) continue;
+    f5.p[t][a * (NY + 2) + b] += sv[k];
+  }
+}
+
+// reduction helpers (deterministic two-pass FP64 misfit)
+constexpr unsigned FULLM = 0xffffffffu;
+template <typename T>
+__global__ void k_el_misfit(const T* __restrict__ tr, const T* __restrict__ obs,
+                            T* __restrict__ resid, int64_t n, double* __restrict__ partial) {
+  double acc = 0.0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const double d = (double)tr[e] - (double)obs[e];
+    resid[e] = (T)(2 * d);
+    acc += d * d;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(FULLM, acc, o);
+  __shared__ double sm[32];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    acc = threadIdx.x < (blockDim.x >> 5) ? sm[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(FULLM, acc, o);
+    if (threadIdx.x == 0) partial[blockIdx.x] = acc;
+  }
+}
+
+__global__ void k_el_reduce(const double* __restrict__ partial, int n, double* out) {
+  double acc = 0.0;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) acc += partial[e];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(FULLM, acc, o);
+  __shared__ double sm[32];
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    acc = threadIdx.x < (blockDim.x >> 5) ? sm[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(FULLM, acc, o);
+    if (threadIdx.x == 0) *out = acc;
+  }
+}
+
+template <typename T>
+ElModel<T> make_model(int NX, int NY, int64_t P, int off, double dt, double dx, double dy,
+                      const T* lam, const T* mu, const T* rho, const T* prof) {
+  // prof: axi, axh, bxi, bxh (NX each), ayi, ayh, byi, byh (NY each)
+  ElModel<T> M{};
+  M.lam = lam;
+  M.mu = mu;
+  M.rho = rho;
+  M.axi = prof;
+  M.axh = prof + NX;
+  M.bxi = prof + 2 * NX;
+  M.bxh = prof + 3 * NX;
+  M.ayi = prof + 4 * NX;
+  M.ayh = prof + 4 * NX + NY;
+  M.byi = prof + 4 * NX + 2 * NY;
+  M.byh = prof + 4 * NX + 3 * NY;
+  M.dt = (T)dt;
+  M.hx24 = (T)(24 * dx);
+  M.hy24 = (T)(24 * dy);
+  M.NX = NX;
+  M.NY = NY;
+  M.OFF = off;
+  M.P = P;
+  return M;
+}
+
+// Host: pack profile rows as the kernels index them (I-1 / J-1).
+template <typename T>
+std::vector<T> pack_profiles(int64_t NX, int64_t NY, const double* ax, const double* bx,
+                             const double* ay, const double* by) {
+  std::vector<T> p(4 * NX + 4 * NY);
+  for (int64_t i = 0; i < NX; i++) {
+    p[i] = (T)ax[i];
+    p[NX + i] = (T)ax[NX + i];
+    p[2 * NX + i] = (T)bx[i];
+    p[3 * NX + i] = (T)bx[NX + i];
+  }
+  for (int64_t j = 0; j < NY; j++) {
+    p[4 * NX + j] = (T)ay[j];
+    p[4 * NX + NY + j] = (T)ay[NY + j];
+    p[4 * NX + 2 * NY + j] = (T)by[j];
+    p[4 * NX + 3 * NY + j] = (T)by[NY + j];
+  }
+  return p;
+}
+
+}  // namespace
+
+// ======================================================================
+// whole-path elastic plan
+// ======================================================================
+
+struct ElPlanBase {
+  virtual ~ElPlanBase() = default;
+  virtual int forward(const double* l, const double* m, const double* r, void* traces,
+                      cudaStream_t st) = 0;
+  virtual int gradient(const double* l, const double* m, const double* r, const void* obs,
+                       double* loss, double* gl, double* gm, double* gr, void* tr_out,
+                       cudaStream_t st) = 0;
+  std::vector<int64_t> trace_off;
+  int64_t trace_total = 0, bytes = 0, launches_fwd = 0, launches_grad = 0;
+};
+
+namespace {
+
+template <typename T>
+struct ElPlan final : ElPlanBase {
+  ads_elastic_config cfg{};
+  int nshots = 0, K = 0, nseg = 0, NX = 0, NY = 0, NSTEP = 0;
+  int64_t P = 0, fs = 0;
+  char* pool = nullptr;
+  ElShot<T>* d_shots = nullptr;
+  ElModel<T> M{};
+  T *d_lam = nullptr, *d_mu = nullptr, *d_rho = nullptr, *d_traces = nullptr,
+    *d_resid = nullptr;
+  double* d_partial = nullptr;
+  static constexpr int kBlocks = 512;
+  size_t zero_fwd_off = 0, zero_fwd_len = 0, zero_adj_off = 0, zero_adj_len = 0;
+  cudaStream_t cap = nullptr;
+  cudaGraphExec_t eF = nullptr, eR = nullptr;
+  cudaGraph_t gF = nullptr, gR = nullptr;
+  int64_t nF = 0, nR = 0;
+
+  ~ElPlan() override {
+    if (eF) cudaGraphExecDestroy(eF);
+    if (eR) cudaGraphExecDestroy(eR);
+    if (gF) cudaGraphDestroy(gF);
+    if (gR) cudaGraphDestroy(gR);
+    if (cap) cudaStreamDestroy(cap);
+    if (pool) cudaFree(pool);
+  }
+
+  dim3 grid3() const {
+    return dim3((unsigned)div_up(NY + 2, BX), (unsigned)div_up(NX + 2, BY), (unsigned)nshots);
+  }
+
+  int create(const ads_elastic_config& c, const ads_elastic_shot* shots, int64_t ns,
+             cudaStream_t st);
+  int step(cudaStream_t st, int n, bool store, int slot, bool record);
+  int issue_forward(cudaStream_t st, int64_t* count);
+  int issue_reverse(cudaStream_t st, int64_t* count);
+  int prep(const double* l, const double* m, const double* r, cudaStream_t st);
+  int forward(const double* l, const double* m, const double* r, void* traces,
+              cudaStream_t st) override;
+  int gradient(const double* l, const double* m, const double* r, const void* obs,
+               double* loss, double* gl, double* gm, double* gr, void* tr_out,
+               cudaStream_t st) override;
+};
+
+template <typename T>
+int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots, int64_t ns,
+                      cudaStream_t st) {
+  cfg = c;
+  ADS_REQUIRE(ns >= 1 && ns < 65536, "nshots must be in [1, 65535]");
+  ADS_REQUIRE(c.NX >= 4 && c.NY >= 4 && c.NX < (1 << 20) && c.NY < (1 << 20),
+              "NX, NY must be in [4, 2^20)");
+  ADS_REQUIRE(c.NSTEP >= 1 && c.NSTEP < (1 << 24), "NSTEP must be >= 1");
+  ADS_REQUIRE(c.dx > 0 && c.dy > 0 && c.dt > 0, "dx, dy, dt must be positive");
+  ADS_REQUIRE(c.npml >= 1 && c.Rcoef > 0 && c.Rcoef < 1, "invalid CPML parameters");
+  ADS_REQUIRE(c.ckpt_every >= 0, "negative ckpt_every");
+  nshots = (int)ns;
+  NX = (int)c.NX;
+  NY = (int)c.NY;
+  NSTEP = (int)c.NSTEP;
+  for (int s = 0; s < ns; s++) {
+    const ads_elastic_shot& h = shots[s];
+    ADS_REQUIRE(h.nsrc >= 0 && h.nrcv >= 0, "shot %d: negative counts", s);
+    ADS_REQUIRE(h.nsrc == 0 || (h.srci && h.srcj && h.srctype && h.srcv && h.srcv_rows >= NSTEP),
+                "shot %d: source arrays missing or srcv_rows < NSTEP", s);
+    ADS_REQUIRE(h.nrcv == 0 || (h.rcvi && h.rcvj && h.rcvtype), "shot %d: null receivers", s);
+    for (int64_t k = 0; k < h.nsrc; k++)
+      ADS_REQUIRE(h.srci[k] >= 1 && h.srci[k] <= NX + 2 && h.srcj[k] >= 1 &&
+                      h.srcj[k] <= NY + 2,
+                  "shot %d source %lld outside the padded grid", s, (long long)k);
+    for (int64_t k = 0; k < h.nrcv; k++)
+      ADS_REQUIRE(h.rcvi[k] >= 1 && h.rcvi[k] <= NX + 2 && h.rcvj[k] >= 1 &&
+                      h.rcvj[k] <= NY + 2,
+                  "shot %d receiver %lld outside the padded grid", s, (long long)k);
+  }
+  K = c.ckpt_every > 0 ? (int)std::min<int64_t>(c.ckpt_every, NSTEP) : std::min(NSTEP, 100);
+  nseg = (int)div_up(NSTEP, K);
+  P = grid_pitch(NY);
+  fs = (int64_t)(NX + 2) * P;
+  trace_off.resize(ns);
+  trace_total = 0;
+  for (int s = 0; s < ns; s++) {
+    trace_off[s] = trace_total;
+    trace_total += shots[s].nrcv * (int64_t)(NSTEP + 1);
+  }
+  // ---- layout
+  struct Off {
+    size_t state, g, tmp, store, ckpt, acc, srcv, scell, stype, rcell, rtype;
+  };
+  std::vector<Off> o(ns);
+  size_t used = 0;
+  auto take = [&](size_t b) {
+    const size_t r = used;
+    used += (b + 255) & ~size_t(255);
+    return r;
+  };
+  const size_t F = sizeof(T) * fs;
+  const size_t fwd0 = used;
+  for (int s = 0; s < ns; s++) o[s].state = take(NF * F);
+  const size_t traces_o = take(sizeof(T) * std::max<int64_t>(trace_total, 1));
+  zero_fwd_off = fwd0;
+  zero_fwd_len = used - fwd0;
+  const size_t adj0 = used;
+  for (int s = 0; s < ns; s++) {
+    o[s].g = take(NF * F);
+    o[s].acc = take(3 * sizeof(double) * fs);
+  }
+  zero_adj_off = adj0;
+  zero_adj_len = used - adj0;
+  for (int s = 0; s < ns; s++) {
+    const ads_elastic_shot& h = shots[s];
+    o[s].tmp = take(NTMP * F);
+    o[s].store = take((size_t)K * NSTORE * F);
+    o[s].ckpt = take((size_t)nseg * NF * F);
+    o[s].srcv = take(sizeof(T) * std::max<int64_t>(NSTEP * h.nsrc, 1));
+    o[s].scell = take(sizeof(int64_t) * std::max<int64_t>(h.nsrc, 1));
+    o[s].stype = take(sizeof(int) * std::max<int64_t>(h.nsrc, 1));
+    o[s].rcell = take(sizeof(int64_t) * std::max<int64_t>(h.nrcv, 1));
+    o[s].rtype = take(sizeof(int) * std::max<int64_t>(h.nrcv, 1));
+  }
+  const size_t model_o = take(3 * F);
+  const size_t prof_o = take(sizeof(T) * (4 * NX + 4 * NY));
+  const size_t resid_o = take(sizeof(T) * std::max<int64_t>(trace_total, 1));
+  const size_t part_o = take(sizeof(double) * kBlocks);
+  const size_t shots_o = take(sizeof(ElShot<T>) * ns);
+  bytes = (int64_t)used;
+  {
+    cudaError_t e = cudaMalloc(&pool, used);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      pool = nullptr;
+      return fail(ADS_ERR_NOMEM, "device allocation of %.3f GB for the plan failed: %s",
+                  used / 1e9, cudaGetErrorString(e));
+    }
+  }
+  ADS_CUDA(cudaMemsetAsync(pool, 0, used, st));
+  d_lam = (T*)(pool + model_o);
+  d_mu = d_lam + fs;
+  d_rho = d_mu + fs;
+  d_traces = (T*)(pool + traces_o);
+  d_resid = (T*)(pool + resid_o);
+  d_partial = (double*)(pool + part_o);
+  d_shots = (ElShot<T>*)(pool + shots_o);
+  // profiles
+  std::vector<double> ax(2 * NX), bx(2 * NX), kx(2 * NX), ay(2 * NY), by(2 * NY), ky(2 * NY);
+  elastic_cpml(NX, NY, c.dx, c.dy, c.dt, c.npml, c.npower, c.k_max, c.alpha_max, c.vp_ref,
+               c.Rcoef, c.use_pml, ax.data(), bx.data(), kx.data(), ay.data(), by.data(),
+               ky.data());
+  std::vector<T> prof = pack_profiles<T>(NX, NY, ax.data(), bx.data(), ay.data(), by.data());
+  ADS_CUDA(cudaMemcpyAsync(pool + prof_o, prof.data(), sizeof(T) * prof.size(),
+                           cudaMemcpyHostToDevice, st));
+  M = make_model<T>(NX, NY, P, JOFF, c.dt, c.dx, c.dy, d_lam, d_mu, d_rho,
+                    (const T*)(pool + prof_o));
+  // shots
+  std::vector<ElShot<T>> hs(ns);
+  std::vector<std::vector<char>> stage;
+  for (int s = 0; s < ns; s++) {
+    const ads_elastic_shot& h = shots[s];
+    ElShot<T>& d = hs[s];
+    for (int f = 0; f < NF; f++) {
+      d.f[f] = (T*)(pool + o[s].state) + f * fs;
+      d.fin[f] = d.f[f];
+      d.g[f] = (T*)(pool + o[s].g) + f * fs;
+    }
+    for (int k = 0; k < NTMP; k++) d.tmp[k] = (T*)(pool + o[s].tmp) + k * fs;
+    d.store = (T*)(pool + o[s].store);
+    d.ckpt = (T*)(pool + o[s].ckpt);
+    d.glam = (double*)(pool + o[s].acc);
+    d.gmu = d.glam + fs;
+    d.grho = d.gmu + fs;
+    d.traces = d_traces + trace_off[s];
+    d.resid = d_resid + trace_off[s];
+    d.srcv = (const T*)(pool + o[s].srcv);
+    d.src_cell = (const int64_t*)(pool + o[s].scell);
+    d.src_type = (const int*)(pool + o[s].stype);
+    d.rcv_cell = (const int64_t*)(pool + o[s].rcell);
+    d.rcv_type = (const int*)(pool + o[s].rtype);
+    d.nsrc = (int)h.nsrc;
+    d.nrcv = (int)h.nrcv;
+    d.fs = fs;
+    if (h.nsrc > 0) {
+      std::vector<T> sv((size_t)NSTEP * h.nsrc);
+      for (int64_t r = 0; r < NSTEP; r++)
+        for (int64_t k = 0; k < h.nsrc; k++) sv[r * h.nsrc + k] = (T)h.srcv[r * h.nsrc + k];
+      std::vector<int64_t> cell(h.nsrc);
+      std::vector<int> type(h.nsrc);
+      for (int64_t k = 0; k < h.nsrc; k++) {
+        cell[k] = (h.srci[k] - 1) * P + (h.srcj[k] - 1) + JOFF;
+        type[k] = (int)h.srctype[k];
+      }
+      stage.emplace_back((char*)sv.data(), (char*)(sv.data() + sv.size()));
+      ADS_CUDA(cudaMemcpyAsync((void*)d.srcv, stage.back().data(), stage.back().size(),
+                               cudaMemcpyHostToDevice, st));
+      stage.emplace_back((char*)cell.data(), (char*)(cell.data() + cell.size()));
+      ADS_CUDA(cudaMemcpyAsync((void*)d.src_cell, stage.back().data(), stage.back().size(),
+                               cudaMemcpyHostToDevice, st));
+      stage.emplace_back((char*)type.data(), (char*)(type.data() + type.size()));
+      ADS_CUDA(cudaMemcpyAsync((void*)d.src_type, stage.back().data(), stage.back().size(),
+                               cudaMemcpyHostToDevice, st));
+    }
+    if (h.nrcv > 0) {
+      std::vector<int64_t> cell(h.nrcv);
+      std::vector<int> type(h.nrcv);
+      for (int64_t k = 0; k < h.nrcv; k++) {
+        cell[k] = (h.rcvi[k] - 1) * P + (h.rcvj[k] - 1) + JOFF;
+        type[k] = (int)h.rcvtype[k];
+      }
+      stage.emplace_back((char*)cell.data(), (char*)(cell.data() + cell.size()));
+      ADS_CUDA(cudaMemcpyAsync((void*)d.rcv_cell, stage.back().data(), stage.back().size(),
+                               cudaMemcpyHostToDevice, st));
+      stage.emplace_back((char*)type.data(), (char*)(type.data() + type.size()));
+      ADS_CUDA(cudaMemcpyAsync((void*)d.rcv_type, stage.back().data(), stage.back().size(),
+                               cudaMemcpyHostToDevice, st));
+    }
+  }
+  ADS_CUDA(cudaMemcpyAsync(d_shots, hs.data(), sizeof(ElShot<T>) * ns, cudaMemcpyHostToDevice,
+                           st));
+  ADS_CUDA(cudaStreamSynchronize(st));
+  {
+    int64_t n = 0;
+    issue_forward(nullptr, &n);
+    nF = n;
+    issue_reverse(nullptr, &n);
+    nR = n;
+  }
+  launches_fwd = 3 + nF;
+  launches_grad = 3 + nF + 2 + nR + 1;
+  if (c.use_graph) {
+    ADS_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    for (int which = 0; which < 2; which++) {
+      ADS_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+      set_launch_counting(false);
+      int rc = which == 0 ? issue_forward(cap, nullptr) : issue_reverse(cap, nullptr);
+      set_launch_counting(true);
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamEndCapture(cap, &g);
+      if (rc != ADS_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      ADS_CUDA(e);
+      cudaGraphExec_t ex = nullptr;
+      ADS_CUDA(cudaGraphInstantiate(&ex, g, 0));
+      (which == 0 ? gF : gR) = g;
+      (which == 0 ? eF : eR) = ex;
+    }
+  }
+  return ADS_OK;
+}
+
+// One forward step n (slot n-1 -> slot n) for every shot.
+template <typename T>
+int ElPlan<T>::step(cudaStream_t st, int n, bool store, int slot, bool record) {
+  const ElShot<T> none{};
+  if (store) {
+    k_el_stress<T, false, true><<<grid3(), dim3(BX, BY), 0, st>>>(M, d_shots, none, slot);
+    ADS_LAUNCHED(1);
+    k_el_velocity<T, false, true><<<grid3(), dim3(BX, BY), 0, st>>>(M, d_shots, none, slot);
+    ADS_LAUNCHED(1);
+  } else {
+    k_el_stress<T, false, false><<<grid3(), dim3(BX, BY), 0, st>>>(M, d_shots, none, 0);
+    ADS_LAUNCHED(1);
+    k_el_velocity<T, false, false><<<grid3(), dim3(BX, BY), 0, st>>>(M, d_shots, none, 0);
+    ADS_LAUNCHED(1);
+  }
+  k_el_src_rcv<T><<<nshots, 128, 0, st>>>(d_shots, n, NSTEP + 1, record ? 1 : 0);
+  ADS_LAUNCHED(1);
+  return ADS_OK;
+}
+
+template <typename T>
+int ElPlan<T>::issue_forward(cudaStream_t st, int64_t* count) {
+  if (count) {
+    int64_t c = 0;
+    for (int n = 1; n <= NSTEP; n++) c += 3 + ((n % K == 0 && n / K < nseg) ? 1 : 0);
+    *count = c;
+    return ADS_OK;
+  }
+  ADS_CUDA(cudaMemsetAsync(pool + zero_fwd_off, 0, zero_fwd_len, st));
+  for (int n = 1; n <= NSTEP; n++) {
+    if (int e = step(st, n, false, 0, true)) return e;
+    if (n % K == 0 && n / K < nseg) {  // checkpoint s holds slot s*K (state before step sK+1)
+      k_el_ckpt<T><<<dim3(256, nshots), 256, 0, st>>>(d_shots, n / K, 1);
+      ADS_LAUNCHED(1);
+    }
+  }
+  return ADS_OK;
+}
+
+template <typename T>
+int ElPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
+  if (count) {
+    int64_t c = 1;
+    for (int s = nseg - 1; s >= 0; s--) {
+      const int a = 1 + s * K, b = std::min(a + K - 1, NSTEP);
+      c += 1 + 3 * (b - a + 1) + 3 * (b - a + 1) + (b - std::max(a, 2) + 1);
+    }
+    *count = c;
+    return ADS_OK;
+  }
+  const ElShot<T> none{};
+  ADS_CUDA(cudaMemsetAsync(pool + zero_adj_off, 0, zero_adj_len, st));
+  k_el_resid<T><<<nshots, 128, 0, st>>>(d_shots, NSTEP, NSTEP + 1);
+  ADS_LAUNCHED(1);
+  for (int s = nseg - 1; s >= 0; s--) {
+    const int a = 1 + s * K, b = std::min(a + K - 1, NSTEP);
+    k_el_ckpt<T><<<dim3(256, nshots), 256, 0, st>>>(d_shots, s, 0);
+    ADS_LAUNCHED(1);
+    for (int n = a; n <= b; n++)
+      if (int e = step(st, n, true, n - a, false)) return e;
+    for (int n = b; n >= a; n--) {
+      k_el_adj1<T, false><<<grid3(), dim3(BX, BY), 0, st>>>(M, d_shots, none, n - a);
+      ADS_LAUNCHED(1);
+      k_el_adj2<T, false><<<grid3(), dim3(BX, BY), 0, st>>>(M, d_shots, none, n - a);
+      ADS_LAUNCHED(1);
+      k_el_adj3<T, false><<<grid3(), dim3(BX, BY), 0, st>>>(M, d_shots, none);
+      ADS_LAUNCHED(1);
+      // the adjoint state now refers to slot n-1: add its residual (slot 0 is
+      // the constant zero state and takes none)
+      if (n - 1 >= 1) {
+        k_el_resid<T><<<nshots, 128, 0, st>>>(d_shots, n - 1, NSTEP + 1);
+        ADS_LAUNCHED(1);
+      }
+    }
+  }
+  return ADS_OK;
+}
+
+template <typename T>
+int ElPlan<T>::prep(const double* l, const double* m, const double* r, cudaStream_t st) {
+  ADS_REQUIRE(l && m && r, "null model arrays");
+  const unsigned g = (unsigned)std::min<int64_t>(div_up((int64_t)(NX + 2) * (NY + 2), 256), 4096);
+  k_el_cast<T><<<g, 256, 0, st>>>(d_lam, l, NX, NY, P, JOFF);
+  ADS_LAUNCHED(1);
+  k_el_cast<T><<<g, 256, 0, st>>>(d_mu, m, NX, NY, P, JOFF);
+  ADS_LAUNCHED(1);
+  k_el_cast<T><<<g, 256, 0, st>>>(d_rho, r, NX, NY, P, JOFF);
+  ADS_LAUNCHED(1);
+  return ADS_OK;
+}
+
+template <typename T>
+int ElPlan<T>::forward(const double* l, const double* m, const double* r, void* traces,
+                       cudaStream_t st) {
+  if (int e = prep(l, m, r, st)) return e;
+  if (eF) {
+    ADS_CUDA(cudaGraphLaunch(eF, st));
+    note_launches(nF);
+  } else if (int e = issue_forward(st, nullptr)) {
+    return e;
+  }
+  if (traces)
+    ADS_CUDA(cudaMemcpyAsync(traces, d_traces, sizeof(T) * trace_total,
+                             cudaMemcpyDeviceToDevice, st));
+  return ADS_OK;
+}
+
+template <typename T>
+int ElPlan<T>::gradient(const double* l, const double* m, const double* r, const void* obs,
+                        double* loss, double* gl, double* gm, double* gr, void* tr_out,
+                        cudaStream_t st) {
+  ADS_REQUIRE(obs && loss && gl && gm && gr, "null argument");
+  if (int e = forward(l, m, r, nullptr, st)) return e;
+  k_el_misfit<T><<<kBlocks, 256, 0, st>>>(d_traces, (const T*)obs, d_resid, trace_total,
+                                          d_partial);
+  ADS_LAUNCHED(1);
+  k_el_reduce<<<1, 1024, 0, st>>>(d_partial, kBlocks, loss);
+  ADS_LAUNCHED(1);
+  if (eR) {
+    ADS_CUDA(cudaGraphLaunch(eR, st));
+    note_launches(nR);
+  } else if (int e = issue_reverse(st, nullptr)) {
+    return e;
+  }
+  const unsigned g = (unsigned)std::min<int64_t>(div_up((int64_t)(NX + 2) * (NY + 2), 256), 4096);
+  k_el_gather_grads<T><<<g, 256, 0, st>>>(d_shots, nshots, NX, NY, P, JOFF, gl, gm, gr);
+  ADS_LAUNCHED(1);
+  if (tr_out)
+    ADS_CUDA(cudaMemcpyAsync(tr_out, d_traces, sizeof(T) * trace_total,
+                             cudaMemcpyDeviceToDevice, st));
+  return ADS_OK;
+}
+
+}  // namespace
+}  // namespace ads
+
+struct ads_elastic_plan {
+  std::unique_ptr<ads::ElPlanBase> impl;
+};
+
+using namespace ads;
+
+extern "C" {
+
+int ads_elastic_step_fwd_f64(const double* state_in, double* state_out, const double* lambda,
+                             const double* mu, const double* rho, const double* ax,
+                             const double* bx, const double* kx, const double* ay,
+                             const double* by, const double* ky, double dt, double dx,
+                             double dy, int64_t NX, int64_t NY, const int64_t* srci,
+                             const int64_t* srcj, const int64_t* srctype, const double* srcv,
+                             int64_t nsrc, ads_stream_t stream) {
+  (void)kx;
+  (void)ky;
+  if (int e = require_device()) return e;
+  ADS_REQUIRE(NX >= 4 && NY >= 4 && NX < (1 << 24) && NY < (1 << 24), "NX, NY out of range");
+  ADS_REQUIRE(state_in && state_out && lambda && mu && rho && ax && bx && ay && by,
+              "null pointer argument");
+  ADS_REQUIRE(state_in != state_out, "state_out must not alias state_in");
+  ADS_REQUIRE(nsrc >= 0 && (nsrc == 0 || (srci && srcj && srctype && srcv)),
+              "invalid source arrays");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t N = (NX + 2) * (NY + 2);
+  // profiles, repacked on the device-side scratch
+  double* scratch = nullptr;
+  const size_t prof_n = 4 * NX + 4 * NY;
+  ADS_CUDA(cudaMallocAsync((void**)&scratch, sizeof(double) * prof_n, st));
+  // rows are already in the right order on the device: copy them into place
+  double* prof = scratch;
+  ADS_CUDA(cudaMemcpyAsync(prof, ax, sizeof(double) * 2 * NX, cudaMemcpyDeviceToDevice, st));
+  ADS_CUDA(cudaMemcpyAsync(prof + 2 * NX, bx, sizeof(double) * 2 * NX, cudaMemcpyDeviceToDevice,
+                           st));
+  ADS_CUDA(cudaMemcpyAsync(prof + 4 * NX, ay, sizeof(double) * 2 * NY, cudaMemcpyDeviceToDevice,
+                           st));
+  ADS_CUDA(cudaMemcpyAsync(prof + 4 * NX + 2 * NY, by, sizeof(double) * 2 * NY,
+                           cudaMemcpyDeviceToDevice, st));
+  ElModel<double> M =
+      make_model<double>((int)NX, (int)NY, NY + 2, 0, dt, dx, dy, lambda, mu, rho, prof);
+  ElShot<double> one{};
+  for (int f = 0; f < NF; f++) {
+    one.fin[f] = state_in + f * N;
+    one.f[f] = state_out + f * N;
+  }
+  one.fs = N;
+  dim3 grd((unsigned)div_up(NY + 2, BX), (unsigned)div_up(NX + 2, BY), 1);
+  k_el_stress<double, true, false><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  ADS_LAUNCHED(1);
+  k_el_velocity<double, true, false><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  ADS_LAUNCHED(1);
+  if (nsrc > 0) {
+    Fields5 f5{{state_out, state_out + N, state_out + 2 * N, state_out + 3 * N,
+                state_out + 4 * N}};
+    k_el_step_src<<<1, 32, 0, st>>>(f5, srci, srcj, srctype, srcv, nsrc, (int)NX, (int)NY);
+    ADS_LAUNCHED(1);
+  }
+  ADS_CUDA(cudaFreeAsync(scratch, st));
+  return ADS_OK;
+}
+
+int ads_elastic_step_bwd_f64(const double* state_in, const double* grad_out, double* grad_in,
+                             double* grad_lambda, double* grad_mu, double* grad_rho,
+                             const double* lambda, const double* mu, const double* rho,
+                             const double* ax, const double* bx, const double* ay,
+                             const double* by, double dt, double dx, double dy, int64_t NX,
+                             int64_t NY, ads_stream_t stream) {
+  if (int e = require_device()) return e;
+  ADS_REQUIRE(NX >= 4 && NY >= 4 && NX < (1 << 24) && NY < (1 << 24), "NX, NY out of range");
+  ADS_REQUIRE(state_in && grad_out && grad_in && grad_lambda && grad_mu && grad_rho &&
+                  lambda && mu && rho && ax && bx && ay && by,
+              "null pointer argument");
+  ADS_REQUIRE(grad_in != grad_out, "grad_in must not alias grad_out");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t N = (NX + 2) * (NY + 2);
+  const size_t prof_n = 4 * NX + 4 * NY;
+  // scratch: profiles, forward output state, per-step store, adjoint temps
+  const size_t n_scr = prof_n + (size_t)(NF + NSTORE + NTMP) * N;
+  double* scratch = nullptr;
+  ADS_CUDA(cudaMallocAsync((void**)&scratch, sizeof(double) * n_scr, st));
+  ADS_CUDA(cudaMemsetAsync(scratch, 0, sizeof(double) * n_scr, st));
+  double* prof = scratch;
+  ADS_CUDA(cudaMemcpyAsync(prof, ax, sizeof(double) * 2 * NX, cudaMemcpyDeviceToDevice, st));
+  ADS_CUDA(cudaMemcpyAsync(prof + 2 * NX, bx, sizeof(double) * 2 * NX, cudaMemcpyDeviceToDevice,
+                           st));
+  ADS_CUDA(cudaMemcpyAsync(prof + 4 * NX, ay, sizeof(double) * 2 * NY, cudaMemcpyDeviceToDevice,
+                           st));
+  ADS_CUDA(cudaMemcpyAsync(prof + 4 * NX + 2 * NY, by, sizeof(double) * 2 * NY,
+                           cudaMemcpyDeviceToDevice, st));
+  double* fout = scratch + prof_n;
+  double* store = fout + NF * N;
+  double* tmp = store + NSTORE * N;
+  ElModel<double> M =
+      make_model<double>((int)NX, (int)NY, NY + 2, 0, dt, dx, dy, lambda, mu, rho, prof);
+  ElShot<double> one{};
+  for (int f = 0; f < NF; f++) {
+    one.fin[f] = state_in + f * N;
+    one.f[f] = fout + f * N;
+    one.g[f] = grad_in + f * N;
+  }
+  for (int k = 0; k < NTMP; k++) one.tmp[k] = tmp + k * N;
+  one.store = store;
+  one.fs = N;
+  one.glam = grad_lambda;
+  one.gmu = grad_mu;
+  one.grho = grad_rho;
+  dim3 grd((unsigned)div_up(NY + 2, BX), (unsigned)div_up(NX + 2, BY), 1);
+  k_el_stress<double, true, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  ADS_LAUNCHED(1);
+  k_el_velocity<double, true, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  ADS_LAUNCHED(1);
+  ADS_CUDA(cudaMemcpyAsync(grad_in, grad_out, sizeof(double) * NF * N,
+                           cudaMemcpyDeviceToDevice, st));
+  k_el_adj1<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  ADS_LAUNCHED(1);
+  k_el_adj2<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  ADS_LAUNCHED(1);
+  k_el_adj3<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one);
+  ADS_LAUNCHED(1);
+  ADS_CUDA(cudaFreeAsync(scratch, st));
+  return ADS_OK;
+}
+
+int ads_elastic_plan_create(ads_elastic_plan** plan, const ads_elastic_config* cfg,
+                            const ads_elastic_shot* shots, int64_t nshots,
+                            ads_stream_t stream) {
+  ADS_REQUIRE(plan && cfg && shots, "null argument");
+  *plan = nullptr;
+  if (int e = require_device()) return e;
+  ADS_REQUIRE(cfg->precision == ADS_F64 || cfg->precision == ADS_F32,
+              "precision must be ADS_F64 or ADS_F32");
+  std::unique_ptr<ads_elastic_plan> p(new ads_elastic_plan);
+  int rc;
+  if (cfg->precision == ADS_F64) {
+    auto* q = new ElPlan<double>();
+    p->impl.reset(q);
+    rc = q->create(*cfg, shots, nshots, (cudaStream_t)stream);
+  } else {
+    auto* q = new ElPlan<float>();
+    p->impl.reset(q);
+    rc = q->create(*cfg, shots, nshots, (cudaStream_t)stream);
+  }
+  if (rc != ADS_OK) return rc;
+  *plan = p.release();
+  return ADS_OK;
+}
+
+int ads_elastic_plan_destroy(ads_elastic_plan* plan) {
+  if (!plan) return ADS_OK;
+  cudaDeviceSynchronize();
+  delete plan;
+  return ADS_OK;
+}
+
+int64_t ads_elastic_plan_trace_offset(const ads_elastic_plan* plan, int64_t shot) {
+  if (!plan || shot < 0 || shot >= (int64_t)plan->impl->trace_off.size()) return -1;
+  return plan->impl->trace_off[shot];
+}
+
+int64_t ads_elastic_plan_trace_count(const ads_elastic_plan* plan) {
+  return plan ? plan->impl->trace_total : -1;
+}
+
+int64_t ads_elastic_plan_device_bytes(const ads_elastic_plan* plan) {
+  return plan ? plan->impl->bytes : -1;
+}
+
+int64_t ads_elastic_plan_launches(const ads_elastic_plan* plan, int gradient) {
+  if (!plan) return -1;
+  return gradient ? plan->impl->launches_grad : plan->impl->launches_fwd;
+}
+
+int ads_elastic_plan_forward(ads_elastic_plan* plan, const double* lambda, const double* mu,
+                             const double* rho, void* traces, ads_stream_t stream) {
+  ADS_REQUIRE(plan, "null plan");
+  return plan->impl->forward(lambda, mu, rho, traces, (cudaStream_t)stream);
+}
+
+int ads_elastic_plan_gradient(ads_elastic_plan* plan, const double* lambda, const double* mu,
+                              const double* rho, const void* observed, double* loss,
+                              double* grad_lambda, double* grad_mu, double* grad_rho,
+                              void* traces_out, ads_stream_t stream) {
+  ADS_REQUIRE(plan, "null plan");
+  return plan->impl->gradient(lambda, mu, rho, observed, loss, grad_lambda, grad_mu, grad_rho,
+                              traces_out, (cudaStream_t)stream);
+}
+
+}  // extern "C"

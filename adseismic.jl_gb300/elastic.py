@@ -1,0 +1,248 @@
+"""Elastic host API mirroring ADSeismic's src/Struct.jl:4-78 and
+src/Core.jl:31-412,659-712 on top of the C ABI."""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import ADS_F32, ADS_F64, call, lib
+from .acoustic import _ptr, _require_cuda, _stream
+
+NFIELD = 13  # vx, vy, sigmaxx, sigmayy, sigmaxy, mem[1..8]
+
+
+@dataclass
+class ElasticPropagatorParams:
+    """src/Struct.jl:4-32 (same fields and defaults)."""
+    NX: int = 101
+    NY: int = 641
+    NSTEP: int = 2000 * 2
+    DELTAX: float = 10.0
+    DELTAY: float = 10.0
+    DELTAT: float = 2.0e-3 / 2
+    f0: float = 5.0
+    vp_ref: float = 2000.0
+    USE_PML_XMIN: bool = True
+    USE_PML_XMAX: bool = True
+    USE_PML_YMIN: bool = True
+    USE_PML_YMAX: bool = True
+    NPOINTS_PML: int = 12
+    NPOWER: float = 2.0
+    K_MAX_PML: float = 1.0
+    ALPHA_MAX_PML: float = None  # default 2 pi (f0/2), as Struct.jl:25
+    Rcoef: float = 0.001
+    IT_DISPLAY: int = 0
+
+    def __post_init__(self):
+        if self.ALPHA_MAX_PML is None:
+            self.ALPHA_MAX_PML = 2.0 * math.pi * (self.f0 / 2.0)
+
+    @property
+    def use_pml(self) -> int:
+        return (int(self.USE_PML_XMIN) | int(self.USE_PML_XMAX) << 1 |
+                int(self.USE_PML_YMIN) << 2 | int(self.USE_PML_YMAX) << 3)
+
+
+@dataclass
+class ElasticSource:
+    """src/Struct.jl:50-55: srctype 0 vx, 1 vy, 2 sxx, 3 syy, 4 sxy; srcv (NSTEP, nsrc)."""
+    srci: np.ndarray
+    srcj: np.ndarray
+    srctype: np.ndarray
+    srcv: np.ndarray
+
+
+@dataclass
+class ElasticReceiver:
+    """src/Struct.jl:57-62; rcvv (nrcv, NSTEP+1) after SimulatedObservation."""
+    rcvi: np.ndarray
+    rcvj: np.ndarray
+    rcvtype: np.ndarray
+    rcvv: object = None
+
+
+def compute_PML_Params(param: ElasticPropagatorParams):
+    """src/Core.jl:231-407: (ax, bx, kx, ay, by, ky) as (2, NX) and (2, NY) arrays."""
+    NX, NY = param.NX, param.NY
+    a = [np.empty(2 * NX) for _ in range(3)] + [np.empty(2 * NY) for _ in range(3)]
+    call("ads_elastic_cpml_profiles", NX, NY, param.DELTAX, param.DELTAY, param.DELTAT,
+         param.NPOINTS_PML, param.NPOWER, param.K_MAX_PML, param.ALPHA_MAX_PML, param.vp_ref,
+         param.Rcoef, param.use_pml, *[x.ctypes.data_as(C.c_void_p) for x in a])
+    return tuple(x.reshape(2, -1) for x in a)
+
+
+def elastic_one_step(param: ElasticPropagatorParams, rho, lam, mu, state, profiles,
+                     srci=None, srcj=None, srcv=None, srctype=None):
+    """one_step of src/Core.jl:215-228 on CUDA float64 tensors.  state: (13, N)
+    (vx, vy, sxx, syy, sxy, mem[1..8]); profiles: (ax, bx, kx, ay, by, ky) tensors;
+    srcv: this step's (nsrc,) values.  Returns the new (13, N) state."""
+    NX, NY = param.NX, param.NY
+    ts = [rho, lam, mu, state]
+    _require_cuda(*ts)
+    state = state.contiguous().to(torch.float64)
+    out = torch.empty_like(state)
+    ax, bx, kx, ay, by, ky = [torch.as_tensor(p, dtype=torch.float64, device=state.device)
+                              .contiguous() for p in profiles]
+    if srci is not None and len(srci):
+        dev = state.device
+        si = torch.as_tensor(np.asarray(srci), dtype=torch.int64, device=dev)
+        sj = torch.as_tensor(np.asarray(srcj), dtype=torch.int64, device=dev)
+        stp = torch.as_tensor(np.asarray(srctype), dtype=torch.int64, device=dev)
+        sv = torch.as_tensor(srcv, dtype=torch.float64, device=dev).contiguous()
+        nsrc = len(srci)
+    else:
+        si = sj = stp = sv = None
+        nsrc = 0
+    lam, mu, rho = (t.contiguous().to(torch.float64) for t in (lam, mu, rho))
+    call("ads_elastic_step_fwd_f64", _ptr(state), _ptr(out), _ptr(lam), _ptr(mu), _ptr(rho),
+         _ptr(ax), _ptr(bx), _ptr(kx), _ptr(ay), _ptr(by), _ptr(ky), param.DELTAT,
+         param.DELTAX, param.DELTAY, NX, NY, _ptr(si), _ptr(sj), _ptr(stp), _ptr(sv), nsrc,
+         _stream())
+    return out
+
+
+def elastic_one_step_grad(param: ElasticPropagatorParams, rho, lam, mu, state, grad_out,
+                          profiles):
+    """Transpose of elastic_one_step about `state`: returns (grad_state, grad_lambda,
+    grad_mu, grad_rho)."""
+    dev = state.device
+    state = state.contiguous().to(torch.float64)
+    gout = grad_out.contiguous().to(torch.float64)
+    gin = torch.empty_like(state)
+    N = state.shape[-1]
+    gl, gm, gr = (torch.zeros(N, dtype=torch.float64, device=dev) for _ in range(3))
+    ax, bx, kx, ay, by, ky = [torch.as_tensor(p, dtype=torch.float64, device=dev).contiguous()
+                              for p in profiles]
+    lam, mu, rho = (t.contiguous().to(torch.float64) for t in (lam, mu, rho))
+    call("ads_elastic_step_bwd_f64", _ptr(state), _ptr(gout), _ptr(gin), _ptr(gl), _ptr(gm),
+         _ptr(gr), _ptr(lam), _ptr(mu), _ptr(rho), _ptr(ax), _ptr(bx), _ptr(ay), _ptr(by),
+         param.DELTAT, param.DELTAX, param.DELTAY, param.NX, param.NY, _stream())
+    return gin, gl, gm, gr
+
+
+class ElasticPlan:
+    """Persistent multi-shot elastic plan: forward traces, misfit and the
+    gradient w.r.t. lambda, mu, rho.  shots: list of dicts with srci, srcj,
+    srctype, srcv (NSTEP, nsrc), rcvi, rcvj, rcvtype."""
+
+    def __init__(self, param: ElasticPropagatorParams, shots, precision="f64",
+                 use_graph=True, ckpt_every=0, stream=None):
+        cfg = _lib.ElasticConfig()
+        cfg.NX, cfg.NY, cfg.NSTEP = param.NX, param.NY, param.NSTEP
+        cfg.dx, cfg.dy, cfg.dt = param.DELTAX, param.DELTAY, param.DELTAT
+        cfg.npml, cfg.npower, cfg.k_max = param.NPOINTS_PML, param.NPOWER, param.K_MAX_PML
+        cfg.alpha_max, cfg.vp_ref, cfg.Rcoef = param.ALPHA_MAX_PML, param.vp_ref, param.Rcoef
+        cfg.use_pml = param.use_pml
+        cfg.precision = ADS_F64 if precision == "f64" else ADS_F32
+        cfg.use_graph = int(bool(use_graph))
+        cfg.ckpt_every = ckpt_every
+        self.param = param
+        self.dtype = torch.float64 if precision == "f64" else torch.float32
+        self._keep = []
+        arr = (_lib.ElasticShot * len(shots))()
+        for k, s in enumerate(shots):
+            vals = [np.ascontiguousarray(s[n], dtype=np.int64)
+                    for n in ("srci", "srcj", "srctype", "rcvi", "rcvj", "rcvtype")]
+            nsrc = len(vals[0])
+            srcv = np.ascontiguousarray(s["srcv"], dtype=np.float64)
+            srcv = srcv.reshape(-1, nsrc) if nsrc else np.zeros((0, 1))
+            self._keep += vals + [srcv]
+            a = arr[k]
+            a.nsrc = nsrc
+            a.srci, a.srcj, a.srctype = (v.ctypes.data for v in vals[:3])
+            a.srcv, a.srcv_rows = srcv.ctypes.data, srcv.shape[0] if nsrc else 0
+            a.nrcv = len(vals[3])
+            a.rcvi, a.rcvj, a.rcvtype = (v.ctypes.data for v in vals[3:])
+        self.shots = shots
+        h = C.c_void_p()
+        call("ads_elastic_plan_create", C.byref(h), C.byref(cfg), arr, len(shots),
+             stream if stream is not None else _stream())
+        self._h = h
+        L = lib()
+        self.trace_count = L.ads_elastic_plan_trace_count(h)
+        self.trace_offsets = [L.ads_elastic_plan_trace_offset(h, k) for k in range(len(shots))]
+        self.device_bytes = L.ads_elastic_plan_device_bytes(h)
+        self.launches_forward = L.ads_elastic_plan_launches(h, 0)
+        self.launches_gradient = L.ads_elastic_plan_launches(h, 1)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ads_elastic_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def split_traces(self, packed):
+        nt = self.param.NSTEP + 1
+        out = []
+        for k, s in enumerate(self.shots):
+            n = len(s["rcvi"]) * nt
+            o = self.trace_offsets[k]
+            out.append(packed[o:o + n].view(len(s["rcvi"]), nt))
+        return out
+
+    def pack(self, per_shot):
+        return torch.cat([t.reshape(-1).to(self.dtype) for t in per_shot])
+
+    def forward(self, lam, mu, rho):
+        _require_cuda(lam, mu, rho)
+        lam, mu, rho = (t.contiguous().to(torch.float64) for t in (lam, mu, rho))
+        tr = torch.empty(max(self.trace_count, 1), dtype=self.dtype, device=lam.device)
+        call("ads_elastic_plan_forward", self._h, _ptr(lam), _ptr(mu), _ptr(rho), _ptr(tr),
+             _stream())
+        return tr[:self.trace_count]
+
+    def gradient(self, lam, mu, rho, observed, want_traces=False):
+        _require_cuda(lam, mu, rho, observed)
+        lam, mu, rho = (t.contiguous().to(torch.float64) for t in (lam, mu, rho))
+        obs = observed.contiguous().to(self.dtype)
+        loss = torch.empty(1, dtype=torch.float64, device=lam.device)
+        gl, gm, gr = (torch.empty_like(lam) for _ in range(3))
+        tr = (torch.empty(max(self.trace_count, 1), dtype=self.dtype, device=lam.device)
+              if want_traces else None)
+        call("ads_elastic_plan_gradient", self._h, _ptr(lam), _ptr(mu), _ptr(rho), _ptr(obs),
+             _ptr(loss), _ptr(gl), _ptr(gm), _ptr(gr), _ptr(tr), _stream())
+        if want_traces:
+            return loss[0], gl, gm, gr, tr[:self.trace_count]
+        return loss[0], gl, gm, gr
+
+
+class ElasticPropagator:
+    """Result handle of ElasticPropagatorSolver (src/Struct.jl:64-73)."""
+
+    def __init__(self, param, src, rho, lam, mu, precision):
+        self.param, self.src, self.rho, self.lam, self.mu = param, src, rho, lam, mu
+        self.precision = precision
+
+
+def ElasticPropagatorSolver(param: ElasticPropagatorParams, src: ElasticSource, rho, lam, mu,
+                            precision="f64"):
+    """src/Core.jl:31-94 (argument order rho, lambda, mu as the reference)."""
+    return ElasticPropagator(param, src, rho, lam, mu, precision)
+
+
+def _eshot(src, rcv):
+    return dict(srci=src.srci, srcj=src.srcj, srctype=src.srctype, srcv=src.srcv,
+                rcvi=rcv.rcvi, rcvj=rcv.rcvj, rcvtype=rcv.rcvtype)
+
+
+def SimulatedObservation(ep: ElasticPropagator, rcv: ElasticReceiver):
+    """src/Core.jl:701-712: rcv.rcvv = (nrcv, NSTEP+1) traces."""
+    plan = ElasticPlan(ep.param, [_eshot(ep.src, rcv)], precision=ep.precision,
+                       use_graph=False)
+    dev = "cuda"
+    f = lambda a: torch.as_tensor(a, dtype=torch.float64, device=dev).reshape(-1)
+    tr = plan.forward(f(ep.lam), f(ep.mu), f(ep.rho))
+    torch.cuda.current_stream().synchronize()
+    plan.close()
+    rcv.rcvv = tr.view(len(rcv.rcvi), ep.param.NSTEP + 1)
+    return rcv.rcvv

@@ -1,0 +1,244 @@
+"""Acoustic parity on the GPU through the C ABI: the single-step drop-in against
+the reference's compiled operator (golden, bit-exact), the whole-path FP64
+forward/gradient against the oracle (rel-L2 <= 1e-12), FP32 against the FP64
+oracle (rel-L2 <= 1e-4 on the gradient), uneven multi-shot batches, edge cases."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12   # FP64 drop-in vs reference CPU operators (rel-L2)
+TOL32 = 1e-4    # FP32 stencils / FP64 accumulation vs FP64 oracle (rel-L2, gradient)
+
+
+def rel(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def T(x, dev, dtype=torch.float64):
+    return torch.as_tensor(np.asarray(x), dtype=dtype, device=dev)
+
+
+def test_step_forward_bitexact_with_reference(ads, cuda):
+    g = golden("acoustic_step.npz")
+    NX, NY = int(g["NX"]), int(g["NY"])
+    ins = [T(g[k], cuda) for k in ("w", "wold", "phi", "psi", "sigma", "tau", "c")]
+    u, po, qo = ads.acoustic_one_step(*ins, float(g["dt"]), float(g["hx"]), float(g["hy"]), NX,
+                                      NY)
+    assert np.array_equal(u.cpu().numpy(), g["u"])
+    assert np.array_equal(po.cpu().numpy(), g["phiout"])
+    assert np.array_equal(qo.cpu().numpy(), g["psiout"])
+
+
+def test_step_backward_matches_reference(ads, cuda):
+    g = golden("acoustic_step.npz")
+    NX, NY = int(g["NX"]), int(g["NY"])
+    ins = [T(g[k], cuda) for k in ("w", "wold", "phi", "psi", "sigma", "tau", "c")]
+    gs = [T(g[k], cuda) for k in ("grad_u", "grad_phiout", "grad_psiout")]
+    outs = [T(g[k], cuda) for k in ("u", "phiout", "psiout")]
+    got = ads.acoustic_one_step_grad(*gs, *ins, float(g["dt"]), float(g["hx"]), float(g["hy"]),
+                                     NX, NY, *outs)
+    for t, k in zip(got, ("grad_w", "grad_wold", "grad_phi", "grad_psi", "grad_c")):
+        assert rel(t.cpu().numpy(), g[k]) <= 1e-14, k
+
+
+@pytest.mark.parametrize("variant", [0, 1])
+@pytest.mark.parametrize("shape", [(1, 1), (7, 3), (45, 70)])
+def test_step_random_vs_oracle(ads, orc, cuda, variant, shape):
+    NX, NY = shape
+    N = (NX + 2) * (NY + 2)
+    rng = np.random.default_rng(NX * 100 + NY + variant)
+    ins = [rng.standard_normal(N) for _ in range(7)]
+    ref = orc.acoustic_step_fwd(*ins, 0.01, 0.3, 0.2, NX, NY, variant=variant)
+    got = ads.acoustic_one_step(*[T(x, cuda) for x in ins], 0.01, 0.3, 0.2, NX, NY, variant)
+    for a, b in zip(got, ref):
+        assert rel(a.cpu().numpy(), b) <= 1e-15
+    gs = [rng.standard_normal(N) for _ in range(3)]
+    refg = orc.acoustic_step_bwd(*gs, *ins, 0.01, 0.3, 0.2, NX, NY, *ref, variant=variant)
+    gotg = ads.acoustic_one_step_grad(*[T(x, cuda) for x in gs], *[T(x, cuda) for x in ins],
+                                      0.01, 0.3, 0.2, NX, NY, *[T(x, cuda) for x in ref],
+                                      variant)
+    for a, b in zip(gotg, refg):
+        assert rel(a.cpu().numpy(), b) <= 1e-13
+
+
+def test_step_f32_close_to_f64(ads, orc, cuda):
+    NX, NY = 30, 41
+    N = (NX + 2) * (NY + 2)
+    rng = np.random.default_rng(0)
+    ins = [rng.random(N) for _ in range(7)]
+    ref = orc.acoustic_step_fwd(*ins, 0.1, 1.0, 1.0, NX, NY)
+    got = ads.acoustic_one_step(*[T(x, cuda, torch.float32) for x in ins], 0.1, 1.0, 1.0, NX, NY)
+    for a, b in zip(got, ref):
+        assert rel(a.double().cpu().numpy(), b) <= 1e-6
+
+
+def test_autograd_function_matches_oracle(ads, orc, cuda):
+    NX, NY = 12, 9
+    N = (NX + 2) * (NY + 2)
+    rng = np.random.default_rng(5)
+    ins = [T(rng.random(N), cuda).requires_grad_(True) for _ in range(7)]
+    u, po, qo = ads.AcousticOneStep.apply(*ins, 0.1, 0.5, 0.5, NX, NY, 0)
+    wu, wp, wq = (rng.standard_normal(N) for _ in range(3))
+    (u * T(wu, cuda) + po * T(wp, cuda) + qo * T(wq, cuda)).sum().backward()
+    args = [t.detach().cpu().numpy() for t in ins]
+    refo = orc.acoustic_step_fwd(*args, 0.1, 0.5, 0.5, NX, NY)
+    refg = orc.acoustic_step_bwd(wu, wp, wq, *args, 0.1, 0.5, 0.5, NX, NY, *refo)
+    for t, r in zip((ins[0], ins[1], ins[2], ins[3], ins[6]), refg):
+        assert rel(t.grad.cpu().numpy(), r) <= 1e-13
+
+
+def loop_case(g):
+    NX, NY, Tn = int(g["NX"]), int(g["NY"]), int(g["NSTEP"])
+    shot = dict(x0=0, nx=NX, nstep=Tn, srci=g["srci"], srcj=g["srcj"], srcv=g["srcv"],
+                rcvi=g["rcvi"], rcvj=g["rcvj"])
+    return NX, NY, Tn, shot
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+@pytest.mark.parametrize("ckpt", [0, 1, 7, 79])
+def test_plan_fp64_matches_reference_golden(ads, cuda, use_graph, ckpt):
+    g = golden("acoustic_loop.npz")
+    NX, NY, Tn, shot = loop_case(g)
+    h, dt = float(g["h"]), float(g["dt"])
+    plan = ads.AcousticPlan(NX, NY, h, h, dt, [shot], npml=int(g["npml"]),
+                            vp_ref=float(g["vp_ref"]), precision="f64", use_graph=use_graph,
+                            ckpt_every=ckpt)
+    vp = T(g["vp"].reshape(NX + 2, NY + 2), cuda)
+    tr = plan.forward(vp)
+    assert rel(tr.cpu().numpy(), g["rcvv"].reshape(-1)) <= TOL64
+    loss, grad, tr2 = plan.gradient(vp, T(g["obs"].reshape(-1), cuda), want_traces=True)
+    torch.cuda.synchronize()
+    assert abs(float(loss) - float(g["loss"])) <= TOL64 * float(g["loss"])
+    assert rel(grad.cpu().numpy().reshape(-1), g["grad_vp"]) <= TOL64
+    assert torch.equal(tr, tr2)
+    plan.close()
+
+
+def test_plan_fp32_vs_fp64_oracle(ads, cuda):
+    g = golden("acoustic_loop.npz")
+    NX, NY, Tn, shot = loop_case(g)
+    h, dt = float(g["h"]), float(g["dt"])
+    plan = ads.AcousticPlan(NX, NY, h, h, dt, [shot], npml=int(g["npml"]),
+                            vp_ref=float(g["vp_ref"]), precision="f32", ckpt_every=10)
+    vp = T(g["vp"].reshape(NX + 2, NY + 2), cuda)
+    loss, grad, tr = plan.gradient(vp, T(g["obs"].reshape(-1), cuda, torch.float32),
+                                   want_traces=True)
+    torch.cuda.synchronize()
+    assert rel(tr.double().cpu().numpy(), g["rcvv"].reshape(-1)) <= 1e-5
+    assert rel(grad.cpu().numpy().reshape(-1), g["grad_vp"]) <= TOL32
+    assert abs(float(loss) - float(g["loss"])) <= 1e-4 * float(g["loss"])
+    plan.close()
+
+
+def uneven_case(seed, MX=70, MY=33, nshots=5, precision_rows=None):
+    rng = np.random.default_rng(seed)
+    shots = []
+    for s in range(nshots):
+        nx = int(rng.integers(20, 50))
+        x0 = int(rng.integers(0, MX - nx + 1))
+        nstep = int(rng.integers(30, 90))
+        nsrc = int(rng.integers(0, 3)) if s else 1
+        nrcv = int(rng.integers(0, nx - 2)) if s != 1 else 0
+        srci = rng.integers(2, nx + 2, nsrc)
+        srcj = rng.integers(2, MY + 2, nsrc)
+        rcvi = rng.integers(1, nx + 3, nrcv)
+        rcvj = rng.integers(1, MY + 3, nrcv)
+        if nrcv > 3:  # duplicate receivers and a frame receiver
+            rcvi[1], rcvj[1] = rcvi[0], rcvj[0]
+            rcvi[2] = 1
+        if nsrc == 2:  # two sources on one cell
+            srci[1], srcj[1] = srci[0], srcj[0]
+        shots.append(dict(x0=x0, nx=nx, nstep=nstep, srci=srci, srcj=srcj,
+                          srcv=rng.standard_normal((nstep, nsrc)) * 1e3, rcvi=rcvi,
+                          rcvj=rcvj))
+    vp = 1800 + 900 * rng.random((MX + 2, MY + 2))
+    return MX, MY, shots, vp
+
+
+def oracle_multishot(orc, MX, MY, shots, vp, h, dt, npml, vp_ref, obs=None):
+    traces, loss, grad = [], 0.0, np.zeros_like(vp)
+    for k, s in enumerate(shots):
+        nx = s["nx"]
+        win = vp[s["x0"]:s["x0"] + nx + 2].reshape(-1)
+        sx, ty = orc.acoustic_pml(nx, MY, h, h, npml, vp_ref)
+        if obs is None:
+            traces.append(orc.acoustic_forward(nx, MY, s["nstep"], dt, h, h, sx, ty, win,
+                                               s["srci"], s["srcj"], s["srcv"], s["rcvi"],
+                                               s["rcvj"]))
+        else:
+            l, gk = orc.acoustic_gradient(nx, MY, s["nstep"], dt, h, h, sx, ty, win, s["srci"],
+                                          s["srcj"], s["srcv"], s["rcvi"], s["rcvj"], obs[k])
+            loss += l
+            grad[s["x0"]:s["x0"] + nx + 2] += gk.reshape(nx + 2, MY + 2)
+    return traces if obs is None else (loss, grad)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+@pytest.mark.parametrize("rows", [0, 1, 3])
+def test_plan_uneven_multishot_vs_oracle(ads, orc, cuda, precision, rows):
+    MX, MY, shots, vp = uneven_case(21)
+    h, dt, npml, vref = 10.0, 1e-3, 5, 1500.0
+    ref_tr = oracle_multishot(orc, MX, MY, shots, vp, h, dt, npml, vref)
+    rng = np.random.default_rng(3)
+    obs = [t * 0.95 + 1e-3 * rng.standard_normal(t.shape) for t in ref_tr]
+    ref_loss, ref_grad = oracle_multishot(orc, MX, MY, shots, vp, h, dt, npml, vref, obs)
+    plan = ads.AcousticPlan(MX, MY, h, h, dt, shots, npml=npml, vp_ref=vref,
+                            precision=precision, ckpt_every=13, rows_per_thread=rows)
+    dtype = plan.dtype
+    tr = plan.forward(T(vp, cuda))
+    got = plan.split_traces(tr)
+    tol_tr = TOL64 if precision == "f64" else 1e-5
+    for a, b in zip(got, ref_tr):
+        if b.size:
+            assert rel(a.double().cpu().numpy(), b) <= tol_tr
+    loss, grad = plan.gradient(T(vp, cuda), plan.pack([T(o, cuda, dtype) for o in obs]))
+    torch.cuda.synchronize()
+    tol = TOL64 if precision == "f64" else TOL32
+    assert abs(float(loss) - ref_loss) <= tol * ref_loss
+    assert rel(grad.cpu().numpy(), ref_grad) <= tol
+    plan.close()
+
+
+def test_repeated_calls_are_deterministic(ads, cuda):
+    MX, MY, shots, vp = uneven_case(5, nshots=3)
+    plan = ads.AcousticPlan(MX, MY, 10.0, 10.0, 1e-3, shots, npml=5, precision="f32")
+    obs = torch.zeros(plan.trace_count, dtype=torch.float32, device=cuda)
+    l1, g1 = plan.gradient(T(vp, cuda), obs)
+    l2, g2 = plan.gradient(T(vp, cuda), obs)
+    assert torch.equal(g1, g2) and float(l1) == float(l2)
+    plan.close()
+
+
+def test_invalid_geometry_rejected(ads, cuda):
+    shot = dict(x0=0, nx=10, nstep=20, srci=[1], srcj=[5], srcv=np.zeros((20, 1)),
+                rcvi=[3], rcvj=[3])
+    with pytest.raises(ads.AdsError, match="interior"):
+        ads.AcousticPlan(10, 10, 10.0, 10.0, 1e-3, [shot])
+    shot = dict(x0=5, nx=10, nstep=20, srci=[4], srcj=[5], srcv=np.zeros((20, 1)),
+                rcvi=[3], rcvj=[3])
+    with pytest.raises(ads.AdsError, match="window"):
+        ads.AcousticPlan(10, 10, 10.0, 10.0, 1e-3, [shot])
+    shot = dict(x0=0, nx=10, nstep=20, srci=[4], srcj=[5], srcv=np.zeros((19, 1)),
+                rcvi=[3], rcvj=[3])
+    with pytest.raises(ads.AdsError, match="rows"):
+        ads.AcousticPlan(10, 10, 10.0, 10.0, 1e-3, [shot])
+
+
+def test_julia_style_api(ads, orc, cuda):
+    g = golden("acoustic_loop.npz")
+    NX, NY, Tn = int(g["NX"]), int(g["NY"]), int(g["NSTEP"])
+    p = ads.AcousticPropagatorParams(NX=NX, NY=NY, NSTEP=Tn, DELTAX=float(g["h"]),
+                                     DELTAY=float(g["h"]), DELTAT=float(g["dt"]),
+                                     NPOINTS_PML=int(g["npml"]), vp_ref=float(g["vp_ref"]))
+    src = ads.AcousticSource(g["srci"], g["srcj"], g["srcv"])
+    rcv = ads.AcousticReceiver(g["rcvi"], g["rcvj"])
+    ap = ads.AcousticPropagatorSolver(p, src, g["vp"])
+    ads.SimulatedObservation(ap, rcv)
+    assert rel(rcv.rcvv.cpu().numpy(), g["rcvv"]) <= TOL64
+    loss, grad = ads.compute_loss_and_grads_GPU(p, [src], [rcv], [g["obs"]], g["vp"])
+    assert rel(grad.cpu().numpy().reshape(-1), g["grad_vp"]) <= TOL64

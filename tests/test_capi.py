@@ -1,0 +1,82 @@
+"""The C-ABI library loads and exports every symbol include/*.h declares; the
+host-only helpers agree with the oracle.  No device compute is called here."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(ads_\w+)\s*\(", src,
+                             re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for n in ("ads_acoustic_step_fwd_f64", "ads_acoustic_step_bwd_f64", "ads_add_source_f64",
+              "ads_get_receive_f64", "ads_elastic_step_fwd_f64", "ads_acoustic_plan_gradient",
+              "ads_elastic_plan_gradient"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(ads):
+    lib = ctypes.CDLL(ads.LIB_PATH)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_the_header(ads):
+    from adseismic_gb300 import _lib
+
+    assert set(declared_functions()) <= set(_lib.EXPORTED)
+
+
+def test_pml_profiles_match_oracle(ads, orc):
+    NX, NY = 40, 30
+    p = ads.AcousticPropagatorParams(NX=NX, NY=NY, DELTAX=10.0, DELTAY=12.0, NPOINTS_PML=7,
+                                     vp_ref=1800.0)
+    Sx, Sy = ads.compute_acoustic_PML_Params(p)
+    s, t = orc.acoustic_pml(NX, NY, 10.0, 12.0, 7, 1800.0)
+    assert np.array_equal(Sx.reshape(-1), s) and np.array_equal(Sy.reshape(-1), t)
+
+
+def test_cpml_profiles_match_oracle(ads, orc):
+    p = ads.ElasticPropagatorParams(NX=50, NY=40, DELTAX=10.0, DELTAY=11.0, DELTAT=8e-4,
+                                    NPOINTS_PML=9, vp_ref=3100.0, f0=7.0)
+    got = ads.compute_elastic_PML_Params(p)
+    ref = orc.elastic_cpml(50, 40, 10.0, 11.0, 8e-4, 9, 3100.0, 7.0)
+    for a, b in zip(got, ref):
+        assert np.allclose(a.reshape(-1), b, rtol=1e-15, atol=1e-300)
+
+
+def test_invalid_arguments_are_rejected_without_launch(ads):
+    from adseismic_gb300 import _lib
+
+    L = _lib.lib()
+    rc = L.ads_acoustic_pml_profiles(0, 5, 1.0, 1.0, 3, 1000.0, 0.001, 15, None, None)
+    assert rc == _lib.ADS_ERR_INVALID
+    assert "NX" in L.ads_last_error().decode()
+
+
+def test_compute_calls_fail_loudly_without_gpu(ads):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from adseismic_gb300 import _lib
+
+    rc = _lib.lib().ads_acoustic_step_fwd_f64(*([None] * 7), 0.1, 0.1, 0.1, 4, 4, None, None,
+                                             None, 0, None)
+    assert rc == _lib.ADS_ERR_CUDA
+    assert "no CUDA device" in _lib.lib().ads_last_error().decode()

@@ -1,0 +1,134 @@
+"""Elastic parity on the GPU: single step and its transpose against the oracle,
+whole-path FP64 traces/gradients (rel-L2 <= 1e-12) and FP32 against the FP64
+oracle."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def params(ads, g, T=None):
+    return ads.ElasticPropagatorParams(NX=int(g["NX"]), NY=int(g["NY"]),
+                                       NSTEP=int(T or g["NSTEP"]), DELTAX=float(g["dx"]),
+                                       DELTAY=float(g["dy"]), DELTAT=float(g["dt"]),
+                                       NPOINTS_PML=int(g["npml"]), vp_ref=float(g["vp_ref"]),
+                                       f0=float(g["f0"]))
+
+
+def test_step_forward_and_transpose_vs_oracle(ads, orc, cuda):
+    g = golden("elastic_small.npz")
+    p = params(ads, g)
+    NX, NY = p.NX, p.NY
+    N = (NX + 2) * (NY + 2)
+    prof = ads.compute_elastic_PML_Params(p)
+    ax, bx, kx, ay, by, ky = [a.reshape(-1) for a in prof]
+    rng = np.random.default_rng(12)
+    st = rng.standard_normal(13 * N)
+    lam, mu, rho = g["lam"], g["mu"], g["rho"]
+    srci, srcj, srct, srcv = [15, 3, 15], [10, 4, 10], [2, 0, 2], [1.5, -2.0, 0.25]
+    ref = orc.elastic_step_fwd(st, lam, mu, rho, ax, bx, ay, by, p.DELTAT, p.DELTAX, p.DELTAY,
+                               NX, NY, srci, srcj, srct, srcv)
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=cuda)
+    got = ads.elastic_one_step(p, t(rho), t(lam), t(mu), t(st).view(13, N), prof, srci, srcj,
+                               srcv, srct)
+    assert rel(got.cpu().numpy().reshape(-1), ref) <= 1e-14
+    w = rng.standard_normal(13 * N)
+    gin, gl, gm, gr = orc.elastic_step_bwd(st, w, lam, mu, rho, ax, bx, ay, by, p.DELTAT,
+                                           p.DELTAX, p.DELTAY, NX, NY)
+    Gin, Gl, Gm, Gr = ads.elastic_one_step_grad(p, t(rho), t(lam), t(mu), t(st).view(13, N),
+                                                t(w).view(13, N), prof)
+    assert rel(Gin.cpu().numpy().reshape(-1), gin) <= 1e-13
+    for a, b in ((Gl, gl), (Gm, gm), (Gr, gr)):
+        assert rel(a.cpu().numpy(), b) <= 1e-13
+
+
+def shots_from(g):
+    return [dict(srci=g["srci"], srcj=g["srcj"], srctype=g["srctype"], srcv=g["srcv"],
+                 rcvi=g["rcvi"], rcvj=g["rcvj"], rcvtype=g["rcvtype"])]
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+@pytest.mark.parametrize("ckpt", [0, 1, 17])
+def test_plan_fp64_vs_oracle(ads, cuda, use_graph, ckpt):
+    g = golden("elastic_small.npz")
+    p = params(ads, g)
+    plan = ads.ElasticPlan(p, shots_from(g), precision="f64", use_graph=use_graph,
+                           ckpt_every=ckpt)
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=cuda)
+    tr = plan.forward(t(g["lam"]), t(g["mu"]), t(g["rho"]))
+    assert rel(tr.cpu().numpy(), g["rcvv"].reshape(-1)) <= 1e-12
+    loss, gl, gm, gr = plan.gradient(t(g["lam"]), t(g["mu"]), t(g["rho"]),
+                                     t(g["obs"].reshape(-1)))
+    torch.cuda.synchronize()
+    assert abs(float(loss) - float(g["loss"])) <= 1e-12 * float(g["loss"])
+    for a, k in ((gl, "grad_lambda"), (gm, "grad_mu"), (gr, "grad_rho")):
+        assert rel(a.cpu().numpy(), g[k]) <= 1e-12, k
+    plan.close()
+
+
+def test_plan_fp32_vs_fp64_oracle(ads, cuda):
+    g = golden("elastic_small.npz")
+    p = params(ads, g)
+    plan = ads.ElasticPlan(p, shots_from(g), precision="f32", ckpt_every=9)
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=cuda)
+    loss, gl, gm, gr, tr = plan.gradient(t(g["lam"]), t(g["mu"]), t(g["rho"]),
+                                         torch.as_tensor(g["obs"].reshape(-1), device=cuda),
+                                         want_traces=True)
+    torch.cuda.synchronize()
+    assert rel(tr.double().cpu().numpy(), g["rcvv"].reshape(-1)) <= 1e-5
+    for a, k in ((gl, "grad_lambda"), (gm, "grad_mu"), (gr, "grad_rho")):
+        assert rel(a.cpu().numpy(), g[k]) <= 1e-4, k
+    plan.close()
+
+
+def test_multishot_sum_and_julia_api(ads, orc, cuda):
+    g = golden("elastic_small.npz")
+    p = params(ads, g, T=35)
+    NX, NY = p.NX, p.NY
+    prof = ads.compute_elastic_PML_Params(p)
+    ax, bx, kx, ay, by, ky = [a.reshape(-1) for a in prof]
+    rng = np.random.default_rng(2)
+    shots, obs = [], []
+    for s in range(3):
+        ns = s + 1
+        sh = dict(srci=rng.integers(3, NX, ns), srcj=rng.integers(3, NY, ns),
+                  srctype=rng.integers(0, 5, ns), srcv=rng.standard_normal((35, ns)) * 1e5,
+                  rcvi=rng.integers(1, NX + 3, 7), rcvj=rng.integers(1, NY + 3, 7),
+                  rcvtype=rng.integers(0, 5, 7))
+        shots.append(sh)
+        obs.append(rng.standard_normal((7, 36)) * 1e-3)
+    ref_loss, RL, RM, RR = 0.0, 0, 0, 0
+    for sh, o in zip(shots, obs):
+        l, a, b, c = orc.elastic_gradient(NX, NY, 35, p.DELTAT, p.DELTAX, p.DELTAY, ax, bx, ay,
+                                          by, g["lam"], g["mu"], g["rho"], sh["srci"],
+                                          sh["srcj"], sh["srctype"], sh["srcv"], sh["rcvi"],
+                                          sh["rcvj"], sh["rcvtype"], o)
+        ref_loss += l
+        RL, RM, RR = RL + a, RM + b, RR + c
+    plan = ads.ElasticPlan(p, shots, precision="f64", ckpt_every=8)
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=cuda)
+    loss, gl, gm, gr = plan.gradient(t(g["lam"]), t(g["mu"]), t(g["rho"]),
+                                     plan.pack([t(o) for o in obs]))
+    torch.cuda.synchronize()
+    assert abs(float(loss) - ref_loss) <= 1e-12 * ref_loss
+    for a, b in ((gl, RL), (gm, RM), (gr, RR)):
+        assert rel(a.cpu().numpy(), b) <= 1e-12
+    plan.close()
+    src = ads.ElasticSource(shots[0]["srci"], shots[0]["srcj"], shots[0]["srctype"],
+                            shots[0]["srcv"])
+    rcv = ads.ElasticReceiver(shots[0]["rcvi"], shots[0]["rcvj"], shots[0]["rcvtype"])
+    ep = ads.ElasticPropagatorSolver(p, src, g["rho"], g["lam"], g["mu"])
+    ads.ElasticSimulatedObservation(ep, rcv)
+    ref = orc.elastic_forward(NX, NY, 35, p.DELTAT, p.DELTAX, p.DELTAY, ax, bx, ay, by,
+                              g["lam"], g["mu"], g["rho"], shots[0]["srci"], shots[0]["srcj"],
+                              shots[0]["srctype"], shots[0]["srcv"], shots[0]["rcvi"],
+                              shots[0]["rcvj"], shots[0]["rcvtype"])
+    assert rel(rcv.rcvv.cpu().numpy(), ref) <= 1e-12

@@ -1,0 +1,41 @@
+"""Host-side logic: wavelets and material transforms against the reference
+formulas, synthetic model generators, parameter defaults."""
+import math
+
+import numpy as np
+
+
+def test_ricker_matches_formula(ads):
+    p = ads.AcousticPropagatorParams(NSTEP=300, DELTAT=1e-3)
+    a, shift = ads.ricker_width_samples(10.0, 1e-3), 150.0
+    w = ads.Ricker(p, a, shift, 2.0)
+    x = np.arange(1, 301) - shift
+    A = 2 / (math.sqrt(3 * a) * math.pi ** 0.25)
+    ref = 2.0 * A * (1 - x ** 2 / a ** 2) * np.exp(-x ** 2 / (2 * a ** 2))
+    assert np.allclose(w, ref, rtol=1e-14, atol=0)
+    assert np.argmax(w) == 149
+
+
+def test_material_transforms(ads):
+    vp, vs, rho = np.array([3000.0]), np.array([1700.0]), np.array([2200.0])
+    lam, mu, r = ads.compute_properties(vp, vs, rho)
+    assert mu[0] == 2200.0 * 1700.0 * 1700.0
+    assert lam[0] == 2200.0 * 3000.0 * 3000.0 - 2 * mu[0]
+    lam2, mu2, _ = ads.compute_lame_parameters(vp, vs, rho)
+    assert np.allclose(lam2, lam) and np.allclose(mu2, mu)
+
+
+def test_param_defaults_follow_reference(ads):
+    a = ads.AcousticPropagatorParams()
+    assert (a.NX, a.NY, a.NSTEP, a.NPOINTS_PML, a.vp_ref, a.Rcoef) == (101, 641, 4000, 12, 1000.0, 0.001)
+    e = ads.ElasticPropagatorParams(f0=5.0)
+    assert e.ALPHA_MAX_PML == 2 * math.pi * 2.5 and e.vp_ref == 2000.0 and e.K_MAX_PML == 1.0
+    assert a.use_pml == 15
+
+
+def test_models_are_seeded(ads):
+    a = ads.folded_layer_model(100, 50, seed=3)
+    b = ads.folded_layer_model(100, 50, seed=3)
+    assert np.array_equal(a, b) and a.min() >= 1500 and a.max() <= 4500
+    v = ads.layered_gaussian_model(60, 60, seed=1)
+    assert v.shape == (60, 60) and 1700 < v.min() < v.max() < 4000
