@@ -96,7 +96,7 @@ _SIGS = {
     "ads_acoustic_plan_trace_count": [P],
     "ads_acoustic_plan_device_bytes": [P],
     "ads_acoustic_plan_launches": [P, I32],
-    "ads_acoustic_plan_loop_timing": [P, P],
+    "ads_acoustic_plan_profile": [P, P, P, P, P],
     "ads_acoustic_plan_forward": [P, P, P, P],
     "ads_acoustic_plan_gradient": [P, P, P, P, P, P, P],
     "ads_acoustic_forward": [P, P, P, P, P],

@@ -209,11 +209,15 @@ class AcousticPlan:
         except Exception:
             pass
 
-    def loop_timing(self):
-        """Device-timed loops of the last forward + gradient calls:
+    def profile(self, vp, observed):
+        """One gradient with direct launches and device-timed ranges:
         {'forward'|'recompute'|'adjoint': (ms, launches, interior cell-steps)}."""
+        _require_cuda(vp, observed)
+        vp = vp.contiguous().to(torch.float64)
+        obs = observed.contiguous().to(self.dtype)
         out = np.zeros(9)
-        call("ads_acoustic_plan_loop_timing", self._h, out.ctypes.data_as(C.c_void_p))
+        call("ads_acoustic_plan_profile", self._h, _ptr(vp), _ptr(obs),
+             out.ctypes.data_as(C.c_void_p), _stream())
         return {k: tuple(out[3 * i:3 * i + 3])
                 for i, k in enumerate(("forward", "recompute", "adjoint"))}
 

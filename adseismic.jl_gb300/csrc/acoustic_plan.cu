@@ -58,6 +58,7 @@ struct AcShot {
   T *lu, *lp, *lq;    // adjoint rings (2 fields each)
   T *c, *sx, *ty;     // c = vp^2 (pitched), PML profiles along i and j
   double* gc;         // FP64 gradient accumulator (pitched)
+  float* gc32;        // FP32 per-segment partial of grad_c (FP32 plans)
   const T* srcv;      // (nstep, nsrc), already multiplied by dt^2
   T *traces, *resid;  // (nstep+1, nrcv) packed views
 };
@@ -69,9 +70,23 @@ struct AcConst {
 
 // ---------------------------------------------------------------- kernels
 
+// Columns of a warp whose tau profile is zero at j-1..j+1 (for every lane):
+// there phi and psi can only be non-zero in rows whose sigma is non-zero.
+// In cells with sigma = tau = 0 the forward phi/psi are identically zero
+// (phi' = (1 - 0) phi + 0) and their adjoints never reach lambdaU or grad_c
+// (they are multiplied by tau - sigma = 0), so those loads and stores are
+// skipped; the arithmetic is unchanged (the skipped values enter as exact 0).
+template <typename T>
+__device__ __forceinline__ bool warp_tau_free(const T* __restrict__ ty, int j, int ny) {
+  const bool z = j > ny + 1 ||
+                 (ty[j - 1] == T(0) && ty[j] == T(0) && (j + 1 > ny + 1 || ty[j + 1] == T(0)));
+  return __all_sync(FULL, z);
+}
+
 // One forward step (variant W: phi/psi from the old field).  SEG=false: rings
 // of two (u_t written over u_{t-2}), optional checkpoint write; SEG=true:
-// segment store addressed by slot t - base.
+// segment store addressed by slot t - base.  Each thread slides down its column
+// with the next row's loads issued one iteration ahead.
 template <typename T, bool SEG>
 __global__ void __launch_bounds__(TJ)
 k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
@@ -98,61 +113,104 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   T* pout = sh.p + (int64_t)(t & 1) * fs;
   const T* qin = sh.q + (int64_t)((t - 1) & 1) * fs;
   T* qout = sh.q + (int64_t)(t & 1) * fs;
+  const T* __restrict__ cc = sh.c;
+  const T* __restrict__ sx = sh.sx;
+  const T* __restrict__ srcv = sh.srcv;
   const bool jin = j <= ny;
   const bool jld = j <= ny + 1;
+  const bool jr = j + 1 <= ny + 1;  // lane 31's right neighbour exists
   const int64_t col = j + JOFF;
   const T tj = jld ? sh.ty[j] : T(0);
-  const int i_end = min(it.i0 + ri, nx + 1);
-  const T* __restrict__ cc_ = sh.c;
-  const T* __restrict__ srcv = sh.srcv;
-
-  T wm = jld ? w[(int64_t)(it.i0 - 1) * P + col] : T(0);
-  T w0 = jld ? w[(int64_t)it.i0 * P + col] : T(0);
-  T pm = jld ? pin[(int64_t)(it.i0 - 1) * P + col] : T(0);
-  T p0 = jld ? pin[(int64_t)it.i0 * P + col] : T(0);
-  for (int i = it.i0; i < i_end; i++) {
+  const bool tfree = warp_tau_free<T>(sh.ty, j, ny);
+  auto nz = [&](int r) { return !(tfree && sx[r] == T(0)); };  // phi/psi may be non-zero
+  auto LD = [&](const T* a, int r, bool on) -> T {
+    return (jld && on) ? a[(int64_t)r * P + col] : T(0);
+  };
+  const int i0 = it.i0, i_end = min(i0 + ri, nx + 1);
+  bool n0 = nz(i0);
+  T wm = LD(w, i0 - 1, true), w0 = LD(w, i0, true), wp = LD(w, i0 + 1, true);
+  T pm = LD(pin, i0 - 1, nz(i0 - 1)), p0 = LD(pin, i0, n0), pp = LD(pin, i0 + 1, nz(i0 + 1));
+  T q0 = LD(qin, i0, n0), wo0 = LD(wo, i0, true), c0 = LD(cc, i0, true);
+  T hw = 0, hq = 0;  // lane 0: (i, j-1); lane 31: (i, j+1)
+  {
+    const int64_t r = (int64_t)i0 * P + col;
+    if (lane == 0 && jld) {
+      hw = w[r - 1];
+      hq = n0 ? qin[r - 1] : T(0);
+    } else if (lane == 31 && jr) {
+      hw = w[r + 1];
+      hq = n0 ? qin[r + 1] : T(0);
+    }
+  }
+  for (int i = i0; i < i_end; i++) {
     const int64_t row = (int64_t)i * P + col;
-    const T wp = jld ? w[row + P] : T(0);
-    const T pp = jld ? pin[row + P] : T(0);
-    const T q0 = jld ? qin[row] : T(0);
+    // prefetch: row i+2 of w and phi, row i+1 of psi, w_old, c and the halos
+    const bool more = i + 1 < i_end;
+    const bool n1 = more && nz(i + 1);
+    T wn = 0, pn_ = 0, qn = 0, won = 0, cn = 0, hwn = 0, hqn = 0;
+    if (more) {
+      wn = LD(w, i + 2, true);
+      pn_ = LD(pin, i + 2, nz(i + 2));
+      qn = LD(qin, i + 1, n1);
+      won = LD(wo, i + 1, true);
+      cn = LD(cc, i + 1, true);
+      if (lane == 0 && jld) {
+        hwn = w[row + P - 1];
+        hqn = n1 ? qin[row + P - 1] : T(0);
+      } else if (lane == 31 && jr) {
+        hwn = w[row + P + 1];
+        hqn = n1 ? qin[row + P + 1] : T(0);
+      }
+    }
     T wS = __shfl_up_sync(FULL, w0, 1), wN = __shfl_down_sync(FULL, w0, 1);
     T qS = __shfl_up_sync(FULL, q0, 1), qN = __shfl_down_sync(FULL, q0, 1);
-    if (lane == 0 && jld) {
-      wS = w[row - 1];
-      qS = qin[row - 1];
-    }
-    if (lane == 31) {
-      const bool ok = j + 1 <= ny + 1;
-      wN = ok ? w[row + 1] : T(0);
-      qN = ok ? qin[row + 1] : T(0);
+    if (lane == 0) {
+      wS = hw;
+      qS = hq;
+    } else if (lane == 31) {
+      wN = hw;
+      qN = hq;
     }
     if (jin) {
-      const T c = cc_[row], sg = sh.sx[i], s = sg + tj;
+      const T c = c0, sg = sx[i], s = sg + tj;
       T v = (T(2) - sg * tj * K.dt2 - K.kxy * c) * w0 + c * K.cx * (wp + wm) +
             c * K.cy * (wN + wS) + K.fx * (pp - pm) + K.fy * (qN - qS) -
-            (T(1) - s * K.hdt) * wo[row];
+            (T(1) - s * K.hdt) * wo0;
       if (s != T(0)) v = v / (T(1) + s * K.hdt);
       for (int e = it.src_b; e < it.src_e; e++) {
         const CellRef r = srcs[e];
         if (r.cell == row) v += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
       }
-      const T pn = (T(1) - K.dt * sg) * p0 + K.ex * c * (tj - sg) * (wp - wm);
-      const T qn = (T(1) - K.dt * tj) * q0 + K.ey * c * (sg - tj) * (wN - wS);
       out[row] = v;
-      pout[row] = pn;
-      qout[row] = qn;
+      T pnew = T(0), qnew = T(0);
+      if (n0) {
+        pnew = (T(1) - K.dt * sg) * p0 + K.ex * c * (tj - sg) * (wp - wm);
+        qnew = (T(1) - K.dt * tj) * q0 + K.ey * c * (sg - tj) * (wN - wS);
+        pout[row] = pnew;
+        qout[row] = qnew;
+      }
       if (!SEG && ckpt_slot > 0 && ckpt_slot < sh.nseg) {
         T* ck = sh.ckpt + (int64_t)ckpt_slot * 4 * fs;
         ck[row] = v;
         ck[fs + row] = w0;
-        ck[2 * fs + row] = pn;
-        ck[3 * fs + row] = qn;
+        if (n0) {
+          ck[2 * fs + row] = pnew;
+          ck[3 * fs + row] = qnew;
+        }
       }
     }
     wm = w0;
     w0 = wp;
+    wp = wn;
     pm = p0;
     p0 = pp;
+    pp = pn_;
+    q0 = qn;
+    wo0 = won;
+    c0 = cn;
+    hw = hwn;
+    hq = hqn;
+    n0 = n1;
   }
   if (!SEG && it.rcv_e > it.rcv_b) {
     __syncthreads();  // the tile's u_t is in global memory and visible block-wide
@@ -224,8 +282,10 @@ __device__ __forceinline__ void col_terms(T gui, T gq, T c, T sg, T tj, const Ac
 
 // One adjoint step k (gather form of the transpose of step k):
 //   lambdaU_{k-1} = D lambdaU_{k+1} + sum of what u_k, phi_k, psi_k send to w,
-//   lambdaPhi_{k-1}, lambdaPsi_{k-1} likewise, gc += d(step k)/dc . lambda_k,
-// then lambdaU_{k-1} += residual_{k-1} at the receivers.
+//   lambdaPhi_{k-1}, lambdaPsi_{k-1} likewise, grad_c += d(step k)/dc . lambda_k,
+// then lambdaU_{k-1} += residual_{k-1} at the receivers.  FP32 plans add the
+// grad_c contribution to a per-segment FP32 partial (flushed into the FP64
+// accumulator at the end of each segment); FP64 plans accumulate in FP64.
 template <typename T>
 __global__ void __launch_bounds__(TJ)
 k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
@@ -243,27 +303,64 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   T* lpo = sh.lp + (int64_t)((k - 1) & 1) * fs;
   const T* lqc = sh.lq + (int64_t)(k & 1) * fs;
   T* lqo = sh.lq + (int64_t)((k - 1) & 1) * fs;
-  const T* __restrict__ cc_ = sh.c;
+  const T* __restrict__ cc = sh.c;
   const T* __restrict__ sx = sh.sx;
+  const T* __restrict__ ty = sh.ty;
   const bool jin = j <= ny;
   const bool jld = j <= ny + 1;
+  const bool jr = j + 1 <= ny + 1;
   const int64_t col = j + JOFF;
-  const T tj = jld ? sh.ty[j] : T(0);
-  const int i_end = min(it.i0 + ri, nx + 1);
-  auto ld = [&](const T* a, int64_t off) -> T { return jld ? a[off] : T(0); };
+  const T tj = jld ? ty[j] : T(0);
+  const bool tfree = warp_tau_free<T>(ty, j, ny);
+  auto nz = [&](int r) { return !(tfree && sx[r] == T(0)); };
+  auto LD = [&](const T* a, int r, bool on) -> T {
+    return (jld && on) ? a[(int64_t)r * P + col] : T(0);
+  };
+  // halo cell (i, j -+ 1) terms for lanes 0 / 31
+  const T th = lane == 0 ? ty[j - 1] : (jr ? ty[j + 1] : T(0));
+  const int64_t hoff = lane == 0 ? -1 : 1;
+  const bool hon = (lane == 0 && jld) || (lane == 31 && jr);
 
-  // window rows i-1 (m), i (0), i+1 (p)
-  int64_t r0 = (int64_t)it.i0 * P + col;
-  RowTerms<T> Rm = row_terms<T>(ld(luc, r0 - P), ld(lpc, r0 - P), ld(cc_, r0 - P),
-                                sx[it.i0 - 1], tj, K);
-  RowTerms<T> R0 = row_terms<T>(ld(luc, r0), ld(lpc, r0), ld(cc_, r0), sx[it.i0], tj, K);
-  T wm = ld(w, r0 - P), w0 = ld(w, r0);
-  for (int i = it.i0; i < i_end; i++) {
+  const int i0 = it.i0, i_end = min(i0 + ri, nx + 1);
+  RowTerms<T> Rm = row_terms<T>(LD(luc, i0 - 1, true), LD(lpc, i0 - 1, nz(i0 - 1)),
+                                LD(cc, i0 - 1, true), sx[i0 - 1], tj, K);
+  RowTerms<T> R0 = row_terms<T>(LD(luc, i0, true), LD(lpc, i0, nz(i0)), LD(cc, i0, true),
+                                sx[i0], tj, K);
+  T gu1 = LD(luc, i0 + 1, true), gp1 = LD(lpc, i0 + 1, nz(i0 + 1)), c1 = LD(cc, i0 + 1, true);
+  T wm = LD(w, i0 - 1, true), w0 = LD(w, i0, true), wp = LD(w, i0 + 1, true);
+  bool n0 = nz(i0);
+  T gq = LD(lqc, i0, n0), lu_next = LD(lun, i0, true);
+  T hgu = 0, hgq = 0, hc = 0, hw = 0;
+  if (hon) {
+    const int64_t r = (int64_t)i0 * P + col + hoff;
+    hgu = luc[r];
+    hgq = n0 ? lqc[r] : T(0);
+    hc = cc[r];
+    hw = w[r];
+  }
+  for (int i = i0; i < i_end; i++) {
     const int64_t row = (int64_t)i * P + col;
-    const RowTerms<T> Rp =
-        row_terms<T>(ld(luc, row + P), ld(lpc, row + P), ld(cc_, row + P), sx[i + 1], tj, K);
-    const T wp = ld(w, row + P);
-    const T gq = ld(lqc, row);
+    const RowTerms<T> Rp = row_terms<T>(gu1, gp1, c1, sx[i + 1], tj, K);
+    // prefetch: row i+2 (lambdaU_k, lambdaPhi_k, c, u_{k-1}), row i+1 (lambdaPsi_k,
+    // lambdaU_{k+1}) and the halo cells of row i+1
+    const bool more = i + 1 < i_end;
+    const bool n1 = more && nz(i + 1);
+    T gu2 = 0, gp2 = 0, c2 = 0, w2 = 0, gqn = 0, lun1 = 0, hgun = 0, hgqn = 0, hcn = 0, hwn = 0;
+    if (more) {
+      gu2 = LD(luc, i + 2, true);
+      gp2 = LD(lpc, i + 2, nz(i + 2));
+      c2 = LD(cc, i + 2, true);
+      w2 = LD(w, i + 2, true);
+      gqn = LD(lqc, i + 1, n1);
+      lun1 = LD(lun, i + 1, true);
+      if (hon) {
+        const int64_t r = row + P + hoff;
+        hgun = luc[r];
+        hgqn = n1 ? lqc[r] : T(0);
+        hcn = cc[r];
+        hwn = w[r];
+      }
+    }
     const T sg = sx[i];
     const T gui = R0.gu * R0.inv;
     T YP, YM, YR;
@@ -271,48 +368,52 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     T YPl = __shfl_up_sync(FULL, YP, 1), YRl = __shfl_up_sync(FULL, YR, 1);
     T YMr = __shfl_down_sync(FULL, YM, 1), YRr = __shfl_down_sync(FULL, YR, 1);
     T wS = __shfl_up_sync(FULL, w0, 1), wN = __shfl_down_sync(FULL, w0, 1);
-    if (lane == 0 && jld) {  // cell (i, j-1): j-1 >= 0 always holds
-      const T c1 = cc_[row - 1], t1 = sh.ty[j - 1];
-      const T s1 = sg + t1;
+    if (lane == 0 || lane == 31) {
+      const T s1 = sg + th;
       const T inv1 = s1 != T(0) ? T(1) / (T(1) + s1 * K.hdt) : T(1);
-      T a, b;
-      col_terms<T>(luc[row - 1] * inv1, lqc[row - 1], c1, sg, t1, K, YPl, a, b);
-      YRl = b;
-      wS = w[row - 1];
-    }
-    if (lane == 31) {
-      if (j + 1 <= ny + 1) {
-        const T c1 = cc_[row + 1], t1 = sh.ty[j + 1];
-        const T s1 = sg + t1;
-        const T inv1 = s1 != T(0) ? T(1) / (T(1) + s1 * K.hdt) : T(1);
-        T a, b;
-        col_terms<T>(luc[row + 1] * inv1, lqc[row + 1], c1, sg, t1, K, a, YMr, b);
-        YRr = b;
-        wN = w[row + 1];
+      T a, b, r;
+      col_terms<T>(hgu * inv1, hgq, hc, sg, th, K, a, b, r);
+      if (lane == 0) {
+        YPl = a;
+        YRl = r;
+        wS = hw;
       } else {
-        YMr = T(0);
-        YRr = T(0);
-        wN = T(0);
+        YMr = b;
+        YRr = r;
+        wN = hw;
       }
     }
     if (jin) {
       const T c = R0.c, gp = R0.gp, s = sg + tj;
-      const T lu_next = lun[row];
       const T nu = -(T(1) - s * K.hdt) * R0.inv * lu_next +
                    (T(2) - sg * tj * K.dt2 - K.kxy * c) * gui + Rm.XP + Rp.XM + YPl + YMr;
-      const T np = (T(1) - K.dt * sg) * gp + Rm.XR - Rp.XR;
-      const T nq = (T(1) - K.dt * tj) * gq + YRl - YRr;
       const T g = (-K.kxy * w0 + K.cx * (wp + wm) + K.cy * (wN + wS)) * gui +
                   K.ex * (tj - sg) * (wp - wm) * gp + K.ey * (sg - tj) * (wN - wS) * gq;
       lun[row] = nu;
-      lpo[row] = np;
-      lqo[row] = nq;
-      sh.gc[row] += (double)g;
+      if (n0) {
+        lpo[row] = (T(1) - K.dt * sg) * gp + Rm.XR - Rp.XR;
+        lqo[row] = (T(1) - K.dt * tj) * gq + YRl - YRr;
+      }
+      if (sizeof(T) == 4)
+        sh.gc32[row] += (float)g;
+      else
+        sh.gc[row] += (double)g;
     }
     Rm = R0;
     R0 = Rp;
+    gu1 = gu2;
+    gp1 = gp2;
+    c1 = c2;
     wm = w0;
     w0 = wp;
+    wp = w2;
+    gq = gqn;
+    lu_next = lun1;
+    hgu = hgun;
+    hgq = hgqn;
+    hc = hcn;
+    hw = hwn;
+    n0 = n1;
   }
   if (k - 1 >= 2 && it.rcv_e > it.rcv_b) {
     __syncthreads();
@@ -320,6 +421,23 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       const CellRef r = rcvs[e];
       atomicAdd(lun + r.cell, sh.resid[(int64_t)(k - 1) * sh.nrcv + r.idx]);
     }
+  }
+}
+
+// End of a segment (FP32 plans): grad_c (FP64) += the segment's FP32 partial,
+// which is reset to zero.
+template <typename T>
+__global__ void __launch_bounds__(TJ)
+k_ac_flush_gc(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots, int ri) {
+  const AcItem it = items[blockIdx.x];
+  const AcShot<T>& sh = shots[it.shot];
+  const int j = it.j0 + threadIdx.x;
+  if (j > sh.ny) return;
+  const int i_end = min(it.i0 + ri, sh.nx + 1);
+  for (int i = it.i0; i < i_end; i++) {
+    const int64_t row = (int64_t)i * sh.pitch + j + JOFF;
+    sh.gc[row] += (double)sh.gc32[row];
+    sh.gc32[row] = 0.f;
   }
 }
 
@@ -428,7 +546,7 @@ struct AcPlanBase {
   virtual int forward(const double* vp, void* traces, cudaStream_t st) = 0;
   virtual int gradient(const double* vp, const void* obs, double* loss, double* grad,
                        void* traces_out, cudaStream_t st) = 0;
-  virtual int loop_timing(double* out) const = 0;
+  virtual int profile(const double* vp, const void* obs, double* out, cudaStream_t st) = 0;
   std::vector<int64_t> trace_off;
   int64_t trace_total = 0;
   int64_t bytes = 0;
@@ -471,6 +589,7 @@ struct AcPlan final : AcPlanBase {
   // launches; with the launch and interior cell-step counts of each range.
   cudaEvent_t ev[6] = {};
   int seg_timed = -1;
+  bool timing_run = false;  // set only for profile(): direct launches, events recorded
   double tcount[6] = {};  // launches, cell-steps for fwd / recompute / adjoint
 
   ~AcPlan() override {
@@ -489,7 +608,7 @@ struct AcPlan final : AcPlanBase {
   }
   std::vector<int64_t> cells_prefix;  // interior cells of the first n sorted shots
   int64_t cells_upto(int n) const { return n <= 0 ? 0 : cells_prefix[n - 1]; }
-  int loop_timing(double* out) const override;
+  int profile(const double* vp, const void* obs, double* out, cudaStream_t st) override;
   // number of sorted shots with nstep >= t
   int shots_with_nstep_ge(int t) const {
     int n = 0;
@@ -600,7 +719,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   size_t off_fwd_begin, off_fwd_end, off_adj_begin, off_adj_end;
   DevPool L;
   struct Offs {
-    size_t u, p, q, seg, ckpt, lu, lp, lq, c, sx, ty, gc, srcv;
+    size_t u, p, q, seg, ckpt, lu, lp, lq, c, sx, ty, gc, gc32, srcv;
   };
   std::vector<Offs> offs(ns);
   std::vector<int> nseg(ns);
@@ -625,6 +744,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     offs[s].lp = L.take(2 * fs);
     offs[s].lq = L.take(2 * fs);
     offs[s].gc = L.take((shots[order[s]].nx + 2) * pitch * sizeof(double));
+    offs[s].gc32 = L.take(sizeof(T) == 4 ? (shots[order[s]].nx + 2) * pitch * sizeof(float) : 0);
   }
   off_adj_end = L.used;
   for (int s = 0; s < ns; s++) {
@@ -743,6 +863,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     d.sx = (T*)(pool + offs[s].sx);
     d.ty = (T*)(pool + offs[s].ty);
     d.gc = (double*)(pool + offs[s].gc);
+    d.gc32 = sizeof(T) == 4 ? (float*)(pool + offs[s].gc32) : nullptr;
     d.srcv = (const T*)(pool + offs[s].srcv);
     d.traces = d_traces + trace_off[order[s]];
     d.resid = d_resid + trace_off[order[s]];
@@ -847,7 +968,7 @@ int AcPlan<T>::issue_forward(cudaStream_t st, int64_t* count) {
     return ADS_OK;
   }
   ADS_CUDA(cudaMemsetAsync(pool + zero_fwd_off, 0, zero_fwd_len, st));
-  ADS_CUDA(cudaEventRecord(ev[0], st));
+  if (timing_run) ADS_CUDA(cudaEventRecord(ev[0], st));
   for (int t = 2; t <= nstep[0]; t++) {
     const int na = shots_with_nstep_ge(t);
     const int nit = items_upto(na);
@@ -856,7 +977,7 @@ int AcPlan<T>::issue_forward(cudaStream_t st, int64_t* count) {
     k_ac_fwd<T, false><<<nit, TJ, 0, st>>>(d_items, d_shots, d_srcs, d_rcvs, kc, t, 0, ck, ri);
     ADS_LAUNCHED(1);
   }
-  ADS_CUDA(cudaEventRecord(ev[1], st));
+  if (timing_run) ADS_CUDA(cudaEventRecord(ev[1], st));
   return ADS_OK;
 }
 
@@ -883,7 +1004,7 @@ int AcPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     }
     n++;
     const bool timed = s == seg_timed;
-    if (timed && !count) ADS_CUDA(cudaEventRecord(ev[2], st));
+    if (timed && timing_run) ADS_CUDA(cudaEventRecord(ev[2], st));
     if (timed && count) tcount[2] = tcount[3] = tcount[4] = tcount[5] = 0;
     for (int t = a; t <= b_max - 1; t++) {
       // active while t < b_shot = min(a+K-1, nstep), i.e. nstep >= t+1
@@ -899,7 +1020,7 @@ int AcPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
       }
       n++;
     }
-    if (timed && !count) {
+    if (timed && timing_run) {
       ADS_CUDA(cudaEventRecord(ev[3], st));
       ADS_CUDA(cudaEventRecord(ev[4], st));
     }
@@ -915,7 +1036,14 @@ int AcPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
       }
       n++;
     }
-    if (timed && !count) ADS_CUDA(cudaEventRecord(ev[5], st));
+    if (timed && timing_run) ADS_CUDA(cudaEventRecord(ev[5], st));
+    if (sizeof(T) == 4) {  // fold the segment's FP32 grad_c partial into FP64
+      if (!count) {
+        k_ac_flush_gc<T><<<items_upto(na), TJ, 0, st>>>(d_items, d_shots, ri);
+        ADS_LAUNCHED(1);
+      }
+      n++;
+    }
   }
   if (count) *count = n;
   return ADS_OK;
@@ -966,19 +1094,27 @@ int AcPlan<T>::gradient(const double* vp, const void* obs, double* loss, double*
   return ADS_OK;
 }
 
+// One gradient with direct launches (no graphs) and CUDA events around the
+// forward loop and around one full segment's recompute and adjoint launches.
 template <typename T>
-int AcPlan<T>::loop_timing(double* out) const {
-  float ms[3] = {0, 0, 0};
-  for (int r = 0; r < 3; r++) {
-    cudaError_t e = cudaEventElapsedTime(&ms[r], ev[2 * r], ev[2 * r + 1]);
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      return fail(ADS_ERR_CUDA, "loop timing unavailable (run forward and gradient first): %s",
-                  cudaGetErrorString(e));
-    }
+int AcPlan<T>::profile(const double* vp, const void* obs, double* out, cudaStream_t st) {
+  ADS_REQUIRE(vp && obs && out, "null argument");
+  k_ac_prep<T><<<dim3(256, nshots), 256, 0, st>>>(d_shots, vp, cfg.MY + 2);
+  ADS_LAUNCHED(1);
+  timing_run = true;
+  int rc = issue_forward(st, nullptr);
+  if (rc == ADS_OK) {
+    k_misfit<T><<<kMisfitBlocks, 256, 0, st>>>(d_traces, (const T*)obs, d_resid, trace_total,
+                                               d_partial);
+    rc = issue_reverse(st, nullptr);
   }
+  timing_run = false;
+  if (rc != ADS_OK) return rc;
+  ADS_CUDA(cudaStreamSynchronize(st));
   for (int r = 0; r < 3; r++) {
-    out[3 * r] = ms[r];
+    float ms = 0.f;
+    ADS_CUDA(cudaEventElapsedTime(&ms, ev[2 * r], ev[2 * r + 1]));
+    out[3 * r] = ms;
     out[3 * r + 1] = tcount[2 * r];
     out[3 * r + 2] = tcount[2 * r + 1];
   }
@@ -1047,9 +1183,10 @@ int64_t ads_acoustic_plan_launches(const ads_acoustic_plan* plan, int gradient) 
   return gradient ? plan->impl->launches_grad : plan->impl->launches_fwd;
 }
 
-int ads_acoustic_plan_loop_timing(const ads_acoustic_plan* plan, double* out9) {
-  ADS_REQUIRE(plan && out9, "null argument");
-  return plan->impl->loop_timing(out9);
+int ads_acoustic_plan_profile(ads_acoustic_plan* plan, const double* vp, const void* observed,
+                              double* out9, ads_stream_t stream) {
+  ADS_REQUIRE(plan, "null plan");
+  return plan->impl->profile(vp, observed, out9, (cudaStream_t)stream);
 }
 
 int ads_acoustic_plan_forward(ads_acoustic_plan* plan, const double* vp, void* traces,

@@ -1,0 +1,399 @@
+#!/usr/bin/env python
+"""Benchmark: FWI shot-gradients/s and Gcell-updates/s on one GB300.
+
+Default workload: batched acoustic FWI gradient with FP32 stencils and FP64
+misfit/gradient accumulation, 1000 x 500 cells (PML 40 inside), h = 10 m,
+dt = 0.8 ms, 3000 steps, 64 shots with 15 Hz Ricker sources and 500 receivers
+each, forward checkpoints every 100 steps, seeded folded-layer model (synthetic
+data: observed traces are simulated on the true model, the gradient is taken at
+a smoothed start model).  One step = one full gradient of all shots (forward,
+misfit, checkpointed adjoint, gradient assembly) with everything resident in HBM.
+
+Also reported: the plain FP64 path on the same per-shot geometry (one shot per
+call, no batching), the end-to-end rate through the C ABI with host buffers,
+the roofline of the dominant kernel from CUDA events recorded inside the time
+loops, SM clocks sampled during the timed region, and the CPU baseline.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FWI shot-gradients/s & Gcell-updates/s, FP32-batched vs FP64-plain, 1 GB300"
+UNIT = "shot-gradients/s"
+
+# algorithmic bytes per interior cell-step (each array counted once per step)
+BYTES = {
+    ("fwd", "f32"): 32,   # read w, w_old, phi, psi, c; write u, phi', psi'
+    ("fwd", "f64"): 64,
+    ("adj", "f32"): 52,   # adjoint state 32 + forward w 4 + FP64 grad_c RMW 16
+    ("adj", "f64"): 88,   # 64 + 8 + 16
+}
+
+
+def workload(MX=1000, MY=500, npml=40, nstep=3000, nshots=64, nrcv=500, fpeak=15.0,
+             dt=0.8e-3, h=10.0, seed=1234):
+    import __graft_entry__ as g
+
+    ads = g.load_package()
+    rng = np.random.default_rng(seed)
+    vp_true = ads.folded_layer_model(MX + 2, MY + 2, 1500.0, 4500.0, seed=seed)
+    vp0 = ads.gaussian_smooth(vp_true, sigma=0.05 * MX)
+    a = ads.ricker_width_samples(fpeak, dt)
+    shift = 1.5 / fpeak / dt
+    p = ads.AcousticPropagatorParams(NX=MX, NY=MY, NSTEP=nstep, DELTAT=dt)
+    wav = ads.Ricker(p, a, shift, 1e6)
+    lo, hi = npml + 2, MX - npml
+    shots = []
+    for s in range(nshots):
+        si = int(round(lo + (s + 0.5) * (hi - lo) / nshots))
+        rcvi = np.round(np.linspace(npml + 2, MX - npml, nrcv)).astype(np.int64)
+        shots.append(dict(x0=0, nx=MX, nstep=nstep, srci=[si], srcj=[npml + 11],
+                          srcv=wav[:, None], rcvi=rcvi, rcvj=np.full(nrcv, npml + 6)))
+    cfg = dict(MX=MX, MY=MY, h=h, dt=dt, npml=npml, vp_ref=float(vp_true.mean()))
+    return ads, cfg, shots, vp_true, vp0, rng
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (read-only queries)."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, n in enumerate(names):
+                if len(r) > 4 + k and r[4 + k].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.rows)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_sample(cfg, shot, vp, steps, reps=1, use_ref=False):
+    """Acoustic gradient of one shot over a bounded number of steps on one core:
+    the oracle port, or (use_ref) the reference's own compiled CPU operators
+    driven by the restated loop.  Returns seconds per run."""
+    import oracle
+
+    oracle.build(ref=False)
+    MX, MY, h, dt = cfg["MX"], cfg["MY"], cfg["h"], cfg["dt"]
+    sx, ty = oracle.acoustic_pml(MX, MY, h, h, cfg["npml"], cfg["vp_ref"])
+    srcv = np.asarray(shot["srcv"])[:steps]
+    obs = np.zeros((steps + 1, len(shot["rcvi"])))
+    best = math.inf
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        oracle.acoustic_gradient(MX, MY, steps, dt, h, h, sx, ty, vp.reshape(-1), shot["srci"],
+                                 shot["srcj"], srcv, shot["rcvi"], shot["rcvj"], obs,
+                                 use_ref=use_ref)
+        best = min(best, time.perf_counter() - t0)
+    return best
+
+
+def _cpu_worker(args):
+    cfg, shot, vp, steps, use_ref = args
+    return cpu_sample(cfg, shot, vp, steps, use_ref=use_ref)
+
+
+def cpu_baseline(cfg, shots, vp, nstep, cores=1, steps=40, use_ref=False):
+    """Shot-gradients/s on `cores` processes (one shot each), from a bounded
+    sample of `steps` time steps scaled linearly to nstep."""
+    if cores == 1:
+        t = cpu_sample(cfg, shots[0], vp, steps, use_ref=use_ref)
+    else:
+        import multiprocessing as mp
+
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(cores) as pool:
+            ts = pool.map(_cpu_worker, [(cfg, shots[k % len(shots)], vp, steps, use_ref)
+                                        for k in range(cores)])
+        t = max(ts)
+    per_shot = t * (nstep - 1) / (steps - 1)
+    return cores / per_shot, t
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU operators (compiled from the
+    reference checkout when present, else the oracle's bit-identical port) timed
+    on all host cores over bounded samples of the same workload."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import oracle
+
+    ads, cfg, shots, vp_true, vp0, _ = workload()
+    cores = os.cpu_count() or 1
+    use_ref = oracle.ref_available()
+    kind = "reference" if use_ref else "port"
+    steps = 40
+    vals = []
+    for k in range(args.warmup + args.steps):
+        v, t = cpu_baseline(cfg, shots, vp0, 3000, cores=cores, steps=steps, use_ref=use_ref)
+        if k >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "acoustic FWI gradient 1000x500 (PML 40), 3000 steps, "
+                               "64 shots x 500 receivers"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": f"{cores} shots in parallel, {steps} of 3000 steps each "
+                                   "(forward + full-history adjoint), scaled linearly"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--shots", type=int, default=64)
+    ap.add_argument("--nstep", type=int, default=3000)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+
+    ads, cfg, shots, vp_true, vp0, rng = workload(nstep=args.nstep, nshots=args.shots,
+                                                  seed=1234 + rank)
+    nstep, MX, MY = args.nstep, cfg["MX"], cfg["MY"]
+    mk = lambda prec, sh, **kw: ads.AcousticPlan(MX, MY, cfg["h"], cfg["h"], cfg["dt"], sh,
+                                                 npml=cfg["npml"], vp_ref=cfg["vp_ref"],
+                                                 precision=prec, ckpt_every=100, **kw)
+    t_setup = time.perf_counter()
+    plan = mk("f32", shots)
+    vt = torch.tensor(vp_true, device=dev)
+    v0 = torch.tensor(vp0, device=dev)
+    obs = plan.forward(vt).clone()
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t_setup
+
+    from adseismic_gb300.distributed import allreduce_loss_grad
+
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        loss, grad = plan.gradient(v0, obs)
+        if dist:
+            allreduce_loss_grad(loss, grad)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    n0 = ads.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            loss, grad = plan.gradient(v0, obs)
+            if dist:
+                allreduce_loss_grad(loss, grad)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = ads.launch_count() - n0
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t)
+    total_shots = args.shots * world
+    value = total_shots / (ms / 1e3)
+    cell_steps = sum(s["nx"] * MY * (s["nstep"] - 1) for s in shots) * world
+    gcell = 2 * cell_steps / (ms / 1e3) / 1e9  # forward + adjoint updates per second
+    timing = plan.profile(v0, obs)
+
+    # roofline: kernels timed by CUDA events recorded inside the time loops
+    peak, peak_kind = measured_peak()
+    fwd_ms, fwd_n, fwd_cells = timing["forward"]
+    rc_ms, rc_n, rc_cells = timing["recompute"]
+    adj_ms, adj_n, adj_cells = timing["adjoint"]
+    nseg = math.ceil((nstep - 1) / 100)
+    kern = {
+        "k_ac_fwd": dict(ms_per_launch=fwd_ms / fwd_n, bytes=BYTES[("fwd", "f32")] * fwd_cells / fwd_n,
+                         launches=fwd_n + rc_n * nseg),
+        "k_ac_adj": dict(ms_per_launch=adj_ms / adj_n, bytes=BYTES[("adj", "f32")] * adj_cells / adj_n,
+                         launches=adj_n * nseg),
+    }
+    for k, v in kern.items():
+        v["achieved_gbs"] = v["bytes"] / (v["ms_per_launch"] / 1e3) / 1e9
+        v["total_ms"] = v["ms_per_launch"] * v["launches"]
+    dom = max(kern, key=lambda k: kern[k]["total_ms"])
+    d = kern[dom]
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get(dom)
+        except ValueError:
+            traffic = None
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(d["achieved_gbs"], 1),
+                "peak": peak, "unit": "GB/s", "frac": round(d["achieved_gbs"] / peak, 4),
+                "peak_source": peak_kind, "traffic": traffic,
+                "bytes_per_launch": d["bytes"], "ms_per_launch": d["ms_per_launch"],
+                "kernels": {k: {"achieved_gbs": round(v["achieved_gbs"], 1),
+                                "ms_per_launch": round(v["ms_per_launch"], 4),
+                                "share_of_step": round(v["total_ms"] / ms, 3)}
+                            for k, v in kern.items()}}
+
+    # e2e through the C ABI with host buffers (pinned), copies inside the timed region
+    vp_host = torch.tensor(vp0).pin_memory()
+    obs_host = obs.cpu().pin_memory()
+    grad_host = torch.empty_like(vp_host).pin_memory()
+    loss_host = torch.empty(1, dtype=torch.float64).pin_memory()
+    vdev = torch.empty_like(v0)
+    odev = torch.empty_like(obs)
+    torch.cuda.synchronize()
+    e2e_steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        vdev.copy_(vp_host, non_blocking=True)
+        odev.copy_(obs_host, non_blocking=True)
+        l, g = plan.gradient(vdev, odev)
+        grad_host.copy_(g, non_blocking=True)
+        loss_host.copy_(l.reshape(1), non_blocking=True)
+        torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e = {"value": args.shots / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": vp_host.numel() * 8 + obs_host.numel() * 4,
+           "d2h_bytes_per_step": grad_host.numel() * 8 + 8}
+
+    # plain FP64 on the same per-shot geometry, one shot per call
+    fp64 = None
+    if not args.no_fp64:
+        p64 = mk("f64", shots[:1])
+        o64 = p64.forward(vt).clone()
+        p64.gradient(v0, o64)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        reps = 2
+        for _ in range(reps):
+            p64.gradient(v0, o64)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms64 = a.elapsed_time(b) / reps
+        t64 = p64.profile(v0, o64)
+        fwd64 = t64["forward"]
+        fp64 = {"value": 1e3 / ms64, "unit": UNIT, "ms_per_shot_gradient": ms64,
+                "gcell_updates_per_s": 2 * shots[0]["nx"] * MY * (nstep - 1) / (ms64 / 1e3) / 1e9,
+                "k_ac_fwd_f64_gbs": BYTES[("fwd", "f64")] * fwd64[2] / (fwd64[0] / 1e3) / 1e9,
+                "fp32_batched_over_fp64_plain": value / world / (1e3 / ms64)}
+        p64.close()
+
+    cpu = None
+    if not args.no_cpu and rank == 0:
+        v, t = cpu_baseline(cfg, shots, vp0, nstep, cores=1, steps=100)
+        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"one shot, 100 of {nstep} steps (forward + full-history adjoint, "
+                         f"{t:.1f} s), scaled linearly to {nstep} steps"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"acoustic FWI gradient {MX}x{MY} (PML {cfg['npml']}), "
+                                   f"{nstep} steps, {args.shots} shots x 500 receivers per GPU, "
+                                   "15 Hz Ricker, folded-layer model, checkpoints every 100",
+                       "precision": "FP32 stencils, FP64 misfit and gradient accumulation",
+                       "l2": f"working set {plan.device_bytes / 1e9:.1f} GB per GPU >> 126 MB L2",
+                       "parallelism": f"shots sharded over {world} GPU(s), gradient all-reduce"},
+            "gcell_updates_per_s": gcell,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "fp64_plain": fp64,
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+            "loss": float(loss),
+            "setup_s": t_setup,
+        }
+        print(json.dumps(line))
+    plan.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

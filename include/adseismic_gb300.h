@@ -255,13 +255,14 @@ int64_t ads_acoustic_plan_trace_count(const ads_acoustic_plan* plan);
 int64_t ads_acoustic_plan_device_bytes(const ads_acoustic_plan* plan);
 /* Kernel launches one forward / one gradient call issues. */
 int64_t ads_acoustic_plan_launches(const ads_acoustic_plan* plan, int gradient);
-/* Device-timed kernel durations of the last forward and gradient calls, from
- * CUDA events recorded inside the time loops (graph event nodes when graphs
- * are used): out9 = {ms, launches, interior cell-steps} for (0) the forward
- * loop (k_ac_fwd only), (1) one full checkpoint segment's recompute launches,
- * (2) the same segment's adjoint launches.  Call after synchronising.  No
- * reference counterpart (instrumentation for roofline reporting). */
-int ads_acoustic_plan_loop_timing(const ads_acoustic_plan* plan, double* out9);
+/* Kernel timing: runs one gradient with direct launches (no graphs) and CUDA
+ * events recorded around (0) the forward loop (k_ac_fwd launches only), (1)
+ * one full checkpoint segment's recompute launches and (2) the same segment's
+ * adjoint launches; out9 = {ms, launches, interior cell-steps} for each range.
+ * Synchronises `stream`.  Same arguments as ads_acoustic_plan_gradient minus
+ * the outputs.  No reference counterpart (instrumentation for the roofline). */
+int ads_acoustic_plan_profile(ads_acoustic_plan* plan, const double* vp,
+                              const void* observed, double* out9, ads_stream_t stream);
 /* Forward: traces (device, plan precision: double for ADS_F64, float for
  * ADS_F32) receive every shot's (nstep+1, nrcv) receiver record. */
 int ads_acoustic_plan_forward(ads_acoustic_plan* plan, const double* vp, void* traces,
