@@ -16,6 +16,7 @@
 #include <cmath>
 #include <memory>
 #include <numeric>
+#include <mutex>
 #include <vector>
 
 #include "ads_internal.h"
@@ -1085,6 +1086,120 @@ int ads_elastic_step_bwd_f64(const double* state_in, const double* grad_out, dou
   k_el_adj3<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one);
   ADS_LAUNCHED(1);
   ADS_CUDA(cudaFreeAsync(scratch, st));
+  return ADS_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the elastic step transpose.
+//
+// Some callers cannot allocate device memory at the time they run this step:
+// code executing inside another framework's stream capture or custom-call
+// hook, where cudaMalloc/cudaMallocAsync would break the capture or the
+// framework's memory accounting, and callers that must not touch the CUDA
+// allocator at all (pre-planned real-time loops).  For them the scratch this
+// step needs (forward output state, per-step strains, adjoint temporaries and
+// the packed CPML rows) lives in one fixed array in device global memory,
+// compiled into the library.  Every GPU that loads the library holds the array
+// (34 x 65536 doubles, about 17.8 MB) until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int64_t kNoAllocMaxCells = 65536;  // (NX+2)*(NY+2) limit
+constexpr size_t kNoAllocDoubles = (size_t)(NF + NSTORE + NTMP + 4) * kNoAllocMaxCells;
+static __device__ __align__(256) double g_el_bwd_scratch[kNoAllocDoubles];
+
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[128] = {};  // device address of g_el_bwd_scratch, per device
+
+// Device address of the scratch array for the current device, looked up once
+// per device (the host-side symbol is only a stand-in, never a device address).
+int noalloc_scratch(double** out) {
+  int dev = 0;
+  ADS_CUDA(cudaGetDevice(&dev));
+  ADS_REQUIRE(dev >= 0 && dev < 128, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_el_bwd_scratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      return fail(ADS_ERR_CUDA, "cudaGetSymbolAddress(scratch) failed on device %d: %s", dev,
+                  cudaGetErrorString(e));
+    }
+    g_noalloc_ptr[dev] = (double*)p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return ADS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ads_elastic_step_bwd_f64_noalloc(const double* state_in, const double* grad_out,
+                                     double* grad_in, double* grad_lambda, double* grad_mu,
+                                     double* grad_rho, const double* lambda, const double* mu,
+                                     const double* rho, const double* ax, const double* bx,
+                                     const double* ay, const double* by, double dt, double dx,
+                                     double dy, int64_t NX, int64_t NY, ads_stream_t stream) {
+  if (int e = require_device()) return e;
+  ADS_REQUIRE(NX >= 4 && NY >= 4 && NX < (1 << 24) && NY < (1 << 24), "NX, NY out of range");
+  const int64_t N = (NX + 2) * (NY + 2);
+  ADS_REQUIRE(N <= kNoAllocMaxCells,
+              "grid (NX+2)*(NY+2) = %lld exceeds the %lld cells the allocation-free "
+              "scratch holds; use ads_elastic_step_bwd_f64",
+              (long long)N, (long long)kNoAllocMaxCells);
+  ADS_REQUIRE(state_in && grad_out && grad_in && grad_lambda && grad_mu && grad_rho &&
+                  lambda && mu && rho && ax && bx && ay && by,
+              "null pointer argument");
+  ADS_REQUIRE(grad_in != grad_out, "grad_in must not alias grad_out");
+  double* scratch = nullptr;
+  if (int e = noalloc_scratch(&scratch)) return e;
+  cudaStream_t st = (cudaStream_t)stream;
+  const size_t prof_n = 4 * NX + 4 * NY;
+  const size_t n_scr = prof_n + (size_t)(NF + NSTORE + NTMP) * N;
+  // the array keeps the previous call's contents: clear the part used here
+  ADS_CUDA(cudaMemsetAsync(scratch, 0, sizeof(double) * n_scr, st));
+  double* prof = scratch;
+  ADS_CUDA(cudaMemcpyAsync(prof, ax, sizeof(double) * 2 * NX, cudaMemcpyDeviceToDevice, st));
+  ADS_CUDA(cudaMemcpyAsync(prof + 2 * NX, bx, sizeof(double) * 2 * NX, cudaMemcpyDeviceToDevice,
+                           st));
+  ADS_CUDA(cudaMemcpyAsync(prof + 4 * NX, ay, sizeof(double) * 2 * NY, cudaMemcpyDeviceToDevice,
+                           st));
+  ADS_CUDA(cudaMemcpyAsync(prof + 4 * NX + 2 * NY, by, sizeof(double) * 2 * NY,
+                           cudaMemcpyDeviceToDevice, st));
+  double* fout = scratch + prof_n;
+  double* store = fout + NF * N;
+  double* tmp = store + NSTORE * N;
+  ElModel<double> M =
+      make_model<double>((int)NX, (int)NY, NY + 2, 0, dt, dx, dy, lambda, mu, rho, prof);
+  ElShot<double> one{};
+  for (int f = 0; f < NF; f++) {
+    one.fin[f] = state_in + f * N;
+    one.f[f] = fout + f * N;
+    one.g[f] = grad_in + f * N;
+  }
+  for (int k = 0; k < NTMP; k++) one.tmp[k] = tmp + k * N;
+  one.store = store;
+  one.fs = N;
+  one.glam = grad_lambda;
+  one.gmu = grad_mu;
+  one.grho = grad_rho;
+  dim3 grd((unsigned)div_up(NY + 2, BX), (unsigned)div_up(NX + 2, BY), 1);
+  k_el_stress<double, true, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  ADS_LAUNCHED(1);
+  k_el_velocity<double, true, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  ADS_LAUNCHED(1);
+  ADS_CUDA(cudaMemcpyAsync(grad_in, grad_out, sizeof(double) * NF * N,
+                           cudaMemcpyDeviceToDevice, st));
+  k_el_adj1<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  ADS_LAUNCHED(1);
+  k_el_adj2<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  ADS_LAUNCHED(1);
+  k_el_adj3<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one);
+  ADS_LAUNCHED(1);
   return ADS_OK;
 }
 

@@ -172,6 +172,26 @@ int ads_elastic_step_bwd_f64(const double* state_in, const double* grad_out,
                              const double* ay, const double* by, double dt, double dx,
                              double dy, int64_t NX, int64_t NY, ads_stream_t stream);
 
+/* Allocation-free form of ads_elastic_step_bwd_f64 (same arguments, same
+ * results).  No counterpart in the reference: it exists for callers that cannot
+ * allocate device memory when they run the step, such as code inside another
+ * framework's stream capture or custom-call hook (where cudaMalloc or
+ * cudaMallocAsync would break the capture or bypass that framework's memory
+ * accounting) or loops that must never enter the CUDA allocator.  Its scratch is
+ * one fixed array of 34 x 65536 doubles (about 17.8 MB) compiled into the
+ * library and resident on every GPU that loads it until the process exits;
+ * grids with (NX+2)*(NY+2) > 65536 are rejected with ADS_ERR_INVALID.  The
+ * first call on each device looks up the array's device address (make that
+ * first call before any stream capture).  All calls share the one array: calls
+ * whose executions overlap on the GPU (different streams without ordering, or
+ * threads racing on one device) corrupt each other's scratch. */
+int ads_elastic_step_bwd_f64_noalloc(const double* state_in, const double* grad_out,
+                                     double* grad_in, double* grad_lambda, double* grad_mu,
+                                     double* grad_rho, const double* lambda, const double* mu,
+                                     const double* rho, const double* ax, const double* bx,
+                                     const double* ay, const double* by, double dt, double dx,
+                                     double dy, int64_t NX, int64_t NY, ads_stream_t stream);
+
 /* Out-of-range indices given to the index operators above are skipped on the
  * device (never dereferenced) and recorded: bit 0 scatter/gather, bit 1
  * AddSource, bit 2 GetReceive.  Reads the flags into *flags (clearing them when
