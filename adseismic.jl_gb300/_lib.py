@@ -39,7 +39,8 @@ class AcousticConfig(C.Structure):
         ("npml", C.c_int64), ("Rcoef", C.c_double), ("vp_ref", C.c_double),
         ("use_pml", C.c_int32), ("precision", C.c_int32), ("variant", C.c_int32),
         ("use_graph", C.c_int32), ("ckpt_every", C.c_int64),
-        ("rows_per_thread", C.c_int32), ("reserved", C.c_int32 * 7),
+        ("rows_per_thread", C.c_int32), ("steps_per_block", C.c_int32),
+        ("block_rows", C.c_int32), ("reserved", C.c_int32 * 5),
     ]
 
 

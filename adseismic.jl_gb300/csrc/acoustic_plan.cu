@@ -33,9 +33,25 @@
 namespace ads {
 namespace {
 
-constexpr int WARPS = 4;
-constexpr int TJ = 32 * WARPS;  // tile width along j (one warp per 32 columns)
 constexpr unsigned FULL = 0xffffffffu;
+
+// Tiles: a CTA owns `J` columns x rows_per_thread rows of one shot.  The
+// forward step gives each thread CF adjacent columns, the adjoint CA (fewer,
+// it carries more state per cell); rows are loaded as 16/8-byte vectors.
+template <typename T>
+struct Tile {
+  static constexpr int J = sizeof(T) == 4 ? 512 : 256;
+  static constexpr int CF = sizeof(T) == 4 ? 4 : 2;
+  static constexpr int CA = sizeof(T) == 4 ? 2 : 1;
+  static constexpr int NF = J / CF;  // forward threads per CTA (128)
+  static constexpr int NA = J / CA;  // adjoint threads per CTA (256)
+  static constexpr int NC = 128;     // threads of the column-loop helpers
+};
+
+template <typename T, int C>
+struct alignas(sizeof(T) * C) Vec {
+  T v[C];
+};
 
 struct CellRef {
   int64_t cell;  // element offset inside the shot's pitched field
@@ -54,6 +70,8 @@ struct AcShot {
   int64_t pitch, fs;  // row pitch and elements per field
   int nsrc, nrcv, nseg, pad_;
   T *u, *p, *q;       // forward rings (2 fields each)
+  T* u2;              // time-blocked forward: U_{t-1} of the two state sets
+  const int* rcv_next; // next receiver on the same cell, or -1 (time-blocked forward)
   T *seg, *ckpt;      // segment store (k+1 fields), checkpoints (nseg x 4 fields)
   T *lu, *lp, *lq;    // adjoint rings (2 fields each)
   T *c, *sx, *ty;     // c = vp^2 (pitched), PML profiles along i and j
@@ -83,19 +101,66 @@ __device__ __forceinline__ bool warp_tau_free(const T* __restrict__ ty, int j, i
   return __all_sync(FULL, z);
 }
 
+// C-wide loads and stores of a thread's columns.  Full-width stores only when
+// all C cells are interior; otherwise per cell (the frame must stay zero).
+template <typename T, int C>
+__device__ __forceinline__ Vec<T, C> ldv(const T* base, int64_t off, bool on) {
+  Vec<T, C> x;
+  if (on) {
+    x = *reinterpret_cast<const Vec<T, C>*>(base + off);
+  } else {
+#pragma unroll
+    for (int c = 0; c < C; c++) x.v[c] = T(0);
+  }
+  return x;
+}
+
+template <typename T, int C>
+__device__ __forceinline__ void stv(T* base, int64_t off, const Vec<T, C>& x, int j, int ny) {
+  if (j + C - 1 <= ny) {
+    *reinterpret_cast<Vec<T, C>*>(base + off) = x;
+  } else {
+#pragma unroll
+    for (int c = 0; c < C; c++)
+      if (j + c <= ny) base[off + c] = x.v[c];
+  }
+}
+
+// True when tau is zero at every column the warp reads (j-1 .. j+C): there
+// phi and psi can only be non-zero in rows whose sigma is non-zero.  In cells
+// with sigma = tau = 0 the forward phi/psi are identically zero
+// (phi' = (1 - 0) phi + 0) and their adjoints never reach lambdaU or grad_c
+// (they are multiplied by tau - sigma = 0), so those loads and stores are
+// skipped; the arithmetic is unchanged (the skipped values enter as exact 0).
+template <typename T, int C>
+__device__ __forceinline__ bool warp_tau_free(const T* __restrict__ ty, int j, int ny) {
+  bool z = true;
+  if (j <= ny + 1) {
+    z = ty[j - 1] == T(0);
+#pragma unroll
+    for (int c = 0; c <= C; c++)
+      if (j + c <= ny + 1) z = z && ty[j + c] == T(0);
+  }
+  return __all_sync(FULL, z);
+}
+
 // One forward step (variant W: phi/psi from the old field).  SEG=false: rings
 // of two (u_t written over u_{t-2}), optional checkpoint write; SEG=true:
-// segment store addressed by slot t - base.  Each thread slides down its column
-// with the next row's loads issued one iteration ahead.
+// segment store addressed by slot t - base.  Each thread owns CF adjacent
+// columns of the tile, walks down its rows with the next row's loads issued
+// one iteration ahead, and takes the j-neighbours of its edge cells from the
+// neighbouring lanes (warp-edge lanes load them).
 template <typename T, bool SEG>
-__global__ void __launch_bounds__(TJ)
+__global__ void __launch_bounds__(Tile<T>::NF)
 k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
          const CellRef* __restrict__ srcs, const CellRef* __restrict__ rcvs, AcConst<T> K,
          int t, int base, int ckpt_slot, int ri) {
+  constexpr int C = Tile<T>::CF;
+  using V = Vec<T, C>;
   const AcItem it = items[blockIdx.x];
   const AcShot<T>& sh = shots[it.shot];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int j = it.j0 + warp * 32 + lane;
+  const int lane = threadIdx.x & 31;
+  const int j = it.j0 + threadIdx.x * C;
   const int nx = sh.nx, ny = sh.ny;
   const int64_t P = sh.pitch, fs = sh.fs;
   const T *w, *wo;
@@ -107,7 +172,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   } else {
     w = sh.u + (int64_t)((t - 1) & 1) * fs;
     out = sh.u + (int64_t)(t & 1) * fs;
-    wo = out;  // u_t overwrites u_{t-2}: each cell reads its own old value first
+    wo = out;  // u_t overwrites u_{t-2}: row r is read one iteration before it is written
   }
   const T* pin = sh.p + (int64_t)((t - 1) & 1) * fs;
   T* pout = sh.p + (int64_t)(t & 1) * fs;
@@ -115,87 +180,95 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   T* qout = sh.q + (int64_t)(t & 1) * fs;
   const T* __restrict__ cc = sh.c;
   const T* __restrict__ sx = sh.sx;
+  const T* __restrict__ ty = sh.ty;
   const T* __restrict__ srcv = sh.srcv;
-  const bool jin = j <= ny;
   const bool jld = j <= ny + 1;
-  const bool jr = j + 1 <= ny + 1;  // lane 31's right neighbour exists
+  const bool hr = j + C <= ny + 1;  // right halo column exists (last lane of a warp)
   const int64_t col = j + JOFF;
-  const T tj = jld ? sh.ty[j] : T(0);
-  const bool tfree = warp_tau_free<T>(sh.ty, j, ny);
+  T tj[C];
+#pragma unroll
+  for (int c = 0; c < C; c++) tj[c] = (j + c <= ny + 1) ? ty[j + c] : T(0);
+  const bool tfree = warp_tau_free<T, C>(ty, j, ny);
   auto nz = [&](int r) { return !(tfree && sx[r] == T(0)); };  // phi/psi may be non-zero
-  auto LD = [&](const T* a, int r, bool on) -> T {
-    return (jld && on) ? a[(int64_t)r * P + col] : T(0);
-  };
   const int i0 = it.i0, i_end = min(i0 + ri, nx + 1);
+  auto off = [&](int r) { return (int64_t)r * P + col; };
   bool n0 = nz(i0);
-  T wm = LD(w, i0 - 1, true), w0 = LD(w, i0, true), wp = LD(w, i0 + 1, true);
-  T pm = LD(pin, i0 - 1, nz(i0 - 1)), p0 = LD(pin, i0, n0), pp = LD(pin, i0 + 1, nz(i0 + 1));
-  T q0 = LD(qin, i0, n0), wo0 = LD(wo, i0, true), c0 = LD(cc, i0, true);
-  T hw = 0, hq = 0;  // lane 0: (i, j-1); lane 31: (i, j+1)
-  {
-    const int64_t r = (int64_t)i0 * P + col;
-    if (lane == 0 && jld) {
-      hw = w[r - 1];
-      hq = n0 ? qin[r - 1] : T(0);
-    } else if (lane == 31 && jr) {
-      hw = w[r + 1];
-      hq = n0 ? qin[r + 1] : T(0);
-    }
+  V wm = ldv<T, C>(w, off(i0 - 1), jld), w0 = ldv<T, C>(w, off(i0), jld),
+    wp = ldv<T, C>(w, off(i0 + 1), jld);
+  V pm = ldv<T, C>(pin, off(i0 - 1), jld && nz(i0 - 1)), p0 = ldv<T, C>(pin, off(i0), jld && n0),
+    pp = ldv<T, C>(pin, off(i0 + 1), jld && nz(i0 + 1));
+  V q0 = ldv<T, C>(qin, off(i0), jld && n0), wo0 = ldv<T, C>(wo, off(i0), jld),
+    c0 = ldv<T, C>(cc, off(i0), jld);
+  T hw = 0, hq = 0;  // lane 0: column j-1; lane 31: column j+C
+  if (lane == 0 && jld) {
+    hw = w[off(i0) - 1];
+    hq = n0 ? qin[off(i0) - 1] : T(0);
+  } else if (lane == 31 && hr) {
+    hw = w[off(i0) + C];
+    hq = n0 ? qin[off(i0) + C] : T(0);
   }
   for (int i = i0; i < i_end; i++) {
-    const int64_t row = (int64_t)i * P + col;
-    // prefetch: row i+2 of w and phi, row i+1 of psi, w_old, c and the halos
+    const int64_t row = off(i);
     const bool more = i + 1 < i_end;
     const bool n1 = more && nz(i + 1);
-    T wn = 0, pn_ = 0, qn = 0, won = 0, cn = 0, hwn = 0, hqn = 0;
+    V wn = ldv<T, C>(w, off(i + 2), jld && more);
+    V pn_ = ldv<T, C>(pin, off(i + 2), jld && more && nz(i + 2));
+    V qn = ldv<T, C>(qin, off(i + 1), jld && n1);
+    V won = ldv<T, C>(wo, off(i + 1), jld && more);
+    V cn = ldv<T, C>(cc, off(i + 1), jld && more);
+    T hwn = 0, hqn = 0;
     if (more) {
-      wn = LD(w, i + 2, true);
-      pn_ = LD(pin, i + 2, nz(i + 2));
-      qn = LD(qin, i + 1, n1);
-      won = LD(wo, i + 1, true);
-      cn = LD(cc, i + 1, true);
       if (lane == 0 && jld) {
         hwn = w[row + P - 1];
         hqn = n1 ? qin[row + P - 1] : T(0);
-      } else if (lane == 31 && jr) {
-        hwn = w[row + P + 1];
-        hqn = n1 ? qin[row + P + 1] : T(0);
+      } else if (lane == 31 && hr) {
+        hwn = w[row + P + C];
+        hqn = n1 ? qin[row + P + C] : T(0);
       }
     }
-    T wS = __shfl_up_sync(FULL, w0, 1), wN = __shfl_down_sync(FULL, w0, 1);
-    T qS = __shfl_up_sync(FULL, q0, 1), qN = __shfl_down_sync(FULL, q0, 1);
+    T wL = __shfl_up_sync(FULL, w0.v[C - 1], 1), wR = __shfl_down_sync(FULL, w0.v[0], 1);
+    T qL = __shfl_up_sync(FULL, q0.v[C - 1], 1), qR = __shfl_down_sync(FULL, q0.v[0], 1);
     if (lane == 0) {
-      wS = hw;
-      qS = hq;
+      wL = hw;
+      qL = hq;
     } else if (lane == 31) {
-      wN = hw;
-      qN = hq;
+      wR = hw;
+      qR = hq;
     }
-    if (jin) {
-      const T c = c0, sg = sx[i], s = sg + tj;
-      T v = (T(2) - sg * tj * K.dt2 - K.kxy * c) * w0 + c * K.cx * (wp + wm) +
-            c * K.cy * (wN + wS) + K.fx * (pp - pm) + K.fy * (qN - qS) -
-            (T(1) - s * K.hdt) * wo0;
-      if (s != T(0)) v = v / (T(1) + s * K.hdt);
-      for (int e = it.src_b; e < it.src_e; e++) {
-        const CellRef r = srcs[e];
-        if (r.cell == row) v += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
+    if (jld) {
+      const T sg = sx[i];
+      V vo, po, qo;
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        const T wS = c == 0 ? wL : w0.v[c - 1];
+        const T wN = c == C - 1 ? wR : w0.v[c + 1];
+        const T qS = c == 0 ? qL : q0.v[c - 1];
+        const T qN = c == C - 1 ? qR : q0.v[c + 1];
+        const T cv = c0.v[c], s = sg + tj[c];
+        T v = (T(2) - sg * tj[c] * K.dt2 - K.kxy * cv) * w0.v[c] + cv * K.cx * (wp.v[c] + wm.v[c]) +
+              cv * K.cy * (wN + wS) + K.fx * (pp.v[c] - pm.v[c]) + K.fy * (qN - qS) -
+              (T(1) - s * K.hdt) * wo0.v[c];
+        if (s != T(0)) v = v / (T(1) + s * K.hdt);
+        for (int e = it.src_b; e < it.src_e; e++) {
+          const CellRef r = srcs[e];
+          if (r.cell == row + c) v += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
+        }
+        vo.v[c] = v;
+        po.v[c] = (T(1) - K.dt * sg) * p0.v[c] + K.ex * cv * (tj[c] - sg) * (wp.v[c] - wm.v[c]);
+        qo.v[c] = (T(1) - K.dt * tj[c]) * q0.v[c] + K.ey * cv * (sg - tj[c]) * (wN - wS);
       }
-      out[row] = v;
-      T pnew = T(0), qnew = T(0);
+      stv<T, C>(out, row, vo, j, ny);
       if (n0) {
-        pnew = (T(1) - K.dt * sg) * p0 + K.ex * c * (tj - sg) * (wp - wm);
-        qnew = (T(1) - K.dt * tj) * q0 + K.ey * c * (sg - tj) * (wN - wS);
-        pout[row] = pnew;
-        qout[row] = qnew;
+        stv<T, C>(pout, row, po, j, ny);
+        stv<T, C>(qout, row, qo, j, ny);
       }
       if (!SEG && ckpt_slot > 0 && ckpt_slot < sh.nseg) {
         T* ck = sh.ckpt + (int64_t)ckpt_slot * 4 * fs;
-        ck[row] = v;
-        ck[fs + row] = w0;
+        stv<T, C>(ck, row, vo, j, ny);
+        stv<T, C>(ck + fs, row, w0, j, ny);
         if (n0) {
-          ck[2 * fs + row] = pnew;
-          ck[3 * fs + row] = qnew;
+          stv<T, C>(ck + 2 * fs, row, po, j, ny);
+          stv<T, C>(ck + 3 * fs, row, qo, j, ny);
         }
       }
     }
@@ -213,10 +286,14 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     n0 = n1;
   }
   if (!SEG && it.rcv_e > it.rcv_b) {
-    __syncthreads();  // the tile's u_t is in global memory and visible block-wide
-    for (int e = it.rcv_b + threadIdx.x; e < it.rcv_e; e += blockDim.x) {
+    // each warp records the receivers in its own columns: their cells were
+    // written by its lanes, so a warp barrier suffices
+    __syncwarp();
+    const int wj0 = it.j0 + (threadIdx.x >> 5) * 32 * C;
+    for (int e = it.rcv_b + lane; e < it.rcv_e; e += 32) {
       const CellRef r = rcvs[e];
-      sh.traces[(int64_t)t * sh.nrcv + r.idx] = out[r.cell];
+      const int rj = (int)(r.cell % P) - JOFF;
+      if (rj >= wj0 && rj < wj0 + 32 * C) sh.traces[(int64_t)t * sh.nrcv + r.idx] = out[r.cell];
     }
   }
 }
@@ -224,53 +301,32 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
 // Restore checkpoint `slot` of every active shot into the segment store
 // (slot 0 <- u_{a-2}, slot 1 <- u_{a-1}) and the phi/psi rings at a-1.
 template <typename T>
-__global__ void __launch_bounds__(TJ)
+__global__ void __launch_bounds__(Tile<T>::NC)
 k_ac_restore(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
-             int slot, int a, int ri) {
+             int slot, int a, int ri, int pset) {
   const AcItem it = items[blockIdx.x];
   const AcShot<T>& sh = shots[it.shot];
-  const int j = it.j0 + threadIdx.x;
-  if (j > sh.ny) return;
-  const int64_t P = sh.pitch, fs = sh.fs, col = j + JOFF;
+  const int64_t P = sh.pitch, fs = sh.fs;
   const T* ck = sh.ckpt + (int64_t)slot * 4 * fs;
-  T* pr = sh.p + (int64_t)((a - 1) & 1) * fs;
-  T* qr = sh.q + (int64_t)((a - 1) & 1) * fs;
+  const int ps = pset >= 0 ? pset : ((a - 1) & 1);  // phi/psi set the recompute reads
+  T* pr = sh.p + (int64_t)ps * fs;
+  T* qr = sh.q + (int64_t)ps * fs;
   const int i_end = min(it.i0 + ri, sh.nx + 1);
-  for (int i = it.i0; i < i_end; i++) {
-    const int64_t row = (int64_t)i * P + col;
-    sh.seg[row] = ck[fs + row];
-    sh.seg[fs + row] = ck[row];
-    pr[row] = ck[2 * fs + row];
-    qr[row] = ck[3 * fs + row];
+  const int j_end = min(it.j0 + Tile<T>::J, sh.ny + 1);
+  for (int j = it.j0 + threadIdx.x; j < j_end; j += blockDim.x) {
+    const int64_t col = j + JOFF;
+    for (int i = it.i0; i < i_end; i++) {
+      const int64_t row = (int64_t)i * P + col;
+      sh.seg[row] = ck[fs + row];
+      sh.seg[fs + row] = ck[row];
+      pr[row] = ck[2 * fs + row];
+      qr[row] = ck[3 * fs + row];
+    }
   }
 }
 
-// Gradient-side terms of one cell for the i direction (XP: what the cell's
-// stencil sends to its i+1 neighbour, XM: to its i-1 neighbour, XR: to
-// phi's i+-1 neighbours).
-template <typename T>
-struct RowTerms {
-  T gu, gp, c, inv, XP, XM, XR;
-};
-
-template <typename T>
-__device__ __forceinline__ RowTerms<T> row_terms(T gu, T gp, T c, T sg, T tj,
-                                                 const AcConst<T>& K) {
-  RowTerms<T> r;
-  const T s = sg + tj;
-  r.gu = gu;
-  r.gp = gp;
-  r.c = c;
-  r.inv = s != T(0) ? T(1) / (T(1) + s * K.hdt) : T(1);
-  const T gui = gu * r.inv;
-  const T bx = c * K.cx * gui, exg = K.ex * c * (tj - sg) * gp;
-  r.XP = bx + exg;
-  r.XM = bx - exg;
-  r.XR = K.fx * gui;
-  return r;
-}
-
-// j-direction terms of one cell (YP to j+1, YM to j-1, YR to psi's j+-1).
+// One cell's j-direction adjoint terms: YP (to its j+1 neighbour), YM (to its
+// j-1 neighbour), YR (to psi's j+-1 neighbours).
 template <typename T>
 __device__ __forceinline__ void col_terms(T gui, T gq, T c, T sg, T tj, const AcConst<T>& K,
                                           T& YP, T& YM, T& YR) {
@@ -280,20 +336,31 @@ __device__ __forceinline__ void col_terms(T gui, T gq, T c, T sg, T tj, const Ac
   YR = K.fy * gui;
 }
 
+template <typename T>
+__device__ __forceinline__ T inv_den(T s, const AcConst<T>& K) {
+  return s != T(0) ? T(1) / (T(1) + s * K.hdt) : T(1);
+}
+
 // One adjoint step k (gather form of the transpose of step k):
 //   lambdaU_{k-1} = D lambdaU_{k+1} + sum of what u_k, phi_k, psi_k send to w,
 //   lambdaPhi_{k-1}, lambdaPsi_{k-1} likewise, grad_c += d(step k)/dc . lambda_k,
-// then lambdaU_{k-1} += residual_{k-1} at the receivers.  FP32 plans add the
-// grad_c contribution to a per-segment FP32 partial (flushed into the FP64
-// accumulator at the end of each segment); FP64 plans accumulate in FP64.
+// then lambdaU_{k-1} += residual_{k-1} at the receivers.  What a cell of row
+// i+-1 sends to row i (XP/XM: through u's w-stencil and phi's w-difference;
+// XR: through u's phi-difference) is formed from that row's lambdaU_k,
+// lambdaPhi_k, c and 1/den, carried in registers as the thread walks down.
+// FP32 plans add the grad_c contribution to a per-segment FP32 partial
+// (flushed into the FP64 accumulator at the end of each segment); FP64 plans
+// accumulate in FP64.
 template <typename T>
-__global__ void __launch_bounds__(TJ)
+__global__ void __launch_bounds__(Tile<T>::NA, sizeof(T) == 4 ? 3 : 2)
 k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
          const CellRef* __restrict__ rcvs, AcConst<T> K, int k, int base, int ri) {
+  constexpr int C = Tile<T>::CA;
+  using V = Vec<T, C>;
   const AcItem it = items[blockIdx.x];
   const AcShot<T>& sh = shots[it.shot];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int j = it.j0 + warp * 32 + lane;
+  const int lane = threadIdx.x & 31;
+  const int j = it.j0 + threadIdx.x * C;
   const int nx = sh.nx, ny = sh.ny;
   const int64_t P = sh.pitch, fs = sh.fs;
   const T* w = sh.seg + (int64_t)(k - 1 - base) * fs;   // u_{k-1}
@@ -306,138 +373,354 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   const T* __restrict__ cc = sh.c;
   const T* __restrict__ sx = sh.sx;
   const T* __restrict__ ty = sh.ty;
-  const bool jin = j <= ny;
   const bool jld = j <= ny + 1;
-  const bool jr = j + 1 <= ny + 1;
+  const bool hr = j + C <= ny + 1;
   const int64_t col = j + JOFF;
-  const T tj = jld ? ty[j] : T(0);
-  const bool tfree = warp_tau_free<T>(ty, j, ny);
+  T tj[C];
+#pragma unroll
+  for (int c = 0; c < C; c++) tj[c] = (j + c <= ny + 1) ? ty[j + c] : T(0);
+  const bool tfree = warp_tau_free<T, C>(ty, j, ny);
   auto nz = [&](int r) { return !(tfree && sx[r] == T(0)); };
-  auto LD = [&](const T* a, int r, bool on) -> T {
-    return (jld && on) ? a[(int64_t)r * P + col] : T(0);
-  };
-  // halo cell (i, j -+ 1) terms for lanes 0 / 31
-  const T th = lane == 0 ? ty[j - 1] : (jr ? ty[j + 1] : T(0));
-  const int64_t hoff = lane == 0 ? -1 : 1;
-  const bool hon = (lane == 0 && jld) || (lane == 31 && jr);
-
+  // halo column of a warp-edge lane and its tau
+  const int64_t hoff = lane == 0 ? -1 : C;
+  const bool hon = (lane == 0 && jld) || (lane == 31 && hr);
+  const T th = hon ? ty[j + (int)hoff] : T(0);
+  auto off = [&](int r) { return (int64_t)r * P + col; };
   const int i0 = it.i0, i_end = min(i0 + ri, nx + 1);
-  RowTerms<T> Rm = row_terms<T>(LD(luc, i0 - 1, true), LD(lpc, i0 - 1, nz(i0 - 1)),
-                                LD(cc, i0 - 1, true), sx[i0 - 1], tj, K);
-  RowTerms<T> R0 = row_terms<T>(LD(luc, i0, true), LD(lpc, i0, nz(i0)), LD(cc, i0, true),
-                                sx[i0], tj, K);
-  T gu1 = LD(luc, i0 + 1, true), gp1 = LD(lpc, i0 + 1, nz(i0 + 1)), c1 = LD(cc, i0 + 1, true);
-  T wm = LD(w, i0 - 1, true), w0 = LD(w, i0, true), wp = LD(w, i0 + 1, true);
+  // rows i-1 (m), i (0), i+1 (p): lambdaU_k, lambdaPhi_k, c and 1/den per cell
+  V gum = ldv<T, C>(luc, off(i0 - 1), jld), gpm = ldv<T, C>(lpc, off(i0 - 1), jld && nz(i0 - 1)),
+    cm = ldv<T, C>(cc, off(i0 - 1), jld);
+  V gu0 = ldv<T, C>(luc, off(i0), jld), gp0 = ldv<T, C>(lpc, off(i0), jld && nz(i0)),
+    c0 = ldv<T, C>(cc, off(i0), jld);
+  V gu1 = ldv<T, C>(luc, off(i0 + 1), jld), gp1 = ldv<T, C>(lpc, off(i0 + 1), jld && nz(i0 + 1)),
+    c1 = ldv<T, C>(cc, off(i0 + 1), jld);
+  V invm, inv0;
+#pragma unroll
+  for (int c = 0; c < C; c++) {
+    invm.v[c] = inv_den<T>(sx[i0 - 1] + tj[c], K);
+    inv0.v[c] = inv_den<T>(sx[i0] + tj[c], K);
+  }
+  V wm = ldv<T, C>(w, off(i0 - 1), jld), w0 = ldv<T, C>(w, off(i0), jld),
+    wp = ldv<T, C>(w, off(i0 + 1), jld);
   bool n0 = nz(i0);
-  T gq = LD(lqc, i0, n0), lu_next = LD(lun, i0, true);
+  V gq = ldv<T, C>(lqc, off(i0), jld && n0), ln = ldv<T, C>(lun, off(i0), jld);
   T hgu = 0, hgq = 0, hc = 0, hw = 0;
   if (hon) {
-    const int64_t r = (int64_t)i0 * P + col + hoff;
+    const int64_t r = off(i0) + hoff;
     hgu = luc[r];
     hgq = n0 ? lqc[r] : T(0);
     hc = cc[r];
     hw = w[r];
   }
+  T sgm = sx[i0 - 1], sg0 = sx[i0];
   for (int i = i0; i < i_end; i++) {
-    const int64_t row = (int64_t)i * P + col;
-    const RowTerms<T> Rp = row_terms<T>(gu1, gp1, c1, sx[i + 1], tj, K);
+    const int64_t row = off(i);
+    const T sgp = sx[i + 1];
+    V invp;
+#pragma unroll
+    for (int c = 0; c < C; c++) invp.v[c] = inv_den<T>(sgp + tj[c], K);
     // prefetch: row i+2 (lambdaU_k, lambdaPhi_k, c, u_{k-1}), row i+1 (lambdaPsi_k,
-    // lambdaU_{k+1}) and the halo cells of row i+1
+    // lambdaU_{k+1}) and the halo cell of row i+1
     const bool more = i + 1 < i_end;
     const bool n1 = more && nz(i + 1);
-    T gu2 = 0, gp2 = 0, c2 = 0, w2 = 0, gqn = 0, lun1 = 0, hgun = 0, hgqn = 0, hcn = 0, hwn = 0;
-    if (more) {
-      gu2 = LD(luc, i + 2, true);
-      gp2 = LD(lpc, i + 2, nz(i + 2));
-      c2 = LD(cc, i + 2, true);
-      w2 = LD(w, i + 2, true);
-      gqn = LD(lqc, i + 1, n1);
-      lun1 = LD(lun, i + 1, true);
-      if (hon) {
-        const int64_t r = row + P + hoff;
-        hgun = luc[r];
-        hgqn = n1 ? lqc[r] : T(0);
-        hcn = cc[r];
-        hwn = w[r];
-      }
+    V gu2 = ldv<T, C>(luc, off(i + 2), jld && more);
+    V gp2 = ldv<T, C>(lpc, off(i + 2), jld && more && nz(i + 2));
+    V c2 = ldv<T, C>(cc, off(i + 2), jld && more);
+    V w2 = ldv<T, C>(w, off(i + 2), jld && more);
+    V gqn = ldv<T, C>(lqc, off(i + 1), jld && n1);
+    V lnn = ldv<T, C>(lun, off(i + 1), jld && more);
+    T hgun = 0, hgqn = 0, hcn = 0, hwn = 0;
+    if (more && hon) {
+      const int64_t r = row + P + hoff;
+      hgun = luc[r];
+      hgqn = n1 ? lqc[r] : T(0);
+      hcn = cc[r];
+      hwn = w[r];
     }
-    const T sg = sx[i];
-    const T gui = R0.gu * R0.inv;
-    T YP, YM, YR;
-    col_terms<T>(gui, gq, R0.c, sg, tj, K, YP, YM, YR);
-    T YPl = __shfl_up_sync(FULL, YP, 1), YRl = __shfl_up_sync(FULL, YR, 1);
-    T YMr = __shfl_down_sync(FULL, YM, 1), YRr = __shfl_down_sync(FULL, YR, 1);
-    T wS = __shfl_up_sync(FULL, w0, 1), wN = __shfl_down_sync(FULL, w0, 1);
+    // j-direction terms of this thread's cells and of the neighbouring columns
+    T YP[C], YM[C], YR[C], gui[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      gui[c] = gu0.v[c] * inv0.v[c];
+      col_terms<T>(gui[c], gq.v[c], c0.v[c], sg0, tj[c], K, YP[c], YM[c], YR[c]);
+    }
+    T YPl = __shfl_up_sync(FULL, YP[C - 1], 1), YRl = __shfl_up_sync(FULL, YR[C - 1], 1);
+    T YMr = __shfl_down_sync(FULL, YM[0], 1), YRr = __shfl_down_sync(FULL, YR[0], 1);
+    T wL = __shfl_up_sync(FULL, w0.v[C - 1], 1), wR = __shfl_down_sync(FULL, w0.v[0], 1);
     if (lane == 0 || lane == 31) {
-      const T s1 = sg + th;
-      const T inv1 = s1 != T(0) ? T(1) / (T(1) + s1 * K.hdt) : T(1);
-      T a, b, r;
-      col_terms<T>(hgu * inv1, hgq, hc, sg, th, K, a, b, r);
+      T a = 0, b = 0, r = 0;
+      if (hon) col_terms<T>(hgu * inv_den<T>(sg0 + th, K), hgq, hc, sg0, th, K, a, b, r);
       if (lane == 0) {
         YPl = a;
         YRl = r;
-        wS = hw;
+        wL = hw;
       } else {
         YMr = b;
         YRr = r;
-        wN = hw;
+        wR = hw;
       }
     }
-    if (jin) {
-      const T c = R0.c, gp = R0.gp, s = sg + tj;
-      const T nu = -(T(1) - s * K.hdt) * R0.inv * lu_next +
-                   (T(2) - sg * tj * K.dt2 - K.kxy * c) * gui + Rm.XP + Rp.XM + YPl + YMr;
-      const T g = (-K.kxy * w0 + K.cx * (wp + wm) + K.cy * (wN + wS)) * gui +
-                  K.ex * (tj - sg) * (wp - wm) * gp + K.ey * (sg - tj) * (wN - wS) * gq;
-      lun[row] = nu;
+    if (jld) {
+      V nu, np, nq;
+      T g[C];
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        const T ypl = c == 0 ? YPl : YP[c - 1], yrl = c == 0 ? YRl : YR[c - 1];
+        const T ymr = c == C - 1 ? YMr : YM[c + 1], yrr = c == C - 1 ? YRr : YR[c + 1];
+        const T wS = c == 0 ? wL : w0.v[c - 1], wN = c == C - 1 ? wR : w0.v[c + 1];
+        const T guim = gum.v[c] * invm.v[c], guip = gu1.v[c] * invp.v[c];
+        const T XPm = cm.v[c] * K.cx * guim + K.ex * cm.v[c] * (tj[c] - sgm) * gpm.v[c];
+        const T XMp = c1.v[c] * K.cx * guip - K.ex * c1.v[c] * (tj[c] - sgp) * gp1.v[c];
+        const T cv = c0.v[c], s = sg0 + tj[c];
+        nu.v[c] = -(T(1) - s * K.hdt) * inv0.v[c] * ln.v[c] +
+                  (T(2) - sg0 * tj[c] * K.dt2 - K.kxy * cv) * gui[c] + XPm + XMp + ypl + ymr;
+        np.v[c] = (T(1) - K.dt * sg0) * gp0.v[c] + K.fx * guim - K.fx * guip;
+        nq.v[c] = (T(1) - K.dt * tj[c]) * gq.v[c] + yrl - yrr;
+        g[c] = (-K.kxy * w0.v[c] + K.cx * (wp.v[c] + wm.v[c]) + K.cy * (wN + wS)) * gui[c] +
+               K.ex * (tj[c] - sg0) * (wp.v[c] - wm.v[c]) * gp0.v[c] +
+               K.ey * (sg0 - tj[c]) * (wN - wS) * gq.v[c];
+      }
+      stv<T, C>(lun, row, nu, j, ny);
       if (n0) {
-        lpo[row] = (T(1) - K.dt * sg) * gp + Rm.XR - Rp.XR;
-        lqo[row] = (T(1) - K.dt * tj) * gq + YRl - YRr;
+        stv<T, C>(lpo, row, np, j, ny);
+        stv<T, C>(lqo, row, nq, j, ny);
       }
-      if (sizeof(T) == 4)
-        sh.gc32[row] += (float)g;
-      else
-        sh.gc[row] += (double)g;
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        if (j + c > ny) break;
+        if (sizeof(T) == 4)
+          sh.gc32[row + c] += (float)g[c];
+        else
+          sh.gc[row + c] += (double)g[c];
+      }
     }
-    Rm = R0;
-    R0 = Rp;
-    gu1 = gu2;
-    gp1 = gp2;
-    c1 = c2;
-    wm = w0;
-    w0 = wp;
-    wp = w2;
-    gq = gqn;
-    lu_next = lun1;
-    hgu = hgun;
-    hgq = hgqn;
-    hc = hcn;
-    hw = hwn;
+    gum = gu0; gpm = gp0; cm = c0; invm = inv0; sgm = sg0;
+    gu0 = gu1; gp0 = gp1; c0 = c1; inv0 = invp; sg0 = sgp;
+    gu1 = gu2; gp1 = gp2; c1 = c2;
+    wm = w0; w0 = wp; wp = w2;
+    gq = gqn; ln = lnn;
+    hgu = hgun; hgq = hgqn; hc = hcn; hw = hwn;
     n0 = n1;
   }
   if (k - 1 >= 2 && it.rcv_e > it.rcv_b) {
-    __syncthreads();
-    for (int e = it.rcv_b + threadIdx.x; e < it.rcv_e; e += blockDim.x) {
+    // residuals go to cells this warp's lanes wrote: a warp barrier suffices
+    __syncwarp();
+    const int wj0 = it.j0 + (threadIdx.x >> 5) * 32 * C;
+    for (int e = it.rcv_b + lane; e < it.rcv_e; e += 32) {
       const CellRef r = rcvs[e];
-      atomicAdd(lun + r.cell, sh.resid[(int64_t)(k - 1) * sh.nrcv + r.idx]);
+      const int rj = (int)(r.cell % P) - JOFF;
+      if (rj >= wj0 && rj < wj0 + 32 * C)
+        atomicAdd(lun + r.cell, sh.resid[(int64_t)(k - 1) * sh.nrcv + r.idx]);
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Time-blocked forward (FP32 plans): NS <= KB steps per launch.
+//
+// A CTA of TB_THREADS threads owns one column each: output columns
+// [jo, jo + TB_THREADS - 2 KB) and rows [i0, i0 + RB) of one shot, and reads a
+// KB-cell halo around them.  It streams down the rows once; stage s (s = 0..NS-1)
+// turns level s (time t0 + s - 1) into level s + 1 one row behind stage s - 1,
+// so every level lives in registers (a 3-row window per stage) and only level 0
+// is read from and the last level written to HBM.  j-neighbours come from the
+// neighbouring lanes (warp edges through shared memory, exchanged once per
+// row).  Cells outside the grid act as zeros; the halo's wrong values stay
+// outside the output region (one column/row per stage).  FIRST mode reads and
+// writes two alternating state sets (U_t, U_{t-1}, phi, psi) and writes
+// checkpoints and receiver traces of every level; SEG mode takes U from the
+// segment store and writes every level there.
+// ---------------------------------------------------------------------------
+constexpr int TB_THREADS = 256;
+constexpr int TB_WARPS = TB_THREADS / 32;
+
+struct TbItem {
+  int shot, i0, jo, pad;
+  int src_b, src_e;  // sources in the loaded region
+  int rr_b, rr_e;    // receiver rows of the output region
+};
+struct TbSrc {
+  int row, col, idx, pad;
+};
+struct TbRcvRow {
+  int row, map_off;  // receiver index per thread of the tile row (-1: none)
+};
+
+template <typename T, bool SEG, int KB>
+__global__ void __launch_bounds__(TB_THREADS)
+k_ac_fwd_tb(const TbItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
+            const TbSrc* __restrict__ tsrc, const TbRcvRow* __restrict__ trow,
+            const int* __restrict__ tmap, AcConst<T> K, int t0, int NS, int base, int in_set,
+            int ckpt_slot, int RB) {
+  __shared__ T edge[2][TB_WARPS][2][KB][2];  // [row parity][warp][lane 0 | 31][stage][u | psi]
+  const TbItem it = items[blockIdx.x];
+  const AcShot<T>& sh = shots[it.shot];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nx = sh.nx, ny = sh.ny;
+  const int jc = it.jo - KB + tid;
+  const bool inside = jc >= 0 && jc <= ny + 1;
+  const bool icol = jc >= 1 && jc <= ny;
+  const bool outcol = icol && jc >= it.jo && jc < it.jo + TB_THREADS - 2 * KB;
+  const int64_t P = sh.pitch, fs = sh.fs;
+  const int64_t col = (int64_t)jc + JOFF;
+  const int os = 1 - in_set;
+  const T *w, *wo;
+  if (SEG) {
+    w = sh.seg + (int64_t)(t0 - 1 - base) * fs;
+    wo = sh.seg + (int64_t)(t0 - 2 - base) * fs;
+  } else {
+    w = sh.u + (int64_t)in_set * fs;
+    wo = sh.u2 + (int64_t)in_set * fs;
+  }
+  const T* pin = sh.p + (int64_t)in_set * fs;
+  const T* qin = sh.q + (int64_t)in_set * fs;
+  const T* __restrict__ cc = sh.c;
+  const T* __restrict__ sx = sh.sx;
+  const T tj = inside ? sh.ty[jc] : T(0);
+  const int i1 = min(it.i0 + RB, nx + 1);
+  auto ld = [&](const T* a, int r) -> T {
+    return (inside && r >= 0 && r <= nx + 1) ? a[(int64_t)r * P + col] : T(0);
+  };
+  T ua[KB], ub[KB], pa[KB], pb[KB], qb[KB], ou[KB], op[KB], oq[KB], cl[KB + 1];
+#pragma unroll
+  for (int s = 0; s < KB; s++) {
+    ua[s] = ub[s] = pa[s] = pb[s] = qb[s] = ou[s] = op[s] = oq[s] = T(0);
+    cl[s] = T(0);
+  }
+  cl[KB] = T(0);
+  const int rA = it.i0 - NS, rB = it.i0 - NS + 1;
+  ua[0] = ld(w, rA);
+  ub[0] = ld(w, rB);
+  pa[0] = ld(pin, rA);
+  pb[0] = ld(pin, rB);
+  qb[0] = ld(qin, rB);
+  cl[0] = ld(cc, rB);
+  T uo1 = ld(wo, rB);
+  const int r_first = it.i0 - NS + 2, r_last = i1 + NS - 1;
+  if (lane == 0 || lane == 31) {
+#pragma unroll
+    for (int s = 0; s < KB; s++) {
+      edge[r_first & 1][warp][lane == 31][s][0] = ub[s];
+      edge[r_first & 1][warp][lane == 31][s][1] = qb[s];
+    }
+  }
+  __syncthreads();
+  for (int r = r_first; r <= r_last; r++) {
+    const int par = r & 1;
+    const T nu_in = ld(w, r), np_in = ld(pin, r), nq_in = ld(qin, r), nwo = ld(wo, r);
+#pragma unroll
+    for (int s = KB; s > 0; s--) cl[s] = cl[s - 1];
+    cl[0] = ld(cc, r);
+    T prevA = uo1;
+#pragma unroll
+    for (int s = 0; s < KB; s++) {
+      if (s < NS) {
+        const int x = r - s - 1;
+        const int t = t0 + s;  // time of the level this stage produces
+        const T uc = s == 0 ? nu_in : ou[s - 1];
+        const T pc = s == 0 ? np_in : op[s - 1];
+        T uS = __shfl_up_sync(FULL, ub[s], 1), uN = __shfl_down_sync(FULL, ub[s], 1);
+        T qS = __shfl_up_sync(FULL, qb[s], 1), qN = __shfl_down_sync(FULL, qb[s], 1);
+        if (lane == 0) {
+          uS = warp > 0 ? edge[par][warp - 1][1][s][0] : T(0);
+          qS = warp > 0 ? edge[par][warp - 1][1][s][1] : T(0);
+        } else if (lane == 31) {
+          uN = warp < TB_WARPS - 1 ? edge[par][warp + 1][0][s][0] : T(0);
+          qN = warp < TB_WARPS - 1 ? edge[par][warp + 1][0][s][1] : T(0);
+        }
+        T v = T(0), pn = T(0), qn = T(0);
+        if (icol && x >= 1 && x <= nx) {
+          const T sg = sx[x], c = cl[s + 1], sm = sg + tj;
+          v = (T(2) - sg * tj * K.dt2 - K.kxy * c) * ub[s] + c * K.cx * (uc + ua[s]) +
+              c * K.cy * (uN + uS) + K.fx * (pc - pa[s]) + K.fy * (qN - qS) -
+              (T(1) - sm * K.hdt) * prevA;
+          if (sm != T(0)) v = v / (T(1) + sm * K.hdt);
+          if (t <= sh.nstep)
+            for (int e = it.src_b; e < it.src_e; e++) {
+              const TbSrc q = tsrc[e];
+              if (q.row == x && q.col == jc) v += sh.srcv[(int64_t)(t - 1) * sh.nsrc + q.idx];
+            }
+          pn = (T(1) - K.dt * sg) * pb[s] + K.ex * c * (tj - sg) * (uc - ua[s]);
+          qn = (T(1) - K.dt * tj) * qb[s] + K.ey * c * (sg - tj) * (uN - uS);
+        }
+        if (outcol && x >= it.i0 && x < i1) {
+          const int64_t cell = (int64_t)x * P + col;
+          if (SEG) sh.seg[(int64_t)(t - base) * fs + cell] = v;
+          if (!SEG && t <= sh.nstep) {
+            for (int e = it.rr_b; e < it.rr_e; e++) {
+              const TbRcvRow rr = trow[e];
+              if (rr.row != x) continue;
+              for (int idx = tmap[rr.map_off + tid]; idx >= 0; idx = sh.rcv_next[idx])
+                sh.traces[(int64_t)t * sh.nrcv + idx] = v;
+            }
+          }
+        }
+        const T nextA = ua[s];  // level s at row x-1: the old field of stage s+1
+        ua[s] = ub[s];
+        ub[s] = uc;
+        pa[s] = pb[s];
+        pb[s] = pc;
+        qb[s] = s == 0 ? nq_in : oq[s - 1];
+        ou[s] = v;
+        op[s] = pn;
+        oq[s] = qn;
+        prevA = nextA;
+      }
+    }
+    uo1 = nwo;
+    // the last stage finished row r - NS: write the block's final state
+    const int xf = r - NS;
+    if (outcol && xf >= it.i0 && xf < i1) {
+      const int64_t cell = (int64_t)xf * P + col;
+      T uf = T(0), ul = T(0), pf = T(0), qf = T(0);
+#pragma unroll
+      for (int s = 0; s < KB; s++)
+        if (s == NS - 1) {
+          uf = ou[s];
+          ul = ua[s];
+          pf = op[s];
+          qf = oq[s];
+        }
+      if (!SEG) {
+        sh.u[(int64_t)os * fs + cell] = uf;
+        sh.u2[(int64_t)os * fs + cell] = ul;
+        if (ckpt_slot > 0 && ckpt_slot < sh.nseg) {
+          T* ck = sh.ckpt + (int64_t)ckpt_slot * 4 * fs;
+          ck[cell] = uf;
+          ck[fs + cell] = ul;
+          ck[2 * fs + cell] = pf;
+          ck[3 * fs + cell] = qf;
+        }
+      }
+      sh.p[(int64_t)os * fs + cell] = pf;
+      sh.q[(int64_t)os * fs + cell] = qf;
+    }
+    if (lane == 0 || lane == 31) {
+#pragma unroll
+      for (int s = 0; s < KB; s++) {
+        edge[par ^ 1][warp][lane == 31][s][0] = ub[s];
+        edge[par ^ 1][warp][lane == 31][s][1] = qb[s];
+      }
+    }
+    __syncthreads();
   }
 }
 
 // End of a segment (FP32 plans): grad_c (FP64) += the segment's FP32 partial,
 // which is reset to zero.
 template <typename T>
-__global__ void __launch_bounds__(TJ)
+__global__ void __launch_bounds__(Tile<T>::NC)
 k_ac_flush_gc(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots, int ri) {
   const AcItem it = items[blockIdx.x];
   const AcShot<T>& sh = shots[it.shot];
-  const int j = it.j0 + threadIdx.x;
-  if (j > sh.ny) return;
   const int i_end = min(it.i0 + ri, sh.nx + 1);
-  for (int i = it.i0; i < i_end; i++) {
-    const int64_t row = (int64_t)i * sh.pitch + j + JOFF;
-    sh.gc[row] += (double)sh.gc32[row];
-    sh.gc32[row] = 0.f;
+  const int j_end = min(it.j0 + Tile<T>::J, sh.ny + 1);
+  for (int j = it.j0 + threadIdx.x; j < j_end; j += blockDim.x) {
+    for (int i = it.i0; i < i_end; i++) {
+      const int64_t row = (int64_t)i * sh.pitch + j + JOFF;
+      sh.gc[row] += (double)sh.gc32[row];
+      sh.gc32[row] = 0.f;
+    }
   }
 }
 
@@ -591,6 +874,16 @@ struct AcPlan final : AcPlanBase {
   int seg_timed = -1;
   bool timing_run = false;  // set only for profile(): direct launches, events recorded
   double tcount[6] = {};  // launches, cell-steps for fwd / recompute / adjoint
+  // time-blocked forward (FP32): steps per block, tile rows, tile lists
+  int KB = 1, RB = 32;
+  std::vector<int> tb_shot_end;  // per sorted shot: TB items of shots [0..s]
+  TbItem* d_tb_items = nullptr;
+  TbSrc* d_tb_srcs = nullptr;
+  TbRcvRow* d_tb_rows = nullptr;
+  int* d_tb_map = nullptr;
+  int tb_items_upto(int n) const { return n <= 0 ? 0 : tb_shot_end[n - 1]; }
+  int launch_tb(cudaStream_t st, bool seg, int nit, int t0, int NS, int base, int in_set,
+                int ck);
 
   ~AcPlan() override {
     for (auto& e : ev)
@@ -705,7 +998,20 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     ri = c.rows_per_thread;
   } else {
     ri = 16;
-    while (ri > 2 && cells / ((int64_t)ri * TJ) < 152 * 8) ri /= 2;
+    while (ri > 2 && cells / ((int64_t)ri * Tile<T>::J) < 152 * 8) ri /= 2;
+  }
+  // ---- time blocking of the forward steps (FP32 plans)
+  KB = sizeof(T) == 4 ? (c.steps_per_block > 0 ? c.steps_per_block : 1) : 1;
+  ADS_REQUIRE(c.steps_per_block >= 0 && (KB == 1 || KB == 2 || KB == 4 || KB == 8),
+              "steps_per_block must be 0 (automatic), 1, 2, 4 or 8");
+  ADS_REQUIRE(sizeof(T) == 4 || c.steps_per_block <= 1,
+              "time blocking is implemented for FP32 plans (steps_per_block 0 or 1 for FP64)");
+  if (c.block_rows > 0) {
+    RB = c.block_rows;
+  } else {
+    RB = 32;
+    const int64_t colw = TB_THREADS - 2 * KB;
+    while (RB > 4 && cells / ((int64_t)RB * colw) < 152 * 4) RB /= 2;
   }
   // ---- trace layout (packed in the caller's shot order)
   trace_off.resize(ns);
@@ -719,7 +1025,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   size_t off_fwd_begin, off_fwd_end, off_adj_begin, off_adj_end;
   DevPool L;
   struct Offs {
-    size_t u, p, q, seg, ckpt, lu, lp, lq, c, sx, ty, gc, gc32, srcv;
+    size_t u, u2, p, q, seg, ckpt, lu, lp, lq, c, sx, ty, gc, gc32, srcv;
   };
   std::vector<Offs> offs(ns);
   std::vector<int> nseg(ns);
@@ -732,6 +1038,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   for (int s = 0; s < ns; s++) {
     const int64_t fs = (shots[order[s]].nx + 2) * pitch * (int64_t)sizeof(T);
     offs[s].u = L.take(2 * fs);
+    offs[s].u2 = L.take(KB > 1 ? 2 * fs : 0);
     offs[s].p = L.take(2 * fs);
     offs[s].q = L.take(2 * fs);
   }
@@ -750,7 +1057,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   for (int s = 0; s < ns; s++) {
     const ads_acoustic_shot& h = shots[order[s]];
     const int64_t fs = (h.nx + 2) * pitch * (int64_t)sizeof(T);
-    offs[s].seg = L.take((size_t)(K + 1) * fs);
+    offs[s].seg = L.take((size_t)(K + 2) * fs);
     offs[s].ckpt = L.take((size_t)nseg[s] * 4 * fs);
     offs[s].c = L.take(fs);
     offs[s].sx = L.take(sizeof(T) * (h.nx + 2));
@@ -776,7 +1083,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     }
     rcv_e_host[s] = (int)shot_rcvs.size();
     for (int i0 = 1; i0 <= nx; i0 += ri) {
-      for (int j0 = 1; j0 <= ny; j0 += TJ) {
+      for (int j0 = 1; j0 <= ny; j0 += Tile<T>::J) {
         AcItem it{};
         it.shot = s;
         it.i0 = i0;
@@ -784,14 +1091,15 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
         it.src_b = (int)srcs.size();
         for (int64_t k = 0; k < h.nsrc; k++) {
           const int64_t i = h.srci[k] - 1, j = h.srcj[k] - 1;
-          if (i >= i0 && i < i0 + ri && j >= j0 && j < j0 + TJ)
+          if (i >= i0 && i < i0 + ri && j >= j0 && j < j0 + Tile<T>::J)
             srcs.push_back({i * pitch + j + JOFF, (int)k, 0});
         }
         it.src_e = (int)srcs.size();
         it.rcv_b = (int)rcvs.size();
         for (int64_t r = 0; r < h.nrcv; r++) {
           const int64_t i = h.rcvi[r] - 1, j = h.rcvj[r] - 1;
-          if (i >= i0 && i < i0 + ri && i <= nx && j >= j0 && j < j0 + TJ && j <= ny && j >= 1)
+          if (i >= i0 && i < i0 + ri && i <= nx && j >= j0 && j < j0 + Tile<T>::J && j <= ny &&
+              j >= 1)
             rcvs.push_back({i * pitch + j + JOFF, (int)r, 0});
         }
         it.rcv_e = (int)rcvs.size();
@@ -801,6 +1109,72 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     item_shot_end[s] = (int)items.size();
   }
   nitems = (int)items.size();
+  // time-blocked tiles: output columns [jo, jo + W), rows [i0, i0 + RB); sources
+  // of the loaded region (halo KB); receiver maps of the output region
+  std::vector<TbItem> tb_items;
+  std::vector<TbSrc> tb_srcs;
+  std::vector<TbRcvRow> tb_rows;
+  std::vector<int> tb_map, rcv_next_all;
+  std::vector<int> rcv_next_off(ns, 0);
+  tb_shot_end.assign(ns, 0);
+  if (KB > 1) {
+    const int W = TB_THREADS - 2 * KB;
+    for (int s = 0; s < ns; s++) {
+      const ads_acoustic_shot& h = shots[order[s]];
+      const int nx = (int)h.nx, ny = (int)MY;
+      rcv_next_off[s] = (int)rcv_next_all.size();
+      std::vector<int> next(h.nrcv, -1);
+      for (int64_t r = 0; r < h.nrcv; r++)  // chain receivers sharing a cell
+        for (int64_t q = r + 1; q < h.nrcv; q++)
+          if (h.rcvi[q] == h.rcvi[r] && h.rcvj[q] == h.rcvj[r]) {
+            next[r] = (int)q;
+            break;
+          }
+      rcv_next_all.insert(rcv_next_all.end(), next.begin(), next.end());
+      for (int i0 = 1; i0 <= nx; i0 += RB) {
+        const int i1 = std::min(i0 + RB, nx + 1);
+        for (int jo = 1; jo <= ny; jo += W) {
+          TbItem it{};
+          it.shot = s;
+          it.i0 = i0;
+          it.jo = jo;
+          it.src_b = (int)tb_srcs.size();
+          for (int64_t k = 0; k < h.nsrc; k++) {
+            const int i = (int)h.srci[k] - 1, j = (int)h.srcj[k] - 1;
+            if (i >= i0 - KB && i < i1 + KB && j >= jo - KB && j < jo - KB + TB_THREADS)
+              tb_srcs.push_back({i, j, (int)k, 0});
+          }
+          it.src_e = (int)tb_srcs.size();
+          it.rr_b = (int)tb_rows.size();
+          for (int i = i0; i < i1; i++) {
+            int off = -1;
+            for (int64_t r = 0; r < h.nrcv; r++) {
+              const int ri_ = (int)h.rcvi[r] - 1, rj = (int)h.rcvj[r] - 1;
+              if (ri_ != i || rj < jo || rj >= jo + W || rj < 1 || rj > ny) continue;
+              bool first = true;  // only the first receiver of a cell enters the map
+              for (int64_t q = 0; q < r; q++)
+                if (h.rcvi[q] == h.rcvi[r] && h.rcvj[q] == h.rcvj[r]) first = false;
+              if (!first) continue;
+              if (off < 0) {
+                off = (int)tb_map.size();
+                tb_map.insert(tb_map.end(), TB_THREADS, -1);
+                tb_rows.push_back({i, off});
+              }
+              tb_map[off + (rj - jo + KB)] = (int)r;
+            }
+          }
+          it.rr_e = (int)tb_rows.size();
+          tb_items.push_back(it);
+        }
+      }
+      tb_shot_end[s] = (int)tb_items.size();
+    }
+  }
+  const size_t tbi_off = L.take(sizeof(TbItem) * std::max<size_t>(tb_items.size(), 1));
+  const size_t tbs_off = L.take(sizeof(TbSrc) * std::max<size_t>(tb_srcs.size(), 1));
+  const size_t tbr_off = L.take(sizeof(TbRcvRow) * std::max<size_t>(tb_rows.size(), 1));
+  const size_t tbm_off = L.take(sizeof(int) * std::max<size_t>(tb_map.size(), 1));
+  const size_t rnx_off = L.take(sizeof(int) * std::max<size_t>(rcv_next_all.size(), 1));
   const size_t shots_off = L.take(sizeof(AcShot<T>) * ns);
   const size_t items_off = L.take(sizeof(AcItem) * items.size());
   const size_t srcs_off = L.take(sizeof(CellRef) * std::max<size_t>(srcs.size(), 1));
@@ -834,6 +1208,10 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   d_shot_rcvs = (CellRef*)(pool + shot_rcvs_off);
   d_rcv_b = (int*)(pool + rcvb_off);
   d_rcv_e = (int*)(pool + rcve_off);
+  d_tb_items = (TbItem*)(pool + tbi_off);
+  d_tb_srcs = (TbSrc*)(pool + tbs_off);
+  d_tb_rows = (TbRcvRow*)(pool + tbr_off);
+  d_tb_map = (int*)(pool + tbm_off);
   // per-shot structs and host-side data (profiles, scaled wavelets)
   hshots.resize(ns);
   std::vector<double> sx, ty;
@@ -852,6 +1230,8 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     d.nrcv = (int)h.nrcv;
     d.nseg = nseg[s];
     d.u = (T*)(pool + offs[s].u);
+    d.u2 = (T*)(pool + offs[s].u2);
+    d.rcv_next = (const int*)(pool + rnx_off) + rcv_next_off[s];
     d.p = (T*)(pool + offs[s].p);
     d.q = (T*)(pool + offs[s].q);
     d.seg = (T*)(pool + offs[s].seg);
@@ -906,6 +1286,16 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
                            cudaMemcpyHostToDevice, st));
   ADS_CUDA(cudaMemcpyAsync(d_rcv_e, rcv_e_host.data(), sizeof(int) * ns,
                            cudaMemcpyHostToDevice, st));
+  auto up = [&](void* dst, const void* src, size_t n) -> int {
+    if (n) ADS_CUDA(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, st));
+    return ADS_OK;
+  };
+  if (int e = up(d_tb_items, tb_items.data(), sizeof(TbItem) * tb_items.size())) return e;
+  if (int e = up(d_tb_srcs, tb_srcs.data(), sizeof(TbSrc) * tb_srcs.size())) return e;
+  if (int e = up(d_tb_rows, tb_rows.data(), sizeof(TbRcvRow) * tb_rows.size())) return e;
+  if (int e = up(d_tb_map, tb_map.data(), sizeof(int) * tb_map.size())) return e;
+  if (int e = up(pool + rnx_off, rcv_next_all.data(), sizeof(int) * rcv_next_all.size()))
+    return e;
   ADS_CUDA(cudaStreamSynchronize(st));  // host staging buffers go out of scope
   // ---- timing ranges: the first full-length segment the reverse sweep meets
   cells_prefix.resize(ns);
@@ -956,28 +1346,68 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
 // Forward time loop (zero the rings and traces, then one launch per step).
 // count != nullptr: only count kernel launches.
 template <typename T>
+int AcPlan<T>::launch_tb(cudaStream_t st, bool seg, int nit, int t0, int NS, int base,
+                         int in_set, int ck) {
+  if constexpr (sizeof(T) == 4) {
+#define ADS_TB(KBV)                                                                         \
+  if (seg)                                                                                  \
+    k_ac_fwd_tb<T, true, KBV><<<nit, TB_THREADS, 0, st>>>(d_tb_items, d_shots, d_tb_srcs,   \
+                                                          d_tb_rows, d_tb_map, kc, t0, NS,  \
+                                                          base, in_set, ck, RB);            \
+  else                                                                                      \
+    k_ac_fwd_tb<T, false, KBV><<<nit, TB_THREADS, 0, st>>>(d_tb_items, d_shots, d_tb_srcs,  \
+                                                           d_tb_rows, d_tb_map, kc, t0, NS, \
+                                                           base, in_set, ck, RB);
+    switch (KB) {
+      case 2: ADS_TB(2) break;
+      case 4: ADS_TB(4) break;
+      default: ADS_TB(8) break;
+    }
+#undef ADS_TB
+    ADS_LAUNCHED(1);
+    return ADS_OK;
+  } else {
+    (void)st; (void)seg; (void)nit; (void)t0; (void)NS; (void)base; (void)in_set; (void)ck;
+    return fail(ADS_ERR_UNSUPPORTED, "time-blocked steps are implemented for FP32 plans");
+  }
+}
+
+// Forward time loop (zero the state and traces, then the steps 2..NSTEP: one
+// launch per step, or per block of up to KB steps that never crosses a
+// checkpoint time 1 + sK).  count != nullptr: only count launches and the
+// interior cell-steps of the loop.
+template <typename T>
 int AcPlan<T>::issue_forward(cudaStream_t st, int64_t* count) {
   if (count) {
     *count = 0;
     tcount[0] = tcount[1] = 0;
-    for (int t = 2; t <= nstep[0]; t++) {
+  } else {
+    ADS_CUDA(cudaMemsetAsync(pool + zero_fwd_off, 0, zero_fwd_len, st));
+    if (timing_run) ADS_CUDA(cudaEventRecord(ev[0], st));
+  }
+  int t0 = 2, blk = 0;
+  while (t0 <= nstep[0]) {
+    const int bound = 1 + K * (int)div_up(t0 - 1, K);  // next checkpoint time >= t0
+    const int NS = KB > 1 ? std::min({KB, bound - t0 + 1, nstep[0] - t0 + 1}) : 1;
+    const int t1 = t0 + NS - 1;
+    const int na = shots_with_nstep_ge(t0);
+    // checkpoint s >= 1 holds the state before step a_s = 2 + s K, i.e. after t = 1 + s K
+    const int ck = ((t1 - 1) % K == 0) ? (t1 - 1) / K : 0;
+    if (count) {
       *count += 1;
       tcount[0] += 1;
-      tcount[1] += (double)cells_upto(shots_with_nstep_ge(t));
+      for (int t = t0; t <= t1; t++) tcount[1] += (double)cells_upto(shots_with_nstep_ge(t));
+    } else if (KB > 1) {
+      if (int e = launch_tb(st, false, tb_items_upto(na), t0, NS, 0, blk & 1, ck)) return e;
+    } else {
+      k_ac_fwd<T, false><<<items_upto(na), Tile<T>::NF, 0, st>>>(d_items, d_shots, d_srcs,
+                                                                d_rcvs, kc, t0, 0, ck, ri);
+      ADS_LAUNCHED(1);
     }
-    return ADS_OK;
+    t0 = t1 + 1;
+    blk++;
   }
-  ADS_CUDA(cudaMemsetAsync(pool + zero_fwd_off, 0, zero_fwd_len, st));
-  if (timing_run) ADS_CUDA(cudaEventRecord(ev[0], st));
-  for (int t = 2; t <= nstep[0]; t++) {
-    const int na = shots_with_nstep_ge(t);
-    const int nit = items_upto(na);
-    // checkpoint s >= 1 holds the state before step a_s = 2 + s K, i.e. after t = 1 + s K
-    const int ck = ((t - 1) % K == 0) ? (t - 1) / K : 0;
-    k_ac_fwd<T, false><<<nit, TJ, 0, st>>>(d_items, d_shots, d_srcs, d_rcvs, kc, t, 0, ck, ri);
-    ADS_LAUNCHED(1);
-  }
-  if (timing_run) ADS_CUDA(cudaEventRecord(ev[1], st));
+  if (!count && timing_run) ADS_CUDA(cudaEventRecord(ev[1], st));
   return ADS_OK;
 }
 
@@ -999,26 +1429,33 @@ int AcPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     if (na == 0) continue;
     const int b_max = std::min(a + K - 1, nstep[0]);
     if (!count) {
-      k_ac_restore<T><<<items_upto(na), TJ, 0, st>>>(d_items, d_shots, s, a, ri);
+      k_ac_restore<T><<<items_upto(na), Tile<T>::NC, 0, st>>>(d_items, d_shots, s, a, ri,
+                                                              KB > 1 ? 0 : -1);
       ADS_LAUNCHED(1);
     }
     n++;
     const bool timed = s == seg_timed;
     if (timed && timing_run) ADS_CUDA(cudaEventRecord(ev[2], st));
     if (timed && count) tcount[2] = tcount[3] = tcount[4] = tcount[5] = 0;
-    for (int t = a; t <= b_max - 1; t++) {
+    for (int t0 = a, blk = 0; t0 <= b_max - 1; blk++) {
       // active while t < b_shot = min(a+K-1, nstep), i.e. nstep >= t+1
-      const int nt = shots_with_nstep_ge(t + 1);
+      const int NS = KB > 1 ? std::min(KB, b_max - t0) : 1;
+      const int nt = shots_with_nstep_ge(t0 + 1);
       if (timed && count) {
         tcount[2] += 1;
-        tcount[3] += (double)cells_upto(nt);
+        for (int t = t0; t < t0 + NS; t++) tcount[3] += (double)cells_upto(shots_with_nstep_ge(t + 1));
       }
       if (!count) {
-        k_ac_fwd<T, true><<<items_upto(nt), TJ, 0, st>>>(d_items, d_shots, d_srcs, d_rcvs, kc,
-                                                         t, a - 2, 0, ri);
-        ADS_LAUNCHED(1);
+        if (KB > 1) {
+          if (int e = launch_tb(st, true, tb_items_upto(nt), t0, NS, a - 2, blk & 1, 0)) return e;
+        } else {
+          k_ac_fwd<T, true><<<items_upto(nt), Tile<T>::NF, 0, st>>>(d_items, d_shots, d_srcs,
+                                                                   d_rcvs, kc, t0, a - 2, 0, ri);
+          ADS_LAUNCHED(1);
+        }
       }
       n++;
+      t0 += NS;
     }
     if (timed && timing_run) {
       ADS_CUDA(cudaEventRecord(ev[3], st));
@@ -1031,7 +1468,7 @@ int AcPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
         tcount[5] += (double)cells_upto(nk);
       }
       if (!count) {
-        k_ac_adj<T><<<items_upto(nk), TJ, 0, st>>>(d_items, d_shots, d_rcvs, kc, k, a - 2, ri);
+        k_ac_adj<T><<<items_upto(nk), Tile<T>::NA, 0, st>>>(d_items, d_shots, d_rcvs, kc, k, a - 2, ri);
         ADS_LAUNCHED(1);
       }
       n++;
@@ -1039,7 +1476,7 @@ int AcPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     if (timed && timing_run) ADS_CUDA(cudaEventRecord(ev[5], st));
     if (sizeof(T) == 4) {  // fold the segment's FP32 grad_c partial into FP64
       if (!count) {
-        k_ac_flush_gc<T><<<items_upto(na), TJ, 0, st>>>(d_items, d_shots, ri);
+        k_ac_flush_gc<T><<<items_upto(na), Tile<T>::NC, 0, st>>>(d_items, d_shots, ri);
         ADS_LAUNCHED(1);
       }
       n++;

@@ -64,9 +64,11 @@ void elastic_cpml(int64_t NX, int64_t NY, double dx, double dy, double dt, int64
 // Internal grid layout used by the plans: each padded row of ny+2 cells is
 // stored with a pitch that is a multiple of 32 elements and an offset of
 // JOFF = 31, so that interior column j = 1 starts on a 32-element boundary
-// (128 B for FP32, 256 B for FP64) and every warp row load is aligned.
+// (128 B for FP32, 256 B for FP64) and every warp row load is aligned.  The
+// pitch leaves at least 32 spare elements after column ny+1 so that a
+// thread's vector load starting at a valid column never leaves its row.
 // ---------------------------------------------------------------------------
 constexpr int JOFF = 31;
-inline int64_t grid_pitch(int64_t ny) { return round_up(ny + 2 + JOFF, 32); }
+inline int64_t grid_pitch(int64_t ny) { return round_up(ny + 2 + JOFF + 32, 32); }
 
 }  // namespace ads

@@ -237,7 +237,10 @@ typedef struct ads_acoustic_config {
   int32_t use_graph;  /* 1: capture the time loops in CUDA graphs (default) */
   int64_t ckpt_every; /* forward checkpoint spacing k in steps; 0 = automatic */
   int32_t rows_per_thread; /* stencil tile height (autotuner); 0 = automatic */
-  int32_t reserved[7];
+  int32_t steps_per_block; /* time steps per forward launch (FP32: 1, 2, 4, 8;
+                              FP64: 1); 0 = automatic (1) */
+  int32_t block_rows;      /* tile height of the time-blocked forward; 0 = automatic */
+  int32_t reserved[5];
 } ads_acoustic_config;
 
 typedef struct ads_acoustic_shot {

@@ -204,6 +204,27 @@ def test_plan_uneven_multishot_vs_oracle(ads, orc, cuda, precision, rows):
     plan.close()
 
 
+@pytest.mark.parametrize("kb,rows", [(1, 0), (2, 0), (4, 0), (8, 0), (4, 3), (8, 5)])
+def test_plan_fp32_time_blocked_vs_oracle(ads, orc, cuda, kb, rows):
+    MX, MY, shots, vp = uneven_case(77, nshots=4)
+    h, dt, npml, vref = 10.0, 1e-3, 5, 1500.0
+    ref_tr = oracle_multishot(orc, MX, MY, shots, vp, h, dt, npml, vref)
+    rng = np.random.default_rng(8)
+    obs = [t * 0.9 + 1e-3 * rng.standard_normal(t.shape) for t in ref_tr]
+    ref_loss, ref_grad = oracle_multishot(orc, MX, MY, shots, vp, h, dt, npml, vref, obs)
+    plan = ads.AcousticPlan(MX, MY, h, h, dt, shots, npml=npml, vp_ref=vref, precision="f32",
+                            ckpt_every=7, steps_per_block=kb, block_rows=rows)
+    tr = plan.forward(T(vp, cuda))
+    for a, b in zip(plan.split_traces(tr), ref_tr):
+        if b.size:
+            assert rel(a.double().cpu().numpy(), b) <= 1e-5
+    loss, grad = plan.gradient(T(vp, cuda), plan.pack([T(o, cuda, torch.float32) for o in obs]))
+    torch.cuda.synchronize()
+    assert abs(float(loss) - ref_loss) <= TOL32 * ref_loss
+    assert rel(grad.cpu().numpy(), ref_grad) <= TOL32
+    plan.close()
+
+
 def test_repeated_calls_are_deterministic(ads, cuda):
     MX, MY, shots, vp = uneven_case(5, nshots=3)
     plan = ads.AcousticPlan(MX, MY, 10.0, 10.0, 1e-3, shots, npml=5, precision="f32")
