@@ -41,7 +41,7 @@ constexpr unsigned FULL = 0xffffffffu;
 template <typename T>
 struct Tile {
   static constexpr int J = sizeof(T) == 4 ? 512 : 256;
-  static constexpr int CF = sizeof(T) == 4 ? 4 : 2;
+  static constexpr int CF = sizeof(T) == 4 ? 2 : 2;
   static constexpr int CA = sizeof(T) == 4 ? 2 : 1;
   static constexpr int NF = J / CF;  // forward threads per CTA (128)
   static constexpr int NA = J / CA;  // adjoint threads per CTA (256)
