@@ -207,12 +207,215 @@ def run_reference(args):
     return 0
 
 
+def _timed(fn, steps, warmup):
+    """Device time per call (ms) of `fn` on the current stream."""
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def _line(metric, value, unit, args, ms, dtype, workload, extra):
+    out = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+           "config": {"workload": workload}}
+    out.update(extra)
+    print(json.dumps(out))
+
+
+def run_acoustic_fwd_f64(args):
+    """Plain FP64 acoustic forward: 200x200 interior plus a 20-cell PML, h = 10 m,
+    dt = 1 ms, 1000 steps, one 10 Hz Ricker source 20 cells below the PML, 200
+    receivers 5 cells below it (the reference CPU operators' own configuration)."""
+    import torch
+    import __graft_entry__ as g
+    import oracle
+
+    ads = g.load_package()
+    NX = NY = 240
+    npml, T, h, dt = 20, 1000, 10.0, 1e-3
+    vp = ads.layered_gaussian_model(NX + 2, NY + 2, 2000.0, 3500.0, seed=7)
+    p = ads.AcousticPropagatorParams(NX=NX, NY=NY, NSTEP=T, DELTAT=dt)
+    wav = ads.Ricker(p, ads.ricker_width_samples(10.0, dt), 1.5 / 10.0 / dt, 1e6)
+    shot = dict(x0=0, nx=NX, nstep=T, srci=[NX // 2 + 1], srcj=[npml + 21], srcv=wav[:, None],
+                rcvi=np.arange(npml + 2, npml + 202), rcvj=np.full(200, npml + 6))
+    plan = ads.AcousticPlan(NX, NY, h, h, dt, [shot], npml=npml, vp_ref=float(vp.mean()),
+                            precision="f64")
+    vdev = torch.tensor(vp, device="cuda")
+    ms = _timed(lambda: plan.forward(vdev), args.steps, args.warmup)
+    cells = NX * NY * (T - 1)
+    vh = torch.tensor(vp).pin_memory()
+    th = torch.empty(plan.trace_count, dtype=torch.float64).pin_memory()
+
+    def e2e():
+        vdev.copy_(vh, non_blocking=True)
+        th.copy_(plan.forward(vdev), non_blocking=True)
+
+    ms_e2e = _timed(e2e, args.steps, 1)
+    oracle.build(ref=False)
+    sx, ty = oracle.acoustic_pml(NX, NY, h, h, npml, float(vp.mean()))
+    t0 = time.perf_counter()
+    oracle.acoustic_forward(NX, NY, T, dt, h, h, sx, ty, vp.reshape(-1), shot["srci"],
+                            shot["srcj"], wav[:, None], shot["rcvi"], shot["rcvj"],
+                            use_ref=oracle.ref_available())
+    t_cpu = time.perf_counter() - t0
+    _line("acoustic forward Gcell-updates/s, plain FP64 drop-in", cells / (ms / 1e3) / 1e9,
+          "Gcell-updates/s", args, ms, "f64",
+          "acoustic forward 240x240 (200x200 + PML 20), 1000 steps, 1 shot, 200 receivers",
+          {"e2e": {"value": cells / (ms_e2e / 1e3) / 1e9, "unit": "Gcell-updates/s",
+                   "h2d_bytes_per_step": vp.size * 8, "d2h_bytes_per_step": plan.trace_count * 8},
+           "cpu_baseline": {"value": cells / t_cpu / 1e9, "unit": "Gcell-updates/s", "cores": 1,
+                            "kind": "reference" if oracle.ref_available() else "port",
+                            "sample": "the full forward, one core"},
+           "gpu_launches": int(plan.launches_forward)})
+    plan.close()
+
+
+def run_fwi_f64(args):
+    """Plain FP64 acoustic FWI gradient: 400x400 incl. PML 30, 2000 steps, 8 shots
+    20 cells below the PML at the centres of 8 equal segments, one receiver per
+    interior column 5 cells below the PML, observed data from the true model,
+    gradient at a Gaussian-smoothed (20 cells) start model."""
+    import torch
+    import __graft_entry__ as g
+
+    ads = g.load_package()
+    NX = NY = 400
+    npml, T, h, dt = 30, 2000, 10.0, 1e-3
+    vt = ads.layered_gaussian_model(NX + 2, NY + 2, 2000.0, 3500.0, seed=11)
+    v0 = ads.gaussian_smooth(vt, 20.0)
+    p = ads.AcousticPropagatorParams(NX=NX, NY=NY, NSTEP=T, DELTAT=dt)
+    wav = ads.Ricker(p, ads.ricker_width_samples(10.0, dt), 1.5 / 10.0 / dt, 1e6)
+    seg = (NX - 2 * npml) / 8
+    shots = [dict(x0=0, nx=NX, nstep=T, srci=[int(npml + 1 + (k + 0.5) * seg) + 1],
+                  srcj=[npml + 21], srcv=wav[:, None],
+                  rcvi=np.arange(npml + 2, NX - npml + 2), rcvj=np.full(NX - 2 * npml, npml + 6))
+             for k in range(8)]
+    plan = ads.AcousticPlan(NX, NY, h, h, dt, shots, npml=npml, vp_ref=float(vt.mean()),
+                            precision="f64")
+    obs = plan.forward(torch.tensor(vt, device="cuda")).clone()
+    vdev = torch.tensor(v0, device="cuda")
+    ms = _timed(lambda: plan.gradient(vdev, obs), args.steps, args.warmup)
+    cells = 2 * 8 * NX * NY * (T - 1)
+    _line("FWI shot-gradients/s, plain FP64 drop-in", 8 / (ms / 1e3), "shot-gradients/s", args,
+          ms, "f64", "acoustic FWI gradient 400x400 (PML 30), 2000 steps, 8 shots",
+          {"gcell_updates_per_s": cells / (ms / 1e3) / 1e9,
+           "gpu_launches": int(plan.launches_gradient)})
+    plan.close()
+
+
+def elastic_workload(ads, nshots=32, NX=600, NY=300, npml=30, T=4000, h=10.0, dt=0.8e-3,
+                     fpeak=10.0, seed=5):
+    rng = np.random.default_rng(seed)
+    j = np.arange(NY + 2, dtype=np.float64)
+    vp1 = 2500.0 + 2500.0 * np.floor(j / (NY + 2) * 5) / 4
+    vp = np.repeat(vp1[None, :], NX + 2, axis=0)
+    vs = vp / np.sqrt(3) * (1 + 0.05 * (2 * rng.random(vp.shape) - 1))
+    rho = 310.0 * vp ** 0.25
+    lam, mu, rho = ads.compute_properties(vp, vs, rho)
+    p = ads.ElasticPropagatorParams(NX=NX, NY=NY, NSTEP=T, DELTAX=h, DELTAY=h, DELTAT=dt,
+                                    NPOINTS_PML=npml, vp_ref=float(vp.mean()), f0=fpeak)
+    wav = ads.Ricker(p, ads.ricker_width_samples(fpeak, dt), 1.5 / fpeak / dt, 1e6)
+    xr = np.round(np.linspace(npml + 2, NX - npml, 300)).astype(np.int64)
+    shots = []
+    for s in range(nshots):
+        si = int(round(npml + 2 + (s + 0.5) * (NX - 2 * npml - 2) / nshots))
+        shots.append(dict(srci=[si, si], srcj=[npml + 11] * 2, srctype=[2, 3],
+                          srcv=np.repeat(wav[:, None], 2, axis=1),
+                          rcvi=np.concatenate([xr, xr]), rcvj=np.full(600, npml + 6),
+                          rcvtype=np.array([0] * 300 + [1] * 300)))
+    return p, shots, lam, mu, rho
+
+
+def run_elastic_fwi(args):
+    """Elastic CPML FWI gradient w.r.t. lambda, mu, rho: 600x300 incl. CPML 30,
+    4000 steps, FP32 stencils with FP64 accumulation, 32 explosive shots (sigma_xx
+    and sigma_yy, 10 Hz Ricker), 300 two-component receivers."""
+    import torch
+    import __graft_entry__ as g
+
+    ads = g.load_package()
+    p, shots, lam, mu, rho = elastic_workload(ads, nshots=args.shots if args.shots != 64 else 32,
+                                              T=args.nstep if args.nstep != 3000 else 4000)
+    t = lambda a: torch.tensor(a.reshape(-1), device="cuda")
+    plan = ads.ElasticPlan(p, shots, precision="f32", ckpt_every=100)
+    obs = plan.forward(t(lam), t(mu), t(rho)).clone()
+    sm = lambda a: t(ads.gaussian_smooth(a, 10.0))
+    l0, m0, r0 = sm(lam), sm(mu), sm(rho)
+    ms = _timed(lambda: plan.gradient(l0, m0, r0, obs), args.steps, args.warmup)
+    n = len(shots)
+    cells = 2 * n * p.NX * p.NY * p.NSTEP
+    _line("elastic FWI shot-gradients/s (FP32 stencils, FP64 accumulation)", n / (ms / 1e3),
+          "shot-gradients/s", args, ms, "f32",
+          f"elastic CPML gradient {p.NX}x{p.NY} (CPML {p.NPOINTS_PML}), {p.NSTEP} steps, "
+          f"{n} explosive shots x 300 two-component receivers",
+          {"gcell_updates_per_s": cells / (ms / 1e3) / 1e9,
+           "device_bytes": plan.device_bytes, "gpu_launches": int(plan.launches_gradient)})
+    plan.close()
+
+
+def run_fwi_uneven(args):
+    """Uneven batched acoustic FWI gradient: 4000 x 2000 model, 128 shots, each with
+    its own window of 400-1200 columns (PML 40 inside), 200-1200 receivers and
+    2000-6000 steps drawn from the seed; FP32 stencils, FP64 accumulation."""
+    import torch
+    import __graft_entry__ as g
+
+    ads = g.load_package()
+    MX, MY, npml, h, dt = 4000, 2000, 40, 10.0, 0.8e-3
+    rng = np.random.default_rng(2025)
+    vt = ads.folded_layer_model(MX + 2, MY + 2, 1500.0, 4500.0, seed=2025)
+    ii, jj = np.meshgrid(np.arange(MX + 2), np.arange(MY + 2), indexing="ij")
+    for _ in range(6):
+        ci, cj = rng.uniform(0, MX), rng.uniform(0.2 * MY, MY)
+        vt *= 1 + rng.uniform(-0.1, 0.1) * np.exp(-((ii - ci) ** 2 + (jj - cj) ** 2) / (2 * 60.0 ** 2))
+    v0 = ads.gaussian_smooth(vt, 40.0)
+    nshots = args.shots if args.shots != 64 else 128
+    shots = []
+    for s in range(nshots):
+        W = int(rng.integers(400, 1201))
+        x0 = int(rng.integers(0, MX - W + 1))
+        T = int(rng.integers(2000, 6001))
+        R = min(int(rng.integers(200, 1201)), W - 2 * npml)
+        p = ads.AcousticPropagatorParams(NX=W, NY=MY, NSTEP=T, DELTAT=dt)
+        wav = ads.Ricker(p, ads.ricker_width_samples(15.0, dt), 1.5 / 15.0 / dt, 1e6)
+        shots.append(dict(x0=x0, nx=W, nstep=T, srci=[int(rng.integers(npml + 2, W - npml))],
+                          srcj=[npml + 11], srcv=wav[:, None],
+                          rcvi=np.round(np.linspace(npml + 2, W - npml, R)).astype(np.int64),
+                          rcvj=np.full(R, npml + 6)))
+    plan = ads.AcousticPlan(MX, MY, h, h, dt, shots, npml=npml, vp_ref=float(vt.mean()),
+                            precision="f32", ckpt_every=100)
+    obs = plan.forward(torch.tensor(vt, device="cuda")).clone()
+    vdev = torch.tensor(v0, device="cuda")
+    ms = _timed(lambda: plan.gradient(vdev, obs), args.steps, args.warmup)
+    cells = 2 * sum(s["nx"] * MY * (s["nstep"] - 1) for s in shots)
+    _line("FWI shot-gradients/s & Gcell-updates/s, FP32-batched uneven shots",
+          nshots / (ms / 1e3), "shot-gradients/s", args, ms, "f32",
+          "uneven acoustic FWI gradient on a 4000x2000 model, 128 shots, windows 400-1200, "
+          "200-1200 receivers, 2000-6000 steps, PML 40 per window",
+          {"gcell_updates_per_s": cells / (ms / 1e3) / 1e9, "device_bytes": plan.device_bytes,
+           "gpu_launches": int(plan.launches_gradient)})
+    plan.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="fwi-batched",
+                    choices=["fwi-batched", "acoustic-fwd-f64", "fwi-f64", "elastic-fwi",
+                             "fwi-uneven"])
     ap.add_argument("--shots", type=int, default=64)
     ap.add_argument("--nstep", type=int, default=3000)
     ap.add_argument("--no-cpu", action="store_true")
@@ -220,6 +423,10 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    other = {"acoustic-fwd-f64": run_acoustic_fwd_f64, "fwi-f64": run_fwi_f64,
+             "elastic-fwi": run_elastic_fwi, "fwi-uneven": run_fwi_uneven}
+    if args.workload in other:
+        return other[args.workload](args) or 0
 
     import torch
 
