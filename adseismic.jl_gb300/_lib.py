@@ -40,7 +40,7 @@ class AcousticConfig(C.Structure):
         ("use_pml", C.c_int32), ("precision", C.c_int32), ("variant", C.c_int32),
         ("use_graph", C.c_int32), ("ckpt_every", C.c_int64),
         ("rows_per_thread", C.c_int32), ("steps_per_block", C.c_int32),
-        ("block_rows", C.c_int32), ("reserved", C.c_int32 * 5),
+        ("block_rows", C.c_int32), ("autotune", C.c_int32), ("reserved", C.c_int32 * 4),
     ]
 
 

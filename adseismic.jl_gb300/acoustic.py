@@ -156,7 +156,8 @@ class AcousticPlan:
 
     def __init__(self, MX, MY, dx, dy, dt, shots, npml=12, Rcoef=0.001, vp_ref=1000.0,
                  use_pml=15, precision="f64", use_graph=True, ckpt_every=0,
-                 rows_per_thread=0, steps_per_block=0, block_rows=0, stream=None):
+                 rows_per_thread=0, steps_per_block=0, block_rows=0, autotune=False,
+                 stream=None):
         cfg = _lib.AcousticConfig()
         cfg.MX, cfg.MY, cfg.dx, cfg.dy, cfg.dt = MX, MY, dx, dy, dt
         cfg.npml, cfg.Rcoef, cfg.vp_ref, cfg.use_pml = npml, Rcoef, vp_ref, use_pml
@@ -167,6 +168,7 @@ class AcousticPlan:
         cfg.rows_per_thread = rows_per_thread
         cfg.steps_per_block = steps_per_block
         cfg.block_rows = block_rows
+        cfg.autotune = int(bool(autotune))
         self.MX, self.MY = MX, MY
         self.precision = precision
         self.dtype = torch.float64 if precision == "f64" else torch.float32

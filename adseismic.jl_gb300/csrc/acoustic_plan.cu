@@ -847,7 +847,23 @@ struct AcPlan final : AcPlanBase {
   int nseg_max = 0;
   std::vector<int> order;         // shot order (record length descending)
   std::vector<int> nstep;         // per sorted shot
-  std::vector<int> item_shot_end; // per sorted shot: items of shots [0..s] = [0, end)
+  std::vector<int> nxs;           // per sorted shot: window width
+  std::vector<int> item_shot_end; // per sorted shot: adjoint tiles of shots [0..s]
+  std::vector<int> itemf_shot_end; // per sorted shot: forward tiles of shots [0..s]
+  int ri_f = 8;                    // rows per thread of the forward tiles
+  AcItem* d_items_f = nullptr;
+  CellRef *d_srcs_f = nullptr, *d_rcvs_f = nullptr;
+  // per sorted shot, 0-based (i, j, index) of interior sources / receivers
+  std::vector<std::vector<int3>> hsrc, hrcv;
+  struct TileList {
+    std::vector<AcItem> items;
+    std::vector<CellRef> srcs, rcvs;
+    std::vector<int> shot_end;
+  };
+  void build_tiles(int rows, int64_t pitch, TileList& L) const;
+  int upload_tiles(const TileList& L, AcItem* di, CellRef* ds, CellRef* dr, cudaStream_t st);
+  int autotune(cudaStream_t st, int64_t pitch, size_t cap_items);
+  int itemsf_upto(int n) const { return n <= 0 ? 0 : itemf_shot_end[n - 1]; }
   std::vector<int> rcv_b_host, rcv_e_host;
   AcConst<T> kc{};
   // device
@@ -978,6 +994,8 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int b) { return shots[a].nstep > shots[b].nstep; });
   nstep.resize(ns);
+  nxs.resize(ns);
+  for (int s = 0; s < ns; s++) nxs[s] = (int)shots[order[s]].nx;
   int max_nstep = 0;
   for (int s = 0; s < ns; s++) {
     nstep[s] = (int)shots[order[s]].nstep;
@@ -1066,49 +1084,48 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   }
   const size_t resid_off = L.take(sizeof(T) * std::max<int64_t>(trace_total, 1));
   const size_t partial_off = L.take(sizeof(double) * kMisfitBlocks);
-  // items, sources, receivers
-  std::vector<AcItem> items;
-  std::vector<CellRef> srcs, rcvs, shot_rcvs;
-  item_shot_end.resize(ns);
+  // interior sources / receivers per sorted shot, and each shot's receiver list
+  std::vector<CellRef> shot_rcvs;
   rcv_b_host.resize(ns);
   rcv_e_host.resize(ns);
+  hsrc.assign(ns, {});
+  hrcv.assign(ns, {});
   for (int s = 0; s < ns; s++) {
     const ads_acoustic_shot& h = shots[order[s]];
     const int nx = (int)h.nx, ny = (int)MY;
+    for (int64_t k = 0; k < h.nsrc; k++)
+      hsrc[s].push_back(make_int3((int)h.srci[k] - 1, (int)h.srcj[k] - 1, (int)k));
     rcv_b_host[s] = (int)shot_rcvs.size();
     for (int64_t r = 0; r < h.nrcv; r++) {
-      const int64_t i = h.rcvi[r] - 1, j = h.rcvj[r] - 1;
+      const int i = (int)h.rcvi[r] - 1, j = (int)h.rcvj[r] - 1;
       if (i < 1 || i > nx || j < 1 || j > ny) continue;  // frame: trace stays 0
-      shot_rcvs.push_back({i * pitch + j + JOFF, (int)r, 0});
+      hrcv[s].push_back(make_int3(i, j, (int)r));
+      shot_rcvs.push_back({(int64_t)i * pitch + j + JOFF, (int)r, 0});
     }
     rcv_e_host[s] = (int)shot_rcvs.size();
-    for (int i0 = 1; i0 <= nx; i0 += ri) {
-      for (int j0 = 1; j0 <= ny; j0 += Tile<T>::J) {
-        AcItem it{};
-        it.shot = s;
-        it.i0 = i0;
-        it.j0 = j0;
-        it.src_b = (int)srcs.size();
-        for (int64_t k = 0; k < h.nsrc; k++) {
-          const int64_t i = h.srci[k] - 1, j = h.srcj[k] - 1;
-          if (i >= i0 && i < i0 + ri && j >= j0 && j < j0 + Tile<T>::J)
-            srcs.push_back({i * pitch + j + JOFF, (int)k, 0});
-        }
-        it.src_e = (int)srcs.size();
-        it.rcv_b = (int)rcvs.size();
-        for (int64_t r = 0; r < h.nrcv; r++) {
-          const int64_t i = h.rcvi[r] - 1, j = h.rcvj[r] - 1;
-          if (i >= i0 && i < i0 + ri && i <= nx && j >= j0 && j < j0 + Tile<T>::J && j <= ny &&
-              j >= 1)
-            rcvs.push_back({i * pitch + j + JOFF, (int)r, 0});
-        }
-        it.rcv_e = (int)rcvs.size();
-        items.push_back(it);
-      }
-    }
-    item_shot_end[s] = (int)items.size();
   }
-  nitems = (int)items.size();
+  // forward and adjoint tiles (rows per thread chosen separately; the
+  // autotuner may replace both once the plan's buffers exist)
+  if (c.rows_per_thread <= 0) {
+    ri_f = 8;
+    while (ri_f > 2 && cells / ((int64_t)ri_f * Tile<T>::J) < 152 * 8) ri_f /= 2;
+    ri = 32;
+    while (ri > 2 && cells / ((int64_t)ri * Tile<T>::J) < 152 * 4) ri /= 2;
+  } else {
+    ri_f = ri;
+  }
+  TileList tiles_a, tiles_f;
+  build_tiles(ri, pitch, tiles_a);
+  build_tiles(ri_f, pitch, tiles_f);
+  // capacity: the autotuner tries rows down to 2 per thread
+  size_t cap_items = std::max(tiles_a.items.size(), tiles_f.items.size());
+  if (c.autotune) {
+    size_t n2 = 0;
+    for (int s = 0; s < ns; s++)
+      n2 += (size_t)div_up(shots[order[s]].nx, 2) * (size_t)div_up(MY, Tile<T>::J);
+    cap_items = std::max(cap_items, n2);
+  }
+  nitems = (int)tiles_a.items.size();
   // time-blocked tiles: output columns [jo, jo + W), rows [i0, i0 + RB); sources
   // of the loaded region (halo KB); receiver maps of the output region
   std::vector<TbItem> tb_items;
@@ -1176,9 +1193,12 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   const size_t tbm_off = L.take(sizeof(int) * std::max<size_t>(tb_map.size(), 1));
   const size_t rnx_off = L.take(sizeof(int) * std::max<size_t>(rcv_next_all.size(), 1));
   const size_t shots_off = L.take(sizeof(AcShot<T>) * ns);
-  const size_t items_off = L.take(sizeof(AcItem) * items.size());
-  const size_t srcs_off = L.take(sizeof(CellRef) * std::max<size_t>(srcs.size(), 1));
-  const size_t rcvs_off = L.take(sizeof(CellRef) * std::max<size_t>(rcvs.size(), 1));
+  const size_t items_off = L.take(sizeof(AcItem) * cap_items);
+  const size_t srcs_off = L.take(sizeof(CellRef) * std::max<size_t>(tiles_a.srcs.size(), 1));
+  const size_t rcvs_off = L.take(sizeof(CellRef) * std::max<size_t>(tiles_a.rcvs.size(), 1));
+  const size_t itemsf_off = L.take(sizeof(AcItem) * cap_items);
+  const size_t srcsf_off = L.take(sizeof(CellRef) * std::max<size_t>(tiles_f.srcs.size(), 1));
+  const size_t rcvsf_off = L.take(sizeof(CellRef) * std::max<size_t>(tiles_f.rcvs.size(), 1));
   const size_t shot_rcvs_off = L.take(sizeof(CellRef) * std::max<size_t>(shot_rcvs.size(), 1));
   const size_t rcvb_off = L.take(sizeof(int) * ns);
   const size_t rcve_off = L.take(sizeof(int) * ns);
@@ -1205,6 +1225,9 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   d_items = (AcItem*)(pool + items_off);
   d_srcs = (CellRef*)(pool + srcs_off);
   d_rcvs = (CellRef*)(pool + rcvs_off);
+  d_items_f = (AcItem*)(pool + itemsf_off);
+  d_srcs_f = (CellRef*)(pool + srcsf_off);
+  d_rcvs_f = (CellRef*)(pool + rcvsf_off);
   d_shot_rcvs = (CellRef*)(pool + shot_rcvs_off);
   d_rcv_b = (int*)(pool + rcvb_off);
   d_rcv_e = (int*)(pool + rcve_off);
@@ -1271,14 +1294,10 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   }
   ADS_CUDA(cudaMemcpyAsync(d_shots, hshots.data(), sizeof(AcShot<T>) * ns,
                            cudaMemcpyHostToDevice, st));
-  ADS_CUDA(cudaMemcpyAsync(d_items, items.data(), sizeof(AcItem) * items.size(),
-                           cudaMemcpyHostToDevice, st));
-  if (!srcs.empty())
-    ADS_CUDA(cudaMemcpyAsync(d_srcs, srcs.data(), sizeof(CellRef) * srcs.size(),
-                             cudaMemcpyHostToDevice, st));
-  if (!rcvs.empty())
-    ADS_CUDA(cudaMemcpyAsync(d_rcvs, rcvs.data(), sizeof(CellRef) * rcvs.size(),
-                             cudaMemcpyHostToDevice, st));
+  if (int e = upload_tiles(tiles_a, d_items, d_srcs, d_rcvs, st)) return e;
+  item_shot_end = tiles_a.shot_end;
+  if (int e = upload_tiles(tiles_f, d_items_f, d_srcs_f, d_rcvs_f, st)) return e;
+  itemf_shot_end = tiles_f.shot_end;
   if (!shot_rcvs.empty())
     ADS_CUDA(cudaMemcpyAsync(d_shot_rcvs, shot_rcvs.data(), sizeof(CellRef) * shot_rcvs.size(),
                              cudaMemcpyHostToDevice, st));
@@ -1297,6 +1316,9 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   if (int e = up(pool + rnx_off, rcv_next_all.data(), sizeof(int) * rcv_next_all.size()))
     return e;
   ADS_CUDA(cudaStreamSynchronize(st));  // host staging buffers go out of scope
+  // ---- autotuner: time candidate tilings on the plan's own buffers
+  if (c.autotune)
+    if (int e = autotune(st, pitch, cap_items)) return e;
   // ---- timing ranges: the first full-length segment the reverse sweep meets
   cells_prefix.resize(ns);
   for (int s = 0; s < ns; s++)
@@ -1345,6 +1367,143 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
 
 // Forward time loop (zero the rings and traces, then one launch per step).
 // count != nullptr: only count kernel launches.
+// Tiles of `rows` rows x Tile::J columns over every sorted shot, with the
+// sources and receivers of each tile (bucketed once per shot).
+template <typename T>
+void AcPlan<T>::build_tiles(int rows, int64_t pitch, TileList& L) const {
+  L.items.clear();
+  L.srcs.clear();
+  L.rcvs.clear();
+  L.shot_end.assign(nshots, 0);
+  const int ny = (int)cfg.MY, J = Tile<T>::J;
+  for (int s = 0; s < nshots; s++) {
+    const int nx = nxs[s];
+    const int nti = (int)div_up(nx, rows), ntj = (int)div_up(ny, J);
+    std::vector<std::vector<int>> bs((size_t)nti * ntj), br((size_t)nti * ntj);
+    for (size_t k = 0; k < hsrc[s].size(); k++) {
+      const int3 q = hsrc[s][k];
+      bs[(size_t)((q.x - 1) / rows) * ntj + (q.y - 1) / J].push_back((int)k);
+    }
+    for (size_t k = 0; k < hrcv[s].size(); k++) {
+      const int3 q = hrcv[s][k];
+      br[(size_t)((q.x - 1) / rows) * ntj + (q.y - 1) / J].push_back((int)k);
+    }
+    for (int ti = 0; ti < nti; ti++)
+      for (int tj = 0; tj < ntj; tj++) {
+        AcItem it{};
+        it.shot = s;
+        it.i0 = 1 + ti * rows;
+        it.j0 = 1 + tj * J;
+        const size_t b = (size_t)ti * ntj + tj;
+        it.src_b = (int)L.srcs.size();
+        for (int k : bs[b]) {
+          const int3 q = hsrc[s][k];
+          L.srcs.push_back({(int64_t)q.x * pitch + q.y + JOFF, q.z, 0});
+        }
+        it.src_e = (int)L.srcs.size();
+        it.rcv_b = (int)L.rcvs.size();
+        for (int k : br[b]) {
+          const int3 q = hrcv[s][k];
+          L.rcvs.push_back({(int64_t)q.x * pitch + q.y + JOFF, q.z, 0});
+        }
+        it.rcv_e = (int)L.rcvs.size();
+        L.items.push_back(it);
+      }
+    L.shot_end[s] = (int)L.items.size();
+  }
+}
+
+template <typename T>
+int AcPlan<T>::upload_tiles(const TileList& L, AcItem* di, CellRef* ds, CellRef* dr,
+                            cudaStream_t st) {
+  if (!L.items.empty())
+    ADS_CUDA(cudaMemcpyAsync(di, L.items.data(), sizeof(AcItem) * L.items.size(),
+                             cudaMemcpyHostToDevice, st));
+  if (!L.srcs.empty())
+    ADS_CUDA(cudaMemcpyAsync(ds, L.srcs.data(), sizeof(CellRef) * L.srcs.size(),
+                             cudaMemcpyHostToDevice, st));
+  if (!L.rcvs.empty())
+    ADS_CUDA(cudaMemcpyAsync(dr, L.rcvs.data(), sizeof(CellRef) * L.rcvs.size(),
+                             cudaMemcpyHostToDevice, st));
+  return ADS_OK;
+}
+
+// Autotuner: for each candidate tile height, time a few forward steps and a
+// few adjoint steps of the real kernels on the plan's buffers (CUDA events on
+// `st`) and keep the fastest height for each kernel.  The buffers the trials
+// touch are reset by every forward / gradient call.
+template <typename T>
+int AcPlan<T>::autotune(cudaStream_t st, int64_t pitch, size_t cap) {
+  const int cand[] = {2, 4, 8, 16, 32, 64};
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  ADS_CUDA(cudaEventCreate(&e0));
+  ADS_CUDA(cudaEventCreate(&e1));
+  const int tf_end = std::min(7, nstep[0]);
+  const int ka_end = std::min(std::min(7, K + 1), nstep[0]);
+  float best_f = 1e30f, best_a = 1e30f;
+  int bf = ri_f, ba = ri;
+  int rc = ADS_OK;
+  for (int rows : cand) {
+    TileList L;
+    build_tiles(rows, pitch, L);
+    if (L.items.size() > cap) continue;
+    if ((rc = upload_tiles(L, d_items_f, d_srcs_f, d_rcvs_f, st))) break;
+    if ((rc = upload_tiles(L, d_items, d_srcs, d_rcvs, st))) break;
+    float ms_f = 0.f, ms_a = 0.f;
+    for (int pass = 0; pass < 2 && rc == ADS_OK; pass++) {  // pass 0 warms up
+      if (cudaEventRecord(e0, st) != cudaSuccess) rc = ADS_ERR_CUDA;
+      for (int t = 2; t <= tf_end; t++) {
+        const int nit = L.shot_end[shots_with_nstep_ge(t) - 1];
+        k_ac_fwd<T, false><<<nit, Tile<T>::NF, 0, st>>>(d_items_f, d_shots, d_srcs_f, d_rcvs_f,
+                                                        kc, t, 0, 0, rows);
+      }
+      cudaEventRecord(e1, st);
+      cudaEvent_t e2 = e0;  // reused to time the adjoint range after the forward one
+      if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+        rc = fail(ADS_ERR_CUDA, "autotuner trial failed");
+        break;
+      }
+      cudaEventElapsedTime(&ms_f, e0, e1);
+      cudaEventRecord(e2, st);
+      for (int k = 2; k <= ka_end; k++) {
+        const int nit = L.shot_end[shots_with_nstep_ge(k) - 1];
+        k_ac_adj<T><<<nit, Tile<T>::NA, 0, st>>>(d_items, d_shots, d_rcvs, kc, k, 0, rows);
+      }
+      cudaEventRecord(e1, st);
+      if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+        rc = fail(ADS_ERR_CUDA, "autotuner trial failed");
+        break;
+      }
+      cudaEventElapsedTime(&ms_a, e2, e1);
+    }
+    if (rc != ADS_OK) break;
+    note_launches(2 * (tf_end - 1) + 2 * (ka_end - 1));
+    if (ms_f < best_f) {
+      best_f = ms_f;
+      bf = rows;
+    }
+    if (ms_a < best_a) {
+      best_a = ms_a;
+      ba = rows;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != ADS_OK) return rc;
+  ri_f = bf;
+  ri = ba;
+  TileList Lf, La;
+  build_tiles(ri_f, pitch, Lf);
+  build_tiles(ri, pitch, La);
+  if (int e = upload_tiles(Lf, d_items_f, d_srcs_f, d_rcvs_f, st)) return e;
+  if (int e = upload_tiles(La, d_items, d_srcs, d_rcvs, st)) return e;
+  itemf_shot_end = Lf.shot_end;
+  item_shot_end = La.shot_end;
+  nitems = (int)La.items.size();
+  ADS_CUDA(cudaStreamSynchronize(st));
+  return ADS_OK;
+}
+
 template <typename T>
 int AcPlan<T>::launch_tb(cudaStream_t st, bool seg, int nit, int t0, int NS, int base,
                          int in_set, int ck) {
@@ -1400,8 +1559,8 @@ int AcPlan<T>::issue_forward(cudaStream_t st, int64_t* count) {
     } else if (KB > 1) {
       if (int e = launch_tb(st, false, tb_items_upto(na), t0, NS, 0, blk & 1, ck)) return e;
     } else {
-      k_ac_fwd<T, false><<<items_upto(na), Tile<T>::NF, 0, st>>>(d_items, d_shots, d_srcs,
-                                                                d_rcvs, kc, t0, 0, ck, ri);
+      k_ac_fwd<T, false><<<itemsf_upto(na), Tile<T>::NF, 0, st>>>(
+          d_items_f, d_shots, d_srcs_f, d_rcvs_f, kc, t0, 0, ck, ri_f);
       ADS_LAUNCHED(1);
     }
     t0 = t1 + 1;
@@ -1449,8 +1608,8 @@ int AcPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
         if (KB > 1) {
           if (int e = launch_tb(st, true, tb_items_upto(nt), t0, NS, a - 2, blk & 1, 0)) return e;
         } else {
-          k_ac_fwd<T, true><<<items_upto(nt), Tile<T>::NF, 0, st>>>(d_items, d_shots, d_srcs,
-                                                                   d_rcvs, kc, t0, a - 2, 0, ri);
+          k_ac_fwd<T, true><<<itemsf_upto(nt), Tile<T>::NF, 0, st>>>(
+              d_items_f, d_shots, d_srcs_f, d_rcvs_f, kc, t0, a - 2, 0, ri_f);
           ADS_LAUNCHED(1);
         }
       }

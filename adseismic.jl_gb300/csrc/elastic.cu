@@ -61,6 +61,19 @@ struct ElShot {
   int64_t fs;                   // elements per field
 };
 
+// The plans pass their shot table (one shot per blockIdx.z, FULL = false);
+// the single-step operators pass their one shot by value (FULL = true).  The
+// choice is made at compile time so no generic pointer or struct copy arises.
+template <typename T, bool FULL>
+__device__ __forceinline__ const ElShot<T>& shot_of(const ElShot<T>* shots,
+                                                    const ElShot<T>& one) {
+  if constexpr (FULL) {
+    return one;
+  } else {
+    return shots[blockIdx.z];
+  }
+}
+
 template <typename T>
 __device__ __forceinline__ T d4(T a0, T am1, T ap1, T am2, T h24) {
   return (T(27) * a0 - T(27) * am1 - ap1 + am2) / h24;
@@ -78,7 +91,7 @@ __device__ __forceinline__ bool active(const T* a, const T* b, int k) {
 template <typename T, bool FULL, bool STORE>
 __global__ void __launch_bounds__(BX* BY)
 k_el_stress(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
-  const ElShot<T>& sh = shots ? shots[blockIdx.z] : one;
+  const ElShot<T>& sh = shot_of<T, FULL>(shots, one);
   const int j = blockIdx.x * BX + threadIdx.x;
   const int i = blockIdx.y * BY + threadIdx.y;
   const int NX = M.NX, NY = M.NY;
@@ -150,7 +163,7 @@ k_el_stress(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot)
 template <typename T, bool FULL, bool STORE>
 __global__ void __launch_bounds__(BX* BY)
 k_el_velocity(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
-  const ElShot<T>& sh = shots ? shots[blockIdx.z] : one;
+  const ElShot<T>& sh = shot_of<T, FULL>(shots, one);
   const int j = blockIdx.x * BX + threadIdx.x;
   const int i = blockIdx.y * BY + threadIdx.y;
   const int NX = M.NX, NY = M.NY;
@@ -216,7 +229,7 @@ k_el_velocity(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slo
 template <typename T, bool FULL>
 __global__ void __launch_bounds__(BX* BY)
 k_el_adj1(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
-  const ElShot<T>& sh = shots ? shots[blockIdx.z] : one;
+  const ElShot<T>& sh = shot_of<T, FULL>(shots, one);
   const int j = blockIdx.x * BX + threadIdx.x;
   const int i = blockIdx.y * BY + threadIdx.y;
   const int NX = M.NX, NY = M.NY;
@@ -277,7 +290,7 @@ __device__ __forceinline__ T tld(const T* a, const ElModel<T>& M, int i, int j) 
 template <typename T, bool FULL>
 __global__ void __launch_bounds__(BX* BY)
 k_el_adj2(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
-  const ElShot<T>& sh = shots ? shots[blockIdx.z] : one;
+  const ElShot<T>& sh = shot_of<T, FULL>(shots, one);
   const int j = blockIdx.x * BX + threadIdx.x;
   const int i = blockIdx.y * BY + threadIdx.y;
   const int NX = M.NX, NY = M.NY;
@@ -351,7 +364,7 @@ k_el_adj2(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
 template <typename T, bool FULL>
 __global__ void __launch_bounds__(BX* BY)
 k_el_adj3(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one) {
-  const ElShot<T>& sh = shots ? shots[blockIdx.z] : one;
+  const ElShot<T>& sh = shot_of<T, FULL>(shots, one);
   const int j = blockIdx.x * BX + threadIdx.x;
   const int i = blockIdx.y * BY + threadIdx.y;
   const int NX = M.NX, NY = M.NY;

@@ -448,7 +448,7 @@ def main():
                                                  npml=cfg["npml"], vp_ref=cfg["vp_ref"],
                                                  precision=prec, ckpt_every=100, **kw)
     t_setup = time.perf_counter()
-    plan = mk("f32", shots)
+    plan = mk("f32", shots, autotune=True)
     vt = torch.tensor(vp_true, device=dev)
     v0 = torch.tensor(vp0, device=dev)
     obs = plan.forward(vt).clone()

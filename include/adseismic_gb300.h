@@ -240,7 +240,9 @@ typedef struct ads_acoustic_config {
   int32_t steps_per_block; /* time steps per forward launch (FP32: 1, 2, 4, 8;
                               FP64: 1); 0 = automatic (1) */
   int32_t block_rows;      /* tile height of the time-blocked forward; 0 = automatic */
-  int32_t reserved[5];
+  int32_t autotune;        /* 1: time candidate tile heights of the forward and adjoint
+                              kernels at plan creation and keep the fastest */
+  int32_t reserved[4];
 } ads_acoustic_config;
 
 typedef struct ads_acoustic_shot {

@@ -225,6 +225,24 @@ def test_plan_fp32_time_blocked_vs_oracle(ads, orc, cuda, kb, rows):
     plan.close()
 
 
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_autotuned_plan_vs_oracle(ads, orc, cuda, precision):
+    MX, MY, shots, vp = uneven_case(31, nshots=5)
+    h, dt, npml, vref = 10.0, 1e-3, 5, 1500.0
+    ref_tr = oracle_multishot(orc, MX, MY, shots, vp, h, dt, npml, vref)
+    obs = [t * 0.97 for t in ref_tr]
+    ref_loss, ref_grad = oracle_multishot(orc, MX, MY, shots, vp, h, dt, npml, vref, obs)
+    plan = ads.AcousticPlan(MX, MY, h, h, dt, shots, npml=npml, vp_ref=vref, precision=precision,
+                            ckpt_every=11, autotune=True)
+    dtype = plan.dtype
+    loss, grad = plan.gradient(T(vp, cuda), plan.pack([T(o, cuda, dtype) for o in obs]))
+    torch.cuda.synchronize()
+    tol = TOL64 if precision == "f64" else TOL32
+    assert abs(float(loss) - ref_loss) <= tol * ref_loss
+    assert rel(grad.cpu().numpy(), ref_grad) <= tol
+    plan.close()
+
+
 def test_repeated_calls_are_deterministic(ads, cuda):
     MX, MY, shots, vp = uneven_case(5, nshots=3)
     plan = ads.AcousticPlan(MX, MY, 10.0, 10.0, 1e-3, shots, npml=5, precision="f32")
