@@ -313,6 +313,85 @@ def compute_loss_and_grads_GPU(param: AcousticPropagatorParams, srcs, rcvs, Rs, 
     return loss, grad
 
 
+def dropin_loss_and_grad(param: AcousticPropagatorParams, src: AcousticSource,
+                         rcv: AcousticReceiver, observed, vp):
+    """The plain FP64 operator chain of one shot, as the reference's graph runs
+    it: one C-ABI operator call per op and time step, the whole wavefield
+    history kept on the device (TensorFlow keeps every while_loop output for
+    its gradient).
+
+    Forward (src/Core.jl:600-614): AcousticOneStep, then ScatterAdd of the
+    dt^2-scaled source row; receivers by one Gather over the history
+    (SimulatedObservation!, src/Core.jl:726-730).  Loss = sum((rcvv - obs)^2)
+    (src/Utils.jl:308).  Reverse (the gradients call of src/Utils.jl:312): the
+    Gather's transpose (a ScatterAdd of the residual), then
+    AcousticOneStepGrad per step; ScatterAdd passes its input gradient
+    through.  Variant W only.  Returns (loss, grad_vp) as FP64 CUDA tensors.
+    """
+    if param.PropagatorKernel != ADS_VARIANT_W:
+        raise ValueError("the drop-in chain is written for PropagatorKernel 0")
+    dev = torch.device("cuda")
+    NX, NY, T = param.NX, param.NY, param.NSTEP
+    S, N = NY + 2, (NX + 2) * (NY + 2)
+    dt, hx, hy = param.DELTAT, param.DELTAX, param.DELTAY
+    f64 = dict(dtype=torch.float64, device=dev)
+    Sx, Sy = compute_PML_Params(param)
+    sigma = torch.as_tensor(Sx, **f64).reshape(-1).contiguous()
+    tau = torch.as_tensor(Sy, **f64).reshape(-1).contiguous()
+    vpt = torch.as_tensor(vp, **f64).reshape(-1).contiguous()
+    c = vpt * vpt
+    srci, srcj = np.asarray(src.srci, np.int64), np.asarray(src.srcj, np.int64)
+    rcvi, rcvj = np.asarray(rcv.rcvi, np.int64), np.asarray(rcv.rcvj, np.int64)
+    nsrc, nrcv = len(srci), len(rcvi)
+    sii = torch.as_tensor((srci - 1) * S + srcj, device=dev)            # 1-based cells
+    upd = torch.as_tensor(np.asarray(src.srcv, np.float64).reshape(-1, nsrc), **f64) * (dt * dt)
+    rcell = (rcvi - 1) * S + rcvj                                         # 1-based cells
+    hist_ii = torch.as_tensor((np.arange(T + 1)[:, None] * N + rcell[None, :]).reshape(-1),
+                              device=dev)
+    rii = torch.as_tensor(rcell, device=dev)
+    U = torch.zeros(T + 1, N, **f64)
+    Ph = torch.zeros(T + 1, N, **f64)
+    Qh = torch.zeros(T + 1, N, **f64)
+    st = _stream()
+    L = lib()
+    P = _ptr
+    for k in range(2, T + 1):
+        _lib.check(L.ads_acoustic_step_fwd_f64(
+            P(U[k - 1]), P(U[k - 2]), P(Ph[k - 1]), P(Qh[k - 1]), P(sigma), P(tau), P(c),
+            dt, hx, hy, NX, NY, P(U[k]), P(Ph[k]), P(Qh[k]), ADS_VARIANT_W, st))
+        if nsrc:
+            _lib.check(L.ads_scatter_add_f64(P(U[k]), P(U[k]), P(sii), P(upd[k - 1]), N,
+                                             nsrc, st))
+    rcvv = torch.empty((T + 1) * nrcv, **f64)
+    if nrcv:
+        _lib.check(L.ads_gather_f64(P(rcvv), P(U), P(hist_ii), (T + 1) * nrcv, st))
+    obs = torch.as_tensor(observed, **f64).reshape(-1)
+    resid = 2.0 * (rcvv - obs)
+    loss = torch.sum((rcvv - obs) ** 2)
+    resid = resid.reshape(T + 1, nrcv).contiguous()
+    LU = torch.zeros(3, N, **f64)        # lambdaU of slots k, k-1, k-2 (ring of 3)
+    LP = torch.zeros(2, N, **f64)
+    LQ = torch.zeros(2, N, **f64)
+    gw = torch.empty(N, **f64)
+    gcs = torch.empty(N, **f64)
+    gc = torch.zeros(N, **f64)
+    for k in range(T, 1, -1):
+        lu = LU[k % 3]
+        if nrcv:
+            _lib.check(L.ads_scatter_add_f64(P(lu), P(lu), P(rii), P(resid[k]), N, nrcv, st))
+        # slot k-2 is first reached by this step (grad_wold); slot k-1 already
+        # holds grad_wold of step k+1 and gains grad_w of this step
+        _lib.check(L.ads_acoustic_step_bwd_f64(
+            P(gw), P(LU[(k - 2) % 3]), P(LP[(k - 1) % 2]), P(LQ[(k - 1) % 2]), P(gcs),
+            P(lu), P(LP[k % 2]), P(LQ[k % 2]),
+            P(U[k - 1]), P(U[k - 2]), P(Ph[k - 1]), P(Qh[k - 1]), P(sigma), P(tau), P(c),
+            dt, hx, hy, NX, NY, P(U[k]), P(Ph[k]), P(Qh[k]), ADS_VARIANT_W, st))
+        LU[(k - 1) % 3].add_(gw)
+        gc.add_(gcs)
+    grad_vp = (gc * 2.0) * vpt
+    return loss, grad_vp.reshape(NX + 2, NY + 2)
+
+
 class AcousticMisfit(torch.autograd.Function):
     """loss = sum((traces(vp) - observed)^2) as an autograd node whose backward is
     the plan's checkpointed adjoint (the gradient TF builds in src/Utils.jl:312)."""

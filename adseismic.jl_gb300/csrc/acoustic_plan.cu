@@ -144,6 +144,33 @@ __device__ __forceinline__ bool warp_tau_free(const T* __restrict__ ty, int j, i
   return __all_sync(FULL, z);
 }
 
+// True when the warp's columns are tau-free and sigma is zero on rows
+// i0-1 .. i_end (every row a tile of rows [i0, i_end) reads): phi, psi and
+// their adjoints are then zero throughout and the interior update applies.
+template <typename T>
+__device__ __forceinline__ bool interior_rows(bool tfree, const T* __restrict__ sx, int i0,
+                                              int i_end, int lane) {
+  bool z = true;
+  for (int r = i0 - 1 + lane; r <= i_end; r += 32) z = z && sx[r] == T(0);
+  return tfree && __all_sync(FULL, z);
+}
+
+// Each warp records the receivers in its own columns after a forward step:
+// their cells were written by its lanes, so a warp barrier suffices.
+template <typename T, int C, bool SEG>
+__device__ __forceinline__ void record_traces(const AcItem& it, const AcShot<T>& sh,
+                                              const CellRef* __restrict__ rcvs, const T* out,
+                                              int t, int lane) {
+  if (SEG || it.rcv_e <= it.rcv_b) return;
+  __syncwarp();
+  const int wj0 = it.j0 + (threadIdx.x >> 5) * 32 * C;
+  for (int e = it.rcv_b + lane; e < it.rcv_e; e += 32) {
+    const CellRef r = rcvs[e];
+    const int rj = (int)(r.cell % sh.pitch) - JOFF;
+    if (rj >= wj0 && rj < wj0 + 32 * C) sh.traces[(int64_t)t * sh.nrcv + r.idx] = out[r.cell];
+  }
+}
+
 // One forward step (variant W: phi/psi from the old field).  SEG=false: rings
 // of two (u_t written over u_{t-2}), optional checkpoint write; SEG=true:
 // segment store addressed by slot t - base.  Each thread owns CF adjacent
@@ -192,6 +219,63 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   auto nz = [&](int r) { return !(tfree && sx[r] == T(0)); };  // phi/psi may be non-zero
   const int i0 = it.i0, i_end = min(i0 + ri, nx + 1);
   auto off = [&](int r) { return (int64_t)r * P + col; };
+  const bool ck_on = !SEG && ckpt_slot > 0 && ckpt_slot < sh.nseg;
+  if (interior_rows<T>(tfree, sx, i0, i_end, lane)) {
+    // Interior tile: sigma = tau = 0 on every row and column the warp reads,
+    // so phi = psi = 0 there and the step reduces to the plain wave update
+    // (the dropped terms are exact zeros).
+    V wm = ldv<T, C>(w, off(i0 - 1), jld), w0 = ldv<T, C>(w, off(i0), jld),
+      wp = ldv<T, C>(w, off(i0 + 1), jld);
+    V wo0 = ldv<T, C>(wo, off(i0), jld), c0 = ldv<T, C>(cc, off(i0), jld);
+    T hw = 0;
+    if (lane == 0 && jld) hw = w[off(i0) - 1];
+    else if (lane == 31 && hr) hw = w[off(i0) + C];
+    for (int i = i0; i < i_end; i++) {
+      const int64_t row = off(i);
+      const bool more = i + 1 < i_end;
+      V wn = ldv<T, C>(w, off(i + 2), jld && more);
+      V won = ldv<T, C>(wo, off(i + 1), jld && more);
+      V cn = ldv<T, C>(cc, off(i + 1), jld && more);
+      T hwn = 0;
+      if (more) {
+        if (lane == 0 && jld) hwn = w[row + P - 1];
+        else if (lane == 31 && hr) hwn = w[row + P + C];
+      }
+      T wL = __shfl_up_sync(FULL, w0.v[C - 1], 1), wR = __shfl_down_sync(FULL, w0.v[0], 1);
+      if (lane == 0) wL = hw;
+      else if (lane == 31) wR = hw;
+      if (jld) {
+        V vo;
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+          const T wS = c == 0 ? wL : w0.v[c - 1];
+          const T wN = c == C - 1 ? wR : w0.v[c + 1];
+          const T cv = c0.v[c];
+          T v = (T(2) - K.kxy * cv) * w0.v[c] + cv * K.cx * (wp.v[c] + wm.v[c]) +
+                cv * K.cy * (wN + wS) - wo0.v[c];
+          for (int e = it.src_b; e < it.src_e; e++) {
+            const CellRef r = srcs[e];
+            if (r.cell == row + c) v += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
+          }
+          vo.v[c] = v;
+        }
+        stv<T, C>(out, row, vo, j, ny);
+        if (ck_on) {
+          T* ck = sh.ckpt + (int64_t)ckpt_slot * 4 * fs;
+          stv<T, C>(ck, row, vo, j, ny);
+          stv<T, C>(ck + fs, row, w0, j, ny);
+        }
+      }
+      wm = w0;
+      w0 = wp;
+      wp = wn;
+      wo0 = won;
+      c0 = cn;
+      hw = hwn;
+    }
+    record_traces<T, C, SEG>(it, sh, rcvs, out, t, lane);
+    return;
+  }
   bool n0 = nz(i0);
   V wm = ldv<T, C>(w, off(i0 - 1), jld), w0 = ldv<T, C>(w, off(i0), jld),
     wp = ldv<T, C>(w, off(i0 + 1), jld);
@@ -262,7 +346,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
         stv<T, C>(pout, row, po, j, ny);
         stv<T, C>(qout, row, qo, j, ny);
       }
-      if (!SEG && ckpt_slot > 0 && ckpt_slot < sh.nseg) {
+      if (ck_on) {
         T* ck = sh.ckpt + (int64_t)ckpt_slot * 4 * fs;
         stv<T, C>(ck, row, vo, j, ny);
         stv<T, C>(ck + fs, row, w0, j, ny);
@@ -285,17 +369,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     hq = hqn;
     n0 = n1;
   }
-  if (!SEG && it.rcv_e > it.rcv_b) {
-    // each warp records the receivers in its own columns: their cells were
-    // written by its lanes, so a warp barrier suffices
-    __syncwarp();
-    const int wj0 = it.j0 + (threadIdx.x >> 5) * 32 * C;
-    for (int e = it.rcv_b + lane; e < it.rcv_e; e += 32) {
-      const CellRef r = rcvs[e];
-      const int rj = (int)(r.cell % P) - JOFF;
-      if (rj >= wj0 && rj < wj0 + 32 * C) sh.traces[(int64_t)t * sh.nrcv + r.idx] = out[r.cell];
-    }
-  }
+  record_traces<T, C, SEG>(it, sh, rcvs, out, t, lane);
 }
 
 // Restore checkpoint `slot` of every active shot into the segment store
@@ -339,6 +413,48 @@ __device__ __forceinline__ void col_terms(T gui, T gq, T c, T sg, T tj, const Ac
 template <typename T>
 __device__ __forceinline__ T inv_den(T s, const AcConst<T>& K) {
   return s != T(0) ? T(1) / (T(1) + s * K.hdt) : T(1);
+}
+
+// grad_c += g for a thread's C cells: the FP32 per-segment partial in FP32
+// plans, the FP64 accumulator in FP64 plans; one vector access when all C
+// cells are interior.
+template <typename T, int C>
+__device__ __forceinline__ void add_grad(const AcShot<T>& sh, int64_t row, const T (&g)[C], int j,
+                                         int ny) {
+  if (sizeof(T) == 4) {
+    float* gp = sh.gc32 + row;
+    if (j + C - 1 <= ny) {
+      Vec<float, C> a = *reinterpret_cast<const Vec<float, C>*>(gp);
+#pragma unroll
+      for (int c = 0; c < C; c++) a.v[c] += (float)g[c];
+      *reinterpret_cast<Vec<float, C>*>(gp) = a;
+    } else {
+#pragma unroll
+      for (int c = 0; c < C; c++)
+        if (j + c <= ny) gp[c] += (float)g[c];
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < C; c++)
+      if (j + c <= ny) sh.gc[row + c] += (double)g[c];
+  }
+}
+
+// Residuals of step k-1 go to receiver cells this warp's lanes wrote in the
+// adjoint step: a warp barrier suffices.
+template <typename T, int C>
+__device__ __forceinline__ void inject_residuals(const AcItem& it, const AcShot<T>& sh,
+                                                 const CellRef* __restrict__ rcvs, T* lun, int k,
+                                                 int lane) {
+  if (k - 1 < 2 || it.rcv_e <= it.rcv_b) return;
+  __syncwarp();
+  const int wj0 = it.j0 + (threadIdx.x >> 5) * 32 * C;
+  for (int e = it.rcv_b + lane; e < it.rcv_e; e += 32) {
+    const CellRef r = rcvs[e];
+    const int rj = (int)(r.cell % sh.pitch) - JOFF;
+    if (rj >= wj0 && rj < wj0 + 32 * C)
+      atomicAdd(lun + r.cell, sh.resid[(int64_t)(k - 1) * sh.nrcv + r.idx]);
+  }
 }
 
 // One adjoint step k (gather form of the transpose of step k):
@@ -387,6 +503,77 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   const T th = hon ? ty[j + (int)hoff] : T(0);
   auto off = [&](int r) { return (int64_t)r * P + col; };
   const int i0 = it.i0, i_end = min(i0 + ri, nx + 1);
+  if (interior_rows<T>(tfree, sx, i0, i_end, lane)) {
+    // Interior tile (1/den = 1, lambdaPhi = lambdaPsi = 0): the transpose of
+    // the plain wave update; rows i-1 (m), i (0), i+1 (1) of lambdaU_k and c.
+    V gum = ldv<T, C>(luc, off(i0 - 1), jld), cm = ldv<T, C>(cc, off(i0 - 1), jld);
+    V gu0 = ldv<T, C>(luc, off(i0), jld), c0 = ldv<T, C>(cc, off(i0), jld);
+    V gu1 = ldv<T, C>(luc, off(i0 + 1), jld), c1 = ldv<T, C>(cc, off(i0 + 1), jld);
+    V wm = ldv<T, C>(w, off(i0 - 1), jld), w0 = ldv<T, C>(w, off(i0), jld),
+      wp = ldv<T, C>(w, off(i0 + 1), jld);
+    V ln = ldv<T, C>(lun, off(i0), jld);
+    T hgu = 0, hc = 0, hw = 0;
+    if (hon) {
+      const int64_t r = off(i0) + hoff;
+      hgu = luc[r];
+      hc = cc[r];
+      hw = w[r];
+    }
+    for (int i = i0; i < i_end; i++) {
+      const int64_t row = off(i);
+      const bool more = i + 1 < i_end;
+      V gu2 = ldv<T, C>(luc, off(i + 2), jld && more);
+      V c2 = ldv<T, C>(cc, off(i + 2), jld && more);
+      V w2 = ldv<T, C>(w, off(i + 2), jld && more);
+      V lnn = ldv<T, C>(lun, off(i + 1), jld && more);
+      T hgun = 0, hcn = 0, hwn = 0;
+      if (more && hon) {
+        const int64_t r = row + P + hoff;
+        hgun = luc[r];
+        hcn = cc[r];
+        hwn = w[r];
+      }
+      // what each cell sends to its j-neighbours: c cy lambdaU
+      T Y[C];
+#pragma unroll
+      for (int c = 0; c < C; c++) Y[c] = c0.v[c] * K.cy * gu0.v[c];
+      T Yl = __shfl_up_sync(FULL, Y[C - 1], 1), Yr = __shfl_down_sync(FULL, Y[0], 1);
+      T wL = __shfl_up_sync(FULL, w0.v[C - 1], 1), wR = __shfl_down_sync(FULL, w0.v[0], 1);
+      if (lane == 0 || lane == 31) {
+        const T h = hon ? hc * K.cy * hgu : T(0);
+        if (lane == 0) {
+          Yl = h;
+          wL = hw;
+        } else {
+          Yr = h;
+          wR = hw;
+        }
+      }
+      if (jld) {
+        V nu;
+        T g[C];
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+          const T yl = c == 0 ? Yl : Y[c - 1], yr = c == C - 1 ? Yr : Y[c + 1];
+          const T wS = c == 0 ? wL : w0.v[c - 1], wN = c == C - 1 ? wR : w0.v[c + 1];
+          const T cv = c0.v[c];
+          nu.v[c] = -ln.v[c] + (T(2) - K.kxy * cv) * gu0.v[c] + cm.v[c] * K.cx * gum.v[c] +
+                    c1.v[c] * K.cx * gu1.v[c] + yl + yr;
+          g[c] = (-K.kxy * w0.v[c] + K.cx * (wp.v[c] + wm.v[c]) + K.cy * (wN + wS)) * gu0.v[c];
+        }
+        stv<T, C>(lun, row, nu, j, ny);
+        add_grad<T, C>(sh, row, g, j, ny);
+      }
+      gum = gu0; cm = c0;
+      gu0 = gu1; c0 = c1;
+      gu1 = gu2; c1 = c2;
+      wm = w0; w0 = wp; wp = w2;
+      ln = lnn;
+      hgu = hgun; hc = hcn; hw = hwn;
+    }
+    inject_residuals<T, C>(it, sh, rcvs, lun, k, lane);
+    return;
+  }
   // rows i-1 (m), i (0), i+1 (p): lambdaU_k, lambdaPhi_k, c and 1/den per cell
   V gum = ldv<T, C>(luc, off(i0 - 1), jld), gpm = ldv<T, C>(lpc, off(i0 - 1), jld && nz(i0 - 1)),
     cm = ldv<T, C>(cc, off(i0 - 1), jld);
@@ -485,14 +672,7 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
         stv<T, C>(lpo, row, np, j, ny);
         stv<T, C>(lqo, row, nq, j, ny);
       }
-#pragma unroll
-      for (int c = 0; c < C; c++) {
-        if (j + c > ny) break;
-        if (sizeof(T) == 4)
-          sh.gc32[row + c] += (float)g[c];
-        else
-          sh.gc[row + c] += (double)g[c];
-      }
+      add_grad<T, C>(sh, row, g, j, ny);
     }
     gum = gu0; gpm = gp0; cm = c0; invm = inv0; sgm = sg0;
     gu0 = gu1; gp0 = gp1; c0 = c1; inv0 = invp; sg0 = sgp;
@@ -502,17 +682,7 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     hgu = hgun; hgq = hgqn; hc = hcn; hw = hwn;
     n0 = n1;
   }
-  if (k - 1 >= 2 && it.rcv_e > it.rcv_b) {
-    // residuals go to cells this warp's lanes wrote: a warp barrier suffices
-    __syncwarp();
-    const int wj0 = it.j0 + (threadIdx.x >> 5) * 32 * C;
-    for (int e = it.rcv_b + lane; e < it.rcv_e; e += 32) {
-      const CellRef r = rcvs[e];
-      const int rj = (int)(r.cell % P) - JOFF;
-      if (rj >= wj0 && rj < wj0 + 32 * C)
-        atomicAdd(lun + r.cell, sh.resid[(int64_t)(k - 1) * sh.nrcv + r.idx]);
-    }
-  }
+  inject_residuals<T, C>(it, sh, rcvs, lun, k, lane);
 }
 
 // ---------------------------------------------------------------------------

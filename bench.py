@@ -560,11 +560,34 @@ def main():
         ms64 = a.elapsed_time(b) / reps
         t64 = p64.profile(v0, o64)
         fwd64 = t64["forward"]
-        fp64 = {"value": 1e3 / ms64, "unit": UNIT, "ms_per_shot_gradient": ms64,
-                "gcell_updates_per_s": 2 * shots[0]["nx"] * MY * (nstep - 1) / (ms64 / 1e3) / 1e9,
-                "k_ac_fwd_f64_gbs": BYTES[("fwd", "f64")] * fwd64[2] / (fwd64[0] / 1e3) / 1e9,
-                "fp32_batched_over_fp64_plain": value / world / (1e3 / ms64)}
+        plan64 = {"value": 1e3 / ms64, "unit": UNIT, "ms_per_shot_gradient": ms64,
+                  "gcell_updates_per_s": 2 * shots[0]["nx"] * MY * (nstep - 1) / (ms64 / 1e3) / 1e9,
+                  "k_ac_fwd_f64_gbs": BYTES[("fwd", "f64")] * fwd64[2] / (fwd64[0] / 1e3) / 1e9,
+                  "fp32_batched_over_this": value / world / (1e3 / ms64)}
         p64.close()
+        # the plain FP64 drop-in: the reference's operator chain, one C-ABI call
+        # per operator and step, full history on the device, one shot
+        s0 = shots[0]
+        prm = ads.AcousticPropagatorParams(NX=MX, NY=MY, NSTEP=nstep, DELTAX=cfg["h"],
+                                           DELTAY=cfg["h"], DELTAT=cfg["dt"],
+                                           NPOINTS_PML=cfg["npml"], vp_ref=cfg["vp_ref"])
+        src = ads.AcousticSource(np.asarray(s0["srci"]), np.asarray(s0["srcj"]),
+                                 np.asarray(s0["srcv"]))
+        rcv = ads.AcousticReceiver(s0["rcvi"], s0["rcvj"])
+        ads.dropin_loss_and_grad(prm, src, rcv, o64, vp0)
+        torch.cuda.synchronize()
+        a.record(stream)
+        ads.dropin_loss_and_grad(prm, src, rcv, o64, vp0)
+        b.record(stream)
+        torch.cuda.synchronize()
+        msd = a.elapsed_time(b)
+        fp64 = {"value": 1e3 / msd, "unit": UNIT, "ms_per_shot_gradient": msd,
+                "path": "FP64 drop-in operator chain (step, ScatterAdd, Gather and their "
+                        "gradients per time step, full history), one shot",
+                "gcell_updates_per_s": 2 * s0["nx"] * MY * (nstep - 1) / (msd / 1e3) / 1e9,
+                "fp32_batched_over_fp64_plain": value / world / (1e3 / msd),
+                "fp64_plan_one_shot": plan64}
+        torch.cuda.empty_cache()
 
     cpu = None
     if not args.no_cpu and rank == 0:

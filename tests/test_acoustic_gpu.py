@@ -281,3 +281,19 @@ def test_julia_style_api(ads, orc, cuda):
     assert rel(rcv.rcvv.cpu().numpy(), g["rcvv"]) <= TOL64
     loss, grad = ads.compute_loss_and_grads_GPU(p, [src], [rcv], [g["obs"]], g["vp"])
     assert rel(grad.cpu().numpy().reshape(-1), g["grad_vp"]) <= TOL64
+
+
+def test_dropin_operator_chain_matches_reference_golden(ads, cuda):
+    """The per-step FP64 operator chain (step, ScatterAdd, Gather and their
+    gradients, full history) reproduces the reference loss and gradient."""
+    g = golden("acoustic_loop.npz")
+    NX, NY, Tn = int(g["NX"]), int(g["NY"]), int(g["NSTEP"])
+    p = ads.AcousticPropagatorParams(NX=NX, NY=NY, NSTEP=Tn, DELTAX=float(g["h"]),
+                                     DELTAY=float(g["h"]), DELTAT=float(g["dt"]),
+                                     NPOINTS_PML=int(g["npml"]), vp_ref=float(g["vp_ref"]))
+    src = ads.AcousticSource(g["srci"], g["srcj"], g["srcv"])
+    rcv = ads.AcousticReceiver(g["rcvi"], g["rcvj"])
+    loss, grad = ads.dropin_loss_and_grad(p, src, rcv, g["obs"], g["vp"])
+    torch.cuda.synchronize()
+    assert abs(float(loss) - float(g["loss"])) <= TOL64 * float(g["loss"])
+    assert rel(grad.cpu().numpy().reshape(-1), g["grad_vp"]) <= TOL64
