@@ -60,7 +60,7 @@ class ElasticConfig(C.Structure):
         ("npml", C.c_int64), ("npower", C.c_double), ("k_max", C.c_double),
         ("alpha_max", C.c_double), ("vp_ref", C.c_double), ("Rcoef", C.c_double),
         ("use_pml", C.c_int32), ("precision", C.c_int32), ("use_graph", C.c_int32),
-        ("reserved0", C.c_int32), ("ckpt_every", C.c_int64), ("reserved", C.c_int32 * 8),
+        ("rows_per_warp", C.c_int32), ("ckpt_every", C.c_int64), ("reserved", C.c_int32 * 8),
     ]
 
 

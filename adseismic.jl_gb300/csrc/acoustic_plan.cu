@@ -35,6 +35,14 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 
+#ifndef ADS_PF32
+#define ADS_PF32 1
+#endif
+#ifndef ADS_MINB_A32
+#define ADS_MINB_A32 3
+#endif
+
+
 // Tiles: a CTA owns `J` columns x rows_per_thread rows of one shot.  The
 // forward step gives each thread CF adjacent columns, the adjoint CA (fewer,
 // it carries more state per cell); rows are loaded as 16/8-byte vectors.
@@ -46,6 +54,10 @@ struct Tile {
   static constexpr int NF = J / CF;  // forward threads per CTA (128)
   static constexpr int NA = J / CA;  // adjoint threads per CTA (256)
   static constexpr int NC = 128;     // threads of the column-loop helpers
+  // rows of register prefetch in the interior loops (bytes in flight per warp)
+  static constexpr int PF = sizeof(T) == 4 ? ADS_PF32 : 1;
+  // resident CTAs per SM the adjoint's register allocation must allow
+  static constexpr int MINB_A = sizeof(T) == 4 ? ADS_MINB_A32 : 2;
 };
 
 template <typename T, int C>
@@ -224,35 +236,48 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     // Interior tile: sigma = tau = 0 on every row and column the warp reads,
     // so phi = psi = 0 there and the step reduces to the plain wave update
     // (the dropped terms are exact zeros).
-    V wm = ldv<T, C>(w, off(i0 - 1), jld), w0 = ldv<T, C>(w, off(i0), jld),
-      wp = ldv<T, C>(w, off(i0 + 1), jld);
-    V wo0 = ldv<T, C>(wo, off(i0), jld), c0 = ldv<T, C>(cc, off(i0), jld);
-    T hw = 0;
-    if (lane == 0 && jld) hw = w[off(i0) - 1];
-    else if (lane == 31 && hr) hw = w[off(i0) + C];
+    // Register queues PF rows deep: w rows i-1 .. i+PF, wo / c / halo rows
+    // i .. i+PF-1; each iteration issues the loads of the farthest rows.
+    constexpr int PF = Tile<T>::PF;
+    V wq[PF + 2], oq[PF], cq[PF];
+    T hq[PF];
+    auto halo = [&](int r) -> T {
+      if (r >= i_end) return T(0);
+      if (lane == 0 && jld) return w[off(r) - 1];
+      if (lane == 31 && hr) return w[off(r) + C];
+      return T(0);
+    };
+#pragma unroll
+    for (int q = 0; q < PF + 2; q++) wq[q] = ldv<T, C>(w, off(i0 - 1 + q), jld && i0 - 1 + q <= i_end);
+#pragma unroll
+    for (int q = 0; q < PF; q++) {
+      const bool on = jld && i0 + q < i_end;
+      oq[q] = ldv<T, C>(wo, off(i0 + q), on);
+      cq[q] = ldv<T, C>(cc, off(i0 + q), on);
+      hq[q] = halo(i0 + q);
+    }
     for (int i = i0; i < i_end; i++) {
       const int64_t row = off(i);
-      const bool more = i + 1 < i_end;
-      V wn = ldv<T, C>(w, off(i + 2), jld && more);
-      V won = ldv<T, C>(wo, off(i + 1), jld && more);
-      V cn = ldv<T, C>(cc, off(i + 1), jld && more);
-      T hwn = 0;
-      if (more) {
-        if (lane == 0 && jld) hwn = w[row + P - 1];
-        else if (lane == 31 && hr) hwn = w[row + P + C];
-      }
+      const int rn = i + PF;  // farthest row of the wo / c / halo queues
+      V wn = ldv<T, C>(w, off(rn + 1), jld && rn + 1 <= i_end);
+      V on = ldv<T, C>(wo, off(rn), jld && rn < i_end);
+      V cn = ldv<T, C>(cc, off(rn), jld && rn < i_end);
+      const T hn = halo(rn);
+      const V& wm = wq[0];
+      const V& w0 = wq[1];
+      const V& wp = wq[2];
       T wL = __shfl_up_sync(FULL, w0.v[C - 1], 1), wR = __shfl_down_sync(FULL, w0.v[0], 1);
-      if (lane == 0) wL = hw;
-      else if (lane == 31) wR = hw;
+      if (lane == 0) wL = hq[0];
+      else if (lane == 31) wR = hq[0];
       if (jld) {
         V vo;
 #pragma unroll
         for (int c = 0; c < C; c++) {
           const T wS = c == 0 ? wL : w0.v[c - 1];
           const T wN = c == C - 1 ? wR : w0.v[c + 1];
-          const T cv = c0.v[c];
+          const T cv = cq[0].v[c];
           T v = (T(2) - K.kxy * cv) * w0.v[c] + cv * K.cx * (wp.v[c] + wm.v[c]) +
-                cv * K.cy * (wN + wS) - wo0.v[c];
+                cv * K.cy * (wN + wS) - oq[0].v[c];
           for (int e = it.src_b; e < it.src_e; e++) {
             const CellRef r = srcs[e];
             if (r.cell == row + c) v += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
@@ -266,12 +291,18 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
           stv<T, C>(ck + fs, row, w0, j, ny);
         }
       }
-      wm = w0;
-      w0 = wp;
-      wp = wn;
-      wo0 = won;
-      c0 = cn;
-      hw = hwn;
+#pragma unroll
+      for (int q = 0; q < PF + 1; q++) wq[q] = wq[q + 1];
+      wq[PF + 1] = wn;
+#pragma unroll
+      for (int q = 0; q < PF - 1; q++) {
+        oq[q] = oq[q + 1];
+        cq[q] = cq[q + 1];
+        hq[q] = hq[q + 1];
+      }
+      oq[PF - 1] = on;
+      cq[PF - 1] = cn;
+      hq[PF - 1] = hn;
     }
     record_traces<T, C, SEG>(it, sh, rcvs, out, t, lane);
     return;
@@ -415,6 +446,19 @@ __device__ __forceinline__ T inv_den(T s, const AcConst<T>& K) {
   return s != T(0) ? T(1) / (T(1) + s * K.hdt) : T(1);
 }
 
+// The grad_c accumulator an adjoint step adds to: the FP32 per-segment
+// partial in FP32 plans, the FP64 accumulator in FP64 plans.
+template <typename T>
+struct GradOf {
+  using type = double;
+};
+template <>
+struct GradOf<float> {
+  using type = float;
+};
+__device__ __forceinline__ float* grad_base(const AcShot<float>& sh) { return sh.gc32; }
+__device__ __forceinline__ double* grad_base(const AcShot<double>& sh) { return sh.gc; }
+
 // grad_c += g for a thread's C cells: the FP32 per-segment partial in FP32
 // plans, the FP64 accumulator in FP64 plans; one vector access when all C
 // cells are interior.
@@ -468,7 +512,7 @@ __device__ __forceinline__ void inject_residuals(const AcItem& it, const AcShot<
 // (flushed into the FP64 accumulator at the end of each segment); FP64 plans
 // accumulate in FP64.
 template <typename T>
-__global__ void __launch_bounds__(Tile<T>::NA, sizeof(T) == 4 ? 3 : 2)
+__global__ void __launch_bounds__(Tile<T>::NA, Tile<T>::MINB_A)
 k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
          const CellRef* __restrict__ rcvs, AcConst<T> K, int k, int base, int ri) {
   constexpr int C = Tile<T>::CA;
@@ -506,33 +550,53 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   if (interior_rows<T>(tfree, sx, i0, i_end, lane)) {
     // Interior tile (1/den = 1, lambdaPhi = lambdaPsi = 0): the transpose of
     // the plain wave update; rows i-1 (m), i (0), i+1 (1) of lambdaU_k and c.
-    V gum = ldv<T, C>(luc, off(i0 - 1), jld), cm = ldv<T, C>(cc, off(i0 - 1), jld);
-    V gu0 = ldv<T, C>(luc, off(i0), jld), c0 = ldv<T, C>(cc, off(i0), jld);
-    V gu1 = ldv<T, C>(luc, off(i0 + 1), jld), c1 = ldv<T, C>(cc, off(i0 + 1), jld);
-    V wm = ldv<T, C>(w, off(i0 - 1), jld), w0 = ldv<T, C>(w, off(i0), jld),
-      wp = ldv<T, C>(w, off(i0 + 1), jld);
-    V ln = ldv<T, C>(lun, off(i0), jld);
-    T hgu = 0, hc = 0, hw = 0;
-    if (hon) {
-      const int64_t r = off(i0) + hoff;
-      hgu = luc[r];
-      hc = cc[r];
-      hw = w[r];
+    // Register queues PF rows deep: lambdaU_k, c, u_{k-1} rows i-1 .. i+PF;
+    // lambdaU_{k+1}, the grad_c accumulator and the halo cells rows
+    // i .. i+PF-1.
+    constexpr int PF = Tile<T>::PF;
+    using G = typename GradOf<T>::type;
+    using VG = Vec<G, C>;
+    G* gb = grad_base(sh);
+    V uq[PF + 2], cq[PF + 2], wq[PF + 2], lq[PF];
+    VG gq[PF];
+    T hu[PF], hcq[PF], hwq[PF];
+    auto load_halo = [&](int r, T& a, T& b, T& d) {
+      a = b = d = T(0);
+      if (hon && r < i_end) {
+        const int64_t o = off(r) + hoff;
+        a = luc[o];
+        b = cc[o];
+        d = w[o];
+      }
+    };
+#pragma unroll
+    for (int q = 0; q < PF + 2; q++) {
+      const bool on = jld && i0 - 1 + q <= i_end;
+      uq[q] = ldv<T, C>(luc, off(i0 - 1 + q), on);
+      cq[q] = ldv<T, C>(cc, off(i0 - 1 + q), on);
+      wq[q] = ldv<T, C>(w, off(i0 - 1 + q), on);
+    }
+#pragma unroll
+    for (int q = 0; q < PF; q++) {
+      const bool on = jld && i0 + q < i_end;
+      lq[q] = ldv<T, C>(lun, off(i0 + q), on);
+      gq[q] = ldv<G, C>(gb, off(i0 + q), on);
+      load_halo(i0 + q, hu[q], hcq[q], hwq[q]);
     }
     for (int i = i0; i < i_end; i++) {
       const int64_t row = off(i);
-      const bool more = i + 1 < i_end;
-      V gu2 = ldv<T, C>(luc, off(i + 2), jld && more);
-      V c2 = ldv<T, C>(cc, off(i + 2), jld && more);
-      V w2 = ldv<T, C>(w, off(i + 2), jld && more);
-      V lnn = ldv<T, C>(lun, off(i + 1), jld && more);
-      T hgun = 0, hcn = 0, hwn = 0;
-      if (more && hon) {
-        const int64_t r = row + P + hoff;
-        hgun = luc[r];
-        hcn = cc[r];
-        hwn = w[r];
-      }
+      const int rn = i + PF;
+      const bool on1 = jld && rn + 1 <= i_end, on0 = jld && rn < i_end;
+      V un = ldv<T, C>(luc, off(rn + 1), on1);
+      V cn = ldv<T, C>(cc, off(rn + 1), on1);
+      V wn = ldv<T, C>(w, off(rn + 1), on1);
+      V ln = ldv<T, C>(lun, off(rn), on0);
+      VG gn = ldv<G, C>(gb, off(rn), on0);
+      T hun, hcn, hwn;
+      load_halo(rn, hun, hcn, hwn);
+      const V &gum = uq[0], &gu0 = uq[1], &gu1 = uq[2];
+      const V &cm = cq[0], &c0 = cq[1], &c1 = cq[2];
+      const V &wm = wq[0], &w0 = wq[1], &wp = wq[2];
       // what each cell sends to its j-neighbours: c cy lambdaU
       T Y[C];
 #pragma unroll
@@ -540,36 +604,53 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       T Yl = __shfl_up_sync(FULL, Y[C - 1], 1), Yr = __shfl_down_sync(FULL, Y[0], 1);
       T wL = __shfl_up_sync(FULL, w0.v[C - 1], 1), wR = __shfl_down_sync(FULL, w0.v[0], 1);
       if (lane == 0 || lane == 31) {
-        const T h = hon ? hc * K.cy * hgu : T(0);
+        const T h = hon ? hcq[0] * K.cy * hu[0] : T(0);
         if (lane == 0) {
           Yl = h;
-          wL = hw;
+          wL = hwq[0];
         } else {
           Yr = h;
-          wR = hw;
+          wR = hwq[0];
         }
       }
       if (jld) {
         V nu;
-        T g[C];
+        VG ga = gq[0];
 #pragma unroll
         for (int c = 0; c < C; c++) {
           const T yl = c == 0 ? Yl : Y[c - 1], yr = c == C - 1 ? Yr : Y[c + 1];
           const T wS = c == 0 ? wL : w0.v[c - 1], wN = c == C - 1 ? wR : w0.v[c + 1];
           const T cv = c0.v[c];
-          nu.v[c] = -ln.v[c] + (T(2) - K.kxy * cv) * gu0.v[c] + cm.v[c] * K.cx * gum.v[c] +
+          nu.v[c] = -lq[0].v[c] + (T(2) - K.kxy * cv) * gu0.v[c] + cm.v[c] * K.cx * gum.v[c] +
                     c1.v[c] * K.cx * gu1.v[c] + yl + yr;
-          g[c] = (-K.kxy * w0.v[c] + K.cx * (wp.v[c] + wm.v[c]) + K.cy * (wN + wS)) * gu0.v[c];
+          ga.v[c] += (G)((-K.kxy * w0.v[c] + K.cx * (wp.v[c] + wm.v[c]) + K.cy * (wN + wS)) *
+                         gu0.v[c]);
         }
         stv<T, C>(lun, row, nu, j, ny);
-        add_grad<T, C>(sh, row, g, j, ny);
+        stv<G, C>(gb, row, ga, j, ny);
       }
-      gum = gu0; cm = c0;
-      gu0 = gu1; c0 = c1;
-      gu1 = gu2; c1 = c2;
-      wm = w0; w0 = wp; wp = w2;
-      ln = lnn;
-      hgu = hgun; hc = hcn; hw = hwn;
+#pragma unroll
+      for (int q = 0; q < PF + 1; q++) {
+        uq[q] = uq[q + 1];
+        cq[q] = cq[q + 1];
+        wq[q] = wq[q + 1];
+      }
+      uq[PF + 1] = un;
+      cq[PF + 1] = cn;
+      wq[PF + 1] = wn;
+#pragma unroll
+      for (int q = 0; q < PF - 1; q++) {
+        lq[q] = lq[q + 1];
+        gq[q] = gq[q + 1];
+        hu[q] = hu[q + 1];
+        hcq[q] = hcq[q + 1];
+        hwq[q] = hwq[q + 1];
+      }
+      lq[PF - 1] = ln;
+      gq[PF - 1] = gn;
+      hu[PF - 1] = hun;
+      hcq[PF - 1] = hcn;
+      hwq[PF - 1] = hwn;
     }
     inject_residuals<T, C>(it, sh, rcvs, lun, k, lane);
     return;

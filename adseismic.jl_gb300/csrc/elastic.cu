@@ -38,6 +38,7 @@ struct ElModel {
   const T *lam, *mu, *rho;
   const T *axi, *axh, *bxi, *bxh, *ayi, *ayh, *byi, *byh;  // 1D, index I-1 / J-1
   T dt, hx24, hy24;
+  T rhx24, rhy24;  // 1 / hx24, 1 / hy24 (FP32 row kernels)
   int NX, NY, OFF, pad;
   int64_t P;
 };
@@ -396,6 +397,353 @@ k_el_adj3(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one) {
 
 #undef ELIDX
 
+// ---------------------------------------------------------------------------
+// Row-streaming forms of the two forward kernels for the plans.
+//
+// A warp owns a strip of rows of one shot, two adjacent columns per lane
+// (loaded as one 8/16-byte vector), and walks down its rows: the
+// i-neighbours of the 4th-order stencils sit in a 4-row register window whose
+// next row is loaded one iteration ahead, the j-neighbours (up to two columns
+// away) come from the neighbouring lanes.  Lanes 0 and 31 only supply those
+// neighbours: lanes 1..30 update ESTRIP = 60 columns and consecutive strips
+// overlap by two columns on each side.  The arithmetic and its order are
+// those of k_el_stress / k_el_velocity; cells outside the update boxes are
+// neither computed nor written.
+// ---------------------------------------------------------------------------
+constexpr int EC = 2;             // columns per lane
+constexpr int ESTRIP = 30 * EC;   // columns a warp strip updates
+constexpr int EW = 4;             // warps per CTA (independent strips)
+#ifndef ADS_EL_MINB
+#define ADS_EL_MINB 6                 // resident CTAs per SM the FP32 kernels are built for
+#endif
+template <typename T>
+constexpr int el_minb() { return sizeof(T) == 4 ? ADS_EL_MINB : 2; }
+
+template <typename T>
+struct alignas(2 * sizeof(T)) V2 {
+  T v[2];
+};
+
+template <typename T>
+__device__ __forceinline__ V2<T> ld2(const T* p, int64_t o, bool on) {
+  V2<T> x;
+  if (on) {
+    x = *reinterpret_cast<const V2<T>*>(p + o);
+  } else {
+    x.v[0] = T(0);
+    x.v[1] = T(0);
+  }
+  return x;
+}
+
+// Store the two cells of a lane, each only where its box flag is set.
+template <typename T>
+__device__ __forceinline__ void st2(T* p, int64_t o, const T (&x)[2], bool k0, bool k1) {
+  if (k0 && k1) {
+    V2<T> y;
+    y.v[0] = x[0];
+    y.v[1] = x[1];
+    *reinterpret_cast<V2<T>*>(p + o) = y;
+  } else {
+    if (k0) p[o] = x[0];
+    if (k1) p[o + 1] = x[1];
+  }
+}
+
+__device__ __forceinline__ float shup(float v) { return __shfl_up_sync(0xffffffffu, v, 1); }
+__device__ __forceinline__ double shup(double v) { return __shfl_up_sync(0xffffffffu, v, 1); }
+__device__ __forceinline__ float shdn(float v) { return __shfl_down_sync(0xffffffffu, v, 1); }
+__device__ __forceinline__ double shdn(double v) { return __shfl_down_sync(0xffffffffu, v, 1); }
+
+// Geometry of one warp's strip: columns j, j+1 of this lane, rows [i0, i_end)
+// (all inside 1..NX), whether the lane updates its cells, and the guarded
+// row loader.
+template <typename T>
+struct Strip {
+  int lane, j, i0, i_end, NX, NY;
+  bool out;
+  int64_t P;
+  __device__ Strip(const ElModel<T>& M, int ncolw, int R, int wi) {
+    lane = threadIdx.x & 31;
+    NX = M.NX;
+    NY = M.NY;
+    P = M.P;
+    const int strip = wi % ncolw, rt = wi / ncolw;
+    j = strip * ESTRIP - 1 + lane * EC;  // odd: 8/16-byte aligned pairs
+    out = lane >= 1 && lane <= 30;
+    i0 = 1 + rt * R;
+    i_end = min(i0 + R, NX + 1);
+  }
+  __device__ int64_t off(int r) const { return (int64_t)r * P + j + JOFF; }
+  // both cells of this lane at row r (zeros outside the padded grid)
+  __device__ V2<T> row(const T* p, int r) const {
+    return ld2<T>(p, off(r), j <= NY + 1 && r >= 0 && r <= NX + 1);
+  }
+};
+
+// FP32 row kernels multiply by 1 / (24 h) and divide by the density with the
+// fast reciprocal (within 2 ulp); FP64 keeps the exact divisions.
+template <typename T>
+__device__ __forceinline__ T d4r(T a0, T am1, T ap1, T am2, T h24, T rh24) {
+  if constexpr (sizeof(T) == 4) {
+    return (T(27) * a0 - T(27) * am1 - ap1 + am2) * rh24;
+  } else {
+    return (T(27) * a0 - T(27) * am1 - ap1 + am2) / h24;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T divr(T a, T b) {
+  if constexpr (sizeof(T) == 4) {
+    return __fdividef(a, b);
+  } else {
+    return a / b;
+  }
+}
+
+// y-profile coefficients of a lane's two columns (integer and half grid) and
+// whether the memory variable they drive is active there.
+template <typename T>
+struct ColProf {
+  T ai[2], bi[2], ah[2], bh[2];
+  bool acti[2], acth[2];
+  __device__ ColProf(const ElModel<T>& M, int j) {
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      const int jc = j + c;
+      const bool in = jc >= 1 && jc <= M.NY;
+      ai[c] = in ? M.ayi[jc - 1] : T(0);
+      bi[c] = in ? M.byi[jc - 1] : T(1);
+      ah[c] = in ? M.ayh[jc - 1] : T(0);
+      bh[c] = in ? M.byh[jc - 1] : T(1);
+      acti[c] = in && (ai[c] != T(0) || bi[c] != T(1));
+      acth[c] = in && (ah[c] != T(0) || bh[c] != T(1));
+    }
+  }
+};
+
+// Stress update (fw1 + fw2) of a strip.
+template <typename T, bool STORE>
+__global__ void __launch_bounds__(EW * 32, el_minb<T>())
+k_el_stress_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int R, int nwt,
+                 int store_slot) {
+  const int wi = blockIdx.x * EW + (threadIdx.x >> 5);
+  if (wi >= nwt) return;
+  const ElShot<T>& sh = shots[blockIdx.y];
+  const Strip<T> S(M, ncolw, R, wi);
+  const int j = S.j, NX = S.NX, NY = S.NY;
+  const T* __restrict__ vx = sh.f[VX];
+  const T* __restrict__ vy = sh.f[VY];
+  T* __restrict__ sxx = sh.f[SXX];
+  T* __restrict__ syy = sh.f[SYY];
+  T* __restrict__ sxy = sh.f[SXY];
+  T* __restrict__ m1p = sh.f[M1 + 0];
+  T* __restrict__ m2p = sh.f[M1 + 1];
+  T* __restrict__ m3p = sh.f[M1 + 2];
+  T* __restrict__ m4p = sh.f[M1 + 3];
+  T* __restrict__ st = STORE ? sh.store + (int64_t)store_slot * NSTORE * sh.fs : nullptr;
+  const int64_t fs = sh.fs;
+  const ColProf<T> Y(M, j);
+  bool c1[2], c2[2];  // column parts of the fw1 / fw2 boxes
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    c1[c] = S.out && j + c >= 2 && j + c <= NY;
+    c2[c] = S.out && j + c >= 1 && j + c <= NY - 1;
+  }
+  const int i0 = S.i0;
+  // windows: vx rows i-1..i+2, vy rows i-2..i+1, lam / mu rows i, i+1
+  V2<T> X0 = S.row(vx, i0 - 1), X1 = S.row(vx, i0), X2 = S.row(vx, i0 + 1), X3 = S.row(vx, i0 + 2);
+  V2<T> Y0 = S.row(vy, i0 - 2), Y1 = S.row(vy, i0 - 1), Y2 = S.row(vy, i0), Y3 = S.row(vy, i0 + 1);
+  V2<T> L0 = S.row(M.lam, i0), L1 = S.row(M.lam, i0 + 1);
+  V2<T> U0 = S.row(M.mu, i0), U1 = S.row(M.mu, i0 + 1);
+  V2<T> A0 = S.row(sxx, i0), B0 = S.row(syy, i0), C0 = S.row(sxy, i0);
+  for (int i = i0; i < S.i_end; i++) {
+    const int64_t o = S.off(i);
+    // next row's loads
+    const bool more = i + 1 < S.i_end;
+    const int rn = more ? i + 1 : -1;
+    const V2<T> X4 = S.row(vx, more ? i + 3 : -1), Y4 = S.row(vy, more ? i + 2 : -1),
+                L2 = S.row(M.lam, more ? i + 2 : -1), U2 = S.row(M.mu, more ? i + 2 : -1);
+    const V2<T> An = S.row(sxx, rn), Bn = S.row(syy, rn), Cn = S.row(sxy, rn);
+    // row i across columns (neighbouring lanes): vx at j-1..j+3, vy at j-2..j+2, mu at j..j+2
+    T xr[5], yr[5], ur[3];
+    xr[0] = shup(X1.v[1]);
+    xr[1] = X1.v[0];
+    xr[2] = X1.v[1];
+    xr[3] = shdn(X1.v[0]);
+    xr[4] = shdn(X1.v[1]);
+    yr[0] = shup(Y2.v[0]);
+    yr[1] = shup(Y2.v[1]);
+    yr[2] = Y2.v[0];
+    yr[3] = Y2.v[1];
+    yr[4] = shdn(Y2.v[0]);
+    ur[0] = U0.v[0];
+    ur[1] = U0.v[1];
+    ur[2] = shdn(U0.v[0]);
+    // x profiles of row i: m1 on the half grid (fw1 rows), m3 on the integer grid (fw2 rows)
+    const T axh = M.axh[i - 1], bxh = M.bxh[i - 1], axi = M.axi[i - 1], bxi = M.bxi[i - 1];
+    const bool r1 = i <= NX - 1, r2 = i >= 2;
+    const bool rx1 = r1 && (axh != T(0) || bxh != T(1));
+    const bool rx3 = r2 && (axi != T(0) || bxi != T(1));
+    T nsxx[2], nsyy[2], nsxy[2], e1s[2], e2s[2], e12s[2];
+    bool k1[2], k2[2];
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      k1[c] = r1 && c1[c];
+      k2[c] = r2 && c2[c];
+      // fw1
+      const T lam_ = T(0.5) * (L1.v[c] + L0.v[c]);
+      const T mu1 = T(0.5) * (U1.v[c] + U0.v[c]);
+      const T lm = lam_ + T(2) * mu1;
+      const T dvx = d4r<T>(X2.v[c], X1.v[c], X3.v[c], X0.v[c], M.hx24, M.rhx24);
+      const T dvy = d4r<T>(yr[2 + c], yr[1 + c], yr[3 + c], yr[c], M.hy24, M.rhy24);
+      const bool u1 = k1[c] && rx1, u2 = k1[c] && Y.acti[c];
+      const T m1 = u1 ? bxh * m1p[o + c] + axh * dvx : T(0);
+      const T m2 = u2 ? Y.bi[c] * m2p[o + c] + Y.ai[c] * dvy : T(0);
+      if (u1) m1p[o + c] = m1;
+      if (u2) m2p[o + c] = m2;
+      const T e1 = dvx + m1, e2 = dvy + m2;
+      nsxx[c] = A0.v[c] + (lm * e1 + lam_ * e2) * M.dt;
+      nsyy[c] = B0.v[c] + (lm * e2 + lam_ * e1) * M.dt;
+      e1s[c] = e1;
+      e2s[c] = e2;
+      // fw2
+      const T mu2 = T(0.5) * (ur[c] + ur[c + 1]);
+      const T dvydx = d4r<T>(Y2.v[c], Y1.v[c], Y3.v[c], Y0.v[c], M.hx24, M.rhx24);
+      const T dvxdy = d4r<T>(xr[2 + c], xr[1 + c], xr[3 + c], xr[c], M.hy24, M.rhy24);
+      const bool u3 = k2[c] && rx3, u4 = k2[c] && Y.acth[c];
+      const T m3 = u3 ? bxi * m3p[o + c] + axi * dvydx : T(0);
+      const T m4 = u4 ? Y.bh[c] * m4p[o + c] + Y.ah[c] * dvxdy : T(0);
+      if (u3) m3p[o + c] = m3;
+      if (u4) m4p[o + c] = m4;
+      const T e12 = (dvydx + m3) + (dvxdy + m4);
+      nsxy[c] = C0.v[c] + mu2 * e12 * M.dt;
+      e12s[c] = e12;
+    }
+    st2<T>(sxx, o, nsxx, k1[0], k1[1]);
+    st2<T>(syy, o, nsyy, k1[0], k1[1]);
+    st2<T>(sxy, o, nsxy, k2[0], k2[1]);
+    if (STORE) {
+      st2<T>(st + E1 * fs, o, e1s, k1[0], k1[1]);
+      st2<T>(st + E2 * fs, o, e2s, k1[0], k1[1]);
+      st2<T>(st + E12 * fs, o, e12s, k2[0], k2[1]);
+    }
+    X0 = X1; X1 = X2; X2 = X3; X3 = X4;
+    Y0 = Y1; Y1 = Y2; Y2 = Y3; Y3 = Y4;
+    L0 = L1; L1 = L2; U0 = U1; U1 = U2;
+    A0 = An; B0 = Bn; C0 = Cn;
+  }
+}
+
+// Velocity update (fw3 + fw4) of a strip, from the new stresses.
+template <typename T, bool STORE>
+__global__ void __launch_bounds__(EW * 32, el_minb<T>())
+k_el_velocity_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int R, int nwt,
+                   int store_slot) {
+  const int wi = blockIdx.x * EW + (threadIdx.x >> 5);
+  if (wi >= nwt) return;
+  const ElShot<T>& sh = shots[blockIdx.y];
+  const Strip<T> S(M, ncolw, R, wi);
+  const int j = S.j, NX = S.NX, NY = S.NY;
+  const T* __restrict__ sxx = sh.f[SXX];
+  const T* __restrict__ syy = sh.f[SYY];
+  const T* __restrict__ sxy = sh.f[SXY];
+  T* __restrict__ vx = sh.f[VX];
+  T* __restrict__ vy = sh.f[VY];
+  T* __restrict__ m5p = sh.f[M1 + 4];
+  T* __restrict__ m6p = sh.f[M1 + 5];
+  T* __restrict__ m7p = sh.f[M1 + 6];
+  T* __restrict__ m8p = sh.f[M1 + 7];
+  T* __restrict__ st = STORE ? sh.store + (int64_t)store_slot * NSTORE * sh.fs : nullptr;
+  const int64_t fs = sh.fs;
+  const ColProf<T> Y(M, j);
+  bool c3[2], c4[2];  // column parts of the fw3 / fw4 boxes
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    c3[c] = S.out && j + c >= 2 && j + c <= NY;
+    c4[c] = S.out && j + c >= 1 && j + c <= NY - 1;
+  }
+  const int i0 = S.i0;
+  // windows: sxx rows i-2..i+1, sxy rows i-1..i+2, syy row i, rho rows i, i+1
+  V2<T> S0 = S.row(sxx, i0 - 2), S1 = S.row(sxx, i0 - 1), S2 = S.row(sxx, i0), S3 = S.row(sxx, i0 + 1);
+  V2<T> Q0 = S.row(sxy, i0 - 1), Q1 = S.row(sxy, i0), Q2 = S.row(sxy, i0 + 1), Q3 = S.row(sxy, i0 + 2);
+  V2<T> W0 = S.row(syy, i0);
+  V2<T> R0 = S.row(M.rho, i0), R1 = S.row(M.rho, i0 + 1);
+  V2<T> VX0 = S.row(vx, i0), VY0 = S.row(vy, i0);
+  for (int i = i0; i < S.i_end; i++) {
+    const int64_t o = S.off(i);
+    const bool more = i + 1 < S.i_end;
+    const int rn = more ? i + 1 : -1;
+    const V2<T> S4 = S.row(sxx, more ? i + 2 : -1), Q4 = S.row(sxy, more ? i + 3 : -1),
+                R2 = S.row(M.rho, more ? i + 2 : -1);
+    const V2<T> Wn = S.row(syy, rn), VXn = S.row(vx, rn), VYn = S.row(vy, rn);
+    // row i across columns (neighbouring lanes): sxy at j-2..j+2, syy at j-1..j+3,
+    // rho rows i, i+1 at j..j+2
+    T qr[5], wr[5], r0[3], r1[3];
+    qr[0] = shup(Q1.v[0]);
+    qr[1] = shup(Q1.v[1]);
+    qr[2] = Q1.v[0];
+    qr[3] = Q1.v[1];
+    qr[4] = shdn(Q1.v[0]);
+    wr[0] = shup(W0.v[1]);
+    wr[1] = W0.v[0];
+    wr[2] = W0.v[1];
+    wr[3] = shdn(W0.v[0]);
+    wr[4] = shdn(W0.v[1]);
+    r0[0] = R0.v[0];
+    r0[1] = R0.v[1];
+    r0[2] = shdn(R0.v[0]);
+    r1[0] = R1.v[0];
+    r1[1] = R1.v[1];
+    r1[2] = shdn(R1.v[0]);
+    // x profiles of row i: m5 on the integer grid (fw3 rows), m7 on the half grid (fw4 rows)
+    const T axi = M.axi[i - 1], bxi = M.bxi[i - 1], axh = M.axh[i - 1], bxh = M.bxh[i - 1];
+    const bool r3 = i >= 2, r4 = i <= NX - 1;
+    const bool rx5 = r3 && (axi != T(0) || bxi != T(1));
+    const bool rx7 = r4 && (axh != T(0) || bxh != T(1));
+    T nvx[2], nvy[2], a3s[2], a4s[2];
+    bool k3[2], k4[2];
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      k3[c] = r3 && c3[c];
+      k4[c] = r4 && c4[c];
+      // fw3
+      const T a = d4r<T>(S2.v[c], S1.v[c], S3.v[c], S0.v[c], M.hx24, M.rhx24);
+      const T b = d4r<T>(qr[2 + c], qr[1 + c], qr[3 + c], qr[c], M.hy24, M.rhy24);
+      const bool u5 = k3[c] && rx5, u6 = k3[c] && Y.acti[c];
+      const T m5 = u5 ? bxi * m5p[o + c] + axi * a : T(0);
+      const T m6 = u6 ? Y.bi[c] * m6p[o + c] + Y.ai[c] * b : T(0);
+      if (u5) m5p[o + c] = m5;
+      if (u6) m6p[o + c] = m6;
+      const T e3 = (a + m5) + (b + m6);
+      nvx[c] = VX0.v[c] + divr<T>(e3 * M.dt, r0[c]);
+      a3s[c] = e3;
+      // fw4
+      const T rho_ = T(0.25) * (r0[c] + r1[c] + r1[c + 1] + r0[c + 1]);
+      const T a4 = d4r<T>(Q2.v[c], Q1.v[c], Q3.v[c], Q0.v[c], M.hx24, M.rhx24);
+      const T b4 = d4r<T>(wr[2 + c], wr[1 + c], wr[3 + c], wr[c], M.hy24, M.rhy24);
+      const bool u7 = k4[c] && rx7, u8 = k4[c] && Y.acth[c];
+      const T m7 = u7 ? bxh * m7p[o + c] + axh * a4 : T(0);
+      const T m8 = u8 ? Y.bh[c] * m8p[o + c] + Y.ah[c] * b4 : T(0);
+      if (u7) m7p[o + c] = m7;
+      if (u8) m8p[o + c] = m8;
+      const T e4 = (a4 + m7) + (b4 + m8);
+      nvy[c] = VY0.v[c] + divr<T>(e4 * M.dt, rho_);
+      a4s[c] = e4;
+    }
+    st2<T>(vx, o, nvx, k3[0], k3[1]);
+    st2<T>(vy, o, nvy, k4[0], k4[1]);
+    if (STORE) {
+      st2<T>(st + A3 * fs, o, a3s, k3[0], k3[1]);
+      st2<T>(st + A4 * fs, o, a4s, k4[0], k4[1]);
+    }
+    S0 = S1; S1 = S2; S2 = S3; S3 = S4;
+    Q0 = Q1; Q1 = Q2; Q2 = Q3; Q3 = Q4;
+    R0 = R1; R1 = R2;
+    W0 = Wn; VX0 = VXn; VY0 = VYn;
+  }
+}
+
 // Sources of slot n (added in order by one thread), then receivers of slot n.
 template <typename T>
 __global__ void k_el_src_rcv(const ElShot<T>* __restrict__ shots, int n, int nt, int record) {
@@ -547,6 +895,8 @@ ElModel<T> make_model(int NX, int NY, int64_t P, int off, double dt, double dx, 
   M.dt = (T)dt;
   M.hx24 = (T)(24 * dx);
   M.hy24 = (T)(24 * dy);
+  M.rhx24 = (T)(1.0 / (24 * dx));
+  M.rhy24 = (T)(1.0 / (24 * dy));
   M.NX = NX;
   M.NY = NY;
   M.OFF = off;
@@ -597,6 +947,7 @@ template <typename T>
 struct ElPlan final : ElPlanBase {
   ads_elastic_config cfg{};
   int nshots = 0, K = 0, nseg = 0, NX = 0, NY = 0, NSTEP = 0;
+  int ncolw = 0, rows_w = 0, nwt = 0;  // warp strips of the row-streaming step kernels
   int64_t P = 0, fs = 0;
   char* pool = nullptr;
   ElShot<T>* d_shots = nullptr;
@@ -623,6 +974,7 @@ struct ElPlan final : ElPlanBase {
   dim3 grid3() const {
     return dim3((unsigned)div_up(NY + 2, BX), (unsigned)div_up(NX + 2, BY), (unsigned)nshots);
   }
+  dim3 grid_rows() const { return dim3((unsigned)div_up(nwt, EW), (unsigned)nshots); }
 
   int create(const ads_elastic_config& c, const ads_elastic_shot* shots, int64_t ns,
              cudaStream_t st);
@@ -671,6 +1023,21 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   nseg = (int)div_up(NSTEP, K);
   P = grid_pitch(NY);
   fs = (int64_t)(NX + 2) * P;
+  // strips of ESTRIP columns cover 1..NY; rows per warp sized for about one
+  // warp per SM slot (at least 8 rows to amortise the 4-row windows) unless given
+  ncolw = (int)div_up(NY, ESTRIP);
+  {
+    int sms = 152;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess)
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t target = (int64_t)sms * 64;
+    const int64_t work = (int64_t)ncolw * NX * ns;
+    rows_w = c.rows_per_warp > 0 ? (int)c.rows_per_warp
+                                 : (int)std::min<int64_t>(32, std::max<int64_t>(8, div_up(work, target)));
+    ADS_REQUIRE(rows_w >= 1 && rows_w <= NX, "rows_per_warp must be in [1, NX]");
+  }
+  nwt = ncolw * (int)div_up(NX, rows_w);
   trace_off.resize(ns);
   trace_total = 0;
   for (int s = 0; s < ns; s++) {
@@ -845,16 +1212,19 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
 // One forward step n (slot n-1 -> slot n) for every shot.
 template <typename T>
 int ElPlan<T>::step(cudaStream_t st, int n, bool store, int slot, bool record) {
-  const ElShot<T> none{};
   if (store) {
-    k_el_stress<T, false, true><<<grid3(), dim3(BX, BY), 0, st>>>(M, d_shots, none, slot);
+    k_el_stress_rows<T, true><<<grid_rows(), EW * 32, 0, st>>>(M, d_shots, ncolw, rows_w, nwt,
+                                                                slot);
     ADS_LAUNCHED(1);
-    k_el_velocity<T, false, true><<<grid3(), dim3(BX, BY), 0, st>>>(M, d_shots, none, slot);
+    k_el_velocity_rows<T, true><<<grid_rows(), EW * 32, 0, st>>>(M, d_shots, ncolw, rows_w, nwt,
+                                                                  slot);
     ADS_LAUNCHED(1);
   } else {
-    k_el_stress<T, false, false><<<grid3(), dim3(BX, BY), 0, st>>>(M, d_shots, none, 0);
+    k_el_stress_rows<T, false><<<grid_rows(), EW * 32, 0, st>>>(M, d_shots, ncolw, rows_w, nwt,
+                                                                 0);
     ADS_LAUNCHED(1);
-    k_el_velocity<T, false, false><<<grid3(), dim3(BX, BY), 0, st>>>(M, d_shots, none, 0);
+    k_el_velocity_rows<T, false><<<grid_rows(), EW * 32, 0, st>>>(M, d_shots, ncolw, rows_w,
+                                                                   nwt, 0);
     ADS_LAUNCHED(1);
   }
   k_el_src_rcv<T><<<nshots, 128, 0, st>>>(d_shots, n, NSTEP + 1, record ? 1 : 0);

@@ -131,7 +131,7 @@ class ElasticPlan:
     srctype, srcv (NSTEP, nsrc), rcvi, rcvj, rcvtype."""
 
     def __init__(self, param: ElasticPropagatorParams, shots, precision="f64",
-                 use_graph=True, ckpt_every=0, stream=None):
+                 use_graph=True, ckpt_every=0, stream=None, rows_per_warp=0):
         cfg = _lib.ElasticConfig()
         cfg.NX, cfg.NY, cfg.NSTEP = param.NX, param.NY, param.NSTEP
         cfg.dx, cfg.dy, cfg.dt = param.DELTAX, param.DELTAY, param.DELTAT
@@ -141,6 +141,7 @@ class ElasticPlan:
         cfg.precision = ADS_F64 if precision == "f64" else ADS_F32
         cfg.use_graph = int(bool(use_graph))
         cfg.ckpt_every = ckpt_every
+        cfg.rows_per_warp = int(rows_per_warp)
         self.param = param
         self.dtype = torch.float64 if precision == "f64" else torch.float32
         self._keep = []

@@ -324,7 +324,7 @@ typedef struct ads_elastic_config {
   int32_t use_pml;    /* bitmask, 15 = all sides */
   int32_t precision;  /* ADS_F64 or ADS_F32 */
   int32_t use_graph;
-  int32_t reserved0;
+  int32_t rows_per_warp; /* rows a warp streams in the step kernels; 0 = automatic */
   int64_t ckpt_every; /* 0 = automatic */
   int32_t reserved[8];
 } ads_elastic_config;
