@@ -52,11 +52,15 @@ struct ElShot {
   T* store;          // K slots x NSTORE fields
   T* ckpt;           // nseg x NF fields
   double *glam, *gmu, *grho;
+  float *gl32, *gm32, *gr32;  // FP32 plans: per-segment partials of glam, gmu, grho
   T *traces, *resid;            // (nrcv, NSTEP+1)
   const T* srcv;                // (NSTEP, nsrc)
   const int64_t* src_cell;      // pitched cell offsets
   const int* src_type;
   const int64_t* rcv_cell;
+  T* const* src_ptr;   // per source: its cell in the state (nullptr: type ignored)
+  T* const* rcv_ptr;   // per receiver: its cell in the state (nullptr: records 0)
+  T* const* rcv_gptr;  // per receiver: its cell in the adjoint state
   const int* rcv_type;
   int nsrc, nrcv;
   int64_t fs;                   // elements per field
@@ -416,8 +420,13 @@ constexpr int EW = 4;             // warps per CTA (independent strips)
 #ifndef ADS_EL_MINB
 #define ADS_EL_MINB 6                 // resident CTAs per SM the FP32 kernels are built for
 #endif
+#ifndef ADS_EL_MINB_ADJ
+#define ADS_EL_MINB_ADJ 4             // the same for the two gather-heavy adjoint kernels
+#endif
 template <typename T>
 constexpr int el_minb() { return sizeof(T) == 4 ? ADS_EL_MINB : 2; }
+template <typename T>
+constexpr int el_minb_adj() { return sizeof(T) == 4 ? ADS_EL_MINB_ADJ : 2; }
 
 template <typename T>
 struct alignas(2 * sizeof(T)) V2 {
@@ -744,34 +753,424 @@ k_el_velocity_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Row-streaming forms of the three adjoint kernels for the plans (same strips
+// as the forward ones).  FP32 plans add the lambda / mu / rho contributions of
+// a step to FP32 per-segment partials (flushed into the FP64 accumulators by
+// k_el_flush_acc at the end of each checkpoint segment); FP64 plans add to
+// the FP64 accumulators directly.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct ElAcc {
+  using type = double;
+  static __device__ double* lam(const ElShot<T>& sh) { return sh.glam; }
+  static __device__ double* mu(const ElShot<T>& sh) { return sh.gmu; }
+  static __device__ double* rho(const ElShot<T>& sh) { return sh.grho; }
+};
+template <>
+struct ElAcc<float> {
+  using type = float;
+  static __device__ float* lam(const ElShot<float>& sh) { return sh.gl32; }
+  static __device__ float* mu(const ElShot<float>& sh) { return sh.gm32; }
+  static __device__ float* rho(const ElShot<float>& sh) { return sh.gr32; }
+};
+
+// x / (24 h): FP32 multiplies by the reciprocal, FP64 divides.
+template <typename T>
+__device__ __forceinline__ T hdiv(T x, T h24, T rh24) {
+  if constexpr (sizeof(T) == 4) {
+    return x * rh24;
+  } else {
+    return x / h24;
+  }
+}
+
+// Adjoint 1 (velocity cells) of a strip: transposes of fw3 and fw4.
+template <typename T>
+__global__ void __launch_bounds__(EW * 32, el_minb<T>())
+k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int R, int nwt,
+               int store_slot) {
+  using A = typename ElAcc<T>::type;
+  const int wi = blockIdx.x * EW + (threadIdx.x >> 5);
+  if (wi >= nwt) return;
+  const ElShot<T>& sh = shots[blockIdx.y];
+  const Strip<T> S(M, ncolw, R, wi);
+  const int j = S.j, NX = S.NX, NY = S.NY;
+  const int64_t fs = sh.fs;
+  const T* __restrict__ gvx = sh.g[VX];
+  const T* __restrict__ gvy = sh.g[VY];
+  T* __restrict__ g5 = sh.g[M1 + 4];
+  T* __restrict__ g6 = sh.g[M1 + 5];
+  T* __restrict__ g7 = sh.g[M1 + 6];
+  T* __restrict__ g8 = sh.g[M1 + 7];
+  T* __restrict__ d5 = sh.tmp[D5];
+  T* __restrict__ d6 = sh.tmp[D6];
+  T* __restrict__ d7 = sh.tmp[D7];
+  T* __restrict__ d8 = sh.tmp[D8];
+  T* __restrict__ r4p = sh.tmp[R4];
+  const T* __restrict__ st = sh.store + (int64_t)store_slot * NSTORE * fs;
+  const T* __restrict__ a3p = st + A3 * fs;
+  const T* __restrict__ a4p = st + A4 * fs;
+  A* __restrict__ grp = ElAcc<T>::rho(sh);
+  const ColProf<T> Y(M, j);
+  bool c3[2], c4[2];
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    c3[c] = S.out && j + c >= 2 && j + c <= NY;
+    c4[c] = S.out && j + c >= 1 && j + c <= NY - 1;
+  }
+  const int i0 = S.i0;
+  V2<T> R0 = S.row(M.rho, i0), R1 = S.row(M.rho, i0 + 1);
+  V2<T> GX = S.row(gvx, i0), GY = S.row(gvy, i0), E3 = S.row(a3p, i0), E4 = S.row(a4p, i0);
+  V2<A> GR = S.row(grp, i0);
+  for (int i = i0; i < S.i_end; i++) {
+    const int64_t o = S.off(i);
+    const bool more = i + 1 < S.i_end;
+    const int rn = more ? i + 1 : -1;
+    const V2<T> R2 = S.row(M.rho, more ? i + 2 : -1);
+    const V2<T> GXn = S.row(gvx, rn), GYn = S.row(gvy, rn), E3n = S.row(a3p, rn),
+                E4n = S.row(a4p, rn);
+    const V2<A> GRn = S.row(grp, rn);
+    T r0[3], r1[3];
+    r0[0] = R0.v[0];
+    r0[1] = R0.v[1];
+    r0[2] = shdn(R0.v[0]);
+    r1[0] = R1.v[0];
+    r1[1] = R1.v[1];
+    r1[2] = shdn(R1.v[0]);
+    const T axi = M.axi[i - 1], bxi = M.bxi[i - 1], axh = M.axh[i - 1], bxh = M.bxh[i - 1];
+    const bool r3 = i >= 2, r4 = i <= NX - 1;
+    const bool rx5 = r3 && (axi != T(0) || bxi != T(1));
+    const bool rx7 = r4 && (axh != T(0) || bxh != T(1));
+    T o5[2], o6[2], o7[2], o8[2], o4[2];
+    A gr[2];
+    bool k3[2], k4[2];
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      k3[c] = r3 && c3[c];
+      k4[c] = r4 && c4[c];
+      // fw3 transpose
+      const T gv = GX.v[c], r = r0[c];
+      const T q = divr<T>(gv * M.dt, r);
+      const bool u5 = k3[c] && rx5, u6 = k3[c] && Y.acti[c];
+      const T gm5 = u5 ? q + g5[o + c] : q;
+      const T gm6 = u6 ? q + g6[o + c] : q;
+      if (u5) g5[o + c] = bxi * gm5;
+      if (u6) g6[o + c] = Y.bi[c] * gm6;
+      o5[c] = hdiv<T>(q + axi * gm5, M.hx24, M.rhx24);
+      o6[c] = hdiv<T>(q + Y.ai[c] * gm6, M.hy24, M.rhy24);
+      gr[c] = GR.v[c] + (A)divr<T>(-gv * E3.v[c] * M.dt, r * r);
+      // fw4 transpose
+      const T gw = GY.v[c];
+      const T rho_ = T(0.25) * (r0[c] + r1[c] + r1[c + 1] + r0[c + 1]);
+      const T q4 = divr<T>(gw * M.dt, rho_);
+      const bool u7 = k4[c] && rx7, u8 = k4[c] && Y.acth[c];
+      const T gm7 = u7 ? q4 + g7[o + c] : q4;
+      const T gm8 = u8 ? q4 + g8[o + c] : q4;
+      if (u7) g7[o + c] = bxh * gm7;
+      if (u8) g8[o + c] = Y.bh[c] * gm8;
+      o7[c] = hdiv<T>(q4 + axh * gm7, M.hx24, M.rhx24);
+      o8[c] = hdiv<T>(q4 + Y.ah[c] * gm8, M.hy24, M.rhy24);
+      o4[c] = divr<T>(-gw * E4.v[c] * M.dt, rho_ * rho_) * T(0.25);
+    }
+    st2<T>(d5, o, o5, k3[0], k3[1]);
+    st2<T>(d6, o, o6, k3[0], k3[1]);
+    st2<A>(grp, o, gr, k3[0], k3[1]);
+    st2<T>(d7, o, o7, k4[0], k4[1]);
+    st2<T>(d8, o, o8, k4[0], k4[1]);
+    st2<T>(r4p, o, o4, k4[0], k4[1]);
+    R0 = R1; R1 = R2;
+    GX = GXn; GY = GYn; E3 = E3n; E4 = E4n; GR = GRn;
+  }
+}
+
+// Adjoint 2 (stress cells) of a strip: gather D5..D8 into the stress
+// adjoints, then the transposes of fw1 and fw2.
+template <typename T>
+__global__ void __launch_bounds__(EW * 32, el_minb_adj<T>())
+k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int R, int nwt,
+               int store_slot) {
+  const int wi = blockIdx.x * EW + (threadIdx.x >> 5);
+  if (wi >= nwt) return;
+  const ElShot<T>& sh = shots[blockIdx.y];
+  const Strip<T> S(M, ncolw, R, wi);
+  const int j = S.j, NX = S.NX, NY = S.NY;
+  const int64_t fs = sh.fs;
+  T* __restrict__ gxx = sh.g[SXX];
+  T* __restrict__ gyy = sh.g[SYY];
+  T* __restrict__ gxy = sh.g[SXY];
+  T* __restrict__ g1 = sh.g[M1 + 0];
+  T* __restrict__ g2 = sh.g[M1 + 1];
+  T* __restrict__ g3 = sh.g[M1 + 2];
+  T* __restrict__ g4 = sh.g[M1 + 3];
+  const T* __restrict__ d5 = sh.tmp[D5];
+  const T* __restrict__ d6 = sh.tmp[D6];
+  const T* __restrict__ d7 = sh.tmp[D7];
+  const T* __restrict__ d8 = sh.tmp[D8];
+  T* __restrict__ d1 = sh.tmp[D1];
+  T* __restrict__ d2 = sh.tmp[D2];
+  T* __restrict__ d3 = sh.tmp[D3];
+  T* __restrict__ d4p = sh.tmp[D4];
+  T* __restrict__ gl1 = sh.tmp[GL1];
+  T* __restrict__ gm1p = sh.tmp[GM1];
+  T* __restrict__ gm2p = sh.tmp[GM2];
+  const T* __restrict__ st = sh.store + (int64_t)store_slot * NSTORE * fs;
+  const T* __restrict__ e1p = st + E1 * fs;
+  const T* __restrict__ e2p = st + E2 * fs;
+  const T* __restrict__ e12p = st + E12 * fs;
+  const ColProf<T> Y(M, j);
+  bool c1[2], c2[2];
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    c1[c] = S.out && j + c >= 2 && j + c <= NY;
+    c2[c] = S.out && j + c >= 1 && j + c <= NY - 1;
+  }
+  const int i0 = S.i0;
+  // windows: D5 rows i-1..i+2, D7 rows i-2..i+1, lam / mu rows i, i+1
+  V2<T> P0 = S.row(d5, i0 - 1), P1 = S.row(d5, i0), P2 = S.row(d5, i0 + 1), P3 = S.row(d5, i0 + 2);
+  V2<T> Q0 = S.row(d7, i0 - 2), Q1 = S.row(d7, i0 - 1), Q2 = S.row(d7, i0), Q3 = S.row(d7, i0 + 1);
+  V2<T> L0 = S.row(M.lam, i0), L1 = S.row(M.lam, i0 + 1);
+  V2<T> U0 = S.row(M.mu, i0), U1 = S.row(M.mu, i0 + 1);
+  V2<T> F6 = S.row(d6, i0), F8 = S.row(d8, i0);
+  V2<T> GA = S.row(gxx, i0), GB = S.row(gyy, i0), GC = S.row(gxy, i0);
+  V2<T> EA = S.row(e1p, i0), EB = S.row(e2p, i0), EC12 = S.row(e12p, i0);
+  for (int i = i0; i < S.i_end; i++) {
+    const int64_t o = S.off(i);
+    const bool more = i + 1 < S.i_end;
+    const int rn = more ? i + 1 : -1;
+    const V2<T> P4 = S.row(d5, more ? i + 3 : -1), Q4 = S.row(d7, more ? i + 2 : -1),
+                L2 = S.row(M.lam, more ? i + 2 : -1), U2 = S.row(M.mu, more ? i + 2 : -1);
+    const V2<T> F6n = S.row(d6, rn), F8n = S.row(d8, rn);
+    const V2<T> GAn = S.row(gxx, rn), GBn = S.row(gyy, rn), GCn = S.row(gxy, rn);
+    const V2<T> EAn = S.row(e1p, rn), EBn = S.row(e2p, rn), ECn = S.row(e12p, rn);
+    // row i across columns: D6 at j-1..j+3, D8 at j-2..j+2, mu at j..j+2
+    T f6[5], f8[5], ur[3];
+    f6[0] = shup(F6.v[1]);
+    f6[1] = F6.v[0];
+    f6[2] = F6.v[1];
+    f6[3] = shdn(F6.v[0]);
+    f6[4] = shdn(F6.v[1]);
+    f8[0] = shup(F8.v[0]);
+    f8[1] = shup(F8.v[1]);
+    f8[2] = F8.v[0];
+    f8[3] = F8.v[1];
+    f8[4] = shdn(F8.v[0]);
+    ur[0] = U0.v[0];
+    ur[1] = U0.v[1];
+    ur[2] = shdn(U0.v[0]);
+    const T axh = M.axh[i - 1], bxh = M.bxh[i - 1], axi = M.axi[i - 1], bxi = M.bxi[i - 1];
+    const bool r1 = i <= NX - 1, r2 = i >= 2;
+    const bool rx1 = r1 && (axh != T(0) || bxh != T(1));
+    const bool rx3 = r2 && (axi != T(0) || bxi != T(1));
+    T oxx[2], oyy[2], oxy[2], ol1[2], om1[2], od1[2], od2[2], om2[2], od3[2], od4[2];
+    bool k1[2], k2[2], k12[2];
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      k1[c] = r1 && c1[c];
+      k2[c] = r2 && c2[c];
+      k12[c] = k1[c] || k2[c];
+      // gathers (zero outside the padded grid: those rows load as zeros and
+      // the frame / padding columns of the temporaries are never written)
+      const T gsxx = GA.v[c] + T(27) * P1.v[c] - T(27) * P2.v[c] - P0.v[c] + P3.v[c];
+      const T gsxy = GC.v[c] + T(27) * f6[1 + c] - T(27) * f6[2 + c] - f6[c] + f6[3 + c] +
+                     T(27) * Q1.v[c] - T(27) * Q2.v[c] - Q0.v[c] + Q3.v[c];
+      const T gsyy = GB.v[c] + T(27) * f8[1 + c] - T(27) * f8[2 + c] - f8[c] + f8[3 + c];
+      oxx[c] = gsxx;
+      oyy[c] = gsyy;
+      oxy[c] = gsxy;
+      // fw1 transpose
+      const T lam_ = T(0.5) * (L1.v[c] + L0.v[c]);
+      const T mu1 = T(0.5) * (U1.v[c] + U0.v[c]);
+      const T lm = lam_ + T(2) * mu1;
+      const T e1 = EA.v[c], e2 = EB.v[c];
+      const T gE1 = M.dt * (lm * gsxx + lam_ * gsyy);
+      const T gE2 = M.dt * (lam_ * gsxx + lm * gsyy);
+      const T glm = M.dt * (e1 * gsxx + e2 * gsyy);
+      const T glam = M.dt * (e2 * gsxx + e1 * gsyy) + glm;
+      ol1[c] = T(0.5) * glam;
+      om1[c] = glm;
+      const bool u1 = k1[c] && rx1, u2 = k1[c] && Y.acti[c];
+      const T gm1 = u1 ? gE1 + g1[o + c] : gE1;
+      const T gm2 = u2 ? gE2 + g2[o + c] : gE2;
+      if (u1) g1[o + c] = bxh * gm1;
+      if (u2) g2[o + c] = Y.bi[c] * gm2;
+      od1[c] = hdiv<T>(gE1 + axh * gm1, M.hx24, M.rhx24);
+      od2[c] = hdiv<T>(gE2 + Y.ai[c] * gm2, M.hy24, M.rhy24);
+      // fw2 transpose
+      const T mu2 = T(0.5) * (ur[c] + ur[c + 1]);
+      const T q = gsxy * mu2 * M.dt;
+      om2[c] = gsxy * EC12.v[c] * M.dt * T(0.5);
+      const bool u3 = k2[c] && rx3, u4 = k2[c] && Y.acth[c];
+      const T gm3 = u3 ? q + g3[o + c] : q;
+      const T gm4 = u4 ? q + g4[o + c] : q;
+      if (u3) g3[o + c] = bxi * gm3;
+      if (u4) g4[o + c] = Y.bh[c] * gm4;
+      od3[c] = hdiv<T>(q + axi * gm3, M.hx24, M.rhx24);
+      od4[c] = hdiv<T>(q + Y.ah[c] * gm4, M.hy24, M.rhy24);
+    }
+    st2<T>(gxx, o, oxx, k12[0], k12[1]);
+    st2<T>(gyy, o, oyy, k12[0], k12[1]);
+    st2<T>(gxy, o, oxy, k12[0], k12[1]);
+    st2<T>(gl1, o, ol1, k1[0], k1[1]);
+    st2<T>(gm1p, o, om1, k1[0], k1[1]);
+    st2<T>(d1, o, od1, k1[0], k1[1]);
+    st2<T>(d2, o, od2, k1[0], k1[1]);
+    st2<T>(gm2p, o, om2, k2[0], k2[1]);
+    st2<T>(d3, o, od3, k2[0], k2[1]);
+    st2<T>(d4p, o, od4, k2[0], k2[1]);
+    P0 = P1; P1 = P2; P2 = P3; P3 = P4;
+    Q0 = Q1; Q1 = Q2; Q2 = Q3; Q3 = Q4;
+    L0 = L1; L1 = L2; U0 = U1; U1 = U2;
+    F6 = F6n; F8 = F8n;
+    GA = GAn; GB = GBn; GC = GCn;
+    EA = EAn; EB = EBn; EC12 = ECn;
+  }
+}
+
+// Adjoint 3 (velocity cells + parameters) of a strip: gather D1..D4 into the
+// velocity adjoints and the lambda / mu / rho parts into the accumulators.
+template <typename T>
+__global__ void __launch_bounds__(EW * 32, el_minb_adj<T>())
+k_el_adj3_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int R, int nwt) {
+  using A = typename ElAcc<T>::type;
+  const int wi = blockIdx.x * EW + (threadIdx.x >> 5);
+  if (wi >= nwt) return;
+  const ElShot<T>& sh = shots[blockIdx.y];
+  const Strip<T> S(M, ncolw, R, wi);
+  const int j = S.j, NX = S.NX, NY = S.NY;
+  T* __restrict__ gvx = sh.g[VX];
+  T* __restrict__ gvy = sh.g[VY];
+  const T* __restrict__ d1 = sh.tmp[D1];
+  const T* __restrict__ d2 = sh.tmp[D2];
+  const T* __restrict__ d3 = sh.tmp[D3];
+  const T* __restrict__ d4p = sh.tmp[D4];
+  const T* __restrict__ gl1 = sh.tmp[GL1];
+  const T* __restrict__ gm1p = sh.tmp[GM1];
+  const T* __restrict__ gm2p = sh.tmp[GM2];
+  const T* __restrict__ r4p = sh.tmp[R4];
+  A* __restrict__ al = ElAcc<T>::lam(sh);
+  A* __restrict__ am = ElAcc<T>::mu(sh);
+  A* __restrict__ ar = ElAcc<T>::rho(sh);
+  bool c3[2], c4[2], cp[2];
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    c3[c] = S.out && j + c >= 2 && j + c <= NY;
+    c4[c] = S.out && j + c >= 1 && j + c <= NY - 1;
+    cp[c] = S.out && j + c >= 1 && j + c <= NY;
+  }
+  const int i0 = S.i0;
+  // windows: D1 rows i-2..i+1, D3 rows i-1..i+2, GL1 / GM1 / R4 rows i-1, i
+  V2<T> P0 = S.row(d1, i0 - 2), P1 = S.row(d1, i0 - 1), P2 = S.row(d1, i0), P3 = S.row(d1, i0 + 1);
+  V2<T> Q0 = S.row(d3, i0 - 1), Q1 = S.row(d3, i0), Q2 = S.row(d3, i0 + 1), Q3 = S.row(d3, i0 + 2);
+  V2<T> GLm = S.row(gl1, i0 - 1), GL0 = S.row(gl1, i0);
+  V2<T> GMm = S.row(gm1p, i0 - 1), GM0 = S.row(gm1p, i0);
+  V2<T> RRm = S.row(r4p, i0 - 1), RR0 = S.row(r4p, i0);
+  V2<T> F2 = S.row(d2, i0), F4 = S.row(d4p, i0), F12 = S.row(gm2p, i0);
+  V2<T> VX0 = S.row(gvx, i0), VY0 = S.row(gvy, i0);
+  V2<A> AL = S.row(al, i0), AM = S.row(am, i0), AR = S.row(ar, i0);
+  for (int i = i0; i < S.i_end; i++) {
+    const int64_t o = S.off(i);
+    const bool more = i + 1 < S.i_end;
+    const int rn = more ? i + 1 : -1;
+    const V2<T> P4 = S.row(d1, more ? i + 2 : -1), Q4 = S.row(d3, more ? i + 3 : -1);
+    const V2<T> GLn = S.row(gl1, rn), GMn = S.row(gm1p, rn), RRn = S.row(r4p, rn);
+    const V2<T> F2n = S.row(d2, rn), F4n = S.row(d4p, rn), F12n = S.row(gm2p, rn);
+    const V2<T> VXn = S.row(gvx, rn), VYn = S.row(gvy, rn);
+    const V2<A> ALn = S.row(al, rn), AMn = S.row(am, rn), ARn = S.row(ar, rn);
+    // row i across columns: D4 at j-2..j+2, D2 at j-1..j+3, GM2 / R4 (rows i-1, i) at j-1..j+1
+    T f4[5], f2[5], g12[3], rm[3], r0[3];
+    f4[0] = shup(F4.v[0]);
+    f4[1] = shup(F4.v[1]);
+    f4[2] = F4.v[0];
+    f4[3] = F4.v[1];
+    f4[4] = shdn(F4.v[0]);
+    f2[0] = shup(F2.v[1]);
+    f2[1] = F2.v[0];
+    f2[2] = F2.v[1];
+    f2[3] = shdn(F2.v[0]);
+    f2[4] = shdn(F2.v[1]);
+    g12[0] = shup(F12.v[1]);
+    g12[1] = F12.v[0];
+    g12[2] = F12.v[1];
+    rm[0] = shup(RRm.v[1]);
+    rm[1] = RRm.v[0];
+    rm[2] = RRm.v[1];
+    r0[0] = shup(RR0.v[1]);
+    r0[1] = RR0.v[0];
+    r0[2] = RR0.v[1];
+    const bool r3 = i >= 2, r4 = i <= NX - 1;
+    T ovx[2], ovy[2];
+    A ol[2], om[2], orr[2];
+    bool k3[2], k4[2];
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      k3[c] = r3 && c3[c];
+      k4[c] = r4 && c4[c];
+      // D1 rows i-2..i+1 = P0..P3; D4 columns jc-2..jc+1 = f4[c..c+3]
+      ovx[c] = VX0.v[c] + (T(27) * P1.v[c] - T(27) * P2.v[c] - P0.v[c] + P3.v[c] +
+                           T(27) * f4[1 + c] - T(27) * f4[2 + c] - f4[c] + f4[3 + c]);
+      // D2 columns jc-1..jc+2 = f2[c..c+3]; D3 rows i-1..i+2 = Q0..Q3
+      ovy[c] = VY0.v[c] + (T(27) * f2[1 + c] - T(27) * f2[2 + c] - f2[c] + f2[3 + c] +
+                           T(27) * Q1.v[c] - T(27) * Q2.v[c] - Q0.v[c] + Q3.v[c]);
+      ol[c] = AL.v[c] + (A)(GL0.v[c] + GLm.v[c]);
+      om[c] = AM.v[c] + (A)(GM0.v[c] + GMm.v[c] + g12[1 + c] + g12[c]);
+      orr[c] = AR.v[c] + (A)(r0[1 + c] + rm[1 + c] + rm[c] + r0[c]);
+    }
+    st2<T>(gvx, o, ovx, k3[0], k3[1]);
+    st2<T>(gvy, o, ovy, k4[0], k4[1]);
+    st2<A>(al, o, ol, cp[0], cp[1]);
+    st2<A>(am, o, om, cp[0], cp[1]);
+    st2<A>(ar, o, orr, cp[0], cp[1]);
+    P0 = P1; P1 = P2; P2 = P3; P3 = P4;
+    Q0 = Q1; Q1 = Q2; Q2 = Q3; Q3 = Q4;
+    GLm = GL0; GL0 = GLn; GMm = GM0; GM0 = GMn; RRm = RR0; RR0 = RRn;
+    F2 = F2n; F4 = F4n; F12 = F12n;
+    VX0 = VXn; VY0 = VYn;
+    AL = ALn; AM = AMn; AR = ARn;
+  }
+}
+
+// End of a checkpoint segment (FP32 plans): accumulators += partials, partials = 0.
+__global__ void k_el_flush_acc(const ElShot<float>* __restrict__ shots, int64_t n) {
+  const ElShot<float>& sh = shots[blockIdx.y];
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    sh.glam[e] += (double)sh.gl32[e];
+    sh.gmu[e] += (double)sh.gm32[e];
+    sh.grho[e] += (double)sh.gr32[e];
+    sh.gl32[e] = 0.0f;
+    sh.gm32[e] = 0.0f;
+    sh.gr32[e] = 0.0f;
+  }
+}
+
 // Sources of slot n (added in order by one thread), then receivers of slot n.
 template <typename T>
 __global__ void k_el_src_rcv(const ElShot<T>* __restrict__ shots, int n, int nt, int record) {
   const ElShot<T>& sh = shots[blockIdx.x];
   if (threadIdx.x == 0) {
+    const T* row = sh.srcv + (int64_t)(n - 1) * sh.nsrc;
     for (int k = 0; k < sh.nsrc; k++) {
-      const int t = sh.src_type[k];
-      if (t < 0 || t > 4) continue;
-      sh.f[t][sh.src_cell[k]] += sh.srcv[(int64_t)(n - 1) * sh.nsrc + k];
+      T* p = sh.src_ptr[k];
+      if (p) *p += row[k];
     }
   }
   if (!record) return;
   __syncthreads();
   for (int r = threadIdx.x; r < sh.nrcv; r += blockDim.x) {
-    const int t = sh.rcv_type[r];
-    sh.traces[(int64_t)r * nt + n] = (t >= 0 && t <= 4) ? sh.f[t][sh.rcv_cell[r]] : T(0);
+    const T* p = sh.rcv_ptr[r];
+    sh.traces[(int64_t)r * nt + n] = p ? *p : T(0);
   }
 }
 
-// Adjoint state += residual of slot n at the receivers.
+// Adjoint state += residual of slot n at the receivers (one thread each).
 template <typename T>
 __global__ void k_el_resid(const ElShot<T>* __restrict__ shots, int n, int nt) {
-  const ElShot<T>& sh = shots[blockIdx.x];
-  for (int r = threadIdx.x; r < sh.nrcv; r += blockDim.x) {
-    const int t = sh.rcv_type[r];
-    if (t < 0 || t > 4) continue;
-    atomicAdd(sh.g[t] + sh.rcv_cell[r], sh.resid[(int64_t)r * nt + n]);
-  }
+  const ElShot<T>& sh = shots[blockIdx.y];
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= sh.nrcv) return;
+  T* p = sh.rcv_gptr[r];
+  if (p) atomicAdd(p, sh.resid[(int64_t)r * nt + n]);
 }
 
 // State <-> checkpoint copies (13 contiguous fields per shot).
@@ -934,6 +1333,8 @@ struct ElPlanBase {
   virtual ~ElPlanBase() = default;
   virtual int forward(const double* l, const double* m, const double* r, void* traces,
                       cudaStream_t st) = 0;
+  virtual int profile(const double* l, const double* m, const double* r, double* out,
+                      cudaStream_t st) = 0;
   virtual int gradient(const double* l, const double* m, const double* r, const void* obs,
                        double* loss, double* gl, double* gm, double* gr, void* tr_out,
                        cudaStream_t st) = 0;
@@ -948,6 +1349,7 @@ struct ElPlan final : ElPlanBase {
   ads_elastic_config cfg{};
   int nshots = 0, K = 0, nseg = 0, NX = 0, NY = 0, NSTEP = 0;
   int ncolw = 0, rows_w = 0, nwt = 0;  // warp strips of the row-streaming step kernels
+  int max_rcv = 0;                      // most receivers of a shot
   int64_t P = 0, fs = 0;
   char* pool = nullptr;
   ElShot<T>* d_shots = nullptr;
@@ -975,6 +1377,13 @@ struct ElPlan final : ElPlanBase {
     return dim3((unsigned)div_up(NY + 2, BX), (unsigned)div_up(NX + 2, BY), (unsigned)nshots);
   }
   dim3 grid_rows() const { return dim3((unsigned)div_up(nwt, EW), (unsigned)nshots); }
+  // sources / receivers: one CTA per shot, a thread per receiver (up to 1024)
+  unsigned rcv_threads() const {
+    return (unsigned)std::min<int64_t>(1024, std::max<int64_t>(32, div_up(max_rcv, 32) * 32));
+  }
+  dim3 grid_resid() const {
+    return dim3((unsigned)std::max<int64_t>(1, div_up(max_rcv, 256)), (unsigned)nshots);
+  }
 
   int create(const ads_elastic_config& c, const ads_elastic_shot* shots, int64_t ns,
              cudaStream_t st);
@@ -983,6 +1392,8 @@ struct ElPlan final : ElPlanBase {
   int issue_reverse(cudaStream_t st, int64_t* count);
   int prep(const double* l, const double* m, const double* r, cudaStream_t st);
   int forward(const double* l, const double* m, const double* r, void* traces,
+              cudaStream_t st) override;
+  int profile(const double* l, const double* m, const double* r, double* out,
               cudaStream_t st) override;
   int gradient(const double* l, const double* m, const double* r, const void* obs,
                double* loss, double* gl, double* gm, double* gr, void* tr_out,
@@ -1001,6 +1412,8 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   ADS_REQUIRE(c.npml >= 1 && c.Rcoef > 0 && c.Rcoef < 1, "invalid CPML parameters");
   ADS_REQUIRE(c.ckpt_every >= 0, "negative ckpt_every");
   nshots = (int)ns;
+  max_rcv = 0;
+  for (int64_t s = 0; s < ns; s++) max_rcv = std::max<int>(max_rcv, (int)shots[s].nrcv);
   NX = (int)c.NX;
   NY = (int)c.NY;
   NSTEP = (int)c.NSTEP;
@@ -1046,7 +1459,8 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   }
   // ---- layout
   struct Off {
-    size_t state, g, tmp, store, ckpt, acc, srcv, scell, stype, rcell, rtype;
+    size_t state, g, tmp, store, ckpt, acc, acc32, srcv, scell, stype, rcell, rtype, sptr, rptr,
+        gptr;
   };
   std::vector<Off> o(ns);
   size_t used = 0;
@@ -1065,6 +1479,7 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   for (int s = 0; s < ns; s++) {
     o[s].g = take(NF * F);
     o[s].acc = take(3 * sizeof(double) * fs);
+    o[s].acc32 = sizeof(T) == 4 ? take(3 * sizeof(float) * fs) : 0;
   }
   zero_adj_off = adj0;
   zero_adj_len = used - adj0;
@@ -1078,6 +1493,9 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
     o[s].stype = take(sizeof(int) * std::max<int64_t>(h.nsrc, 1));
     o[s].rcell = take(sizeof(int64_t) * std::max<int64_t>(h.nrcv, 1));
     o[s].rtype = take(sizeof(int) * std::max<int64_t>(h.nrcv, 1));
+    o[s].sptr = take(sizeof(T*) * std::max<int64_t>(h.nsrc, 1));
+    o[s].rptr = take(sizeof(T*) * std::max<int64_t>(h.nrcv, 1));
+    o[s].gptr = take(sizeof(T*) * std::max<int64_t>(h.nrcv, 1));
   }
   const size_t model_o = take(3 * F);
   const size_t prof_o = take(sizeof(T) * (4 * NX + 4 * NY));
@@ -1129,6 +1547,9 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
     d.glam = (double*)(pool + o[s].acc);
     d.gmu = d.glam + fs;
     d.grho = d.gmu + fs;
+    d.gl32 = sizeof(T) == 4 ? (float*)(pool + o[s].acc32) : nullptr;
+    d.gm32 = d.gl32 ? d.gl32 + fs : nullptr;
+    d.gr32 = d.gl32 ? d.gm32 + fs : nullptr;
     d.traces = d_traces + trace_off[s];
     d.resid = d_resid + trace_off[s];
     d.srcv = (const T*)(pool + o[s].srcv);
@@ -1136,6 +1557,9 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
     d.src_type = (const int*)(pool + o[s].stype);
     d.rcv_cell = (const int64_t*)(pool + o[s].rcell);
     d.rcv_type = (const int*)(pool + o[s].rtype);
+    d.src_ptr = (T* const*)(pool + o[s].sptr);
+    d.rcv_ptr = (T* const*)(pool + o[s].rptr);
+    d.rcv_gptr = (T* const*)(pool + o[s].gptr);
     d.nsrc = (int)h.nsrc;
     d.nrcv = (int)h.nrcv;
     d.fs = fs;
@@ -1158,6 +1582,12 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
       stage.emplace_back((char*)type.data(), (char*)(type.data() + type.size()));
       ADS_CUDA(cudaMemcpyAsync((void*)d.src_type, stage.back().data(), stage.back().size(),
                                cudaMemcpyHostToDevice, st));
+      std::vector<T*> ptr(h.nsrc);
+      for (int64_t k = 0; k < h.nsrc; k++)
+        ptr[k] = (type[k] >= 0 && type[k] <= 4) ? d.f[type[k]] + cell[k] : nullptr;
+      stage.emplace_back((char*)ptr.data(), (char*)(ptr.data() + ptr.size()));
+      ADS_CUDA(cudaMemcpyAsync((void*)d.src_ptr, stage.back().data(), stage.back().size(),
+                               cudaMemcpyHostToDevice, st));
     }
     if (h.nrcv > 0) {
       std::vector<int64_t> cell(h.nrcv);
@@ -1171,6 +1601,18 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
                                cudaMemcpyHostToDevice, st));
       stage.emplace_back((char*)type.data(), (char*)(type.data() + type.size()));
       ADS_CUDA(cudaMemcpyAsync((void*)d.rcv_type, stage.back().data(), stage.back().size(),
+                               cudaMemcpyHostToDevice, st));
+      std::vector<T*> ptr(h.nrcv), gptr(h.nrcv);
+      for (int64_t k = 0; k < h.nrcv; k++) {
+        const bool ok = type[k] >= 0 && type[k] <= 4;
+        ptr[k] = ok ? d.f[type[k]] + cell[k] : nullptr;
+        gptr[k] = ok ? d.g[type[k]] + cell[k] : nullptr;
+      }
+      stage.emplace_back((char*)ptr.data(), (char*)(ptr.data() + ptr.size()));
+      ADS_CUDA(cudaMemcpyAsync((void*)d.rcv_ptr, stage.back().data(), stage.back().size(),
+                               cudaMemcpyHostToDevice, st));
+      stage.emplace_back((char*)gptr.data(), (char*)(gptr.data() + gptr.size()));
+      ADS_CUDA(cudaMemcpyAsync((void*)d.rcv_gptr, stage.back().data(), stage.back().size(),
                                cudaMemcpyHostToDevice, st));
     }
   }
@@ -1227,7 +1669,7 @@ int ElPlan<T>::step(cudaStream_t st, int n, bool store, int slot, bool record) {
                                                                    nwt, 0);
     ADS_LAUNCHED(1);
   }
-  k_el_src_rcv<T><<<nshots, 128, 0, st>>>(d_shots, n, NSTEP + 1, record ? 1 : 0);
+  k_el_src_rcv<T><<<nshots, rcv_threads(), 0, st>>>(d_shots, n, NSTEP + 1, record ? 1 : 0);
   ADS_LAUNCHED(1);
   return ADS_OK;
 }
@@ -1257,14 +1699,15 @@ int ElPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     int64_t c = 1;
     for (int s = nseg - 1; s >= 0; s--) {
       const int a = 1 + s * K, b = std::min(a + K - 1, NSTEP);
-      c += 1 + 3 * (b - a + 1) + 3 * (b - a + 1) + (b - std::max(a, 2) + 1);
+      c += 1 + 3 * (b - a + 1) + 3 * (b - a + 1) + (b - std::max(a, 2) + 1) +
+           (sizeof(T) == 4 ? 1 : 0);
     }
     *count = c;
     return ADS_OK;
   }
   const ElShot<T> none{};
   ADS_CUDA(cudaMemsetAsync(pool + zero_adj_off, 0, zero_adj_len, st));
-  k_el_resid<T><<<nshots, 128, 0, st>>>(d_shots, NSTEP, NSTEP + 1);
+  k_el_resid<T><<<grid_resid(), 256, 0, st>>>(d_shots, NSTEP, NSTEP + 1);
   ADS_LAUNCHED(1);
   for (int s = nseg - 1; s >= 0; s--) {
     const int a = 1 + s * K, b = std::min(a + K - 1, NSTEP);
@@ -1273,18 +1716,22 @@ int ElPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     for (int n = a; n <= b; n++)
       if (int e = step(st, n, true, n - a, false)) return e;
     for (int n = b; n >= a; n--) {
-      k_el_adj1<T, false><<<grid3(), dim3(BX, BY), 0, st>>>(M, d_shots, none, n - a);
+      k_el_adj1_rows<T><<<grid_rows(), EW * 32, 0, st>>>(M, d_shots, ncolw, rows_w, nwt, n - a);
       ADS_LAUNCHED(1);
-      k_el_adj2<T, false><<<grid3(), dim3(BX, BY), 0, st>>>(M, d_shots, none, n - a);
+      k_el_adj2_rows<T><<<grid_rows(), EW * 32, 0, st>>>(M, d_shots, ncolw, rows_w, nwt, n - a);
       ADS_LAUNCHED(1);
-      k_el_adj3<T, false><<<grid3(), dim3(BX, BY), 0, st>>>(M, d_shots, none);
+      k_el_adj3_rows<T><<<grid_rows(), EW * 32, 0, st>>>(M, d_shots, ncolw, rows_w, nwt);
       ADS_LAUNCHED(1);
       // the adjoint state now refers to slot n-1: add its residual (slot 0 is
       // the constant zero state and takes none)
       if (n - 1 >= 1) {
-        k_el_resid<T><<<nshots, 128, 0, st>>>(d_shots, n - 1, NSTEP + 1);
+        k_el_resid<T><<<grid_resid(), 256, 0, st>>>(d_shots, n - 1, NSTEP + 1);
         ADS_LAUNCHED(1);
       }
+    }
+    if constexpr (sizeof(T) == 4) {
+      k_el_flush_acc<<<dim3(256, nshots), 256, 0, st>>>(d_shots, fs);
+      ADS_LAUNCHED(1);
     }
   }
   return ADS_OK;
@@ -1342,6 +1789,62 @@ int ElPlan<T>::gradient(const double* l, const double* m, const double* r, const
   if (tr_out)
     ADS_CUDA(cudaMemcpyAsync(tr_out, d_traces, sizeof(T) * trace_total,
                              cudaMemcpyDeviceToDevice, st));
+  return ADS_OK;
+}
+
+// Per-kernel durations: each step kernel of the plan launched kProfileReps
+// times back to back on the plan's buffers between two events (direct
+// launches; the state is scratch afterwards and the next forward / gradient
+// starts from zero as always).  out[2k] = ms per launch, out[2k+1] = interior
+// cell-updates per launch, for k = stress, velocity, stress (storing),
+// velocity (storing), adjoint 1, adjoint 2, adjoint 3, sources / receivers,
+// residual injection.
+template <typename T>
+int ElPlan<T>::profile(const double* l, const double* m, const double* r, double* out,
+                       cudaStream_t st) {
+  ADS_REQUIRE(out, "null argument");
+  if (int e = prep(l, m, r, st)) return e;
+  constexpr int kProfileReps = 20;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  ADS_CUDA(cudaEventCreate(&e0));
+  ADS_CUDA(cudaEventCreate(&e1));
+  const double cells = (double)nshots * NX * NY;
+  auto timed = [&](int k, auto&& launch) -> int {
+    launch();  // warm-up
+    ADS_CUDA(cudaEventRecord(e0, st));
+    for (int rep = 0; rep < kProfileReps; rep++) launch();
+    ADS_CUDA(cudaEventRecord(e1, st));
+    ADS_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    ADS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    out[2 * k] = ms / kProfileReps;
+    out[2 * k + 1] = cells;
+    return ADS_OK;
+  };
+  const dim3 g = grid_rows(), b(EW * 32);
+  int rc = ADS_OK;
+  auto run = [&](int k, auto&& launch) {
+    if (rc == ADS_OK) rc = timed(k, launch);
+  };
+  ADS_CUDA(cudaMemsetAsync(pool + zero_fwd_off, 0, zero_fwd_len, st));
+  ADS_CUDA(cudaMemsetAsync(pool + zero_adj_off, 0, zero_adj_len, st));
+  run(0, [&] { k_el_stress_rows<T, false><<<g, b, 0, st>>>(M, d_shots, ncolw, rows_w, nwt, 0); });
+  run(1, [&] { k_el_velocity_rows<T, false><<<g, b, 0, st>>>(M, d_shots, ncolw, rows_w, nwt, 0); });
+  run(2, [&] { k_el_stress_rows<T, true><<<g, b, 0, st>>>(M, d_shots, ncolw, rows_w, nwt, 0); });
+  run(3, [&] { k_el_velocity_rows<T, true><<<g, b, 0, st>>>(M, d_shots, ncolw, rows_w, nwt, 0); });
+  run(4, [&] { k_el_adj1_rows<T><<<g, b, 0, st>>>(M, d_shots, ncolw, rows_w, nwt, 0); });
+  run(5, [&] { k_el_adj2_rows<T><<<g, b, 0, st>>>(M, d_shots, ncolw, rows_w, nwt, 0); });
+  run(6, [&] { k_el_adj3_rows<T><<<g, b, 0, st>>>(M, d_shots, ncolw, rows_w, nwt); });
+  run(7, [&] { k_el_src_rcv<T><<<nshots, rcv_threads(), 0, st>>>(d_shots, 1, NSTEP + 1, 1); });
+  run(8, [&] { k_el_resid<T><<<grid_resid(), 256, 0, st>>>(d_shots, 1, NSTEP + 1); });
+  ADS_LAUNCHED(9 * (kProfileReps + 1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != ADS_OK) return rc;
+  ADS_CUDA(cudaGetLastError());
+  // leave zeroed state behind
+  ADS_CUDA(cudaMemsetAsync(pool + zero_fwd_off, 0, zero_fwd_len, st));
+  ADS_CUDA(cudaMemsetAsync(pool + zero_adj_off, 0, zero_adj_len, st));
   return ADS_OK;
 }
 
@@ -1648,6 +2151,12 @@ int ads_elastic_plan_gradient(ads_elastic_plan* plan, const double* lambda, cons
   ADS_REQUIRE(plan, "null plan");
   return plan->impl->gradient(lambda, mu, rho, observed, loss, grad_lambda, grad_mu, grad_rho,
                               traces_out, (cudaStream_t)stream);
+}
+
+int ads_elastic_plan_profile(ads_elastic_plan* plan, const double* lambda, const double* mu,
+                             const double* rho, double* out, ads_stream_t stream) {
+  ADS_REQUIRE(plan, "null plan");
+  return plan->impl->profile(lambda, mu, rho, out, (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -354,11 +354,36 @@ def run_elastic_fwi(args):
     ms = _timed(lambda: plan.gradient(l0, m0, r0, obs), args.steps, args.warmup)
     n = len(shots)
     cells = 2 * n * p.NX * p.NY * p.NSTEP
+    # roofline: algorithmic bytes per cell-update, forward (13 + 16 f_pml) x 4 B
+    # (5 fields read + written, lambda / mu / rho, 8 memory variables in CPML
+    # cells), adjoint step = forward + 68 B
+    f_pml = 1 - (p.NX - 2 * p.NPOINTS_PML) * (p.NY - 2 * p.NPOINTS_PML) / (p.NX * p.NY)
+    b_fwd = (13 + 16 * f_pml) * 4
+    b_adj = b_fwd + 68
+    prof = plan.profile(l0, m0, r0)
+    peak, peak_kind = measured_peak()
+    fwd_ms = prof["stress"][0] + prof["velocity"][0]
+    adj_ms = prof["adj1"][0] + prof["adj2"][0] + prof["adj3"][0]
+    c1 = prof["stress"][1]
+    groups = {
+        "k_el_stress_rows+k_el_velocity_rows": (fwd_ms, b_fwd * c1),
+        "k_el_adj1_rows+k_el_adj2_rows+k_el_adj3_rows": (adj_ms, b_adj * c1),
+    }
+    kern = {k: {"ms_per_step": round(t, 4), "achieved_gbs": round(b / (t / 1e3) / 1e9, 1),
+                "frac": round(b / (t / 1e3) / 1e9 / peak, 4)} for k, (t, b) in groups.items()}
+    kern.update({k: {"ms_per_launch": round(v[0], 4)} for k, v in prof.items()})
+    dom = "k_el_adj1_rows+k_el_adj2_rows+k_el_adj3_rows"
+    t, b = groups[dom]
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(b / (t / 1e3) / 1e9, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(b / (t / 1e3) / 1e9 / peak, 4),
+                "peak_source": peak_kind, "traffic": None, "bytes_per_launch": b,
+                "bytes_per_cell": {"forward": b_fwd, "adjoint": b_adj, "f_pml": round(f_pml, 4)},
+                "kernels": kern}
     _line("elastic FWI shot-gradients/s (FP32 stencils, FP64 accumulation)", n / (ms / 1e3),
           "shot-gradients/s", args, ms, "f32",
           f"elastic CPML gradient {p.NX}x{p.NY} (CPML {p.NPOINTS_PML}), {p.NSTEP} steps, "
           f"{n} explosive shots x 300 two-component receivers",
-          {"gcell_updates_per_s": cells / (ms / 1e3) / 1e9,
+          {"gcell_updates_per_s": cells / (ms / 1e3) / 1e9, "roofline": roofline,
            "device_bytes": plan.device_bytes, "gpu_launches": int(plan.launches_gradient)})
     plan.close()
 
