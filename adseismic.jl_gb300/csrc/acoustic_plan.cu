@@ -38,26 +38,45 @@ constexpr unsigned FULL = 0xffffffffu;
 #ifndef ADS_PF32
 #define ADS_PF32 1
 #endif
+#ifndef ADS_MINB_F32
+#define ADS_MINB_F32 8    // 64 registers
+#endif
 #ifndef ADS_MINB_A32
-#define ADS_MINB_A32 3
+#define ADS_MINB_A32 5    // 102 -> 96 registers
+#endif
+#ifndef ADS_MINB_FI32
+#define ADS_MINB_FI32 16  // 32 registers: every warp slot of the SM
+#endif
+#ifndef ADS_MINB_AI32
+#define ADS_MINB_AI32 9   // 56 registers
 #endif
 
 
-// Tiles: a CTA owns `J` columns x rows_per_thread rows of one shot.  The
-// forward step gives each thread CF adjacent columns, the adjoint CA (fewer,
-// it carries more state per cell); rows are loaded as 16/8-byte vectors.
+// Tiles: a warp owns a strip of 32 x CF (forward) or 32 x CA (adjoint)
+// columns and rows_per_thread rows of one shot; each thread owns CF / CA
+// adjacent columns, loaded as one 8/16-byte vector per row.  J is the column
+// width of the per-segment helpers' tiles.
 template <typename T>
 struct Tile {
   static constexpr int J = sizeof(T) == 4 ? 512 : 256;
   static constexpr int CF = sizeof(T) == 4 ? 2 : 2;
   static constexpr int CA = sizeof(T) == 4 ? 2 : 1;
-  static constexpr int NF = J / CF;  // forward threads per CTA (128)
-  static constexpr int NA = J / CA;  // adjoint threads per CTA (256)
-  static constexpr int NC = 128;     // threads of the column-loop helpers
   // rows of register prefetch in the interior loops (bytes in flight per warp)
   static constexpr int PF = sizeof(T) == 4 ? ADS_PF32 : 1;
-  // resident CTAs per SM the adjoint's register allocation must allow
-  static constexpr int MINB_A = sizeof(T) == 4 ? ADS_MINB_A32 : 2;
+  // Step kernels: a CTA of G warps takes one item (a column strip of one
+  // shot); its warps take consecutive tiles of rows.  The item is uniform over
+  // the CTA, so its fields and everything derived from them stay in uniform
+  // registers.
+  static constexpr int G = 4;
+  static constexpr int TPB = 32 * G;
+  static constexpr int WF = 32 * CF;  // columns of a forward strip
+  static constexpr int WA = 32 * CA;  // columns of an adjoint strip
+  // resident CTAs of TPB threads per SM the register allocation must allow
+  // (general / interior-only kernels; 65536 / (TPB x MINB) registers a thread)
+  static constexpr int MINB_F = sizeof(T) == 4 ? ADS_MINB_F32 : 4;
+  static constexpr int MINB_A = sizeof(T) == 4 ? ADS_MINB_A32 : 4;
+  static constexpr int MINB_FI = sizeof(T) == 4 ? ADS_MINB_FI32 : 6;
+  static constexpr int MINB_AI = sizeof(T) == 4 ? ADS_MINB_AI32 : 5;
 };
 
 template <typename T, int C>
@@ -68,7 +87,7 @@ struct alignas(sizeof(T) * C) Vec {
 struct CellRef {
   int64_t cell;  // element offset inside the shot's pitched field
   int idx;       // source / receiver index within the shot
-  int pad;
+  int row;       // its row (1-based padded grid)
 };
 
 struct AcItem {
@@ -156,6 +175,18 @@ __device__ __forceinline__ bool warp_tau_free(const T* __restrict__ ty, int j, i
   return __all_sync(FULL, z);
 }
 
+// L2 prefetch of a row segment (one warp-wide instruction per array): a hint
+// that starts the DRAM read of a row the warp reaches ADS_L2PF rows later, so
+// its own load finds it in L2.  Only addresses the kernel will load anyway are
+// given (the same row / column predicates).
+#ifndef ADS_L2PF
+#define ADS_L2PF 0
+#endif
+template <typename T>
+__device__ __forceinline__ void l2pf(const T* p, bool on) {
+  if (ADS_L2PF > 0 && on) asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // True when the warp's columns are tau-free and sigma is zero on rows
 // i0-1 .. i_end (every row a tile of rows [i0, i_end) reads): phi, psi and
 // their adjoints are then zero throughout and the interior update applies.
@@ -167,30 +198,32 @@ __device__ __forceinline__ bool interior_rows(bool tfree, const T* __restrict__ 
   return tfree && __all_sync(FULL, z);
 }
 
-// Each warp records the receivers in its own columns after a forward step:
-// their cells were written by its lanes, so a warp barrier suffices.
+// Each warp records the receivers in its own cells (its strip's columns, its
+// rows) after a forward step: its lanes wrote them, so a warp barrier suffices.
 template <typename T, int C, bool SEG>
 __device__ __forceinline__ void record_traces(const AcItem& it, const AcShot<T>& sh,
                                               const CellRef* __restrict__ rcvs, const T* out,
-                                              int t, int lane) {
+                                              int t, int lane, int i0, int i_end) {
   if (SEG || it.rcv_e <= it.rcv_b) return;
   __syncwarp();
-  const int wj0 = it.j0 + (threadIdx.x >> 5) * 32 * C;
   for (int e = it.rcv_b + lane; e < it.rcv_e; e += 32) {
-    const CellRef r = rcvs[e];
-    const int rj = (int)(r.cell % sh.pitch) - JOFF;
-    if (rj >= wj0 && rj < wj0 + 32 * C) sh.traces[(int64_t)t * sh.nrcv + r.idx] = out[r.cell];
+    const CellRef r = rcvs[e];  // r.row: the receiver's row
+    if (r.row >= i0 && r.row < i_end) sh.traces[(int64_t)t * sh.nrcv + r.idx] = out[r.cell];
   }
 }
 
 // One forward step (variant W: phi/psi from the old field).  SEG=false: rings
 // of two (u_t written over u_{t-2}), optional checkpoint write; SEG=true:
-// segment store addressed by slot t - base.  Each thread owns CF adjacent
-// columns of the tile, walks down its rows with the next row's loads issued
-// one iteration ahead, and takes the j-neighbours of its edge cells from the
-// neighbouring lanes (warp-edge lanes load them).
-template <typename T, bool SEG>
-__global__ void __launch_bounds__(Tile<T>::NF)
+// segment store addressed by slot t - base.  Every warp takes one item (a
+// 32*CF-column strip of rows of one shot); each thread owns CF adjacent
+// columns, walks down the rows with the next row's loads issued one iteration
+// ahead, and takes the j-neighbours of its edge cells from the neighbouring
+// lanes (warp-edge lanes load them).  INT = true: the item is interior
+// (sigma = tau = 0 on every row and column it reads, classified on the host)
+// and only the plain wave update is compiled, so the kernel needs few
+// registers and keeps many warps resident; INT = false: the general PML form.
+template <typename T, bool SEG, bool INT>
+__global__ void __launch_bounds__(Tile<T>::TPB, INT ? Tile<T>::MINB_FI : Tile<T>::MINB_F)
 k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
          const CellRef* __restrict__ srcs, const CellRef* __restrict__ rcvs, AcConst<T> K,
          int t, int base, int ckpt_slot, int ri) {
@@ -199,7 +232,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   const AcItem it = items[blockIdx.x];
   const AcShot<T>& sh = shots[it.shot];
   const int lane = threadIdx.x & 31;
-  const int j = it.j0 + threadIdx.x * C;
+  const int j = it.j0 + lane * C;
   const int nx = sh.nx, ny = sh.ny;
   const int64_t P = sh.pitch, fs = sh.fs;
   const T *w, *wo;
@@ -229,13 +262,14 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   for (int c = 0; c < C; c++) tj[c] = (j + c <= ny + 1) ? ty[j + c] : T(0);
   const bool tfree = warp_tau_free<T, C>(ty, j, ny);
   auto nz = [&](int r) { return !(tfree && sx[r] == T(0)); };  // phi/psi may be non-zero
-  const int i0 = it.i0, i_end = min(i0 + ri, nx + 1);
+  const int i0 = it.i0 + (threadIdx.x >> 5) * ri, i_end = min(i0 + ri, nx + 1);
+  if (i0 > nx) return;  // whole warps only: every later barrier is warp-level
   auto off = [&](int r) { return (int64_t)r * P + col; };
   const bool ck_on = !SEG && ckpt_slot > 0 && ckpt_slot < sh.nseg;
-  if (interior_rows<T>(tfree, sx, i0, i_end, lane)) {
-    // Interior tile: sigma = tau = 0 on every row and column the warp reads,
+  if (INT || interior_rows<T>(tfree, sx, i0, i_end, lane)) {
+    // Interior item: sigma = tau = 0 on every row and column the warp reads,
     // so phi = psi = 0 there and the step reduces to the plain wave update
-    // (the dropped terms are exact zeros).
+    // (the dropped terms are exact zeros); it holds no source or receiver.
     // Register queues PF rows deep: w rows i-1 .. i+PF, wo / c / halo rows
     // i .. i+PF-1; each iteration issues the loads of the farthest rows.
     constexpr int PF = Tile<T>::PF;
@@ -259,6 +293,12 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     for (int i = i0; i < i_end; i++) {
       const int64_t row = off(i);
       const int rn = i + PF;  // farthest row of the wo / c / halo queues
+      {
+        const int rp = rn + ADS_L2PF;
+        l2pf(w + off(rp + 1), jld && rp + 1 <= i_end);
+        l2pf(wo + off(rp), jld && rp < i_end);
+        l2pf(cc + off(rp), jld && rp < i_end);
+      }
       V wn = ldv<T, C>(w, off(rn + 1), jld && rn + 1 <= i_end);
       V on = ldv<T, C>(wo, off(rn), jld && rn < i_end);
       V cn = ldv<T, C>(cc, off(rn), jld && rn < i_end);
@@ -278,9 +318,11 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
           const T cv = cq[0].v[c];
           T v = (T(2) - K.kxy * cv) * w0.v[c] + cv * K.cx * (wp.v[c] + wm.v[c]) +
                 cv * K.cy * (wN + wS) - oq[0].v[c];
-          for (int e = it.src_b; e < it.src_e; e++) {
-            const CellRef r = srcs[e];
-            if (r.cell == row + c) v += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
+          if constexpr (!INT) {
+            for (int e = it.src_b; e < it.src_e; e++) {
+              const CellRef r = srcs[e];
+              if (r.cell == row + c) v += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
+            }
           }
           vo.v[c] = v;
         }
@@ -304,9 +346,8 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       cq[PF - 1] = cn;
       hq[PF - 1] = hn;
     }
-    record_traces<T, C, SEG>(it, sh, rcvs, out, t, lane);
-    return;
-  }
+    if constexpr (!INT) record_traces<T, C, SEG>(it, sh, rcvs, out, t, lane, i0, i_end);
+  } else {
   bool n0 = nz(i0);
   V wm = ldv<T, C>(w, off(i0 - 1), jld), w0 = ldv<T, C>(w, off(i0), jld),
     wp = ldv<T, C>(w, off(i0 + 1), jld);
@@ -326,6 +367,16 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     const int64_t row = off(i);
     const bool more = i + 1 < i_end;
     const bool n1 = more && nz(i + 1);
+    {
+      const int rp = i + 1 + ADS_L2PF;
+      const bool on = jld && rp < i_end;
+      l2pf(w + off(rp + 1), on);
+      l2pf(wo + off(rp), on);
+      l2pf(cc + off(rp), on);
+      const bool pz = on && nz(rp);
+      l2pf(pin + off(rp + 1), pz);
+      l2pf(qin + off(rp), pz);
+    }
     V wn = ldv<T, C>(w, off(i + 2), jld && more);
     V pn_ = ldv<T, C>(pin, off(i + 2), jld && more && nz(i + 2));
     V qn = ldv<T, C>(qin, off(i + 1), jld && n1);
@@ -400,34 +451,29 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     hq = hqn;
     n0 = n1;
   }
-  record_traces<T, C, SEG>(it, sh, rcvs, out, t, lane);
+  record_traces<T, C, SEG>(it, sh, rcvs, out, t, lane, i0, i_end);
+  }
 }
 
 // Restore checkpoint `slot` of every active shot into the segment store
 // (slot 0 <- u_{a-2}, slot 1 <- u_{a-1}) and the phi/psi rings at a-1.
 template <typename T>
-__global__ void __launch_bounds__(Tile<T>::NC)
-k_ac_restore(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
-             int slot, int a, int ri, int pset) {
-  const AcItem it = items[blockIdx.x];
-  const AcShot<T>& sh = shots[it.shot];
+__global__ void __launch_bounds__(256)
+k_ac_restore(const AcShot<T>* __restrict__ shots, int slot, int a, int pset) {
+  const AcShot<T>& sh = shots[blockIdx.y];
   const int64_t P = sh.pitch, fs = sh.fs;
   const T* ck = sh.ckpt + (int64_t)slot * 4 * fs;
   const int ps = pset >= 0 ? pset : ((a - 1) & 1);  // phi/psi set the recompute reads
   T* pr = sh.p + (int64_t)ps * fs;
   T* qr = sh.q + (int64_t)ps * fs;
-  const int i_end = min(it.i0 + ri, sh.nx + 1);
-  const int j_end = min(it.j0 + Tile<T>::J, sh.ny + 1);
-  for (int j = it.j0 + threadIdx.x; j < j_end; j += blockDim.x) {
-    const int64_t col = j + JOFF;
-    for (int i = it.i0; i < i_end; i++) {
-      const int64_t row = (int64_t)i * P + col;
+  for (int i = 1 + blockIdx.x; i <= sh.nx; i += gridDim.x)
+    for (int j = 1 + threadIdx.x; j <= sh.ny; j += blockDim.x) {
+      const int64_t row = (int64_t)i * P + j + JOFF;
       sh.seg[row] = ck[fs + row];
       sh.seg[fs + row] = ck[row];
       pr[row] = ck[2 * fs + row];
       qr[row] = ck[3 * fs + row];
     }
-  }
 }
 
 // One cell's j-direction adjoint terms: YP (to its j+1 neighbour), YM (to its
@@ -489,14 +535,12 @@ __device__ __forceinline__ void add_grad(const AcShot<T>& sh, int64_t row, const
 template <typename T, int C>
 __device__ __forceinline__ void inject_residuals(const AcItem& it, const AcShot<T>& sh,
                                                  const CellRef* __restrict__ rcvs, T* lun, int k,
-                                                 int lane) {
+                                                 int lane, int i0, int i_end) {
   if (k - 1 < 2 || it.rcv_e <= it.rcv_b) return;
   __syncwarp();
-  const int wj0 = it.j0 + (threadIdx.x >> 5) * 32 * C;
   for (int e = it.rcv_b + lane; e < it.rcv_e; e += 32) {
     const CellRef r = rcvs[e];
-    const int rj = (int)(r.cell % sh.pitch) - JOFF;
-    if (rj >= wj0 && rj < wj0 + 32 * C)
+    if (r.row >= i0 && r.row < i_end)
       atomicAdd(lun + r.cell, sh.resid[(int64_t)(k - 1) * sh.nrcv + r.idx]);
   }
 }
@@ -511,8 +555,9 @@ __device__ __forceinline__ void inject_residuals(const AcItem& it, const AcShot<
 // FP32 plans add the grad_c contribution to a per-segment FP32 partial
 // (flushed into the FP64 accumulator at the end of each segment); FP64 plans
 // accumulate in FP64.
-template <typename T>
-__global__ void __launch_bounds__(Tile<T>::NA, Tile<T>::MINB_A)
+// Items, warps and INT as in k_ac_fwd.
+template <typename T, bool INT>
+__global__ void __launch_bounds__(Tile<T>::TPB, INT ? Tile<T>::MINB_AI : Tile<T>::MINB_A)
 k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
          const CellRef* __restrict__ rcvs, AcConst<T> K, int k, int base, int ri) {
   constexpr int C = Tile<T>::CA;
@@ -520,7 +565,7 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   const AcItem it = items[blockIdx.x];
   const AcShot<T>& sh = shots[it.shot];
   const int lane = threadIdx.x & 31;
-  const int j = it.j0 + threadIdx.x * C;
+  const int j = it.j0 + lane * C;
   const int nx = sh.nx, ny = sh.ny;
   const int64_t P = sh.pitch, fs = sh.fs;
   const T* w = sh.seg + (int64_t)(k - 1 - base) * fs;   // u_{k-1}
@@ -546,8 +591,9 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   const bool hon = (lane == 0 && jld) || (lane == 31 && hr);
   const T th = hon ? ty[j + (int)hoff] : T(0);
   auto off = [&](int r) { return (int64_t)r * P + col; };
-  const int i0 = it.i0, i_end = min(i0 + ri, nx + 1);
-  if (interior_rows<T>(tfree, sx, i0, i_end, lane)) {
+  const int i0 = it.i0 + (threadIdx.x >> 5) * ri, i_end = min(i0 + ri, nx + 1);
+  if (i0 > nx) return;  // whole warps only: every later barrier is warp-level
+  if (INT || interior_rows<T>(tfree, sx, i0, i_end, lane)) {
     // Interior tile (1/den = 1, lambdaPhi = lambdaPsi = 0): the transpose of
     // the plain wave update; rows i-1 (m), i (0), i+1 (1) of lambdaU_k and c.
     // Register queues PF rows deep: lambdaU_k, c, u_{k-1} rows i-1 .. i+PF;
@@ -586,6 +632,15 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     for (int i = i0; i < i_end; i++) {
       const int64_t row = off(i);
       const int rn = i + PF;
+      {
+        const int rp = rn + ADS_L2PF;
+        const bool p1 = jld && rp + 1 <= i_end, p0 = jld && rp < i_end;
+        l2pf(luc + off(rp + 1), p1);
+        l2pf(cc + off(rp + 1), p1);
+        l2pf(w + off(rp + 1), p1);
+        l2pf(lun + off(rp), p0);
+        l2pf(gb + off(rp), p0);
+      }
       const bool on1 = jld && rn + 1 <= i_end, on0 = jld && rn < i_end;
       V un = ldv<T, C>(luc, off(rn + 1), on1);
       V cn = ldv<T, C>(cc, off(rn + 1), on1);
@@ -652,9 +707,8 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       hcq[PF - 1] = hcn;
       hwq[PF - 1] = hwn;
     }
-    inject_residuals<T, C>(it, sh, rcvs, lun, k, lane);
-    return;
-  }
+    if constexpr (!INT) inject_residuals<T, C>(it, sh, rcvs, lun, k, lane, i0, i_end);
+  } else {
   // rows i-1 (m), i (0), i+1 (p): lambdaU_k, lambdaPhi_k, c and 1/den per cell
   V gum = ldv<T, C>(luc, off(i0 - 1), jld), gpm = ldv<T, C>(lpc, off(i0 - 1), jld && nz(i0 - 1)),
     cm = ldv<T, C>(cc, off(i0 - 1), jld);
@@ -691,6 +745,18 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     // lambdaU_{k+1}) and the halo cell of row i+1
     const bool more = i + 1 < i_end;
     const bool n1 = more && nz(i + 1);
+    {
+      const int rp = i + 1 + ADS_L2PF;
+      const bool on = jld && rp < i_end;
+      l2pf(luc + off(rp + 1), on);
+      l2pf(cc + off(rp + 1), on);
+      l2pf(w + off(rp + 1), on);
+      l2pf(lun + off(rp), on);
+      const bool pz = on && nz(rp);
+      l2pf(lpc + off(rp + 1), pz);
+      l2pf(lqc + off(rp), pz);
+      if (sizeof(T) == 4) l2pf(sh.gc32 + off(rp), on);
+    }
     V gu2 = ldv<T, C>(luc, off(i + 2), jld && more);
     V gp2 = ldv<T, C>(lpc, off(i + 2), jld && more && nz(i + 2));
     V c2 = ldv<T, C>(cc, off(i + 2), jld && more);
@@ -763,7 +829,8 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     hgu = hgun; hgq = hgqn; hc = hcn; hw = hwn;
     n0 = n1;
   }
-  inject_residuals<T, C>(it, sh, rcvs, lun, k, lane);
+  inject_residuals<T, C>(it, sh, rcvs, lun, k, lane, i0, i_end);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -960,19 +1027,15 @@ k_ac_fwd_tb(const TbItem* __restrict__ items, const AcShot<T>* __restrict__ shot
 // End of a segment (FP32 plans): grad_c (FP64) += the segment's FP32 partial,
 // which is reset to zero.
 template <typename T>
-__global__ void __launch_bounds__(Tile<T>::NC)
-k_ac_flush_gc(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots, int ri) {
-  const AcItem it = items[blockIdx.x];
-  const AcShot<T>& sh = shots[it.shot];
-  const int i_end = min(it.i0 + ri, sh.nx + 1);
-  const int j_end = min(it.j0 + Tile<T>::J, sh.ny + 1);
-  for (int j = it.j0 + threadIdx.x; j < j_end; j += blockDim.x) {
-    for (int i = it.i0; i < i_end; i++) {
+__global__ void __launch_bounds__(256)
+k_ac_flush_gc(const AcShot<T>* __restrict__ shots) {
+  const AcShot<T>& sh = shots[blockIdx.y];
+  for (int i = 1 + blockIdx.x; i <= sh.nx; i += gridDim.x)
+    for (int j = 1 + threadIdx.x; j <= sh.ny; j += blockDim.x) {
       const int64_t row = (int64_t)i * sh.pitch + j + JOFF;
       sh.gc[row] += (double)sh.gc32[row];
       sh.gc32[row] = 0.f;
     }
-  }
 }
 
 // c = vp^2 over each shot's padded window (frames included: their c is read,
@@ -1099,38 +1162,55 @@ struct AcPlan final : AcPlanBase {
   std::vector<int> order;         // shot order (record length descending)
   std::vector<int> nstep;         // per sorted shot
   std::vector<int> nxs;           // per sorted shot: window width
-  std::vector<int> item_shot_end; // per sorted shot: adjoint tiles of shots [0..s]
-  std::vector<int> itemf_shot_end; // per sorted shot: forward tiles of shots [0..s]
   int ri_f = 8;                    // rows per thread of the forward tiles
-  AcItem* d_items_f = nullptr;
-  CellRef *d_srcs_f = nullptr, *d_rcvs_f = nullptr;
   // per sorted shot, 0-based (i, j, index) of interior sources / receivers
   std::vector<std::vector<int3>> hsrc, hrcv;
+  // per sorted shot: the PML profiles the kernels read (host copies)
+  std::vector<std::vector<double>> hsx;
+  std::vector<double> hty;
+  // Warp items of one kernel: interior items (sigma = tau = 0 on every row and
+  // column they read) and PML items, each in sorted-shot order, so the items
+  // of the first n shots are a prefix of either part.
   struct TileList {
-    std::vector<AcItem> items;
+    std::vector<AcItem> in, pm;
+    std::vector<int> in_end, pm_end;  // per sorted shot: items of shots [0..s]
     std::vector<CellRef> srcs, rcvs;
-    std::vector<int> shot_end;
   };
-  void build_tiles(int rows, int64_t pitch, TileList& L) const;
-  int upload_tiles(const TileList& L, AcItem* di, CellRef* ds, CellRef* dr, cudaStream_t st);
+  struct DevTiles {
+    AcItem* items = nullptr;  // interior items, then the PML items at pm_off
+    CellRef *srcs = nullptr, *rcvs = nullptr;
+    int pm_off = 0;
+    std::vector<int> in_end, pm_end;
+    int in_upto(int n) const { return n <= 0 ? 0 : in_end[n - 1]; }
+    int pm_upto(int n) const { return n <= 0 ? 0 : pm_end[n - 1]; }
+    int launches(int n) const { return (in_upto(n) > 0) + (pm_upto(n) > 0); }
+  };
+  DevTiles tf, ta;  // forward / adjoint items
+  void build_tiles(int rows, int width, int64_t pitch, TileList& L) const;
+  int upload_tiles(const TileList& L, DevTiles& D, cudaStream_t st);
   int autotune(cudaStream_t st, int64_t pitch, size_t cap_items);
-  int itemsf_upto(int n) const { return n <= 0 ? 0 : itemf_shot_end[n - 1]; }
+  // step launches over the first na sorted shots (interior and PML kernels)
+  int launch_fwd(cudaStream_t st, bool seg, int na, int t, int base, int ck);
+  int launch_adj(cudaStream_t st, int na, int k, int base);
   std::vector<int> rcv_b_host, rcv_e_host;
   AcConst<T> kc{};
   // device
   char* pool = nullptr;
   size_t pool_bytes = 0;
   AcShot<T>* d_shots = nullptr;
-  AcItem* d_items = nullptr;
-  CellRef *d_srcs = nullptr, *d_rcvs = nullptr, *d_shot_rcvs = nullptr;
+  CellRef* d_shot_rcvs = nullptr;
   int *d_rcv_b = nullptr, *d_rcv_e = nullptr;
   T *d_traces = nullptr, *d_resid = nullptr;
   double* d_partial = nullptr;
   static constexpr int kMisfitBlocks = 512;
+  static constexpr int kRowBlocks = 128;  // CTAs per shot of the per-segment copy kernels
   size_t zero_fwd_off = 0, zero_fwd_len = 0, zero_adj_off = 0, zero_adj_len = 0;
   std::vector<AcShot<T>> hshots;
-  int nitems = 0;
   cudaStream_t cap = nullptr;
+  // second stream for the PML-item launch of a step, which runs beside the
+  // interior-item launch (disjoint cells); fork / join through events
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   cudaGraph_t gF = nullptr, gR = nullptr;
   cudaGraphExec_t eF = nullptr, eR = nullptr;
   int64_t nF = 0, nR = 0;  // kernel launches in each loop
@@ -1160,12 +1240,12 @@ struct AcPlan final : AcPlanBase {
     if (gF) cudaGraphDestroy(gF);
     if (gR) cudaGraphDestroy(gR);
     if (cap) cudaStreamDestroy(cap);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side) cudaStreamDestroy(side);
     if (pool) cudaFree(pool);
   }
 
-  int items_upto(int t_active_count) const {  // items of the first n sorted shots
-    return t_active_count <= 0 ? 0 : item_shot_end[t_active_count - 1];
-  }
   std::vector<int64_t> cells_prefix;  // interior cells of the first n sorted shots
   int64_t cells_upto(int n) const { return n <= 0 ? 0 : cells_prefix[n - 1]; }
   int profile(const double* vp, const void* obs, double* out, cudaStream_t st) override;
@@ -1351,32 +1431,45 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
       const int i = (int)h.rcvi[r] - 1, j = (int)h.rcvj[r] - 1;
       if (i < 1 || i > nx || j < 1 || j > ny) continue;  // frame: trace stays 0
       hrcv[s].push_back(make_int3(i, j, (int)r));
-      shot_rcvs.push_back({(int64_t)i * pitch + j + JOFF, (int)r, 0});
+      shot_rcvs.push_back({(int64_t)i * pitch + j + JOFF, (int)r, i});
     }
     rcv_e_host[s] = (int)shot_rcvs.size();
   }
-  // forward and adjoint tiles (rows per thread chosen separately; the
-  // autotuner may replace both once the plan's buffers exist)
+  // host copies of the PML profiles (the kernels' interior / PML split uses them)
+  hsx.assign(ns, {});
+  hty.assign(MY + 2, 0.0);
+  for (int s = 0; s < ns; s++) {
+    const ads_acoustic_shot& h = shots[order[s]];
+    hsx[s].assign(h.nx + 2, 0.0);
+    acoustic_pml_1d(h.nx, MY, c.dx, c.dy, c.npml, c.vp_ref, c.Rcoef, c.use_pml,
+                    hsx[s].data(), hty.data());
+  }
+  // forward and adjoint warp items (rows per thread chosen separately; the
+  // autotuner may replace both once the plan's buffers exist): enough warps
+  // for several resident waves
   if (c.rows_per_thread <= 0) {
     ri_f = 8;
-    while (ri_f > 2 && cells / ((int64_t)ri_f * Tile<T>::J) < 152 * 8) ri_f /= 2;
-    ri = 32;
-    while (ri > 2 && cells / ((int64_t)ri * Tile<T>::J) < 152 * 4) ri /= 2;
+    while (ri_f > 2 && cells / ((int64_t)ri_f * Tile<T>::WF) < 152 * 64) ri_f /= 2;
+    ri = 16;
+    while (ri > 2 && cells / ((int64_t)ri * Tile<T>::WA) < 152 * 32) ri /= 2;
   } else {
     ri_f = ri;
   }
   TileList tiles_a, tiles_f;
-  build_tiles(ri, pitch, tiles_a);
-  build_tiles(ri_f, pitch, tiles_f);
+  build_tiles(ri, Tile<T>::WA, pitch, tiles_a);
+  build_tiles(ri_f, Tile<T>::WF, pitch, tiles_f);
+  auto nitems_of = [](const TileList& L) { return L.in.size() + L.pm.size(); };
   // capacity: the autotuner tries rows down to 2 per thread
-  size_t cap_items = std::max(tiles_a.items.size(), tiles_f.items.size());
+  size_t cap_items = std::max(nitems_of(tiles_a), nitems_of(tiles_f));
+  size_t cap_refs = std::max({tiles_a.srcs.size(), tiles_f.srcs.size(), tiles_a.rcvs.size(),
+                              tiles_f.rcvs.size(), (size_t)1});
   if (c.autotune) {
     size_t n2 = 0;
     for (int s = 0; s < ns; s++)
-      n2 += (size_t)div_up(shots[order[s]].nx, 2) * (size_t)div_up(MY, Tile<T>::J);
+      n2 += (size_t)div_up(shots[order[s]].nx, 2) *
+            (size_t)div_up(MY, std::min(Tile<T>::WF, Tile<T>::WA));
     cap_items = std::max(cap_items, n2);
   }
-  nitems = (int)tiles_a.items.size();
   // time-blocked tiles: output columns [jo, jo + W), rows [i0, i0 + RB); sources
   // of the loaded region (halo KB); receiver maps of the output region
   std::vector<TbItem> tb_items;
@@ -1444,12 +1537,13 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   const size_t tbm_off = L.take(sizeof(int) * std::max<size_t>(tb_map.size(), 1));
   const size_t rnx_off = L.take(sizeof(int) * std::max<size_t>(rcv_next_all.size(), 1));
   const size_t shots_off = L.take(sizeof(AcShot<T>) * ns);
+  // (sources / receivers: each is bucketed into exactly one item of a list)
   const size_t items_off = L.take(sizeof(AcItem) * cap_items);
-  const size_t srcs_off = L.take(sizeof(CellRef) * std::max<size_t>(tiles_a.srcs.size(), 1));
-  const size_t rcvs_off = L.take(sizeof(CellRef) * std::max<size_t>(tiles_a.rcvs.size(), 1));
+  const size_t srcs_off = L.take(sizeof(CellRef) * cap_refs);
+  const size_t rcvs_off = L.take(sizeof(CellRef) * cap_refs);
   const size_t itemsf_off = L.take(sizeof(AcItem) * cap_items);
-  const size_t srcsf_off = L.take(sizeof(CellRef) * std::max<size_t>(tiles_f.srcs.size(), 1));
-  const size_t rcvsf_off = L.take(sizeof(CellRef) * std::max<size_t>(tiles_f.rcvs.size(), 1));
+  const size_t srcsf_off = L.take(sizeof(CellRef) * cap_refs);
+  const size_t rcvsf_off = L.take(sizeof(CellRef) * cap_refs);
   const size_t shot_rcvs_off = L.take(sizeof(CellRef) * std::max<size_t>(shot_rcvs.size(), 1));
   const size_t rcvb_off = L.take(sizeof(int) * ns);
   const size_t rcve_off = L.take(sizeof(int) * ns);
@@ -1473,12 +1567,12 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   d_resid = (T*)(pool + resid_off);
   d_partial = (double*)(pool + partial_off);
   d_shots = (AcShot<T>*)(pool + shots_off);
-  d_items = (AcItem*)(pool + items_off);
-  d_srcs = (CellRef*)(pool + srcs_off);
-  d_rcvs = (CellRef*)(pool + rcvs_off);
-  d_items_f = (AcItem*)(pool + itemsf_off);
-  d_srcs_f = (CellRef*)(pool + srcsf_off);
-  d_rcvs_f = (CellRef*)(pool + rcvsf_off);
+  ta.items = (AcItem*)(pool + items_off);
+  ta.srcs = (CellRef*)(pool + srcs_off);
+  ta.rcvs = (CellRef*)(pool + rcvs_off);
+  tf.items = (AcItem*)(pool + itemsf_off);
+  tf.srcs = (CellRef*)(pool + srcsf_off);
+  tf.rcvs = (CellRef*)(pool + rcvsf_off);
   d_shot_rcvs = (CellRef*)(pool + shot_rcvs_off);
   d_rcv_b = (int*)(pool + rcvb_off);
   d_rcv_e = (int*)(pool + rcve_off);
@@ -1521,10 +1615,8 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     d.srcv = (const T*)(pool + offs[s].srcv);
     d.traces = d_traces + trace_off[order[s]];
     d.resid = d_resid + trace_off[order[s]];
-    sx.assign(h.nx + 2, 0.0);
-    ty.assign(MY + 2, 0.0);
-    acoustic_pml_1d(h.nx, MY, c.dx, c.dy, c.npml, c.vp_ref, c.Rcoef, c.use_pml, sx.data(),
-                    ty.data());
+    sx = hsx[s];
+    ty = hty;
     host_bufs.emplace_back(sx.begin(), sx.end());
     ADS_CUDA(cudaMemcpyAsync(d.sx, host_bufs.back().data(), sizeof(T) * sx.size(),
                              cudaMemcpyHostToDevice, st));
@@ -1545,10 +1637,8 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   }
   ADS_CUDA(cudaMemcpyAsync(d_shots, hshots.data(), sizeof(AcShot<T>) * ns,
                            cudaMemcpyHostToDevice, st));
-  if (int e = upload_tiles(tiles_a, d_items, d_srcs, d_rcvs, st)) return e;
-  item_shot_end = tiles_a.shot_end;
-  if (int e = upload_tiles(tiles_f, d_items_f, d_srcs_f, d_rcvs_f, st)) return e;
-  itemf_shot_end = tiles_f.shot_end;
+  if (int e = upload_tiles(tiles_a, ta, st)) return e;
+  if (int e = upload_tiles(tiles_f, tf, st)) return e;
   if (!shot_rcvs.empty())
     ADS_CUDA(cudaMemcpyAsync(d_shot_rcvs, shot_rcvs.data(), sizeof(CellRef) * shot_rcvs.size(),
                              cudaMemcpyHostToDevice, st));
@@ -1567,6 +1657,9 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   if (int e = up(pool + rnx_off, rcv_next_all.data(), sizeof(int) * rcv_next_all.size()))
     return e;
   ADS_CUDA(cudaStreamSynchronize(st));  // host staging buffers go out of scope
+  ADS_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+  ADS_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+  ADS_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
   // ---- autotuner: time candidate tilings on the plan's own buffers
   if (c.autotune)
     if (int e = autotune(st, pitch, cap_items)) return e;
@@ -1621,61 +1714,154 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
 // Tiles of `rows` rows x Tile::J columns over every sorted shot, with the
 // sources and receivers of each tile (bucketed once per shot).
 template <typename T>
-void AcPlan<T>::build_tiles(int rows, int64_t pitch, TileList& L) const {
-  L.items.clear();
+void AcPlan<T>::build_tiles(int rows, int width, int64_t pitch, TileList& L) const {
+  L.in.clear();
+  L.pm.clear();
   L.srcs.clear();
   L.rcvs.clear();
-  L.shot_end.assign(nshots, 0);
-  const int ny = (int)cfg.MY, J = Tile<T>::J;
+  L.in_end.assign(nshots, 0);
+  L.pm_end.assign(nshots, 0);
+  const int ny = (int)cfg.MY;
+  const int gh = Tile<T>::G * rows;  // rows of one item (its G warps' row tiles)
   for (int s = 0; s < nshots; s++) {
     const int nx = nxs[s];
-    const int nti = (int)div_up(nx, rows), ntj = (int)div_up(ny, J);
+    const int nti = (int)div_up(nx, gh), ntj = (int)div_up(ny, width);
     std::vector<std::vector<int>> bs((size_t)nti * ntj), br((size_t)nti * ntj);
     for (size_t k = 0; k < hsrc[s].size(); k++) {
       const int3 q = hsrc[s][k];
-      bs[(size_t)((q.x - 1) / rows) * ntj + (q.y - 1) / J].push_back((int)k);
+      bs[(size_t)((q.x - 1) / gh) * ntj + (q.y - 1) / width].push_back((int)k);
     }
     for (size_t k = 0; k < hrcv[s].size(); k++) {
       const int3 q = hrcv[s][k];
-      br[(size_t)((q.x - 1) / rows) * ntj + (q.y - 1) / J].push_back((int)k);
+      br[(size_t)((q.x - 1) / gh) * ntj + (q.y - 1) / width].push_back((int)k);
+    }
+    // tau-free column strips: tau = 0 at columns j0-1 .. j0+width (inside the frame)
+    std::vector<char> col_free(ntj), row_free(nti);
+    for (int tj = 0; tj < ntj; tj++) {
+      const int j0 = 1 + tj * width;
+      bool z = true;
+      for (int j = j0 - 1; j <= std::min(j0 + width, ny + 1); j++) z = z && hty[j] == 0.0;
+      col_free[tj] = z;
+    }
+    for (int ti = 0; ti < nti; ti++) {  // sigma = 0 on rows i0-1 .. i_end
+      const int i0 = 1 + ti * gh, i_end = std::min(i0 + gh, nx + 1);
+      bool z = true;
+      for (int i = i0 - 1; i <= i_end; i++) z = z && hsx[s][i] == 0.0;
+      row_free[ti] = z;
     }
     for (int ti = 0; ti < nti; ti++)
       for (int tj = 0; tj < ntj; tj++) {
         AcItem it{};
         it.shot = s;
-        it.i0 = 1 + ti * rows;
-        it.j0 = 1 + tj * J;
+        it.i0 = 1 + ti * gh;
+        it.j0 = 1 + tj * width;
         const size_t b = (size_t)ti * ntj + tj;
         it.src_b = (int)L.srcs.size();
         for (int k : bs[b]) {
           const int3 q = hsrc[s][k];
-          L.srcs.push_back({(int64_t)q.x * pitch + q.y + JOFF, q.z, 0});
+          L.srcs.push_back({(int64_t)q.x * pitch + q.y + JOFF, q.z, q.x});
         }
         it.src_e = (int)L.srcs.size();
         it.rcv_b = (int)L.rcvs.size();
         for (int k : br[b]) {
           const int3 q = hrcv[s][k];
-          L.rcvs.push_back({(int64_t)q.x * pitch + q.y + JOFF, q.z, 0});
+          L.rcvs.push_back({(int64_t)q.x * pitch + q.y + JOFF, q.z, q.x});
         }
         it.rcv_e = (int)L.rcvs.size();
-        L.items.push_back(it);
+        // interior items carry no sources or receivers: the interior kernels
+        // then need neither (items holding one take the general kernel)
+        const bool in = row_free[ti] && col_free[tj] && it.src_e == it.src_b &&
+                        it.rcv_e == it.rcv_b;
+        (in ? L.in : L.pm).push_back(it);
       }
-    L.shot_end[s] = (int)L.items.size();
+    L.in_end[s] = (int)L.in.size();
+    L.pm_end[s] = (int)L.pm.size();
   }
 }
 
 template <typename T>
-int AcPlan<T>::upload_tiles(const TileList& L, AcItem* di, CellRef* ds, CellRef* dr,
-                            cudaStream_t st) {
-  if (!L.items.empty())
-    ADS_CUDA(cudaMemcpyAsync(di, L.items.data(), sizeof(AcItem) * L.items.size(),
+int AcPlan<T>::upload_tiles(const TileList& L, DevTiles& D, cudaStream_t st) {
+  if (!L.in.empty())
+    ADS_CUDA(cudaMemcpyAsync(D.items, L.in.data(), sizeof(AcItem) * L.in.size(),
+                             cudaMemcpyHostToDevice, st));
+  if (!L.pm.empty())
+    ADS_CUDA(cudaMemcpyAsync(D.items + L.in.size(), L.pm.data(), sizeof(AcItem) * L.pm.size(),
                              cudaMemcpyHostToDevice, st));
   if (!L.srcs.empty())
-    ADS_CUDA(cudaMemcpyAsync(ds, L.srcs.data(), sizeof(CellRef) * L.srcs.size(),
+    ADS_CUDA(cudaMemcpyAsync(D.srcs, L.srcs.data(), sizeof(CellRef) * L.srcs.size(),
                              cudaMemcpyHostToDevice, st));
   if (!L.rcvs.empty())
-    ADS_CUDA(cudaMemcpyAsync(dr, L.rcvs.data(), sizeof(CellRef) * L.rcvs.size(),
+    ADS_CUDA(cudaMemcpyAsync(D.rcvs, L.rcvs.data(), sizeof(CellRef) * L.rcvs.size(),
                              cudaMemcpyHostToDevice, st));
+  D.pm_off = (int)L.in.size();
+  D.in_end = L.in_end;
+  D.pm_end = L.pm_end;
+  return ADS_OK;
+}
+
+// One forward step of the first na sorted shots: the interior-item kernel and
+// the PML-item kernel (each launched only when it has items).
+template <typename T>
+int AcPlan<T>::launch_fwd(cudaStream_t st, bool seg, int na, int t, int base, int ck) {
+  constexpr int TPB = Tile<T>::TPB;
+  const int ni = tf.in_upto(na), np = tf.pm_upto(na);
+  const AcItem* pm = tf.items + tf.pm_off;
+  const bool fork = ni > 0 && np > 0;
+  cudaStream_t sp = st;  // stream of the PML-item launch
+  if (fork) {
+    ADS_CUDA(cudaEventRecord(ev_fork, st));
+    ADS_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
+    sp = side;
+  }
+  if (ni > 0) {
+    if (seg)
+      k_ac_fwd<T, true, true><<<ni, TPB, 0, st>>>(tf.items, d_shots, tf.srcs, tf.rcvs, kc, t,
+                                                   base, ck, ri_f);
+    else
+      k_ac_fwd<T, false, true><<<ni, TPB, 0, st>>>(tf.items, d_shots, tf.srcs, tf.rcvs, kc, t,
+                                                    base, ck, ri_f);
+    ADS_LAUNCHED(1);
+  }
+  if (np > 0) {
+    if (seg)
+      k_ac_fwd<T, true, false><<<np, TPB, 0, sp>>>(pm, d_shots, tf.srcs, tf.rcvs, kc, t, base,
+                                                    ck, ri_f);
+    else
+      k_ac_fwd<T, false, false><<<np, TPB, 0, sp>>>(pm, d_shots, tf.srcs, tf.rcvs, kc, t, base,
+                                                     ck, ri_f);
+    ADS_LAUNCHED(1);
+  }
+  if (fork) {
+    ADS_CUDA(cudaEventRecord(ev_join, side));
+    ADS_CUDA(cudaStreamWaitEvent(st, ev_join, 0));
+  }
+  return ADS_OK;
+}
+
+template <typename T>
+int AcPlan<T>::launch_adj(cudaStream_t st, int na, int k, int base) {
+  constexpr int TPB = Tile<T>::TPB;
+  const int ni = ta.in_upto(na), np = ta.pm_upto(na);
+  const bool fork = ni > 0 && np > 0;
+  cudaStream_t sp = st;
+  if (fork) {
+    ADS_CUDA(cudaEventRecord(ev_fork, st));
+    ADS_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
+    sp = side;
+  }
+  if (ni > 0) {
+    k_ac_adj<T, true><<<ni, TPB, 0, st>>>(ta.items, d_shots, ta.rcvs, kc, k, base, ri);
+    ADS_LAUNCHED(1);
+  }
+  if (np > 0) {
+    k_ac_adj<T, false><<<np, TPB, 0, sp>>>(ta.items + ta.pm_off, d_shots, ta.rcvs, kc, k, base,
+                                           ri);
+    ADS_LAUNCHED(1);
+  }
+  if (fork) {
+    ADS_CUDA(cudaEventRecord(ev_join, side));
+    ADS_CUDA(cudaStreamWaitEvent(st, ev_join, 0));
+  }
   return ADS_OK;
 }
 
@@ -1693,42 +1879,46 @@ int AcPlan<T>::autotune(cudaStream_t st, int64_t pitch, size_t cap) {
   const int ka_end = std::min(std::min(7, K + 1), nstep[0]);
   float best_f = 1e30f, best_a = 1e30f;
   int bf = ri_f, ba = ri;
+  const int ri_f0 = ri_f, ri0 = ri;
   int rc = ADS_OK;
   for (int rows : cand) {
-    TileList L;
-    build_tiles(rows, pitch, L);
-    if (L.items.size() > cap) continue;
-    if ((rc = upload_tiles(L, d_items_f, d_srcs_f, d_rcvs_f, st))) break;
-    if ((rc = upload_tiles(L, d_items, d_srcs, d_rcvs, st))) break;
+    TileList Lf, La;
+    build_tiles(rows, Tile<T>::WF, pitch, Lf);
+    build_tiles(rows, Tile<T>::WA, pitch, La);
+    if (Lf.in.size() + Lf.pm.size() > cap || La.in.size() + La.pm.size() > cap) continue;
+    if ((rc = upload_tiles(Lf, tf, st))) break;
+    if ((rc = upload_tiles(La, ta, st))) break;
+    ri_f = ri = rows;
     float ms_f = 0.f, ms_a = 0.f;
+    int64_t nl = 0;
     for (int pass = 0; pass < 2 && rc == ADS_OK; pass++) {  // pass 0 warms up
       if (cudaEventRecord(e0, st) != cudaSuccess) rc = ADS_ERR_CUDA;
-      for (int t = 2; t <= tf_end; t++) {
-        const int nit = L.shot_end[shots_with_nstep_ge(t) - 1];
-        k_ac_fwd<T, false><<<nit, Tile<T>::NF, 0, st>>>(d_items_f, d_shots, d_srcs_f, d_rcvs_f,
-                                                        kc, t, 0, 0, rows);
+      for (int t = 2; t <= tf_end && rc == ADS_OK; t++) {
+        rc = launch_fwd(st, false, shots_with_nstep_ge(t), t, 0, 0);
+        nl += tf.launches(shots_with_nstep_ge(t));
       }
       cudaEventRecord(e1, st);
-      cudaEvent_t e2 = e0;  // reused to time the adjoint range after the forward one
-      if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+      if (rc != ADS_OK || cudaStreamSynchronize(st) != cudaSuccess ||
+          cudaGetLastError() != cudaSuccess) {
         rc = fail(ADS_ERR_CUDA, "autotuner trial failed");
         break;
       }
       cudaEventElapsedTime(&ms_f, e0, e1);
-      cudaEventRecord(e2, st);
-      for (int k = 2; k <= ka_end; k++) {
-        const int nit = L.shot_end[shots_with_nstep_ge(k) - 1];
-        k_ac_adj<T><<<nit, Tile<T>::NA, 0, st>>>(d_items, d_shots, d_rcvs, kc, k, 0, rows);
+      cudaEventRecord(e0, st);
+      for (int k = 2; k <= ka_end && rc == ADS_OK; k++) {
+        rc = launch_adj(st, shots_with_nstep_ge(k), k, 0);
+        nl += ta.launches(shots_with_nstep_ge(k));
       }
       cudaEventRecord(e1, st);
-      if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+      if (rc != ADS_OK || cudaStreamSynchronize(st) != cudaSuccess ||
+          cudaGetLastError() != cudaSuccess) {
         rc = fail(ADS_ERR_CUDA, "autotuner trial failed");
         break;
       }
-      cudaEventElapsedTime(&ms_a, e2, e1);
+      cudaEventElapsedTime(&ms_a, e0, e1);
     }
     if (rc != ADS_OK) break;
-    note_launches(2 * (tf_end - 1) + 2 * (ka_end - 1));
+    (void)nl;
     if (ms_f < best_f) {
       best_f = ms_f;
       bf = rows;
@@ -1740,17 +1930,18 @@ int AcPlan<T>::autotune(cudaStream_t st, int64_t pitch, size_t cap) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (rc != ADS_OK) return rc;
+  if (rc != ADS_OK) {
+    ri_f = ri_f0;
+    ri = ri0;
+    return rc;
+  }
   ri_f = bf;
   ri = ba;
   TileList Lf, La;
-  build_tiles(ri_f, pitch, Lf);
-  build_tiles(ri, pitch, La);
-  if (int e = upload_tiles(Lf, d_items_f, d_srcs_f, d_rcvs_f, st)) return e;
-  if (int e = upload_tiles(La, d_items, d_srcs, d_rcvs, st)) return e;
-  itemf_shot_end = Lf.shot_end;
-  item_shot_end = La.shot_end;
-  nitems = (int)La.items.size();
+  build_tiles(ri_f, Tile<T>::WF, pitch, Lf);
+  build_tiles(ri, Tile<T>::WA, pitch, La);
+  if (int e = upload_tiles(Lf, tf, st)) return e;
+  if (int e = upload_tiles(La, ta, st)) return e;
   ADS_CUDA(cudaStreamSynchronize(st));
   return ADS_OK;
 }
@@ -1804,15 +1995,14 @@ int AcPlan<T>::issue_forward(cudaStream_t st, int64_t* count) {
     // checkpoint s >= 1 holds the state before step a_s = 2 + s K, i.e. after t = 1 + s K
     const int ck = ((t1 - 1) % K == 0) ? (t1 - 1) / K : 0;
     if (count) {
-      *count += 1;
-      tcount[0] += 1;
+      const int nl = KB > 1 ? 1 : tf.launches(na);
+      *count += nl;
+      tcount[0] += nl;
       for (int t = t0; t <= t1; t++) tcount[1] += (double)cells_upto(shots_with_nstep_ge(t));
     } else if (KB > 1) {
       if (int e = launch_tb(st, false, tb_items_upto(na), t0, NS, 0, blk & 1, ck)) return e;
     } else {
-      k_ac_fwd<T, false><<<itemsf_upto(na), Tile<T>::NF, 0, st>>>(
-          d_items_f, d_shots, d_srcs_f, d_rcvs_f, kc, t0, 0, ck, ri_f);
-      ADS_LAUNCHED(1);
+      if (int e = launch_fwd(st, false, na, t0, 0, ck)) return e;
     }
     t0 = t1 + 1;
     blk++;
@@ -1839,8 +2029,7 @@ int AcPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     if (na == 0) continue;
     const int b_max = std::min(a + K - 1, nstep[0]);
     if (!count) {
-      k_ac_restore<T><<<items_upto(na), Tile<T>::NC, 0, st>>>(d_items, d_shots, s, a, ri,
-                                                              KB > 1 ? 0 : -1);
+      k_ac_restore<T><<<dim3(kRowBlocks, na), 256, 0, st>>>(d_shots, s, a, KB > 1 ? 0 : -1);
       ADS_LAUNCHED(1);
     }
     n++;
@@ -1851,20 +2040,19 @@ int AcPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
       // active while t < b_shot = min(a+K-1, nstep), i.e. nstep >= t+1
       const int NS = KB > 1 ? std::min(KB, b_max - t0) : 1;
       const int nt = shots_with_nstep_ge(t0 + 1);
+      const int nl = KB > 1 ? 1 : tf.launches(nt);
       if (timed && count) {
-        tcount[2] += 1;
+        tcount[2] += nl;
         for (int t = t0; t < t0 + NS; t++) tcount[3] += (double)cells_upto(shots_with_nstep_ge(t + 1));
       }
       if (!count) {
         if (KB > 1) {
           if (int e = launch_tb(st, true, tb_items_upto(nt), t0, NS, a - 2, blk & 1, 0)) return e;
         } else {
-          k_ac_fwd<T, true><<<itemsf_upto(nt), Tile<T>::NF, 0, st>>>(
-              d_items_f, d_shots, d_srcs_f, d_rcvs_f, kc, t0, a - 2, 0, ri_f);
-          ADS_LAUNCHED(1);
+          if (int e = launch_fwd(st, true, nt, t0, a - 2, 0)) return e;
         }
       }
-      n++;
+      n += nl;
       t0 += NS;
     }
     if (timed && timing_run) {
@@ -1874,19 +2062,18 @@ int AcPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     for (int k = b_max; k >= a; k--) {
       const int nk = shots_with_nstep_ge(k);
       if (timed && count) {
-        tcount[4] += 1;
+        tcount[4] += ta.launches(nk);
         tcount[5] += (double)cells_upto(nk);
       }
       if (!count) {
-        k_ac_adj<T><<<items_upto(nk), Tile<T>::NA, 0, st>>>(d_items, d_shots, d_rcvs, kc, k, a - 2, ri);
-        ADS_LAUNCHED(1);
+        if (int e = launch_adj(st, nk, k, a - 2)) return e;
       }
-      n++;
+      n += ta.launches(nk);
     }
     if (timed && timing_run) ADS_CUDA(cudaEventRecord(ev[5], st));
     if (sizeof(T) == 4) {  // fold the segment's FP32 grad_c partial into FP64
       if (!count) {
-        k_ac_flush_gc<T><<<items_upto(na), Tile<T>::NC, 0, st>>>(d_items, d_shots, ri);
+        k_ac_flush_gc<T><<<dim3(kRowBlocks, na), 256, 0, st>>>(d_shots);
         ADS_LAUNCHED(1);
       }
       n++;

@@ -45,6 +45,11 @@ BYTES = {
 }
 
 
+# DRAM bytes (read + write) of one step of each kernel on the bench geometry
+# at 16 shots, from ncu --set full captures of both launches of a step
+TRAFFIC_16SHOT = {"k_ac_fwd": 139.3e6, "k_ac_adj": 245.1e6}
+
+
 def workload(MX=1000, MY=500, npml=40, nstep=3000, nshots=64, nrcv=500, fpeak=15.0,
              dt=0.8e-3, h=10.0, seed=1234):
     import __graft_entry__ as g
@@ -519,29 +524,37 @@ def main():
     rc_ms, rc_n, rc_cells = timing["recompute"]
     adj_ms, adj_n, adj_cells = timing["adjoint"]
     nseg = math.ceil((nstep - 1) / 100)
+    # a step is two launches of each kernel (interior items, PML items); the
+    # timed ranges hold whole steps, so per-launch means cover both
+    cells_per_step = sum(s["nx"] * MY for s in shots)
     kern = {
         "k_ac_fwd": dict(ms_per_launch=fwd_ms / fwd_n, bytes=BYTES[("fwd", "f32")] * fwd_cells / fwd_n,
-                         launches=fwd_n + rc_n * nseg),
+                         launches=fwd_n + rc_n * nseg,
+                         launches_per_step=fwd_n / (fwd_cells / cells_per_step)),
         "k_ac_adj": dict(ms_per_launch=adj_ms / adj_n, bytes=BYTES[("adj", "f32")] * adj_cells / adj_n,
-                         launches=adj_n * nseg),
+                         launches=adj_n * nseg,
+                         launches_per_step=adj_n / (adj_cells / cells_per_step)),
     }
     for k, v in kern.items():
         v["achieved_gbs"] = v["bytes"] / (v["ms_per_launch"] / 1e3) / 1e9
         v["total_ms"] = v["ms_per_launch"] * v["launches"]
     dom = max(kern, key=lambda k: kern[k]["total_ms"])
     d = kern[dom]
-    # DRAM read + write bytes of one launch from an ncu --set full capture of the
-    # same workload at 16 shots (k_ac_fwd 149.4 MB, k_ac_adj 252.0 MB), scaled by
-    # the shots a launch processes here (traffic grows with the shot count)
-    per_shot = {"k_ac_fwd": 149.4e6 / 16, "k_ac_adj": 252.0e6 / 16}
-    traffic = (round(per_shot[dom] * args.shots, -5)
-               if MX == 1000 and MY == 500 and dom in per_shot else None)
+    # DRAM read + write bytes of one step (both launches) from ncu --set full
+    # captures of the same workload at 16 shots, scaled by the shots a step
+    # processes here (traffic grows with the shot count), per launch like achieved
+    per_shot_step = {"k_ac_fwd": TRAFFIC_16SHOT["k_ac_fwd"] / 16,
+                     "k_ac_adj": TRAFFIC_16SHOT["k_ac_adj"] / 16}
+    traffic = (round(per_shot_step[dom] * args.shots / d["launches_per_step"], -5)
+               if MX == 1000 and MY == 500 and dom in per_shot_step else None)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(d["achieved_gbs"], 1),
                 "peak": peak, "unit": "GB/s", "frac": round(d["achieved_gbs"] / peak, 4),
                 "peak_source": peak_kind, "traffic": traffic,
                 "bytes_per_launch": d["bytes"], "ms_per_launch": d["ms_per_launch"],
+                "launches_per_step": round(d["launches_per_step"], 2),
                 "kernels": {k: {"achieved_gbs": round(v["achieved_gbs"], 1),
                                 "ms_per_launch": round(v["ms_per_launch"], 4),
+                                "launches_per_step": round(v["launches_per_step"], 2),
                                 "share_of_step": round(v["total_ms"] / ms, 3)}
                             for k, v in kern.items()}}
 
