@@ -427,6 +427,11 @@ template <typename T>
 constexpr int el_minb() { return sizeof(T) == 4 ? ADS_EL_MINB : 2; }
 template <typename T>
 constexpr int el_minb_adj() { return sizeof(T) == 4 ? ADS_EL_MINB_ADJ : 2; }
+#ifndef ADS_EL_MINB_INT
+#define ADS_EL_MINB_INT 6             // the kernels of CPML-free items (no memory variables)
+#endif
+template <typename T>
+constexpr int el_minb_int() { return sizeof(T) == 4 ? ADS_EL_MINB_INT : 2; }
 
 template <typename T>
 struct alignas(2 * sizeof(T)) V2 {
@@ -532,12 +537,14 @@ struct ColProf {
 };
 
 // Stress update (fw1 + fw2) of a strip.
-template <typename T, bool STORE>
-__global__ void __launch_bounds__(EW * 32, el_minb<T>())
-k_el_stress_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int R, int nwt,
+template <typename T, bool STORE, bool INT>
+__global__ void __launch_bounds__(EW * 32, INT ? el_minb_int<T>() : el_minb<T>())
+k_el_stress_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __restrict__ wlist,
+                 int ncolw, int R, int nwt,
                  int store_slot) {
-  const int wi = blockIdx.x * EW + (threadIdx.x >> 5);
-  if (wi >= nwt) return;
+  const int wl = blockIdx.x * EW + (threadIdx.x >> 5);
+  if (wl >= nwt) return;
+  const int wi = wlist[wl];  // the warp's (strip, row tile)
   const ElShot<T>& sh = shots[blockIdx.y];
   const Strip<T> S(M, ncolw, R, wi);
   const int j = S.j, NX = S.NX, NY = S.NY;
@@ -556,8 +563,8 @@ k_el_stress_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, i
   bool c1[2], c2[2];  // column parts of the fw1 / fw2 boxes
 #pragma unroll
   for (int c = 0; c < 2; c++) {
-    c1[c] = S.out && j + c >= 2 && j + c <= NY;
-    c2[c] = S.out && j + c >= 1 && j + c <= NY - 1;
+    c1[c] = S.out && (INT || (j + c >= 2 && j + c <= NY));
+    c2[c] = S.out && (INT || (j + c >= 1 && j + c <= NY - 1));
   }
   const int i0 = S.i0;
   // windows: vx rows i-1..i+2, vy rows i-2..i+1, lam / mu rows i, i+1
@@ -590,10 +597,11 @@ k_el_stress_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, i
     ur[1] = U0.v[1];
     ur[2] = shdn(U0.v[0]);
     // x profiles of row i: m1 on the half grid (fw1 rows), m3 on the integer grid (fw2 rows)
-    const T axh = M.axh[i - 1], bxh = M.bxh[i - 1], axi = M.axi[i - 1], bxi = M.bxi[i - 1];
-    const bool r1 = i <= NX - 1, r2 = i >= 2;
-    const bool rx1 = r1 && (axh != T(0) || bxh != T(1));
-    const bool rx3 = r2 && (axi != T(0) || bxi != T(1));
+    const T axh = INT ? T(0) : M.axh[i - 1], bxh = INT ? T(1) : M.bxh[i - 1];
+    const T axi = INT ? T(0) : M.axi[i - 1], bxi = INT ? T(1) : M.bxi[i - 1];
+    const bool r1 = INT || i <= NX - 1, r2 = INT || i >= 2;
+    const bool rx1 = !INT && r1 && (axh != T(0) || bxh != T(1));
+    const bool rx3 = !INT && r2 && (axi != T(0) || bxi != T(1));
     T nsxx[2], nsyy[2], nsxy[2], e1s[2], e2s[2], e12s[2];
     bool k1[2], k2[2];
 #pragma unroll
@@ -606,7 +614,7 @@ k_el_stress_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, i
       const T lm = lam_ + T(2) * mu1;
       const T dvx = d4r<T>(X2.v[c], X1.v[c], X3.v[c], X0.v[c], M.hx24, M.rhx24);
       const T dvy = d4r<T>(yr[2 + c], yr[1 + c], yr[3 + c], yr[c], M.hy24, M.rhy24);
-      const bool u1 = k1[c] && rx1, u2 = k1[c] && Y.acti[c];
+      const bool u1 = k1[c] && rx1, u2 = !INT && k1[c] && Y.acti[c];
       const T m1 = u1 ? bxh * m1p[o + c] + axh * dvx : T(0);
       const T m2 = u2 ? Y.bi[c] * m2p[o + c] + Y.ai[c] * dvy : T(0);
       if (u1) m1p[o + c] = m1;
@@ -620,7 +628,7 @@ k_el_stress_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, i
       const T mu2 = T(0.5) * (ur[c] + ur[c + 1]);
       const T dvydx = d4r<T>(Y2.v[c], Y1.v[c], Y3.v[c], Y0.v[c], M.hx24, M.rhx24);
       const T dvxdy = d4r<T>(xr[2 + c], xr[1 + c], xr[3 + c], xr[c], M.hy24, M.rhy24);
-      const bool u3 = k2[c] && rx3, u4 = k2[c] && Y.acth[c];
+      const bool u3 = k2[c] && rx3, u4 = !INT && k2[c] && Y.acth[c];
       const T m3 = u3 ? bxi * m3p[o + c] + axi * dvydx : T(0);
       const T m4 = u4 ? Y.bh[c] * m4p[o + c] + Y.ah[c] * dvxdy : T(0);
       if (u3) m3p[o + c] = m3;
@@ -645,12 +653,14 @@ k_el_stress_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, i
 }
 
 // Velocity update (fw3 + fw4) of a strip, from the new stresses.
-template <typename T, bool STORE>
-__global__ void __launch_bounds__(EW * 32, el_minb<T>())
-k_el_velocity_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int R, int nwt,
+template <typename T, bool STORE, bool INT>
+__global__ void __launch_bounds__(EW * 32, INT ? el_minb_int<T>() : el_minb<T>())
+k_el_velocity_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __restrict__ wlist,
+                   int ncolw, int R, int nwt,
                    int store_slot) {
-  const int wi = blockIdx.x * EW + (threadIdx.x >> 5);
-  if (wi >= nwt) return;
+  const int wl = blockIdx.x * EW + (threadIdx.x >> 5);
+  if (wl >= nwt) return;
+  const int wi = wlist[wl];  // the warp's (strip, row tile)
   const ElShot<T>& sh = shots[blockIdx.y];
   const Strip<T> S(M, ncolw, R, wi);
   const int j = S.j, NX = S.NX, NY = S.NY;
@@ -669,8 +679,8 @@ k_el_velocity_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw,
   bool c3[2], c4[2];  // column parts of the fw3 / fw4 boxes
 #pragma unroll
   for (int c = 0; c < 2; c++) {
-    c3[c] = S.out && j + c >= 2 && j + c <= NY;
-    c4[c] = S.out && j + c >= 1 && j + c <= NY - 1;
+    c3[c] = S.out && (INT || (j + c >= 2 && j + c <= NY));
+    c4[c] = S.out && (INT || (j + c >= 1 && j + c <= NY - 1));
   }
   const int i0 = S.i0;
   // windows: sxx rows i-2..i+1, sxy rows i-1..i+2, syy row i, rho rows i, i+1
@@ -706,10 +716,11 @@ k_el_velocity_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw,
     r1[1] = R1.v[1];
     r1[2] = shdn(R1.v[0]);
     // x profiles of row i: m5 on the integer grid (fw3 rows), m7 on the half grid (fw4 rows)
-    const T axi = M.axi[i - 1], bxi = M.bxi[i - 1], axh = M.axh[i - 1], bxh = M.bxh[i - 1];
-    const bool r3 = i >= 2, r4 = i <= NX - 1;
-    const bool rx5 = r3 && (axi != T(0) || bxi != T(1));
-    const bool rx7 = r4 && (axh != T(0) || bxh != T(1));
+    const T axi = INT ? T(0) : M.axi[i - 1], bxi = INT ? T(1) : M.bxi[i - 1];
+    const T axh = INT ? T(0) : M.axh[i - 1], bxh = INT ? T(1) : M.bxh[i - 1];
+    const bool r3 = INT || i >= 2, r4 = INT || i <= NX - 1;
+    const bool rx5 = !INT && r3 && (axi != T(0) || bxi != T(1));
+    const bool rx7 = !INT && r4 && (axh != T(0) || bxh != T(1));
     T nvx[2], nvy[2], a3s[2], a4s[2];
     bool k3[2], k4[2];
 #pragma unroll
@@ -719,7 +730,7 @@ k_el_velocity_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw,
       // fw3
       const T a = d4r<T>(S2.v[c], S1.v[c], S3.v[c], S0.v[c], M.hx24, M.rhx24);
       const T b = d4r<T>(qr[2 + c], qr[1 + c], qr[3 + c], qr[c], M.hy24, M.rhy24);
-      const bool u5 = k3[c] && rx5, u6 = k3[c] && Y.acti[c];
+      const bool u5 = k3[c] && rx5, u6 = !INT && k3[c] && Y.acti[c];
       const T m5 = u5 ? bxi * m5p[o + c] + axi * a : T(0);
       const T m6 = u6 ? Y.bi[c] * m6p[o + c] + Y.ai[c] * b : T(0);
       if (u5) m5p[o + c] = m5;
@@ -731,7 +742,7 @@ k_el_velocity_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw,
       const T rho_ = T(0.25) * (r0[c] + r1[c] + r1[c + 1] + r0[c + 1]);
       const T a4 = d4r<T>(Q2.v[c], Q1.v[c], Q3.v[c], Q0.v[c], M.hx24, M.rhx24);
       const T b4 = d4r<T>(wr[2 + c], wr[1 + c], wr[3 + c], wr[c], M.hy24, M.rhy24);
-      const bool u7 = k4[c] && rx7, u8 = k4[c] && Y.acth[c];
+      const bool u7 = k4[c] && rx7, u8 = !INT && k4[c] && Y.acth[c];
       const T m7 = u7 ? bxh * m7p[o + c] + axh * a4 : T(0);
       const T m8 = u8 ? Y.bh[c] * m8p[o + c] + Y.ah[c] * b4 : T(0);
       if (u7) m7p[o + c] = m7;
@@ -786,13 +797,15 @@ __device__ __forceinline__ T hdiv(T x, T h24, T rh24) {
 }
 
 // Adjoint 1 (velocity cells) of a strip: transposes of fw3 and fw4.
-template <typename T>
-__global__ void __launch_bounds__(EW * 32, el_minb<T>())
-k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int R, int nwt,
+template <typename T, bool INT>
+__global__ void __launch_bounds__(EW * 32, INT ? el_minb_int<T>() : el_minb<T>())
+k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __restrict__ wlist,
+               int ncolw, int R, int nwt,
                int store_slot) {
   using A = typename ElAcc<T>::type;
-  const int wi = blockIdx.x * EW + (threadIdx.x >> 5);
-  if (wi >= nwt) return;
+  const int wl = blockIdx.x * EW + (threadIdx.x >> 5);
+  if (wl >= nwt) return;
+  const int wi = wlist[wl];  // the warp's (strip, row tile)
   const ElShot<T>& sh = shots[blockIdx.y];
   const Strip<T> S(M, ncolw, R, wi);
   const int j = S.j, NX = S.NX, NY = S.NY;
@@ -816,8 +829,8 @@ k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int
   bool c3[2], c4[2];
 #pragma unroll
   for (int c = 0; c < 2; c++) {
-    c3[c] = S.out && j + c >= 2 && j + c <= NY;
-    c4[c] = S.out && j + c >= 1 && j + c <= NY - 1;
+    c3[c] = S.out && (INT || (j + c >= 2 && j + c <= NY));
+    c4[c] = S.out && (INT || (j + c >= 1 && j + c <= NY - 1));
   }
   const int i0 = S.i0;
   V2<T> R0 = S.row(M.rho, i0), R1 = S.row(M.rho, i0 + 1);
@@ -838,10 +851,11 @@ k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int
     r1[0] = R1.v[0];
     r1[1] = R1.v[1];
     r1[2] = shdn(R1.v[0]);
-    const T axi = M.axi[i - 1], bxi = M.bxi[i - 1], axh = M.axh[i - 1], bxh = M.bxh[i - 1];
-    const bool r3 = i >= 2, r4 = i <= NX - 1;
-    const bool rx5 = r3 && (axi != T(0) || bxi != T(1));
-    const bool rx7 = r4 && (axh != T(0) || bxh != T(1));
+    const T axi = INT ? T(0) : M.axi[i - 1], bxi = INT ? T(1) : M.bxi[i - 1];
+    const T axh = INT ? T(0) : M.axh[i - 1], bxh = INT ? T(1) : M.bxh[i - 1];
+    const bool r3 = INT || i >= 2, r4 = INT || i <= NX - 1;
+    const bool rx5 = !INT && r3 && (axi != T(0) || bxi != T(1));
+    const bool rx7 = !INT && r4 && (axh != T(0) || bxh != T(1));
     T o5[2], o6[2], o7[2], o8[2], o4[2];
     A gr[2];
     bool k3[2], k4[2];
@@ -852,25 +866,25 @@ k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int
       // fw3 transpose
       const T gv = GX.v[c], r = r0[c];
       const T q = divr<T>(gv * M.dt, r);
-      const bool u5 = k3[c] && rx5, u6 = k3[c] && Y.acti[c];
+      const bool u5 = k3[c] && rx5, u6 = !INT && k3[c] && Y.acti[c];
       const T gm5 = u5 ? q + g5[o + c] : q;
       const T gm6 = u6 ? q + g6[o + c] : q;
       if (u5) g5[o + c] = bxi * gm5;
       if (u6) g6[o + c] = Y.bi[c] * gm6;
       o5[c] = hdiv<T>(q + axi * gm5, M.hx24, M.rhx24);
-      o6[c] = hdiv<T>(q + Y.ai[c] * gm6, M.hy24, M.rhy24);
+      o6[c] = hdiv<T>(q + (INT ? T(0) : Y.ai[c]) * gm6, M.hy24, M.rhy24);
       gr[c] = GR.v[c] + (A)divr<T>(-gv * E3.v[c] * M.dt, r * r);
       // fw4 transpose
       const T gw = GY.v[c];
       const T rho_ = T(0.25) * (r0[c] + r1[c] + r1[c + 1] + r0[c + 1]);
       const T q4 = divr<T>(gw * M.dt, rho_);
-      const bool u7 = k4[c] && rx7, u8 = k4[c] && Y.acth[c];
+      const bool u7 = k4[c] && rx7, u8 = !INT && k4[c] && Y.acth[c];
       const T gm7 = u7 ? q4 + g7[o + c] : q4;
       const T gm8 = u8 ? q4 + g8[o + c] : q4;
       if (u7) g7[o + c] = bxh * gm7;
       if (u8) g8[o + c] = Y.bh[c] * gm8;
       o7[c] = hdiv<T>(q4 + axh * gm7, M.hx24, M.rhx24);
-      o8[c] = hdiv<T>(q4 + Y.ah[c] * gm8, M.hy24, M.rhy24);
+      o8[c] = hdiv<T>(q4 + (INT ? T(0) : Y.ah[c]) * gm8, M.hy24, M.rhy24);
       o4[c] = divr<T>(-gw * E4.v[c] * M.dt, rho_ * rho_) * T(0.25);
     }
     st2<T>(d5, o, o5, k3[0], k3[1]);
@@ -886,12 +900,14 @@ k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int
 
 // Adjoint 2 (stress cells) of a strip: gather D5..D8 into the stress
 // adjoints, then the transposes of fw1 and fw2.
-template <typename T>
+template <typename T, bool INT>
 __global__ void __launch_bounds__(EW * 32, el_minb_adj<T>())
-k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int R, int nwt,
+k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __restrict__ wlist,
+               int ncolw, int R, int nwt,
                int store_slot) {
-  const int wi = blockIdx.x * EW + (threadIdx.x >> 5);
-  if (wi >= nwt) return;
+  const int wl = blockIdx.x * EW + (threadIdx.x >> 5);
+  if (wl >= nwt) return;
+  const int wi = wlist[wl];  // the warp's (strip, row tile)
   const ElShot<T>& sh = shots[blockIdx.y];
   const Strip<T> S(M, ncolw, R, wi);
   const int j = S.j, NX = S.NX, NY = S.NY;
@@ -922,8 +938,8 @@ k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int
   bool c1[2], c2[2];
 #pragma unroll
   for (int c = 0; c < 2; c++) {
-    c1[c] = S.out && j + c >= 2 && j + c <= NY;
-    c2[c] = S.out && j + c >= 1 && j + c <= NY - 1;
+    c1[c] = S.out && (INT || (j + c >= 2 && j + c <= NY));
+    c2[c] = S.out && (INT || (j + c >= 1 && j + c <= NY - 1));
   }
   const int i0 = S.i0;
   // windows: D5 rows i-1..i+2, D7 rows i-2..i+1, lam / mu rows i, i+1
@@ -958,10 +974,11 @@ k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int
     ur[0] = U0.v[0];
     ur[1] = U0.v[1];
     ur[2] = shdn(U0.v[0]);
-    const T axh = M.axh[i - 1], bxh = M.bxh[i - 1], axi = M.axi[i - 1], bxi = M.bxi[i - 1];
-    const bool r1 = i <= NX - 1, r2 = i >= 2;
-    const bool rx1 = r1 && (axh != T(0) || bxh != T(1));
-    const bool rx3 = r2 && (axi != T(0) || bxi != T(1));
+    const T axh = INT ? T(0) : M.axh[i - 1], bxh = INT ? T(1) : M.bxh[i - 1];
+    const T axi = INT ? T(0) : M.axi[i - 1], bxi = INT ? T(1) : M.bxi[i - 1];
+    const bool r1 = INT || i <= NX - 1, r2 = INT || i >= 2;
+    const bool rx1 = !INT && r1 && (axh != T(0) || bxh != T(1));
+    const bool rx3 = !INT && r2 && (axi != T(0) || bxi != T(1));
     T oxx[2], oyy[2], oxy[2], ol1[2], om1[2], od1[2], od2[2], om2[2], od3[2], od4[2];
     bool k1[2], k2[2], k12[2];
 #pragma unroll
@@ -989,24 +1006,24 @@ k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int
       const T glam = M.dt * (e2 * gsxx + e1 * gsyy) + glm;
       ol1[c] = T(0.5) * glam;
       om1[c] = glm;
-      const bool u1 = k1[c] && rx1, u2 = k1[c] && Y.acti[c];
+      const bool u1 = k1[c] && rx1, u2 = !INT && k1[c] && Y.acti[c];
       const T gm1 = u1 ? gE1 + g1[o + c] : gE1;
       const T gm2 = u2 ? gE2 + g2[o + c] : gE2;
       if (u1) g1[o + c] = bxh * gm1;
       if (u2) g2[o + c] = Y.bi[c] * gm2;
       od1[c] = hdiv<T>(gE1 + axh * gm1, M.hx24, M.rhx24);
-      od2[c] = hdiv<T>(gE2 + Y.ai[c] * gm2, M.hy24, M.rhy24);
+      od2[c] = hdiv<T>(gE2 + (INT ? T(0) : Y.ai[c]) * gm2, M.hy24, M.rhy24);
       // fw2 transpose
       const T mu2 = T(0.5) * (ur[c] + ur[c + 1]);
       const T q = gsxy * mu2 * M.dt;
       om2[c] = gsxy * EC12.v[c] * M.dt * T(0.5);
-      const bool u3 = k2[c] && rx3, u4 = k2[c] && Y.acth[c];
+      const bool u3 = k2[c] && rx3, u4 = !INT && k2[c] && Y.acth[c];
       const T gm3 = u3 ? q + g3[o + c] : q;
       const T gm4 = u4 ? q + g4[o + c] : q;
       if (u3) g3[o + c] = bxi * gm3;
       if (u4) g4[o + c] = Y.bh[c] * gm4;
       od3[c] = hdiv<T>(q + axi * gm3, M.hx24, M.rhx24);
-      od4[c] = hdiv<T>(q + Y.ah[c] * gm4, M.hy24, M.rhy24);
+      od4[c] = hdiv<T>(q + (INT ? T(0) : Y.ah[c]) * gm4, M.hy24, M.rhy24);
     }
     st2<T>(gxx, o, oxx, k12[0], k12[1]);
     st2<T>(gyy, o, oyy, k12[0], k12[1]);
@@ -1029,12 +1046,14 @@ k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int
 
 // Adjoint 3 (velocity cells + parameters) of a strip: gather D1..D4 into the
 // velocity adjoints and the lambda / mu / rho parts into the accumulators.
-template <typename T>
+template <typename T, bool INT>
 __global__ void __launch_bounds__(EW * 32, el_minb_adj<T>())
-k_el_adj3_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int R, int nwt) {
+k_el_adj3_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __restrict__ wlist,
+               int ncolw, int R, int nwt) {
   using A = typename ElAcc<T>::type;
-  const int wi = blockIdx.x * EW + (threadIdx.x >> 5);
-  if (wi >= nwt) return;
+  const int wl = blockIdx.x * EW + (threadIdx.x >> 5);
+  if (wl >= nwt) return;
+  const int wi = wlist[wl];  // the warp's (strip, row tile)
   const ElShot<T>& sh = shots[blockIdx.y];
   const Strip<T> S(M, ncolw, R, wi);
   const int j = S.j, NX = S.NX, NY = S.NY;
@@ -1054,9 +1073,9 @@ k_el_adj3_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int
   bool c3[2], c4[2], cp[2];
 #pragma unroll
   for (int c = 0; c < 2; c++) {
-    c3[c] = S.out && j + c >= 2 && j + c <= NY;
-    c4[c] = S.out && j + c >= 1 && j + c <= NY - 1;
-    cp[c] = S.out && j + c >= 1 && j + c <= NY;
+    c3[c] = S.out && (INT || (j + c >= 2 && j + c <= NY));
+    c4[c] = S.out && (INT || (j + c >= 1 && j + c <= NY - 1));
+    cp[c] = S.out && (INT || (j + c >= 1 && j + c <= NY));
   }
   const int i0 = S.i0;
   // windows: D1 rows i-2..i+1, D3 rows i-1..i+2, GL1 / GM1 / R4 rows i-1, i
@@ -1098,7 +1117,7 @@ k_el_adj3_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, int ncolw, int
     r0[0] = shup(RR0.v[1]);
     r0[1] = RR0.v[0];
     r0[2] = RR0.v[1];
-    const bool r3 = i >= 2, r4 = i <= NX - 1;
+    const bool r3 = INT || i >= 2, r4 = INT || i <= NX - 1;
     T ovx[2], ovy[2];
     A ol[2], om[2], orr[2];
     bool k3[2], k4[2];
@@ -1349,6 +1368,15 @@ struct ElPlan final : ElPlanBase {
   ads_elastic_config cfg{};
   int nshots = 0, K = 0, nseg = 0, NX = 0, NY = 0, NSTEP = 0;
   int ncolw = 0, rows_w = 0, nwt = 0;  // warp strips of the row-streaming step kernels
+  // warp items (strip, row tile) of CPML-free tiles and of the rest; the two
+  // launches of a step kernel run concurrently (disjoint cells)
+  int* d_wl = nullptr;  // interior items, then the CPML items at nw_in
+  int nw_in = 0, nw_pm = 0;
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  int pair_launches() const { return (nw_in > 0) + (nw_pm > 0); }
+  template <typename FI, typename FP>
+  int pair(cudaStream_t st, FI&& lin, FP&& lpm);
   int max_rcv = 0;                      // most receivers of a shot
   int64_t P = 0, fs = 0;
   char* pool = nullptr;
@@ -1370,13 +1398,16 @@ struct ElPlan final : ElPlanBase {
     if (gF) cudaGraphDestroy(gF);
     if (gR) cudaGraphDestroy(gR);
     if (cap) cudaStreamDestroy(cap);
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
+    if (side) cudaStreamDestroy(side);
     if (pool) cudaFree(pool);
   }
 
   dim3 grid3() const {
     return dim3((unsigned)div_up(NY + 2, BX), (unsigned)div_up(NX + 2, BY), (unsigned)nshots);
   }
-  dim3 grid_rows() const { return dim3((unsigned)div_up(nwt, EW), (unsigned)nshots); }
+  dim3 grid_rows(int nw) const { return dim3((unsigned)div_up(nw, EW), (unsigned)nshots); }
   // sources / receivers: one CTA per shot, a thread per receiver (up to 1024)
   unsigned rcv_threads() const {
     return (unsigned)std::min<int64_t>(1024, std::max<int64_t>(32, div_up(max_rcv, 32) * 32));
@@ -1388,6 +1419,7 @@ struct ElPlan final : ElPlanBase {
   int create(const ads_elastic_config& c, const ads_elastic_shot* shots, int64_t ns,
              cudaStream_t st);
   int step(cudaStream_t st, int n, bool store, int slot, bool record);
+  int adjoint_step(cudaStream_t st, int slot);
   int issue_forward(cudaStream_t st, int64_t* count);
   int issue_reverse(cudaStream_t st, int64_t* count);
   int prep(const double* l, const double* m, const double* r, cudaStream_t st);
@@ -1502,6 +1534,7 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   const size_t resid_o = take(sizeof(T) * std::max<int64_t>(trace_total, 1));
   const size_t part_o = take(sizeof(double) * kBlocks);
   const size_t shots_o = take(sizeof(ElShot<T>) * ns);
+  const size_t wl_o = take(sizeof(int) * std::max(nwt, 1));
   bytes = (int64_t)used;
   {
     cudaError_t e = cudaMalloc(&pool, used);
@@ -1526,6 +1559,40 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
                c.Rcoef, c.use_pml, ax.data(), bx.data(), kx.data(), ay.data(), by.data(),
                ky.data());
   std::vector<T> prof = pack_profiles<T>(NX, NY, ax.data(), bx.data(), ay.data(), by.data());
+  // warp items: a (strip, row tile) is interior when every cell it updates lies
+  // inside all four update boxes (2 <= i <= NX-1, 2 <= j <= NY-1) with no
+  // active CPML profile on its rows and columns (as the kernels see them)
+  std::vector<int> wl_host;
+  {
+    const T *axi = prof.data(), *axh = axi + NX, *bxi = axi + 2 * NX, *bxh = axi + 3 * NX;
+    const T *ayi = axi + 4 * NX, *ayh = ayi + NY, *byi = ayi + 2 * NY, *byh = ayi + 3 * NY;
+    std::vector<char> row_ok(NX + 2, 0), col_ok(NY + 2, 0);
+    for (int i = 2; i <= NX - 1; i++)
+      row_ok[i] = axh[i - 1] == T(0) && bxh[i - 1] == T(1) && axi[i - 1] == T(0) &&
+                  bxi[i - 1] == T(1);
+    for (int jc = 2; jc <= NY - 1; jc++)
+      col_ok[jc] = ayi[jc - 1] == T(0) && byi[jc - 1] == T(1) && ayh[jc - 1] == T(0) &&
+                   byh[jc - 1] == T(1);
+    std::vector<int> wpm;
+    for (int wi = 0; wi < nwt; wi++) {
+      const int strip = wi % ncolw, rt = wi / ncolw;
+      const int i0 = 1 + rt * rows_w, i1 = std::min(i0 + rows_w, NX + 1);
+      bool ok = true;
+      for (int i = i0; i < i1 && ok; i++) ok = row_ok[i];
+      for (int jc = strip * ESTRIP + 1; jc <= strip * ESTRIP + ESTRIP && ok; jc++)
+        ok = jc <= NY - 1 && col_ok[jc];
+      (ok ? wl_host : wpm).push_back(wi);
+    }
+    nw_in = (int)wl_host.size();
+    nw_pm = (int)wpm.size();
+    wl_host.insert(wl_host.end(), wpm.begin(), wpm.end());
+  }
+  d_wl = (int*)(pool + wl_o);
+  ADS_CUDA(cudaMemcpyAsync(d_wl, wl_host.data(), sizeof(int) * wl_host.size(),
+                           cudaMemcpyHostToDevice, st));
+  ADS_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+  ADS_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+  ADS_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
   ADS_CUDA(cudaMemcpyAsync(pool + prof_o, prof.data(), sizeof(T) * prof.size(),
                            cudaMemcpyHostToDevice, st));
   M = make_model<T>(NX, NY, P, JOFF, c.dt, c.dx, c.dy, d_lam, d_mu, d_rho,
@@ -1651,23 +1718,117 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   return ADS_OK;
 }
 
+// The three adjoint passes of step n (store slot `slot`), each as an interior /
+// CPML pair of launches.
+template <typename T>
+int ElPlan<T>::adjoint_step(cudaStream_t st, int slot) {
+  const int* wp = d_wl + nw_in;
+  const dim3 gi = grid_rows(nw_in), gp = grid_rows(nw_pm), b(EW * 32);
+  if (int e = pair(
+          st,
+          [&](cudaStream_t s) {
+            k_el_adj1_rows<T, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in, slot);
+          },
+          [&](cudaStream_t s) {
+            k_el_adj1_rows<T, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm, slot);
+          }))
+    return e;
+  if (int e = pair(
+          st,
+          [&](cudaStream_t s) {
+            k_el_adj2_rows<T, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in, slot);
+          },
+          [&](cudaStream_t s) {
+            k_el_adj2_rows<T, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm, slot);
+          }))
+    return e;
+  return pair(
+      st,
+      [&](cudaStream_t s) {
+        k_el_adj3_rows<T, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in);
+      },
+      [&](cudaStream_t s) {
+        k_el_adj3_rows<T, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm);
+      });
+}
+
+// One forward step n (slot n-1 -> slot n) for every shot.
+template <typename T>
+template <typename FI, typename FP>
+int ElPlan<T>::pair(cudaStream_t st, FI&& lin, FP&& lpm) {
+  const bool fork = nw_in > 0 && nw_pm > 0;
+  cudaStream_t sp = st;
+  if (fork) {
+    ADS_CUDA(cudaEventRecord(ev_fork, st));
+    ADS_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
+    sp = side;
+  }
+  if (nw_in > 0) {
+    lin(st);
+    ADS_LAUNCHED(1);
+  }
+  if (nw_pm > 0) {
+    lpm(sp);
+    ADS_LAUNCHED(1);
+  }
+  if (fork) {
+    ADS_CUDA(cudaEventRecord(ev_join, side));
+    ADS_CUDA(cudaStreamWaitEvent(st, ev_join, 0));
+  }
+  return ADS_OK;
+}
+
 // One forward step n (slot n-1 -> slot n) for every shot.
 template <typename T>
 int ElPlan<T>::step(cudaStream_t st, int n, bool store, int slot, bool record) {
+  const int* wp = d_wl + nw_in;
+  const dim3 gi = grid_rows(nw_in), gp = grid_rows(nw_pm), b(EW * 32);
   if (store) {
-    k_el_stress_rows<T, true><<<grid_rows(), EW * 32, 0, st>>>(M, d_shots, ncolw, rows_w, nwt,
-                                                                slot);
-    ADS_LAUNCHED(1);
-    k_el_velocity_rows<T, true><<<grid_rows(), EW * 32, 0, st>>>(M, d_shots, ncolw, rows_w, nwt,
-                                                                  slot);
-    ADS_LAUNCHED(1);
+    if (int e = pair(
+            st,
+            [&](cudaStream_t s) {
+              k_el_stress_rows<T, true, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w,
+                                                               nw_in, slot);
+            },
+            [&](cudaStream_t s) {
+              k_el_stress_rows<T, true, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w,
+                                                                nw_pm, slot);
+            }))
+      return e;
+    if (int e = pair(
+            st,
+            [&](cudaStream_t s) {
+              k_el_velocity_rows<T, true, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw,
+                                                                 rows_w, nw_in, slot);
+            },
+            [&](cudaStream_t s) {
+              k_el_velocity_rows<T, true, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w,
+                                                                  nw_pm, slot);
+            }))
+      return e;
   } else {
-    k_el_stress_rows<T, false><<<grid_rows(), EW * 32, 0, st>>>(M, d_shots, ncolw, rows_w, nwt,
-                                                                 0);
-    ADS_LAUNCHED(1);
-    k_el_velocity_rows<T, false><<<grid_rows(), EW * 32, 0, st>>>(M, d_shots, ncolw, rows_w,
-                                                                   nwt, 0);
-    ADS_LAUNCHED(1);
+    if (int e = pair(
+            st,
+            [&](cudaStream_t s) {
+              k_el_stress_rows<T, false, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w,
+                                                                nw_in, 0);
+            },
+            [&](cudaStream_t s) {
+              k_el_stress_rows<T, false, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w,
+                                                                 nw_pm, 0);
+            }))
+      return e;
+    if (int e = pair(
+            st,
+            [&](cudaStream_t s) {
+              k_el_velocity_rows<T, false, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw,
+                                                                  rows_w, nw_in, 0);
+            },
+            [&](cudaStream_t s) {
+              k_el_velocity_rows<T, false, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw,
+                                                                   rows_w, nw_pm, 0);
+            }))
+      return e;
   }
   k_el_src_rcv<T><<<nshots, rcv_threads(), 0, st>>>(d_shots, n, NSTEP + 1, record ? 1 : 0);
   ADS_LAUNCHED(1);
@@ -1678,7 +1839,8 @@ template <typename T>
 int ElPlan<T>::issue_forward(cudaStream_t st, int64_t* count) {
   if (count) {
     int64_t c = 0;
-    for (int n = 1; n <= NSTEP; n++) c += 3 + ((n % K == 0 && n / K < nseg) ? 1 : 0);
+    for (int n = 1; n <= NSTEP; n++)
+      c += 2 * pair_launches() + 1 + ((n % K == 0 && n / K < nseg) ? 1 : 0);
     *count = c;
     return ADS_OK;
   }
@@ -1699,7 +1861,8 @@ int ElPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     int64_t c = 1;
     for (int s = nseg - 1; s >= 0; s--) {
       const int a = 1 + s * K, b = std::min(a + K - 1, NSTEP);
-      c += 1 + 3 * (b - a + 1) + 3 * (b - a + 1) + (b - std::max(a, 2) + 1) +
+      c += 1 + (2 * pair_launches() + 1) * (b - a + 1) + 3 * pair_launches() * (b - a + 1) +
+           (b - std::max(a, 2) + 1) +
            (sizeof(T) == 4 ? 1 : 0);
     }
     *count = c;
@@ -1716,12 +1879,7 @@ int ElPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     for (int n = a; n <= b; n++)
       if (int e = step(st, n, true, n - a, false)) return e;
     for (int n = b; n >= a; n--) {
-      k_el_adj1_rows<T><<<grid_rows(), EW * 32, 0, st>>>(M, d_shots, ncolw, rows_w, nwt, n - a);
-      ADS_LAUNCHED(1);
-      k_el_adj2_rows<T><<<grid_rows(), EW * 32, 0, st>>>(M, d_shots, ncolw, rows_w, nwt, n - a);
-      ADS_LAUNCHED(1);
-      k_el_adj3_rows<T><<<grid_rows(), EW * 32, 0, st>>>(M, d_shots, ncolw, rows_w, nwt);
-      ADS_LAUNCHED(1);
+      if (int e = adjoint_step(st, n - a)) return e;
       // the adjoint state now refers to slot n-1: add its residual (slot 0 is
       // the constant zero state and takes none)
       if (n - 1 >= 1) {
@@ -1821,23 +1979,52 @@ int ElPlan<T>::profile(const double* l, const double* m, const double* r, double
     out[2 * k + 1] = cells;
     return ADS_OK;
   };
-  const dim3 g = grid_rows(), b(EW * 32);
+  const int* wp = d_wl + nw_in;
+  const dim3 gi = grid_rows(nw_in), gp = grid_rows(nw_pm), b(EW * 32);
   int rc = ADS_OK;
   auto run = [&](int k, auto&& launch) {
     if (rc == ADS_OK) rc = timed(k, launch);
   };
   ADS_CUDA(cudaMemsetAsync(pool + zero_fwd_off, 0, zero_fwd_len, st));
   ADS_CUDA(cudaMemsetAsync(pool + zero_adj_off, 0, zero_adj_len, st));
-  run(0, [&] { k_el_stress_rows<T, false><<<g, b, 0, st>>>(M, d_shots, ncolw, rows_w, nwt, 0); });
-  run(1, [&] { k_el_velocity_rows<T, false><<<g, b, 0, st>>>(M, d_shots, ncolw, rows_w, nwt, 0); });
-  run(2, [&] { k_el_stress_rows<T, true><<<g, b, 0, st>>>(M, d_shots, ncolw, rows_w, nwt, 0); });
-  run(3, [&] { k_el_velocity_rows<T, true><<<g, b, 0, st>>>(M, d_shots, ncolw, rows_w, nwt, 0); });
-  run(4, [&] { k_el_adj1_rows<T><<<g, b, 0, st>>>(M, d_shots, ncolw, rows_w, nwt, 0); });
-  run(5, [&] { k_el_adj2_rows<T><<<g, b, 0, st>>>(M, d_shots, ncolw, rows_w, nwt, 0); });
-  run(6, [&] { k_el_adj3_rows<T><<<g, b, 0, st>>>(M, d_shots, ncolw, rows_w, nwt); });
+  run(0, [&] {
+    pair(st,
+         [&](cudaStream_t s) { k_el_stress_rows<T, false, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in, 0); },
+         [&](cudaStream_t s) { k_el_stress_rows<T, false, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm, 0); });
+  });
+  run(1, [&] {
+    pair(st,
+         [&](cudaStream_t s) { k_el_velocity_rows<T, false, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in, 0); },
+         [&](cudaStream_t s) { k_el_velocity_rows<T, false, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm, 0); });
+  });
+  run(2, [&] {
+    pair(st,
+         [&](cudaStream_t s) { k_el_stress_rows<T, true, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in, 0); },
+         [&](cudaStream_t s) { k_el_stress_rows<T, true, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm, 0); });
+  });
+  run(3, [&] {
+    pair(st,
+         [&](cudaStream_t s) { k_el_velocity_rows<T, true, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in, 0); },
+         [&](cudaStream_t s) { k_el_velocity_rows<T, true, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm, 0); });
+  });
+  run(4, [&] {
+    pair(st,
+         [&](cudaStream_t s) { k_el_adj1_rows<T, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in, 0); },
+         [&](cudaStream_t s) { k_el_adj1_rows<T, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm, 0); });
+  });
+  run(5, [&] {
+    pair(st,
+         [&](cudaStream_t s) { k_el_adj2_rows<T, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in, 0); },
+         [&](cudaStream_t s) { k_el_adj2_rows<T, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm, 0); });
+  });
+  run(6, [&] {
+    pair(st,
+         [&](cudaStream_t s) { k_el_adj3_rows<T, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in); },
+         [&](cudaStream_t s) { k_el_adj3_rows<T, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm); });
+  });
   run(7, [&] { k_el_src_rcv<T><<<nshots, rcv_threads(), 0, st>>>(d_shots, 1, NSTEP + 1, 1); });
   run(8, [&] { k_el_resid<T><<<grid_resid(), 256, 0, st>>>(d_shots, 1, NSTEP + 1); });
-  ADS_LAUNCHED(9 * (kProfileReps + 1));
+  note_launches(2 * (kProfileReps + 1));  // the pairs count their own launches
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc != ADS_OK) return rc;
