@@ -101,6 +101,8 @@ _SIGS = {
     "ads_acoustic_plan_profile": [P, P, P, P, P],
     "ads_acoustic_plan_forward": [P, P, P, P],
     "ads_acoustic_plan_gradient": [P, P, P, P, P, P, P],
+    "ads_acoustic_plan_gradient_ex": [P, P, P, P, P, P, P, P],
+    "ads_acoustic_plan_source_offset": [P, I64],
     "ads_acoustic_forward": [P, P, P, P, P],
     "ads_acoustic_gradient": [P, P, P, P, P, P, P],
     "ads_elastic_plan_create": [P, P, P, I64, P],
@@ -122,6 +124,7 @@ _RESTYPE = {
     "ads_version": C.c_char_p,
     "ads_launch_count": C.c_int64,
     "ads_acoustic_plan_trace_offset": C.c_int64,
+    "ads_acoustic_plan_source_offset": C.c_int64,
     "ads_acoustic_plan_trace_count": C.c_int64,
     "ads_acoustic_plan_device_bytes": C.c_int64,
     "ads_acoustic_plan_launches": C.c_int64,

@@ -244,7 +244,10 @@ class AcousticPlan:
         call("ads_acoustic_plan_forward", self._h, _ptr(vp), _ptr(tr), _stream())
         return tr[:self.trace_count]
 
-    def gradient(self, vp, observed, want_traces=False):
+    def gradient(self, vp, observed, want_traces=False, want_source_grad=False):
+        """(loss, grad_vp[, traces][, grad_srcv]): grad_srcv is a list of per-shot
+        (nstep, nsrc) FP64 tensors, d loss / d srcv (the gradient the reference's
+        ScatterAdd backward gives a variable source, src/Utils.jl:603-640)."""
         _require_cuda(vp, observed)
         vp = vp.contiguous().to(torch.float64)
         obs = observed.contiguous().to(self.dtype)
@@ -252,6 +255,19 @@ class AcousticPlan:
         grad = torch.empty_like(vp)
         tr = (torch.empty(max(self.trace_count, 1), dtype=self.dtype, device=vp.device)
               if want_traces else None)
+        if want_source_grad:
+            total = sum(int(s["nstep"]) * len(s["srci"]) for s in self.shots)
+            gs = torch.zeros(max(total, 1), dtype=torch.float64, device=vp.device)
+            call("ads_acoustic_plan_gradient_ex", self._h, _ptr(vp), _ptr(obs), _ptr(loss),
+                 _ptr(grad), _ptr(gs), _ptr(tr), _stream())
+            L = lib()
+            per_shot = []
+            for k, s in enumerate(self.shots):
+                o = L.ads_acoustic_plan_source_offset(self._h, k)
+                n, m = int(s["nstep"]), len(s["srci"])
+                per_shot.append(gs[o:o + n * m].view(n, m))
+            out = (loss[0], grad) + ((tr[:self.trace_count],) if want_traces else ())
+            return out + (per_shot,)
         call("ads_acoustic_plan_gradient", self._h, _ptr(vp), _ptr(obs), _ptr(loss), _ptr(grad),
              _ptr(tr), _stream())
         if want_traces:

@@ -110,6 +110,8 @@ struct AcShot {
   float* gc32;        // FP32 per-segment partial of grad_c (FP32 plans)
   const T* srcv;      // (nstep, nsrc), already multiplied by dt^2
   T *traces, *resid;  // (nstep+1, nrcv) packed views
+  double* gsrc;       // d loss / d srcv, (nstep, nsrc) FP64
+  const CellRef* src_list;  // the shot's sources (pitched cell, index, row)
 };
 
 template <typename T>
@@ -530,6 +532,23 @@ __device__ __forceinline__ void add_grad(const AcShot<T>& sh, int64_t row, const
   }
 }
 
+// Source-time gradient: the forward adds srcv[t-1] dt^2 to u_t at a source
+// cell (t >= 2), so d loss / d srcv[t-1] = dt^2 lambdaU_t there.  After the
+// adjoint step k (and the residuals of slot k-1) lambdaU_{k-1} is final: the
+// warp that wrote a source cell records it.
+template <typename T, int C>
+__device__ __forceinline__ void record_src_grad(const AcItem& it, const AcShot<T>& sh,
+                                                const CellRef* __restrict__ srcs, const T* lun,
+                                                int k, int lane, int i0, int i_end, double dt2) {
+  if (k - 1 < 2 || it.src_e <= it.src_b) return;
+  __syncwarp();
+  for (int e = it.src_b + lane; e < it.src_e; e += 32) {
+    const CellRef r = srcs[e];
+    if (r.row >= i0 && r.row < i_end)
+      sh.gsrc[(int64_t)(k - 2) * sh.nsrc + r.idx] = dt2 * (double)lun[r.cell];
+  }
+}
+
 // Residuals of step k-1 go to receiver cells this warp's lanes wrote in the
 // adjoint step: a warp barrier suffices.
 template <typename T, int C>
@@ -559,7 +578,8 @@ __device__ __forceinline__ void inject_residuals(const AcItem& it, const AcShot<
 template <typename T, bool INT>
 __global__ void __launch_bounds__(Tile<T>::TPB, INT ? Tile<T>::MINB_AI : Tile<T>::MINB_A)
 k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
-         const CellRef* __restrict__ rcvs, AcConst<T> K, int k, int base, int ri) {
+         const CellRef* __restrict__ srcs, const CellRef* __restrict__ rcvs, AcConst<T> K,
+         int k, int base, int ri, double dt2) {
   constexpr int C = Tile<T>::CA;
   using V = Vec<T, C>;
   const AcItem it = items[blockIdx.x];
@@ -707,7 +727,10 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       hcq[PF - 1] = hcn;
       hwq[PF - 1] = hwn;
     }
-    if constexpr (!INT) inject_residuals<T, C>(it, sh, rcvs, lun, k, lane, i0, i_end);
+    if constexpr (!INT) {
+      inject_residuals<T, C>(it, sh, rcvs, lun, k, lane, i0, i_end);
+      record_src_grad<T, C>(it, sh, srcs, lun, k, lane, i0, i_end, dt2);
+    }
   } else {
   // rows i-1 (m), i (0), i+1 (p): lambdaU_k, lambdaPhi_k, c and 1/den per cell
   V gum = ldv<T, C>(luc, off(i0 - 1), jld), gpm = ldv<T, C>(lpc, off(i0 - 1), jld && nz(i0 - 1)),
@@ -830,6 +853,7 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     n0 = n1;
   }
   inject_residuals<T, C>(it, sh, rcvs, lun, k, lane, i0, i_end);
+  record_src_grad<T, C>(it, sh, srcs, lun, k, lane, i0, i_end, dt2);
   }
 }
 
@@ -1094,13 +1118,19 @@ __global__ void k_reduce_sum(const double* __restrict__ partial, int n, double* 
 template <typename T>
 __global__ void k_ac_adj_init(const AcShot<T>* __restrict__ shots,
                               const CellRef* __restrict__ rcvs, const int* __restrict__ rcv_b,
-                              const int* __restrict__ rcv_e) {
+                              const int* __restrict__ rcv_e, double dt2) {
   const int s = blockIdx.x;
   const AcShot<T>& sh = shots[s];
   T* lu = sh.lu + (int64_t)(sh.nstep & 1) * sh.fs;
   for (int e = rcv_b[s] + threadIdx.x; e < rcv_e[s]; e += blockDim.x) {
     const CellRef r = rcvs[e];
     atomicAdd(lu + r.cell, sh.resid[(int64_t)sh.nstep * sh.nrcv + r.idx]);
+  }
+  // lambdaU_T is final: source-time gradient of the last row, srcv[T-1]
+  __syncthreads();
+  for (int e = threadIdx.x; e < sh.nsrc; e += blockDim.x) {
+    const CellRef r = sh.src_list[e];
+    sh.gsrc[(int64_t)(sh.nstep - 1) * sh.nsrc + r.idx] = dt2 * (double)lu[r.cell];
   }
 }
 
@@ -1142,10 +1172,12 @@ struct AcPlanBase {
   virtual ~AcPlanBase() = default;
   virtual int forward(const double* vp, void* traces, cudaStream_t st) = 0;
   virtual int gradient(const double* vp, const void* obs, double* loss, double* grad,
-                       void* traces_out, cudaStream_t st) = 0;
+                       void* traces_out, cudaStream_t st, double* grad_srcv) = 0;
   virtual int profile(const double* vp, const void* obs, double* out, cudaStream_t st) = 0;
   std::vector<int64_t> trace_off;
   int64_t trace_total = 0;
+  std::vector<int64_t> src_off;  // per caller shot: offset of its (nstep, nsrc) block
+  int64_t src_total = 0;
   int64_t bytes = 0;
   int64_t launches_fwd = 0, launches_grad = 0;
 };
@@ -1194,6 +1226,7 @@ struct AcPlan final : AcPlanBase {
   int launch_adj(cudaStream_t st, int na, int k, int base);
   std::vector<int> rcv_b_host, rcv_e_host;
   AcConst<T> kc{};
+  double dt2d = 0;  // dt^2 in FP64 (source-time gradient)
   // device
   char* pool = nullptr;
   size_t pool_bytes = 0;
@@ -1263,7 +1296,7 @@ struct AcPlan final : AcPlanBase {
   int run_loop(int which, cudaStream_t st);
   int forward(const double* vp, void* traces, cudaStream_t st) override;
   int gradient(const double* vp, const void* obs, double* loss, double* grad,
-               void* traces_out, cudaStream_t st) override;
+               void* traces_out, cudaStream_t st, double* grad_srcv) override;
 };
 
 template <typename T>
@@ -1312,6 +1345,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   kc.dt = (T)dt;
   kc.hdt = (T)(dt / 2);
   kc.dt2 = (T)(dt * dt);
+  dt2d = dt * dt;
   kc.cx = (T)((dt / hx) * (dt / hx));
   kc.cy = (T)((dt / hy) * (dt / hy));
   kc.kxy = (T)(2 * dt * dt / hx / hx + 2 * dt * dt / hy / hy);
@@ -1365,16 +1399,20 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   // ---- trace layout (packed in the caller's shot order)
   trace_off.resize(ns);
   trace_total = 0;
+  src_off.resize(ns);
+  src_total = 0;
   for (int s = 0; s < ns; s++) {
     trace_off[s] = trace_total;
     trace_total += (shots[s].nstep + 1) * shots[s].nrcv;
+    src_off[s] = src_total;
+    src_total += shots[s].nstep * shots[s].nsrc;
   }
   // ---- memory layout
   const int64_t pitch = grid_pitch(MY);
   size_t off_fwd_begin, off_fwd_end, off_adj_begin, off_adj_end;
   DevPool L;
   struct Offs {
-    size_t u, u2, p, q, seg, ckpt, lu, lp, lq, c, sx, ty, gc, gc32, srcv;
+    size_t u, u2, p, q, seg, ckpt, lu, lp, lq, c, sx, ty, gc, gc32, gsrc, srcv, slist;
   };
   std::vector<Offs> offs(ns);
   std::vector<int> nseg(ns);
@@ -1401,6 +1439,8 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     offs[s].lq = L.take(2 * fs);
     offs[s].gc = L.take((shots[order[s]].nx + 2) * pitch * sizeof(double));
     offs[s].gc32 = L.take(sizeof(T) == 4 ? (shots[order[s]].nx + 2) * pitch * sizeof(float) : 0);
+    offs[s].gsrc = L.take(sizeof(double) * std::max<int64_t>(shots[order[s]].nstep *
+                                                             shots[order[s]].nsrc, 1));
   }
   off_adj_end = L.used;
   for (int s = 0; s < ns; s++) {
@@ -1412,6 +1452,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     offs[s].sx = L.take(sizeof(T) * (h.nx + 2));
     offs[s].ty = L.take(sizeof(T) * (MY + 2));
     offs[s].srcv = L.take(sizeof(T) * std::max<int64_t>(h.nstep * h.nsrc, 1));
+    offs[s].slist = L.take(sizeof(CellRef) * std::max<int64_t>(h.nsrc, 1));
   }
   const size_t resid_off = L.take(sizeof(T) * std::max<int64_t>(trace_total, 1));
   const size_t partial_off = L.take(sizeof(double) * kMisfitBlocks);
@@ -1612,6 +1653,20 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     d.ty = (T*)(pool + offs[s].ty);
     d.gc = (double*)(pool + offs[s].gc);
     d.gc32 = sizeof(T) == 4 ? (float*)(pool + offs[s].gc32) : nullptr;
+    d.gsrc = (double*)(pool + offs[s].gsrc);
+    d.src_list = (const CellRef*)(pool + offs[s].slist);
+    if (h.nsrc > 0) {
+      std::vector<CellRef> sl(h.nsrc);
+      for (int64_t k = 0; k < h.nsrc; k++) {
+        const int i = (int)h.srci[k] - 1, jj = (int)h.srcj[k] - 1;
+        sl[k] = {(int64_t)i * pitch + jj + JOFF, (int)k, i};
+      }
+      std::vector<T> bytes_((sizeof(CellRef) * sl.size() + sizeof(T) - 1) / sizeof(T));
+      std::memcpy(bytes_.data(), sl.data(), sizeof(CellRef) * sl.size());
+      host_bufs.emplace_back(std::move(bytes_));
+      ADS_CUDA(cudaMemcpyAsync((void*)d.src_list, host_bufs.back().data(),
+                               sizeof(CellRef) * sl.size(), cudaMemcpyHostToDevice, st));
+    }
     d.srcv = (const T*)(pool + offs[s].srcv);
     d.traces = d_traces + trace_off[order[s]];
     d.resid = d_resid + trace_off[order[s]];
@@ -1850,12 +1905,13 @@ int AcPlan<T>::launch_adj(cudaStream_t st, int na, int k, int base) {
     sp = side;
   }
   if (ni > 0) {
-    k_ac_adj<T, true><<<ni, TPB, 0, st>>>(ta.items, d_shots, ta.rcvs, kc, k, base, ri);
+    k_ac_adj<T, true><<<ni, TPB, 0, st>>>(ta.items, d_shots, ta.srcs, ta.rcvs, kc, k, base, ri,
+                                          dt2d);
     ADS_LAUNCHED(1);
   }
   if (np > 0) {
-    k_ac_adj<T, false><<<np, TPB, 0, sp>>>(ta.items + ta.pm_off, d_shots, ta.rcvs, kc, k, base,
-                                           ri);
+    k_ac_adj<T, false><<<np, TPB, 0, sp>>>(ta.items + ta.pm_off, d_shots, ta.srcs, ta.rcvs, kc,
+                                           k, base, ri, dt2d);
     ADS_LAUNCHED(1);
   }
   if (fork) {
@@ -2018,7 +2074,7 @@ int AcPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
   int64_t n = 0;
   if (!count) {
     ADS_CUDA(cudaMemsetAsync(pool + zero_adj_off, 0, zero_adj_len, st));
-    k_ac_adj_init<T><<<nshots, 128, 0, st>>>(d_shots, d_shot_rcvs, d_rcv_b, d_rcv_e);
+    k_ac_adj_init<T><<<nshots, 128, 0, st>>>(d_shots, d_shot_rcvs, d_rcv_b, d_rcv_e, dt2d);
     ADS_LAUNCHED(1);
   }
   n++;
@@ -2107,7 +2163,7 @@ int AcPlan<T>::forward(const double* vp, void* traces, cudaStream_t st) {
 
 template <typename T>
 int AcPlan<T>::gradient(const double* vp, const void* obs, double* loss, double* grad,
-                        void* traces_out, cudaStream_t st) {
+                        void* traces_out, cudaStream_t st, double* grad_srcv) {
   ADS_REQUIRE(vp && obs && loss && grad, "null argument");
   k_ac_prep<T><<<dim3(256, nshots), 256, 0, st>>>(d_shots, vp, cfg.MY + 2);
   ADS_LAUNCHED(1);
@@ -2125,6 +2181,14 @@ int AcPlan<T>::gradient(const double* vp, const void* obs, double* loss, double*
   if (traces_out)
     ADS_CUDA(cudaMemcpyAsync(traces_out, d_traces, sizeof(T) * trace_total,
                              cudaMemcpyDeviceToDevice, st));
+  if (grad_srcv)  // per shot (nstep, nsrc), packed in the caller's shot order
+    for (int s = 0; s < nshots; s++) {
+      const AcShot<T>& h = hshots[s];
+      const size_t n = (size_t)h.nstep * h.nsrc;
+      if (n)
+        ADS_CUDA(cudaMemcpyAsync(grad_srcv + src_off[order[s]], h.gsrc, sizeof(double) * n,
+                                 cudaMemcpyDeviceToDevice, st));
+    }
   return ADS_OK;
 }
 
@@ -2233,7 +2297,21 @@ int ads_acoustic_plan_gradient(ads_acoustic_plan* plan, const double* vp,
                                const void* observed, double* loss, double* grad_vp,
                                void* traces_out, ads_stream_t stream) {
   ADS_REQUIRE(plan, "null plan");
-  return plan->impl->gradient(vp, observed, loss, grad_vp, traces_out, (cudaStream_t)stream);
+  return plan->impl->gradient(vp, observed, loss, grad_vp, traces_out, (cudaStream_t)stream,
+                              nullptr);
+}
+
+int ads_acoustic_plan_gradient_ex(ads_acoustic_plan* plan, const double* vp,
+                                  const void* observed, double* loss, double* grad_vp,
+                                  double* grad_srcv, void* traces_out, ads_stream_t stream) {
+  ADS_REQUIRE(plan, "null plan");
+  return plan->impl->gradient(vp, observed, loss, grad_vp, traces_out, (cudaStream_t)stream,
+                              grad_srcv);
+}
+
+int64_t ads_acoustic_plan_source_offset(const ads_acoustic_plan* plan, int64_t shot) {
+  if (!plan || shot < 0 || shot >= (int64_t)plan->impl->src_off.size()) return -1;
+  return plan->impl->src_off[shot];
 }
 
 int ads_acoustic_forward(const ads_acoustic_config* cfg, const ads_acoustic_shot* shot,

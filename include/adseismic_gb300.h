@@ -299,6 +299,17 @@ int ads_acoustic_plan_forward(ads_acoustic_plan* plan, const double* vp, void* t
 int ads_acoustic_plan_gradient(ads_acoustic_plan* plan, const double* vp,
                                const void* observed, double* loss, double* grad_vp,
                                void* traces_out, ads_stream_t stream);
+/* The same plus the source-time gradient grad_srcv = d loss / d srcv: the
+ * gradient ScatterAddOps_backward (ScatterAddOps.h:9-18) gives the wavelet of
+ * a source injected into u by src/Core.jl:600-601 (variable_source,
+ * src/Utils.jl:603-640).  grad_srcv: device doubles, per shot an (nstep, nsrc)
+ * row-major block at ads_acoustic_plan_source_offset(plan, shot), in the
+ * caller's shot order; row 0 (never injected) is 0.  May be NULL. */
+int ads_acoustic_plan_gradient_ex(ads_acoustic_plan* plan, const double* vp,
+                                  const void* observed, double* loss, double* grad_vp,
+                                  double* grad_srcv, void* traces_out, ads_stream_t stream);
+/* Offset (doubles) of a shot's block in grad_srcv; -1 for a bad index. */
+int64_t ads_acoustic_plan_source_offset(const ads_acoustic_plan* plan, int64_t shot);
 
 /* One-shot conveniences (plan + run + destroy; they synchronise `stream`). */
 int ads_acoustic_forward(const ads_acoustic_config* cfg, const ads_acoustic_shot* shot,

@@ -158,17 +158,25 @@ def acoustic_forward(NX, NY, NSTEP, dt, hx, hy, sigma, tau, vp, srci, srcj, srcv
 
 
 def acoustic_gradient(NX, NY, NSTEP, dt, hx, hy, sigma, tau, vp, srci, srcj, srcv,
-                      rcvi, rcvj, obs, variant=0, use_ref=False):
+                      rcvi, rcvj, obs, variant=0, use_ref=False, want_src=False):
+    """(loss, grad_vp), or (loss, grad_vp, grad_srcv (NSTEP, nsrc)) with want_src."""
     N = (NX + 2) * (NY + 2)
     srci, srcj, rcvi, rcvj = map(_i64, (srci, srcj, rcvi, rcvj))
     srcv, obs = _f64(srcv).reshape(-1), _f64(obs).reshape(-1)
     sigma, tau, vp = map(_f64, (sigma, tau, vp))
     g = np.empty(N)
-    f = ref().ref_acoustic_gradient if use_ref else lib().orc_acoustic_gradient
-    f.restype = C.c_double
     args = [C.c_int64(NX), C.c_int64(NY), C.c_int64(NSTEP), C.c_double(dt), C.c_double(hx),
             C.c_double(hy), _d(sigma), _d(tau), _d(vp), C.c_int64(len(srci)), _i(srci),
             _i(srcj), _d(srcv), C.c_int64(len(rcvi)), _i(rcvi), _i(rcvj), _d(obs), _d(g)]
+    if want_src:
+        assert not use_ref
+        gs = np.empty((NSTEP, len(srci)))
+        f = lib().orc_acoustic_gradient_src
+        f.restype = C.c_double
+        loss = f(*args, _d(gs), C.c_int(variant))
+        return loss, g, gs
+    f = ref().ref_acoustic_gradient if use_ref else lib().orc_acoustic_gradient
+    f.restype = C.c_double
     if use_ref:
         assert variant == 0
         loss = f(*args)

@@ -246,6 +246,14 @@ void orc_acoustic_forward(int64_t NX, int64_t NY, int64_t NSTEP, double dt, doub
  * for the while_loop of src/Core.jl:614 and the gradients call of
  * src/Utils.jl:312; loss = sum((rcvv - obs)^2) (Utils.jl:308); c = vp^2
  * (Core.jl:564) so grad_vp = (grad_c * 2) * vp. */
+static double acoustic_gradient_impl(int64_t NX, int64_t NY, int64_t NSTEP, double dt,
+                                     double hx, double hy, const double* sigma,
+                                     const double* tau, const double* vp, int64_t nsrc,
+                                     const int64_t* srci, const int64_t* srcj,
+                                     const double* srcv, int64_t nrcv, const int64_t* rcvi,
+                                     const int64_t* rcvj, const double* obs, double* grad_vp,
+                                     double* grad_srcv, int variant);
+
 double orc_acoustic_gradient(int64_t NX, int64_t NY, int64_t NSTEP, double dt,
                              double hx, double hy, const double* sigma,
                              const double* tau, const double* vp, int64_t nsrc,
@@ -253,6 +261,33 @@ double orc_acoustic_gradient(int64_t NX, int64_t NY, int64_t NSTEP, double dt,
                              const double* srcv, int64_t nrcv, const int64_t* rcvi,
                              const int64_t* rcvj, const double* obs, double* grad_vp,
                              int variant) {
+  return acoustic_gradient_impl(NX, NY, NSTEP, dt, hx, hy, sigma, tau, vp, nsrc, srci, srcj,
+                                srcv, nrcv, rcvi, rcvj, obs, grad_vp, NULL, variant);
+}
+
+/* The same plus the source-time gradient: the loop adds srcv[t-1] dt^2 to
+ * u_t at the source cell (t >= 2), the ScatterAdd of src/Core.jl:600-601, so
+ * d loss / d srcv[t-1][s] = dt^2 lambdaU_t[cell s] (ScatterAddOps_backward,
+ * ScatterAddOps.h:9-18); row 0 is never injected and stays 0.  grad_srcv:
+ * (NSTEP, nsrc). */
+double orc_acoustic_gradient_src(int64_t NX, int64_t NY, int64_t NSTEP, double dt,
+                                 double hx, double hy, const double* sigma,
+                                 const double* tau, const double* vp, int64_t nsrc,
+                                 const int64_t* srci, const int64_t* srcj,
+                                 const double* srcv, int64_t nrcv, const int64_t* rcvi,
+                                 const int64_t* rcvj, const double* obs, double* grad_vp,
+                                 double* grad_srcv, int variant) {
+  return acoustic_gradient_impl(NX, NY, NSTEP, dt, hx, hy, sigma, tau, vp, nsrc, srci, srcj,
+                                srcv, nrcv, rcvi, rcvj, obs, grad_vp, grad_srcv, variant);
+}
+
+static double acoustic_gradient_impl(int64_t NX, int64_t NY, int64_t NSTEP, double dt,
+                                     double hx, double hy, const double* sigma,
+                                     const double* tau, const double* vp, int64_t nsrc,
+                                     const int64_t* srci, const int64_t* srcj,
+                                     const double* srcv, int64_t nrcv, const int64_t* rcvi,
+                                     const int64_t* rcvj, const double* obs, double* grad_vp,
+                                     double* grad_srcv, int variant) {
   const int64_t N = (NX + 2) * (NY + 2), T = NSTEP;
   const int64_t S = NY + 2;
   double* c = (double*)malloc(sizeof(double) * N);
@@ -309,6 +344,12 @@ double orc_acoustic_gradient(int64_t NX, int64_t NY, int64_t NSTEP, double dt,
     }
   }
   for (int64_t x = 0; x < N; x++) grad_vp[x] = gcacc[x] * 2 * vp[x];
+  if (grad_srcv) {
+    for (int64_t k = 0; k < nsrc; k++) grad_srcv[k] = 0.0;
+    for (int64_t t = 2; t <= T; t++)
+      for (int64_t s = 0; s < nsrc; s++)
+        grad_srcv[(t - 1) * nsrc + s] = dt2 * LU[t * N + (srci[s] - 1) * S + srcj[s] - 1];
+  }
   free(c); free(UH); free(PH); free(QH); free(rcvv); free(LU); free(LP); free(LQ);
   free(gw); free(gwo); free(gp); free(gq); free(gc); free(gcacc); free(UP);
   return loss;

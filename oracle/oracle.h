@@ -68,6 +68,14 @@ double orc_acoustic_gradient(int64_t NX, int64_t NY, int64_t NSTEP, double dt,
                              const double* srcv, int64_t nrcv, const int64_t* rcvi,
                              const int64_t* rcvj, const double* obs, double* grad_vp,
                              int variant);
+/* orc_acoustic_gradient plus grad_srcv (NSTEP, nsrc): d loss / d srcv. */
+double orc_acoustic_gradient_src(int64_t NX, int64_t NY, int64_t NSTEP, double dt,
+                                 double hx, double hy, const double* sigma,
+                                 const double* tau, const double* vp, int64_t nsrc,
+                                 const int64_t* srci, const int64_t* srcj,
+                                 const double* srcv, int64_t nrcv, const int64_t* rcvi,
+                                 const int64_t* rcvj, const double* obs, double* grad_vp,
+                                 double* grad_srcv, int variant);
 
 /* ---------------- elastic ---------------- */
 

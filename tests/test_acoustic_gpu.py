@@ -297,3 +297,40 @@ def test_dropin_operator_chain_matches_reference_golden(ads, cuda):
     torch.cuda.synchronize()
     assert abs(float(loss) - float(g["loss"])) <= TOL64 * float(g["loss"])
     assert rel(grad.cpu().numpy().reshape(-1), g["grad_vp"]) <= TOL64
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", TOL64), ("f32", 1e-4)])
+def test_source_time_gradient_vs_oracle(ads, orc, cuda, precision, tol):
+    """d loss / d srcv from the plan's adjoint (two shots of different length
+    and source count, one source on a receiver's cell) against the oracle."""
+    rng = np.random.default_rng(11)
+    NX, NY, h, dt, npml = 40, 36, 10.0, 1e-3, 8
+    N = (NX + 2) * (NY + 2)
+    vp = 2000 + 400 * rng.random(N)
+    s, t = orc.acoustic_pml(NX, NY, h, h, npml, 2000.0)
+    rcvi, rcvj = np.arange(10, 34), np.full(24, 12)
+    cases = [dict(nstep=70, srci=[20, 15], srcj=[20, 12]), dict(nstep=55, srci=[25], srcj=[18])]
+    shots, obs, want = [], [], []
+    for c in cases:
+        nt = c["nstep"]
+        srcv = rng.standard_normal((nt, len(c["srci"]))) * 1e4
+        o = orc.acoustic_forward(NX, NY, nt, dt, h, h, s, t, vp * 1.04, c["srci"], c["srcj"],
+                                 srcv, rcvi, rcvj)
+        _, _, gs = orc.acoustic_gradient(NX, NY, nt, dt, h, h, s, t, vp, c["srci"], c["srcj"],
+                                         srcv, rcvi, rcvj, o, want_src=True)
+        shots.append(dict(x0=0, nx=NX, nstep=nt, srci=c["srci"], srcj=c["srcj"], srcv=srcv,
+                          rcvi=rcvi, rcvj=rcvj))
+        obs.append(T(o.reshape(-1), cuda))
+        want.append(gs)
+    plan = ads.AcousticPlan(NX, NY, h, h, dt, shots, npml=npml, vp_ref=2000.0,
+                            precision=precision, ckpt_every=16)
+    out = plan.gradient(T(vp.reshape(NX + 2, NY + 2), cuda), plan.pack(obs),
+                        want_source_grad=True)
+    torch.cuda.synchronize()
+    got = out[-1]
+    for k in range(len(cases)):
+        g = got[k].cpu().numpy()
+        assert g.shape == want[k].shape
+        assert np.all(g[0] == 0.0)
+        assert rel(g, want[k]) <= tol, (k, rel(g, want[k]))
+    plan.close()

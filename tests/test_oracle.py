@@ -175,3 +175,34 @@ def test_elastic_loss_finite_differences(orc):
         m = list(base); m[k] = base[k] - d
         fd = (loss(*p)[0] - loss(*m)[0]) / 2
         assert abs(fd - np.dot(G, d)) <= 1e-4 * abs(fd), k
+
+
+def test_acoustic_source_gradient_finite_differences(orc):
+    """d loss / d srcv from the oracle's adjoint equals central differences of
+    the loss (two sources, one on a receiver's cell); row 0 is never injected."""
+    rng = np.random.default_rng(4)
+    NX, NY, T = 20, 16, 40
+    N = (NX + 2) * (NY + 2)
+    dt, h = 1e-3, 10.0
+    vp = 2000 + 500 * rng.random(N)
+    s, t = orc.acoustic_pml(NX, NY, h, h, 5, 2000.0)
+    srci, srcj = [11, 8], [6, 3]
+    srcv = rng.standard_normal((T, 2)) * 1e3
+    rcvi, rcvj = np.arange(3, 19), np.full(16, 3)
+    obs = orc.acoustic_forward(NX, NY, T, dt, h, h, s, t, vp * 1.03, srci, srcj, srcv, rcvi,
+                               rcvj)
+    _, _, gs = orc.acoustic_gradient(NX, NY, T, dt, h, h, s, t, vp, srci, srcj, srcv, rcvi,
+                                     rcvj, obs, want_src=True)
+    assert gs.shape == (T, 2) and np.all(gs[0] == 0.0)
+    for (row, k) in [(1, 0), (7, 0), (20, 1), (T - 1, 1), (T - 1, 0)]:
+        e = 1.0
+        sp, sm = srcv.copy(), srcv.copy()
+        sp[row, k] += e
+        sm[row, k] -= e
+        lp = orc.acoustic_gradient(NX, NY, T, dt, h, h, s, t, vp, srci, srcj, sp, rcvi, rcvj,
+                                   obs)[0]
+        lm = orc.acoustic_gradient(NX, NY, T, dt, h, h, s, t, vp, srci, srcj, sm, rcvi, rcvj,
+                                   obs)[0]
+        fd = (lp - lm) / (2 * e)
+        assert abs(fd - gs[row, k]) <= 1e-7 * max(abs(fd), 1e-12 * abs(lp)), (row, k, fd,
+                                                                             gs[row, k])
