@@ -19,6 +19,9 @@ from .elastic import (ElasticPlan, ElasticPropagator, ElasticPropagatorParams,
                       elastic_one_step, elastic_one_step_grad)
 from .elastic import SimulatedObservation as ElasticSimulatedObservation
 from .elastic import compute_PML_Params as compute_elastic_PML_Params
+from .io import (load_acoustic_model, load_acoustic_receiver, load_acoustic_source,
+                 load_elastic_model, load_elastic_receiver, load_elastic_source, load_params)
+from .optim import LBFGS, fwi_lbfgs
 from .utils import (Gauss, Ricker, compute_lame_parameters, compute_properties,
                     folded_layer_model, gaussian_smooth, layered_gaussian_model,
                     ricker_width_samples)

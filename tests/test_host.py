@@ -39,3 +39,30 @@ def test_models_are_seeded(ads):
     assert np.array_equal(a, b) and a.min() >= 1500 and a.max() <= 4500
     v = ads.layered_gaussian_model(60, 60, seed=1)
     assert v.shape == (60, 60) and 1700 < v.min() < v.max() < 4000
+
+
+def test_lbfgs_driver_quadratic():
+    """The L-BFGS loop (f/g from one call, callback(x, iter, loss), loss history)
+    on a convex quadratic: reaches the minimiser."""
+    import pytest
+
+    pytest.importorskip("scipy")
+    import __graft_entry__ as g
+
+    pkg = g.load_package()
+    rng = np.random.default_rng(0)
+    A = rng.standard_normal((12, 12))
+    H = A @ A.T + 12 * np.eye(12)
+    b = rng.standard_normal(12)
+    calls = []
+
+    def fg(x):
+        calls.append(1)
+        return 0.5 * x @ H @ x - b @ x, H @ x - b
+
+    seen = []
+    x, losses = pkg.LBFGS(fg, np.zeros(12), callback=lambda x, it, l: seen.append((it, l)),
+                          max_iter=200, ftol=1e-15, gtol=1e-12)
+    assert np.allclose(x, np.linalg.solve(H, b), rtol=1e-6, atol=1e-8)
+    assert len(losses) == len(seen) and [s[0] for s in seen] == list(range(1, len(seen) + 1))
+    assert all(losses[k + 1] <= losses[k] + 1e-12 for k in range(len(losses) - 1))
