@@ -417,6 +417,10 @@ k_el_adj3(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one) {
 constexpr int EC = 2;             // columns per lane
 constexpr int ESTRIP = 30 * EC;   // columns a warp strip updates
 constexpr int EW = 4;             // warps per CTA (independent strips)
+// Which step kernels launch as two concurrent halves (measured: the stress,
+// velocity and first adjoint kernels gain occupancy from it; the gather-heavy
+// second and third adjoint kernels do better whole).
+constexpr bool kSplitFwd = true, kSplitAdj1 = true, kSplitAdj23 = false;
 #ifndef ADS_EL_MINB
 #define ADS_EL_MINB 6                 // resident CTAs per SM the FP32 kernels are built for
 #endif
@@ -537,7 +541,7 @@ struct ColProf {
 };
 
 // Stress update (fw1 + fw2) of a strip.
-template <typename T, bool STORE, bool INT>
+template <typename T, bool STORE, bool INT, int PART>
 __global__ void __launch_bounds__(EW * 32, INT ? el_minb_int<T>() : el_minb<T>())
 k_el_stress_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __restrict__ wlist,
                  int ncolw, int R, int nwt,
@@ -606,9 +610,10 @@ k_el_stress_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* _
     bool k1[2], k2[2];
 #pragma unroll
     for (int c = 0; c < 2; c++) {
-      k1[c] = r1 && c1[c];
-      k2[c] = r2 && c2[c];
-      // fw1
+      k1[c] = PART != 2 && r1 && c1[c];
+      k2[c] = PART != 1 && r2 && c2[c];
+      nsxx[c] = nsyy[c] = nsxy[c] = e1s[c] = e2s[c] = e12s[c] = T(0);
+      if constexpr (PART != 2) {  // fw1
       const T lam_ = T(0.5) * (L1.v[c] + L0.v[c]);
       const T mu1 = T(0.5) * (U1.v[c] + U0.v[c]);
       const T lm = lam_ + T(2) * mu1;
@@ -624,7 +629,8 @@ k_el_stress_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* _
       nsyy[c] = B0.v[c] + (lm * e2 + lam_ * e1) * M.dt;
       e1s[c] = e1;
       e2s[c] = e2;
-      // fw2
+      }
+      if constexpr (PART != 1) {  // fw2
       const T mu2 = T(0.5) * (ur[c] + ur[c + 1]);
       const T dvydx = d4r<T>(Y2.v[c], Y1.v[c], Y3.v[c], Y0.v[c], M.hx24, M.rhx24);
       const T dvxdy = d4r<T>(xr[2 + c], xr[1 + c], xr[3 + c], xr[c], M.hy24, M.rhy24);
@@ -636,6 +642,7 @@ k_el_stress_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* _
       const T e12 = (dvydx + m3) + (dvxdy + m4);
       nsxy[c] = C0.v[c] + mu2 * e12 * M.dt;
       e12s[c] = e12;
+      }
     }
     st2<T>(sxx, o, nsxx, k1[0], k1[1]);
     st2<T>(syy, o, nsyy, k1[0], k1[1]);
@@ -653,7 +660,7 @@ k_el_stress_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* _
 }
 
 // Velocity update (fw3 + fw4) of a strip, from the new stresses.
-template <typename T, bool STORE, bool INT>
+template <typename T, bool STORE, bool INT, int PART>
 __global__ void __launch_bounds__(EW * 32, INT ? el_minb_int<T>() : el_minb<T>())
 k_el_velocity_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __restrict__ wlist,
                    int ncolw, int R, int nwt,
@@ -725,9 +732,10 @@ k_el_velocity_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int*
     bool k3[2], k4[2];
 #pragma unroll
     for (int c = 0; c < 2; c++) {
-      k3[c] = r3 && c3[c];
-      k4[c] = r4 && c4[c];
-      // fw3
+      k3[c] = PART != 2 && r3 && c3[c];
+      k4[c] = PART != 1 && r4 && c4[c];
+      nvx[c] = nvy[c] = a3s[c] = a4s[c] = T(0);
+      if constexpr (PART != 2) {  // fw3
       const T a = d4r<T>(S2.v[c], S1.v[c], S3.v[c], S0.v[c], M.hx24, M.rhx24);
       const T b = d4r<T>(qr[2 + c], qr[1 + c], qr[3 + c], qr[c], M.hy24, M.rhy24);
       const bool u5 = k3[c] && rx5, u6 = !INT && k3[c] && Y.acti[c];
@@ -738,7 +746,8 @@ k_el_velocity_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int*
       const T e3 = (a + m5) + (b + m6);
       nvx[c] = VX0.v[c] + divr<T>(e3 * M.dt, r0[c]);
       a3s[c] = e3;
-      // fw4
+      }
+      if constexpr (PART != 1) {  // fw4
       const T rho_ = T(0.25) * (r0[c] + r1[c] + r1[c + 1] + r0[c + 1]);
       const T a4 = d4r<T>(Q2.v[c], Q1.v[c], Q3.v[c], Q0.v[c], M.hx24, M.rhx24);
       const T b4 = d4r<T>(wr[2 + c], wr[1 + c], wr[3 + c], wr[c], M.hy24, M.rhy24);
@@ -750,6 +759,7 @@ k_el_velocity_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int*
       const T e4 = (a4 + m7) + (b4 + m8);
       nvy[c] = VY0.v[c] + divr<T>(e4 * M.dt, rho_);
       a4s[c] = e4;
+      }
     }
     st2<T>(vx, o, nvx, k3[0], k3[1]);
     st2<T>(vy, o, nvy, k4[0], k4[1]);
@@ -797,7 +807,7 @@ __device__ __forceinline__ T hdiv(T x, T h24, T rh24) {
 }
 
 // Adjoint 1 (velocity cells) of a strip: transposes of fw3 and fw4.
-template <typename T, bool INT>
+template <typename T, bool INT, int PART>
 __global__ void __launch_bounds__(EW * 32, INT ? el_minb_int<T>() : el_minb<T>())
 k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __restrict__ wlist,
                int ncolw, int R, int nwt,
@@ -861,9 +871,11 @@ k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
     bool k3[2], k4[2];
 #pragma unroll
     for (int c = 0; c < 2; c++) {
-      k3[c] = r3 && c3[c];
-      k4[c] = r4 && c4[c];
-      // fw3 transpose
+      k3[c] = PART != 2 && r3 && c3[c];
+      k4[c] = PART != 1 && r4 && c4[c];
+      o5[c] = o6[c] = o7[c] = o8[c] = o4[c] = T(0);
+      gr[c] = A(0);
+      if constexpr (PART != 2) {  // fw3 transpose
       const T gv = GX.v[c], r = r0[c];
       const T q = divr<T>(gv * M.dt, r);
       const bool u5 = k3[c] && rx5, u6 = !INT && k3[c] && Y.acti[c];
@@ -874,7 +886,8 @@ k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
       o5[c] = hdiv<T>(q + axi * gm5, M.hx24, M.rhx24);
       o6[c] = hdiv<T>(q + (INT ? T(0) : Y.ai[c]) * gm6, M.hy24, M.rhy24);
       gr[c] = GR.v[c] + (A)divr<T>(-gv * E3.v[c] * M.dt, r * r);
-      // fw4 transpose
+      }
+      if constexpr (PART != 1) {  // fw4 transpose
       const T gw = GY.v[c];
       const T rho_ = T(0.25) * (r0[c] + r1[c] + r1[c + 1] + r0[c + 1]);
       const T q4 = divr<T>(gw * M.dt, rho_);
@@ -886,6 +899,7 @@ k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
       o7[c] = hdiv<T>(q4 + axh * gm7, M.hx24, M.rhx24);
       o8[c] = hdiv<T>(q4 + (INT ? T(0) : Y.ah[c]) * gm8, M.hy24, M.rhy24);
       o4[c] = divr<T>(-gw * E4.v[c] * M.dt, rho_ * rho_) * T(0.25);
+      }
     }
     st2<T>(d5, o, o5, k3[0], k3[1]);
     st2<T>(d6, o, o6, k3[0], k3[1]);
@@ -900,7 +914,7 @@ k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
 
 // Adjoint 2 (stress cells) of a strip: gather D5..D8 into the stress
 // adjoints, then the transposes of fw1 and fw2.
-template <typename T, bool INT>
+template <typename T, bool INT, int PART>
 __global__ void __launch_bounds__(EW * 32, el_minb_adj<T>())
 k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __restrict__ wlist,
                int ncolw, int R, int nwt,
@@ -983,19 +997,19 @@ k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
     bool k1[2], k2[2], k12[2];
 #pragma unroll
     for (int c = 0; c < 2; c++) {
-      k1[c] = r1 && c1[c];
-      k2[c] = r2 && c2[c];
-      k12[c] = k1[c] || k2[c];
+      const bool b1 = r1 && c1[c], b2 = r2 && c2[c];
+      k12[c] = b1 || b2;  // the stress adjoints of these cells are updated
+      k1[c] = PART != 2 && b1;
+      k2[c] = PART != 1 && b2;
+      oxx[c] = oyy[c] = oxy[c] = ol1[c] = om1[c] = od1[c] = od2[c] = T(0);
+      om2[c] = od3[c] = od4[c] = T(0);
       // gathers (zero outside the padded grid: those rows load as zeros and
       // the frame / padding columns of the temporaries are never written)
+      if constexpr (PART != 2) {  // sxx / syy adjoints and the fw1 transpose
       const T gsxx = GA.v[c] + T(27) * P1.v[c] - T(27) * P2.v[c] - P0.v[c] + P3.v[c];
-      const T gsxy = GC.v[c] + T(27) * f6[1 + c] - T(27) * f6[2 + c] - f6[c] + f6[3 + c] +
-                     T(27) * Q1.v[c] - T(27) * Q2.v[c] - Q0.v[c] + Q3.v[c];
       const T gsyy = GB.v[c] + T(27) * f8[1 + c] - T(27) * f8[2 + c] - f8[c] + f8[3 + c];
       oxx[c] = gsxx;
       oyy[c] = gsyy;
-      oxy[c] = gsxy;
-      // fw1 transpose
       const T lam_ = T(0.5) * (L1.v[c] + L0.v[c]);
       const T mu1 = T(0.5) * (U1.v[c] + U0.v[c]);
       const T lm = lam_ + T(2) * mu1;
@@ -1013,7 +1027,11 @@ k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
       if (u2) g2[o + c] = Y.bi[c] * gm2;
       od1[c] = hdiv<T>(gE1 + axh * gm1, M.hx24, M.rhx24);
       od2[c] = hdiv<T>(gE2 + (INT ? T(0) : Y.ai[c]) * gm2, M.hy24, M.rhy24);
-      // fw2 transpose
+      }
+      if constexpr (PART != 1) {  // sxy adjoint and the fw2 transpose
+      const T gsxy = GC.v[c] + T(27) * f6[1 + c] - T(27) * f6[2 + c] - f6[c] + f6[3 + c] +
+                     T(27) * Q1.v[c] - T(27) * Q2.v[c] - Q0.v[c] + Q3.v[c];
+      oxy[c] = gsxy;
       const T mu2 = T(0.5) * (ur[c] + ur[c + 1]);
       const T q = gsxy * mu2 * M.dt;
       om2[c] = gsxy * EC12.v[c] * M.dt * T(0.5);
@@ -1024,10 +1042,13 @@ k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
       if (u4) g4[o + c] = Y.bh[c] * gm4;
       od3[c] = hdiv<T>(q + axi * gm3, M.hx24, M.rhx24);
       od4[c] = hdiv<T>(q + (INT ? T(0) : Y.ah[c]) * gm4, M.hy24, M.rhy24);
+      }
     }
-    st2<T>(gxx, o, oxx, k12[0], k12[1]);
-    st2<T>(gyy, o, oyy, k12[0], k12[1]);
-    st2<T>(gxy, o, oxy, k12[0], k12[1]);
+    if constexpr (PART != 2) {
+      st2<T>(gxx, o, oxx, k12[0], k12[1]);
+      st2<T>(gyy, o, oyy, k12[0], k12[1]);
+    }
+    if constexpr (PART != 1) st2<T>(gxy, o, oxy, k12[0], k12[1]);
     st2<T>(gl1, o, ol1, k1[0], k1[1]);
     st2<T>(gm1p, o, om1, k1[0], k1[1]);
     st2<T>(d1, o, od1, k1[0], k1[1]);
@@ -1046,7 +1067,7 @@ k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
 
 // Adjoint 3 (velocity cells + parameters) of a strip: gather D1..D4 into the
 // velocity adjoints and the lambda / mu / rho parts into the accumulators.
-template <typename T, bool INT>
+template <typename T, bool INT, int PART>
 __global__ void __launch_bounds__(EW * 32, el_minb_adj<T>())
 k_el_adj3_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __restrict__ wlist,
                int ncolw, int R, int nwt) {
@@ -1125,21 +1146,31 @@ k_el_adj3_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
     for (int c = 0; c < 2; c++) {
       k3[c] = r3 && c3[c];
       k4[c] = r4 && c4[c];
+      ovx[c] = ovy[c] = T(0);
+      ol[c] = om[c] = orr[c] = A(0);
+      if constexpr (PART != 2) {  // velocity adjoints
       // D1 rows i-2..i+1 = P0..P3; D4 columns jc-2..jc+1 = f4[c..c+3]
       ovx[c] = VX0.v[c] + (T(27) * P1.v[c] - T(27) * P2.v[c] - P0.v[c] + P3.v[c] +
                            T(27) * f4[1 + c] - T(27) * f4[2 + c] - f4[c] + f4[3 + c]);
       // D2 columns jc-1..jc+2 = f2[c..c+3]; D3 rows i-1..i+2 = Q0..Q3
       ovy[c] = VY0.v[c] + (T(27) * f2[1 + c] - T(27) * f2[2 + c] - f2[c] + f2[3 + c] +
                            T(27) * Q1.v[c] - T(27) * Q2.v[c] - Q0.v[c] + Q3.v[c]);
+      }
+      if constexpr (PART != 1) {  // lambda / mu / rho accumulators
       ol[c] = AL.v[c] + (A)(GL0.v[c] + GLm.v[c]);
       om[c] = AM.v[c] + (A)(GM0.v[c] + GMm.v[c] + g12[1 + c] + g12[c]);
       orr[c] = AR.v[c] + (A)(r0[1 + c] + rm[1 + c] + rm[c] + r0[c]);
+      }
     }
-    st2<T>(gvx, o, ovx, k3[0], k3[1]);
-    st2<T>(gvy, o, ovy, k4[0], k4[1]);
-    st2<A>(al, o, ol, cp[0], cp[1]);
-    st2<A>(am, o, om, cp[0], cp[1]);
-    st2<A>(ar, o, orr, cp[0], cp[1]);
+    if constexpr (PART != 2) {
+      st2<T>(gvx, o, ovx, k3[0], k3[1]);
+      st2<T>(gvy, o, ovy, k4[0], k4[1]);
+    }
+    if constexpr (PART != 1) {
+      st2<A>(al, o, ol, cp[0], cp[1]);
+      st2<A>(am, o, om, cp[0], cp[1]);
+      st2<A>(ar, o, orr, cp[0], cp[1]);
+    }
     P0 = P1; P1 = P2; P2 = P3; P3 = P4;
     Q0 = Q1; Q1 = Q2; Q2 = Q3; Q3 = Q4;
     GLm = GL0; GL0 = GLn; GMm = GM0; GM0 = GMn; RRm = RR0; RR0 = RRn;
@@ -1344,6 +1375,70 @@ std::vector<T> pack_profiles(int64_t NX, int64_t NY, const double* ax, const dou
 
 }  // namespace
 
+// Launchers of the row kernels: (store,) interior / CPML items, part 1 / 2.
+#define ADS_EL_SEL(K, ...)                                    \
+  do {                                                        \
+    if (in) {                                                 \
+      if (part == 0) K(__VA_ARGS__, true, 0);                 \
+      else if (part == 1) K(__VA_ARGS__, true, 1);            \
+      else K(__VA_ARGS__, true, 2);                           \
+    } else {                                                  \
+      if (part == 0) K(__VA_ARGS__, false, 0);                \
+      else if (part == 1) K(__VA_ARGS__, false, 1);           \
+      else K(__VA_ARGS__, false, 2);                          \
+    }                                                         \
+  } while (0)
+
+template <typename T>
+void el_stress(bool store, bool in, int part, dim3 g, cudaStream_t s, const ElModel<T>& M,
+               const ElShot<T>* sh, const int* wl, int ncolw, int R, int nw, int slot) {
+#define ADS_K(ST, IN, PT) \
+  k_el_stress_rows<T, ST, IN, PT><<<g, EW * 32, 0, s>>>(M, sh, wl, ncolw, R, nw, slot)
+  if (store) ADS_EL_SEL(ADS_K, true);
+  else ADS_EL_SEL(ADS_K, false);
+#undef ADS_K
+}
+
+template <typename T>
+void el_velocity(bool store, bool in, int part, dim3 g, cudaStream_t s, const ElModel<T>& M,
+                 const ElShot<T>* sh, const int* wl, int ncolw, int R, int nw, int slot) {
+#define ADS_K(ST, IN, PT) \
+  k_el_velocity_rows<T, ST, IN, PT><<<g, EW * 32, 0, s>>>(M, sh, wl, ncolw, R, nw, slot)
+  if (store) ADS_EL_SEL(ADS_K, true);
+  else ADS_EL_SEL(ADS_K, false);
+#undef ADS_K
+}
+
+template <typename T>
+void el_adj1(bool in, int part, dim3 g, cudaStream_t s, const ElModel<T>& M, const ElShot<T>* sh,
+             const int* wl, int ncolw, int R, int nw, int slot) {
+#define ADS_K(IN, PT) \
+  k_el_adj1_rows<T, IN, PT><<<g, EW * 32, 0, s>>>(M, sh, wl, ncolw, R, nw, slot)
+#define ADS_K1(dummy, IN, PT) ADS_K(IN, PT)
+  ADS_EL_SEL(ADS_K1, 0);
+#undef ADS_K1
+#undef ADS_K
+}
+
+template <typename T>
+void el_adj2(bool in, int part, dim3 g, cudaStream_t s, const ElModel<T>& M, const ElShot<T>* sh,
+             const int* wl, int ncolw, int R, int nw, int slot) {
+#define ADS_K1(dummy, IN, PT) \
+  k_el_adj2_rows<T, IN, PT><<<g, EW * 32, 0, s>>>(M, sh, wl, ncolw, R, nw, slot)
+  ADS_EL_SEL(ADS_K1, 0);
+#undef ADS_K1
+}
+
+template <typename T>
+void el_adj3(bool in, int part, dim3 g, cudaStream_t s, const ElModel<T>& M, const ElShot<T>* sh,
+             const int* wl, int ncolw, int R, int nw) {
+#define ADS_K1(dummy, IN, PT) \
+  k_el_adj3_rows<T, IN, PT><<<g, EW * 32, 0, s>>>(M, sh, wl, ncolw, R, nw)
+  ADS_EL_SEL(ADS_K1, 0);
+#undef ADS_K1
+}
+#undef ADS_EL_SEL
+
 // ======================================================================
 // whole-path elastic plan
 // ======================================================================
@@ -1372,11 +1467,15 @@ struct ElPlan final : ElPlanBase {
   // launches of a step kernel run concurrently (disjoint cells)
   int* d_wl = nullptr;  // interior items, then the CPML items at nw_in
   int nw_in = 0, nw_pm = 0;
-  cudaStream_t side = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  int pair_launches() const { return (nw_in > 0) + (nw_pm > 0); }
-  template <typename FI, typename FP>
-  int pair(cudaStream_t st, FI&& lin, FP&& lpm);
+  cudaStream_t side[3] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[3] = {};
+  // launches of one row-kernel step over the interior and CPML lists, whole
+  // (part 0) or as its two halves (parts 1, 2)
+  int group_launches(bool split) const { return (split ? 2 : 1) * ((nw_in > 0) + (nw_pm > 0)); }
+  // fn(stream, interior, part) for each non-empty list and part, launched
+  // concurrently on the main stream and the side streams (disjoint outputs)
+  template <typename F>
+  int group(cudaStream_t st, bool split, F&& fn);
   int max_rcv = 0;                      // most receivers of a shot
   int64_t P = 0, fs = 0;
   char* pool = nullptr;
@@ -1399,8 +1498,10 @@ struct ElPlan final : ElPlanBase {
     if (gR) cudaGraphDestroy(gR);
     if (cap) cudaStreamDestroy(cap);
     if (ev_fork) cudaEventDestroy(ev_fork);
-    if (ev_join) cudaEventDestroy(ev_join);
-    if (side) cudaStreamDestroy(side);
+    for (auto e : ev_join)
+      if (e) cudaEventDestroy(e);
+    for (auto q : side)
+      if (q) cudaStreamDestroy(q);
     if (pool) cudaFree(pool);
   }
 
@@ -1590,9 +1691,9 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   d_wl = (int*)(pool + wl_o);
   ADS_CUDA(cudaMemcpyAsync(d_wl, wl_host.data(), sizeof(int) * wl_host.size(),
                            cudaMemcpyHostToDevice, st));
-  ADS_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+  for (auto& q : side) ADS_CUDA(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
   ADS_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
-  ADS_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+  for (auto& e : ev_join) ADS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   ADS_CUDA(cudaMemcpyAsync(pool + prof_o, prof.data(), sizeof(T) * prof.size(),
                            cudaMemcpyHostToDevice, st));
   M = make_model<T>(NX, NY, P, JOFF, c.dt, c.dx, c.dy, d_lam, d_mu, d_rho,
@@ -1718,118 +1819,71 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   return ADS_OK;
 }
 
-// The three adjoint passes of step n (store slot `slot`), each as an interior /
-// CPML pair of launches.
-template <typename T>
-int ElPlan<T>::adjoint_step(cudaStream_t st, int slot) {
-  const int* wp = d_wl + nw_in;
-  const dim3 gi = grid_rows(nw_in), gp = grid_rows(nw_pm), b(EW * 32);
-  if (int e = pair(
-          st,
-          [&](cudaStream_t s) {
-            k_el_adj1_rows<T, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in, slot);
-          },
-          [&](cudaStream_t s) {
-            k_el_adj1_rows<T, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm, slot);
-          }))
-    return e;
-  if (int e = pair(
-          st,
-          [&](cudaStream_t s) {
-            k_el_adj2_rows<T, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in, slot);
-          },
-          [&](cudaStream_t s) {
-            k_el_adj2_rows<T, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm, slot);
-          }))
-    return e;
-  return pair(
-      st,
-      [&](cudaStream_t s) {
-        k_el_adj3_rows<T, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in);
-      },
-      [&](cudaStream_t s) {
-        k_el_adj3_rows<T, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm);
-      });
-}
-
 // One forward step n (slot n-1 -> slot n) for every shot.
 template <typename T>
-template <typename FI, typename FP>
-int ElPlan<T>::pair(cudaStream_t st, FI&& lin, FP&& lpm) {
-  const bool fork = nw_in > 0 && nw_pm > 0;
-  cudaStream_t sp = st;
-  if (fork) {
+template <typename F>
+int ElPlan<T>::group(cudaStream_t st, bool split, F&& fn) {
+  bool in_[4];
+  int part_[4], n = 0;
+  for (int l = 0; l < 2; l++) {
+    const bool in = l == 0;
+    if ((in ? nw_in : nw_pm) == 0) continue;
+    for (int part = split ? 1 : 0; part <= (split ? 2 : 0); part++) {
+      in_[n] = in;
+      part_[n++] = part;
+    }
+  }
+  if (n > 1) {
     ADS_CUDA(cudaEventRecord(ev_fork, st));
-    ADS_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
-    sp = side;
+    for (int k = 1; k < n; k++) ADS_CUDA(cudaStreamWaitEvent(side[k - 1], ev_fork, 0));
   }
-  if (nw_in > 0) {
-    lin(st);
+  for (int k = 0; k < n; k++) {
+    fn(k == 0 ? st : side[k - 1], in_[k], part_[k]);
     ADS_LAUNCHED(1);
   }
-  if (nw_pm > 0) {
-    lpm(sp);
-    ADS_LAUNCHED(1);
-  }
-  if (fork) {
-    ADS_CUDA(cudaEventRecord(ev_join, side));
-    ADS_CUDA(cudaStreamWaitEvent(st, ev_join, 0));
+  for (int k = 1; k < n; k++) {
+    ADS_CUDA(cudaEventRecord(ev_join[k - 1], side[k - 1]));
+    ADS_CUDA(cudaStreamWaitEvent(st, ev_join[k - 1], 0));
   }
   return ADS_OK;
+}
+
+// The three adjoint passes of step n (store slot `slot`).
+template <typename T>
+int ElPlan<T>::adjoint_step(cudaStream_t st, int slot) {
+  auto wl = [&](bool in) { return in ? d_wl : d_wl + nw_in; };
+  auto nw = [&](bool in) { return in ? nw_in : nw_pm; };
+  if (int e = group(st, kSplitAdj1, [&](cudaStream_t s, bool in, int part) {
+        el_adj1<T>(in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w, nw(in),
+                   slot);
+      }))
+    return e;
+  if (int e = group(st, kSplitAdj23, [&](cudaStream_t s, bool in, int part) {
+        el_adj2<T>(in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w, nw(in),
+                   slot);
+      }))
+    return e;
+  return group(st, kSplitAdj23, [&](cudaStream_t s, bool in, int part) {
+    el_adj3<T>(in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w, nw(in));
+  });
 }
 
 // One forward step n (slot n-1 -> slot n) for every shot.
 template <typename T>
 int ElPlan<T>::step(cudaStream_t st, int n, bool store, int slot, bool record) {
-  const int* wp = d_wl + nw_in;
-  const dim3 gi = grid_rows(nw_in), gp = grid_rows(nw_pm), b(EW * 32);
-  if (store) {
-    if (int e = pair(
-            st,
-            [&](cudaStream_t s) {
-              k_el_stress_rows<T, true, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w,
-                                                               nw_in, slot);
-            },
-            [&](cudaStream_t s) {
-              k_el_stress_rows<T, true, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w,
-                                                                nw_pm, slot);
-            }))
-      return e;
-    if (int e = pair(
-            st,
-            [&](cudaStream_t s) {
-              k_el_velocity_rows<T, true, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw,
-                                                                 rows_w, nw_in, slot);
-            },
-            [&](cudaStream_t s) {
-              k_el_velocity_rows<T, true, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w,
-                                                                  nw_pm, slot);
-            }))
-      return e;
-  } else {
-    if (int e = pair(
-            st,
-            [&](cudaStream_t s) {
-              k_el_stress_rows<T, false, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w,
-                                                                nw_in, 0);
-            },
-            [&](cudaStream_t s) {
-              k_el_stress_rows<T, false, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w,
-                                                                 nw_pm, 0);
-            }))
-      return e;
-    if (int e = pair(
-            st,
-            [&](cudaStream_t s) {
-              k_el_velocity_rows<T, false, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw,
-                                                                  rows_w, nw_in, 0);
-            },
-            [&](cudaStream_t s) {
-              k_el_velocity_rows<T, false, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw,
-                                                                   rows_w, nw_pm, 0);
-            }))
-      return e;
-  }
+  auto wl = [&](bool in) { return in ? d_wl : d_wl + nw_in; };
+  auto nw = [&](bool in) { return in ? nw_in : nw_pm; };
+  const int sl = store ? slot : 0;
+  if (int e = group(st, kSplitFwd, [&](cudaStream_t s, bool in, int part) {
+        el_stress<T>(store, in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w,
+                     nw(in), sl);
+      }))
+    return e;
+  if (int e = group(st, kSplitFwd, [&](cudaStream_t s, bool in, int part) {
+        el_velocity<T>(store, in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw,
+                       rows_w, nw(in), sl);
+      }))
+    return e;
   k_el_src_rcv<T><<<nshots, rcv_threads(), 0, st>>>(d_shots, n, NSTEP + 1, record ? 1 : 0);
   ADS_LAUNCHED(1);
   return ADS_OK;
@@ -1840,7 +1894,7 @@ int ElPlan<T>::issue_forward(cudaStream_t st, int64_t* count) {
   if (count) {
     int64_t c = 0;
     for (int n = 1; n <= NSTEP; n++)
-      c += 2 * pair_launches() + 1 + ((n % K == 0 && n / K < nseg) ? 1 : 0);
+      c += 2 * group_launches(kSplitFwd) + 1 + ((n % K == 0 && n / K < nseg) ? 1 : 0);
     *count = c;
     return ADS_OK;
   }
@@ -1861,7 +1915,8 @@ int ElPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     int64_t c = 1;
     for (int s = nseg - 1; s >= 0; s--) {
       const int a = 1 + s * K, b = std::min(a + K - 1, NSTEP);
-      c += 1 + (2 * pair_launches() + 1) * (b - a + 1) + 3 * pair_launches() * (b - a + 1) +
+      c += 1 + (2 * group_launches(kSplitFwd) + 1) * (b - a + 1) +
+           (group_launches(kSplitAdj1) + 2 * group_launches(kSplitAdj23)) * (b - a + 1) +
            (b - std::max(a, 2) + 1) +
            (sizeof(T) == 4 ? 1 : 0);
     }
@@ -1979,48 +2034,39 @@ int ElPlan<T>::profile(const double* l, const double* m, const double* r, double
     out[2 * k + 1] = cells;
     return ADS_OK;
   };
-  const int* wp = d_wl + nw_in;
-  const dim3 gi = grid_rows(nw_in), gp = grid_rows(nw_pm), b(EW * 32);
   int rc = ADS_OK;
   auto run = [&](int k, auto&& launch) {
     if (rc == ADS_OK) rc = timed(k, launch);
   };
   ADS_CUDA(cudaMemsetAsync(pool + zero_fwd_off, 0, zero_fwd_len, st));
   ADS_CUDA(cudaMemsetAsync(pool + zero_adj_off, 0, zero_adj_len, st));
-  run(0, [&] {
-    pair(st,
-         [&](cudaStream_t s) { k_el_stress_rows<T, false, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in, 0); },
-         [&](cudaStream_t s) { k_el_stress_rows<T, false, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm, 0); });
-  });
-  run(1, [&] {
-    pair(st,
-         [&](cudaStream_t s) { k_el_velocity_rows<T, false, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in, 0); },
-         [&](cudaStream_t s) { k_el_velocity_rows<T, false, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm, 0); });
-  });
-  run(2, [&] {
-    pair(st,
-         [&](cudaStream_t s) { k_el_stress_rows<T, true, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in, 0); },
-         [&](cudaStream_t s) { k_el_stress_rows<T, true, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm, 0); });
-  });
-  run(3, [&] {
-    pair(st,
-         [&](cudaStream_t s) { k_el_velocity_rows<T, true, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in, 0); },
-         [&](cudaStream_t s) { k_el_velocity_rows<T, true, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm, 0); });
-  });
+  auto wl = [&](bool in) { return in ? d_wl : d_wl + nw_in; };
+  auto nw = [&](bool in) { return in ? nw_in : nw_pm; };
+  for (int k = 0; k < 4; k++)
+    run(k, [&] {
+      group(st, kSplitFwd, [&](cudaStream_t s, bool in, int part) {
+        if (k % 2 == 0)
+          el_stress<T>(k >= 2, in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw,
+                       rows_w, nw(in), 0);
+        else
+          el_velocity<T>(k >= 2, in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw,
+                         rows_w, nw(in), 0);
+      });
+    });
   run(4, [&] {
-    pair(st,
-         [&](cudaStream_t s) { k_el_adj1_rows<T, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in, 0); },
-         [&](cudaStream_t s) { k_el_adj1_rows<T, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm, 0); });
+    group(st, kSplitAdj1, [&](cudaStream_t s, bool in, int part) {
+      el_adj1<T>(in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w, nw(in), 0);
+    });
   });
   run(5, [&] {
-    pair(st,
-         [&](cudaStream_t s) { k_el_adj2_rows<T, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in, 0); },
-         [&](cudaStream_t s) { k_el_adj2_rows<T, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm, 0); });
+    group(st, kSplitAdj23, [&](cudaStream_t s, bool in, int part) {
+      el_adj2<T>(in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w, nw(in), 0);
+    });
   });
   run(6, [&] {
-    pair(st,
-         [&](cudaStream_t s) { k_el_adj3_rows<T, true><<<gi, b, 0, s>>>(M, d_shots, d_wl, ncolw, rows_w, nw_in); },
-         [&](cudaStream_t s) { k_el_adj3_rows<T, false><<<gp, b, 0, s>>>(M, d_shots, wp, ncolw, rows_w, nw_pm); });
+    group(st, kSplitAdj23, [&](cudaStream_t s, bool in, int part) {
+      el_adj3<T>(in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w, nw(in));
+    });
   });
   run(7, [&] { k_el_src_rcv<T><<<nshots, rcv_threads(), 0, st>>>(d_shots, 1, NSTEP + 1, 1); });
   run(8, [&] { k_el_resid<T><<<grid_resid(), 256, 0, st>>>(d_shots, 1, NSTEP + 1); });
