@@ -1218,7 +1218,10 @@ struct AcPlan final : AcPlanBase {
     int launches(int n) const { return (in_upto(n) > 0) + (pm_upto(n) > 0); }
   };
   DevTiles tf, ta;  // forward / adjoint items
-  void build_tiles(int rows, int width, int64_t pitch, TileList& L) const;
+  // pm_rows > 0: PML items are cut into items of pm_rows-row tiles (more warps
+  // for the heavier PML kernels); 0 keeps them at `rows`
+  void build_tiles(int rows, int width, int64_t pitch, TileList& L, int pm_rows = 0) const;
+  int ri_pf = 0, ri_pa = 0;  // row tiles of the PML items (0: same as ri_f / ri)
   int upload_tiles(const TileList& L, DevTiles& D, cudaStream_t st);
   int autotune(cudaStream_t st, int64_t pitch, size_t cap_items);
   // step launches over the first na sorted shots (interior and PML kernels)
@@ -1769,7 +1772,8 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
 // Tiles of `rows` rows x Tile::J columns over every sorted shot, with the
 // sources and receivers of each tile (bucketed once per shot).
 template <typename T>
-void AcPlan<T>::build_tiles(int rows, int width, int64_t pitch, TileList& L) const {
+void AcPlan<T>::build_tiles(int rows, int width, int64_t pitch, TileList& L,
+                            int pm_rows) const {
   L.in.clear();
   L.pm.clear();
   L.srcs.clear();
@@ -1827,7 +1831,19 @@ void AcPlan<T>::build_tiles(int rows, int width, int64_t pitch, TileList& L) con
         // then need neither (items holding one take the general kernel)
         const bool in = row_free[ti] && col_free[tj] && it.src_e == it.src_b &&
                         it.rcv_e == it.rcv_b;
-        (in ? L.in : L.pm).push_back(it);
+        if (in) {
+          L.in.push_back(it);
+        } else if (pm_rows > 0 && pm_rows < rows) {
+          // sub-items share the item's source / receiver lists: the kernels
+          // match those by cell and row
+          for (int i0 = it.i0; i0 < it.i0 + gh && i0 <= nx; i0 += Tile<T>::G * pm_rows) {
+            AcItem sub = it;
+            sub.i0 = i0;
+            L.pm.push_back(sub);
+          }
+        } else {
+          L.pm.push_back(it);
+        }
       }
     L.in_end[s] = (int)L.in.size();
     L.pm_end[s] = (int)L.pm.size();
@@ -1880,10 +1896,10 @@ int AcPlan<T>::launch_fwd(cudaStream_t st, bool seg, int na, int t, int base, in
   if (np > 0) {
     if (seg)
       k_ac_fwd<T, true, false><<<np, TPB, 0, sp>>>(pm, d_shots, tf.srcs, tf.rcvs, kc, t, base,
-                                                    ck, ri_f);
+                                                    ck, ri_pf > 0 ? ri_pf : ri_f);
     else
       k_ac_fwd<T, false, false><<<np, TPB, 0, sp>>>(pm, d_shots, tf.srcs, tf.rcvs, kc, t, base,
-                                                     ck, ri_f);
+                                                     ck, ri_pf > 0 ? ri_pf : ri_f);
     ADS_LAUNCHED(1);
   }
   if (fork) {
@@ -1911,7 +1927,7 @@ int AcPlan<T>::launch_adj(cudaStream_t st, int na, int k, int base) {
   }
   if (np > 0) {
     k_ac_adj<T, false><<<np, TPB, 0, sp>>>(ta.items + ta.pm_off, d_shots, ta.srcs, ta.rcvs, kc,
-                                           k, base, ri, dt2d);
+                                           k, base, ri_pa > 0 ? ri_pa : ri, dt2d);
     ADS_LAUNCHED(1);
   }
   if (fork) {
@@ -1984,20 +2000,66 @@ int AcPlan<T>::autotune(cudaStream_t st, int64_t pitch, size_t cap) {
       ba = rows;
     }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   if (rc != ADS_OK) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
     ri_f = ri_f0;
     ri = ri0;
     return rc;
   }
   ri_f = bf;
   ri = ba;
-  TileList Lf, La;
-  build_tiles(ri_f, Tile<T>::WF, pitch, Lf);
-  build_tiles(ri, Tile<T>::WA, pitch, La);
-  if (int e = upload_tiles(Lf, tf, st)) return e;
-  if (int e = upload_tiles(La, ta, st)) return e;
+  // second phase: shorter row tiles for the PML items only
+  auto time_range = [&](bool fwd, float& ms) -> int {
+    for (int pass = 0; pass < 2; pass++) {
+      ADS_CUDA(cudaEventRecord(e0, st));
+      if (fwd) {
+        for (int t = 2; t <= tf_end; t++)
+          if (int e = launch_fwd(st, false, shots_with_nstep_ge(t), t, 0, 0)) return e;
+      } else {
+        for (int k = 2; k <= ka_end; k++)
+          if (int e = launch_adj(st, shots_with_nstep_ge(k), k, 0)) return e;
+      }
+      ADS_CUDA(cudaEventRecord(e1, st));
+      ADS_CUDA(cudaEventSynchronize(e1));
+      ADS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    }
+    return ADS_OK;
+  };
+  for (int which = 0; which < 2; which++) {
+    const bool fwd = which == 0;
+    const int rows = fwd ? ri_f : ri;
+    const int width = fwd ? Tile<T>::WF : Tile<T>::WA;
+    DevTiles& D = fwd ? tf : ta;
+    int& pm = fwd ? ri_pf : ri_pa;
+    pm = 0;
+    TileList L0;
+    build_tiles(rows, width, pitch, L0);
+    if (int e = upload_tiles(L0, D, st)) return e;
+    float best = 0.f;
+    if (int e = time_range(fwd, best)) return e;
+    int keep = 0;
+    for (int d = 2; d <= 4; d *= 2) {
+      if (rows % d != 0) continue;
+      TileList L;
+      build_tiles(rows, width, pitch, L, rows / d);
+      if (L.in.size() + L.pm.size() > cap) continue;
+      if (int e = upload_tiles(L, D, st)) return e;
+      pm = rows / d;
+      float ms = 0.f;
+      if (int e = time_range(fwd, ms)) return e;
+      if (ms < best) {
+        best = ms;
+        keep = rows / d;
+      }
+    }
+    pm = keep;
+    TileList L;
+    build_tiles(rows, width, pitch, L, pm);
+    if (int e = upload_tiles(L, D, st)) return e;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
   ADS_CUDA(cudaStreamSynchronize(st));
   return ADS_OK;
 }
