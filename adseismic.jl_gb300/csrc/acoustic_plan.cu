@@ -177,18 +177,6 @@ __device__ __forceinline__ bool warp_tau_free(const T* __restrict__ ty, int j, i
   return __all_sync(FULL, z);
 }
 
-// L2 prefetch of a row segment (one warp-wide instruction per array): a hint
-// that starts the DRAM read of a row the warp reaches ADS_L2PF rows later, so
-// its own load finds it in L2.  Only addresses the kernel will load anyway are
-// given (the same row / column predicates).
-#ifndef ADS_L2PF
-#define ADS_L2PF 0
-#endif
-template <typename T>
-__device__ __forceinline__ void l2pf(const T* p, bool on) {
-  if (ADS_L2PF > 0 && on) asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-}
-
 // True when the warp's columns are tau-free and sigma is zero on rows
 // i0-1 .. i_end (every row a tile of rows [i0, i_end) reads): phi, psi and
 // their adjoints are then zero throughout and the interior update applies.
@@ -295,12 +283,6 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     for (int i = i0; i < i_end; i++) {
       const int64_t row = off(i);
       const int rn = i + PF;  // farthest row of the wo / c / halo queues
-      {
-        const int rp = rn + ADS_L2PF;
-        l2pf(w + off(rp + 1), jld && rp + 1 <= i_end);
-        l2pf(wo + off(rp), jld && rp < i_end);
-        l2pf(cc + off(rp), jld && rp < i_end);
-      }
       V wn = ldv<T, C>(w, off(rn + 1), jld && rn + 1 <= i_end);
       V on = ldv<T, C>(wo, off(rn), jld && rn < i_end);
       V cn = ldv<T, C>(cc, off(rn), jld && rn < i_end);
@@ -369,16 +351,6 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     const int64_t row = off(i);
     const bool more = i + 1 < i_end;
     const bool n1 = more && nz(i + 1);
-    {
-      const int rp = i + 1 + ADS_L2PF;
-      const bool on = jld && rp < i_end;
-      l2pf(w + off(rp + 1), on);
-      l2pf(wo + off(rp), on);
-      l2pf(cc + off(rp), on);
-      const bool pz = on && nz(rp);
-      l2pf(pin + off(rp + 1), pz);
-      l2pf(qin + off(rp), pz);
-    }
     V wn = ldv<T, C>(w, off(i + 2), jld && more);
     V pn_ = ldv<T, C>(pin, off(i + 2), jld && more && nz(i + 2));
     V qn = ldv<T, C>(qin, off(i + 1), jld && n1);
@@ -652,15 +624,6 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     for (int i = i0; i < i_end; i++) {
       const int64_t row = off(i);
       const int rn = i + PF;
-      {
-        const int rp = rn + ADS_L2PF;
-        const bool p1 = jld && rp + 1 <= i_end, p0 = jld && rp < i_end;
-        l2pf(luc + off(rp + 1), p1);
-        l2pf(cc + off(rp + 1), p1);
-        l2pf(w + off(rp + 1), p1);
-        l2pf(lun + off(rp), p0);
-        l2pf(gb + off(rp), p0);
-      }
       const bool on1 = jld && rn + 1 <= i_end, on0 = jld && rn < i_end;
       V un = ldv<T, C>(luc, off(rn + 1), on1);
       V cn = ldv<T, C>(cc, off(rn + 1), on1);
@@ -768,18 +731,6 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     // lambdaU_{k+1}) and the halo cell of row i+1
     const bool more = i + 1 < i_end;
     const bool n1 = more && nz(i + 1);
-    {
-      const int rp = i + 1 + ADS_L2PF;
-      const bool on = jld && rp < i_end;
-      l2pf(luc + off(rp + 1), on);
-      l2pf(cc + off(rp + 1), on);
-      l2pf(w + off(rp + 1), on);
-      l2pf(lun + off(rp), on);
-      const bool pz = on && nz(rp);
-      l2pf(lpc + off(rp + 1), pz);
-      l2pf(lqc + off(rp), pz);
-      if (sizeof(T) == 4) l2pf(sh.gc32 + off(rp), on);
-    }
     V gu2 = ldv<T, C>(luc, off(i + 2), jld && more);
     V gp2 = ldv<T, C>(lpc, off(i + 2), jld && more && nz(i + 2));
     V c2 = ldv<T, C>(cc, off(i + 2), jld && more);
