@@ -177,6 +177,18 @@ __device__ __forceinline__ bool warp_tau_free(const T* __restrict__ ty, int j, i
   return __all_sync(FULL, z);
 }
 
+// The PML damping division: FP32 plans use the hardware reciprocal (within
+// 2 ulp; their error budget against the FP64 oracle is 1e-4), FP64 plans the
+// exact division (1e-12 parity).
+template <typename T>
+__device__ __forceinline__ T pml_div(T a, T b) {
+  if constexpr (sizeof(T) == 4) {
+    return __fdividef(a, b);
+  } else {
+    return a / b;
+  }
+}
+
 // True when the warp's columns are tau-free and sigma is zero on rows
 // i0-1 .. i_end (every row a tile of rows [i0, i_end) reads): phi, psi and
 // their adjoints are then zero throughout and the interior update applies.
@@ -388,7 +400,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
         T v = (T(2) - sg * tj[c] * K.dt2 - K.kxy * cv) * w0.v[c] + cv * K.cx * (wp.v[c] + wm.v[c]) +
               cv * K.cy * (wN + wS) + K.fx * (pp.v[c] - pm.v[c]) + K.fy * (qN - qS) -
               (T(1) - s * K.hdt) * wo0.v[c];
-        if (s != T(0)) v = v / (T(1) + s * K.hdt);
+        if (s != T(0)) v = pml_div<T>(v, T(1) + s * K.hdt);
         for (int e = it.src_b; e < it.src_e; e++) {
           const CellRef r = srcs[e];
           if (r.cell == row + c) v += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
@@ -463,7 +475,7 @@ __device__ __forceinline__ void col_terms(T gui, T gq, T c, T sg, T tj, const Ac
 
 template <typename T>
 __device__ __forceinline__ T inv_den(T s, const AcConst<T>& K) {
-  return s != T(0) ? T(1) / (T(1) + s * K.hdt) : T(1);
+  return s != T(0) ? pml_div<T>(T(1), T(1) + s * K.hdt) : T(1);
 }
 
 // The grad_c accumulator an adjoint step adds to: the FP32 per-segment
