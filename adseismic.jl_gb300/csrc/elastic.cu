@@ -59,6 +59,7 @@ struct ElShot {
   const int* src_type;
   const int64_t* rcv_cell;
   T* const* src_ptr;   // per source: its cell in the state (nullptr: type ignored)
+  const int* src_dual;  // per source: 1 if no stencil updates its cell
   T* const* rcv_ptr;   // per receiver: its cell in the state (nullptr: records 0)
   T* const* rcv_gptr;  // per receiver: its cell in the adjoint state
   const int* rcv_type;
@@ -402,27 +403,26 @@ k_el_adj3(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one) {
 #undef ELIDX
 
 // ---------------------------------------------------------------------------
-// Row-streaming forms of the two forward kernels for the plans.
+// Row-streaming kernels for the plans (the fused forward step and the three
+// adjoint passes).
 //
 // A warp owns a strip of rows of one shot, two adjacent columns per lane
 // (loaded as one 8/16-byte vector), and walks down its rows: the
-// i-neighbours of the 4th-order stencils sit in a 4-row register window whose
-// next row is loaded one iteration ahead, the j-neighbours (up to two columns
-// away) come from the neighbouring lanes.  Lanes 0 and 31 only supply those
-// neighbours: lanes 1..30 update ESTRIP = 60 columns and consecutive strips
-// overlap by two columns on each side.  The arithmetic and its order are
-// those of k_el_stress / k_el_velocity; cells outside the update boxes are
-// neither computed nor written.
+// i-neighbours of the 4th-order stencils sit in register windows whose next
+// row is loaded one iteration ahead, the j-neighbours (up to two columns
+// away) come from the neighbouring lanes.  In the adjoint passes lanes 0 and
+// 31 only supply those neighbours: lanes 1..30 update ESTRIP = 60 columns and
+// consecutive strips overlap by two columns on each side.  Cells outside the
+// update boxes are neither computed nor written.
 // ---------------------------------------------------------------------------
 constexpr int EC = 2;             // columns per lane
-constexpr int ESTRIP = 30 * EC;   // columns a warp strip updates
+constexpr int ESTRIP = 30 * EC;   // columns an adjoint strip updates
 constexpr int EW = 4;             // warps per CTA (independent strips)
-// Which step kernels launch as two concurrent halves (measured: the stress,
-// velocity and first adjoint kernels gain occupancy from it; the gather-heavy
-// second and third adjoint kernels do better whole).
-constexpr bool kSplitFwd = true, kSplitAdj1 = true, kSplitAdj23 = false;
+// Which adjoint passes launch as two concurrent halves (measured: the first
+// gains occupancy from it; the gather-heavy second and third do better whole).
+constexpr bool kSplitAdj1 = true, kSplitAdj23 = false;
 #ifndef ADS_EL_MINB
-#define ADS_EL_MINB 6                 // resident CTAs per SM the FP32 kernels are built for
+#define ADS_EL_MINB 6                 // resident CTAs per SM, first adjoint pass (CPML items)
 #endif
 #ifndef ADS_EL_MINB_ADJ
 #define ADS_EL_MINB_ADJ 4             // the same for the two gather-heavy adjoint kernels
@@ -432,7 +432,7 @@ constexpr int el_minb() { return sizeof(T) == 4 ? ADS_EL_MINB : 2; }
 template <typename T>
 constexpr int el_minb_adj() { return sizeof(T) == 4 ? ADS_EL_MINB_ADJ : 2; }
 #ifndef ADS_EL_MINB_INT
-#define ADS_EL_MINB_INT 6             // the kernels of CPML-free items (no memory variables)
+#define ADS_EL_MINB_INT 6             // the same for CPML-free items (no memory variables)
 #endif
 template <typename T>
 constexpr int el_minb_int() { return sizeof(T) == 4 ? ADS_EL_MINB_INT : 2; }
@@ -454,6 +454,31 @@ __device__ __forceinline__ V2<T> ld2(const T* p, int64_t o, bool on) {
   return x;
 }
 
+// ld2 as one predicated vector load (zeros where `on` is false), so a mask
+// that differs between the lanes of a warp costs no branch.  The asm has no
+// memory clobber: the row kernels load each cell at most once, and a cell
+// they also write is written later from values that depend on the load.
+__device__ __forceinline__ V2<float> ld2p(const float* p, int64_t o, bool on) {
+  float a = 0.f, b = 0.f;
+  asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %3, 0;\n\t@q ld.global.v2.f32 {%0, %1}, [%2];\n\t}"
+      : "+f"(a), "+f"(b)
+      : "l"(p + o), "r"((unsigned)on));
+  V2<float> x;
+  x.v[0] = a;
+  x.v[1] = b;
+  return x;
+}
+__device__ __forceinline__ V2<double> ld2p(const double* p, int64_t o, bool on) {
+  double a = 0.0, b = 0.0;
+  asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %3, 0;\n\t@q ld.global.v2.f64 {%0, %1}, [%2];\n\t}"
+      : "+d"(a), "+d"(b)
+      : "l"(p + o), "r"((unsigned)on));
+  V2<double> x;
+  x.v[0] = a;
+  x.v[1] = b;
+  return x;
+}
+
 // Store the two cells of a lane, each only where its box flag is set.
 template <typename T>
 __device__ __forceinline__ void st2(T* p, int64_t o, const T (&x)[2], bool k0, bool k1) {
@@ -466,6 +491,29 @@ __device__ __forceinline__ void st2(T* p, int64_t o, const T (&x)[2], bool k0, b
     if (k0) p[o] = x[0];
     if (k1) p[o + 1] = x[1];
   }
+}
+
+// The same as st2 as three independent guarded stores (a vector store when
+// both cells are written, else the single cell), which compile to predicated
+// stores instead of branches.
+template <typename T>
+__device__ __forceinline__ void st2p(T* p, int64_t o, const T (&x)[2], bool k0, bool k1) {
+  if (k0 && k1) {
+    V2<T> y;
+    y.v[0] = x[0];
+    y.v[1] = x[1];
+    *reinterpret_cast<V2<T>*>(p + o) = y;
+  }
+  if (k0 && !k1) p[o] = x[0];
+  if (k1 && !k0) p[o + 1] = x[1];
+}
+
+// Two guarded scalar stores: for store masks that differ between the lanes
+// of a warp (columns at a box edge), where the vector form diverges.
+template <typename T>
+__device__ __forceinline__ void st2s(T* p, int64_t o, const T (&x)[2], bool k0, bool k1) {
+  if (k0) p[o] = x[0];
+  if (k1) p[o + 1] = x[1];
 }
 
 __device__ __forceinline__ float shup(float v) { return __shfl_up_sync(0xffffffffu, v, 1); }
@@ -495,7 +543,7 @@ struct Strip {
   __device__ int64_t off(int r) const { return (int64_t)r * P + j + JOFF; }
   // both cells of this lane at row r (zeros outside the padded grid)
   __device__ V2<T> row(const T* p, int r) const {
-    return ld2<T>(p, off(r), j <= NY + 1 && r >= 0 && r <= NX + 1);
+    return ld2p(p, off(r), j <= NY + 1 && r >= 0 && r <= NX + 1);
   }
 };
 
@@ -540,58 +588,185 @@ struct ColProf {
   }
 };
 
-// Stress update (fw1 + fw2) of a strip.
-template <typename T, bool STORE, bool INT, int PART>
-__global__ void __launch_bounds__(EW * 32, INT ? el_minb_int<T>() : el_minb<T>())
-k_el_stress_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __restrict__ wlist,
-                 int ncolw, int R, int nwt,
-                 int store_slot) {
+// ---------------------------------------------------------------------------
+// Fused forward step (fw1..fw4) for the plans: one pass over the fields
+// instead of two.  The state alternates between two buffers: step n reads
+// slot n-1 from buffer (n-1) & 1 and writes slot n into buffer n & 1, so a
+// warp can update the velocities of its rows right after the stresses they
+// need while the neighbouring strips and row tiles still read the old fields
+// for their own edge stresses.
+//
+// A warp computes the new stresses of lanes 1..30 on rows i0-2 .. i_end+1
+// (one lane and two rows more on each side than it owns) and the new
+// velocities of lanes 2..29 on rows i0 .. i_end-1, two rows behind the stress
+// row.  It stores what it owns (lanes 2..29, rows i0 .. i_end-1): a strip
+// updates FSTRIP = 56 columns.  The arithmetic and its order are those of
+// k_el_stress / k_el_velocity.
+//
+// Cells outside a field's update box are never written: both buffers hold the
+// same value there (sources on such cells are added to both buffers and
+// checkpoints are restored into both), and that value is what the step
+// leaves there.  Out-of-box stresses enter the velocity update with that
+// value, as when the step updates the fields in place.
+// ---------------------------------------------------------------------------
+constexpr int FSTRIP = 28 * EC;
+#ifndef ADS_EL_MINB_F
+#define ADS_EL_MINB_F 3               // resident CTAs per SM, fused kernel of corner items
+#endif
+#ifndef ADS_EL_MINB_FR
+#define ADS_EL_MINB_FR 4              // the same for items with only row or only column logic
+#endif
+#ifndef ADS_EL_MINB_FI
+#define ADS_EL_MINB_FI 5              // the same for CPML-free items
+#endif
+template <typename T, int KIND>
+constexpr int el_minb_step() {
+  return sizeof(T) != 4 ? 2 : KIND == 0 ? ADS_EL_MINB_FI : KIND == 3 ? ADS_EL_MINB_F : ADS_EL_MINB_FR;
+}
+
+template <typename T, bool STORE, int KIND>
+__global__ void __launch_bounds__(EW * 32, el_minb_step<T, KIND>())
+k_el_step_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __restrict__ wlist,
+               int ncolw, int R, int nwt, int store_slot, int pin, int jsh, int ish) {
+  // KIND bit 0: rows need the box edge and x-profile logic; bit 1: columns
+  // need the box edge and y-profile logic (0: neither, CPML-free interior)
+  constexpr bool GR = (KIND & 1) != 0, GC = (KIND & 2) != 0;
   const int wl = blockIdx.x * EW + (threadIdx.x >> 5);
   if (wl >= nwt) return;
   const int wi = wlist[wl];  // the warp's (strip, row tile)
   const ElShot<T>& sh = shots[blockIdx.y];
-  const Strip<T> S(M, ncolw, R, wi);
-  const int j = S.j, NX = S.NX, NY = S.NY;
-  const T* __restrict__ vx = sh.f[VX];
-  const T* __restrict__ vy = sh.f[VY];
-  T* __restrict__ sxx = sh.f[SXX];
-  T* __restrict__ syy = sh.f[SYY];
-  T* __restrict__ sxy = sh.f[SXY];
-  T* __restrict__ m1p = sh.f[M1 + 0];
-  T* __restrict__ m2p = sh.f[M1 + 1];
-  T* __restrict__ m3p = sh.f[M1 + 2];
-  T* __restrict__ m4p = sh.f[M1 + 3];
-  T* __restrict__ st = STORE ? sh.store + (int64_t)store_slot * NSTORE * sh.fs : nullptr;
-  const int64_t fs = sh.fs;
+  const int lane = threadIdx.x & 31, NX = M.NX, NY = M.NY;
+  const int strip = wi % ncolw, rt = wi / ncolw;
+  // strips and row tiles start jsh columns (even, <= 0) and ish rows (<= 0)
+  // before column and row 1
+  const int j = strip * FSTRIP - 3 + lane * EC + jsh;  // odd: 8/16-byte aligned pairs
+  const bool own = lane >= 2 && lane <= 29;
+  const bool colok = j >= -1 && j <= NY + 1;
+  const int i0r = 1 + ish + rt * R;
+  const int i0 = max(i0r, 1), i_end = min(i0r + R, NX + 1);
+  const int64_t fs = sh.fs, P = M.P;
+  const int64_t bin = (int64_t)pin * NF * fs, bout = (int64_t)(1 - pin) * NF * fs;
+  const T* __restrict__ vx = sh.f[VX] + bin;
+  const T* __restrict__ vy = sh.f[VY] + bin;
+  const T* __restrict__ sxx = sh.f[SXX] + bin;
+  const T* __restrict__ syy = sh.f[SYY] + bin;
+  const T* __restrict__ sxy = sh.f[SXY] + bin;
+  T* __restrict__ vxo = sh.f[VX] + bout;
+  T* __restrict__ vyo = sh.f[VY] + bout;
+  T* __restrict__ sxxo = sh.f[SXX] + bout;
+  T* __restrict__ syyo = sh.f[SYY] + bout;
+  T* __restrict__ sxyo = sh.f[SXY] + bout;
+  T* __restrict__ st = STORE ? sh.store + (int64_t)store_slot * NSTORE * fs : nullptr;
+  // stores of a lane's two cells: lane-dependent masks (column logic) use
+  // scalar stores
+  auto stw = [&](T* p, int64_t o, const T (&x)[2], bool k0, bool k1) {
+    if constexpr (GC) {
+      st2s<T>(p, o, x, k0, k1);
+    } else {
+      st2p<T>(p, o, x, k0, k1);
+    }
+  };
+  auto ld = [&](const T* p, int r) {
+    return ld2p(p, (int64_t)r * P + j + JOFF, colok && r >= 0 && r <= NX + 1);
+  };
+  // memory variables 1..8 of the input / output buffer
+  const T* __restrict__ m1i = sh.f[M1 + 0] + bin;
+  const T* __restrict__ m2i = sh.f[M1 + 1] + bin;
+  const T* __restrict__ m3i = sh.f[M1 + 2] + bin;
+  const T* __restrict__ m4i = sh.f[M1 + 3] + bin;
+  const T* __restrict__ m5i = sh.f[M1 + 4] + bin;
+  const T* __restrict__ m6i = sh.f[M1 + 5] + bin;
+  const T* __restrict__ m7i = sh.f[M1 + 6] + bin;
+  const T* __restrict__ m8i = sh.f[M1 + 7] + bin;
+  T* __restrict__ m1o = sh.f[M1 + 0] + bout;
+  T* __restrict__ m2o = sh.f[M1 + 1] + bout;
+  T* __restrict__ m3o = sh.f[M1 + 2] + bout;
+  T* __restrict__ m4o = sh.f[M1 + 3] + bout;
+  T* __restrict__ m5o = sh.f[M1 + 4] + bout;
+  T* __restrict__ m6o = sh.f[M1 + 5] + bout;
+  T* __restrict__ m7o = sh.f[M1 + 6] + bout;
+  T* __restrict__ m8o = sh.f[M1 + 7] + bout;
   const ColProf<T> Y(M, j);
-  bool c1[2], c2[2];  // column parts of the fw1 / fw2 boxes
+  bool cA[2], cB[2];  // columns of the fw1 / fw3 boxes (2..NY) and the fw2 / fw4 boxes (1..NY-1)
 #pragma unroll
   for (int c = 0; c < 2; c++) {
-    c1[c] = S.out && (INT || (j + c >= 2 && j + c <= NY));
-    c2[c] = S.out && (INT || (j + c >= 1 && j + c <= NY - 1));
+    cA[c] = !GC || (j + c >= 2 && j + c <= NY);
+    cB[c] = !GC || (j + c >= 1 && j + c <= NY - 1);
   }
-  const int i0 = S.i0;
-  // windows: vx rows i-1..i+2, vy rows i-2..i+1, lam / mu rows i, i+1
-  V2<T> X0 = S.row(vx, i0 - 1), X1 = S.row(vx, i0), X2 = S.row(vx, i0 + 1), X3 = S.row(vx, i0 + 2);
-  V2<T> Y0 = S.row(vy, i0 - 2), Y1 = S.row(vy, i0 - 1), Y2 = S.row(vy, i0), Y3 = S.row(vy, i0 + 1);
-  V2<T> L0 = S.row(M.lam, i0), L1 = S.row(M.lam, i0 + 1);
-  V2<T> U0 = S.row(M.mu, i0), U1 = S.row(M.mu, i0 + 1);
-  V2<T> A0 = S.row(sxx, i0), B0 = S.row(syy, i0), C0 = S.row(sxy, i0);
-  for (int i = i0; i < S.i_end; i++) {
-    const int64_t o = S.off(i);
-    // next row's loads
-    const bool more = i + 1 < S.i_end;
-    const int rn = more ? i + 1 : -1;
-    const V2<T> X4 = S.row(vx, more ? i + 3 : -1), Y4 = S.row(vy, more ? i + 2 : -1),
-                L2 = S.row(M.lam, more ? i + 2 : -1), U2 = S.row(M.mu, more ? i + 2 : -1);
-    const V2<T> An = S.row(sxx, rn), Bn = S.row(syy, rn), Cn = S.row(sxy, rn);
-    // row i across columns (neighbouring lanes): vx at j-1..j+3, vy at j-2..j+2, mu at j..j+2
+  // lanes whose columns carry memory variables (in a box).  The y-profile
+  // memory variables are updated in every box cell of a strip with column
+  // logic: where the profile is inactive (a = 0, b = 1) the update
+  // b * m + a * d gives exactly +0, the value such cells always hold, so no
+  // per-lane profile test is needed.
+  const bool lA = cA[0] || cA[1], lB = cB[0] || cB[1];
+  const bool lAi = GC && lA, lBh = GC && lB;
+  // row parts of the boxes: stress rows (fw1: 1..NX-1, fw2: 2..NX) and
+  // velocity rows r = s - 2 (fw3: 2..NX, fw4: 1..NX-1)
+  auto rs1 = [&](int s) { return !GR || (s >= 1 && s <= NX - 1); };
+  auto rs2 = [&](int s) { return !GR || (s >= 2 && s <= NX); };
+  auto rv3 = [&](int s) { return !GR || s - 2 >= 2; };
+  auto rv4 = [&](int s) { return !GR || s - 2 <= NX - 1; };
+  // memory variables m1..m4 of stress row s and m5..m8 of velocity row s - 2
+  // (where they can be nonzero), loaded one iteration ahead
+  auto mload = [&](int s, bool on, V2<T> (&m)[8]) {
+    const int64_t o = (int64_t)s * P + j + JOFF, q = o - 2 * P;
+    const bool vr = on && own && s >= i0 + 2;
+    if constexpr (GR) {
+      m[0] = ld2p(m1i, o, on && rs1(s) && lA);
+      m[2] = ld2p(m3i, o, on && rs2(s) && lB);
+      m[4] = ld2p(m5i, q, vr && rv3(s) && lA);
+      m[6] = ld2p(m7i, q, vr && rv4(s) && lB);
+    }
+    if constexpr (GC) {
+      m[1] = ld2p(m2i, o, on && rs1(s) && lAi);
+      m[3] = ld2p(m4i, o, on && rs2(s) && lBh);
+      m[5] = ld2p(m6i, q, vr && rv3(s) && lAi);
+      m[7] = ld2p(m8i, q, vr && rv4(s) && lBh);
+    }
+  };
+  const int s0 = i0 - 2;
+  // windows at stress row s: old vx rows s-2..s+2, old vy rows s-2..s+1,
+  // lam / mu rows s, s+1, old stresses row s, rho rows s-2, s-1; new sxx rows
+  // s-4..s-1, new sxy rows s-3..s-1, new syy rows s-2, s-1
+  V2<T> X0 = ld(vx, s0 - 2), X1 = ld(vx, s0 - 1), X2 = ld(vx, s0), X3 = ld(vx, s0 + 1),
+        X4 = ld(vx, s0 + 2);
+  V2<T> Y0 = ld(vy, s0 - 2), Y1 = ld(vy, s0 - 1), Y2 = ld(vy, s0), Y3 = ld(vy, s0 + 1);
+  V2<T> L0 = ld(M.lam, s0), L1 = ld(M.lam, s0 + 1), U0 = ld(M.mu, s0), U1 = ld(M.mu, s0 + 1);
+  V2<T> A0 = ld(sxx, s0), B0 = ld(syy, s0), C0 = ld(sxy, s0);
+  V2<T> R0 = ld(M.rho, s0 - 2), R1 = ld(M.rho, s0 - 1);
+  V2<T> NA0{}, NA1{}, NA2{}, NA3{}, NC0{}, NC1{}, NC2{}, NB0{}, NB1{};
+  V2<T> mm[8] = {};
+  mload(s0, true, mm);
+  for (int s = s0; s <= i_end + 1; s++) {
+    const bool more = s <= i_end;
+    const V2<T> X5 = ld(vx, more ? s + 3 : -1), Y4 = ld(vy, more ? s + 2 : -1),
+                L2 = ld(M.lam, more ? s + 2 : -1), U2 = ld(M.mu, more ? s + 2 : -1),
+                R2 = ld(M.rho, more ? s : -1);
+    const V2<T> An = ld(sxx, more ? s + 1 : -1), Bn = ld(syy, more ? s + 1 : -1),
+                Cn = ld(sxy, more ? s + 1 : -1);
+    V2<T> mn[8] = {};
+    mload(s + 1, more, mn);
+    const int64_t o = (int64_t)s * P + j + JOFF, q = o - 2 * P;
+    // x profiles of stress row s and velocity row s - 2
+    const int sx = min(max(s, 1), NX) - 1, vx_ = min(max(s - 2, 1), NX) - 1;
+    const T axh = GR ? M.axh[sx] : T(0), bxh = GR ? M.bxh[sx] : T(1);
+    const T axi = GR ? M.axi[sx] : T(0), bxi = GR ? M.bxi[sx] : T(1);
+    const T vaxi = GR ? M.axi[vx_] : T(0), vbxi = GR ? M.bxi[vx_] : T(1);
+    const T vaxh = GR ? M.axh[vx_] : T(0), vbxh = GR ? M.bxh[vx_] : T(1);
+    const bool r1 = rs1(s), r2 = rs2(s);
+    const bool rx1 = GR && r1 && (axh != T(0) || bxh != T(1));
+    const bool rx3 = GR && r2 && (axi != T(0) || bxi != T(1));
+    const bool vrow = s >= i0 + 2;  // velocities of row s - 2 this iteration
+    const bool r3 = rv3(s), r4 = rv4(s);
+    const bool rx5 = GR && vrow && r3 && (vaxi != T(0) || vbxi != T(1));
+    const bool rx7 = GR && vrow && r4 && (vaxh != T(0) || vbxh != T(1));
+    // ---- new stresses of row s
     T xr[5], yr[5], ur[3];
-    xr[0] = shup(X1.v[1]);
-    xr[1] = X1.v[0];
-    xr[2] = X1.v[1];
-    xr[3] = shdn(X1.v[0]);
-    xr[4] = shdn(X1.v[1]);
+    xr[0] = shup(X2.v[1]);
+    xr[1] = X2.v[0];
+    xr[2] = X2.v[1];
+    xr[3] = shdn(X2.v[0]);
+    xr[4] = shdn(X2.v[1]);
     yr[0] = shup(Y2.v[0]);
     yr[1] = shup(Y2.v[1]);
     yr[2] = Y2.v[0];
@@ -600,177 +775,131 @@ k_el_stress_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* _
     ur[0] = U0.v[0];
     ur[1] = U0.v[1];
     ur[2] = shdn(U0.v[0]);
-    // x profiles of row i: m1 on the half grid (fw1 rows), m3 on the integer grid (fw2 rows)
-    const T axh = INT ? T(0) : M.axh[i - 1], bxh = INT ? T(1) : M.bxh[i - 1];
-    const T axi = INT ? T(0) : M.axi[i - 1], bxi = INT ? T(1) : M.bxi[i - 1];
-    const bool r1 = INT || i <= NX - 1, r2 = INT || i >= 2;
-    const bool rx1 = !INT && r1 && (axh != T(0) || bxh != T(1));
-    const bool rx3 = !INT && r2 && (axi != T(0) || bxi != T(1));
-    T nsxx[2], nsyy[2], nsxy[2], e1s[2], e2s[2], e12s[2];
-    bool k1[2], k2[2];
+    const bool wrow = own && s >= i0 && s < i_end;  // this lane stores row s
+    V2<T> NAs, NBs, NCs;
+    T e1s[2], e2s[2], e12s[2], m1v[2], m2v[2], m3v[2], m4v[2];
+    bool k1[2], k2[2], u1[2], u2[2], u3[2], u4[2];
 #pragma unroll
     for (int c = 0; c < 2; c++) {
-      k1[c] = PART != 2 && r1 && c1[c];
-      k2[c] = PART != 1 && r2 && c2[c];
-      nsxx[c] = nsyy[c] = nsxy[c] = e1s[c] = e2s[c] = e12s[c] = T(0);
-      if constexpr (PART != 2) {  // fw1
+      k1[c] = r1 && cA[c];
+      k2[c] = r2 && cB[c];
+      // fw1
       const T lam_ = T(0.5) * (L1.v[c] + L0.v[c]);
       const T mu1 = T(0.5) * (U1.v[c] + U0.v[c]);
       const T lm = lam_ + T(2) * mu1;
-      const T dvx = d4r<T>(X2.v[c], X1.v[c], X3.v[c], X0.v[c], M.hx24, M.rhx24);
+      const T dvx = d4r<T>(X3.v[c], X2.v[c], X4.v[c], X1.v[c], M.hx24, M.rhx24);
       const T dvy = d4r<T>(yr[2 + c], yr[1 + c], yr[3 + c], yr[c], M.hy24, M.rhy24);
-      const bool u1 = k1[c] && rx1, u2 = !INT && k1[c] && Y.acti[c];
-      const T m1 = u1 ? bxh * m1p[o + c] + axh * dvx : T(0);
-      const T m2 = u2 ? Y.bi[c] * m2p[o + c] + Y.ai[c] * dvy : T(0);
-      if (u1) m1p[o + c] = m1;
-      if (u2) m2p[o + c] = m2;
-      const T e1 = dvx + m1, e2 = dvy + m2;
-      nsxx[c] = A0.v[c] + (lm * e1 + lam_ * e2) * M.dt;
-      nsyy[c] = B0.v[c] + (lm * e2 + lam_ * e1) * M.dt;
+      u1[c] = k1[c] && rx1;
+      u2[c] = GC && k1[c];
+      m1v[c] = u1[c] ? bxh * mm[0].v[c] + axh * dvx : T(0);
+      m2v[c] = u2[c] ? Y.bi[c] * mm[1].v[c] + Y.ai[c] * dvy : T(0);
+      const T e1 = dvx + m1v[c], e2 = dvy + m2v[c];
+      NAs.v[c] = k1[c] ? A0.v[c] + (lm * e1 + lam_ * e2) * M.dt : A0.v[c];
+      NBs.v[c] = k1[c] ? B0.v[c] + (lm * e2 + lam_ * e1) * M.dt : B0.v[c];
       e1s[c] = e1;
       e2s[c] = e2;
-      }
-      if constexpr (PART != 1) {  // fw2
+      // fw2
       const T mu2 = T(0.5) * (ur[c] + ur[c + 1]);
       const T dvydx = d4r<T>(Y2.v[c], Y1.v[c], Y3.v[c], Y0.v[c], M.hx24, M.rhx24);
       const T dvxdy = d4r<T>(xr[2 + c], xr[1 + c], xr[3 + c], xr[c], M.hy24, M.rhy24);
-      const bool u3 = k2[c] && rx3, u4 = !INT && k2[c] && Y.acth[c];
-      const T m3 = u3 ? bxi * m3p[o + c] + axi * dvydx : T(0);
-      const T m4 = u4 ? Y.bh[c] * m4p[o + c] + Y.ah[c] * dvxdy : T(0);
-      if (u3) m3p[o + c] = m3;
-      if (u4) m4p[o + c] = m4;
-      const T e12 = (dvydx + m3) + (dvxdy + m4);
-      nsxy[c] = C0.v[c] + mu2 * e12 * M.dt;
+      u3[c] = k2[c] && rx3;
+      u4[c] = GC && k2[c];
+      m3v[c] = u3[c] ? bxi * mm[2].v[c] + axi * dvydx : T(0);
+      m4v[c] = u4[c] ? Y.bh[c] * mm[3].v[c] + Y.ah[c] * dvxdy : T(0);
+      const T e12 = (dvydx + m3v[c]) + (dvxdy + m4v[c]);
+      NCs.v[c] = k2[c] ? C0.v[c] + mu2 * e12 * M.dt : C0.v[c];
       e12s[c] = e12;
+    }
+    if (wrow) {
+      stw(sxxo, o, NAs.v, k1[0], k1[1]);
+      stw(syyo, o, NBs.v, k1[0], k1[1]);
+      stw(sxyo, o, NCs.v, k2[0], k2[1]);
+      if (STORE) {
+        stw(st + E1 * fs, o, e1s, k1[0], k1[1]);
+        stw(st + E2 * fs, o, e2s, k1[0], k1[1]);
+        stw(st + E12 * fs, o, e12s, k2[0], k2[1]);
+      }
+      if constexpr (GR) {
+        stw(m1o, o, m1v, u1[0], u1[1]);
+        stw(m3o, o, m3v, u3[0], u3[1]);
+      }
+      if constexpr (GC) {
+        stw(m2o, o, m2v, u2[0], u2[1]);
+        stw(m4o, o, m4v, u4[0], u4[1]);
       }
     }
-    st2<T>(sxx, o, nsxx, k1[0], k1[1]);
-    st2<T>(syy, o, nsyy, k1[0], k1[1]);
-    st2<T>(sxy, o, nsxy, k2[0], k2[1]);
-    if (STORE) {
-      st2<T>(st + E1 * fs, o, e1s, k1[0], k1[1]);
-      st2<T>(st + E2 * fs, o, e2s, k1[0], k1[1]);
-      st2<T>(st + E12 * fs, o, e12s, k2[0], k2[1]);
+    // ---- new velocities of row s - 2
+    if (vrow) {
+      T qr[5], wr[5], r0[3], r1v[3];
+      qr[0] = shup(NC1.v[0]);
+      qr[1] = shup(NC1.v[1]);
+      qr[2] = NC1.v[0];
+      qr[3] = NC1.v[1];
+      qr[4] = shdn(NC1.v[0]);
+      wr[0] = shup(NB0.v[1]);
+      wr[1] = NB0.v[0];
+      wr[2] = NB0.v[1];
+      wr[3] = shdn(NB0.v[0]);
+      wr[4] = shdn(NB0.v[1]);
+      r0[0] = R0.v[0];
+      r0[1] = R0.v[1];
+      r0[2] = shdn(R0.v[0]);
+      r1v[0] = R1.v[0];
+      r1v[1] = R1.v[1];
+      r1v[2] = shdn(R1.v[0]);
+      T nvx[2], nvy[2], a3s[2], a4s[2], m5v[2], m6v[2], m7v[2], m8v[2];
+      bool k3[2], k4[2], u5[2], u6[2], u7[2], u8[2];
+#pragma unroll
+      for (int c = 0; c < 2; c++) {
+        k3[c] = own && r3 && cA[c];
+        k4[c] = own && r4 && cB[c];
+        // fw3
+        const T a = d4r<T>(NA2.v[c], NA1.v[c], NA3.v[c], NA0.v[c], M.hx24, M.rhx24);
+        const T b = d4r<T>(qr[2 + c], qr[1 + c], qr[3 + c], qr[c], M.hy24, M.rhy24);
+        u5[c] = k3[c] && rx5;
+        u6[c] = GC && k3[c];
+        m5v[c] = u5[c] ? vbxi * mm[4].v[c] + vaxi * a : T(0);
+        m6v[c] = u6[c] ? Y.bi[c] * mm[5].v[c] + Y.ai[c] * b : T(0);
+        const T e3 = (a + m5v[c]) + (b + m6v[c]);
+        nvx[c] = X0.v[c] + divr<T>(e3 * M.dt, r0[c]);
+        a3s[c] = e3;
+        // fw4
+        const T rho_ = T(0.25) * (r0[c] + r1v[c] + r1v[c + 1] + r0[c + 1]);
+        const T a4 = d4r<T>(NC2.v[c], NC1.v[c], NCs.v[c], NC0.v[c], M.hx24, M.rhx24);
+        const T b4 = d4r<T>(wr[2 + c], wr[1 + c], wr[3 + c], wr[c], M.hy24, M.rhy24);
+        u7[c] = k4[c] && rx7;
+        u8[c] = GC && k4[c];
+        m7v[c] = u7[c] ? vbxh * mm[6].v[c] + vaxh * a4 : T(0);
+        m8v[c] = u8[c] ? Y.bh[c] * mm[7].v[c] + Y.ah[c] * b4 : T(0);
+        const T e4 = (a4 + m7v[c]) + (b4 + m8v[c]);
+        nvy[c] = Y0.v[c] + divr<T>(e4 * M.dt, rho_);
+        a4s[c] = e4;
+      }
+      stw(vxo, q, nvx, k3[0], k3[1]);
+      stw(vyo, q, nvy, k4[0], k4[1]);
+      if (STORE) {
+        stw(st + A3 * fs, q, a3s, k3[0], k3[1]);
+        stw(st + A4 * fs, q, a4s, k4[0], k4[1]);
+      }
+      if constexpr (GR) {
+        stw(m5o, q, m5v, u5[0], u5[1]);
+        stw(m7o, q, m7v, u7[0], u7[1]);
+      }
+      if constexpr (GC) {
+        stw(m6o, q, m6v, u6[0], u6[1]);
+        stw(m8o, q, m8v, u8[0], u8[1]);
+      }
     }
-    X0 = X1; X1 = X2; X2 = X3; X3 = X4;
+    X0 = X1; X1 = X2; X2 = X3; X3 = X4; X4 = X5;
     Y0 = Y1; Y1 = Y2; Y2 = Y3; Y3 = Y4;
     L0 = L1; L1 = L2; U0 = U1; U1 = U2;
     A0 = An; B0 = Bn; C0 = Cn;
-  }
-}
-
-// Velocity update (fw3 + fw4) of a strip, from the new stresses.
-template <typename T, bool STORE, bool INT, int PART>
-__global__ void __launch_bounds__(EW * 32, INT ? el_minb_int<T>() : el_minb<T>())
-k_el_velocity_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __restrict__ wlist,
-                   int ncolw, int R, int nwt,
-                   int store_slot) {
-  const int wl = blockIdx.x * EW + (threadIdx.x >> 5);
-  if (wl >= nwt) return;
-  const int wi = wlist[wl];  // the warp's (strip, row tile)
-  const ElShot<T>& sh = shots[blockIdx.y];
-  const Strip<T> S(M, ncolw, R, wi);
-  const int j = S.j, NX = S.NX, NY = S.NY;
-  const T* __restrict__ sxx = sh.f[SXX];
-  const T* __restrict__ syy = sh.f[SYY];
-  const T* __restrict__ sxy = sh.f[SXY];
-  T* __restrict__ vx = sh.f[VX];
-  T* __restrict__ vy = sh.f[VY];
-  T* __restrict__ m5p = sh.f[M1 + 4];
-  T* __restrict__ m6p = sh.f[M1 + 5];
-  T* __restrict__ m7p = sh.f[M1 + 6];
-  T* __restrict__ m8p = sh.f[M1 + 7];
-  T* __restrict__ st = STORE ? sh.store + (int64_t)store_slot * NSTORE * sh.fs : nullptr;
-  const int64_t fs = sh.fs;
-  const ColProf<T> Y(M, j);
-  bool c3[2], c4[2];  // column parts of the fw3 / fw4 boxes
-#pragma unroll
-  for (int c = 0; c < 2; c++) {
-    c3[c] = S.out && (INT || (j + c >= 2 && j + c <= NY));
-    c4[c] = S.out && (INT || (j + c >= 1 && j + c <= NY - 1));
-  }
-  const int i0 = S.i0;
-  // windows: sxx rows i-2..i+1, sxy rows i-1..i+2, syy row i, rho rows i, i+1
-  V2<T> S0 = S.row(sxx, i0 - 2), S1 = S.row(sxx, i0 - 1), S2 = S.row(sxx, i0), S3 = S.row(sxx, i0 + 1);
-  V2<T> Q0 = S.row(sxy, i0 - 1), Q1 = S.row(sxy, i0), Q2 = S.row(sxy, i0 + 1), Q3 = S.row(sxy, i0 + 2);
-  V2<T> W0 = S.row(syy, i0);
-  V2<T> R0 = S.row(M.rho, i0), R1 = S.row(M.rho, i0 + 1);
-  V2<T> VX0 = S.row(vx, i0), VY0 = S.row(vy, i0);
-  for (int i = i0; i < S.i_end; i++) {
-    const int64_t o = S.off(i);
-    const bool more = i + 1 < S.i_end;
-    const int rn = more ? i + 1 : -1;
-    const V2<T> S4 = S.row(sxx, more ? i + 2 : -1), Q4 = S.row(sxy, more ? i + 3 : -1),
-                R2 = S.row(M.rho, more ? i + 2 : -1);
-    const V2<T> Wn = S.row(syy, rn), VXn = S.row(vx, rn), VYn = S.row(vy, rn);
-    // row i across columns (neighbouring lanes): sxy at j-2..j+2, syy at j-1..j+3,
-    // rho rows i, i+1 at j..j+2
-    T qr[5], wr[5], r0[3], r1[3];
-    qr[0] = shup(Q1.v[0]);
-    qr[1] = shup(Q1.v[1]);
-    qr[2] = Q1.v[0];
-    qr[3] = Q1.v[1];
-    qr[4] = shdn(Q1.v[0]);
-    wr[0] = shup(W0.v[1]);
-    wr[1] = W0.v[0];
-    wr[2] = W0.v[1];
-    wr[3] = shdn(W0.v[0]);
-    wr[4] = shdn(W0.v[1]);
-    r0[0] = R0.v[0];
-    r0[1] = R0.v[1];
-    r0[2] = shdn(R0.v[0]);
-    r1[0] = R1.v[0];
-    r1[1] = R1.v[1];
-    r1[2] = shdn(R1.v[0]);
-    // x profiles of row i: m5 on the integer grid (fw3 rows), m7 on the half grid (fw4 rows)
-    const T axi = INT ? T(0) : M.axi[i - 1], bxi = INT ? T(1) : M.bxi[i - 1];
-    const T axh = INT ? T(0) : M.axh[i - 1], bxh = INT ? T(1) : M.bxh[i - 1];
-    const bool r3 = INT || i >= 2, r4 = INT || i <= NX - 1;
-    const bool rx5 = !INT && r3 && (axi != T(0) || bxi != T(1));
-    const bool rx7 = !INT && r4 && (axh != T(0) || bxh != T(1));
-    T nvx[2], nvy[2], a3s[2], a4s[2];
-    bool k3[2], k4[2];
-#pragma unroll
-    for (int c = 0; c < 2; c++) {
-      k3[c] = PART != 2 && r3 && c3[c];
-      k4[c] = PART != 1 && r4 && c4[c];
-      nvx[c] = nvy[c] = a3s[c] = a4s[c] = T(0);
-      if constexpr (PART != 2) {  // fw3
-      const T a = d4r<T>(S2.v[c], S1.v[c], S3.v[c], S0.v[c], M.hx24, M.rhx24);
-      const T b = d4r<T>(qr[2 + c], qr[1 + c], qr[3 + c], qr[c], M.hy24, M.rhy24);
-      const bool u5 = k3[c] && rx5, u6 = !INT && k3[c] && Y.acti[c];
-      const T m5 = u5 ? bxi * m5p[o + c] + axi * a : T(0);
-      const T m6 = u6 ? Y.bi[c] * m6p[o + c] + Y.ai[c] * b : T(0);
-      if (u5) m5p[o + c] = m5;
-      if (u6) m6p[o + c] = m6;
-      const T e3 = (a + m5) + (b + m6);
-      nvx[c] = VX0.v[c] + divr<T>(e3 * M.dt, r0[c]);
-      a3s[c] = e3;
-      }
-      if constexpr (PART != 1) {  // fw4
-      const T rho_ = T(0.25) * (r0[c] + r1[c] + r1[c + 1] + r0[c + 1]);
-      const T a4 = d4r<T>(Q2.v[c], Q1.v[c], Q3.v[c], Q0.v[c], M.hx24, M.rhx24);
-      const T b4 = d4r<T>(wr[2 + c], wr[1 + c], wr[3 + c], wr[c], M.hy24, M.rhy24);
-      const bool u7 = k4[c] && rx7, u8 = !INT && k4[c] && Y.acth[c];
-      const T m7 = u7 ? bxh * m7p[o + c] + axh * a4 : T(0);
-      const T m8 = u8 ? Y.bh[c] * m8p[o + c] + Y.ah[c] * b4 : T(0);
-      if (u7) m7p[o + c] = m7;
-      if (u8) m8p[o + c] = m8;
-      const T e4 = (a4 + m7) + (b4 + m8);
-      nvy[c] = VY0.v[c] + divr<T>(e4 * M.dt, rho_);
-      a4s[c] = e4;
-      }
-    }
-    st2<T>(vx, o, nvx, k3[0], k3[1]);
-    st2<T>(vy, o, nvy, k4[0], k4[1]);
-    if (STORE) {
-      st2<T>(st + A3 * fs, o, a3s, k3[0], k3[1]);
-      st2<T>(st + A4 * fs, o, a4s, k4[0], k4[1]);
-    }
-    S0 = S1; S1 = S2; S2 = S3; S3 = S4;
-    Q0 = Q1; Q1 = Q2; Q2 = Q3; Q3 = Q4;
     R0 = R1; R1 = R2;
-    W0 = Wn; VX0 = VXn; VY0 = VYn;
+    NA0 = NA1; NA1 = NA2; NA2 = NA3; NA3 = NAs;
+    NC0 = NC1; NC1 = NC2; NC2 = NCs;
+    NB0 = NB1; NB1 = NBs;
+#pragma unroll
+    for (int k = 0; k < 8; k++) mm[k] = mn[k];
   }
 }
 
@@ -1195,21 +1324,27 @@ __global__ void k_el_flush_acc(const ElShot<float>* __restrict__ shots, int64_t 
 }
 
 // Sources of slot n (added in order by one thread), then receivers of slot n.
+// par: the state buffer holding slot n (0 for in-place plans); a source on a
+// cell no stencil updates is added to both buffers when dual != 0.
 template <typename T>
-__global__ void k_el_src_rcv(const ElShot<T>* __restrict__ shots, int n, int nt, int record) {
+__global__ void k_el_src_rcv(const ElShot<T>* __restrict__ shots, int n, int nt, int record,
+                             int par, int dual) {
   const ElShot<T>& sh = shots[blockIdx.x];
+  const int64_t d = (int64_t)NF * sh.fs, mine = par ? d : 0, other = par ? -d : d;
   if (threadIdx.x == 0) {
     const T* row = sh.srcv + (int64_t)(n - 1) * sh.nsrc;
     for (int k = 0; k < sh.nsrc; k++) {
       T* p = sh.src_ptr[k];
-      if (p) *p += row[k];
+      if (!p) continue;
+      p[mine] += row[k];
+      if (dual && sh.src_dual[k]) p[mine + other] += row[k];
     }
   }
   if (!record) return;
   __syncthreads();
   for (int r = threadIdx.x; r < sh.nrcv; r += blockDim.x) {
     const T* p = sh.rcv_ptr[r];
-    sh.traces[(int64_t)r * nt + n] = p ? *p : T(0);
+    sh.traces[(int64_t)r * nt + n] = p ? p[mine] : T(0);
   }
 }
 
@@ -1223,19 +1358,25 @@ __global__ void k_el_resid(const ElShot<T>* __restrict__ shots, int n, int nt) {
   if (p) atomicAdd(p, sh.resid[(int64_t)r * nt + n]);
 }
 
-// State <-> checkpoint copies (13 contiguous fields per shot).
+// State <-> checkpoint copies (13 contiguous fields per shot).  Saving reads
+// state buffer par; restoring writes buffer 0 and, for two-buffer plans
+// (both != 0), buffer 1 as well.
 template <typename T>
-__global__ void k_el_ckpt(const ElShot<T>* __restrict__ shots, int slot, int to_ckpt) {
+__global__ void k_el_ckpt(const ElShot<T>* __restrict__ shots, int slot, int to_ckpt, int par,
+                          int both) {
   const ElShot<T>& sh = shots[blockIdx.y];
   const int64_t n = NF * sh.fs;
   T* state = sh.f[0];
   T* ck = sh.ckpt + (int64_t)slot * n;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
        e += (int64_t)gridDim.x * blockDim.x) {
-    if (to_ckpt)
-      ck[e] = state[e];
-    else
-      state[e] = ck[e];
+    if (to_ckpt) {
+      ck[e] = state[par ? n + e : e];
+    } else {
+      const T v = ck[e];
+      state[e] = v;
+      if (both) state[n + e] = v;
+    }
   }
 }
 
@@ -1375,7 +1516,7 @@ std::vector<T> pack_profiles(int64_t NX, int64_t NY, const double* ax, const dou
 
 }  // namespace
 
-// Launchers of the row kernels: (store,) interior / CPML items, part 1 / 2.
+// Launchers of the adjoint row kernels: interior / CPML items, part 1 / 2.
 #define ADS_EL_SEL(K, ...)                                    \
   do {                                                        \
     if (in) {                                                 \
@@ -1388,26 +1529,6 @@ std::vector<T> pack_profiles(int64_t NX, int64_t NY, const double* ax, const dou
       else K(__VA_ARGS__, false, 2);                          \
     }                                                         \
   } while (0)
-
-template <typename T>
-void el_stress(bool store, bool in, int part, dim3 g, cudaStream_t s, const ElModel<T>& M,
-               const ElShot<T>* sh, const int* wl, int ncolw, int R, int nw, int slot) {
-#define ADS_K(ST, IN, PT) \
-  k_el_stress_rows<T, ST, IN, PT><<<g, EW * 32, 0, s>>>(M, sh, wl, ncolw, R, nw, slot)
-  if (store) ADS_EL_SEL(ADS_K, true);
-  else ADS_EL_SEL(ADS_K, false);
-#undef ADS_K
-}
-
-template <typename T>
-void el_velocity(bool store, bool in, int part, dim3 g, cudaStream_t s, const ElModel<T>& M,
-                 const ElShot<T>* sh, const int* wl, int ncolw, int R, int nw, int slot) {
-#define ADS_K(ST, IN, PT) \
-  k_el_velocity_rows<T, ST, IN, PT><<<g, EW * 32, 0, s>>>(M, sh, wl, ncolw, R, nw, slot)
-  if (store) ADS_EL_SEL(ADS_K, true);
-  else ADS_EL_SEL(ADS_K, false);
-#undef ADS_K
-}
 
 template <typename T>
 void el_adj1(bool in, int part, dim3 g, cudaStream_t s, const ElModel<T>& M, const ElShot<T>* sh,
@@ -1439,6 +1560,28 @@ void el_adj3(bool in, int part, dim3 g, cudaStream_t s, const ElModel<T>& M, con
 }
 #undef ADS_EL_SEL
 
+template <typename T>
+void el_step(bool store, int kind, dim3 g, cudaStream_t s, const ElModel<T>& M,
+             const ElShot<T>* sh, const int* wl, int ncolw, int R, int nw, int slot, int pin,
+             int jsh, int ish) {
+#define ADS_K(ST, KD)                                                                     \
+  k_el_step_rows<T, ST, KD><<<g, EW * 32, 0, s>>>(M, sh, wl, ncolw, R, nw, slot, pin, jsh, \
+                                                  ish)
+#define ADS_KS(ST)                   \
+  do {                               \
+    switch (kind) {                  \
+      case 0: ADS_K(ST, 0); break;   \
+      case 1: ADS_K(ST, 1); break;   \
+      case 2: ADS_K(ST, 2); break;   \
+      default: ADS_K(ST, 3); break;  \
+    }                                \
+  } while (0)
+  if (store) ADS_KS(true);
+  else ADS_KS(false);
+#undef ADS_KS
+#undef ADS_K
+}
+
 // ======================================================================
 // whole-path elastic plan
 // ======================================================================
@@ -1467,15 +1610,30 @@ struct ElPlan final : ElPlanBase {
   // launches of a step kernel run concurrently (disjoint cells)
   int* d_wl = nullptr;  // interior items, then the CPML items at nw_in
   int nw_in = 0, nw_pm = 0;
+  // the fused forward step: its own strips (FSTRIP columns), row tiles and
+  // item lists, and the state buffer that holds slot n
+  int ncolf = 0, rows_f = 0, nwtf = 0, jsh = 0, ish = 0;
+  int nwk[4] = {}, owk[4] = {};  // items of each kind (k_el_step_rows KIND) and their offsets
+  int* d_wlf = nullptr;
+  static int par(int n) { return n & 1; }
   cudaStream_t side[3] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[3] = {};
   // launches of one row-kernel step over the interior and CPML lists, whole
   // (part 0) or as its two halves (parts 1, 2)
-  int group_launches(bool split) const { return (split ? 2 : 1) * ((nw_in > 0) + (nw_pm > 0)); }
-  // fn(stream, interior, part) for each non-empty list and part, launched
-  // concurrently on the main stream and the side streams (disjoint outputs)
+  static int group_launches(bool split, int n_in, int n_pm) {
+    return (split ? 2 : 1) * ((n_in > 0) + (n_pm > 0));
+  }
+  int fwd_launches() const {
+    return (nwk[0] > 0) + (nwk[1] > 0) + (nwk[2] > 0) + (nwk[3] > 0);
+  }
+  // fn(stream, kind) for each kind of fused-step items, concurrently
   template <typename F>
-  int group(cudaStream_t st, bool split, F&& fn);
+  int kinds(cudaStream_t st, F&& fn);
+  // fn(stream, interior, part) for each non-empty list (n_in interior items,
+  // n_pm CPML items) and part, launched concurrently on the main stream and
+  // the side streams (disjoint outputs)
+  template <typename F>
+  int group(cudaStream_t st, bool split, int n_in, int n_pm, F&& fn);
   int max_rcv = 0;                      // most receivers of a shot
   int64_t P = 0, fs = 0;
   char* pool = nullptr;
@@ -1582,8 +1740,21 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
     rows_w = c.rows_per_warp > 0 ? (int)c.rows_per_warp
                                  : (int)std::min<int64_t>(32, std::max<int64_t>(8, div_up(work, target)));
     ADS_REQUIRE(rows_w >= 1 && rows_w <= NX, "rows_per_warp must be in [1, NX]");
+    // the fused step recomputes two stress rows on each side of a row tile:
+    // 24-row tiles (measured best on 600 x 300 x 32 shots among 16..32),
+    // shorter when that leaves less than about one wave of ~20 warps per SM
+    const int64_t workf = (int64_t)div_up(NY, FSTRIP) * NX * ns;
+    rows_f = c.rows_per_warp > 0
+                 ? (int)c.rows_per_warp
+                 : (int)std::min<int64_t>(
+                       NX, std::min<int64_t>(24, std::max<int64_t>(
+                                                     8, div_up(workf, (int64_t)sms * 20))));
   }
   nwt = ncolw * (int)div_up(NX, rows_w);
+  // upper bound of the fused items for any shift (the shifts are chosen once
+  // the CPML profiles are known)
+  const int nwtf_max =
+      (int)(div_up(NY + FSTRIP - 2, FSTRIP) * div_up(NX + rows_f - 1, rows_f));
   trace_off.resize(ns);
   trace_total = 0;
   for (int s = 0; s < ns; s++) {
@@ -1592,8 +1763,8 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   }
   // ---- layout
   struct Off {
-    size_t state, g, tmp, store, ckpt, acc, acc32, srcv, scell, stype, rcell, rtype, sptr, rptr,
-        gptr;
+    size_t state, g, tmp, store, ckpt, acc, acc32, srcv, scell, stype, sdual, rcell, rtype, sptr,
+        rptr, gptr;
   };
   std::vector<Off> o(ns);
   size_t used = 0;
@@ -1604,7 +1775,7 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   };
   const size_t F = sizeof(T) * fs;
   const size_t fwd0 = used;
-  for (int s = 0; s < ns; s++) o[s].state = take(NF * F);
+  for (int s = 0; s < ns; s++) o[s].state = take(2 * NF * F);  // two step buffers
   const size_t traces_o = take(sizeof(T) * std::max<int64_t>(trace_total, 1));
   zero_fwd_off = fwd0;
   zero_fwd_len = used - fwd0;
@@ -1624,6 +1795,7 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
     o[s].srcv = take(sizeof(T) * std::max<int64_t>(NSTEP * h.nsrc, 1));
     o[s].scell = take(sizeof(int64_t) * std::max<int64_t>(h.nsrc, 1));
     o[s].stype = take(sizeof(int) * std::max<int64_t>(h.nsrc, 1));
+    o[s].sdual = take(sizeof(int) * std::max<int64_t>(h.nsrc, 1));
     o[s].rcell = take(sizeof(int64_t) * std::max<int64_t>(h.nrcv, 1));
     o[s].rtype = take(sizeof(int) * std::max<int64_t>(h.nrcv, 1));
     o[s].sptr = take(sizeof(T*) * std::max<int64_t>(h.nsrc, 1));
@@ -1636,6 +1808,7 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   const size_t part_o = take(sizeof(double) * kBlocks);
   const size_t shots_o = take(sizeof(ElShot<T>) * ns);
   const size_t wl_o = take(sizeof(int) * std::max(nwt, 1));
+  const size_t wlf_o = take(sizeof(int) * std::max(nwtf_max, 1));
   bytes = (int64_t)used;
   {
     cudaError_t e = cudaMalloc(&pool, used);
@@ -1663,7 +1836,7 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   // warp items: a (strip, row tile) is interior when every cell it updates lies
   // inside all four update boxes (2 <= i <= NX-1, 2 <= j <= NY-1) with no
   // active CPML profile on its rows and columns (as the kernels see them)
-  std::vector<int> wl_host;
+  std::vector<int> wl_host, wlf_host;
   {
     const T *axi = prof.data(), *axh = axi + NX, *bxi = axi + 2 * NX, *bxh = axi + 3 * NX;
     const T *ayi = axi + 4 * NX, *ayh = ayi + NY, *byi = ayi + 2 * NY, *byh = ayi + 3 * NY;
@@ -1687,10 +1860,71 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
     nw_in = (int)wl_host.size();
     nw_pm = (int)wpm.size();
     wl_host.insert(wl_host.end(), wpm.begin(), wpm.end());
+    // fused-step items by kind: bit 0 when a row whose stresses the warp
+    // computes (i0-2 .. i_end+1) lies on a box edge or in the x-CPML, bit 1
+    // when a column of lanes 1..30 (a-2 .. a+FSTRIP+1 for a strip owning
+    // columns from a) lies on a box edge or in the y-CPML
+    auto tile_ok = [&](int rt, int sh_) {
+      const int i0r = 1 + sh_ + rt * rows_f;
+      const int i0 = std::max(i0r, 1), i1 = std::min(i0r + rows_f, NX + 1);
+      for (int i = i0 - 2; i <= i1 + 1; i++)
+        if (i < 0 || i > NX + 1 || !row_ok[i]) return false;
+      return true;
+    };
+    auto strip_ok = [&](int strip, int sh_) {
+      const int a = 1 + sh_ + strip * FSTRIP;
+      for (int jc = a - 2; jc <= a + FSTRIP + 1; jc++)
+        if (jc < 0 || jc > NY + 1 || !col_ok[jc]) return false;
+      return true;
+    };
+    // shifts of the strip and tile origins with the most CPML-free strips
+    // and tiles (then the fewest strips and tiles)
+    {
+      int best = -1, bestn = 0;
+      for (int sh_ = 0; sh_ > -FSTRIP; sh_ -= 2) {
+        const int n = (int)div_up(NY - sh_, FSTRIP);
+        int ok = 0;
+        for (int k = 0; k < n; k++) ok += strip_ok(k, sh_);
+        if (ok > best || (ok == best && n < bestn)) {
+          best = ok;
+          bestn = n;
+          jsh = sh_;
+        }
+      }
+      ncolf = bestn;
+      best = -1;
+      int bestt = 0;
+      for (int sh_ = 0; sh_ > -rows_f; sh_--) {
+        const int n = (int)div_up(NX - sh_, rows_f);
+        int ok = 0;
+        for (int k = 0; k < n; k++) ok += tile_ok(k, sh_);
+        if (ok > best || (ok == best && n < bestt)) {
+          best = ok;
+          bestt = n;
+          ish = sh_;
+        }
+      }
+      nwtf = ncolf * bestt;
+    }
+    std::vector<int> wk[4];
+    for (int wi = 0; wi < nwtf; wi++) {
+      const int strip = wi % ncolf, rt = wi / ncolf;
+      wk[(tile_ok(rt, ish) ? 0 : 1) | (strip_ok(strip, jsh) ? 0 : 2)].push_back(wi);
+    }
+    wlf_host.clear();
+    for (int k = 0; k < 4; k++) {
+      owk[k] = (int)wlf_host.size();
+      nwk[k] = (int)wk[k].size();
+      wlf_host.insert(wlf_host.end(), wk[k].begin(), wk[k].end());
+    }
   }
   d_wl = (int*)(pool + wl_o);
   ADS_CUDA(cudaMemcpyAsync(d_wl, wl_host.data(), sizeof(int) * wl_host.size(),
                            cudaMemcpyHostToDevice, st));
+  d_wlf = (int*)(pool + wlf_o);
+  if (!wlf_host.empty())
+    ADS_CUDA(cudaMemcpyAsync(d_wlf, wlf_host.data(), sizeof(int) * wlf_host.size(),
+                             cudaMemcpyHostToDevice, st));
   for (auto& q : side) ADS_CUDA(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
   ADS_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
   for (auto& e : ev_join) ADS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1723,6 +1957,7 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
     d.srcv = (const T*)(pool + o[s].srcv);
     d.src_cell = (const int64_t*)(pool + o[s].scell);
     d.src_type = (const int*)(pool + o[s].stype);
+    d.src_dual = (const int*)(pool + o[s].sdual);
     d.rcv_cell = (const int64_t*)(pool + o[s].rcell);
     d.rcv_type = (const int*)(pool + o[s].rtype);
     d.src_ptr = (T* const*)(pool + o[s].sptr);
@@ -1749,6 +1984,26 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
                                cudaMemcpyHostToDevice, st));
       stage.emplace_back((char*)type.data(), (char*)(type.data() + type.size()));
       ADS_CUDA(cudaMemcpyAsync((void*)d.src_type, stage.back().data(), stage.back().size(),
+                               cudaMemcpyHostToDevice, st));
+      // sources on cells outside the update box of their field (vx: rows and
+      // columns 2..N; vy: 1..N-1; sxx, syy: rows 1..NX-1, columns 2..NY;
+      // sxy: rows 2..NX, columns 1..NY-1) are added to both state buffers
+      std::vector<int> dual(h.nsrc);
+      for (int64_t k = 0; k < h.nsrc; k++) {
+        const int64_t i = h.srci[k] - 1, jj = h.srcj[k] - 1;
+        bool in = false;
+        switch (type[k]) {
+          case VX: in = i >= 2 && i <= NX && jj >= 2 && jj <= NY; break;
+          case VY: in = i >= 1 && i <= NX - 1 && jj >= 1 && jj <= NY - 1; break;
+          case SXX:
+          case SYY: in = i >= 1 && i <= NX - 1 && jj >= 2 && jj <= NY; break;
+          case SXY: in = i >= 2 && i <= NX && jj >= 1 && jj <= NY - 1; break;
+          default: break;
+        }
+        dual[k] = in ? 0 : 1;
+      }
+      stage.emplace_back((char*)dual.data(), (char*)(dual.data() + dual.size()));
+      ADS_CUDA(cudaMemcpyAsync((void*)d.src_dual, stage.back().data(), stage.back().size(),
                                cudaMemcpyHostToDevice, st));
       std::vector<T*> ptr(h.nsrc);
       for (int64_t k = 0; k < h.nsrc; k++)
@@ -1822,12 +2077,12 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
 // One forward step n (slot n-1 -> slot n) for every shot.
 template <typename T>
 template <typename F>
-int ElPlan<T>::group(cudaStream_t st, bool split, F&& fn) {
+int ElPlan<T>::group(cudaStream_t st, bool split, int n_in, int n_pm, F&& fn) {
   bool in_[4];
   int part_[4], n = 0;
   for (int l = 0; l < 2; l++) {
     const bool in = l == 0;
-    if ((in ? nw_in : nw_pm) == 0) continue;
+    if ((in ? n_in : n_pm) == 0) continue;
     for (int part = split ? 1 : 0; part <= (split ? 2 : 0); part++) {
       in_[n] = in;
       part_[n++] = part;
@@ -1848,43 +2103,59 @@ int ElPlan<T>::group(cudaStream_t st, bool split, F&& fn) {
   return ADS_OK;
 }
 
+template <typename T>
+template <typename F>
+int ElPlan<T>::kinds(cudaStream_t st, F&& fn) {
+  int kd[4], n = 0;
+  for (int k = 0; k < 4; k++)
+    if (nwk[k] > 0) kd[n++] = k;
+  if (n > 1) {
+    ADS_CUDA(cudaEventRecord(ev_fork, st));
+    for (int k = 1; k < n; k++) ADS_CUDA(cudaStreamWaitEvent(side[k - 1], ev_fork, 0));
+  }
+  for (int k = 0; k < n; k++) {
+    fn(k == 0 ? st : side[k - 1], kd[k]);
+    ADS_LAUNCHED(1);
+  }
+  for (int k = 1; k < n; k++) {
+    ADS_CUDA(cudaEventRecord(ev_join[k - 1], side[k - 1]));
+    ADS_CUDA(cudaStreamWaitEvent(st, ev_join[k - 1], 0));
+  }
+  return ADS_OK;
+}
+
 // The three adjoint passes of step n (store slot `slot`).
 template <typename T>
 int ElPlan<T>::adjoint_step(cudaStream_t st, int slot) {
   auto wl = [&](bool in) { return in ? d_wl : d_wl + nw_in; };
   auto nw = [&](bool in) { return in ? nw_in : nw_pm; };
-  if (int e = group(st, kSplitAdj1, [&](cudaStream_t s, bool in, int part) {
+  if (int e = group(st, kSplitAdj1, nw_in, nw_pm, [&](cudaStream_t s, bool in, int part) {
         el_adj1<T>(in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w, nw(in),
                    slot);
       }))
     return e;
-  if (int e = group(st, kSplitAdj23, [&](cudaStream_t s, bool in, int part) {
+  if (int e = group(st, kSplitAdj23, nw_in, nw_pm, [&](cudaStream_t s, bool in, int part) {
         el_adj2<T>(in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w, nw(in),
                    slot);
       }))
     return e;
-  return group(st, kSplitAdj23, [&](cudaStream_t s, bool in, int part) {
+  return group(st, kSplitAdj23, nw_in, nw_pm, [&](cudaStream_t s, bool in, int part) {
     el_adj3<T>(in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w, nw(in));
   });
 }
 
-// One forward step n (slot n-1 -> slot n) for every shot.
+// One forward step n (slot n-1 in buffer par(n-1) -> slot n in buffer
+// par(n)) for every shot.
 template <typename T>
 int ElPlan<T>::step(cudaStream_t st, int n, bool store, int slot, bool record) {
-  auto wl = [&](bool in) { return in ? d_wl : d_wl + nw_in; };
-  auto nw = [&](bool in) { return in ? nw_in : nw_pm; };
   const int sl = store ? slot : 0;
-  if (int e = group(st, kSplitFwd, [&](cudaStream_t s, bool in, int part) {
-        el_stress<T>(store, in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w,
-                     nw(in), sl);
+  if (int e = kinds(st, [&](cudaStream_t s, int k) {
+        el_step<T>(store, k, grid_rows(nwk[k]), s, M, d_shots, d_wlf + owk[k], ncolf, rows_f,
+                   nwk[k], sl, par(n - 1), jsh, ish);
       }))
     return e;
-  if (int e = group(st, kSplitFwd, [&](cudaStream_t s, bool in, int part) {
-        el_velocity<T>(store, in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw,
-                       rows_w, nw(in), sl);
-      }))
-    return e;
-  k_el_src_rcv<T><<<nshots, rcv_threads(), 0, st>>>(d_shots, n, NSTEP + 1, record ? 1 : 0);
+  k_el_src_rcv<T><<<nshots, rcv_threads(), 0, st>>>(d_shots, n, NSTEP + 1, record ? 1 : 0,
+                                                    par(n), 1);
   ADS_LAUNCHED(1);
   return ADS_OK;
 }
@@ -1894,7 +2165,7 @@ int ElPlan<T>::issue_forward(cudaStream_t st, int64_t* count) {
   if (count) {
     int64_t c = 0;
     for (int n = 1; n <= NSTEP; n++)
-      c += 2 * group_launches(kSplitFwd) + 1 + ((n % K == 0 && n / K < nseg) ? 1 : 0);
+      c += fwd_launches() + 1 + ((n % K == 0 && n / K < nseg) ? 1 : 0);
     *count = c;
     return ADS_OK;
   }
@@ -1902,7 +2173,7 @@ int ElPlan<T>::issue_forward(cudaStream_t st, int64_t* count) {
   for (int n = 1; n <= NSTEP; n++) {
     if (int e = step(st, n, false, 0, true)) return e;
     if (n % K == 0 && n / K < nseg) {  // checkpoint s holds slot s*K (state before step sK+1)
-      k_el_ckpt<T><<<dim3(256, nshots), 256, 0, st>>>(d_shots, n / K, 1);
+      k_el_ckpt<T><<<dim3(256, nshots), 256, 0, st>>>(d_shots, n / K, 1, par(n), 0);
       ADS_LAUNCHED(1);
     }
   }
@@ -1915,8 +2186,9 @@ int ElPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     int64_t c = 1;
     for (int s = nseg - 1; s >= 0; s--) {
       const int a = 1 + s * K, b = std::min(a + K - 1, NSTEP);
-      c += 1 + (2 * group_launches(kSplitFwd) + 1) * (b - a + 1) +
-           (group_launches(kSplitAdj1) + 2 * group_launches(kSplitAdj23)) * (b - a + 1) +
+      c += 1 + (fwd_launches() + 1) * (b - a + 1) +
+           (group_launches(kSplitAdj1, nw_in, nw_pm) +
+            2 * group_launches(kSplitAdj23, nw_in, nw_pm)) * (b - a + 1) +
            (b - std::max(a, 2) + 1) +
            (sizeof(T) == 4 ? 1 : 0);
     }
@@ -1929,7 +2201,7 @@ int ElPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
   ADS_LAUNCHED(1);
   for (int s = nseg - 1; s >= 0; s--) {
     const int a = 1 + s * K, b = std::min(a + K - 1, NSTEP);
-    k_el_ckpt<T><<<dim3(256, nshots), 256, 0, st>>>(d_shots, s, 0);
+    k_el_ckpt<T><<<dim3(256, nshots), 256, 0, st>>>(d_shots, s, 0, 0, 1);
     ADS_LAUNCHED(1);
     for (int n = a; n <= b; n++)
       if (int e = step(st, n, true, n - a, false)) return e;
@@ -2009,9 +2281,9 @@ int ElPlan<T>::gradient(const double* l, const double* m, const double* r, const
 // times back to back on the plan's buffers between two events (direct
 // launches; the state is scratch afterwards and the next forward / gradient
 // starts from zero as always).  out[2k] = ms per launch, out[2k+1] = interior
-// cell-updates per launch, for k = stress, velocity, stress (storing),
-// velocity (storing), adjoint 1, adjoint 2, adjoint 3, sources / receivers,
-// residual injection.
+// cell-updates per launch, for k = forward step (the fused kernel's launches
+// over the item kinds), forward step storing the adjoint's strains, adjoint
+// 1, adjoint 2, adjoint 3, sources / receivers, residual injection.
 template <typename T>
 int ElPlan<T>::profile(const double* l, const double* m, const double* r, double* out,
                        cudaStream_t st) {
@@ -2042,34 +2314,32 @@ int ElPlan<T>::profile(const double* l, const double* m, const double* r, double
   ADS_CUDA(cudaMemsetAsync(pool + zero_adj_off, 0, zero_adj_len, st));
   auto wl = [&](bool in) { return in ? d_wl : d_wl + nw_in; };
   auto nw = [&](bool in) { return in ? nw_in : nw_pm; };
-  for (int k = 0; k < 4; k++)
+  for (int k = 0; k < 2; k++)
     run(k, [&] {
-      group(st, kSplitFwd, [&](cudaStream_t s, bool in, int part) {
-        if (k % 2 == 0)
-          el_stress<T>(k >= 2, in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw,
-                       rows_w, nw(in), 0);
-        else
-          el_velocity<T>(k >= 2, in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw,
-                         rows_w, nw(in), 0);
+      kinds(st, [&](cudaStream_t s, int kd) {
+        el_step<T>(k == 1, kd, grid_rows(nwk[kd]), s, M, d_shots, d_wlf + owk[kd], ncolf,
+                   rows_f, nwk[kd], 0, 0, jsh, ish);
       });
     });
-  run(4, [&] {
-    group(st, kSplitAdj1, [&](cudaStream_t s, bool in, int part) {
+  run(2, [&] {
+    group(st, kSplitAdj1, nw_in, nw_pm, [&](cudaStream_t s, bool in, int part) {
       el_adj1<T>(in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w, nw(in), 0);
     });
   });
-  run(5, [&] {
-    group(st, kSplitAdj23, [&](cudaStream_t s, bool in, int part) {
+  run(3, [&] {
+    group(st, kSplitAdj23, nw_in, nw_pm, [&](cudaStream_t s, bool in, int part) {
       el_adj2<T>(in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w, nw(in), 0);
     });
   });
-  run(6, [&] {
-    group(st, kSplitAdj23, [&](cudaStream_t s, bool in, int part) {
+  run(4, [&] {
+    group(st, kSplitAdj23, nw_in, nw_pm, [&](cudaStream_t s, bool in, int part) {
       el_adj3<T>(in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w, nw(in));
     });
   });
-  run(7, [&] { k_el_src_rcv<T><<<nshots, rcv_threads(), 0, st>>>(d_shots, 1, NSTEP + 1, 1); });
-  run(8, [&] { k_el_resid<T><<<grid_resid(), 256, 0, st>>>(d_shots, 1, NSTEP + 1); });
+  run(5, [&] {
+    k_el_src_rcv<T><<<nshots, rcv_threads(), 0, st>>>(d_shots, 1, NSTEP + 1, 1, 0, 0);
+  });
+  run(6, [&] { k_el_resid<T><<<grid_resid(), 256, 0, st>>>(d_shots, 1, NSTEP + 1); });
   note_launches(2 * (kProfileReps + 1));  // the pairs count their own launches
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

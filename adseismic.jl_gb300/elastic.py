@@ -202,8 +202,7 @@ class ElasticPlan:
              _stream())
         return tr[:self.trace_count]
 
-    KERNELS = ("stress", "velocity", "stress_store", "velocity_store", "adj1", "adj2", "adj3",
-               "src_rcv", "resid")
+    KERNELS = ("step", "step_store", "adj1", "adj2", "adj3", "src_rcv", "resid")
 
     def profile(self, lam, mu, rho):
         """Per-kernel durations on this plan's buffers (ads_elastic_plan_profile):
@@ -212,7 +211,7 @@ class ElasticPlan:
 
         _require_cuda(lam, mu, rho)
         lam, mu, rho = (t.contiguous().to(torch.float64) for t in (lam, mu, rho))
-        out = np.zeros(18)
+        out = np.zeros(2 * len(self.KERNELS))
         call("ads_elastic_plan_profile", self._h, _ptr(lam), _ptr(mu), _ptr(rho),
              out.ctypes.data_as(C.c_void_p), _stream())
         return {k: (float(out[2 * i]), float(out[2 * i + 1])) for i, k in enumerate(self.KERNELS)}

@@ -367,11 +367,11 @@ def run_elastic_fwi(args):
     b_adj = b_fwd + 68
     prof = plan.profile(l0, m0, r0)
     peak, peak_kind = measured_peak()
-    fwd_ms = prof["stress"][0] + prof["velocity"][0]
+    fwd_ms = prof["step"][0]
     adj_ms = prof["adj1"][0] + prof["adj2"][0] + prof["adj3"][0]
-    c1 = prof["stress"][1]
+    c1 = prof["step"][1]
     groups = {
-        "k_el_stress_rows+k_el_velocity_rows": (fwd_ms, b_fwd * c1),
+        "k_el_step_rows": (fwd_ms, b_fwd * c1),
         "k_el_adj1_rows+k_el_adj2_rows+k_el_adj3_rows": (adj_ms, b_adj * c1),
     }
     kern = {k: {"ms_per_step": round(t, 4), "achieved_gbs": round(b / (t / 1e3) / 1e9, 1),

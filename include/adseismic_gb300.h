@@ -375,11 +375,11 @@ int ads_elastic_plan_gradient(ads_elastic_plan* plan, const double* lambda,
                               double* loss, double* grad_lambda, double* grad_mu,
                               double* grad_rho, void* traces_out, ads_stream_t stream);
 /* Kernel timing (no reference counterpart): every step kernel of the plan is
- * launched 20 times on the plan's buffers between CUDA events.  out: 18
+ * launched 20 times on the plan's buffers between CUDA events.  out: 14
  * doubles, pairs (ms per launch, interior cell-updates per launch) for the
- * stress, velocity, stress (storing), velocity (storing), adjoint 1..3,
- * source / receiver and residual kernels.  Leaves the plan's state zeroed;
- * synchronises the stream. */
+ * forward step, the forward step storing the adjoint's strains, adjoint
+ * 1..3, the source / receiver and the residual kernels.  Leaves the plan's
+ * state zeroed; synchronises the stream. */
 int ads_elastic_plan_profile(ads_elastic_plan* plan, const double* lambda,
                              const double* mu, const double* rho, double* out,
                              ads_stream_t stream);

@@ -132,3 +132,55 @@ def test_multishot_sum_and_julia_api(ads, orc, cuda):
                               shots[0]["srctype"], shots[0]["srcv"], shots[0]["rcvi"],
                               shots[0]["rcvj"], shots[0]["rcvtype"])
     assert rel(rcv.rcvv.cpu().numpy(), ref) <= 1e-12
+
+
+@pytest.mark.parametrize("rows_per_warp", [0, 5])
+def test_plan_strips_tiles_and_edge_sources_vs_oracle(ads, orc, cuda, rows_per_warp):
+    """Several column strips and row tiles, an odd checkpoint interval (the
+    step buffers alternate, so checkpoints land on both parities) and sources
+    on cells no stencil updates (padded ring, box edges), which keep their
+    value between steps and accumulate the source."""
+    NX, NY, T = 61, 131, 41
+    p = ads.ElasticPropagatorParams(NX=NX, NY=NY, NSTEP=T, DELTAX=10.0, DELTAY=10.0,
+                                    DELTAT=0.8e-3, NPOINTS_PML=9, vp_ref=3000.0, f0=15.0)
+    prof = ads.compute_elastic_PML_Params(p)
+    ax, bx, kx, ay, by, ky = [a.reshape(-1) for a in prof]
+    rng = np.random.default_rng(7)
+    vp = 3000 + 300 * rng.random((NX + 2, NY + 2))
+    lam, mu, rho = ads.compute_properties(vp, vp / 1.8, 2000 + 200 * rng.random((NX + 2, NY + 2)))
+    lam, mu, rho = (a.reshape(-1) for a in (lam, mu, rho))
+    # 1-based padded-grid cells: ring corners and edges, box edges, interior
+    srci = np.array([1, NX + 2, 2, NX + 1, 2, 30, 31, 17, NX + 1, 2])
+    srcj = np.array([1, NY + 2, 2, 5, NY + 1, 1, 60, 90, NY + 1, 70])
+    srct = np.array([0, 1, 2, 4, 3, 2, 0, 4, 0, 1])
+    srcv = rng.standard_normal((T, len(srci))) * 1e3
+    rcvi = rng.integers(1, NX + 3, 25)
+    rcvj = rng.integers(1, NY + 3, 25)
+    rcvi[:3], rcvj[:3] = srci[:3], srcj[:3]
+    rcvt = rng.integers(0, 5, 25)
+    rcvt[:3] = srct[:3]
+    obs = rng.standard_normal((25, T + 1)) * 1e-3
+    sh = dict(srci=srci, srcj=srcj, srctype=srct, srcv=srcv, rcvi=rcvi, rcvj=rcvj, rcvtype=rcvt)
+    ref_tr = orc.elastic_forward(NX, NY, T, p.DELTAT, p.DELTAX, p.DELTAY, ax, bx, ay, by, lam, mu,
+                                 rho, srci, srcj, srct, srcv, rcvi, rcvj, rcvt)
+    ref = orc.elastic_gradient(NX, NY, T, p.DELTAT, p.DELTAX, p.DELTAY, ax, bx, ay, by, lam, mu,
+                               rho, srci, srcj, srct, srcv, rcvi, rcvj, rcvt, obs)
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=cuda)
+    plan = ads.ElasticPlan(p, [sh], precision="f64", ckpt_every=7,
+                           rows_per_warp=rows_per_warp)
+    tr = plan.forward(t(lam), t(mu), t(rho))
+    assert rel(tr.cpu().numpy(), ref_tr.reshape(-1)) <= 1e-12
+    loss, gl, gm, gr = plan.gradient(t(lam), t(mu), t(rho), t(obs.reshape(-1)))
+    torch.cuda.synchronize()
+    assert abs(float(loss) - ref[0]) <= 1e-12 * ref[0]
+    for a, b in zip((gl, gm, gr), ref[1:]):
+        assert rel(a.cpu().numpy(), b) <= 1e-12
+    plan.close()
+    p32 = ads.ElasticPlan(p, [sh], precision="f32", ckpt_every=7, rows_per_warp=rows_per_warp)
+    loss32, gl32, gm32, gr32 = p32.gradient(t(lam), t(mu), t(rho),
+                                            torch.as_tensor(obs.reshape(-1), device=cuda))
+    torch.cuda.synchronize()
+    assert abs(float(loss32) - ref[0]) <= 1e-4 * ref[0]
+    for a, b in zip((gl32, gm32, gr32), ref[1:]):
+        assert rel(a.cpu().numpy(), b) <= 1e-4
+    p32.close()
