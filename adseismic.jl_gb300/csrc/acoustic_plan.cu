@@ -134,8 +134,31 @@ __device__ __forceinline__ bool warp_tau_free(const T* __restrict__ ty, int j, i
   return __all_sync(FULL, z);
 }
 
+// Loads of a thread's cells as predicated PTX loads: zeros where `on` is
+// false, and no branch, so masks that differ between the lanes of a warp (the
+// last columns of a shot, the halo lanes) cost no divergence.  The asm has no
+// memory clobber: the step kernels load each cell at most once per launch,
+// and a cell they also write is written later, from values computed from the
+// load.
+__device__ __forceinline__ float ld1p(const float* p, bool on) {
+  float a = 0.f;
+  asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q ld.global.f32 %0, [%1];\n\t}"
+      : "+f"(a)
+      : "l"(p), "r"((unsigned)on));
+  return a;
+}
+__device__ __forceinline__ double ld1p(const double* p, bool on) {
+  double a = 0.0;
+  asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q ld.global.f64 %0, [%1];\n\t}"
+      : "+d"(a)
+      : "l"(p), "r"((unsigned)on));
+  return a;
+}
+
 // C-wide loads and stores of a thread's columns.  Full-width stores only when
 // all C cells are interior; otherwise per cell (the frame must stay zero).
+// ldv is a guarded load (the interior loops, whose masks agree across a
+// warp); ldvp the predicated form for the PML loops.
 template <typename T, int C>
 __device__ __forceinline__ Vec<T, C> ldv(const T* base, int64_t off, bool on) {
   Vec<T, C> x;
@@ -149,8 +172,37 @@ __device__ __forceinline__ Vec<T, C> ldv(const T* base, int64_t off, bool on) {
 }
 
 template <typename T, int C>
+__device__ __forceinline__ Vec<T, C> ldvp(const T* base, int64_t off, bool on) {
+  Vec<T, C> x;
+  const T* p = base + off;
+  if constexpr (C == 2 && sizeof(T) == 4) {
+    float a = 0.f, b = 0.f;
+    asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %3, 0;\n\t@q ld.global.v2.f32 {%0, %1}, [%2];\n\t}"
+        : "+f"(a), "+f"(b)
+        : "l"(p), "r"((unsigned)on));
+    x.v[0] = a;
+    x.v[1] = b;
+  } else if constexpr (C == 2) {
+    double a = 0.0, b = 0.0;
+    asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %3, 0;\n\t@q ld.global.v2.f64 {%0, %1}, [%2];\n\t}"
+        : "+d"(a), "+d"(b)
+        : "l"(p), "r"((unsigned)on));
+    x.v[0] = a;
+    x.v[1] = b;
+  } else {
+#pragma unroll
+    for (int c = 0; c < C; c++) x.v[c] = ld1p(p + c, on);
+  }
+  return x;
+}
+
+template <typename T, int C>
 __device__ __forceinline__ void stv(T* base, int64_t off, const Vec<T, C>& x, int j, int ny) {
-  if (j + C - 1 <= ny) {
+  if constexpr (C == 2) {
+    // two guarded stores, predicated rather than branched
+    if (j + 1 <= ny) *reinterpret_cast<Vec<T, C>*>(base + off) = x;
+    if (j == ny) base[off] = x.v[0];
+  } else if (j + C - 1 <= ny) {
     *reinterpret_cast<Vec<T, C>*>(base + off) = x;
   } else {
 #pragma unroll
@@ -177,15 +229,16 @@ __device__ __forceinline__ bool warp_tau_free(const T* __restrict__ ty, int j, i
   return __all_sync(FULL, z);
 }
 
-// The PML damping division: FP32 plans use the hardware reciprocal (within
-// 2 ulp; their error budget against the FP64 oracle is 1e-4), FP64 plans the
-// exact division (1e-12 parity).
-template <typename T>
-__device__ __forceinline__ T pml_div(T a, T b) {
+// The PML damping v / (1 + s dt/2): FP32 plans use the hardware divide
+// (within 2 ulp; their error budget against the FP64 oracle is 1e-4) on every
+// cell, s = 0 dividing by exactly 1, so lanes with and without damping take
+// one path; FP64 plans divide exactly, only where s != 0 (1e-12 parity).
+template <typename T, typename K>
+__device__ __forceinline__ T pml_damp(T v, T s, const K& k) {
   if constexpr (sizeof(T) == 4) {
-    return __fdividef(a, b);
+    return __fdividef(v, T(1) + s * k.hdt);
   } else {
-    return a / b;
+    return s != T(0) ? v / (T(1) + s * k.hdt) : v;
   }
 }
 
@@ -345,39 +398,27 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     if constexpr (!INT) record_traces<T, C, SEG>(it, sh, rcvs, out, t, lane, i0, i_end);
   } else {
   bool n0 = nz(i0);
-  V wm = ldv<T, C>(w, off(i0 - 1), jld), w0 = ldv<T, C>(w, off(i0), jld),
-    wp = ldv<T, C>(w, off(i0 + 1), jld);
-  V pm = ldv<T, C>(pin, off(i0 - 1), jld && nz(i0 - 1)), p0 = ldv<T, C>(pin, off(i0), jld && n0),
-    pp = ldv<T, C>(pin, off(i0 + 1), jld && nz(i0 + 1));
-  V q0 = ldv<T, C>(qin, off(i0), jld && n0), wo0 = ldv<T, C>(wo, off(i0), jld),
-    c0 = ldv<T, C>(cc, off(i0), jld);
-  T hw = 0, hq = 0;  // lane 0: column j-1; lane 31: column j+C
-  if (lane == 0 && jld) {
-    hw = w[off(i0) - 1];
-    hq = n0 ? qin[off(i0) - 1] : T(0);
-  } else if (lane == 31 && hr) {
-    hw = w[off(i0) + C];
-    hq = n0 ? qin[off(i0) + C] : T(0);
-  }
+  V wm = ldvp<T, C>(w, off(i0 - 1), jld), w0 = ldvp<T, C>(w, off(i0), jld),
+    wp = ldvp<T, C>(w, off(i0 + 1), jld);
+  V pm = ldvp<T, C>(pin, off(i0 - 1), jld && nz(i0 - 1)), p0 = ldvp<T, C>(pin, off(i0), jld && n0),
+    pp = ldvp<T, C>(pin, off(i0 + 1), jld && nz(i0 + 1));
+  V q0 = ldvp<T, C>(qin, off(i0), jld && n0), wo0 = ldvp<T, C>(wo, off(i0), jld),
+    c0 = ldvp<T, C>(cc, off(i0), jld);
+  // lane 0: column j-1; lane 31: column j+C
+  const int64_t hoff = lane == 0 ? -1 : C;
+  const bool hon = (lane == 0 && jld) || (lane == 31 && hr);
+  T hw = ld1p(w + off(i0) + hoff, hon), hq = ld1p(qin + off(i0) + hoff, hon && n0);
   for (int i = i0; i < i_end; i++) {
     const int64_t row = off(i);
     const bool more = i + 1 < i_end;
     const bool n1 = more && nz(i + 1);
-    V wn = ldv<T, C>(w, off(i + 2), jld && more);
-    V pn_ = ldv<T, C>(pin, off(i + 2), jld && more && nz(i + 2));
-    V qn = ldv<T, C>(qin, off(i + 1), jld && n1);
-    V won = ldv<T, C>(wo, off(i + 1), jld && more);
-    V cn = ldv<T, C>(cc, off(i + 1), jld && more);
-    T hwn = 0, hqn = 0;
-    if (more) {
-      if (lane == 0 && jld) {
-        hwn = w[row + P - 1];
-        hqn = n1 ? qin[row + P - 1] : T(0);
-      } else if (lane == 31 && hr) {
-        hwn = w[row + P + C];
-        hqn = n1 ? qin[row + P + C] : T(0);
-      }
-    }
+    V wn = ldvp<T, C>(w, off(i + 2), jld && more);
+    V pn_ = ldvp<T, C>(pin, off(i + 2), jld && more && nz(i + 2));
+    V qn = ldvp<T, C>(qin, off(i + 1), jld && n1);
+    V won = ldvp<T, C>(wo, off(i + 1), jld && more);
+    V cn = ldvp<T, C>(cc, off(i + 1), jld && more);
+    const T hwn = ld1p(w + row + P + hoff, more && hon),
+            hqn = ld1p(qin + row + P + hoff, more && hon && n1);
     T wL = __shfl_up_sync(FULL, w0.v[C - 1], 1), wR = __shfl_down_sync(FULL, w0.v[0], 1);
     T qL = __shfl_up_sync(FULL, q0.v[C - 1], 1), qR = __shfl_down_sync(FULL, q0.v[0], 1);
     if (lane == 0) {
@@ -400,7 +441,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
         T v = (T(2) - sg * tj[c] * K.dt2 - K.kxy * cv) * w0.v[c] + cv * K.cx * (wp.v[c] + wm.v[c]) +
               cv * K.cy * (wN + wS) + K.fx * (pp.v[c] - pm.v[c]) + K.fy * (qN - qS) -
               (T(1) - s * K.hdt) * wo0.v[c];
-        if (s != T(0)) v = pml_div<T>(v, T(1) + s * K.hdt);
+        v = pml_damp<T>(v, s, K);
         for (int e = it.src_b; e < it.src_e; e++) {
           const CellRef r = srcs[e];
           if (r.cell == row + c) v += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
@@ -475,7 +516,7 @@ __device__ __forceinline__ void col_terms(T gui, T gq, T c, T sg, T tj, const Ac
 
 template <typename T>
 __device__ __forceinline__ T inv_den(T s, const AcConst<T>& K) {
-  return s != T(0) ? pml_div<T>(T(1), T(1) + s * K.hdt) : T(1);
+  return pml_damp<T>(T(1), s, K);
 }
 
 // The grad_c accumulator an adjoint step adds to: the FP32 per-segment
@@ -708,29 +749,29 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     }
   } else {
   // rows i-1 (m), i (0), i+1 (p): lambdaU_k, lambdaPhi_k, c and 1/den per cell
-  V gum = ldv<T, C>(luc, off(i0 - 1), jld), gpm = ldv<T, C>(lpc, off(i0 - 1), jld && nz(i0 - 1)),
-    cm = ldv<T, C>(cc, off(i0 - 1), jld);
-  V gu0 = ldv<T, C>(luc, off(i0), jld), gp0 = ldv<T, C>(lpc, off(i0), jld && nz(i0)),
-    c0 = ldv<T, C>(cc, off(i0), jld);
-  V gu1 = ldv<T, C>(luc, off(i0 + 1), jld), gp1 = ldv<T, C>(lpc, off(i0 + 1), jld && nz(i0 + 1)),
-    c1 = ldv<T, C>(cc, off(i0 + 1), jld);
+  V gum = ldvp<T, C>(luc, off(i0 - 1), jld), gpm = ldvp<T, C>(lpc, off(i0 - 1), jld && nz(i0 - 1)),
+    cm = ldvp<T, C>(cc, off(i0 - 1), jld);
+  V gu0 = ldvp<T, C>(luc, off(i0), jld), gp0 = ldvp<T, C>(lpc, off(i0), jld && nz(i0)),
+    c0 = ldvp<T, C>(cc, off(i0), jld);
+  V gu1 = ldvp<T, C>(luc, off(i0 + 1), jld), gp1 = ldvp<T, C>(lpc, off(i0 + 1), jld && nz(i0 + 1)),
+    c1 = ldvp<T, C>(cc, off(i0 + 1), jld);
   V invm, inv0;
 #pragma unroll
   for (int c = 0; c < C; c++) {
     invm.v[c] = inv_den<T>(sx[i0 - 1] + tj[c], K);
     inv0.v[c] = inv_den<T>(sx[i0] + tj[c], K);
   }
-  V wm = ldv<T, C>(w, off(i0 - 1), jld), w0 = ldv<T, C>(w, off(i0), jld),
-    wp = ldv<T, C>(w, off(i0 + 1), jld);
+  V wm = ldvp<T, C>(w, off(i0 - 1), jld), w0 = ldvp<T, C>(w, off(i0), jld),
+    wp = ldvp<T, C>(w, off(i0 + 1), jld);
   bool n0 = nz(i0);
-  V gq = ldv<T, C>(lqc, off(i0), jld && n0), ln = ldv<T, C>(lun, off(i0), jld);
-  T hgu = 0, hgq = 0, hc = 0, hw = 0;
-  if (hon) {
+  V gq = ldvp<T, C>(lqc, off(i0), jld && n0), ln = ldvp<T, C>(lun, off(i0), jld);
+  T hgu, hgq, hc, hw;
+  {
     const int64_t r = off(i0) + hoff;
-    hgu = luc[r];
-    hgq = n0 ? lqc[r] : T(0);
-    hc = cc[r];
-    hw = w[r];
+    hgu = ld1p(luc + r, hon);
+    hgq = ld1p(lqc + r, hon && n0);
+    hc = ld1p(cc + r, hon);
+    hw = ld1p(w + r, hon);
   }
   T sgm = sx[i0 - 1], sg0 = sx[i0];
   for (int i = i0; i < i_end; i++) {
@@ -743,20 +784,15 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     // lambdaU_{k+1}) and the halo cell of row i+1
     const bool more = i + 1 < i_end;
     const bool n1 = more && nz(i + 1);
-    V gu2 = ldv<T, C>(luc, off(i + 2), jld && more);
-    V gp2 = ldv<T, C>(lpc, off(i + 2), jld && more && nz(i + 2));
-    V c2 = ldv<T, C>(cc, off(i + 2), jld && more);
-    V w2 = ldv<T, C>(w, off(i + 2), jld && more);
-    V gqn = ldv<T, C>(lqc, off(i + 1), jld && n1);
-    V lnn = ldv<T, C>(lun, off(i + 1), jld && more);
-    T hgun = 0, hgqn = 0, hcn = 0, hwn = 0;
-    if (more && hon) {
-      const int64_t r = row + P + hoff;
-      hgun = luc[r];
-      hgqn = n1 ? lqc[r] : T(0);
-      hcn = cc[r];
-      hwn = w[r];
-    }
+    V gu2 = ldvp<T, C>(luc, off(i + 2), jld && more);
+    V gp2 = ldvp<T, C>(lpc, off(i + 2), jld && more && nz(i + 2));
+    V c2 = ldvp<T, C>(cc, off(i + 2), jld && more);
+    V w2 = ldvp<T, C>(w, off(i + 2), jld && more);
+    V gqn = ldvp<T, C>(lqc, off(i + 1), jld && n1);
+    V lnn = ldvp<T, C>(lun, off(i + 1), jld && more);
+    const int64_t rh = row + P + hoff;
+    const T hgun = ld1p(luc + rh, more && hon), hgqn = ld1p(lqc + rh, more && hon && n1),
+            hcn = ld1p(cc + rh, more && hon), hwn = ld1p(w + rh, more && hon);
     // j-direction terms of this thread's cells and of the neighbouring columns
     T YP[C], YM[C], YR[C], gui[C];
 #pragma unroll
