@@ -479,23 +479,10 @@ __device__ __forceinline__ V2<double> ld2p(const double* p, int64_t o, bool on) 
   return x;
 }
 
-// Store the two cells of a lane, each only where its box flag is set.
-template <typename T>
-__device__ __forceinline__ void st2(T* p, int64_t o, const T (&x)[2], bool k0, bool k1) {
-  if (k0 && k1) {
-    V2<T> y;
-    y.v[0] = x[0];
-    y.v[1] = x[1];
-    *reinterpret_cast<V2<T>*>(p + o) = y;
-  } else {
-    if (k0) p[o] = x[0];
-    if (k1) p[o + 1] = x[1];
-  }
-}
-
-// The same as st2 as three independent guarded stores (a vector store when
-// both cells are written, else the single cell), which compile to predicated
-// stores instead of branches.
+// Store the two cells of a lane, each only where its flag is set, as three
+// independent guarded stores (a vector store when both cells are written,
+// else the single cell), which compile to predicated stores rather than
+// branches.
 template <typename T>
 __device__ __forceinline__ void st2p(T* p, int64_t o, const T (&x)[2], bool k0, bool k1) {
   if (k0 && k1) {
@@ -972,6 +959,27 @@ k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
     c4[c] = S.out && (INT || (j + c >= 1 && j + c <= NY - 1));
   }
   const int i0 = S.i0;
+  // CPML items: the memory-variable adjoints g5..g8 of a row, loaded one row
+  // ahead where they can be nonzero, with predicated loads
+  const bool lx3 = c3[0] || c3[1], lx4 = c4[0] || c4[1];
+  const bool ly3 = !INT && ((c3[0] && Y.acti[0]) || (c3[1] && Y.acti[1]));
+  const bool ly4 = !INT && ((c4[0] && Y.acth[0]) || (c4[1] && Y.acth[1]));
+  auto gload = [&](int r, V2<T> (&g)[4]) {
+    if constexpr (!INT) {
+      const int rr = min(max(r, 1), NX) - 1;
+      const bool on = r < S.i_end;
+      const bool q3 = on && PART != 2 && r >= 2, q4 = on && PART != 1 && r <= NX - 1;
+      const bool x5 = q3 && (M.axi[rr] != T(0) || M.bxi[rr] != T(1));
+      const bool x7 = q4 && (M.axh[rr] != T(0) || M.bxh[rr] != T(1));
+      const int64_t o = S.off(r);
+      g[0] = ld2p(g5, o, x5 && lx3);
+      g[1] = ld2p(g6, o, q3 && ly3);
+      g[2] = ld2p(g7, o, x7 && lx4);
+      g[3] = ld2p(g8, o, q4 && ly4);
+    }
+  };
+  V2<T> gg[4] = {};
+  gload(i0, gg);
   V2<T> R0 = S.row(M.rho, i0), R1 = S.row(M.rho, i0 + 1);
   V2<T> GX = S.row(gvx, i0), GY = S.row(gvy, i0), E3 = S.row(a3p, i0), E4 = S.row(a4p, i0);
   V2<A> GR = S.row(grp, i0);
@@ -983,6 +991,8 @@ k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
     const V2<T> GXn = S.row(gvx, rn), GYn = S.row(gvy, rn), E3n = S.row(a3p, rn),
                 E4n = S.row(a4p, rn);
     const V2<A> GRn = S.row(grp, rn);
+    V2<T> gn[4] = {};
+    gload(i + 1, gn);
     T r0[3], r1[3];
     r0[0] = R0.v[0];
     r0[1] = R0.v[1];
@@ -995,23 +1005,27 @@ k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
     const bool r3 = INT || i >= 2, r4 = INT || i <= NX - 1;
     const bool rx5 = !INT && r3 && (axi != T(0) || bxi != T(1));
     const bool rx7 = !INT && r4 && (axh != T(0) || bxh != T(1));
-    T o5[2], o6[2], o7[2], o8[2], o4[2];
+    T o5[2], o6[2], o7[2], o8[2], o4[2], sg5[2], sg6[2], sg7[2], sg8[2];
     A gr[2];
-    bool k3[2], k4[2];
+    bool k3[2], k4[2], w5[2], w6[2], w7[2], w8[2];
 #pragma unroll
     for (int c = 0; c < 2; c++) {
       k3[c] = PART != 2 && r3 && c3[c];
       k4[c] = PART != 1 && r4 && c4[c];
       o5[c] = o6[c] = o7[c] = o8[c] = o4[c] = T(0);
+      sg5[c] = sg6[c] = sg7[c] = sg8[c] = T(0);
+      w5[c] = w6[c] = w7[c] = w8[c] = false;
       gr[c] = A(0);
       if constexpr (PART != 2) {  // fw3 transpose
       const T gv = GX.v[c], r = r0[c];
       const T q = divr<T>(gv * M.dt, r);
       const bool u5 = k3[c] && rx5, u6 = !INT && k3[c] && Y.acti[c];
-      const T gm5 = u5 ? q + g5[o + c] : q;
-      const T gm6 = u6 ? q + g6[o + c] : q;
-      if (u5) g5[o + c] = bxi * gm5;
-      if (u6) g6[o + c] = Y.bi[c] * gm6;
+      const T gm5 = u5 ? q + gg[0].v[c] : q;
+      const T gm6 = u6 ? q + gg[1].v[c] : q;
+      sg5[c] = bxi * gm5;
+      sg6[c] = Y.bi[c] * gm6;
+      w5[c] = u5;
+      w6[c] = u6;
       o5[c] = hdiv<T>(q + axi * gm5, M.hx24, M.rhx24);
       o6[c] = hdiv<T>(q + (INT ? T(0) : Y.ai[c]) * gm6, M.hy24, M.rhy24);
       gr[c] = GR.v[c] + (A)divr<T>(-gv * E3.v[c] * M.dt, r * r);
@@ -1021,21 +1035,35 @@ k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
       const T rho_ = T(0.25) * (r0[c] + r1[c] + r1[c + 1] + r0[c + 1]);
       const T q4 = divr<T>(gw * M.dt, rho_);
       const bool u7 = k4[c] && rx7, u8 = !INT && k4[c] && Y.acth[c];
-      const T gm7 = u7 ? q4 + g7[o + c] : q4;
-      const T gm8 = u8 ? q4 + g8[o + c] : q4;
-      if (u7) g7[o + c] = bxh * gm7;
-      if (u8) g8[o + c] = Y.bh[c] * gm8;
+      const T gm7 = u7 ? q4 + gg[2].v[c] : q4;
+      const T gm8 = u8 ? q4 + gg[3].v[c] : q4;
+      sg7[c] = bxh * gm7;
+      sg8[c] = Y.bh[c] * gm8;
+      w7[c] = u7;
+      w8[c] = u8;
       o7[c] = hdiv<T>(q4 + axh * gm7, M.hx24, M.rhx24);
       o8[c] = hdiv<T>(q4 + (INT ? T(0) : Y.ah[c]) * gm8, M.hy24, M.rhy24);
       o4[c] = divr<T>(-gw * E4.v[c] * M.dt, rho_ * rho_) * T(0.25);
       }
     }
-    st2<T>(d5, o, o5, k3[0], k3[1]);
-    st2<T>(d6, o, o6, k3[0], k3[1]);
-    st2<A>(grp, o, gr, k3[0], k3[1]);
-    st2<T>(d7, o, o7, k4[0], k4[1]);
-    st2<T>(d8, o, o8, k4[0], k4[1]);
-    st2<T>(r4p, o, o4, k4[0], k4[1]);
+    if constexpr (!INT) {
+      if constexpr (PART != 2) {
+        st2p<T>(g5, o, sg5, w5[0], w5[1]);
+        st2p<T>(g6, o, sg6, w6[0], w6[1]);
+      }
+      if constexpr (PART != 1) {
+        st2p<T>(g7, o, sg7, w7[0], w7[1]);
+        st2p<T>(g8, o, sg8, w8[0], w8[1]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) gg[q] = gn[q];
+    st2p<T>(d5, o, o5, k3[0], k3[1]);
+    st2p<T>(d6, o, o6, k3[0], k3[1]);
+    st2p<A>(grp, o, gr, k3[0], k3[1]);
+    st2p<T>(d7, o, o7, k4[0], k4[1]);
+    st2p<T>(d8, o, o8, k4[0], k4[1]);
+    st2p<T>(r4p, o, o4, k4[0], k4[1]);
     R0 = R1; R1 = R2;
     GX = GXn; GY = GYn; E3 = E3n; E4 = E4n; GR = GRn;
   }
@@ -1085,6 +1113,27 @@ k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
     c2[c] = S.out && (INT || (j + c >= 1 && j + c <= NY - 1));
   }
   const int i0 = S.i0;
+  // CPML items: the memory-variable adjoints g1..g4 of a row, loaded one row
+  // ahead where they can be nonzero (x-profile active on the row, y-profile
+  // active on the lane's columns) with predicated loads
+  const bool lx1 = c1[0] || c1[1], lx2 = c2[0] || c2[1];
+  const bool ly1 = !INT && ((c1[0] && Y.acti[0]) || (c1[1] && Y.acti[1]));
+  const bool ly2 = !INT && ((c2[0] && Y.acth[0]) || (c2[1] && Y.acth[1]));
+  auto gload = [&](int r, V2<T> (&g)[4]) {
+    if constexpr (!INT) {
+      const int rr = min(max(r, 1), NX) - 1;
+      const bool on = r < S.i_end, q1 = on && r <= NX - 1, q2 = on && r >= 2;
+      const bool x1 = q1 && (M.axh[rr] != T(0) || M.bxh[rr] != T(1));
+      const bool x3 = q2 && (M.axi[rr] != T(0) || M.bxi[rr] != T(1));
+      const int64_t o = S.off(r);
+      g[0] = ld2p(g1, o, x1 && lx1);
+      g[1] = ld2p(g2, o, q1 && ly1);
+      g[2] = ld2p(g3, o, x3 && lx2);
+      g[3] = ld2p(g4, o, q2 && ly2);
+    }
+  };
+  V2<T> gg[4] = {};
+  gload(i0, gg);
   // windows: D5 rows i-1..i+2, D7 rows i-2..i+1, lam / mu rows i, i+1
   V2<T> P0 = S.row(d5, i0 - 1), P1 = S.row(d5, i0), P2 = S.row(d5, i0 + 1), P3 = S.row(d5, i0 + 2);
   V2<T> Q0 = S.row(d7, i0 - 2), Q1 = S.row(d7, i0 - 1), Q2 = S.row(d7, i0), Q3 = S.row(d7, i0 + 1);
@@ -1102,6 +1151,8 @@ k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
     const V2<T> F6n = S.row(d6, rn), F8n = S.row(d8, rn);
     const V2<T> GAn = S.row(gxx, rn), GBn = S.row(gyy, rn), GCn = S.row(gxy, rn);
     const V2<T> EAn = S.row(e1p, rn), EBn = S.row(e2p, rn), ECn = S.row(e12p, rn);
+    V2<T> gn[4] = {};
+    gload(i + 1, gn);
     // row i across columns: D6 at j-1..j+3, D8 at j-2..j+2, mu at j..j+2
     T f6[5], f8[5], ur[3];
     f6[0] = shup(F6.v[1]);
@@ -1123,7 +1174,8 @@ k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
     const bool rx1 = !INT && r1 && (axh != T(0) || bxh != T(1));
     const bool rx3 = !INT && r2 && (axi != T(0) || bxi != T(1));
     T oxx[2], oyy[2], oxy[2], ol1[2], om1[2], od1[2], od2[2], om2[2], od3[2], od4[2];
-    bool k1[2], k2[2], k12[2];
+    T sg1[2], sg2[2], sg3[2], sg4[2];
+    bool k1[2], k2[2], k12[2], w1[2], w2[2], w3[2], w4[2];
 #pragma unroll
     for (int c = 0; c < 2; c++) {
       const bool b1 = r1 && c1[c], b2 = r2 && c2[c];
@@ -1132,6 +1184,8 @@ k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
       k2[c] = PART != 1 && b2;
       oxx[c] = oyy[c] = oxy[c] = ol1[c] = om1[c] = od1[c] = od2[c] = T(0);
       om2[c] = od3[c] = od4[c] = T(0);
+      sg1[c] = sg2[c] = sg3[c] = sg4[c] = T(0);
+      w1[c] = w2[c] = w3[c] = w4[c] = false;
       // gathers (zero outside the padded grid: those rows load as zeros and
       // the frame / padding columns of the temporaries are never written)
       if constexpr (PART != 2) {  // sxx / syy adjoints and the fw1 transpose
@@ -1150,10 +1204,12 @@ k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
       ol1[c] = T(0.5) * glam;
       om1[c] = glm;
       const bool u1 = k1[c] && rx1, u2 = !INT && k1[c] && Y.acti[c];
-      const T gm1 = u1 ? gE1 + g1[o + c] : gE1;
-      const T gm2 = u2 ? gE2 + g2[o + c] : gE2;
-      if (u1) g1[o + c] = bxh * gm1;
-      if (u2) g2[o + c] = Y.bi[c] * gm2;
+      const T gm1 = u1 ? gE1 + gg[0].v[c] : gE1;
+      const T gm2 = u2 ? gE2 + gg[1].v[c] : gE2;
+      sg1[c] = bxh * gm1;
+      sg2[c] = Y.bi[c] * gm2;
+      w1[c] = u1;
+      w2[c] = u2;
       od1[c] = hdiv<T>(gE1 + axh * gm1, M.hx24, M.rhx24);
       od2[c] = hdiv<T>(gE2 + (INT ? T(0) : Y.ai[c]) * gm2, M.hy24, M.rhy24);
       }
@@ -1165,26 +1221,36 @@ k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
       const T q = gsxy * mu2 * M.dt;
       om2[c] = gsxy * EC12.v[c] * M.dt * T(0.5);
       const bool u3 = k2[c] && rx3, u4 = !INT && k2[c] && Y.acth[c];
-      const T gm3 = u3 ? q + g3[o + c] : q;
-      const T gm4 = u4 ? q + g4[o + c] : q;
-      if (u3) g3[o + c] = bxi * gm3;
-      if (u4) g4[o + c] = Y.bh[c] * gm4;
+      const T gm3 = u3 ? q + gg[2].v[c] : q;
+      const T gm4 = u4 ? q + gg[3].v[c] : q;
+      sg3[c] = bxi * gm3;
+      sg4[c] = Y.bh[c] * gm4;
+      w3[c] = u3;
+      w4[c] = u4;
       od3[c] = hdiv<T>(q + axi * gm3, M.hx24, M.rhx24);
       od4[c] = hdiv<T>(q + (INT ? T(0) : Y.ah[c]) * gm4, M.hy24, M.rhy24);
       }
     }
-    if constexpr (PART != 2) {
-      st2<T>(gxx, o, oxx, k12[0], k12[1]);
-      st2<T>(gyy, o, oyy, k12[0], k12[1]);
+    if constexpr (!INT) {
+      st2p<T>(g1, o, sg1, w1[0], w1[1]);
+      st2p<T>(g2, o, sg2, w2[0], w2[1]);
+      st2p<T>(g3, o, sg3, w3[0], w3[1]);
+      st2p<T>(g4, o, sg4, w4[0], w4[1]);
     }
-    if constexpr (PART != 1) st2<T>(gxy, o, oxy, k12[0], k12[1]);
-    st2<T>(gl1, o, ol1, k1[0], k1[1]);
-    st2<T>(gm1p, o, om1, k1[0], k1[1]);
-    st2<T>(d1, o, od1, k1[0], k1[1]);
-    st2<T>(d2, o, od2, k1[0], k1[1]);
-    st2<T>(gm2p, o, om2, k2[0], k2[1]);
-    st2<T>(d3, o, od3, k2[0], k2[1]);
-    st2<T>(d4p, o, od4, k2[0], k2[1]);
+#pragma unroll
+    for (int q = 0; q < 4; q++) gg[q] = gn[q];
+    if constexpr (PART != 2) {
+      st2p<T>(gxx, o, oxx, k12[0], k12[1]);
+      st2p<T>(gyy, o, oyy, k12[0], k12[1]);
+    }
+    if constexpr (PART != 1) st2p<T>(gxy, o, oxy, k12[0], k12[1]);
+    st2p<T>(gl1, o, ol1, k1[0], k1[1]);
+    st2p<T>(gm1p, o, om1, k1[0], k1[1]);
+    st2p<T>(d1, o, od1, k1[0], k1[1]);
+    st2p<T>(d2, o, od2, k1[0], k1[1]);
+    st2p<T>(gm2p, o, om2, k2[0], k2[1]);
+    st2p<T>(d3, o, od3, k2[0], k2[1]);
+    st2p<T>(d4p, o, od4, k2[0], k2[1]);
     P0 = P1; P1 = P2; P2 = P3; P3 = P4;
     Q0 = Q1; Q1 = Q2; Q2 = Q3; Q3 = Q4;
     L0 = L1; L1 = L2; U0 = U1; U1 = U2;
@@ -1292,13 +1358,13 @@ k_el_adj3_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
       }
     }
     if constexpr (PART != 2) {
-      st2<T>(gvx, o, ovx, k3[0], k3[1]);
-      st2<T>(gvy, o, ovy, k4[0], k4[1]);
+      st2p<T>(gvx, o, ovx, k3[0], k3[1]);
+      st2p<T>(gvy, o, ovy, k4[0], k4[1]);
     }
     if constexpr (PART != 1) {
-      st2<A>(al, o, ol, cp[0], cp[1]);
-      st2<A>(am, o, om, cp[0], cp[1]);
-      st2<A>(ar, o, orr, cp[0], cp[1]);
+      st2p<A>(al, o, ol, cp[0], cp[1]);
+      st2p<A>(am, o, om, cp[0], cp[1]);
+      st2p<A>(ar, o, orr, cp[0], cp[1]);
     }
     P0 = P1; P1 = P2; P2 = P3; P3 = P4;
     Q0 = Q1; Q1 = Q2; Q2 = Q3; Q3 = Q4;
