@@ -3,12 +3,15 @@
 // whole-path multi-shot forward / misfit / gradient w.r.t. lambda, mu, rho.
 //
 // The reference composes one step from ~50 gather/scatter custom ops per step
-// (fw1..fw4 + add_source).  Here a step is two kernels (stresses: fw1+fw2;
-// velocities: fw3+fw4) plus a tiny source/receiver launch; the adjoint is three
-// gather-form kernels.  Per-cell work on the eight memory variables only runs
-// where the 1D CPML profile is active (a != 0 or b != 1); elsewhere the
-// forward memory stays exactly zero and its adjoint never reaches a gradient
-// (it is multiplied by a = 0), so skipping it changes no result.
+// (fw1..fw4 + add_source).  Here the single-step operators are two kernels
+// (stresses: fw1+fw2; velocities: fw3+fw4, one thread per cell) and their
+// transpose three; the plans step with one fused row-streaming kernel plus a
+// tiny source/receiver launch, and run the adjoint as three gather-form
+// row-streaming kernels.  In the plans, per-cell work on the eight memory
+// variables only runs where the 1D CPML profile is active (a != 0 or b != 1);
+// elsewhere the forward memory stays exactly zero and its adjoint never
+// reaches a gradient (it is multiplied by a = 0), so skipping it changes no
+// result.
 //
 // Cell indexing: (i, j) -> i*P + j + OFF (P = NY+2, OFF = 0 for the
 // single-step operators; pitched layout for the plans).
@@ -67,37 +70,19 @@ struct ElShot {
   int64_t fs;                   // elements per field
 };
 
-// The plans pass their shot table (one shot per blockIdx.z, FULL = false);
-// the single-step operators pass their one shot by value (FULL = true).  The
-// choice is made at compile time so no generic pointer or struct copy arises.
-template <typename T, bool FULL>
-__device__ __forceinline__ const ElShot<T>& shot_of(const ElShot<T>* shots,
-                                                    const ElShot<T>& one) {
-  if constexpr (FULL) {
-    return one;
-  } else {
-    return shots[blockIdx.z];
-  }
-}
-
 template <typename T>
 __device__ __forceinline__ T d4(T a0, T am1, T ap1, T am2, T h24) {
   return (T(27) * a0 - T(27) * am1 - ap1 + am2) / h24;
 }
 
-template <typename T>
-__device__ __forceinline__ bool active(const T* a, const T* b, int k) {
-  return a[k] != T(0) || b[k] != T(1);
-}
-
 #define ELIDX(ii, jj) ((int64_t)(ii) * M.P + (jj) + M.OFF)
 
-// Stress update (fw1: sxx, syy, m1, m2; fw2: sxy, m3, m4).
-// FULL: every cell written (out-of-place operator); else interior boxes only.
-template <typename T, bool FULL, bool STORE>
+// Stress update (fw1: sxx, syy, m1, m2; fw2: sxy, m3, m4) of the single-step
+// operator: every cell is written (out of place), the memory variables in full.
+template <typename T, bool STORE>
 __global__ void __launch_bounds__(BX* BY)
-k_el_stress(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
-  const ElShot<T>& sh = shot_of<T, FULL>(shots, one);
+k_el_stress(ElModel<T> M, ElShot<T> one, int store_slot) {
+  const ElShot<T>& sh = one;
   const int j = blockIdx.x * BX + threadIdx.x;
   const int i = blockIdx.y * BY + threadIdx.y;
   const int NX = M.NX, NY = M.NY;
@@ -105,7 +90,6 @@ k_el_stress(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot)
   const int64_t x = ELIDX(i, j);
   const bool b1 = i >= 1 && i <= NX - 1 && j >= 2 && j <= NY;
   const bool b2 = i >= 2 && i <= NX && j >= 1 && j <= NY - 1;
-  if (!FULL && !b1 && !b2) return;
   const T* vx = sh.fin[VX];
   const T* vy = sh.fin[VY];
   T* st = STORE ? sh.store + (int64_t)store_slot * NSTORE * sh.fs : nullptr;
@@ -117,15 +101,10 @@ k_el_stress(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot)
                         M.hx24);
     const T dvy = d4<T>(vy[x], vy[ELIDX(i, j - 1)], vy[ELIDX(i, j + 1)], vy[ELIDX(i, j - 2)],
                         M.hy24);
-    T m1 = T(0), m2 = T(0);
-    if (FULL || active(M.axh, M.bxh, i - 1)) {
-      m1 = M.bxh[i - 1] * sh.fin[M1 + 0][x] + M.axh[i - 1] * dvx;
-      sh.f[M1 + 0][x] = m1;
-    }
-    if (FULL || active(M.ayi, M.byi, j - 1)) {
-      m2 = M.byi[j - 1] * sh.fin[M1 + 1][x] + M.ayi[j - 1] * dvy;
-      sh.f[M1 + 1][x] = m2;
-    }
+    const T m1 = M.bxh[i - 1] * sh.fin[M1 + 0][x] + M.axh[i - 1] * dvx;
+    sh.f[M1 + 0][x] = m1;
+    const T m2 = M.byi[j - 1] * sh.fin[M1 + 1][x] + M.ayi[j - 1] * dvy;
+    sh.f[M1 + 1][x] = m2;
     const T e1 = dvx + m1, e2 = dvy + m2;
     sh.f[SXX][x] = sh.fin[SXX][x] + (lm * e1 + lam_ * e2) * M.dt;
     sh.f[SYY][x] = sh.fin[SYY][x] + (lm * e2 + lam_ * e1) * M.dt;
@@ -133,7 +112,7 @@ k_el_stress(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot)
       st[E1 * sh.fs + x] = e1;
       st[E2 * sh.fs + x] = e2;
     }
-  } else if (FULL) {
+  } else {
     sh.f[SXX][x] = sh.fin[SXX][x];
     sh.f[SYY][x] = sh.fin[SYY][x];
     sh.f[M1 + 0][x] = T(0);
@@ -145,19 +124,14 @@ k_el_stress(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot)
                           M.hx24);
     const T dvxdy = d4<T>(vx[ELIDX(i, j + 1)], vx[x], vx[ELIDX(i, j + 2)], vx[ELIDX(i, j - 1)],
                           M.hy24);
-    T m3 = T(0), m4 = T(0);
-    if (FULL || active(M.axi, M.bxi, i - 1)) {
-      m3 = M.bxi[i - 1] * sh.fin[M1 + 2][x] + M.axi[i - 1] * dvydx;
-      sh.f[M1 + 2][x] = m3;
-    }
-    if (FULL || active(M.ayh, M.byh, j - 1)) {
-      m4 = M.byh[j - 1] * sh.fin[M1 + 3][x] + M.ayh[j - 1] * dvxdy;
-      sh.f[M1 + 3][x] = m4;
-    }
+    const T m3 = M.bxi[i - 1] * sh.fin[M1 + 2][x] + M.axi[i - 1] * dvydx;
+    sh.f[M1 + 2][x] = m3;
+    const T m4 = M.byh[j - 1] * sh.fin[M1 + 3][x] + M.ayh[j - 1] * dvxdy;
+    sh.f[M1 + 3][x] = m4;
     const T e12 = (dvydx + m3) + (dvxdy + m4);
     sh.f[SXY][x] = sh.fin[SXY][x] + mu_ * e12 * M.dt;
     if (STORE) st[E12 * sh.fs + x] = e12;
-  } else if (FULL) {
+  } else {
     sh.f[SXY][x] = sh.fin[SXY][x];
     sh.f[M1 + 2][x] = T(0);
     sh.f[M1 + 3][x] = T(0);
@@ -166,10 +140,10 @@ k_el_stress(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot)
 
 // Velocity update (fw3: vx, m5, m6 from the new sxx, sxy; fw4: vy, m7, m8
 // from the new sxy, syy).
-template <typename T, bool FULL, bool STORE>
+template <typename T, bool STORE>
 __global__ void __launch_bounds__(BX* BY)
-k_el_velocity(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
-  const ElShot<T>& sh = shot_of<T, FULL>(shots, one);
+k_el_velocity(ElModel<T> M, ElShot<T> one, int store_slot) {
+  const ElShot<T>& sh = one;
   const int j = blockIdx.x * BX + threadIdx.x;
   const int i = blockIdx.y * BY + threadIdx.y;
   const int NX = M.NX, NY = M.NY;
@@ -177,7 +151,6 @@ k_el_velocity(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slo
   const int64_t x = ELIDX(i, j);
   const bool b3 = i >= 2 && i <= NX && j >= 2 && j <= NY;
   const bool b4 = i >= 1 && i <= NX - 1 && j >= 1 && j <= NY - 1;
-  if (!FULL && !b3 && !b4) return;
   const T* sxx = sh.f[SXX];
   const T* syy = sh.f[SYY];
   const T* sxy = sh.f[SXY];
@@ -187,19 +160,14 @@ k_el_velocity(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slo
                       M.hx24);
     const T b = d4<T>(sxy[x], sxy[ELIDX(i, j - 1)], sxy[ELIDX(i, j + 1)], sxy[ELIDX(i, j - 2)],
                       M.hy24);
-    T m5 = T(0), m6 = T(0);
-    if (FULL || active(M.axi, M.bxi, i - 1)) {
-      m5 = M.bxi[i - 1] * sh.fin[M1 + 4][x] + M.axi[i - 1] * a;
-      sh.f[M1 + 4][x] = m5;
-    }
-    if (FULL || active(M.ayi, M.byi, j - 1)) {
-      m6 = M.byi[j - 1] * sh.fin[M1 + 5][x] + M.ayi[j - 1] * b;
-      sh.f[M1 + 5][x] = m6;
-    }
+    const T m5 = M.bxi[i - 1] * sh.fin[M1 + 4][x] + M.axi[i - 1] * a;
+    sh.f[M1 + 4][x] = m5;
+    const T m6 = M.byi[j - 1] * sh.fin[M1 + 5][x] + M.ayi[j - 1] * b;
+    sh.f[M1 + 5][x] = m6;
     const T e3 = (a + m5) + (b + m6);
     sh.f[VX][x] = sh.fin[VX][x] + e3 * M.dt / M.rho[x];
     if (STORE) st[A3 * sh.fs + x] = e3;
-  } else if (FULL) {
+  } else {
     sh.f[VX][x] = sh.fin[VX][x];
     sh.f[M1 + 4][x] = T(0);
     sh.f[M1 + 5][x] = T(0);
@@ -211,19 +179,14 @@ k_el_velocity(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slo
                       M.hx24);
     const T b = d4<T>(syy[ELIDX(i, j + 1)], syy[x], syy[ELIDX(i, j + 2)], syy[ELIDX(i, j - 1)],
                       M.hy24);
-    T m7 = T(0), m8 = T(0);
-    if (FULL || active(M.axh, M.bxh, i - 1)) {
-      m7 = M.bxh[i - 1] * sh.fin[M1 + 6][x] + M.axh[i - 1] * a;
-      sh.f[M1 + 6][x] = m7;
-    }
-    if (FULL || active(M.ayh, M.byh, j - 1)) {
-      m8 = M.byh[j - 1] * sh.fin[M1 + 7][x] + M.ayh[j - 1] * b;
-      sh.f[M1 + 7][x] = m8;
-    }
+    const T m7 = M.bxh[i - 1] * sh.fin[M1 + 6][x] + M.axh[i - 1] * a;
+    sh.f[M1 + 6][x] = m7;
+    const T m8 = M.byh[j - 1] * sh.fin[M1 + 7][x] + M.ayh[j - 1] * b;
+    sh.f[M1 + 7][x] = m8;
     const T e4 = (a + m7) + (b + m8);
     sh.f[VY][x] = sh.fin[VY][x] + e4 * M.dt / rho_;
     if (STORE) st[A4 * sh.fs + x] = e4;
-  } else if (FULL) {
+  } else {
     sh.f[VY][x] = sh.fin[VY][x];
     sh.f[M1 + 6][x] = T(0);
     sh.f[M1 + 7][x] = T(0);
@@ -232,10 +195,10 @@ k_el_velocity(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slo
 
 // Adjoint 1 (velocity cells): transposes of fw3 and fw4.  Writes D5..D8 and
 // R4, updates the memory adjoints m5..m8 and grho (fw3 part) in place.
-template <typename T, bool FULL>
+template <typename T>
 __global__ void __launch_bounds__(BX* BY)
-k_el_adj1(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
-  const ElShot<T>& sh = shot_of<T, FULL>(shots, one);
+k_el_adj1(ElModel<T> M, ElShot<T> one, int store_slot) {
+  const ElShot<T>& sh = one;
   const int j = blockIdx.x * BX + threadIdx.x;
   const int i = blockIdx.y * BY + threadIdx.y;
   const int NX = M.NX, NY = M.NY;
@@ -248,18 +211,14 @@ k_el_adj1(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
     const T gv = sh.g[VX][x], r = M.rho[x];
     const T q = gv * M.dt / r;
     T gm5 = q, gm6 = q;
-    if (FULL || active(M.axi, M.bxi, i - 1)) {
-      gm5 += sh.g[M1 + 4][x];
-      sh.g[M1 + 4][x] = M.bxi[i - 1] * gm5;
-    }
-    if (FULL || active(M.ayi, M.byi, j - 1)) {
-      gm6 += sh.g[M1 + 5][x];
-      sh.g[M1 + 5][x] = M.byi[j - 1] * gm6;
-    }
+    gm5 += sh.g[M1 + 4][x];
+    sh.g[M1 + 4][x] = M.bxi[i - 1] * gm5;
+    gm6 += sh.g[M1 + 5][x];
+    sh.g[M1 + 5][x] = M.byi[j - 1] * gm6;
     sh.tmp[D5][x] = (q + M.axi[i - 1] * gm5) / M.hx24;
     sh.tmp[D6][x] = (q + M.ayi[j - 1] * gm6) / M.hy24;
     sh.grho[x] += (double)(-gv * st[A3 * sh.fs + x] * M.dt / (r * r));
-  } else if (FULL) {
+  } else {
     sh.g[M1 + 4][x] = T(0);
     sh.g[M1 + 5][x] = T(0);
   }
@@ -269,18 +228,14 @@ k_el_adj1(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
                               M.rho[ELIDX(i, j + 1)]);
     const T q = gv * M.dt / rho_;
     T gm7 = q, gm8 = q;
-    if (FULL || active(M.axh, M.bxh, i - 1)) {
-      gm7 += sh.g[M1 + 6][x];
-      sh.g[M1 + 6][x] = M.bxh[i - 1] * gm7;
-    }
-    if (FULL || active(M.ayh, M.byh, j - 1)) {
-      gm8 += sh.g[M1 + 7][x];
-      sh.g[M1 + 7][x] = M.byh[j - 1] * gm8;
-    }
+    gm7 += sh.g[M1 + 6][x];
+    sh.g[M1 + 6][x] = M.bxh[i - 1] * gm7;
+    gm8 += sh.g[M1 + 7][x];
+    sh.g[M1 + 7][x] = M.byh[j - 1] * gm8;
     sh.tmp[D7][x] = (q + M.axh[i - 1] * gm7) / M.hx24;
     sh.tmp[D8][x] = (q + M.ayh[j - 1] * gm8) / M.hy24;
     sh.tmp[R4][x] = -gv * st[A4 * sh.fs + x] * M.dt / (rho_ * rho_) * T(0.25);
-  } else if (FULL) {
+  } else {
     sh.g[M1 + 6][x] = T(0);
     sh.g[M1 + 7][x] = T(0);
   }
@@ -293,10 +248,10 @@ __device__ __forceinline__ T tld(const T* a, const ElModel<T>& M, int i, int j) 
 
 // Adjoint 2 (stress cells): gather D5..D8 into the stress adjoints, then the
 // transposes of fw1 and fw2 (D1..D4, memory adjoints m1..m4, lambda/mu parts).
-template <typename T, bool FULL>
+template <typename T>
 __global__ void __launch_bounds__(BX* BY)
-k_el_adj2(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
-  const ElShot<T>& sh = shot_of<T, FULL>(shots, one);
+k_el_adj2(ElModel<T> M, ElShot<T> one, int store_slot) {
+  const ElShot<T>& sh = one;
   const int j = blockIdx.x * BX + threadIdx.x;
   const int i = blockIdx.y * BY + threadIdx.y;
   const int NX = M.NX, NY = M.NY;
@@ -304,7 +259,6 @@ k_el_adj2(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
   const int64_t x = ELIDX(i, j);
   const bool b1 = i >= 1 && i <= NX - 1 && j >= 2 && j <= NY;
   const bool b2 = i >= 2 && i <= NX && j >= 1 && j <= NY - 1;
-  if (!FULL && !b1 && !b2) return;
   const T* const* D = sh.tmp;
   const T gsxx = sh.g[SXX][x] + T(27) * D[D5][x] - T(27) * tld(D[D5], M, i + 1, j) -
                  tld(D[D5], M, i - 1, j) + tld(D[D5], M, i + 2, j);
@@ -330,17 +284,13 @@ k_el_adj2(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
     sh.tmp[GL1][x] = T(0.5) * glam;
     sh.tmp[GM1][x] = glm;  // 0.5 * (2 glm) to each of mu[i], mu[i+1]
     T gm1 = gE1, gm2 = gE2;
-    if (FULL || active(M.axh, M.bxh, i - 1)) {
-      gm1 += sh.g[M1 + 0][x];
-      sh.g[M1 + 0][x] = M.bxh[i - 1] * gm1;
-    }
-    if (FULL || active(M.ayi, M.byi, j - 1)) {
-      gm2 += sh.g[M1 + 1][x];
-      sh.g[M1 + 1][x] = M.byi[j - 1] * gm2;
-    }
+    gm1 += sh.g[M1 + 0][x];
+    sh.g[M1 + 0][x] = M.bxh[i - 1] * gm1;
+    gm2 += sh.g[M1 + 1][x];
+    sh.g[M1 + 1][x] = M.byi[j - 1] * gm2;
     sh.tmp[D1][x] = (gE1 + M.axh[i - 1] * gm1) / M.hx24;
     sh.tmp[D2][x] = (gE2 + M.ayi[j - 1] * gm2) / M.hy24;
-  } else if (FULL) {
+  } else {
     sh.g[M1 + 0][x] = T(0);
     sh.g[M1 + 1][x] = T(0);
   }
@@ -349,17 +299,13 @@ k_el_adj2(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
     const T q = gsxy * mu_ * M.dt;
     sh.tmp[GM2][x] = gsxy * st[E12 * sh.fs + x] * M.dt * T(0.5);
     T gm3 = q, gm4 = q;
-    if (FULL || active(M.axi, M.bxi, i - 1)) {
-      gm3 += sh.g[M1 + 2][x];
-      sh.g[M1 + 2][x] = M.bxi[i - 1] * gm3;
-    }
-    if (FULL || active(M.ayh, M.byh, j - 1)) {
-      gm4 += sh.g[M1 + 3][x];
-      sh.g[M1 + 3][x] = M.byh[j - 1] * gm4;
-    }
+    gm3 += sh.g[M1 + 2][x];
+    sh.g[M1 + 2][x] = M.bxi[i - 1] * gm3;
+    gm4 += sh.g[M1 + 3][x];
+    sh.g[M1 + 3][x] = M.byh[j - 1] * gm4;
     sh.tmp[D3][x] = (q + M.axi[i - 1] * gm3) / M.hx24;
     sh.tmp[D4][x] = (q + M.ayh[j - 1] * gm4) / M.hy24;
-  } else if (FULL) {
+  } else {
     sh.g[M1 + 2][x] = T(0);
     sh.g[M1 + 3][x] = T(0);
   }
@@ -367,30 +313,24 @@ k_el_adj2(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one, int store_slot) {
 
 // Adjoint 3 (velocity cells + parameters): gather D1..D4 into the velocity
 // adjoints and the lambda / mu / rho partials into the FP64 accumulators.
-template <typename T, bool FULL>
+template <typename T>
 __global__ void __launch_bounds__(BX* BY)
-k_el_adj3(ElModel<T> M, const ElShot<T>* shots, ElShot<T> one) {
-  const ElShot<T>& sh = shot_of<T, FULL>(shots, one);
+k_el_adj3(ElModel<T> M, ElShot<T> one) {
+  const ElShot<T>& sh = one;
   const int j = blockIdx.x * BX + threadIdx.x;
   const int i = blockIdx.y * BY + threadIdx.y;
   const int NX = M.NX, NY = M.NY;
   if (i > NX + 1 || j > NY + 1) return;
   const int64_t x = ELIDX(i, j);
-  const bool b3 = i >= 2 && i <= NX && j >= 2 && j <= NY;
-  const bool b4 = i >= 1 && i <= NX - 1 && j >= 1 && j <= NY - 1;
   const T* const* D = sh.tmp;
-  if (FULL || b3) {
-    sh.g[VX][x] += T(27) * tld(D[D1], M, i - 1, j) - T(27) * D[D1][x] -
-                   tld(D[D1], M, i - 2, j) + tld(D[D1], M, i + 1, j) +
-                   T(27) * tld(D[D4], M, i, j - 1) - T(27) * D[D4][x] -
-                   tld(D[D4], M, i, j - 2) + tld(D[D4], M, i, j + 1);
-  }
-  if (FULL || b4) {
-    sh.g[VY][x] += T(27) * D[D2][x] - T(27) * tld(D[D2], M, i, j + 1) -
-                   tld(D[D2], M, i, j - 1) + tld(D[D2], M, i, j + 2) + T(27) * D[D3][x] -
-                   T(27) * tld(D[D3], M, i + 1, j) - tld(D[D3], M, i - 1, j) +
-                   tld(D[D3], M, i + 2, j);
-  }
+  sh.g[VX][x] += T(27) * tld(D[D1], M, i - 1, j) - T(27) * D[D1][x] -
+                 tld(D[D1], M, i - 2, j) + tld(D[D1], M, i + 1, j) +
+                 T(27) * tld(D[D4], M, i, j - 1) - T(27) * D[D4][x] -
+                 tld(D[D4], M, i, j - 2) + tld(D[D4], M, i, j + 1);
+  sh.g[VY][x] += T(27) * D[D2][x] - T(27) * tld(D[D2], M, i, j + 1) -
+                 tld(D[D2], M, i, j - 1) + tld(D[D2], M, i, j + 2) + T(27) * D[D3][x] -
+                 T(27) * tld(D[D3], M, i + 1, j) - tld(D[D3], M, i - 1, j) +
+                 tld(D[D3], M, i + 2, j);
   if (i >= 1 && i <= NX && j >= 1 && j <= NY) {
     sh.glam[x] += (double)(D[GL1][x] + tld(D[GL1], M, i - 1, j));
     sh.gmu[x] += (double)(D[GM1][x] + tld(D[GM1], M, i - 1, j) + D[GM2][x] +
@@ -442,22 +382,11 @@ struct alignas(2 * sizeof(T)) V2 {
   T v[2];
 };
 
-template <typename T>
-__device__ __forceinline__ V2<T> ld2(const T* p, int64_t o, bool on) {
-  V2<T> x;
-  if (on) {
-    x = *reinterpret_cast<const V2<T>*>(p + o);
-  } else {
-    x.v[0] = T(0);
-    x.v[1] = T(0);
-  }
-  return x;
-}
-
-// ld2 as one predicated vector load (zeros where `on` is false), so a mask
-// that differs between the lanes of a warp costs no branch.  The asm has no
-// memory clobber: the row kernels load each cell at most once, and a cell
-// they also write is written later from values that depend on the load.
+// Both cells of a lane as one predicated vector load (zeros where `on` is
+// false), so a mask that differs between the lanes of a warp costs no
+// branch.  The asm has no memory clobber: the row kernels load each cell at
+// most once, and a cell they also write is written later from values that
+// depend on the load.
 __device__ __forceinline__ V2<float> ld2p(const float* p, int64_t o, bool on) {
   float a = 0.f, b = 0.f;
   asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %3, 0;\n\t@q ld.global.v2.f32 {%0, %1}, [%2];\n\t}"
@@ -481,8 +410,7 @@ __device__ __forceinline__ V2<double> ld2p(const double* p, int64_t o, bool on) 
 
 // Store the two cells of a lane, each only where its flag is set, as three
 // independent guarded stores (a vector store when both cells are written,
-// else the single cell), which compile to predicated stores rather than
-// branches.
+// else the single cell).
 template <typename T>
 __device__ __forceinline__ void st2p(T* p, int64_t o, const T (&x)[2], bool k0, bool k1) {
   if (k0 && k1) {
@@ -650,7 +578,7 @@ k_el_step_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
     if constexpr (GC) {
       st2s<T>(p, o, x, k0, k1);
     } else {
-      st2p<T>(p, o, x, k0, k1);
+      st2p(p, o, x, k0, k1);
     }
   };
   auto ld = [&](const T* p, int r) {
@@ -1048,22 +976,22 @@ k_el_adj1_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
     }
     if constexpr (!INT) {
       if constexpr (PART != 2) {
-        st2p<T>(g5, o, sg5, w5[0], w5[1]);
-        st2p<T>(g6, o, sg6, w6[0], w6[1]);
+        st2p(g5, o, sg5, w5[0], w5[1]);
+        st2p(g6, o, sg6, w6[0], w6[1]);
       }
       if constexpr (PART != 1) {
-        st2p<T>(g7, o, sg7, w7[0], w7[1]);
-        st2p<T>(g8, o, sg8, w8[0], w8[1]);
+        st2p(g7, o, sg7, w7[0], w7[1]);
+        st2p(g8, o, sg8, w8[0], w8[1]);
       }
     }
 #pragma unroll
     for (int q = 0; q < 4; q++) gg[q] = gn[q];
-    st2p<T>(d5, o, o5, k3[0], k3[1]);
-    st2p<T>(d6, o, o6, k3[0], k3[1]);
-    st2p<A>(grp, o, gr, k3[0], k3[1]);
-    st2p<T>(d7, o, o7, k4[0], k4[1]);
-    st2p<T>(d8, o, o8, k4[0], k4[1]);
-    st2p<T>(r4p, o, o4, k4[0], k4[1]);
+    st2p(d5, o, o5, k3[0], k3[1]);
+    st2p(d6, o, o6, k3[0], k3[1]);
+    st2p(grp, o, gr, k3[0], k3[1]);
+    st2p(d7, o, o7, k4[0], k4[1]);
+    st2p(d8, o, o8, k4[0], k4[1]);
+    st2p(r4p, o, o4, k4[0], k4[1]);
     R0 = R1; R1 = R2;
     GX = GXn; GY = GYn; E3 = E3n; E4 = E4n; GR = GRn;
   }
@@ -1232,25 +1160,25 @@ k_el_adj2_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
       }
     }
     if constexpr (!INT) {
-      st2p<T>(g1, o, sg1, w1[0], w1[1]);
-      st2p<T>(g2, o, sg2, w2[0], w2[1]);
-      st2p<T>(g3, o, sg3, w3[0], w3[1]);
-      st2p<T>(g4, o, sg4, w4[0], w4[1]);
+      st2p(g1, o, sg1, w1[0], w1[1]);
+      st2p(g2, o, sg2, w2[0], w2[1]);
+      st2p(g3, o, sg3, w3[0], w3[1]);
+      st2p(g4, o, sg4, w4[0], w4[1]);
     }
 #pragma unroll
     for (int q = 0; q < 4; q++) gg[q] = gn[q];
     if constexpr (PART != 2) {
-      st2p<T>(gxx, o, oxx, k12[0], k12[1]);
-      st2p<T>(gyy, o, oyy, k12[0], k12[1]);
+      st2p(gxx, o, oxx, k12[0], k12[1]);
+      st2p(gyy, o, oyy, k12[0], k12[1]);
     }
-    if constexpr (PART != 1) st2p<T>(gxy, o, oxy, k12[0], k12[1]);
-    st2p<T>(gl1, o, ol1, k1[0], k1[1]);
-    st2p<T>(gm1p, o, om1, k1[0], k1[1]);
-    st2p<T>(d1, o, od1, k1[0], k1[1]);
-    st2p<T>(d2, o, od2, k1[0], k1[1]);
-    st2p<T>(gm2p, o, om2, k2[0], k2[1]);
-    st2p<T>(d3, o, od3, k2[0], k2[1]);
-    st2p<T>(d4p, o, od4, k2[0], k2[1]);
+    if constexpr (PART != 1) st2p(gxy, o, oxy, k12[0], k12[1]);
+    st2p(gl1, o, ol1, k1[0], k1[1]);
+    st2p(gm1p, o, om1, k1[0], k1[1]);
+    st2p(d1, o, od1, k1[0], k1[1]);
+    st2p(d2, o, od2, k1[0], k1[1]);
+    st2p(gm2p, o, om2, k2[0], k2[1]);
+    st2p(d3, o, od3, k2[0], k2[1]);
+    st2p(d4p, o, od4, k2[0], k2[1]);
     P0 = P1; P1 = P2; P2 = P3; P3 = P4;
     Q0 = Q1; Q1 = Q2; Q2 = Q3; Q3 = Q4;
     L0 = L1; L1 = L2; U0 = U1; U1 = U2;
@@ -1358,13 +1286,13 @@ k_el_adj3_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
       }
     }
     if constexpr (PART != 2) {
-      st2p<T>(gvx, o, ovx, k3[0], k3[1]);
-      st2p<T>(gvy, o, ovy, k4[0], k4[1]);
+      st2p(gvx, o, ovx, k3[0], k3[1]);
+      st2p(gvy, o, ovy, k4[0], k4[1]);
     }
     if constexpr (PART != 1) {
-      st2p<A>(al, o, ol, cp[0], cp[1]);
-      st2p<A>(am, o, om, cp[0], cp[1]);
-      st2p<A>(ar, o, orr, cp[0], cp[1]);
+      st2p(al, o, ol, cp[0], cp[1]);
+      st2p(am, o, om, cp[0], cp[1]);
+      st2p(ar, o, orr, cp[0], cp[1]);
     }
     P0 = P1; P1 = P2; P2 = P3; P3 = P4;
     Q0 = Q1; Q1 = Q2; Q2 = Q3; Q3 = Q4;
@@ -2468,9 +2396,9 @@ int ads_elastic_step_fwd_f64(const double* state_in, double* state_out, const do
   }
   one.fs = N;
   dim3 grd((unsigned)div_up(NY + 2, BX), (unsigned)div_up(NX + 2, BY), 1);
-  k_el_stress<double, true, false><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  k_el_stress<double, false><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
   ADS_LAUNCHED(1);
-  k_el_velocity<double, true, false><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  k_el_velocity<double, false><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
   ADS_LAUNCHED(1);
   if (nsrc > 0) {
     Fields5 f5{{state_out, state_out + N, state_out + 2 * N, state_out + 3 * N,
@@ -2528,17 +2456,17 @@ int ads_elastic_step_bwd_f64(const double* state_in, const double* grad_out, dou
   one.gmu = grad_mu;
   one.grho = grad_rho;
   dim3 grd((unsigned)div_up(NY + 2, BX), (unsigned)div_up(NX + 2, BY), 1);
-  k_el_stress<double, true, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  k_el_stress<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
   ADS_LAUNCHED(1);
-  k_el_velocity<double, true, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  k_el_velocity<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
   ADS_LAUNCHED(1);
   ADS_CUDA(cudaMemcpyAsync(grad_in, grad_out, sizeof(double) * NF * N,
                            cudaMemcpyDeviceToDevice, st));
-  k_el_adj1<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  k_el_adj1<double><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
   ADS_LAUNCHED(1);
-  k_el_adj2<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  k_el_adj2<double><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
   ADS_LAUNCHED(1);
-  k_el_adj3<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one);
+  k_el_adj3<double><<<grd, dim3(BX, BY), 0, st>>>(M, one);
   ADS_LAUNCHED(1);
   ADS_CUDA(cudaFreeAsync(scratch, st));
   return ADS_OK;
@@ -2643,17 +2571,17 @@ int ads_elastic_step_bwd_f64_noalloc(const double* state_in, const double* grad_
   one.gmu = grad_mu;
   one.grho = grad_rho;
   dim3 grd((unsigned)div_up(NY + 2, BX), (unsigned)div_up(NX + 2, BY), 1);
-  k_el_stress<double, true, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  k_el_stress<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
   ADS_LAUNCHED(1);
-  k_el_velocity<double, true, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  k_el_velocity<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
   ADS_LAUNCHED(1);
   ADS_CUDA(cudaMemcpyAsync(grad_in, grad_out, sizeof(double) * NF * N,
                            cudaMemcpyDeviceToDevice, st));
-  k_el_adj1<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  k_el_adj1<double><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
   ADS_LAUNCHED(1);
-  k_el_adj2<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one, 0);
+  k_el_adj2<double><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
   ADS_LAUNCHED(1);
-  k_el_adj3<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, nullptr, one);
+  k_el_adj3<double><<<grd, dim3(BX, BY), 0, st>>>(M, one);
   ADS_LAUNCHED(1);
   return ADS_OK;
 }
