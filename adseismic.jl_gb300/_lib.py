@@ -40,7 +40,9 @@ class AcousticConfig(C.Structure):
         ("use_pml", C.c_int32), ("precision", C.c_int32), ("variant", C.c_int32),
         ("use_graph", C.c_int32), ("ckpt_every", C.c_int64),
         ("rows_per_thread", C.c_int32), ("steps_per_block", C.c_int32),
-        ("block_rows", C.c_int32), ("autotune", C.c_int32), ("reserved", C.c_int32 * 4),
+        ("block_rows", C.c_int32), ("autotune", C.c_int32),
+        ("resident_segments", C.c_int32), ("resident_mem_pct", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 
@@ -98,6 +100,7 @@ _SIGS = {
     "ads_acoustic_plan_trace_count": [P],
     "ads_acoustic_plan_device_bytes": [P],
     "ads_acoustic_plan_launches": [P, I32],
+    "ads_acoustic_plan_resident_segments": [P],
     "ads_acoustic_plan_profile": [P, P, P, P, P],
     "ads_acoustic_plan_forward": [P, P, P, P],
     "ads_acoustic_plan_gradient": [P, P, P, P, P, P, P],
@@ -128,6 +131,7 @@ _RESTYPE = {
     "ads_acoustic_plan_trace_count": C.c_int64,
     "ads_acoustic_plan_device_bytes": C.c_int64,
     "ads_acoustic_plan_launches": C.c_int64,
+    "ads_acoustic_plan_resident_segments": C.c_int64,
     "ads_elastic_plan_trace_offset": C.c_int64,
     "ads_elastic_plan_trace_count": C.c_int64,
     "ads_elastic_plan_device_bytes": C.c_int64,

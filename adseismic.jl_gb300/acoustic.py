@@ -157,7 +157,7 @@ class AcousticPlan:
     def __init__(self, MX, MY, dx, dy, dt, shots, npml=12, Rcoef=0.001, vp_ref=1000.0,
                  use_pml=15, precision="f64", use_graph=True, ckpt_every=0,
                  rows_per_thread=0, steps_per_block=0, block_rows=0, autotune=False,
-                 stream=None):
+                 resident_segments=0, resident_mem_pct=0, stream=None):
         cfg = _lib.AcousticConfig()
         cfg.MX, cfg.MY, cfg.dx, cfg.dy, cfg.dt = MX, MY, dx, dy, dt
         cfg.npml, cfg.Rcoef, cfg.vp_ref, cfg.use_pml = npml, Rcoef, vp_ref, use_pml
@@ -169,6 +169,8 @@ class AcousticPlan:
         cfg.steps_per_block = steps_per_block
         cfg.block_rows = block_rows
         cfg.autotune = int(bool(autotune))
+        cfg.resident_segments = int(resident_segments)
+        cfg.resident_mem_pct = int(resident_mem_pct)
         self.MX, self.MY = MX, MY
         self.precision = precision
         self.dtype = torch.float64 if precision == "f64" else torch.float32
@@ -201,6 +203,7 @@ class AcousticPlan:
         self.device_bytes = L.ads_acoustic_plan_device_bytes(h)
         self.launches_forward = L.ads_acoustic_plan_launches(h, 0)
         self.launches_gradient = L.ads_acoustic_plan_launches(h, 1)
+        self.resident_segments = L.ads_acoustic_plan_resident_segments(h)
 
     def close(self):
         if getattr(self, "_h", None):

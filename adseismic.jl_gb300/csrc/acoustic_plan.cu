@@ -22,6 +22,7 @@
 //  * The forward and the reverse time loops are captured once as CUDA graphs
 //    and replayed each call.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -255,11 +256,11 @@ __device__ __forceinline__ bool interior_rows(bool tfree, const T* __restrict__ 
 
 // Each warp records the receivers in its own cells (its strip's columns, its
 // rows) after a forward step: its lanes wrote them, so a warp barrier suffices.
-template <typename T, int C, bool SEG>
+template <typename T, int C, bool NOREC>
 __device__ __forceinline__ void record_traces(const AcItem& it, const AcShot<T>& sh,
                                               const CellRef* __restrict__ rcvs, const T* out,
                                               int t, int lane, int i0, int i_end) {
-  if (SEG || it.rcv_e <= it.rcv_b) return;
+  if (NOREC || it.rcv_e <= it.rcv_b) return;
   __syncwarp();
   for (int e = it.rcv_b + lane; e < it.rcv_e; e += 32) {
     const CellRef r = rcvs[e];  // r.row: the receiver's row
@@ -267,9 +268,13 @@ __device__ __forceinline__ void record_traces(const AcItem& it, const AcShot<T>&
   }
 }
 
-// One forward step (variant W: phi/psi from the old field).  SEG=false: rings
-// of two (u_t written over u_{t-2}), optional checkpoint write; SEG=true:
-// segment store addressed by slot t - base.  Every warp takes one item (a
+// One forward step (variant W: phi/psi from the old field).  MODE 0 (the
+// forward loop): rings of two (u_t written over u_{t-2}), receiver traces,
+// optional checkpoint write.  MODE 1 (a segment's recompute in the reverse
+// sweep): the shot's store addressed by slot t - base, no traces.  MODE 2
+// (the forward loop over the resident segments): the store as in MODE 1,
+// with traces; those wavefields stay for the reverse sweep, which then needs
+// no recompute of those segments.  Every warp takes one item (a
 // 32*CF-column strip of rows of one shot); each thread owns CF adjacent
 // columns, walks down the rows with the next row's loads issued one iteration
 // ahead, and takes the j-neighbours of its edge cells from the neighbouring
@@ -277,11 +282,13 @@ __device__ __forceinline__ void record_traces(const AcItem& it, const AcShot<T>&
 // (sigma = tau = 0 on every row and column it reads, classified on the host)
 // and only the plain wave update is compiled, so the kernel needs few
 // registers and keeps many warps resident; INT = false: the general PML form.
-template <typename T, bool SEG, bool INT>
+template <typename T, int MODE, bool INT>
 __global__ void __launch_bounds__(Tile<T>::TPB, INT ? Tile<T>::MINB_FI : Tile<T>::MINB_F)
 k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
          const CellRef* __restrict__ srcs, const CellRef* __restrict__ rcvs, AcConst<T> K,
          int t, int base, int ckpt_slot, int ri) {
+  constexpr bool SEG = MODE != 0;  // u from the shot's store, not the rings
+  constexpr bool NOREC = MODE == 1;  // no receiver traces
   constexpr int C = Tile<T>::CF;
   using V = Vec<T, C>;
   const AcItem it = items[blockIdx.x];
@@ -395,7 +402,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       cq[PF - 1] = cn;
       hq[PF - 1] = hn;
     }
-    if constexpr (!INT) record_traces<T, C, SEG>(it, sh, rcvs, out, t, lane, i0, i_end);
+    if constexpr (!INT) record_traces<T, C, NOREC>(it, sh, rcvs, out, t, lane, i0, i_end);
   } else {
   bool n0 = nz(i0);
   V wm = ldvp<T, C>(w, off(i0 - 1), jld), w0 = ldvp<T, C>(w, off(i0), jld),
@@ -478,7 +485,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     hq = hqn;
     n0 = n1;
   }
-  record_traces<T, C, SEG>(it, sh, rcvs, out, t, lane, i0, i_end);
+  record_traces<T, C, NOREC>(it, sh, rcvs, out, t, lane, i0, i_end);
   }
 }
 
@@ -501,6 +508,24 @@ k_ac_restore(const AcShot<T>* __restrict__ shots, int slot, int a, int pset) {
       pr[row] = ck[2 * fs + row];
       qr[row] = ck[3 * fs + row];
     }
+}
+
+// Copy u_{a-2} and u_{a-1} from the rings into the store slots a-2-base and
+// a-1-base of every active shot: the start of the resident segments.
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_ac_seed(const AcShot<T>* __restrict__ shots, int a, int base) {
+  const AcShot<T>& sh = shots[blockIdx.y];
+  const int64_t fs = sh.fs;
+  const T* __restrict__ u2 = sh.u + (int64_t)((a - 2) & 1) * fs;
+  const T* __restrict__ u1 = sh.u + (int64_t)((a - 1) & 1) * fs;
+  T* __restrict__ d2 = sh.seg + (int64_t)(a - 2 - base) * fs;
+  T* __restrict__ d1 = sh.seg + (int64_t)(a - 1 - base) * fs;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < fs;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    d2[e] = u2[e];
+    d1[e] = u1[e];
+  }
 }
 
 // One cell's j-direction adjoint terms: YP (to its j+1 neighbour), YM (to its
@@ -1179,6 +1204,7 @@ struct AcPlanBase {
   int64_t src_total = 0;
   int64_t bytes = 0;
   int64_t launches_fwd = 0, launches_grad = 0;
+  int64_t resident = 0;  // checkpoint segments kept resident (no recompute)
 };
 
 namespace {
@@ -1188,6 +1214,11 @@ struct AcPlan final : AcPlanBase {
   ads_acoustic_config cfg{};
   int nshots = 0;
   int K = 0;          // checkpoint spacing
+  // Resident segments: segments res_seg .. nseg_max-1 keep the forward
+  // wavefields of their steps in the shots' stores (slot t - res_base), so
+  // the reverse sweep neither restores nor recomputes them.  res_seg ==
+  // nseg_max: none.
+  int res_seg = 0, res_base = 0;
   int ri = 8;         // rows per thread
   int nseg_max = 0;
   std::vector<int> order;         // shot order (record length descending)
@@ -1224,7 +1255,7 @@ struct AcPlan final : AcPlanBase {
   int upload_tiles(const TileList& L, DevTiles& D, cudaStream_t st);
   int autotune(cudaStream_t st, int64_t pitch, size_t cap_items);
   // step launches over the first na sorted shots (interior and PML kernels)
-  int launch_fwd(cudaStream_t st, bool seg, int na, int t, int base, int ck);
+  int launch_fwd(cudaStream_t st, int mode, int na, int t, int base, int ck);
   int launch_adj(cudaStream_t st, int na, int k, int base);
   std::vector<int> rcv_b_host, rcv_e_host;
   AcConst<T> kc{};
@@ -1448,7 +1479,6 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   for (int s = 0; s < ns; s++) {
     const ads_acoustic_shot& h = shots[order[s]];
     const int64_t fs = (h.nx + 2) * pitch * (int64_t)sizeof(T);
-    offs[s].seg = L.take((size_t)(K + 2) * fs);
     offs[s].ckpt = L.take((size_t)nseg[s] * 4 * fs);
     offs[s].c = L.take(fs);
     offs[s].sx = L.take(sizeof(T) * (h.nx + 2));
@@ -1590,8 +1620,46 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   const size_t shot_rcvs_off = L.take(sizeof(CellRef) * std::max<size_t>(shot_rcvs.size(), 1));
   const size_t rcvb_off = L.take(sizeof(int) * ns);
   const size_t rcve_off = L.take(sizeof(int) * ns);
+  // ---- the shots' stores: K + 2 slots for a segment's recompute, then the
+  // slots of the resident segments (the last ones whose wavefields fit in
+  // the allowed share of the free device memory)
+  res_seg = nseg_max;
+  {
+    std::vector<size_t> fsb(ns);
+    size_t base_bytes = L.used;
+    for (int q = 0; q < ns; q++) {
+      fsb[q] = (size_t)(shots[order[q]].nx + 2) * pitch * sizeof(T);
+      base_bytes += (K + 2) * fsb[q] + 256;
+    }
+    if (KB == 1 && c.resident_segments >= 0 && nseg_max > 0) {
+      size_t fr = 0, tot = 0, avail = 0;
+      if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && fr > base_bytes) {
+        const int pct = c.resident_mem_pct > 0 ? std::min<int>(c.resident_mem_pct, 95) : 50;
+        avail = (size_t)((double)(fr - base_bytes) * pct / 100.0);
+      } else {
+        cudaGetLastError();
+      }
+      const int lo = c.resident_segments > 0 ? std::max(0, nseg_max - c.resident_segments) : 0;
+      for (int sg = nseg_max - 1; sg >= lo; sg--) {
+        const int a = 2 + sg * K;
+        size_t b = 0;
+        for (int q = 0; q < ns; q++)
+          if (nstep[q] >= a) b += (size_t)(nstep[q] - (a - 2) + 1) * fsb[q] + 256;
+        if (b > avail) break;
+        res_seg = sg;
+      }
+    }
+    res_base = res_seg * K - (K + 2);  // slot K + 2 holds u_{a-2} of segment res_seg
+    for (int q = 0; q < ns; q++) {
+      const int a = 2 + res_seg * K;
+      const size_t slots =
+          (size_t)(K + 2) + (res_seg < nseg_max && nstep[q] >= a ? nstep[q] - (a - 2) + 1 : 0);
+      offs[q].seg = L.take(slots * fsb[q]);
+    }
+  }
   pool_bytes = L.used;
   bytes = (int64_t)pool_bytes;
+  resident = nseg_max - res_seg;
   {
     cudaError_t e = cudaMalloc(&pool, pool_bytes);
     if (e != cudaSuccess) {
@@ -1724,7 +1792,9 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   cells_prefix.resize(ns);
   for (int s = 0; s < ns; s++)
     cells_prefix[s] = (s ? cells_prefix[s - 1] : 0) + (int64_t)shots[order[s]].nx * MY;
-  seg_timed = nseg_max >= 2 ? nseg_max - 2 : 0;
+  // profile() times the recompute and adjoint of the last recomputed segment
+  // (or, when every segment is resident, an adjoint-only segment)
+  seg_timed = res_seg >= 1 ? res_seg - 1 : (nseg_max >= 2 ? nseg_max - 2 : 0);
   for (auto& e : ev) ADS_CUDA(cudaEventCreate(&e));
   // ---- launch counts
   {
@@ -1872,7 +1942,7 @@ int AcPlan<T>::upload_tiles(const TileList& L, DevTiles& D, cudaStream_t st) {
 // One forward step of the first na sorted shots: the interior-item kernel and
 // the PML-item kernel (each launched only when it has items).
 template <typename T>
-int AcPlan<T>::launch_fwd(cudaStream_t st, bool seg, int na, int t, int base, int ck) {
+int AcPlan<T>::launch_fwd(cudaStream_t st, int mode, int na, int t, int base, int ck) {
   constexpr int TPB = Tile<T>::TPB;
   const int ni = tf.in_upto(na), np = tf.pm_upto(na);
   const AcItem* pm = tf.items + tf.pm_off;
@@ -1883,24 +1953,25 @@ int AcPlan<T>::launch_fwd(cudaStream_t st, bool seg, int na, int t, int base, in
     ADS_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
     sp = side;
   }
+#define ADS_FWD(M, IN, items_, n_, s_, rows_)                                            \
+  k_ac_fwd<T, M, IN><<<n_, TPB, 0, s_>>>(items_, d_shots, tf.srcs, tf.rcvs, kc, t, base, ck, \
+                                         rows_)
+#define ADS_FWD_MODE(IN, items_, n_, s_, rows_) \
+  do {                                          \
+    if (mode == 1) ADS_FWD(1, IN, items_, n_, s_, rows_);      \
+    else if (mode == 2) ADS_FWD(2, IN, items_, n_, s_, rows_); \
+    else ADS_FWD(0, IN, items_, n_, s_, rows_);                \
+  } while (0)
   if (ni > 0) {
-    if (seg)
-      k_ac_fwd<T, true, true><<<ni, TPB, 0, st>>>(tf.items, d_shots, tf.srcs, tf.rcvs, kc, t,
-                                                   base, ck, ri_f);
-    else
-      k_ac_fwd<T, false, true><<<ni, TPB, 0, st>>>(tf.items, d_shots, tf.srcs, tf.rcvs, kc, t,
-                                                    base, ck, ri_f);
+    ADS_FWD_MODE(true, tf.items, ni, st, ri_f);
     ADS_LAUNCHED(1);
   }
   if (np > 0) {
-    if (seg)
-      k_ac_fwd<T, true, false><<<np, TPB, 0, sp>>>(pm, d_shots, tf.srcs, tf.rcvs, kc, t, base,
-                                                    ck, ri_pf > 0 ? ri_pf : ri_f);
-    else
-      k_ac_fwd<T, false, false><<<np, TPB, 0, sp>>>(pm, d_shots, tf.srcs, tf.rcvs, kc, t, base,
-                                                     ck, ri_pf > 0 ? ri_pf : ri_f);
+    ADS_FWD_MODE(false, pm, np, sp, ri_pf > 0 ? ri_pf : ri_f);
     ADS_LAUNCHED(1);
   }
+#undef ADS_FWD_MODE
+#undef ADS_FWD
   if (fork) {
     ADS_CUDA(cudaEventRecord(ev_join, side));
     ADS_CUDA(cudaStreamWaitEvent(st, ev_join, 0));
@@ -2103,23 +2174,31 @@ int AcPlan<T>::issue_forward(cudaStream_t st, int64_t* count) {
     ADS_CUDA(cudaMemsetAsync(pool + zero_fwd_off, 0, zero_fwd_len, st));
     if (timing_run) ADS_CUDA(cudaEventRecord(ev[0], st));
   }
+  const int a_res = res_seg < nseg_max ? 2 + res_seg * K : INT_MAX;  // first resident step
   int t0 = 2, blk = 0;
   while (t0 <= nstep[0]) {
     const int bound = 1 + K * (int)div_up(t0 - 1, K);  // next checkpoint time >= t0
     const int NS = KB > 1 ? std::min({KB, bound - t0 + 1, nstep[0] - t0 + 1}) : 1;
     const int t1 = t0 + NS - 1;
     const int na = shots_with_nstep_ge(t0);
-    // checkpoint s >= 1 holds the state before step a_s = 2 + s K, i.e. after t = 1 + s K
-    const int ck = ((t1 - 1) % K == 0) ? (t1 - 1) / K : 0;
+    // checkpoint s >= 1 holds the state before step a_s = 2 + s K, i.e. after
+    // t = 1 + s K; resident segments need none
+    int ck = ((t1 - 1) % K == 0) ? (t1 - 1) / K : 0;
+    if (ck >= res_seg) ck = 0;
+    const bool res = t0 >= a_res;
     if (count) {
-      const int nl = KB > 1 ? 1 : tf.launches(na);
+      const int nl = (KB > 1 ? 1 : tf.launches(na)) + (t0 == a_res ? 1 : 0);
       *count += nl;
       tcount[0] += nl;
       for (int t = t0; t <= t1; t++) tcount[1] += (double)cells_upto(shots_with_nstep_ge(t));
     } else if (KB > 1) {
       if (int e = launch_tb(st, false, tb_items_upto(na), t0, NS, 0, blk & 1, ck)) return e;
     } else {
-      if (int e = launch_fwd(st, false, na, t0, 0, ck)) return e;
+      if (t0 == a_res) {  // u_{a-2}, u_{a-1} into the resident slots
+        k_ac_seed<T><<<dim3(kRowBlocks, na), 256, 0, st>>>(d_shots, a_res, res_base);
+        ADS_LAUNCHED(1);
+      }
+      if (int e = launch_fwd(st, res ? 2 : 0, na, t0, res ? res_base : 0, ck)) return e;
     }
     t0 = t1 + 1;
     blk++;
@@ -2145,15 +2224,19 @@ int AcPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     const int na = shots_with_nstep_ge(a);
     if (na == 0) continue;
     const int b_max = std::min(a + K - 1, nstep[0]);
-    if (!count) {
-      k_ac_restore<T><<<dim3(kRowBlocks, na), 256, 0, st>>>(d_shots, s, a, KB > 1 ? 0 : -1);
-      ADS_LAUNCHED(1);
+    const bool res = s >= res_seg;  // resident: the store already holds the segment
+    const int base = res ? res_base : a - 2;
+    if (!res) {
+      if (!count) {
+        k_ac_restore<T><<<dim3(kRowBlocks, na), 256, 0, st>>>(d_shots, s, a, KB > 1 ? 0 : -1);
+        ADS_LAUNCHED(1);
+      }
+      n++;
     }
-    n++;
     const bool timed = s == seg_timed;
     if (timed && timing_run) ADS_CUDA(cudaEventRecord(ev[2], st));
     if (timed && count) tcount[2] = tcount[3] = tcount[4] = tcount[5] = 0;
-    for (int t0 = a, blk = 0; t0 <= b_max - 1; blk++) {
+    for (int t0 = a, blk = 0; !res && t0 <= b_max - 1; blk++) {
       // active while t < b_shot = min(a+K-1, nstep), i.e. nstep >= t+1
       const int NS = KB > 1 ? std::min(KB, b_max - t0) : 1;
       const int nt = shots_with_nstep_ge(t0 + 1);
@@ -2166,7 +2249,7 @@ int AcPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
         if (KB > 1) {
           if (int e = launch_tb(st, true, tb_items_upto(nt), t0, NS, a - 2, blk & 1, 0)) return e;
         } else {
-          if (int e = launch_fwd(st, true, nt, t0, a - 2, 0)) return e;
+          if (int e = launch_fwd(st, 1, nt, t0, a - 2, 0)) return e;
         }
       }
       n += nl;
@@ -2183,7 +2266,7 @@ int AcPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
         tcount[5] += (double)cells_upto(nk);
       }
       if (!count) {
-        if (int e = launch_adj(st, nk, k, a - 2)) return e;
+        if (int e = launch_adj(st, nk, k, base)) return e;
       }
       n += ta.launches(nk);
     }
@@ -2340,6 +2423,10 @@ int64_t ads_acoustic_plan_device_bytes(const ads_acoustic_plan* plan) {
 int64_t ads_acoustic_plan_launches(const ads_acoustic_plan* plan, int gradient) {
   if (!plan) return -1;
   return gradient ? plan->impl->launches_grad : plan->impl->launches_fwd;
+}
+
+int64_t ads_acoustic_plan_resident_segments(const ads_acoustic_plan* plan) {
+  return plan ? plan->impl->resident : -1;
 }
 
 int ads_acoustic_plan_profile(ads_acoustic_plan* plan, const double* vp, const void* observed,

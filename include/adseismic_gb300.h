@@ -242,7 +242,15 @@ typedef struct ads_acoustic_config {
   int32_t block_rows;      /* tile height of the time-blocked forward; 0 = automatic */
   int32_t autotune;        /* 1: time candidate tile heights of the forward and adjoint
                               kernels at plan creation and keep the fastest */
-  int32_t reserved[4];
+  int32_t resident_segments; /* checkpoint segments (the last ones) whose forward
+                                wavefields stay in device memory for the reverse sweep,
+                                which then neither restores nor recomputes them:
+                                -1 = none, 0 = as many as fit (see resident_mem_pct),
+                                N > 0 = at most N.  Results are identical either way. */
+  int32_t resident_mem_pct;  /* share of the device memory free at plan creation (after
+                                the plan's other buffers) those wavefields may use, in
+                                percent (1..95); 0 = 50 */
+  int32_t reserved[2];
 } ads_acoustic_config;
 
 typedef struct ads_acoustic_shot {
@@ -280,6 +288,8 @@ int64_t ads_acoustic_plan_trace_count(const ads_acoustic_plan* plan);
 int64_t ads_acoustic_plan_device_bytes(const ads_acoustic_plan* plan);
 /* Kernel launches one forward / one gradient call issues. */
 int64_t ads_acoustic_plan_launches(const ads_acoustic_plan* plan, int gradient);
+/* Checkpoint segments kept resident (see resident_segments); -1 for a null plan. */
+int64_t ads_acoustic_plan_resident_segments(const ads_acoustic_plan* plan);
 /* Kernel timing: runs one gradient with direct launches (no graphs) and CUDA
  * events recorded around (0) the forward loop (k_ac_fwd launches only), (1)
  * one full checkpoint segment's recompute launches and (2) the same segment's

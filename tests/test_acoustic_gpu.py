@@ -101,13 +101,20 @@ def loop_case(g):
 
 @pytest.mark.parametrize("use_graph", [True, False])
 @pytest.mark.parametrize("ckpt", [0, 1, 7, 79])
-def test_plan_fp64_matches_reference_golden(ads, cuda, use_graph, ckpt):
+@pytest.mark.parametrize("resident", [-1, 0, 2])
+def test_plan_fp64_matches_reference_golden(ads, cuda, use_graph, ckpt, resident):
+    """resident: checkpoint segments whose wavefields stay on the device
+    (-1 none: every segment recomputed; 0 as many as fit: all of them here;
+    2 the last two)."""
     g = golden("acoustic_loop.npz")
     NX, NY, Tn, shot = loop_case(g)
     h, dt = float(g["h"]), float(g["dt"])
     plan = ads.AcousticPlan(NX, NY, h, h, dt, [shot], npml=int(g["npml"]),
                             vp_ref=float(g["vp_ref"]), precision="f64", use_graph=use_graph,
-                            ckpt_every=ckpt)
+                            ckpt_every=ckpt, resident_segments=resident)
+    nseg = -(-(Tn - 1) // (ckpt if ckpt else 100 if Tn >= 400 else
+                         max(1, int(np.ceil(np.sqrt(Tn) * 2)))))
+    assert plan.resident_segments == {-1: 0, 0: nseg, 2: min(2, nseg)}[resident]
     vp = T(g["vp"].reshape(NX + 2, NY + 2), cuda)
     tr = plan.forward(vp)
     assert rel(tr.cpu().numpy(), g["rcvv"].reshape(-1)) <= TOL64
@@ -180,7 +187,8 @@ def oracle_multishot(orc, MX, MY, shots, vp, h, dt, npml, vp_ref, obs=None):
 
 @pytest.mark.parametrize("precision", ["f64", "f32"])
 @pytest.mark.parametrize("rows", [0, 1, 3])
-def test_plan_uneven_multishot_vs_oracle(ads, orc, cuda, precision, rows):
+@pytest.mark.parametrize("resident", [-1, 0, 3])
+def test_plan_uneven_multishot_vs_oracle(ads, orc, cuda, precision, rows, resident):
     MX, MY, shots, vp = uneven_case(21)
     h, dt, npml, vref = 10.0, 1e-3, 5, 1500.0
     ref_tr = oracle_multishot(orc, MX, MY, shots, vp, h, dt, npml, vref)
@@ -188,7 +196,8 @@ def test_plan_uneven_multishot_vs_oracle(ads, orc, cuda, precision, rows):
     obs = [t * 0.95 + 1e-3 * rng.standard_normal(t.shape) for t in ref_tr]
     ref_loss, ref_grad = oracle_multishot(orc, MX, MY, shots, vp, h, dt, npml, vref, obs)
     plan = ads.AcousticPlan(MX, MY, h, h, dt, shots, npml=npml, vp_ref=vref,
-                            precision=precision, ckpt_every=13, rows_per_thread=rows)
+                            precision=precision, ckpt_every=13, rows_per_thread=rows,
+                            resident_segments=resident)
     dtype = plan.dtype
     tr = plan.forward(T(vp, cuda))
     got = plan.split_traces(tr)
@@ -300,7 +309,8 @@ def test_dropin_operator_chain_matches_reference_golden(ads, cuda):
 
 
 @pytest.mark.parametrize("precision,tol", [("f64", TOL64), ("f32", 1e-4)])
-def test_source_time_gradient_vs_oracle(ads, orc, cuda, precision, tol):
+@pytest.mark.parametrize("resident", [-1, 0])
+def test_source_time_gradient_vs_oracle(ads, orc, cuda, precision, tol, resident):
     """d loss / d srcv from the plan's adjoint (two shots of different length
     and source count, one source on a receiver's cell) against the oracle."""
     rng = np.random.default_rng(11)
@@ -323,7 +333,7 @@ def test_source_time_gradient_vs_oracle(ads, orc, cuda, precision, tol):
         obs.append(T(o.reshape(-1), cuda))
         want.append(gs)
     plan = ads.AcousticPlan(NX, NY, h, h, dt, shots, npml=npml, vp_ref=2000.0,
-                            precision=precision, ckpt_every=16)
+                            precision=precision, ckpt_every=16, resident_segments=resident)
     out = plan.gradient(T(vp.reshape(NX + 2, NY + 2), cuda), plan.pack(obs),
                         want_source_grad=True)
     torch.cuda.synchronize()
