@@ -62,7 +62,9 @@ class ElasticConfig(C.Structure):
         ("npml", C.c_int64), ("npower", C.c_double), ("k_max", C.c_double),
         ("alpha_max", C.c_double), ("vp_ref", C.c_double), ("Rcoef", C.c_double),
         ("use_pml", C.c_int32), ("precision", C.c_int32), ("use_graph", C.c_int32),
-        ("rows_per_warp", C.c_int32), ("ckpt_every", C.c_int64), ("reserved", C.c_int32 * 8),
+        ("rows_per_warp", C.c_int32), ("ckpt_every", C.c_int64),
+        ("resident_segments", C.c_int32), ("resident_mem_pct", C.c_int32),
+        ("reserved", C.c_int32 * 6),
     ]
 
 
@@ -114,6 +116,7 @@ _SIGS = {
     "ads_elastic_plan_trace_count": [P],
     "ads_elastic_plan_device_bytes": [P],
     "ads_elastic_plan_launches": [P, I32],
+    "ads_elastic_plan_resident_segments": [P],
     "ads_elastic_plan_forward": [P, P, P, P, P, P],
     "ads_elastic_plan_gradient": [P, P, P, P, P, P, P, P, P, P, P],
     "ads_elastic_plan_profile": [P, P, P, P, P, P],
@@ -136,6 +139,7 @@ _RESTYPE = {
     "ads_elastic_plan_trace_count": C.c_int64,
     "ads_elastic_plan_device_bytes": C.c_int64,
     "ads_elastic_plan_launches": C.c_int64,
+    "ads_elastic_plan_resident_segments": C.c_int64,
 }
 EXPORTED = sorted(_SIGS)
 

@@ -152,7 +152,11 @@ class AcousticPlan:
     """A persistent multi-shot plan (forward traces, misfit, gradient).
 
     shots: list of dicts with keys x0, nx, nstep, srci, srcj, srcv, rcvi, rcvj
-    (window-local, 1-based indices).  The model vp is (MX+2, MY+2)."""
+    (window-local, 1-based indices).  The model vp is (MX+2, MY+2).
+    resident_segments / resident_mem_pct: how many of the last checkpoint
+    segments keep their forward wavefields on the device instead of being
+    recomputed in the reverse sweep (-1 none, 0 as many as fit in
+    resident_mem_pct percent, default 50, of the free device memory)."""
 
     def __init__(self, MX, MY, dx, dy, dt, shots, npml=12, Rcoef=0.001, vp_ref=1000.0,
                  use_pml=15, precision="f64", use_graph=True, ckpt_every=0,

@@ -1591,6 +1591,7 @@ struct ElPlanBase {
                        cudaStream_t st) = 0;
   std::vector<int64_t> trace_off;
   int64_t trace_total = 0, bytes = 0, launches_fwd = 0, launches_grad = 0;
+  int64_t resident = 0;  // checkpoint segments kept resident (no recompute)
 };
 
 namespace {
@@ -1600,6 +1601,12 @@ struct ElPlan final : ElPlanBase {
   ads_elastic_config cfg{};
   int nshots = 0, K = 0, nseg = 0, NX = 0, NY = 0, NSTEP = 0;
   int ncolw = 0, rows_w = 0, nwt = 0;  // warp strips of the row-streaming step kernels
+  // Resident segments res_seg .. nseg-1: the forward loop stores their steps'
+  // strains / accelerations (store slot K + n - a_res, a_res = 1 + res_seg K)
+  // and the reverse sweep neither restores nor recomputes them.  res_seg ==
+  // nseg: none.
+  int res_seg = 0;
+  int a_res() const { return 1 + res_seg * K; }
   // warp items (strip, row tile) of CPML-free tiles and of the rest; the two
   // launches of a step kernel run concurrently (disjoint cells)
   int* d_wl = nullptr;  // interior items, then the CPML items at nw_in
@@ -1784,7 +1791,6 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   for (int s = 0; s < ns; s++) {
     const ads_elastic_shot& h = shots[s];
     o[s].tmp = take(NTMP * F);
-    o[s].store = take((size_t)K * NSTORE * F);
     o[s].ckpt = take((size_t)nseg * NF * F);
     o[s].srcv = take(sizeof(T) * std::max<int64_t>(NSTEP * h.nsrc, 1));
     o[s].scell = take(sizeof(int64_t) * std::max<int64_t>(h.nsrc, 1));
@@ -1803,7 +1809,33 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   const size_t shots_o = take(sizeof(ElShot<T>) * ns);
   const size_t wl_o = take(sizeof(int) * std::max(nwt, 1));
   const size_t wlf_o = take(sizeof(int) * std::max(nwtf_max, 1));
+  // ---- the shots' stores: K slots for a segment's recompute, then one slot
+  // per step of the resident segments (the last ones that fit in the allowed
+  // share of the free device memory)
+  res_seg = nseg;
+  {
+    const size_t slot = (size_t)NSTORE * F;
+    const size_t base_bytes = used + (size_t)ns * ((size_t)K * slot + 256);
+    if (c.resident_segments >= 0) {
+      size_t fr = 0, tot = 0, avail = 0;
+      if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && fr > base_bytes) {
+        const int pct = c.resident_mem_pct > 0 ? std::min<int>(c.resident_mem_pct, 95) : 50;
+        avail = (size_t)((double)(fr - base_bytes) * pct / 100.0);
+      } else {
+        cudaGetLastError();
+      }
+      const int lo = c.resident_segments > 0 ? std::max(0, nseg - (int)c.resident_segments) : 0;
+      for (int sg = nseg - 1; sg >= lo; sg--) {
+        const size_t b = (size_t)ns * ((size_t)(NSTEP - sg * K) * slot + 256);
+        if (b > avail) break;
+        res_seg = sg;
+      }
+    }
+    const size_t slots = (size_t)K + (res_seg < nseg ? NSTEP - res_seg * K : 0);
+    for (int s = 0; s < ns; s++) o[s].store = take(slots * slot);
+  }
   bytes = (int64_t)used;
+  resident = nseg - res_seg;
   {
     cudaError_t e = cudaMalloc(&pool, used);
     if (e != cudaSuccess) {
@@ -2159,14 +2191,17 @@ int ElPlan<T>::issue_forward(cudaStream_t st, int64_t* count) {
   if (count) {
     int64_t c = 0;
     for (int n = 1; n <= NSTEP; n++)
-      c += fwd_launches() + 1 + ((n % K == 0 && n / K < nseg) ? 1 : 0);
+      c += fwd_launches() + 1 + ((n % K == 0 && n / K < res_seg) ? 1 : 0);
     *count = c;
     return ADS_OK;
   }
   ADS_CUDA(cudaMemsetAsync(pool + zero_fwd_off, 0, zero_fwd_len, st));
   for (int n = 1; n <= NSTEP; n++) {
-    if (int e = step(st, n, false, 0, true)) return e;
-    if (n % K == 0 && n / K < nseg) {  // checkpoint s holds slot s*K (state before step sK+1)
+    // steps of resident segments store what their adjoint steps read
+    const bool res = n >= a_res();
+    if (int e = step(st, n, res, res ? K + n - a_res() : 0, true)) return e;
+    // checkpoint s holds slot s*K (state before step sK+1); resident segments need none
+    if (n % K == 0 && n / K < res_seg) {
       k_el_ckpt<T><<<dim3(256, nshots), 256, 0, st>>>(d_shots, n / K, 1, par(n), 0);
       ADS_LAUNCHED(1);
     }
@@ -2180,8 +2215,8 @@ int ElPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     int64_t c = 1;
     for (int s = nseg - 1; s >= 0; s--) {
       const int a = 1 + s * K, b = std::min(a + K - 1, NSTEP);
-      c += 1 + (fwd_launches() + 1) * (b - a + 1) +
-           (group_launches(kSplitAdj1, nw_in, nw_pm) +
+      if (s < res_seg) c += 1 + (fwd_launches() + 1) * (b - a + 1);
+      c += (group_launches(kSplitAdj1, nw_in, nw_pm) +
             2 * group_launches(kSplitAdj23, nw_in, nw_pm)) * (b - a + 1) +
            (b - std::max(a, 2) + 1) +
            (sizeof(T) == 4 ? 1 : 0);
@@ -2195,12 +2230,16 @@ int ElPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
   ADS_LAUNCHED(1);
   for (int s = nseg - 1; s >= 0; s--) {
     const int a = 1 + s * K, b = std::min(a + K - 1, NSTEP);
-    k_el_ckpt<T><<<dim3(256, nshots), 256, 0, st>>>(d_shots, s, 0, 0, 1);
-    ADS_LAUNCHED(1);
-    for (int n = a; n <= b; n++)
-      if (int e = step(st, n, true, n - a, false)) return e;
+    const bool res = s >= res_seg;  // resident: the store already holds the segment
+    const int slot0 = res ? K + a - a_res() : 0;  // store slot of step a
+    if (!res) {
+      k_el_ckpt<T><<<dim3(256, nshots), 256, 0, st>>>(d_shots, s, 0, 0, 1);
+      ADS_LAUNCHED(1);
+      for (int n = a; n <= b; n++)
+        if (int e = step(st, n, true, n - a, false)) return e;
+    }
     for (int n = b; n >= a; n--) {
-      if (int e = adjoint_step(st, n - a)) return e;
+      if (int e = adjoint_step(st, slot0 + n - a)) return e;
       // the adjoint state now refers to slot n-1: add its residual (slot 0 is
       // the constant zero state and takes none)
       if (n - 1 >= 1) {
@@ -2628,6 +2667,10 @@ int64_t ads_elastic_plan_trace_count(const ads_elastic_plan* plan) {
 
 int64_t ads_elastic_plan_device_bytes(const ads_elastic_plan* plan) {
   return plan ? plan->impl->bytes : -1;
+}
+
+int64_t ads_elastic_plan_resident_segments(const ads_elastic_plan* plan) {
+  return plan ? plan->impl->resident : -1;
 }
 
 int64_t ads_elastic_plan_launches(const ads_elastic_plan* plan, int gradient) {

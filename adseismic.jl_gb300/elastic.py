@@ -128,10 +128,15 @@ def elastic_one_step_grad(param: ElasticPropagatorParams, rho, lam, mu, state, g
 class ElasticPlan:
     """Persistent multi-shot elastic plan: forward traces, misfit and the
     gradient w.r.t. lambda, mu, rho.  shots: list of dicts with srci, srcj,
-    srctype, srcv (NSTEP, nsrc), rcvi, rcvj, rcvtype."""
+    srctype, srcv (NSTEP, nsrc), rcvi, rcvj, rcvtype.  resident_segments /
+    resident_mem_pct: how many of the last checkpoint segments keep their
+    per-step adjoint inputs on the device instead of being recomputed (-1
+    none, 0 as many as fit in resident_mem_pct percent, default 50, of the
+    free device memory)."""
 
     def __init__(self, param: ElasticPropagatorParams, shots, precision="f64",
-                 use_graph=True, ckpt_every=0, stream=None, rows_per_warp=0):
+                 use_graph=True, ckpt_every=0, stream=None, rows_per_warp=0,
+                 resident_segments=0, resident_mem_pct=0):
         cfg = _lib.ElasticConfig()
         cfg.NX, cfg.NY, cfg.NSTEP = param.NX, param.NY, param.NSTEP
         cfg.dx, cfg.dy, cfg.dt = param.DELTAX, param.DELTAY, param.DELTAT
@@ -142,6 +147,8 @@ class ElasticPlan:
         cfg.use_graph = int(bool(use_graph))
         cfg.ckpt_every = ckpt_every
         cfg.rows_per_warp = int(rows_per_warp)
+        cfg.resident_segments = int(resident_segments)
+        cfg.resident_mem_pct = int(resident_mem_pct)
         self.param = param
         self.dtype = torch.float64 if precision == "f64" else torch.float32
         self._keep = []
@@ -170,6 +177,7 @@ class ElasticPlan:
         self.device_bytes = L.ads_elastic_plan_device_bytes(h)
         self.launches_forward = L.ads_elastic_plan_launches(h, 0)
         self.launches_gradient = L.ads_elastic_plan_launches(h, 1)
+        self.resident_segments = L.ads_elastic_plan_resident_segments(h)
 
     def close(self):
         if getattr(self, "_h", None):

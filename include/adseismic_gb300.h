@@ -347,7 +347,15 @@ typedef struct ads_elastic_config {
   int32_t use_graph;
   int32_t rows_per_warp; /* rows a warp streams in the step kernels; 0 = automatic */
   int64_t ckpt_every; /* 0 = automatic */
-  int32_t reserved[8];
+  int32_t resident_segments; /* checkpoint segments (the last ones) whose per-step strains
+                                and accelerations the forward loop stores for the
+                                reverse sweep, which then neither restores nor
+                                recomputes them: -1 = none, 0 = as many as fit
+                                (resident_mem_pct), N > 0 = at most N */
+  int32_t resident_mem_pct;  /* share of the device memory free at plan creation (after
+                                the plan's other buffers) they may use, in percent
+                                (1..95); 0 = 50 */
+  int32_t reserved[6];
 } ads_elastic_config;
 
 typedef struct ads_elastic_shot {
@@ -375,6 +383,8 @@ int64_t ads_elastic_plan_trace_offset(const ads_elastic_plan* plan, int64_t shot
 int64_t ads_elastic_plan_trace_count(const ads_elastic_plan* plan);
 int64_t ads_elastic_plan_device_bytes(const ads_elastic_plan* plan);
 int64_t ads_elastic_plan_launches(const ads_elastic_plan* plan, int gradient);
+/* Checkpoint segments kept resident (see resident_segments); -1 for a null plan. */
+int64_t ads_elastic_plan_resident_segments(const ads_elastic_plan* plan);
 /* lambda, mu, rho: device, N doubles. */
 int ads_elastic_plan_forward(ads_elastic_plan* plan, const double* lambda,
                              const double* mu, const double* rho, void* traces,

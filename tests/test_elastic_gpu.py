@@ -57,11 +57,18 @@ def shots_from(g):
 
 @pytest.mark.parametrize("use_graph", [True, False])
 @pytest.mark.parametrize("ckpt", [0, 1, 17])
-def test_plan_fp64_vs_oracle(ads, cuda, use_graph, ckpt):
+@pytest.mark.parametrize("resident", [-1, 0, 2])
+def test_plan_fp64_vs_oracle(ads, cuda, use_graph, ckpt, resident):
+    """resident: checkpoint segments whose adjoint inputs stay on the device
+    (-1 none: every segment recomputed; 0 as many as fit: all here; 2 the
+    last two)."""
     g = golden("elastic_small.npz")
     p = params(ads, g)
     plan = ads.ElasticPlan(p, shots_from(g), precision="f64", use_graph=use_graph,
-                           ckpt_every=ckpt)
+                           ckpt_every=ckpt, resident_segments=resident)
+    K = min(ckpt, p.NSTEP) if ckpt else min(p.NSTEP, 100)
+    nseg = -(-p.NSTEP // K)
+    assert plan.resident_segments == {-1: 0, 0: nseg, 2: min(2, nseg)}[resident]
     t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=cuda)
     tr = plan.forward(t(g["lam"]), t(g["mu"]), t(g["rho"]))
     assert rel(tr.cpu().numpy(), g["rcvv"].reshape(-1)) <= 1e-12
@@ -134,8 +141,8 @@ def test_multishot_sum_and_julia_api(ads, orc, cuda):
     assert rel(rcv.rcvv.cpu().numpy(), ref) <= 1e-12
 
 
-@pytest.mark.parametrize("rows_per_warp", [0, 5])
-def test_plan_strips_tiles_and_edge_sources_vs_oracle(ads, orc, cuda, rows_per_warp):
+@pytest.mark.parametrize("rows_per_warp,resident", [(0, 3), (5, -1), (5, 0)])
+def test_plan_strips_tiles_and_edge_sources_vs_oracle(ads, orc, cuda, rows_per_warp, resident):
     """Several column strips and row tiles, an odd checkpoint interval (the
     step buffers alternate, so checkpoints land on both parities) and sources
     on cells no stencil updates (padded ring, box edges), which keep their
@@ -167,7 +174,7 @@ def test_plan_strips_tiles_and_edge_sources_vs_oracle(ads, orc, cuda, rows_per_w
                                rho, srci, srcj, srct, srcv, rcvi, rcvj, rcvt, obs)
     t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=cuda)
     plan = ads.ElasticPlan(p, [sh], precision="f64", ckpt_every=7,
-                           rows_per_warp=rows_per_warp)
+                           rows_per_warp=rows_per_warp, resident_segments=resident)
     tr = plan.forward(t(lam), t(mu), t(rho))
     assert rel(tr.cpu().numpy(), ref_tr.reshape(-1)) <= 1e-12
     loss, gl, gm, gr = plan.gradient(t(lam), t(mu), t(rho), t(obs.reshape(-1)))
@@ -176,7 +183,8 @@ def test_plan_strips_tiles_and_edge_sources_vs_oracle(ads, orc, cuda, rows_per_w
     for a, b in zip((gl, gm, gr), ref[1:]):
         assert rel(a.cpu().numpy(), b) <= 1e-12
     plan.close()
-    p32 = ads.ElasticPlan(p, [sh], precision="f32", ckpt_every=7, rows_per_warp=rows_per_warp)
+    p32 = ads.ElasticPlan(p, [sh], precision="f32", ckpt_every=7, rows_per_warp=rows_per_warp,
+                          resident_segments=resident)
     loss32, gl32, gm32, gr32 = p32.gradient(t(lam), t(mu), t(rho),
                                             torch.as_tensor(obs.reshape(-1), device=cuda))
     torch.cuda.synchronize()
