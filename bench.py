@@ -353,8 +353,8 @@ def run_elastic_fwi(args):
                                               T=args.nstep if args.nstep != 3000 else 4000)
     t = lambda a: torch.tensor(a.reshape(-1), device="cuda")
     # the last checkpoint segments' adjoint inputs stay resident in HBM (up to
-    # 85% of the memory free after the plan's other buffers)
-    plan = ads.ElasticPlan(p, shots, precision="f32", ckpt_every=100, resident_mem_pct=85)
+    # 92% of the memory free after the plan's other buffers)
+    plan = ads.ElasticPlan(p, shots, precision="f32", ckpt_every=100, resident_mem_pct=92)
     obs = plan.forward(t(lam), t(mu), t(rho)).clone()
     sm = lambda a: t(ads.gaussian_smooth(a, 10.0))
     l0, m0, r0 = sm(lam), sm(mu), sm(rho)
@@ -481,10 +481,10 @@ def main():
                                                  npml=cfg["npml"], vp_ref=cfg["vp_ref"],
                                                  precision=prec, ckpt_every=100, **kw)
     t_setup = time.perf_counter()
-    # the last checkpoint segments' wavefields stay resident in HBM (up to 85%
+    # the last checkpoint segments' wavefields stay resident in HBM (up to 92%
     # of the memory free after the plan's other buffers): the reverse sweep
     # recomputes only the others
-    plan = mk("f32", shots, autotune=True, resident_mem_pct=85)
+    plan = mk("f32", shots, autotune=True, resident_mem_pct=92)
     vt = torch.tensor(vp_true, device=dev)
     v0 = torch.tensor(vp0, device=dev)
     obs = plan.forward(vt).clone()
