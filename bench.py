@@ -47,7 +47,7 @@ BYTES = {
 
 # DRAM bytes (read + write) of one step of each kernel on the bench geometry
 # at 16 shots, from ncu --set full captures of both launches of a step
-TRAFFIC_16SHOT = {"k_ac_fwd": 139.3e6, "k_ac_adj": 245.1e6}
+TRAFFIC_16SHOT = {"k_ac_fwd": 139.4e6, "k_ac_adj": 246.2e6}
 
 
 def workload(MX=1000, MY=500, npml=40, nstep=3000, nshots=64, nrcv=500, fpeak=15.0,
