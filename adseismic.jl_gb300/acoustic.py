@@ -10,13 +10,13 @@ libadseismic_gb300.so.
 from __future__ import annotations
 
 import ctypes as C
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 import torch
 
 from . import _lib
-from ._lib import ADS_F32, ADS_F64, ADS_VARIANT_U, ADS_VARIANT_W, call, lib
+from ._lib import ADS_F32, ADS_F64, ADS_VARIANT_W, call, lib
 
 
 def _stream():
