@@ -80,3 +80,35 @@ def test_compute_calls_fail_loudly_without_gpu(ads):
                                              None, 0, None)
     assert rc == _lib.ADS_ERR_CUDA
     assert "no CUDA device" in _lib.lib().ads_last_error().decode()
+
+
+def test_ctypes_structs_match_the_header_layout(ads, tmp_path):
+    """Sizes and field offsets of the config / shot structs as the C compiler
+    lays them out from include/adseismic_gb300.h, against the ctypes binding."""
+    import shutil
+    import subprocess
+
+    from adseismic_gb300 import _lib
+
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    structs = {"ads_acoustic_config": _lib.AcousticConfig, "ads_acoustic_shot": _lib.AcousticShot,
+               "ads_elastic_config": _lib.ElasticConfig, "ads_elastic_shot": _lib.ElasticShot}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "adseismic_gb300.h"',
+             "int main(void) {"]
+    for cname, cls in structs.items():
+        lines.append(f'  printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'  printf("{cname}.{fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                    str(exe)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                 text=True).stdout.splitlines())
+    for cname, cls in structs.items():
+        assert int(got[cname]) == ctypes.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert int(got[f"{cname}.{fname}"]) == getattr(cls, fname).offset, (cname, fname)
