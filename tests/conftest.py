@@ -17,7 +17,10 @@ def pytest_configure(config):
 def ads():
     import __graft_entry__ as g
 
-    return g.load_package()
+    pkg = g.load_package()
+    if not os.path.exists(pkg.LIB_PATH):  # a fresh checkout: compile the library first
+        pkg.build_library()
+    return pkg
 
 
 @pytest.fixture(scope="session")
