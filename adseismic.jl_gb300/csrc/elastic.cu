@@ -48,8 +48,9 @@ struct ElModel {
 
 template <typename T>
 struct ElShot {
-  const T* fin[NF];  // step input state
-  T* f[NF];          // step output state (== fin in the plans: updated in place)
+  const T* fin[NF];  // single-step operators: step input state
+  T* f[NF];          // single-step operators: step output state; plans: state
+                     // buffer 0 (buffer 1 follows at f[0] + NF * fs)
   T* g[NF];          // adjoint state (in place)
   T* tmp[NTMP];
   T* store;          // K slots x NSTORE fields
