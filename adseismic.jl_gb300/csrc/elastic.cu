@@ -66,6 +66,8 @@ struct ElShot {
   const int* src_dual;  // per source: 1 if no stencil updates its cell
   T* const* rcv_ptr;   // per receiver: its cell in the state (nullptr: records 0)
   T* const* rcv_gptr;  // per receiver: its cell in the adjoint state
+  T* const* src_gptr;  // per source: its cell in the adjoint state (source gradients)
+  double* gsrc;        // d loss / d srcv, (NSTEP, nsrc) FP64 (source gradients)
   const int* rcv_type;
   int nsrc, nrcv;
   int64_t fs;                   // elements per field
@@ -1353,6 +1355,18 @@ __global__ void k_el_resid(const ElShot<T>* __restrict__ shots, int n, int nt) {
   if (p) atomicAdd(p, sh.resid[(int64_t)r * nt + n]);
 }
 
+// d loss / d srcv row n-1: srcv row n-1 is added to state n, so its gradient
+// is the adjoint of state n (residual of slot n included) at the source cell
+// (AddSource.cpp:91-155 gathers grad_srcv the same way).  One thread a source.
+template <typename T>
+__global__ void k_el_src_grad(const ElShot<T>* __restrict__ shots, int n) {
+  const ElShot<T>& sh = shots[blockIdx.y];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= sh.nsrc) return;
+  const T* p = sh.src_gptr[k];
+  sh.gsrc[(int64_t)(n - 1) * sh.nsrc + k] = p ? (double)*p : 0.0;
+}
+
 // State <-> checkpoint copies (13 contiguous fields per shot).  Saving reads
 // state buffer par; restoring writes buffer 0 and, for two-buffer plans
 // (both != 0), buffer 1 as well.
@@ -1581,6 +1595,20 @@ void el_step(bool store, int kind, dim3 g, cudaStream_t s, const ElModel<T>& M,
 // whole-path elastic plan
 // ======================================================================
 
+// Whether the stencil of field `type` updates 0-based padded cell (i, j)
+// (src/Core.jl:96-228): vx rows 2..NX, columns 2..NY; vy 1..NX-1, 1..NY-1;
+// sxx, syy 1..NX-1, 2..NY; sxy 2..NX, 1..NY-1.
+static bool el_cell_updated(int type, int64_t i, int64_t j, int NX, int NY) {
+  switch (type) {
+    case VX: return i >= 2 && i <= NX && j >= 2 && j <= NY;
+    case VY: return i >= 1 && i <= NX - 1 && j >= 1 && j <= NY - 1;
+    case SXX:
+    case SYY: return i >= 1 && i <= NX - 1 && j >= 2 && j <= NY;
+    case SXY: return i >= 2 && i <= NX && j >= 1 && j <= NY - 1;
+    default: return false;
+  }
+}
+
 struct ElPlanBase {
   virtual ~ElPlanBase() = default;
   virtual int forward(const double* l, const double* m, const double* r, void* traces,
@@ -1589,8 +1617,10 @@ struct ElPlanBase {
                       cudaStream_t st) = 0;
   virtual int gradient(const double* l, const double* m, const double* r, const void* obs,
                        double* loss, double* gl, double* gm, double* gr, void* tr_out,
-                       cudaStream_t st) = 0;
+                       cudaStream_t st, double* grad_srcv) = 0;
   std::vector<int64_t> trace_off;
+  std::vector<int64_t> src_off;  // per shot: offset of its (NSTEP, nsrc) grad_srcv block
+  int64_t src_total = 0;
   int64_t trace_total = 0, bytes = 0, launches_fwd = 0, launches_grad = 0;
   int64_t resident = 0;  // checkpoint segments kept resident (no recompute)
 };
@@ -1644,6 +1674,7 @@ struct ElPlan final : ElPlanBase {
   T *d_lam = nullptr, *d_mu = nullptr, *d_rho = nullptr, *d_traces = nullptr,
     *d_resid = nullptr;
   double* d_partial = nullptr;
+  double* d_gsrc = nullptr;  // every shot's d loss / d srcv block (source gradients)
   static constexpr int kBlocks = 512;
   size_t zero_fwd_off = 0, zero_fwd_len = 0, zero_adj_off = 0, zero_adj_len = 0;
   cudaStream_t cap = nullptr;
@@ -1690,7 +1721,9 @@ struct ElPlan final : ElPlanBase {
               cudaStream_t st) override;
   int gradient(const double* l, const double* m, const double* r, const void* obs,
                double* loss, double* gl, double* gm, double* gr, void* tr_out,
-               cudaStream_t st) override;
+               cudaStream_t st, double* grad_srcv) override;
+  int max_src = 0;  // most sources of a shot
+  bool src_grad = false;  // the reverse sweep records d loss / d srcv
 };
 
 template <typename T>
@@ -1727,6 +1760,26 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   }
   K = c.ckpt_every > 0 ? (int)std::min<int64_t>(c.ckpt_every, NSTEP) : std::min(NSTEP, 100);
   nseg = (int)div_up(NSTEP, K);
+  src_grad = c.source_gradient != 0;
+  // The reverse sweep computes adjoint fields only on cells a stencil updates,
+  // so d loss / d srcv exists for sources on those cells alone.
+  for (int s = 0; s < ns && src_grad; s++)
+    for (int64_t k = 0; k < shots[s].nsrc; k++) {
+      const int64_t t = shots[s].srctype[k];
+      ADS_REQUIRE(t < 0 || t > 4 ||
+                      el_cell_updated((int)t, shots[s].srci[k] - 1, shots[s].srcj[k] - 1, NX, NY),
+                  "shot %d source %lld: source_gradient needs a cell the stencil of its field "
+                  "updates, not the padded frame",
+                  s, (long long)k);
+    }
+  src_off.resize(ns);
+  src_total = 0;
+  max_src = 0;
+  for (int s = 0; s < ns; s++) {
+    src_off[s] = src_total;
+    src_total += (int64_t)NSTEP * shots[s].nsrc;
+    max_src = std::max<int>(max_src, (int)shots[s].nsrc);
+  }
   P = grid_pitch(NY);
   fs = (int64_t)(NX + 2) * P;
   // strips of ESTRIP columns cover 1..NY; rows per warp sized for about one
@@ -1767,7 +1820,7 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   // ---- layout
   struct Off {
     size_t state, g, tmp, store, ckpt, acc, acc32, srcv, scell, stype, sdual, rcell, rtype, sptr,
-        rptr, gptr;
+        rptr, gptr, sgptr;
   };
   std::vector<Off> o(ns);
   size_t used = 0;
@@ -1803,11 +1856,13 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
     o[s].sptr = take(sizeof(T*) * std::max<int64_t>(h.nsrc, 1));
     o[s].rptr = take(sizeof(T*) * std::max<int64_t>(h.nrcv, 1));
     o[s].gptr = take(sizeof(T*) * std::max<int64_t>(h.nrcv, 1));
+    o[s].sgptr = take(sizeof(T*) * std::max<int64_t>(h.nsrc, 1));
   }
   const size_t model_o = take(3 * F);
   const size_t prof_o = take(sizeof(T) * (4 * NX + 4 * NY));
   const size_t resid_o = take(sizeof(T) * std::max<int64_t>(trace_total, 1));
   const size_t part_o = take(sizeof(double) * kBlocks);
+  const size_t gsrc_o = take(sizeof(double) * (src_grad ? std::max<int64_t>(src_total, 1) : 1));
   const size_t shots_o = take(sizeof(ElShot<T>) * ns);
   const size_t wl_o = take(sizeof(int) * std::max(nwt, 1));
   const size_t wlf_o = take(sizeof(int) * std::max(nwtf_max, 1));
@@ -1854,6 +1909,7 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   d_traces = (T*)(pool + traces_o);
   d_resid = (T*)(pool + resid_o);
   d_partial = (double*)(pool + part_o);
+  d_gsrc = (double*)(pool + gsrc_o);
   d_shots = (ElShot<T>*)(pool + shots_o);
   // profiles
   std::vector<double> ax(2 * NX), bx(2 * NX), kx(2 * NX), ay(2 * NY), by(2 * NY), ky(2 * NY);
@@ -1991,6 +2047,8 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
     d.src_ptr = (T* const*)(pool + o[s].sptr);
     d.rcv_ptr = (T* const*)(pool + o[s].rptr);
     d.rcv_gptr = (T* const*)(pool + o[s].gptr);
+    d.src_gptr = (T* const*)(pool + o[s].sgptr);
+    d.gsrc = src_grad ? d_gsrc + src_off[s] : nullptr;
     d.nsrc = (int)h.nsrc;
     d.nrcv = (int)h.nrcv;
     d.fs = fs;
@@ -2019,25 +2077,22 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
       std::vector<int> dual(h.nsrc);
       for (int64_t k = 0; k < h.nsrc; k++) {
         const int64_t i = h.srci[k] - 1, jj = h.srcj[k] - 1;
-        bool in = false;
-        switch (type[k]) {
-          case VX: in = i >= 2 && i <= NX && jj >= 2 && jj <= NY; break;
-          case VY: in = i >= 1 && i <= NX - 1 && jj >= 1 && jj <= NY - 1; break;
-          case SXX:
-          case SYY: in = i >= 1 && i <= NX - 1 && jj >= 2 && jj <= NY; break;
-          case SXY: in = i >= 2 && i <= NX && jj >= 1 && jj <= NY - 1; break;
-          default: break;
-        }
-        dual[k] = in ? 0 : 1;
+        dual[k] = el_cell_updated(type[k], i, jj, NX, NY) ? 0 : 1;
       }
       stage.emplace_back((char*)dual.data(), (char*)(dual.data() + dual.size()));
       ADS_CUDA(cudaMemcpyAsync((void*)d.src_dual, stage.back().data(), stage.back().size(),
                                cudaMemcpyHostToDevice, st));
-      std::vector<T*> ptr(h.nsrc);
-      for (int64_t k = 0; k < h.nsrc; k++)
-        ptr[k] = (type[k] >= 0 && type[k] <= 4) ? d.f[type[k]] + cell[k] : nullptr;
+      std::vector<T*> ptr(h.nsrc), gptr(h.nsrc);
+      for (int64_t k = 0; k < h.nsrc; k++) {
+        const bool ok = type[k] >= 0 && type[k] <= 4;
+        ptr[k] = ok ? d.f[type[k]] + cell[k] : nullptr;
+        gptr[k] = ok ? d.g[type[k]] + cell[k] : nullptr;
+      }
       stage.emplace_back((char*)ptr.data(), (char*)(ptr.data() + ptr.size()));
       ADS_CUDA(cudaMemcpyAsync((void*)d.src_ptr, stage.back().data(), stage.back().size(),
+                               cudaMemcpyHostToDevice, st));
+      stage.emplace_back((char*)gptr.data(), (char*)(gptr.data() + gptr.size()));
+      ADS_CUDA(cudaMemcpyAsync((void*)d.src_gptr, stage.back().data(), stage.back().size(),
                                cudaMemcpyHostToDevice, st));
     }
     if (h.nrcv > 0) {
@@ -2220,7 +2275,7 @@ int ElPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
       if (s < res_seg) c += 1 + (fwd_launches() + 1) * (b - a + 1);
       c += (group_launches(kSplitAdj1, nw_in, nw_pm) +
             2 * group_launches(kSplitAdj23, nw_in, nw_pm)) * (b - a + 1) +
-           (b - std::max(a, 2) + 1) +
+           (b - std::max(a, 2) + 1) + (src_grad ? b - a + 1 : 0) +
            (sizeof(T) == 4 ? 1 : 0);
     }
     *count = c;
@@ -2240,6 +2295,11 @@ int ElPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
         if (int e = step(st, n, true, n - a, false)) return e;
     }
     for (int n = b; n >= a; n--) {
+      if (src_grad) {  // the adjoint state refers to slot n, its residual included
+        k_el_src_grad<T><<<dim3((unsigned)div_up(std::max(max_src, 1), 128), nshots), 128, 0,
+                            st>>>(d_shots, n);
+        ADS_LAUNCHED(1);
+      }
       if (int e = adjoint_step(st, slot0 + n - a)) return e;
       // the adjoint state now refers to slot n-1: add its residual (slot 0 is
       // the constant zero state and takes none)
@@ -2288,8 +2348,10 @@ int ElPlan<T>::forward(const double* l, const double* m, const double* r, void* 
 template <typename T>
 int ElPlan<T>::gradient(const double* l, const double* m, const double* r, const void* obs,
                         double* loss, double* gl, double* gm, double* gr, void* tr_out,
-                        cudaStream_t st) {
+                        cudaStream_t st, double* grad_srcv) {
   ADS_REQUIRE(obs && loss && gl && gm && gr, "null argument");
+  ADS_REQUIRE(!grad_srcv || src_grad,
+              "grad_srcv needs a plan created with source_gradient = 1");
   if (int e = forward(l, m, r, nullptr, st)) return e;
   k_el_misfit<T><<<kBlocks, 256, 0, st>>>(d_traces, (const T*)obs, d_resid, trace_total,
                                           d_partial);
@@ -2307,6 +2369,9 @@ int ElPlan<T>::gradient(const double* l, const double* m, const double* r, const
   ADS_LAUNCHED(1);
   if (tr_out)
     ADS_CUDA(cudaMemcpyAsync(tr_out, d_traces, sizeof(T) * trace_total,
+                             cudaMemcpyDeviceToDevice, st));
+  if (grad_srcv && src_total > 0)  // the shots' blocks are contiguous, in the caller's order
+    ADS_CUDA(cudaMemcpyAsync(grad_srcv, d_gsrc, sizeof(double) * src_total,
                              cudaMemcpyDeviceToDevice, st));
   return ADS_OK;
 }
@@ -2691,7 +2756,22 @@ int ads_elastic_plan_gradient(ads_elastic_plan* plan, const double* lambda, cons
                               void* traces_out, ads_stream_t stream) {
   ADS_REQUIRE(plan, "null plan");
   return plan->impl->gradient(lambda, mu, rho, observed, loss, grad_lambda, grad_mu, grad_rho,
-                              traces_out, (cudaStream_t)stream);
+                              traces_out, (cudaStream_t)stream, nullptr);
+}
+
+int ads_elastic_plan_gradient_ex(ads_elastic_plan* plan, const double* lambda,
+                                 const double* mu, const double* rho, const void* observed,
+                                 double* loss, double* grad_lambda, double* grad_mu,
+                                 double* grad_rho, double* grad_srcv, void* traces_out,
+                                 ads_stream_t stream) {
+  ADS_REQUIRE(plan, "null plan");
+  return plan->impl->gradient(lambda, mu, rho, observed, loss, grad_lambda, grad_mu, grad_rho,
+                              traces_out, (cudaStream_t)stream, grad_srcv);
+}
+
+int64_t ads_elastic_plan_source_offset(const ads_elastic_plan* plan, int64_t shot) {
+  if (!plan || shot < 0 || shot >= (int64_t)plan->impl->src_off.size()) return -1;
+  return plan->impl->src_off[shot];
 }
 
 int ads_elastic_plan_profile(ads_elastic_plan* plan, const double* lambda, const double* mu,

@@ -132,11 +132,12 @@ class ElasticPlan:
     resident_mem_pct: how many of the last checkpoint segments keep their
     per-step adjoint inputs on the device instead of being recomputed (-1
     none, 0 as many as fit in resident_mem_pct percent, default 50, of the
-    free device memory)."""
+    free device memory).  source_gradient: the reverse sweep also records
+    d loss / d srcv (gradient(..., want_source_grad=True))."""
 
     def __init__(self, param: ElasticPropagatorParams, shots, precision="f64",
                  use_graph=True, ckpt_every=0, stream=None, rows_per_warp=0,
-                 resident_segments=0, resident_mem_pct=0):
+                 resident_segments=0, resident_mem_pct=0, source_gradient=False):
         cfg = _lib.ElasticConfig()
         cfg.NX, cfg.NY, cfg.NSTEP = param.NX, param.NY, param.NSTEP
         cfg.dx, cfg.dy, cfg.dt = param.DELTAX, param.DELTAY, param.DELTAT
@@ -149,6 +150,7 @@ class ElasticPlan:
         cfg.rows_per_warp = int(rows_per_warp)
         cfg.resident_segments = int(resident_segments)
         cfg.resident_mem_pct = int(resident_mem_pct)
+        cfg.source_gradient = int(bool(source_gradient))
         self.param = param
         self.dtype = torch.float64 if precision == "f64" else torch.float32
         self._keep = []
@@ -224,7 +226,10 @@ class ElasticPlan:
              out.ctypes.data_as(C.c_void_p), _stream())
         return {k: (float(out[2 * i]), float(out[2 * i + 1])) for i, k in enumerate(self.KERNELS)}
 
-    def gradient(self, lam, mu, rho, observed, want_traces=False):
+    def gradient(self, lam, mu, rho, observed, want_traces=False, want_source_grad=False):
+        """(loss, grad_lambda, grad_mu, grad_rho[, traces][, grad_srcv]): grad_srcv is
+        a list of per-shot (NSTEP, nsrc) FP64 tensors, d loss / d srcv (the gradient
+        AddSource's backward gives, AddSource.cpp:91-155); needs source_gradient."""
         _require_cuda(lam, mu, rho, observed)
         lam, mu, rho = (t.contiguous().to(torch.float64) for t in (lam, mu, rho))
         obs = observed.contiguous().to(self.dtype)
@@ -232,6 +237,21 @@ class ElasticPlan:
         gl, gm, gr = (torch.empty_like(lam) for _ in range(3))
         tr = (torch.empty(max(self.trace_count, 1), dtype=self.dtype, device=lam.device)
               if want_traces else None)
+        if want_source_grad:
+            T = self.param.NSTEP
+            total = sum(T * len(s["srci"]) for s in self.shots)
+            gs = torch.zeros(max(total, 1), dtype=torch.float64, device=lam.device)
+            call("ads_elastic_plan_gradient_ex", self._h, _ptr(lam), _ptr(mu), _ptr(rho),
+                 _ptr(obs), _ptr(loss), _ptr(gl), _ptr(gm), _ptr(gr), _ptr(gs), _ptr(tr),
+                 _stream())
+            L = lib()
+            per_shot = []
+            for k, s in enumerate(self.shots):
+                o = L.ads_elastic_plan_source_offset(self._h, k)
+                m = len(s["srci"])
+                per_shot.append(gs[o:o + T * m].view(T, m))
+            out = (loss[0], gl, gm, gr) + ((tr[:self.trace_count],) if want_traces else ())
+            return out + (per_shot,)
         call("ads_elastic_plan_gradient", self._h, _ptr(lam), _ptr(mu), _ptr(rho), _ptr(obs),
              _ptr(loss), _ptr(gl), _ptr(gm), _ptr(gr), _ptr(tr), _stream())
         if want_traces:

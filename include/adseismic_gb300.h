@@ -355,7 +355,9 @@ typedef struct ads_elastic_config {
   int32_t resident_mem_pct;  /* share of the device memory free at plan creation (after
                                 the plan's other buffers) they may use, in percent
                                 (1..95); 0 = 50 */
-  int32_t reserved[6];
+  int32_t source_gradient;   /* 1: the reverse sweep also records d loss / d srcv
+                                (ads_elastic_plan_gradient_ex); 0: not */
+  int32_t reserved[5];
 } ads_elastic_config;
 
 typedef struct ads_elastic_shot {
@@ -385,6 +387,18 @@ int64_t ads_elastic_plan_device_bytes(const ads_elastic_plan* plan);
 int64_t ads_elastic_plan_launches(const ads_elastic_plan* plan, int gradient);
 /* Checkpoint segments kept resident (see resident_segments); -1 for a null plan. */
 int64_t ads_elastic_plan_resident_segments(const ads_elastic_plan* plan);
+/* ads_elastic_plan_gradient plus the source-time gradient grad_srcv = d loss /
+ * d srcv, the gradient AddSource's backward (AddSource.cpp:91-155) gathers:
+ * device doubles, per shot an (NSTEP, nsrc) row-major block at
+ * ads_elastic_plan_source_offset(plan, shot); 0 for sources of a type outside
+ * 0..4.  Needs a plan created with source_gradient = 1; may be NULL. */
+int ads_elastic_plan_gradient_ex(ads_elastic_plan* plan, const double* lambda,
+                                 const double* mu, const double* rho, const void* observed,
+                                 double* loss, double* grad_lambda, double* grad_mu,
+                                 double* grad_rho, double* grad_srcv, void* traces_out,
+                                 ads_stream_t stream);
+/* Offset (doubles) of a shot's block in grad_srcv; -1 for a bad index. */
+int64_t ads_elastic_plan_source_offset(const ads_elastic_plan* plan, int64_t shot);
 /* lambda, mu, rho: device, N doubles. */
 int ads_elastic_plan_forward(ads_elastic_plan* plan, const double* lambda,
                              const double* mu, const double* rho, void* traces,

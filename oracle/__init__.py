@@ -252,21 +252,24 @@ def elastic_forward(NX, NY, NSTEP, dt, dx, dy, ax, bx, ay, by, lam, mu, rho, src
 
 
 def elastic_gradient(NX, NY, NSTEP, dt, dx, dy, ax, bx, ay, by, lam, mu, rho, srci, srcj,
-                     srctype, srcv, rcvi, rcvj, rcvtype, obs):
+                     srctype, srcv, rcvi, rcvj, rcvtype, obs, want_src=False):
+    """(loss, grad_lambda, grad_mu, grad_rho), plus grad_srcv (NSTEP, nsrc) with
+    want_src."""
     N = (NX + 2) * (NY + 2)
     srci, srcj, srctype, rcvi, rcvj, rcvtype = map(_i64, (srci, srcj, srctype, rcvi, rcvj,
                                                           rcvtype))
     srcv, obs = _f64(srcv).reshape(-1), _f64(obs).reshape(-1)
     lam, mu, rho, ax, bx, ay, by = map(_f64, (lam, mu, rho, ax, bx, ay, by))
     gl, gm, gr = np.empty(N), np.empty(N), np.empty(N)
-    f = lib().orc_elastic_gradient
+    gs = np.zeros((NSTEP, len(srci)))
+    f = lib().orc_elastic_gradient_src
     f.restype = C.c_double
     loss = f(C.c_int64(NX), C.c_int64(NY), C.c_int64(NSTEP), C.c_double(dt), C.c_double(dx),
              C.c_double(dy), _d(ax), _d(bx), _d(ay), _d(by), _d(lam), _d(mu), _d(rho),
              C.c_int64(len(srci)), _i(srci), _i(srcj), _i(srctype), _d(srcv),
              C.c_int64(len(rcvi)), _i(rcvi), _i(rcvj), _i(rcvtype), _d(obs), _d(gl), _d(gm),
-             _d(gr))
-    return loss, gl, gm, gr
+             _d(gr), _d(gs) if want_src else None)
+    return (loss, gl, gm, gr, gs) if want_src else (loss, gl, gm, gr)
 
 
 def add_source_fwd(in5, srci, srcj, srctype, srcv, NX, NY, use_ref=False):

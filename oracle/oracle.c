@@ -697,6 +697,24 @@ double orc_elastic_gradient(int64_t NX, int64_t NY, int64_t NSTEP, double dt, do
                             const int64_t* rcvi, const int64_t* rcvj,
                             const int64_t* rcvtype, const double* obs, double* glambda,
                             double* gmu, double* grho) {
+  return orc_elastic_gradient_src(NX, NY, NSTEP, dt, dx, dy, ax, bx, ay, by, lambda, mu, rho,
+                                  nsrc, srci, srcj, srctype, srcv, nrcv, rcvi, rcvj, rcvtype,
+                                  obs, glambda, gmu, grho, NULL);
+}
+
+/* The gradient above plus d loss / d srcv (gsrc: (NSTEP, nsrc), or NULL).
+ * srcv row n-1 is added to state n (AddSource.cpp:33-89), so its gradient is
+ * the adjoint of state n at the source cell, residual of slot n included
+ * (AddSource.cpp:91-155 gathers grad_srcv the same way). */
+double orc_elastic_gradient_src(int64_t NX, int64_t NY, int64_t NSTEP, double dt, double dx,
+                                double dy, const double* ax, const double* bx,
+                                const double* ay, const double* by, const double* lambda,
+                                const double* mu, const double* rho, int64_t nsrc,
+                                const int64_t* srci, const int64_t* srcj,
+                                const int64_t* srctype, const double* srcv, int64_t nrcv,
+                                const int64_t* rcvi, const int64_t* rcvj,
+                                const int64_t* rcvtype, const double* obs, double* glambda,
+                                double* gmu, double* grho, double* gsrc) {
   const int64_t N = (NX + 2) * (NY + 2), SZ = ORC_EL_NFIELD * N, nt = NSTEP + 1;
   double* hist = (double*)malloc(sizeof(double) * (size_t)(nt * SZ));
   double* rcvv = (double*)malloc(sizeof(double) * (size_t)(nrcv * nt));
@@ -721,6 +739,12 @@ double orc_elastic_gradient(int64_t NX, int64_t NY, int64_t NSTEP, double dt, do
       g[t * N + (rcvi[r] - 1) * (NY + 2) + rcvj[r] - 1] +=
           2 * (rcvv[r * nt + n] - obs[r * nt + n]);
     }
+    if (gsrc)
+      for (int64_t k = 0; k < nsrc; k++) {
+        const int64_t t = srctype[k];
+        gsrc[(n - 1) * nsrc + k] =
+            (t >= 0 && t <= 4) ? g[t * N + (srci[k] - 1) * (NY + 2) + srcj[k] - 1] : 0.0;
+      }
     orc_elastic_step_bwd(hist + (n - 1) * SZ, g, gp, glambda, gmu, grho, lambda, mu, rho,
                          ax, bx, ay, by, dt, dx, dy, NX, NY);
     double* t = g; g = gp; gp = t;

@@ -130,6 +130,16 @@ double orc_elastic_gradient(int64_t NX, int64_t NY, int64_t NSTEP, double dt, do
                             const int64_t* rcvi, const int64_t* rcvj,
                             const int64_t* rcvtype, const double* obs, double* glambda,
                             double* gmu, double* grho);
+/* ... and d loss / d srcv into gsrc ((NSTEP, nsrc), or NULL). */
+double orc_elastic_gradient_src(int64_t NX, int64_t NY, int64_t NSTEP, double dt, double dx,
+                                double dy, const double* ax, const double* bx,
+                                const double* ay, const double* by, const double* lambda,
+                                const double* mu, const double* rho, int64_t nsrc,
+                                const int64_t* srci, const int64_t* srcj,
+                                const int64_t* srctype, const double* srcv, int64_t nrcv,
+                                const int64_t* rcvi, const int64_t* rcvj,
+                                const int64_t* rcvtype, const double* obs, double* glambda,
+                                double* gmu, double* grho, double* gsrc);
 
 /* AddSource forward/backward (AddSource.cpp:33-155), GetReceive forward/backward
  * (GetReceive.cpp:10-96), restated. */

@@ -192,3 +192,55 @@ def test_plan_strips_tiles_and_edge_sources_vs_oracle(ads, orc, cuda, rows_per_w
     for a, b in zip((gl32, gm32, gr32), ref[1:]):
         assert rel(a.cpu().numpy(), b) <= 1e-4
     p32.close()
+
+
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-12), ("f32", 1e-4)])
+@pytest.mark.parametrize("resident", [-1, 2, 0])
+def test_source_time_gradient_vs_oracle(ads, orc, cuda, precision, tol, resident):
+    """d loss / d srcv of an elastic plan (two shots, sources of every field
+    type, one on the first row its stencil updates, one of an ignored type)
+    against the oracle; a source on the padded frame is rejected."""
+    g = golden("elastic_small.npz")
+    p = params(ads, g, T=41)
+    NX, NY, T = p.NX, p.NY, p.NSTEP
+    prof = ads.compute_elastic_PML_Params(p)
+    ax, bx, kx, ay, by, ky = [a.reshape(-1) for a in prof]
+    rng = np.random.default_rng(8)
+    cases = [dict(srci=[10, 15, 8, 20, 12, 2, 9], srcj=[9, 12, 14, 7, 10, 5, 9],
+                  srctype=[0, 1, 2, 3, 4, 2, 7]),
+             dict(srci=[14], srcj=[11], srctype=[2])]
+    shots, obs, want = [], [], []
+    for c in cases:
+        srcv = rng.standard_normal((T, len(c["srci"]))) * 1e2
+        sh = dict(srci=np.array(c["srci"]), srcj=np.array(c["srcj"]),
+                  srctype=np.array(c["srctype"]), srcv=srcv, rcvi=g["rcvi"], rcvj=g["rcvj"],
+                  rcvtype=g["rcvtype"])
+        o = g["obs"][:, :T + 1] * 0.5
+        out = orc.elastic_gradient(NX, NY, T, p.DELTAT, p.DELTAX, p.DELTAY, ax, bx, ay, by,
+                                   g["lam"], g["mu"], g["rho"], sh["srci"], sh["srcj"],
+                                   sh["srctype"], srcv, sh["rcvi"], sh["rcvj"], sh["rcvtype"],
+                                   o, want_src=True)
+        shots.append(sh)
+        obs.append(o)
+        want.append(out[4])
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=cuda)
+    plan = ads.ElasticPlan(p, shots, precision=precision, ckpt_every=9,
+                           resident_segments=resident, source_gradient=True)
+    dtype = torch.float64 if precision == "f64" else torch.float32
+    packed = torch.cat([torch.as_tensor(o.reshape(-1), dtype=dtype, device=cuda) for o in obs])
+    out = plan.gradient(t(g["lam"]), t(g["mu"]), t(g["rho"]), packed, want_source_grad=True)
+    torch.cuda.synchronize()
+    got = out[-1]
+    for k in range(len(cases)):
+        gk = got[k].cpu().numpy()
+        assert gk.shape == want[k].shape
+        assert rel(gk, want[k]) <= tol, (k, rel(gk, want[k]))
+    assert np.all(got[0].cpu().numpy()[:, -1] == 0.0)  # the ignored type
+    plan.close()
+    p2 = ads.ElasticPlan(p, shots, precision=precision, ckpt_every=9)
+    with pytest.raises(ads.AdsError):
+        p2.gradient(t(g["lam"]), t(g["mu"]), t(g["rho"]), packed, want_source_grad=True)
+    p2.close()
+    frame = dict(shots[1], srci=np.array([1]))  # sxx on row 0: read, never updated
+    with pytest.raises(ads.AdsError, match="padded frame"):
+        ads.ElasticPlan(p, [frame], precision=precision, ckpt_every=9, source_gradient=True)

@@ -206,3 +206,42 @@ def test_acoustic_source_gradient_finite_differences(orc):
         fd = (lp - lm) / (2 * e)
         assert abs(fd - gs[row, k]) <= 1e-7 * max(abs(fd), 1e-12 * abs(lp)), (row, k, fd,
                                                                              gs[row, k])
+
+
+def test_elastic_source_gradient_finite_differences(orc):
+    """d loss / d srcv from the oracle's elastic adjoint equals central
+    differences of the loss: one source of each field type (one on a
+    receiver's cell, one on the padded ring) and an ignored type."""
+    g = golden("elastic_small.npz")
+    NX, NY, T = int(g["NX"]), int(g["NY"]), 30
+    a = dict(dt=float(g["dt"]), dx=float(g["dx"]), dy=float(g["dy"]))
+    rng = np.random.default_rng(6)
+    srci = np.array([10, 15, 8, 20, 12, 1, 9])
+    srcj = np.array([9, 12, 14, 7, 10, 5, 9])
+    srct = np.array([0, 1, 2, 3, 4, 2, 7])
+    srcv = rng.standard_normal((T, len(srci))) * 1e2
+    rcvi, rcvj, rcvt = g["rcvi"], g["rcvj"], g["rcvtype"]
+    srci[0], srcj[0], srct[0] = rcvi[0], rcvj[0], rcvt[0] if rcvt[0] <= 4 else 0
+    obs = g["obs"][:, :T + 1].copy()
+    lam, mu, rho = g["lam"], g["mu"], g["rho"]
+
+    def run(sv, want=False):
+        return orc.elastic_gradient(NX, NY, T, a["dt"], a["dx"], a["dy"], g["ax"], g["bx"],
+                                    g["ay"], g["by"], lam, mu, rho, srci, srcj, srct, sv, rcvi,
+                                    rcvj, rcvt, obs, want_src=want)
+
+    L, _, _, _, gs = run(srcv, True)
+    assert gs.shape == (T, len(srci)) and np.all(gs[:, -1] == 0.0)
+    assert L == run(srcv)[0]
+    # the loss is quadratic in srcv, so central differences are exact up to
+    # rounding of the loss (~1e-16 L / e): a large step keeps that below the
+    # stress-source gradients, which are small in these units
+    for row, k in [(0, 0), (5, 1), (12, 2), (20, 3), (T - 1, 4), (9, 5), (T - 2, 0)]:
+        e = 1e4
+        sp, sm = srcv.copy(), srcv.copy()
+        sp[row, k] += e
+        sm[row, k] -= e
+        lp, lm = run(sp)[0], run(sm)[0]
+        fd = (lp - lm) / (2 * e)
+        tol = 1e-7 * abs(fd) + 1e-15 * max(lp, lm) / e
+        assert abs(fd - gs[row, k]) <= tol, (row, k, fd, gs[row, k])
