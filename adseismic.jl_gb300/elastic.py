@@ -133,7 +133,9 @@ class ElasticPlan:
     per-step adjoint inputs on the device instead of being recomputed (-1
     none, 0 as many as fit in resident_mem_pct percent, default 50, of the
     free device memory).  source_gradient: the reverse sweep also records
-    d loss / d srcv (gradient(..., want_source_grad=True))."""
+    d loss / d srcv (gradient(..., want_source_grad=True)); the plan then
+    rejects (AdsError) sources on the padded frame, the cells the stencil of
+    their field does not update."""
 
     def __init__(self, param: ElasticPropagatorParams, shots, precision="f64",
                  use_graph=True, ckpt_every=0, stream=None, rows_per_warp=0,

@@ -356,7 +356,12 @@ typedef struct ads_elastic_config {
                                 the plan's other buffers) they may use, in percent
                                 (1..95); 0 = 50 */
   int32_t source_gradient;   /* 1: the reverse sweep also records d loss / d srcv
-                                (ads_elastic_plan_gradient_ex); 0: not */
+                                (ads_elastic_plan_gradient_ex); plan creation then
+                                rejects sources of type 0..4 on a cell the stencil
+                                of their field does not update (the padded frame:
+                                vx rows/columns 3..NX+1 / 3..NY+1 1-based, vy
+                                2..NX / 2..NY, sxx and syy 2..NX / 3..NY+1, sxy
+                                3..NX+1 / 2..NY are updated); 0: not */
   int32_t reserved[5];
 } ads_elastic_config;
 
