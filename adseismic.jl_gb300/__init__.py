@@ -24,7 +24,7 @@ from .io import (load_acoustic_model, load_acoustic_receiver, load_acoustic_sour
 from .optim import LBFGS, fwi_lbfgs
 from .utils import (Gauss, Ricker, compute_lame_parameters, compute_properties,
                     folded_layer_model, gaussian_smooth, layered_gaussian_model,
-                    ricker_width_samples)
+                    ricker_width_samples, variable_source, variable_source_grad)
 
 
 def version() -> str:

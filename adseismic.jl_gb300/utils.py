@@ -48,6 +48,106 @@ def compute_properties(vp, vs, rho):
     return lam, mu, rho
 
 
+# ------------------------------------------------------------------ variable sources
+
+def _source_cells(param, srctype):
+    """1-based (i, j) of the padded-grid cells a plan accepts as source cells,
+    in the reference's row-major order (j fastest): the interior
+    2..NX+1 x 2..NY+1 for acoustic parameters; for elastic ones the cells the
+    stencil of field `srctype` updates (vx 3..NX+1 x 3..NY+1, vy 2..NX x 2..NY,
+    sxx / syy 2..NX x 3..NY+1, sxy 3..NX+1 x 2..NY; src/Core.jl:96-213)."""
+    NX, NY = int(param.NX), int(param.NY)
+    if srctype is None:
+        ri, rj = (2, NX + 1), (2, NY + 1)
+    else:
+        boxes = {0: ((3, NX + 1), (3, NY + 1)), 1: ((2, NX), (2, NY)),
+                 2: ((2, NX), (3, NY + 1)), 3: ((2, NX), (3, NY + 1)),
+                 4: ((3, NX + 1), (2, NY))}
+        if int(srctype) not in boxes:
+            raise ValueError(f"srctype must be 0..4, got {srctype}")
+        ri, rj = boxes[int(srctype)]
+    i, j = np.meshgrid(np.arange(ri[0], ri[1] + 1, dtype=np.int64),
+                       np.arange(rj[0], rj[1] + 1, dtype=np.int64), indexing="ij")
+    return i.reshape(-1), j.reshape(-1)
+
+
+def _gauss_weights(param, x, y, sigma, i, j):
+    """magn of src/Utils.jl:625-627 at 1-based cells (i, j), cell (i, j) at
+    ((i-1) DELTAX, (j-1) DELTAY); also (xs - x) / (sigma DELTAX^2) and
+    (ys - y) / (sigma DELTAY^2), the factors of d magn / d x and d magn / d y."""
+    hx, hy = float(param.DELTAX), float(param.DELTAY)
+    dx = (i - 1) * hx - float(x)
+    dy = (j - 1) * hy - float(y)
+    magn = 1.0 / (2 * math.pi * sigma) * np.exp(-((dx / (math.sqrt(2 * sigma) * hx)) ** 2 +
+                                                 (dy / (math.sqrt(2 * sigma) * hy)) ** 2))
+    return magn, dx / (sigma * hx * hx), dy / (sigma * hy * hy)
+
+
+def variable_source(param, x, y, v=None, sigma=None, srctype=None, source_scale=1.0):
+    """The two forms of src/Utils.jl:603-640.
+
+    Gaussian form, variable_source(param, x, y, v; sigma): a source at every
+    cell with wavelet v scaled by magn = exp(-((xs - x)^2 / (2 sigma DELTAX^2)
+    + (ys - y)^2 / (2 sigma DELTAY^2))) / (2 pi sigma), xs = (i-1) DELTAX,
+    ys = (j-1) DELTAY, sigma = 1 by default.  Returns (srci, srcj, srcv) with
+    srcv = v magn^T of shape (len(v), ncells).  The reference covers the whole
+    padded grid; the plans hold the padded frame at zero and take no sources
+    there, so the cells returned are the ones a plan accepts (`srctype`
+    selects the elastic field's box; None means acoustic).  The dropped frame
+    terms are below magn at the frame, exp(-d^2 / (2 sigma)) / (2 pi sigma)
+    for a source d cells inside it.  d loss / d (x, y, v) then follows from the
+    plan's d loss / d srcv through variable_source_grad.
+
+    Index form, variable_source(param, ix, iy; source_scale) for acoustic
+    parameters: an AcousticSource at the given cells whose (NSTEP+1, n)
+    wavelet is the trainable variable, zero at the start."""
+    if v is None:
+        from .acoustic import AcousticSource
+
+        ix = np.asarray(x, dtype=np.int64).reshape(-1)
+        iy = np.asarray(y, dtype=np.int64).reshape(-1)
+        if ix.shape != iy.shape:
+            raise ValueError("ix and iy differ in length")
+        return AcousticSource(ix, iy, np.zeros((int(param.NSTEP) + 1, ix.size)) * source_scale)
+    sigma = 1.0 if sigma is None else float(sigma)
+    i, j = _source_cells(param, srctype)
+    magn, _, _ = _gauss_weights(param, x, y, sigma, i, j)
+    v = np.asarray(v, dtype=np.float64).reshape(-1)
+    return i, j, np.ascontiguousarray(v[:, None] * magn[None, :])
+
+
+def variable_source_grad(param, x, y, v, grad_srcv, sigma=None, srctype=None):
+    """Chain rule of the Gaussian variable_source: from G = d loss / d srcv,
+    (rows, ncells) as a plan's gradient_ex returns it for the source set
+    variable_source made (rows <= len(v); rows past G's count are not
+    injected), gives (d loss / d x, d loss / d y, d loss / d v):
+    dv[t] = sum_k G[t, k] magn_k, dx = sum_t v[t] sum_k G[t, k] magn_k
+    (xs_k - x) / (sigma DELTAX^2), and dy likewise.  G may be a numpy array or
+    a torch tensor (the sums then run on its device); dv has G's kind."""
+    import torch
+
+    sigma = 1.0 if sigma is None else float(sigma)
+    i, j = _source_cells(param, srctype)
+    magn, fx, fy = _gauss_weights(param, x, y, sigma, i, j)
+    G = torch.as_tensor(grad_srcv, dtype=torch.float64)
+    if G.dim() != 2 or G.shape[1] != i.size:
+        raise ValueError(f"grad_srcv has shape {tuple(G.shape)}, expected (rows, {i.size})")
+    v = np.asarray(v, dtype=np.float64).reshape(-1)
+    rows = G.shape[0]
+    if rows > v.size:
+        raise ValueError(f"grad_srcv has {rows} rows, v only {v.size}")
+    W = torch.as_tensor(np.stack([magn, magn * fx, magn * fy], axis=1), device=G.device)
+    P = G @ W  # (rows, 3)
+    vt = torch.as_tensor(v[:rows], device=G.device)
+    gx = float(vt @ P[:, 1])
+    gy = float(vt @ P[:, 2])
+    dv = torch.zeros(v.size, dtype=torch.float64, device=G.device)
+    dv[:rows] = P[:, 0]
+    if not isinstance(grad_srcv, torch.Tensor):
+        dv = dv.numpy()
+    return gx, gy, dv
+
+
 # ------------------------------------------------------------------ synthetic models
 
 def layered_gaussian_model(nx2, ny2, vmin=2000.0, vmax=3500.0, sigma=15.0, amp=0.10,

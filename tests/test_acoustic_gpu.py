@@ -346,6 +346,40 @@ def test_source_time_gradient_vs_oracle(ads, orc, cuda, precision, tol, resident
     plan.close()
 
 
+@pytest.mark.parametrize("precision,tol", [("f64", TOL64), ("f32", 1e-4)])
+def test_location_gradient_of_gaussian_source_vs_oracle(ads, orc, cuda, precision, tol):
+    """A Gaussian variable source (a source on every interior cell,
+    src/Utils.jl:603-633) through a plan: d loss / d srcv against the oracle,
+    then the location gradient d loss / d (x, y) and d loss / d v from it."""
+    rng = np.random.default_rng(13)
+    NX, NY, h, dt, npml, nt = 40, 36, 10.0, 1e-3, 8, 60
+    p = ads.AcousticPropagatorParams(NX=NX, NY=NY, NSTEP=nt, DELTAX=h, DELTAY=h, DELTAT=dt)
+    vp = 2000 + 400 * rng.random((NX + 2) * (NY + 2))
+    s, t = orc.acoustic_pml(NX, NY, h, h, npml, 2000.0)
+    rcvi, rcvj = np.arange(10, 34), np.full(24, 12)
+    v = ads.Ricker(p, 5.0, 15.0) * 1e5
+    x, y = 203.0, 177.0
+    i, j, srcv = ads.variable_source(p, x, y, v, sigma=1.3)
+    o = orc.acoustic_forward(NX, NY, nt, dt, h, h, s, t, vp * 1.04, i, j, srcv, rcvi, rcvj)
+    _, _, G = orc.acoustic_gradient(NX, NY, nt, dt, h, h, s, t, vp, i, j, srcv, rcvi, rcvj, o,
+                                    want_src=True)
+    plan = ads.AcousticPlan(NX, NY, h, h, dt, [dict(x0=0, nx=NX, nstep=nt, srci=i, srcj=j,
+                                                    srcv=srcv, rcvi=rcvi, rcvj=rcvj)],
+                            npml=npml, vp_ref=2000.0, precision=precision, ckpt_every=16)
+    out = plan.gradient(T(vp.reshape(NX + 2, NY + 2), cuda), plan.pack([T(o.reshape(-1), cuda)]),
+                        want_source_grad=True)
+    torch.cuda.synchronize()
+    got = out[-1][0]
+    assert got.shape == G.shape and rel(got.cpu().numpy(), G) <= tol
+    gx, gy, gv = ads.variable_source_grad(p, x, y, v, got, sigma=1.3)
+    wx, wy, wv = ads.variable_source_grad(p, x, y, v, G, sigma=1.3)
+    # (x, y) sums G against weights of both signs: FP32 is held to 1e-3 there
+    txy = tol if precision == "f64" else 1e-3
+    assert np.hypot(gx - wx, gy - wy) <= txy * np.hypot(wx, wy), (gx, wx, gy, wy)
+    assert gv.device == got.device and rel(gv.cpu().numpy(), wv) <= tol
+    plan.close()
+
+
 def test_fwi_lbfgs_reduces_misfit(ads, cuda):
     """The L-BFGS FWI loop on the batched FP32 gradient (4 shots): the misfit
     falls well below its starting value and the loss history is recorded."""
