@@ -23,6 +23,7 @@ from .io import (load_acoustic_model, load_acoustic_receiver, load_acoustic_sour
                  load_elastic_model, load_elastic_receiver, load_elastic_source, load_params)
 from .optim import LBFGS, fwi_lbfgs
 from .utils import (Gauss, Ricker, compute_lame_parameters, compute_properties,
+                    compute_properties_grad,
                     folded_layer_model, gaussian_smooth, layered_gaussian_model,
                     ricker_width_samples, variable_source, variable_source_grad)
 

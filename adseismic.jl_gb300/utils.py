@@ -48,6 +48,19 @@ def compute_properties(vp, vs, rho):
     return lam, mu, rho
 
 
+def compute_properties_grad(vp, vs, rho, grad_lambda, grad_mu, grad_rho):
+    """Chain rule of compute_properties (src/Utils.jl:249-258: mu = rho vs^2,
+    lambda = rho vp^2 - 2 mu, rho passed through): from the gradients of a
+    loss with respect to lambda, mu and rho, as the elastic plans return them,
+    the gradients with respect to vp, vs and rho, which the reference's
+    elastic inversion (inv_vp / inv_vs / inv_rho, src/IO.jl:27-40) trains.
+    Elementwise; takes numpy arrays or torch tensors (on any device)."""
+    g_vp = 2.0 * rho * vp * grad_lambda
+    g_vs = 2.0 * rho * vs * (grad_mu - 2.0 * grad_lambda)
+    g_rho = grad_rho + (vp * vp - 2.0 * vs * vs) * grad_lambda + vs * vs * grad_mu
+    return g_vp, g_vs, g_rho
+
+
 # ------------------------------------------------------------------ variable sources
 
 def _source_cells(param, srctype):

@@ -25,6 +25,32 @@ def test_material_transforms(ads):
     assert np.allclose(lam2, lam) and np.allclose(mu2, mu)
 
 
+def test_properties_chain_rule_matches_finite_differences(ads):
+    """d L / d (vp, vs, rho) for L = <a, lambda> + <b, mu> + <c, rho> through
+    compute_properties, against central differences."""
+    rng = np.random.default_rng(2)
+    vp = 2500 + 1000 * rng.random(6)
+    vs = vp / np.sqrt(3) * (1 + 0.05 * rng.standard_normal(6))
+    rho = 310 * vp ** 0.25
+    a, b, c = rng.standard_normal((3, 6))
+
+    def L(vp, vs, rho):
+        lam, mu, r = ads.compute_properties(vp, vs, rho)
+        return a @ lam + b @ mu + c @ r
+
+    g = ads.compute_properties_grad(vp, vs, rho, a, b, c)
+    for k, x in enumerate((vp, vs, rho)):
+        for m in range(6):
+            e = 1e-3 * x[m]
+            xp, xm = x.copy(), x.copy()
+            xp[m] += e
+            xm[m] -= e
+            args_p = [xp if q == k else y for q, y in enumerate((vp, vs, rho))]
+            args_m = [xm if q == k else y for q, y in enumerate((vp, vs, rho))]
+            fd = (L(*args_p) - L(*args_m)) / (2 * e)
+            assert abs(fd - g[k][m]) <= 1e-7 * max(abs(fd), 1e-3 * np.abs(g[k]).max()), (k, m)
+
+
 def test_param_defaults_follow_reference(ads):
     a = ads.AcousticPropagatorParams()
     assert (a.NX, a.NY, a.NSTEP, a.NPOINTS_PML, a.vp_ref, a.Rcoef) == (101, 641, 4000, 12, 1000.0, 0.001)
