@@ -108,6 +108,7 @@ _SIGS = {
     "ads_acoustic_plan_gradient": [P, P, P, P, P, P, P],
     "ads_acoustic_plan_gradient_ex": [P, P, P, P, P, P, P, P],
     "ads_acoustic_plan_source_offset": [P, I64],
+    "ads_acoustic_plan_set_source_values": [P, I64, P, P],
     "ads_acoustic_forward": [P, P, P, P, P],
     "ads_acoustic_gradient": [P, P, P, P, P, P, P],
     "ads_elastic_plan_create": [P, P, P, I64, P],
@@ -119,6 +120,7 @@ _SIGS = {
     "ads_elastic_plan_resident_segments": [P],
     "ads_elastic_plan_gradient_ex": [P, P, P, P, P, P, P, P, P, P, P, P],
     "ads_elastic_plan_source_offset": [P, I64],
+    "ads_elastic_plan_set_source_values": [P, I64, P, P],
     "ads_elastic_plan_forward": [P, P, P, P, P, P],
     "ads_elastic_plan_gradient": [P, P, P, P, P, P, P, P, P, P, P],
     "ads_elastic_plan_profile": [P, P, P, P, P, P],

@@ -251,6 +251,21 @@ class AcousticPlan:
         call("ads_acoustic_plan_forward", self._h, _ptr(vp), _ptr(tr), _stream())
         return tr[:self.trace_count]
 
+    def set_source_values(self, shot, srcv):
+        """Replace shot `shot`'s source wavelets in place (same cells, no plan
+        rebuild): srcv is a CUDA tensor of at least (nstep, nsrc), as at
+        creation.  Ordered on the current stream, like the plan's calls."""
+        _require_cuda(srcv)
+        v = srcv
+        if 0 <= shot < len(self.shots):  # (the library rejects other indices)
+            s = self.shots[shot]
+            n, m = int(s["nstep"]), len(s["srci"])
+            if m:
+                v = srcv.to(torch.float64).reshape(-1, m)[:n].contiguous()
+                if v.shape[0] < n:
+                    raise ValueError(f"srcv has {v.shape[0]} rows, shot {shot} needs {n}")
+        call("ads_acoustic_plan_set_source_values", self._h, shot, _ptr(v), _stream())
+
     def gradient(self, vp, observed, want_traces=False, want_source_grad=False):
         """(loss, grad_vp[, traces][, grad_srcv]): grad_srcv is a list of per-shot
         (nstep, nsrc) FP64 tensors, d loss / d srcv (the gradient the reference's

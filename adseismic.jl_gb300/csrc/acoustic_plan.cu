@@ -1198,6 +1198,8 @@ struct AcPlanBase {
   virtual int gradient(const double* vp, const void* obs, double* loss, double* grad,
                        void* traces_out, cudaStream_t st, double* grad_srcv) = 0;
   virtual int profile(const double* vp, const void* obs, double* out, cudaStream_t st) = 0;
+  // new wavelets for a shot's sources (device FP64, (nstep, nsrc) row-major)
+  virtual int set_source_values(int64_t shot, const double* srcv, cudaStream_t st) = 0;
   std::vector<int64_t> trace_off;
   int64_t trace_total = 0;
   std::vector<int64_t> src_off;  // per caller shot: offset of its (nstep, nsrc) block
@@ -1222,6 +1224,8 @@ struct AcPlan final : AcPlanBase {
   int ri = 8;         // rows per thread
   int nseg_max = 0;
   std::vector<int> order;         // shot order (record length descending)
+  std::vector<T*> srcv_dev;        // per caller shot: its wavelets times dt^2
+  std::vector<int64_t> srcv_n;     // per caller shot: nstep * nsrc
   std::vector<int> nstep;         // per sorted shot
   std::vector<int> nxs;           // per sorted shot: window width
   int ri_f = 8;                    // rows per thread of the forward tiles
@@ -1315,6 +1319,12 @@ struct AcPlan final : AcPlanBase {
   std::vector<int64_t> cells_prefix;  // interior cells of the first n sorted shots
   int64_t cells_upto(int n) const { return n <= 0 ? 0 : cells_prefix[n - 1]; }
   int profile(const double* vp, const void* obs, double* out, cudaStream_t st) override;
+  int set_source_values(int64_t shot, const double* srcv, cudaStream_t st) override {
+    ADS_REQUIRE(shot >= 0 && shot < nshots, "shot %lld out of range [0, %d)", (long long)shot,
+                nshots);
+    ADS_REQUIRE(srcv || srcv_n[shot] == 0, "null srcv");
+    return cast_scaled(srcv_dev[shot], srcv, srcv_n[shot], cfg.dt * cfg.dt, st);
+  }
   // number of sorted shots with nstep >= t
   int shots_with_nstep_ge(int t) const {
     int n = 0;
@@ -1693,6 +1703,8 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   d_tb_map = (int*)(pool + tbm_off);
   // per-shot structs and host-side data (profiles, scaled wavelets)
   hshots.resize(ns);
+  srcv_dev.assign(ns, nullptr);
+  srcv_n.assign(ns, 0);
   std::vector<double> sx, ty;
   std::vector<std::vector<T>> host_bufs;
   // trace offsets in sorted order
@@ -1738,6 +1750,8 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
                                sizeof(CellRef) * sl.size(), cudaMemcpyHostToDevice, st));
     }
     d.srcv = (const T*)(pool + offs[s].srcv);
+    srcv_dev[order[s]] = (T*)d.srcv;
+    srcv_n[order[s]] = h.nstep * h.nsrc;
     d.traces = d_traces + trace_off[order[s]];
     d.resid = d_resid + trace_off[order[s]];
     sx = hsx[s];
@@ -2455,6 +2469,12 @@ int ads_acoustic_plan_gradient_ex(ads_acoustic_plan* plan, const double* vp,
   ADS_REQUIRE(plan, "null plan");
   return plan->impl->gradient(vp, observed, loss, grad_vp, traces_out, (cudaStream_t)stream,
                               grad_srcv);
+}
+
+int ads_acoustic_plan_set_source_values(ads_acoustic_plan* plan, int64_t shot,
+                                        const double* srcv, ads_stream_t stream) {
+  ADS_REQUIRE(plan, "null plan");
+  return plan->impl->set_source_values(shot, srcv, (cudaStream_t)stream);
 }
 
 int64_t ads_acoustic_plan_source_offset(const ads_acoustic_plan* plan, int64_t shot) {

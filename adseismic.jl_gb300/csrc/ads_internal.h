@@ -49,6 +49,10 @@ void set_launch_counting(bool on);
 // Fail loudly when no usable device is present (no CPU fallback exists).
 int require_device();
 
+// out[e] = (T)(in[e] * scale) for e < n, launched on st (one kernel).
+int cast_scaled(float* out, const double* in, int64_t n, double scale, cudaStream_t st);
+int cast_scaled(double* out, const double* in, int64_t n, double scale, cudaStream_t st);
+
 inline int64_t div_up(int64_t a, int64_t b) { return (a + b - 1) / b; }
 inline int64_t round_up(int64_t a, int64_t b) { return div_up(a, b) * b; }
 

@@ -1,4 +1,5 @@
 // common.cu -- error state, version, launch accounting and host-side PML setup.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -127,6 +128,33 @@ void elastic_cpml(int64_t NX, int64_t NY, double dx, double dy, double dt, int64
       }
     }
   }
+}
+
+// out[e] = (T)(in[e] * scale): a plan's source wavelets from a caller's FP64
+// device array, rounded as plan creation rounds them on the host.
+template <typename T>
+__global__ void k_cast_scaled(T* __restrict__ out, const double* __restrict__ in, int64_t n,
+                              double scale) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    out[e] = (T)(in[e] * scale);
+}
+
+template <typename T>
+static int cast_scaled(T* out, const double* in, int64_t n, double scale, cudaStream_t st) {
+  if (n <= 0) return ADS_OK;
+  const int64_t blocks = std::min<int64_t>(div_up(n, 256), 152 * 16);
+  k_cast_scaled<T><<<(unsigned)blocks, 256, 0, st>>>(out, in, n, scale);
+  ADS_LAUNCHED(1);
+  return ADS_OK;
+}
+
+int cast_scaled(float* out, const double* in, int64_t n, double scale, cudaStream_t st) {
+  return cast_scaled<float>(out, in, n, scale, st);
+}
+
+int cast_scaled(double* out, const double* in, int64_t n, double scale, cudaStream_t st) {
+  return cast_scaled<double>(out, in, n, scale, st);
 }
 
 }  // namespace ads

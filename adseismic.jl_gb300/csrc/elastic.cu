@@ -1618,6 +1618,8 @@ struct ElPlanBase {
   virtual int gradient(const double* l, const double* m, const double* r, const void* obs,
                        double* loss, double* gl, double* gm, double* gr, void* tr_out,
                        cudaStream_t st, double* grad_srcv) = 0;
+  // new wavelets for a shot's sources (device FP64, (NSTEP, nsrc) row-major)
+  virtual int set_source_values(int64_t shot, const double* srcv, cudaStream_t st) = 0;
   std::vector<int64_t> trace_off;
   std::vector<int64_t> src_off;  // per shot: offset of its (NSTEP, nsrc) grad_srcv block
   int64_t src_total = 0;
@@ -1631,6 +1633,14 @@ template <typename T>
 struct ElPlan final : ElPlanBase {
   ads_elastic_config cfg{};
   int nshots = 0, K = 0, nseg = 0, NX = 0, NY = 0, NSTEP = 0;
+  std::vector<T*> srcv_dev;     // per shot: its wavelets, (NSTEP, nsrc)
+  std::vector<int64_t> srcv_n;  // per shot: NSTEP * nsrc
+  int set_source_values(int64_t shot, const double* srcv, cudaStream_t st) override {
+    ADS_REQUIRE(shot >= 0 && shot < nshots, "shot %lld out of range [0, %d)", (long long)shot,
+                nshots);
+    ADS_REQUIRE(srcv || srcv_n[shot] == 0, "null srcv");
+    return cast_scaled(srcv_dev[shot], srcv, srcv_n[shot], 1.0, st);
+  }
   int ncolw = 0, rows_w = 0, nwt = 0;  // warp strips of the row-streaming step kernels
   // Resident segments res_seg .. nseg-1: the forward loop stores their steps'
   // strains / accelerations (store slot K + n - a_res, a_res = 1 + res_seg K)
@@ -2018,6 +2028,8 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
                     (const T*)(pool + prof_o));
   // shots
   std::vector<ElShot<T>> hs(ns);
+  srcv_dev.assign(ns, nullptr);
+  srcv_n.assign(ns, 0);
   std::vector<std::vector<char>> stage;
   for (int s = 0; s < ns; s++) {
     const ads_elastic_shot& h = shots[s];
@@ -2039,6 +2051,8 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
     d.traces = d_traces + trace_off[s];
     d.resid = d_resid + trace_off[s];
     d.srcv = (const T*)(pool + o[s].srcv);
+    srcv_dev[s] = (T*)d.srcv;
+    srcv_n[s] = (int64_t)NSTEP * h.nsrc;
     d.src_cell = (const int64_t*)(pool + o[s].scell);
     d.src_type = (const int*)(pool + o[s].stype);
     d.src_dual = (const int*)(pool + o[s].sdual);
@@ -2767,6 +2781,12 @@ int ads_elastic_plan_gradient_ex(ads_elastic_plan* plan, const double* lambda,
   ADS_REQUIRE(plan, "null plan");
   return plan->impl->gradient(lambda, mu, rho, observed, loss, grad_lambda, grad_mu, grad_rho,
                               traces_out, (cudaStream_t)stream, grad_srcv);
+}
+
+int ads_elastic_plan_set_source_values(ads_elastic_plan* plan, int64_t shot,
+                                       const double* srcv, ads_stream_t stream) {
+  ADS_REQUIRE(plan, "null plan");
+  return plan->impl->set_source_values(shot, srcv, (cudaStream_t)stream);
 }
 
 int64_t ads_elastic_plan_source_offset(const ads_elastic_plan* plan, int64_t shot) {

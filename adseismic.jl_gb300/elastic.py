@@ -228,6 +228,20 @@ class ElasticPlan:
              out.ctypes.data_as(C.c_void_p), _stream())
         return {k: (float(out[2 * i]), float(out[2 * i + 1])) for i, k in enumerate(self.KERNELS)}
 
+    def set_source_values(self, shot, srcv):
+        """Replace shot `shot`'s source wavelets in place (same cells and types,
+        no plan rebuild): srcv is a CUDA tensor of at least (NSTEP, nsrc), as at
+        creation.  Ordered on the current stream, like the plan's calls."""
+        _require_cuda(srcv)
+        v = srcv
+        if 0 <= shot < len(self.shots):  # (the library rejects other indices)
+            n, m = int(self.param.NSTEP), len(self.shots[shot]["srci"])
+            if m:
+                v = srcv.to(torch.float64).reshape(-1, m)[:n].contiguous()
+                if v.shape[0] < n:
+                    raise ValueError(f"srcv has {v.shape[0]} rows, NSTEP = {n}")
+        call("ads_elastic_plan_set_source_values", self._h, shot, _ptr(v), _stream())
+
     def gradient(self, lam, mu, rho, observed, want_traces=False, want_source_grad=False):
         """(loss, grad_lambda, grad_mu, grad_rho[, traces][, grad_srcv]): grad_srcv is
         a list of per-shot (NSTEP, nsrc) FP64 tensors, d loss / d srcv (the gradient

@@ -74,3 +74,77 @@ def fwi_lbfgs(plan, vp0, observed, max_iter=20, callback=None, vmin=None, vmax=N
     x, losses = LBFGS(fg, vp0.reshape(-1) / scale, callback=callback, max_iter=max_iter,
                       bounds=bounds)
     return x.reshape(shape) * scale, losses
+
+
+
+def source_objective(plan, param, vp, observed, sigma=0.5, source_scale=1.0, shot=0):
+    """The objective of the reference's source location and wavelet inversion
+    (examples/invert_source_location_time_function/AcousticFWI-LayerModel-Source.jl):
+    unknowns z = (a, b, w) with x = sigmoid(a) DELTAX NX, y = sigmoid(b)
+    DELTAY NY and wavelet v = w source_scale; the source is the Gaussian
+    variable_source(param, x, y, v; sigma).
+
+    `plan` is an AcousticPlan whose shot `shot` was created with the cells of
+    that source (variable_source's srci / srcj, which do not depend on x, y,
+    v) and whose window `param` describes (NX = nx, NY = MY, NSTEP = nstep).
+    Returns (fg, unpack): fg(z) -> (loss, d loss / d z) writes v magn^T into
+    the plan on the device (set_source_values), runs one gradient with
+    d loss / d srcv and applies variable_source_grad and the sigmoid chain
+    rule (the model vp stays fixed); unpack(z) -> (x, y, v)."""
+    import torch
+
+    from .utils import _gauss_weights, _source_cells, variable_source_grad
+
+    sig = float(sigma)
+    Lx, Ly = param.DELTAX * param.NX, param.DELTAY * param.NY
+    i, j = _source_cells(param, None)
+    dev = observed.device
+
+    def parts(z):
+        sa, sb = 1 / (1 + np.exp(-z[0])), 1 / (1 + np.exp(-z[1]))
+        return sa, sb, sa * Lx, sb * Ly, np.asarray(z[2:], dtype=np.float64) * source_scale
+
+    def fg(z):
+        sa, sb, x, y, v = parts(z)
+        magn, _, _ = _gauss_weights(param, x, y, sig, i, j)
+        srcv = (torch.as_tensor(v, device=dev)[:, None] *
+                torch.as_tensor(magn, device=dev)[None, :])
+        plan.set_source_values(shot, srcv)
+        loss, _, gs = plan.gradient(vp, observed, want_source_grad=True)
+        gx, gy, gv = variable_source_grad(param, x, y, v, gs[shot], sigma=sig)
+        gv = gv.cpu().numpy() if isinstance(gv, torch.Tensor) else gv
+        g = np.concatenate([[gx * Lx * sa * (1 - sa), gy * Ly * sb * (1 - sb)],
+                            gv * source_scale])
+        return float(loss), g
+
+    def unpack(z):
+        return parts(z)[2:]
+
+    return fg, unpack
+
+
+def source_lbfgs(plan, param, vp, observed, x0, y0, v0, sigma=0.5, source_scale=1.0, shot=0,
+                 max_iter=20, callback=None):
+    """L-BFGS over source_objective from the source position (x0, y0) and
+    wavelet v0 (length >= NSTEP).  The optimiser sees the loss divided by its
+    starting value, so its stopping tolerances are relative; the callback and
+    the returned history carry the loss itself.  Returns (x, y, v, losses)."""
+    fg, unpack = source_objective(plan, param, vp, observed, sigma, source_scale, shot)
+    Lx, Ly = param.DELTAX * param.NX, param.DELTAY * param.NY
+
+    def logit(p):
+        return float(np.log(p / (1 - p)))
+
+    z0 = np.concatenate([[logit(x0 / Lx), logit(y0 / Ly)],
+                         np.asarray(v0, dtype=np.float64).reshape(-1) / source_scale])
+    L0 = fg(z0)[0]
+    scale = 1.0 / L0 if L0 > 0 else 1.0
+
+    def fgn(z):
+        loss, g = fg(z)
+        return loss * scale, g * scale
+
+    cb = None if callback is None else (lambda z, it, loss: callback(z, it, loss / scale))
+    z, losses = LBFGS(fgn, z0, callback=cb, max_iter=max_iter)
+    x, y, v = unpack(z)
+    return x, y, v, [l / scale for l in losses]

@@ -320,6 +320,15 @@ int ads_acoustic_plan_gradient_ex(ads_acoustic_plan* plan, const double* vp,
                                   double* grad_srcv, void* traces_out, ads_stream_t stream);
 /* Offset (doubles) of a shot's block in grad_srcv; -1 for a bad index. */
 int64_t ads_acoustic_plan_source_offset(const ads_acoustic_plan* plan, int64_t shot);
+/* Replace shot `shot`'s source wavelets (same cells) in place, with no plan
+ * rebuild: srcv is DEVICE memory, (nstep, nsrc) FP64 row-major as srcv was at
+ * creation, read on `stream`; later calls on that stream use the new values,
+ * stored exactly as plan creation stores them.  This is what assigning the
+ * trainable wavelet of variable_source (src/Utils.jl:603-640) does between
+ * the reference's session runs, as in its source-location and wavelet
+ * inversion.  ADS_ERR_INVALID for a bad shot index or a null srcv. */
+int ads_acoustic_plan_set_source_values(ads_acoustic_plan* plan, int64_t shot,
+                                        const double* srcv, ads_stream_t stream);
 
 /* One-shot conveniences (plan + run + destroy; they synchronise `stream`). */
 int ads_acoustic_forward(const ads_acoustic_config* cfg, const ads_acoustic_shot* shot,
@@ -404,6 +413,10 @@ int ads_elastic_plan_gradient_ex(ads_elastic_plan* plan, const double* lambda,
                                  ads_stream_t stream);
 /* Offset (doubles) of a shot's block in grad_srcv; -1 for a bad index. */
 int64_t ads_elastic_plan_source_offset(const ads_elastic_plan* plan, int64_t shot);
+/* As ads_acoustic_plan_set_source_values: srcv is DEVICE memory, (NSTEP, nsrc)
+ * FP64 row-major. */
+int ads_elastic_plan_set_source_values(ads_elastic_plan* plan, int64_t shot,
+                                       const double* srcv, ads_stream_t stream);
 /* lambda, mu, rho: device, N doubles. */
 int ads_elastic_plan_forward(ads_elastic_plan* plan, const double* lambda,
                              const double* mu, const double* rho, void* traces,

@@ -244,3 +244,35 @@ def test_source_time_gradient_vs_oracle(ads, orc, cuda, precision, tol, resident
     frame = dict(shots[1], srci=np.array([1]))  # sxx on row 0: read, never updated
     with pytest.raises(ads.AdsError, match="padded frame"):
         ads.ElasticPlan(p, [frame], precision=precision, ckpt_every=9, source_gradient=True)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_set_source_values_matches_a_fresh_plan(ads, cuda, precision):
+    """Wavelets replaced in place (a source on the padded frame, which is
+    added to both state buffers; an ignored type; a shot without sources)
+    give bitwise the traces, loss and gradients of a plan created with them."""
+    g = golden("elastic_small.npz")
+    p = params(ads, g, T=40)
+    rng = np.random.default_rng(9)
+    base = dict(rcvi=g["rcvi"], rcvj=g["rcvj"], rcvtype=g["rcvtype"])
+    shots = [dict(base, srci=g["srci"], srcj=g["srcj"], srctype=g["srctype"],
+                  srcv=rng.standard_normal((40, len(g["srci"]))) * 1e2),
+             dict(base, srci=[1, 14, 9], srcj=[5, 11, 9], srctype=[2, 4, 7],
+                  srcv=rng.standard_normal((40, 3)) * 1e2),
+             dict(base, srci=[], srcj=[], srctype=[], srcv=np.zeros((40, 0)))]
+    zeroed = [dict(s, srcv=np.zeros_like(s["srcv"])) for s in shots]
+    a = ads.ElasticPlan(p, shots, precision=precision, ckpt_every=9)
+    b = ads.ElasticPlan(p, zeroed, precision=precision, ckpt_every=9)
+    for k, s in enumerate(shots):
+        b.set_source_values(k, torch.as_tensor(s["srcv"], dtype=torch.float64, device=cuda))
+    t = lambda x: torch.as_tensor(x, dtype=torch.float64, device=cuda)
+    m = (t(g["lam"]), t(g["mu"]), t(g["rho"]))
+    ta, tb = a.forward(*m), b.forward(*m)
+    assert torch.equal(ta, tb)
+    ra, rb = a.gradient(*m, ta * 0.9), b.gradient(*m, ta * 0.9)
+    torch.cuda.synchronize()
+    assert all(torch.equal(x, y) for x, y in zip(ra, rb))
+    with pytest.raises(ads.AdsError):
+        b.set_source_values(-1, t(shots[0]["srcv"]))
+    a.close()
+    b.close()

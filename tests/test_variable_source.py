@@ -95,3 +95,73 @@ def test_elastic_location_gradient_finite_differences(ads, orc):
     fy = (loss(x, y + e)[0] - loss(x, y - e)[0]) / (2 * e)
     assert abs(fx - gx) <= 1e-6 * abs(fx) and abs(fy - gy) <= 1e-6 * abs(fy), (fx, gx, fy, gy)
     assert gv.shape == v.shape
+
+
+class _OraclePlan:
+    """A CPU stand-in for an acoustic plan with one shot, computed by the
+    oracle: the two calls source_objective makes (set_source_values and
+    gradient with d loss / d srcv)."""
+
+    def __init__(self, orc, p, sig, tau, vp, i, j, rcvi, rcvj):
+        self.orc, self.p, self.sig, self.tau = orc, p, sig, tau
+        self.i, self.j, self.rcvi, self.rcvj = i, j, rcvi, rcvj
+        self.srcv = None
+
+    def set_source_values(self, shot, srcv):
+        assert shot == 0
+        self.srcv = srcv.cpu().numpy()[:self.p.NSTEP]
+
+    def gradient(self, vp, observed, want_source_grad=False):
+        import torch
+
+        p = self.p
+        L, g, G = self.orc.acoustic_gradient(p.NX, p.NY, p.NSTEP, p.DELTAT, p.DELTAX, p.DELTAY,
+                                             self.sig, self.tau, vp.numpy().reshape(-1),
+                                             self.i, self.j, self.srcv, self.rcvi, self.rcvj,
+                                             observed.numpy(), want_src=True)
+        return torch.tensor(L, dtype=torch.float64), torch.as_tensor(g), [torch.as_tensor(G)]
+
+
+def _source_case(ads, orc):
+    import torch
+
+    rng = np.random.default_rng(21)
+    p = ads.AcousticPropagatorParams(NX=20, NY=16, NSTEP=60, DELTAX=10.0, DELTAY=10.0,
+                                     DELTAT=1e-3)
+    vp = 2000 + 300 * rng.random((p.NX + 2) * (p.NY + 2))
+    s, t = orc.acoustic_pml(p.NX, p.NY, 10.0, 10.0, 4, 2000.0)
+    rcvi, rcvj = np.arange(3, 21), np.full(18, 3)
+    v = ads.Ricker(p, 3.0, 10.0)
+    i, j, sv = ads.variable_source(p, 103.0, 86.0, v * 1e3, sigma=0.5)
+    obs = orc.acoustic_forward(p.NX, p.NY, p.NSTEP, p.DELTAT, 10.0, 10.0, s, t, vp, i, j, sv,
+                               rcvi, rcvj)
+    plan = _OraclePlan(orc, p, s, t, vp, i, j, rcvi, rcvj)
+    return p, plan, torch.as_tensor(vp), torch.as_tensor(obs), v
+
+
+def test_source_objective_gradient_finite_differences(ads, orc):
+    """d loss / d (a, b, w) of the source inversion objective (sigmoid
+    position, scaled wavelet) against central differences."""
+    p, plan, vp, obs, v = _source_case(ads, orc)
+    fg, unpack = ads.source_objective(plan, p, vp, obs, sigma=0.5, source_scale=1e3)
+    z = np.concatenate([[0.3, 0.1], 0.9 * v])
+    L, g = fg(z)
+    x, y, vv = unpack(z)
+    assert abs(x - 200 / (1 + np.exp(-0.3))) < 1e-12 and np.allclose(vv, 0.9e3 * v)
+    for k, e in [(0, 1e-5), (1, 1e-5), (12, 1e-3), (30, 1e-3)]:
+        zp, zm = z.copy(), z.copy()
+        zp[k] += e
+        zm[k] -= e
+        fd = (fg(zp)[0] - fg(zm)[0]) / (2 * e)
+        assert abs(fd - g[k]) <= 1e-6 * abs(fd) + 1e-12 * L, (k, fd, g[k])
+
+
+def test_source_lbfgs_recovers_location(ads, orc):
+    """The inversion loop moves a misplaced Gaussian source back onto the
+    one that made the data (wavelet known up to a 20% scale)."""
+    p, plan, vp, obs, v = _source_case(ads, orc)
+    x, y, vv, losses = ads.source_lbfgs(plan, p, vp, obs, 116.0, 77.0, 0.8 * v, sigma=0.5,
+                                        source_scale=1e3, max_iter=25)
+    err0 = np.hypot(116.0 - 103.0, 77.0 - 86.0)
+    assert losses[-1] < 1e-3 * losses[0], losses
+    assert np.hypot(x - 103.0, y - 86.0) < 0.05 * err0, (x, y)
