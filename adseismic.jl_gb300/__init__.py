@@ -21,7 +21,7 @@ from .elastic import SimulatedObservation as ElasticSimulatedObservation
 from .elastic import compute_PML_Params as compute_elastic_PML_Params
 from .io import (load_acoustic_model, load_acoustic_receiver, load_acoustic_source,
                  load_elastic_model, load_elastic_receiver, load_elastic_source, load_params)
-from .optim import LBFGS, fwi_lbfgs, source_lbfgs, source_objective
+from .optim import LBFGS, fwi_lbfgs, source_lbfgs, source_objective, wavelet_lbfgs
 from .utils import (Gauss, Ricker, compute_lame_parameters, compute_properties,
                     compute_properties_grad,
                     folded_layer_model, gaussian_smooth, layered_gaussian_model,

@@ -148,3 +148,46 @@ def source_lbfgs(plan, param, vp, observed, x0, y0, v0, sigma=0.5, source_scale=
     z, losses = LBFGS(fgn, z0, callback=cb, max_iter=max_iter)
     x, y, v = unpack(z)
     return x, y, v, [l / scale for l in losses]
+
+
+def wavelet_lbfgs(plan, model, observed, v0, source_scale=1.0, shot=0, max_iter=20,
+                  callback=None):
+    """Wavelet (rupture-process) inversion with the parameterisation of the
+    reference's example (examples/invert_rupture_process/AcousticFWI-LayerModel-Rupture.jl):
+    the unknown is shot `shot`'s wavelet matrix w, srcv = w source_scale, as
+    variable_source's index form (src/Utils.jl:636-640) makes it trainable.
+
+    `plan` is an AcousticPlan (model = vp) or an ElasticPlan created with
+    source_gradient (model = (lambda, mu, rho)); v0 is the starting srcv,
+    (rows, nsrc) with rows >= the shot's step count.  Every evaluation writes
+    srcv into the plan (set_source_values) and takes d loss / d srcv from one
+    gradient; rows the plan never injects have a zero gradient.  The
+    optimiser sees the loss divided by its starting value.  Returns
+    (srcv, losses)."""
+    import torch
+
+    model = (model,) if isinstance(model, torch.Tensor) else tuple(model)
+    v0 = np.asarray(v0, dtype=np.float64)
+    shape = v0.shape
+    dev = observed.device
+
+    def fg(z):
+        srcv = torch.as_tensor(z.reshape(shape) * source_scale, device=dev)
+        plan.set_source_values(shot, srcv)
+        out = plan.gradient(*model, observed, want_source_grad=True)
+        G = out[-1][shot]
+        g = np.zeros(shape)
+        g[:G.shape[0]] = G.cpu().numpy()
+        return float(out[0]), g.reshape(-1) * source_scale
+
+    z0 = v0.reshape(-1) / source_scale
+    L0 = fg(z0)[0]
+    scale = 1.0 / L0 if L0 > 0 else 1.0
+
+    def fgn(z):
+        loss, g = fg(z)
+        return loss * scale, g * scale
+
+    cb = None if callback is None else (lambda z, it, loss: callback(z, it, loss / scale))
+    z, losses = LBFGS(fgn, z0, callback=cb, max_iter=max_iter)
+    return z.reshape(shape) * source_scale, [l / scale for l in losses]
