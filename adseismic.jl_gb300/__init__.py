@@ -11,7 +11,7 @@ from .build import build_library, LIB_PATH
 from .acoustic import (AcousticMisfit, AcousticOneStep, AcousticPlan, AcousticPropagator,
                        AcousticPropagatorParams, AcousticPropagatorSolver, AcousticReceiver,
                        AcousticSource, SimulatedObservation, acoustic_one_step,
-                       acoustic_one_step_grad, compute_loss_and_grads_GPU,
+                       acoustic_one_step_grad, compute_forward_GPU, compute_loss_and_grads_GPU,
                        dropin_loss_and_grad)
 from .acoustic import compute_PML_Params as compute_acoustic_PML_Params
 from .elastic import (ElasticPlan, ElasticPropagator, ElasticPropagatorParams,

@@ -333,10 +333,36 @@ def SimulatedObservation(ap: AcousticPropagator, rcv: AcousticReceiver):
     return rcv.rcvv
 
 
+def compute_forward_GPU(param: AcousticPropagatorParams, srcs, rcvs, vp, precision="f64"):
+    """src/Utils.jl:574-601 for one GPU: every shot's (NSTEP+1, nrcv) traces
+    from one batched plan.  With ElasticPropagatorParams the model is
+    (rho, lambda, mu), as the reference's elastic solver takes it."""
+    if not isinstance(param, AcousticPropagatorParams):
+        from .elastic import compute_forward_GPU as elastic_forward
+
+        return elastic_forward(param, srcs, rcvs, vp, precision)
+    shots = [_shot_dict(param, s, r) for s, r in zip(srcs, rcvs)]
+    plan = AcousticPlan(param.NX, param.NY, param.DELTAX, param.DELTAY, param.DELTAT, shots,
+                        npml=param.NPOINTS_PML, Rcoef=param.Rcoef, vp_ref=param.vp_ref,
+                        use_pml=param.use_pml, precision=precision, use_graph=False)
+    vp = torch.as_tensor(vp, dtype=torch.float64, device="cuda").reshape(param.NX + 2,
+                                                                         param.NY + 2)
+    out = [t.clone() for t in plan.split_traces(plan.forward(vp))]
+    torch.cuda.current_stream().synchronize()
+    plan.close()
+    return out
+
+
 def compute_loss_and_grads_GPU(param: AcousticPropagatorParams, srcs, rcvs, Rs, vp,
                                precision="f64", ckpt_every=0):
     """src/Utils.jl:300-332 for one GPU: loss = sum over shots of sum((rcvv - Rs)^2)
-    and its gradient w.r.t. vp, all shots in one batched plan."""
+    and its gradient w.r.t. vp, all shots in one batched plan.  With
+    ElasticPropagatorParams the model is (rho, lambda, mu) and the result
+    (loss, grad_lambda, grad_mu, grad_rho)."""
+    if not isinstance(param, AcousticPropagatorParams):
+        from .elastic import compute_loss_and_grads_GPU as elastic_grads
+
+        return elastic_grads(param, srcs, rcvs, Rs, vp, precision, ckpt_every)
     shots = [_shot_dict(param, s, r) for s, r in zip(srcs, rcvs)]
     plan = AcousticPlan(param.NX, param.NY, param.DELTAX, param.DELTAY, param.DELTAT, shots,
                         npml=param.NPOINTS_PML, Rcoef=param.Rcoef, vp_ref=param.vp_ref,

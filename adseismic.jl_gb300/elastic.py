@@ -305,3 +305,41 @@ def SimulatedObservation(ep: ElasticPropagator, rcv: ElasticReceiver):
     plan.close()
     rcv.rcvv = tr.view(len(rcv.rcvi), ep.param.NSTEP + 1)
     return rcv.rcvv
+
+
+def _batched_plan(param, srcs, rcvs, precision, ckpt_every=0):
+    return ElasticPlan(param, [_eshot(s, r) for s, r in zip(srcs, rcvs)], precision=precision,
+                       use_graph=False, ckpt_every=ckpt_every)
+
+
+def _materials(model):
+    """(rho, lambda, mu) in the reference's argument order -> FP64 CUDA vectors."""
+    rho, lam, mu = model
+    f = lambda a: torch.as_tensor(a, dtype=torch.float64, device="cuda").reshape(-1)
+    return f(lam), f(mu), f(rho)
+
+
+def compute_forward_GPU(param: ElasticPropagatorParams, srcs, rcvs, model, precision="f64"):
+    """src/Utils.jl:574-601 with elastic sources, one GPU: every shot's
+    (nrcv, NSTEP+1) traces from one batched plan; model = (rho, lambda, mu)."""
+    plan = _batched_plan(param, srcs, rcvs, precision)
+    tr = plan.forward(*_materials(model))
+    out = [t.clone() for t in plan.split_traces(tr)]
+    torch.cuda.current_stream().synchronize()
+    plan.close()
+    return out
+
+
+def compute_loss_and_grads_GPU(param: ElasticPropagatorParams, srcs, rcvs, Rs, model,
+                               precision="f64", ckpt_every=0):
+    """src/Utils.jl:300-332 with elastic sources, one GPU: loss = sum over
+    shots of sum((rcvv - Rs)^2) and its gradients with respect to lambda, mu
+    and rho, all shots in one batched plan; model = (rho, lambda, mu), Rs per
+    shot (nrcv, NSTEP+1).  Returns (loss, grad_lambda, grad_mu, grad_rho);
+    compute_properties_grad turns these into vp / vs / rho gradients."""
+    plan = _batched_plan(param, srcs, rcvs, precision, ckpt_every)
+    obs = plan.pack([torch.as_tensor(r, device="cuda") for r in Rs])
+    out = plan.gradient(*_materials(model), obs)
+    torch.cuda.current_stream().synchronize()
+    plan.close()
+    return out

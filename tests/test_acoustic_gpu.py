@@ -430,6 +430,21 @@ def test_source_lbfgs_on_the_plan(ads, cuda):
     plan.close()
 
 
+def test_compute_forward_GPU_matches_the_golden_traces(ads, cuda):
+    """compute_forward_GPU (src/Utils.jl:574-601): every shot's traces from
+    one batched plan, against the reference's golden traces."""
+    g = golden("acoustic_loop.npz")
+    NX, NY, Tn, _ = loop_case(g)
+    p = ads.AcousticPropagatorParams(NX=NX, NY=NY, NSTEP=Tn, DELTAX=float(g["h"]),
+                                     DELTAY=float(g["h"]), DELTAT=float(g["dt"]),
+                                     NPOINTS_PML=int(g["npml"]), vp_ref=float(g["vp_ref"]))
+    src = ads.AcousticSource(g["srci"], g["srcj"], g["srcv"])
+    rcv = ads.AcousticReceiver(g["rcvi"], g["rcvj"])
+    tr = ads.compute_forward_GPU(p, [src, src], [rcv, rcv], g["vp"])
+    assert len(tr) == 2 and tuple(tr[0].shape) == g["rcvv"].shape
+    assert rel(tr[0].cpu().numpy(), g["rcvv"]) <= TOL64 and torch.equal(tr[0], tr[1])
+
+
 def test_fwi_lbfgs_reduces_misfit(ads, cuda):
     """The L-BFGS FWI loop on the batched FP32 gradient (4 shots): the misfit
     falls well below its starting value and the loss history is recorded."""
