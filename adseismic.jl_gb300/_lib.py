@@ -124,6 +124,8 @@ _SIGS = {
     "ads_elastic_plan_forward": [P, P, P, P, P, P],
     "ads_elastic_plan_gradient": [P, P, P, P, P, P, P, P, P, P, P],
     "ads_elastic_plan_profile": [P, P, P, P, P, P],
+    "ads_elastic_forward": [P, P, P, P, P, P, P],
+    "ads_elastic_gradient": [P, P, P, P, P, P, P, P, P, P, P],
     "ads_device_index_errors": [I32, P],
     "ads_last_error": [],
     "ads_version": [],

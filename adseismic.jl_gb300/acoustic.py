@@ -201,6 +201,7 @@ class AcousticPlan:
         st = stream if stream is not None else _stream()
         call("ads_acoustic_plan_create", C.byref(h), C.byref(cfg), arr, len(shots), st)
         self._h = h
+        self._cfg, self._arr = cfg, arr  # what the one-shot entry points take
         L = lib()
         self.trace_count = L.ads_acoustic_plan_trace_count(h)
         self.trace_offsets = [L.ads_acoustic_plan_trace_offset(h, k) for k in range(len(shots))]

@@ -2484,6 +2484,7 @@ int64_t ads_acoustic_plan_source_offset(const ads_acoustic_plan* plan, int64_t s
 
 int ads_acoustic_forward(const ads_acoustic_config* cfg, const ads_acoustic_shot* shot,
                          const double* vp, void* traces, ads_stream_t stream) {
+  ADS_REQUIRE(cfg && shot, "null argument");
   ads_acoustic_plan* p = nullptr;
   ads_acoustic_config c = *cfg;
   c.use_graph = 0;
@@ -2498,6 +2499,7 @@ int ads_acoustic_forward(const ads_acoustic_config* cfg, const ads_acoustic_shot
 int ads_acoustic_gradient(const ads_acoustic_config* cfg, const ads_acoustic_shot* shot,
                           const double* vp, const void* observed, double* loss,
                           double* grad_vp, ads_stream_t stream) {
+  ADS_REQUIRE(cfg && shot, "null argument");
   ads_acoustic_plan* p = nullptr;
   ads_acoustic_config c = *cfg;
   c.use_graph = 0;

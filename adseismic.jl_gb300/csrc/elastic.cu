@@ -2800,4 +2800,36 @@ int ads_elastic_plan_profile(ads_elastic_plan* plan, const double* lambda, const
   return plan->impl->profile(lambda, mu, rho, out, (cudaStream_t)stream);
 }
 
+int ads_elastic_forward(const ads_elastic_config* cfg, const ads_elastic_shot* shot,
+                        const double* lambda, const double* mu, const double* rho,
+                        void* traces, ads_stream_t stream) {
+  ADS_REQUIRE(cfg && shot, "null argument");
+  ads_elastic_plan* p = nullptr;
+  ads_elastic_config c = *cfg;
+  c.use_graph = 0;
+  if (int e = ads_elastic_plan_create(&p, &c, shot, 1, stream)) return e;
+  int rc = ads_elastic_plan_forward(p, lambda, mu, rho, traces, stream);
+  if (rc == ADS_OK && cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess)
+    rc = fail(ADS_ERR_CUDA, "stream synchronisation failed");
+  ads_elastic_plan_destroy(p);
+  return rc;
+}
+
+int ads_elastic_gradient(const ads_elastic_config* cfg, const ads_elastic_shot* shot,
+                         const double* lambda, const double* mu, const double* rho,
+                         const void* observed, double* loss, double* grad_lambda,
+                         double* grad_mu, double* grad_rho, ads_stream_t stream) {
+  ADS_REQUIRE(cfg && shot, "null argument");
+  ads_elastic_plan* p = nullptr;
+  ads_elastic_config c = *cfg;
+  c.use_graph = 0;
+  if (int e = ads_elastic_plan_create(&p, &c, shot, 1, stream)) return e;
+  int rc = ads_elastic_plan_gradient(p, lambda, mu, rho, observed, loss, grad_lambda, grad_mu,
+                                     grad_rho, nullptr, stream);
+  if (rc == ADS_OK && cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess)
+    rc = fail(ADS_ERR_CUDA, "stream synchronisation failed");
+  ads_elastic_plan_destroy(p);
+  return rc;
+}
+
 }  // extern "C"

@@ -426,6 +426,16 @@ int ads_elastic_plan_gradient(ads_elastic_plan* plan, const double* lambda,
                               const double* mu, const double* rho, const void* observed,
                               double* loss, double* grad_lambda, double* grad_mu,
                               double* grad_rho, void* traces_out, ads_stream_t stream);
+/* One-shot conveniences (plan + run + destroy; they synchronise `stream`):
+ * ElasticPropagatorSolver + SimulatedObservation! for one source
+ * (src/Core.jl:31-94,701-712), and with the misfit and its gradients. */
+int ads_elastic_forward(const ads_elastic_config* cfg, const ads_elastic_shot* shot,
+                        const double* lambda, const double* mu, const double* rho,
+                        void* traces, ads_stream_t stream);
+int ads_elastic_gradient(const ads_elastic_config* cfg, const ads_elastic_shot* shot,
+                         const double* lambda, const double* mu, const double* rho,
+                         const void* observed, double* loss, double* grad_lambda,
+                         double* grad_mu, double* grad_rho, ads_stream_t stream);
 /* Kernel timing (no reference counterpart): every step kernel of the plan is
  * launched 20 times on the plan's buffers between CUDA events.  out: 14
  * doubles, pairs (ms per launch, interior cell-updates per launch) for the

@@ -445,6 +445,38 @@ def test_compute_forward_GPU_matches_the_golden_traces(ads, cuda):
     assert rel(tr[0].cpu().numpy(), g["rcvv"]) <= TOL64 and torch.equal(tr[0], tr[1])
 
 
+def test_one_shot_entry_points_match_the_golden(ads, cuda):
+    """ads_acoustic_forward / ads_acoustic_gradient (plan, run, destroy in one
+    call) on the reference's golden loop: bitwise the plan's own results."""
+    import ctypes
+
+    g = golden("acoustic_loop.npz")
+    NX, NY, Tn, shot = loop_case(g)
+    h, dt = float(g["h"]), float(g["dt"])
+    plan = ads.AcousticPlan(NX, NY, h, h, dt, [shot], npml=int(g["npml"]),
+                            vp_ref=float(g["vp_ref"]), precision="f64")
+    vp = T(g["vp"].reshape(NX + 2, NY + 2), cuda)
+    obs = T(g["obs"].reshape(-1), cuda)
+    tr = plan.forward(vp)
+    loss, grad = plan.gradient(vp, obs)
+    L = ads.lib()
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    tr1 = torch.empty_like(tr)
+    ads._lib.check(L.ads_acoustic_forward(ctypes.byref(plan._cfg), plan._arr, vp.data_ptr(),
+                                          tr1.data_ptr(), st))
+    loss1 = torch.empty(1, dtype=torch.float64, device=cuda)
+    grad1 = torch.empty_like(grad)
+    ads._lib.check(L.ads_acoustic_gradient(ctypes.byref(plan._cfg), plan._arr, vp.data_ptr(),
+                                           obs.data_ptr(), loss1.data_ptr(), grad1.data_ptr(),
+                                           st))
+    assert torch.equal(tr, tr1) and torch.equal(loss.reshape(1), loss1)
+    assert torch.equal(grad, grad1)
+    assert rel(tr1.cpu().numpy(), g["rcvv"].reshape(-1)) <= TOL64
+    with pytest.raises(ads.AdsError):
+        ads._lib.check(L.ads_acoustic_forward(None, plan._arr, vp.data_ptr(), tr1.data_ptr(), st))
+    plan.close()
+
+
 def test_fwi_lbfgs_reduces_misfit(ads, cuda):
     """The L-BFGS FWI loop on the batched FP32 gradient (4 shots): the misfit
     falls well below its starting value and the loss history is recorded."""

@@ -294,3 +294,34 @@ def test_julia_named_multishot_helpers(ads, cuda):
     assert abs(float(loss) - float(g["loss"])) <= 1e-12 * float(g["loss"])
     for a, k in ((gl, "grad_lambda"), (gm, "grad_mu"), (gr, "grad_rho")):
         assert rel(a.cpu().numpy(), g[k]) <= 1e-12, k
+
+
+def test_one_shot_entry_points_match_the_plan(ads, cuda):
+    """ads_elastic_forward / ads_elastic_gradient (plan, run, destroy in one
+    call): bitwise the plan's own traces, loss and gradients."""
+    import ctypes
+
+    g = golden("elastic_small.npz")
+    p = params(ads, g)
+    plan = ads.ElasticPlan(p, shots_from(g), precision="f64", ckpt_every=17)
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=cuda)
+    lam, mu, rho, obs = t(g["lam"]), t(g["mu"]), t(g["rho"]), t(g["obs"].reshape(-1))
+    tr = plan.forward(lam, mu, rho)
+    loss, gl, gm, gr = plan.gradient(lam, mu, rho, obs)
+    L = ads.lib()
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    tr1 = torch.empty_like(tr)
+    ads._lib.check(L.ads_elastic_forward(ctypes.byref(plan._cfg), plan._arr, lam.data_ptr(),
+                                         mu.data_ptr(), rho.data_ptr(), tr1.data_ptr(), st))
+    out = [torch.empty(1, dtype=torch.float64, device=cuda)] + [torch.empty_like(lam)
+                                                                 for _ in range(3)]
+    ads._lib.check(L.ads_elastic_gradient(ctypes.byref(plan._cfg), plan._arr, lam.data_ptr(),
+                                          mu.data_ptr(), rho.data_ptr(), obs.data_ptr(),
+                                          *[o.data_ptr() for o in out], st))
+    assert torch.equal(tr, tr1) and torch.equal(loss.reshape(1), out[0])
+    assert all(torch.equal(a, b) for a, b in zip((gl, gm, gr), out[1:]))
+    assert rel(tr1.cpu().numpy(), g["rcvv"].reshape(-1)) <= 1e-12
+    with pytest.raises(ads.AdsError):
+        ads._lib.check(L.ads_elastic_forward(ctypes.byref(plan._cfg), None, lam.data_ptr(),
+                                             mu.data_ptr(), rho.data_ptr(), tr1.data_ptr(), st))
+    plan.close()
