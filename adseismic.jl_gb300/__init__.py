@@ -22,8 +22,8 @@ from .elastic import compute_PML_Params as compute_elastic_PML_Params
 from .io import (load_acoustic_model, load_acoustic_receiver, load_acoustic_source,
                  load_elastic_model, load_elastic_receiver, load_elastic_source, load_params)
 from .optim import LBFGS, fwi_lbfgs, source_lbfgs, source_objective, wavelet_lbfgs
-from .utils import (Gauss, Ricker, compute_lame_parameters, compute_properties,
-                    compute_properties_grad,
+from .utils import (Gauss, Ricker, add_initial_model, compute_lame_parameters,
+                    compute_properties, compute_properties_grad, gradtest,
                     folded_layer_model, gaussian_smooth, layered_gaussian_model,
                     ricker_width_samples, variable_source, variable_source_grad)
 

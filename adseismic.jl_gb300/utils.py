@@ -61,6 +61,47 @@ def compute_properties_grad(vp, vs, rho, grad_lambda, grad_mu, grad_rho):
     return g_vp, g_vs, g_rho
 
 
+def gradtest(fg, x, direction=None, seed=0):
+    """Taylor-remainder gradient check of src/Utils.jl:260-289, without the
+    plot: with G = grad L(x) and a direction v (default uniform [0, 1) times
+    median(x), as the reference draws it), for gamma = 1e-1 .. 1e-5 returns
+    (gammas, s, w) where s = L(x + gamma v) - L(x) shrinks as O(gamma) and
+    w = s - gamma <v, G> as O(gamma^2) when G is right.  fg(x) -> (loss,
+    gradient), numpy vectors (a plan's gradient, flattened, works)."""
+    x = np.asarray(x, dtype=np.float64)
+    L, G = fg(x)
+    G = np.asarray(G, dtype=np.float64).reshape(x.shape)
+    if direction is None:
+        direction = np.random.default_rng(seed).random(x.shape) * np.median(x)
+    v = np.asarray(direction, dtype=np.float64).reshape(x.shape)
+    gammas = 1.0 / 10.0 ** np.arange(1, 6)
+    s = np.empty(5)
+    w = np.empty(5)
+    for k, g in enumerate(gammas):
+        Li = float(fg(x + g * v)[0])
+        s[k] = Li - float(L)
+        w[k] = s[k] - g * float(np.sum(v * G))
+    return gammas, s, w
+
+
+def add_initial_model(x, v):
+    """src/Utils.jl:140-166: add x (a model update, or a stack of them along
+    the first axis) to the model v, centred: x smaller than v is added into
+    v's centre, x larger than v contributes its centred window of v's size."""
+    x = np.asarray(x, dtype=np.float64)
+    v = np.asarray(v, dtype=np.float64)
+    sx = x.shape[1:] if x.ndim == 3 else x.shape
+    if sx[0] <= v.shape[0] and sx[1] <= v.shape[1]:
+        i0, j0 = (v.shape[0] - sx[0]) // 2, (v.shape[1] - sx[1]) // 2
+        out = np.repeat(v[None], x.shape[0], axis=0) if x.ndim == 3 else v.copy()
+        out[..., i0:i0 + sx[0], j0:j0 + sx[1]] += x
+        return out
+    if sx[0] >= v.shape[0] and sx[1] >= v.shape[1]:
+        i0, j0 = (sx[0] - v.shape[0]) // 2, (sx[1] - v.shape[1]) // 2
+        return v + x[..., i0:i0 + v.shape[0], j0:j0 + v.shape[1]]
+    raise ValueError(f"size error: model {v.shape}, update {sx}")
+
+
 # ------------------------------------------------------------------ variable sources
 
 def _source_cells(param, srctype):

@@ -3,6 +3,7 @@ formulas, synthetic model generators, parameter defaults."""
 import math
 
 import numpy as np
+import pytest
 
 
 def test_ricker_matches_formula(ads):
@@ -49,6 +50,44 @@ def test_properties_chain_rule_matches_finite_differences(ads):
             args_m = [xm if q == k else y for q, y in enumerate((vp, vs, rho))]
             fd = (L(*args_p) - L(*args_m)) / (2 * e)
             assert abs(fd - g[k][m]) <= 1e-7 * max(abs(fd), 1e-3 * np.abs(g[k]).max()), (k, m)
+
+
+def test_gradtest_orders(ads, orc):
+    """gradtest on the oracle's acoustic loss and gradient (a small case):
+    the first-order difference falls as O(gamma), the Taylor remainder with
+    the adjoint gradient as O(gamma^2); a wrong gradient stays O(gamma)."""
+    rng = np.random.default_rng(3)
+    NX, NY, T = 16, 12, 40
+    s, t = orc.acoustic_pml(NX, NY, 10.0, 10.0, 4, 2000.0)
+    vp0 = 2000 + 300 * rng.random((NX + 2) * (NY + 2))
+    srcv = rng.standard_normal((T, 1)) * 1e3
+    rcvi, rcvj = np.arange(3, 15), np.full(12, 3)
+    obs = orc.acoustic_forward(NX, NY, T, 1e-3, 10.0, 10.0, s, t, vp0 * 1.02, [9], [7], srcv,
+                               rcvi, rcvj)
+
+    def fg(vp):
+        return orc.acoustic_gradient(NX, NY, T, 1e-3, 10.0, 10.0, s, t, vp, [9], [7], srcv,
+                                     rcvi, rcvj, obs)
+
+    g, S, W = ads.gradtest(fg, vp0, direction=rng.random(vp0.size) * 10.0)
+    assert np.allclose(g, [1e-1, 1e-2, 1e-3, 1e-4, 1e-5])
+    assert all(1 / 12 < abs(S[k + 1] / S[k]) < 1 / 8 for k in range(4))
+    assert all(abs(W[k + 1] / W[k]) < 1 / 50 for k in range(3))
+    _, _, W2 = ads.gradtest(lambda v: (fg(v)[0], fg(v)[1] * 1.1), vp0,
+                            direction=rng.random(vp0.size) * 10.0)
+    assert abs(W2[3] / W2[2]) > 1 / 12
+
+
+def test_add_initial_model_centres_the_update(ads):
+    v = np.zeros((6, 8))
+    out = ads.add_initial_model(np.ones((2, 4)), v)
+    assert out.sum() == 8 and np.all(out[2:4, 2:6] == 1)
+    stack = ads.add_initial_model(np.ones((3, 2, 2)), v)
+    assert stack.shape == (3, 6, 8) and np.all(stack[:, 2:4, 3:5] == 1)
+    big = np.arange(10 * 12, dtype=float).reshape(10, 12)
+    assert np.array_equal(ads.add_initial_model(big, v), big[2:8, 2:10])
+    with pytest.raises(ValueError):
+        ads.add_initial_model(np.ones((8, 2)), v)
 
 
 def test_param_defaults_follow_reference(ads):
