@@ -12,7 +12,7 @@ from .acoustic import (AcousticMisfit, AcousticOneStep, AcousticPlan, AcousticPr
                        AcousticPropagatorParams, AcousticPropagatorSolver, AcousticReceiver,
                        AcousticSource, SimulatedObservation, acoustic_one_step,
                        acoustic_one_step_grad, compute_forward_GPU, compute_loss_and_grads_GPU,
-                       dropin_loss_and_grad)
+                       dropin_loss_and_grad, step_variant)
 from .acoustic import compute_PML_Params as compute_acoustic_PML_Params
 from .elastic import (ElasticPlan, ElasticPropagator, ElasticPropagatorParams,
                       ElasticPropagatorSolver, ElasticReceiver, ElasticSource,

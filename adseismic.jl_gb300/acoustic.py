@@ -16,7 +16,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import ADS_F32, ADS_F64, ADS_VARIANT_W, call, lib
+from ._lib import ADS_F32, ADS_F64, ADS_VARIANT_U, ADS_VARIANT_W, call, lib
 
 
 def _stream():
@@ -307,11 +307,24 @@ class AcousticPropagator:
         self.param, self.src, self.vp, self.precision = param, src, vp, precision
 
 
-def AcousticPropagatorSolver(param: AcousticPropagatorParams, src: AcousticSource, vp,
-                             precision="f64"):
-    """src/Core.jl:562-620 (c = vp^2, PML from param, zero initial slots)."""
+def step_variant(param: AcousticPropagatorParams) -> int:
+    """The one-step form param.PropagatorKernel selects (src/Core.jl:580-591):
+    0 runs one_step (src/Core.jl:528-549: phi, psi from the new u,
+    ADS_VARIANT_U); 1 the custom operator and 2 its TF restatement
+    acoustic_one_step_customop_ref (src/Core.jl:504-525), both with phi, psi
+    from the old w (ADS_VARIANT_W)."""
     if param.PropagatorKernel not in (0, 1, 2):
         raise ValueError("PropagatorKernel must be 0, 1 or 2")
+    return ADS_VARIANT_U if param.PropagatorKernel == 0 else ADS_VARIANT_W
+
+
+def AcousticPropagatorSolver(param: AcousticPropagatorParams, src: AcousticSource, vp,
+                             precision="f64"):
+    """src/Core.jl:562-620 (c = vp^2, PML from param, zero initial slots).
+    PropagatorKernel 1 and 2 (the custom operator's form) run on the batched
+    plans; 0 (one_step, phi / psi from the new u, which the plans do not
+    implement) runs the single-step operator chain in FP64."""
+    step_variant(param)
     return AcousticPropagator(param, src, vp, precision)
 
 
@@ -323,6 +336,10 @@ def _shot_dict(param, src, rcv):
 def SimulatedObservation(ap: AcousticPropagator, rcv: AcousticReceiver):
     """src/Core.jl:726-730: fills rcv.rcvv with the (NSTEP+1, nrcv) traces."""
     p = ap.param
+    if step_variant(p) == ADS_VARIANT_U:
+        rcv.rcvv = _chain_forward(p, ap.src, rcv, ap.vp)[0].view(p.NSTEP + 1, len(rcv.rcvi))
+        torch.cuda.current_stream().synchronize()
+        return rcv.rcvv
     plan = AcousticPlan(p.NX, p.NY, p.DELTAX, p.DELTAY, p.DELTAT, [_shot_dict(p, ap.src, rcv)],
                         npml=p.NPOINTS_PML, Rcoef=p.Rcoef, vp_ref=p.vp_ref,
                         use_pml=p.use_pml, precision=ap.precision, use_graph=False)
@@ -342,6 +359,11 @@ def compute_forward_GPU(param: AcousticPropagatorParams, srcs, rcvs, vp, precisi
         from .elastic import compute_forward_GPU as elastic_forward
 
         return elastic_forward(param, srcs, rcvs, vp, precision)
+    if step_variant(param) == ADS_VARIANT_U:
+        out = [_chain_forward(param, s, r, vp)[0].view(param.NSTEP + 1, len(r.rcvi))
+               for s, r in zip(srcs, rcvs)]
+        torch.cuda.current_stream().synchronize()
+        return out
     shots = [_shot_dict(param, s, r) for s, r in zip(srcs, rcvs)]
     plan = AcousticPlan(param.NX, param.NY, param.DELTAX, param.DELTAY, param.DELTAT, shots,
                         npml=param.NPOINTS_PML, Rcoef=param.Rcoef, vp_ref=param.vp_ref,
@@ -364,6 +386,13 @@ def compute_loss_and_grads_GPU(param: AcousticPropagatorParams, srcs, rcvs, Rs, 
         from .elastic import compute_loss_and_grads_GPU as elastic_grads
 
         return elastic_grads(param, srcs, rcvs, Rs, vp, precision, ckpt_every)
+    if step_variant(param) == ADS_VARIANT_U:
+        loss, grad = 0.0, 0.0
+        for s, r, o in zip(srcs, rcvs, Rs):
+            l, g = dropin_loss_and_grad(param, s, r, o, vp)
+            loss, grad = loss + l, grad + g
+        torch.cuda.current_stream().synchronize()
+        return loss, grad
     shots = [_shot_dict(param, s, r) for s, r in zip(srcs, rcvs)]
     plan = AcousticPlan(param.NX, param.NY, param.DELTAX, param.DELTAY, param.DELTAT, shots,
                         npml=param.NPOINTS_PML, Rcoef=param.Rcoef, vp_ref=param.vp_ref,
@@ -378,23 +407,14 @@ def compute_loss_and_grads_GPU(param: AcousticPropagatorParams, srcs, rcvs, Rs, 
     return loss, grad
 
 
-def dropin_loss_and_grad(param: AcousticPropagatorParams, src: AcousticSource,
-                         rcv: AcousticReceiver, observed, vp):
-    """The plain FP64 operator chain of one shot, as the reference's graph runs
-    it: one C-ABI operator call per op and time step, the whole wavefield
-    history kept on the device (TensorFlow keeps every while_loop output for
-    its gradient).
-
-    Forward (src/Core.jl:600-614): AcousticOneStep, then ScatterAdd of the
-    dt^2-scaled source row; receivers by one Gather over the history
-    (SimulatedObservation!, src/Core.jl:726-730).  Loss = sum((rcvv - obs)^2)
-    (src/Utils.jl:308).  Reverse (the gradients call of src/Utils.jl:312): the
-    Gather's transpose (a ScatterAdd of the residual), then
-    AcousticOneStepGrad per step; ScatterAdd passes its input gradient
-    through.  Variant W only.  Returns (loss, grad_vp) as FP64 CUDA tensors.
-    """
-    if param.PropagatorKernel != ADS_VARIANT_W:
-        raise ValueError("the drop-in chain is written for PropagatorKernel 0")
+def _chain_forward(param: AcousticPropagatorParams, src: AcousticSource,
+                   rcv: AcousticReceiver, vp):
+    """The forward half of the operator chain (src/Core.jl:600-614 and
+    SimulatedObservation!, src/Core.jl:726-730): AcousticOneStep in the form
+    step_variant(param) selects, then ScatterAdd of the dt^2-scaled source
+    row, per step; receivers by one Gather over the history.  Returns the
+    packed (NSTEP+1, nrcv) traces and what the reverse half needs."""
+    variant = step_variant(param)
     dev = torch.device("cuda")
     NX, NY, T = param.NX, param.NY, param.NSTEP
     S, N = NY + 2, (NX + 2) * (NY + 2)
@@ -413,7 +433,6 @@ def dropin_loss_and_grad(param: AcousticPropagatorParams, src: AcousticSource,
     rcell = (rcvi - 1) * S + rcvj                                         # 1-based cells
     hist_ii = torch.as_tensor((np.arange(T + 1)[:, None] * N + rcell[None, :]).reshape(-1),
                               device=dev)
-    rii = torch.as_tensor(rcell, device=dev)
     U = torch.zeros(T + 1, N, **f64)
     Ph = torch.zeros(T + 1, N, **f64)
     Qh = torch.zeros(T + 1, N, **f64)
@@ -423,13 +442,38 @@ def dropin_loss_and_grad(param: AcousticPropagatorParams, src: AcousticSource,
     for k in range(2, T + 1):
         _lib.check(L.ads_acoustic_step_fwd_f64(
             P(U[k - 1]), P(U[k - 2]), P(Ph[k - 1]), P(Qh[k - 1]), P(sigma), P(tau), P(c),
-            dt, hx, hy, NX, NY, P(U[k]), P(Ph[k]), P(Qh[k]), ADS_VARIANT_W, st))
+            dt, hx, hy, NX, NY, P(U[k]), P(Ph[k]), P(Qh[k]), variant, st))
         if nsrc:
             _lib.check(L.ads_scatter_add_f64(P(U[k]), P(U[k]), P(sii), P(upd[k - 1]), N,
                                              nsrc, st))
     rcvv = torch.empty((T + 1) * nrcv, **f64)
     if nrcv:
         _lib.check(L.ads_gather_f64(P(rcvv), P(U), P(hist_ii), (T + 1) * nrcv, st))
+    return rcvv, (U, Ph, Qh, sigma, tau, c, vpt, rcell, variant)
+
+
+def dropin_loss_and_grad(param: AcousticPropagatorParams, src: AcousticSource,
+                         rcv: AcousticReceiver, observed, vp):
+    """The plain FP64 operator chain of one shot, as the reference's graph runs
+    it: one C-ABI operator call per op and time step, the whole wavefield
+    history kept on the device (TensorFlow keeps every while_loop output for
+    its gradient).
+
+    Forward: _chain_forward.  Loss = sum((rcvv - obs)^2) (src/Utils.jl:308).
+    Reverse (the gradients call of src/Utils.jl:312): the Gather's transpose
+    (a ScatterAdd of the residual), then AcousticOneStepGrad per step in the
+    same form; ScatterAdd passes its input gradient through.  PropagatorKernel
+    1 or 2 gives the custom operators' chain (the plain FP64 drop-in), 0 the
+    one_step form.  Returns (loss, grad_vp) as FP64 CUDA tensors.
+    """
+    rcvv, (U, Ph, Qh, sigma, tau, c, vpt, rcell, variant) = _chain_forward(param, src, rcv, vp)
+    dev = U.device
+    NX, NY, T = param.NX, param.NY, param.NSTEP
+    N = (NX + 2) * (NY + 2)
+    dt, hx, hy = param.DELTAT, param.DELTAX, param.DELTAY
+    f64 = dict(dtype=torch.float64, device=dev)
+    nrcv = len(rcell)
+    rii = torch.as_tensor(rcell, device=dev)
     obs = torch.as_tensor(observed, **f64).reshape(-1)
     resid = 2.0 * (rcvv - obs)
     loss = torch.sum((rcvv - obs) ** 2)
@@ -440,6 +484,9 @@ def dropin_loss_and_grad(param: AcousticPropagatorParams, src: AcousticSource,
     gw = torch.empty(N, **f64)
     gcs = torch.empty(N, **f64)
     gc = torch.zeros(N, **f64)
+    st = _stream()
+    L = lib()
+    P = _ptr
     for k in range(T, 1, -1):
         lu = LU[k % 3]
         if nrcv:
@@ -450,7 +497,7 @@ def dropin_loss_and_grad(param: AcousticPropagatorParams, src: AcousticSource,
             P(gw), P(LU[(k - 2) % 3]), P(LP[(k - 1) % 2]), P(LQ[(k - 1) % 2]), P(gcs),
             P(lu), P(LP[k % 2]), P(LQ[k % 2]),
             P(U[k - 1]), P(U[k - 2]), P(Ph[k - 1]), P(Qh[k - 1]), P(sigma), P(tau), P(c),
-            dt, hx, hy, NX, NY, P(U[k]), P(Ph[k]), P(Qh[k]), ADS_VARIANT_W, st))
+            dt, hx, hy, NX, NY, P(U[k]), P(Ph[k]), P(Qh[k]), variant, st))
         LU[(k - 1) % 3].add_(gw)
         gc.add_(gcs)
     grad_vp = (gc * 2.0) * vpt

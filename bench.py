@@ -616,7 +616,8 @@ def main():
         s0 = shots[0]
         prm = ads.AcousticPropagatorParams(NX=MX, NY=MY, NSTEP=nstep, DELTAX=cfg["h"],
                                            DELTAY=cfg["h"], DELTAT=cfg["dt"],
-                                           NPOINTS_PML=cfg["npml"], vp_ref=cfg["vp_ref"])
+                                           NPOINTS_PML=cfg["npml"], vp_ref=cfg["vp_ref"],
+                                           PropagatorKernel=1)  # the custom operators
         src = ads.AcousticSource(np.asarray(s0["srci"]), np.asarray(s0["srcj"]),
                                  np.asarray(s0["srcv"]))
         rcv = ads.AcousticReceiver(s0["rcvi"], s0["rcvj"])

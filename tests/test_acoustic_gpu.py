@@ -278,18 +278,38 @@ def test_invalid_geometry_rejected(ads, cuda):
 
 
 def test_julia_style_api(ads, orc, cuda):
+    """PropagatorKernel 1 (the custom operator's form, on the plans) against the
+    reference's golden loop; 0 (one_step: phi / psi from the new u, on the
+    single-step operator chain) against the oracle's restatement of it."""
     g = golden("acoustic_loop.npz")
     NX, NY, Tn = int(g["NX"]), int(g["NY"]), int(g["NSTEP"])
-    p = ads.AcousticPropagatorParams(NX=NX, NY=NY, NSTEP=Tn, DELTAX=float(g["h"]),
-                                     DELTAY=float(g["h"]), DELTAT=float(g["dt"]),
-                                     NPOINTS_PML=int(g["npml"]), vp_ref=float(g["vp_ref"]))
+    h, dt = float(g["h"]), float(g["dt"])
     src = ads.AcousticSource(g["srci"], g["srcj"], g["srcv"])
     rcv = ads.AcousticReceiver(g["rcvi"], g["rcvj"])
+    kw = dict(NX=NX, NY=NY, NSTEP=Tn, DELTAX=h, DELTAY=h, DELTAT=dt,
+              NPOINTS_PML=int(g["npml"]), vp_ref=float(g["vp_ref"]))
+    p = ads.AcousticPropagatorParams(PropagatorKernel=1, **kw)
     ap = ads.AcousticPropagatorSolver(p, src, g["vp"])
     ads.SimulatedObservation(ap, rcv)
     assert rel(rcv.rcvv.cpu().numpy(), g["rcvv"]) <= TOL64
     loss, grad = ads.compute_loss_and_grads_GPU(p, [src], [rcv], [g["obs"]], g["vp"])
     assert rel(grad.cpu().numpy().reshape(-1), g["grad_vp"]) <= TOL64
+    pu = ads.AcousticPropagatorParams(**kw)
+    assert pu.PropagatorKernel == 0 and ads.step_variant(pu) == ads.ADS_VARIANT_U
+    s, t = orc.acoustic_pml(NX, NY, h, h, int(g["npml"]), float(g["vp_ref"]))
+    args = (NX, NY, Tn, dt, h, h, s, t, g["vp"], g["srci"], g["srcj"], g["srcv"], g["rcvi"],
+            g["rcvj"])
+    ref_tr = orc.acoustic_forward(*args, variant=1)
+    ref_loss, ref_grad = orc.acoustic_gradient(*args, g["obs"], variant=1)
+    assert rel(ref_tr, g["rcvv"]) > 1e-8  # the two forms differ in the PML
+    ads.SimulatedObservation(ads.AcousticPropagatorSolver(pu, src, g["vp"]), rcv)
+    assert rel(rcv.rcvv.cpu().numpy(), ref_tr) <= TOL64
+    tr = ads.compute_forward_GPU(pu, [src], [rcv], g["vp"])
+    assert rel(tr[0].cpu().numpy(), ref_tr) <= TOL64
+    loss, grad = ads.compute_loss_and_grads_GPU(pu, [src, src], [rcv, rcv],
+                                                [g["obs"], g["obs"]], g["vp"])
+    assert abs(float(loss) - 2 * ref_loss) <= TOL64 * 2 * ref_loss
+    assert rel(grad.cpu().numpy().reshape(-1), 2 * ref_grad) <= TOL64
 
 
 def test_dropin_operator_chain_matches_reference_golden(ads, cuda):
@@ -299,7 +319,8 @@ def test_dropin_operator_chain_matches_reference_golden(ads, cuda):
     NX, NY, Tn = int(g["NX"]), int(g["NY"]), int(g["NSTEP"])
     p = ads.AcousticPropagatorParams(NX=NX, NY=NY, NSTEP=Tn, DELTAX=float(g["h"]),
                                      DELTAY=float(g["h"]), DELTAT=float(g["dt"]),
-                                     NPOINTS_PML=int(g["npml"]), vp_ref=float(g["vp_ref"]))
+                                     NPOINTS_PML=int(g["npml"]), vp_ref=float(g["vp_ref"]),
+                                     PropagatorKernel=1)
     src = ads.AcousticSource(g["srci"], g["srcj"], g["srcv"])
     rcv = ads.AcousticReceiver(g["rcvi"], g["rcvj"])
     loss, grad = ads.dropin_loss_and_grad(p, src, rcv, g["obs"], g["vp"])
@@ -437,7 +458,8 @@ def test_compute_forward_GPU_matches_the_golden_traces(ads, cuda):
     NX, NY, Tn, _ = loop_case(g)
     p = ads.AcousticPropagatorParams(NX=NX, NY=NY, NSTEP=Tn, DELTAX=float(g["h"]),
                                      DELTAY=float(g["h"]), DELTAT=float(g["dt"]),
-                                     NPOINTS_PML=int(g["npml"]), vp_ref=float(g["vp_ref"]))
+                                     NPOINTS_PML=int(g["npml"]), vp_ref=float(g["vp_ref"]),
+                                     PropagatorKernel=1)
     src = ads.AcousticSource(g["srci"], g["srcj"], g["srcv"])
     rcv = ads.AcousticReceiver(g["rcvi"], g["rcvj"])
     tr = ads.compute_forward_GPU(p, [src, src], [rcv, rcv], g["vp"])
