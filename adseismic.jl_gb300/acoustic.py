@@ -48,6 +48,8 @@ class AcousticPropagatorParams:
     USE_PML_YMAX: bool = True
     NPOINTS_PML: int = 12
     NPOWER: int = 2
+    damping_x: float = None  # set by compute_PML_Params, as the reference does
+    damping_y: float = None
     Rcoef: float = 0.001
     vp_ref: float = 1000.0
     IT_DISPLAY: int = 0
@@ -76,7 +78,11 @@ class AcousticReceiver:
 
 
 def compute_PML_Params(param: AcousticPropagatorParams):
-    """src/Core.jl:622-655: returns (Sigma_x, Sigma_y) as (NX+2, NY+2) arrays."""
+    """src/Core.jl:622-655: returns (Sigma_x, Sigma_y) as (NX+2, NY+2) arrays
+    and, as the reference does, sets param.damping_x / damping_y to
+    vp_ref / L ln(1 / Rcoef) with L the PML thickness along x / y."""
+    param.damping_x = param.vp_ref / (param.NPOINTS_PML * param.DELTAX) * np.log(1 / param.Rcoef)
+    param.damping_y = param.vp_ref / (param.NPOINTS_PML * param.DELTAY) * np.log(1 / param.Rcoef)
     sx = np.empty(param.NX + 2)
     ty = np.empty(param.NY + 2)
     call("ads_acoustic_pml_profiles", param.NX, param.NY, param.DELTAX, param.DELTAY,

@@ -49,6 +49,9 @@ def test_pml_profiles_match_oracle(ads, orc):
     Sx, Sy = ads.compute_acoustic_PML_Params(p)
     s, t = orc.acoustic_pml(NX, NY, 10.0, 12.0, 7, 1800.0)
     assert np.array_equal(Sx.reshape(-1), s) and np.array_equal(Sy.reshape(-1), t)
+    assert p.damping_x == pytest.approx(1800.0 / 70.0 * np.log(1000.0), rel=1e-15)
+    assert p.damping_y == pytest.approx(1800.0 / 84.0 * np.log(1000.0), rel=1e-15)
+    assert Sx[0].max() == pytest.approx(p.damping_x, rel=1e-12)  # d = L at the edge
 
 
 def test_cpml_profiles_match_oracle(ads, orc):
