@@ -32,9 +32,19 @@ def Gauss(param, a, shift=None, amp=1.0):
     return amp * 2.0 * A * np.exp(-A * (t - shift) ** 2)
 
 
-def compute_lame_parameters(vp, vs, rho):
-    """src/Utils.jl:237-243: mu = rho vs vs, lambda = rho (vp vp - 2 vs vs)."""
-    vp, vs, rho = (np.asarray(x, dtype=np.float64) for x in (vp, vs, rho))
+def compute_lame_parameters(*args):
+    """src/Utils.jl:223-243: compute_lame_parameters(vp, vs, rho) on arrays,
+    mu = rho vs vs, lambda = rho (vp vp - 2 vs vs); or
+    compute_lame_parameters(NX, NY, vp, vs, rho) with scalars, the same
+    values filled into (NX+2, NY+2) grids.  Returns (lambda, mu, rho)."""
+    if len(args) == 5:
+        NX, NY, vp, vs, rho = args
+        shape = (int(NX) + 2, int(NY) + 2)
+        return (np.full(shape, rho * (vp * vp - 2.0 * vs * vs)), np.full(shape, rho * vs * vs),
+                np.full(shape, float(rho)))
+    if len(args) != 3:
+        raise TypeError("compute_lame_parameters(vp, vs, rho) or (NX, NY, vp, vs, rho)")
+    vp, vs, rho = (np.asarray(x, dtype=np.float64) for x in args)
     mu = rho * vs * vs
     lam = rho * (vp * vp - 2.0 * vs * vs)
     return lam, mu, rho

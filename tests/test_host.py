@@ -24,6 +24,10 @@ def test_material_transforms(ads):
     assert lam[0] == 2200.0 * 3000.0 * 3000.0 - 2 * mu[0]
     lam2, mu2, _ = ads.compute_lame_parameters(vp, vs, rho)
     assert np.allclose(lam2, lam) and np.allclose(mu2, mu)
+    lg, mg, rg = ads.compute_lame_parameters(4, 3, 3300.0, 3300.0 / 1.732, 2800.0)
+    assert lg.shape == mg.shape == rg.shape == (6, 5) and np.all(rg == 2800.0)
+    assert np.all(mg == 2800.0 * (3300.0 / 1.732) ** 2)
+    assert np.all(lg == 2800.0 * (3300.0 ** 2 - 2.0 * (3300.0 / 1.732) ** 2))
 
 
 def test_properties_chain_rule_matches_finite_differences(ads):
