@@ -305,12 +305,37 @@ class AcousticPlan:
 
 
 class AcousticPropagator:
-    """Result handle of AcousticPropagatorSolver (src/Struct.jl:140-147).  The
-    wavefield history is not materialised (the GPU path keeps O(1) steps in
-    memory); receiver traces come from SimulatedObservation."""
+    """Result handle of AcousticPropagatorSolver (src/Struct.jl:140-147).
+    Receiver traces come from SimulatedObservation without any history (the
+    plans keep O(1) steps per shot).  The reference's u, phi and psi fields,
+    the (NSTEP+1, NX+2, NY+2) histories, are formed on first access by the
+    FP64 single-step operator chain in the form PropagatorKernel selects,
+    and kept on the device."""
 
     def __init__(self, param, src, vp, precision):
         self.param, self.src, self.vp, self.precision = param, src, vp, precision
+        self._hist = None
+
+    def _history(self):
+        if self._hist is None:
+            p = self.param
+            none = AcousticReceiver(np.zeros(0, np.int64), np.zeros(0, np.int64))
+            U, Ph, Qh = _chain_forward(p, self.src, none, self.vp)[1][:3]
+            shape = (p.NSTEP + 1, p.NX + 2, p.NY + 2)
+            self._hist = (U.view(shape), Ph.view(shape), Qh.view(shape))
+        return self._hist
+
+    @property
+    def u(self):
+        return self._history()[0]
+
+    @property
+    def phi(self):
+        return self._history()[1]
+
+    @property
+    def psi(self):
+        return self._history()[2]
 
 
 def step_variant(param: AcousticPropagatorParams) -> int:

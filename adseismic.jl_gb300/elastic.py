@@ -277,11 +277,46 @@ class ElasticPlan:
 
 
 class ElasticPropagator:
-    """Result handle of ElasticPropagatorSolver (src/Struct.jl:64-73)."""
+    """Result handle of ElasticPropagatorSolver (src/Struct.jl:64-73).
+    Receiver traces come from SimulatedObservation without any history.  The
+    reference's vx, vy, sigmaxx, sigmayy, sigmaxy ((NSTEP+1, NX+2, NY+2)
+    histories) and mem ((NSTEP+1, 8, NX+2, NY+2)) are formed on first access
+    by the FP64 single-step operator (the loop of src/Core.jl:31-94: slot 0
+    zero, slot n = one_step of slot n-1 with source row n-1) and kept on the
+    device."""
 
     def __init__(self, param, src, rho, lam, mu, precision):
         self.param, self.src, self.rho, self.lam, self.mu = param, src, rho, lam, mu
         self.precision = precision
+        self._hist = None
+
+    def _history(self):
+        if self._hist is None:
+            p = self.param
+            dev = torch.device("cuda")
+            f = lambda a: torch.as_tensor(a, dtype=torch.float64,
+                                          device=dev).reshape(-1).contiguous()
+            rho, lam, mu = f(self.rho), f(self.lam), f(self.mu)
+            prof = [torch.as_tensor(a, dtype=torch.float64, device=dev).contiguous()
+                    for a in compute_PML_Params(p)]
+            s = self.src
+            nsrc = len(s.srci)
+            sv = (torch.as_tensor(np.asarray(s.srcv, np.float64).reshape(-1, nsrc),
+                                  device=dev) if nsrc else None)
+            H = torch.zeros(p.NSTEP + 1, 13, (p.NX + 2) * (p.NY + 2), dtype=torch.float64,
+                            device=dev)
+            for n in range(1, p.NSTEP + 1):
+                H[n] = elastic_one_step(p, rho, lam, mu, H[n - 1], prof, s.srci, s.srcj,
+                                        sv[n - 1] if nsrc else None, s.srctype)
+            self._hist = H.view(p.NSTEP + 1, 13, p.NX + 2, p.NY + 2)
+        return self._hist
+
+    vx = property(lambda self: self._history()[:, 0])
+    vy = property(lambda self: self._history()[:, 1])
+    sigmaxx = property(lambda self: self._history()[:, 2])
+    sigmayy = property(lambda self: self._history()[:, 3])
+    sigmaxy = property(lambda self: self._history()[:, 4])
+    mem = property(lambda self: self._history()[:, 5:])
 
 
 def ElasticPropagatorSolver(param: ElasticPropagatorParams, src: ElasticSource, rho, lam, mu,

@@ -302,8 +302,14 @@ def test_julia_style_api(ads, orc, cuda):
     ref_tr = orc.acoustic_forward(*args, variant=1)
     ref_loss, ref_grad = orc.acoustic_gradient(*args, g["obs"], variant=1)
     assert rel(ref_tr, g["rcvv"]) > 1e-8  # the two forms differ in the PML
-    ads.SimulatedObservation(ads.AcousticPropagatorSolver(pu, src, g["vp"]), rcv)
+    apu = ads.AcousticPropagatorSolver(pu, src, g["vp"])
+    ads.SimulatedObservation(apu, rcv)
     assert rel(rcv.rcvv.cpu().numpy(), ref_tr) <= TOL64
+    # the reference's wavefield histories on the propagator (src/Struct.jl:140-147)
+    for prop, variant in ((ap, 0), (apu, 1)):
+        hist = orc.acoustic_forward(*args, variant=variant, keep_history=True)[1]
+        assert tuple(prop.u.shape) == (Tn + 1, NX + 2, NY + 2) == tuple(prop.psi.shape)
+        assert rel(prop.u.cpu().numpy(), hist) <= TOL64, variant
     tr = ads.compute_forward_GPU(pu, [src], [rcv], g["vp"])
     assert rel(tr[0].cpu().numpy(), ref_tr) <= TOL64
     loss, grad = ads.compute_loss_and_grads_GPU(pu, [src, src], [rcv, rcv],

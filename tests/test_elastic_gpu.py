@@ -137,8 +137,14 @@ def test_multishot_sum_and_julia_api(ads, orc, cuda):
     ref = orc.elastic_forward(NX, NY, 35, p.DELTAT, p.DELTAX, p.DELTAY, ax, bx, ay, by,
                               g["lam"], g["mu"], g["rho"], shots[0]["srci"], shots[0]["srcj"],
                               shots[0]["srctype"], shots[0]["srcv"], shots[0]["rcvi"],
-                              shots[0]["rcvj"], shots[0]["rcvtype"])
-    assert rel(rcv.rcvv.cpu().numpy(), ref) <= 1e-12
+                              shots[0]["rcvj"], shots[0]["rcvtype"], keep_history=True)
+    assert rel(rcv.rcvv.cpu().numpy(), ref[0]) <= 1e-12
+    # the reference's wavefield histories on the propagator (src/Struct.jl:64-73)
+    hist = ref[1]
+    assert tuple(ep.vx.shape) == (36, NX + 2, NY + 2) and tuple(ep.mem.shape)[1] == 8
+    for k, f in enumerate((ep.vx, ep.vy, ep.sigmaxx, ep.sigmayy, ep.sigmaxy)):
+        assert rel(f.cpu().numpy(), hist[:, k]) <= 1e-12, k
+    assert rel(ep.mem.cpu().numpy(), hist[:, 5:]) <= 1e-12
 
 
 @pytest.mark.parametrize("rows_per_warp,resident", [(0, 3), (5, -1), (5, 0)])
