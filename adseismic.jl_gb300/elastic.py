@@ -371,11 +371,13 @@ def compute_loss_and_grads_GPU(param: ElasticPropagatorParams, srcs, rcvs, Rs, m
     """src/Utils.jl:300-332 with elastic sources, one GPU: loss = sum over
     shots of sum((rcvv - Rs)^2) and its gradients with respect to lambda, mu
     and rho, all shots in one batched plan; model = (rho, lambda, mu), Rs per
-    shot (nrcv, NSTEP+1).  Returns (loss, grad_lambda, grad_mu, grad_rho);
-    compute_properties_grad turns these into vp / vs / rho gradients."""
+    shot (nrcv, NSTEP+1).  Returns (loss, grad_lambda, grad_mu, grad_rho), the
+    gradients shaped like lambda; compute_properties_grad turns them into
+    vp / vs / rho gradients."""
     plan = _batched_plan(param, srcs, rcvs, precision, ckpt_every)
     obs = plan.pack([torch.as_tensor(r, device="cuda") for r in Rs])
-    out = plan.gradient(*_materials(model), obs)
+    loss, *grads = plan.gradient(*_materials(model), obs)
     torch.cuda.current_stream().synchronize()
     plan.close()
-    return out
+    shape = tuple(np.shape(model[1]))
+    return (loss, *(g.view(shape) for g in grads))
