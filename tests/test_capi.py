@@ -72,6 +72,28 @@ def test_invalid_arguments_are_rejected_without_launch(ads):
     assert "NX" in L.ads_last_error().decode()
 
 
+def test_null_arguments_are_rejected_before_any_device_call(ads):
+    """The plan and one-shot entry points check their handles and configs
+    first, so these fail the same way with or without a GPU."""
+    from adseismic_gb300 import _lib
+
+    L = _lib.lib()
+    calls = [
+        L.ads_acoustic_forward(None, None, None, None, None),
+        L.ads_acoustic_gradient(None, None, None, None, None, None, None),
+        L.ads_elastic_forward(None, None, None, None, None, None, None),
+        L.ads_elastic_gradient(*([None] * 11)),
+        L.ads_acoustic_plan_set_source_values(None, 0, None, None),
+        L.ads_elastic_plan_set_source_values(None, 0, None, None),
+        L.ads_acoustic_plan_gradient_ex(*([None] * 8)),
+        L.ads_elastic_plan_gradient_ex(*([None] * 12)),
+    ]
+    assert calls == [_lib.ADS_ERR_INVALID] * len(calls), calls
+    assert L.ads_acoustic_plan_source_offset(None, 0) == -1
+    assert L.ads_elastic_plan_source_offset(None, 0) == -1
+    assert L.ads_elastic_plan_resident_segments(None) == -1
+
+
 def test_compute_calls_fail_loudly_without_gpu(ads):
     import torch
 
