@@ -14,7 +14,7 @@ from .acoustic import (AcousticMisfit, AcousticOneStep, AcousticPlan, AcousticPr
                        acoustic_one_step_grad, compute_forward_GPU, compute_loss_and_grads_GPU,
                        dropin_loss_and_grad, step_variant)
 from .acoustic import compute_PML_Params as compute_acoustic_PML_Params
-from .elastic import (ElasticPlan, ElasticPropagator, ElasticPropagatorParams,
+from .elastic import (ElasticMisfit, ElasticPlan, ElasticPropagator, ElasticPropagatorParams,
                       ElasticPropagatorSolver, ElasticReceiver, ElasticSource,
                       elastic_one_step, elastic_one_step_grad)
 from .elastic import SimulatedObservation as ElasticSimulatedObservation

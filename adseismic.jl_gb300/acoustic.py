@@ -543,9 +543,10 @@ class AcousticMisfit(torch.autograd.Function):
     def forward(ctx, vp, plan: AcousticPlan, observed):
         loss, grad = plan.gradient(vp, observed)
         ctx.save_for_backward(grad)
+        ctx.dtype = vp.dtype
         return loss
 
     @staticmethod
     def backward(ctx, gl):
         (grad,) = ctx.saved_tensors
-        return gl * grad, None, None
+        return (gl * grad).to(ctx.dtype), None, None

@@ -276,6 +276,25 @@ class ElasticPlan:
         return loss[0], gl, gm, gr
 
 
+class ElasticMisfit(torch.autograd.Function):
+    """loss = sum((traces(lambda, mu, rho) - observed)^2) as an autograd node
+    whose backward is the elastic plan's checkpointed adjoint (the gradient TF
+    builds in src/Utils.jl:312 for elastic sources): apply(lam, mu, rho, plan,
+    observed)."""
+
+    @staticmethod
+    def forward(ctx, lam, mu, rho, plan: ElasticPlan, observed):
+        loss, gl, gm, gr = plan.gradient(lam, mu, rho, observed)
+        ctx.save_for_backward(gl, gm, gr)
+        ctx.dtypes = (lam.dtype, mu.dtype, rho.dtype)
+        return loss
+
+    @staticmethod
+    def backward(ctx, g):
+        grads = ctx.saved_tensors
+        return tuple((g * x).to(d) for x, d in zip(grads, ctx.dtypes)) + (None, None)
+
+
 class ElasticPropagator:
     """Result handle of ElasticPropagatorSolver (src/Struct.jl:64-73).
     Receiver traces come from SimulatedObservation without any history.  The
