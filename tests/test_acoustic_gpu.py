@@ -335,6 +335,33 @@ def test_dropin_operator_chain_matches_reference_golden(ads, cuda):
     assert rel(grad.cpu().numpy().reshape(-1), g["grad_vp"]) <= TOL64
 
 
+def test_dropin_chain_at_the_reference_cpu_case_vs_oracle(ads, orc, cuda):
+    """The plain FP64 drop-in at the reference CPU operators' own case: 200 x 200
+    interior plus a 20-cell PML, h = 10 m, dt = 1 ms, 1000 steps, a 10 Hz Ricker
+    20 cells below the PML, 200 receivers 5 cells below it.  Loss and velocity
+    gradient against the oracle (bit-identical to the compiled reference
+    operators) within 1e-12."""
+    NX = NY = 240
+    npml, T, h, dt = 20, 1000, 10.0, 1e-3
+    vp = ads.layered_gaussian_model(NX + 2, NY + 2, 2000.0, 3500.0, seed=7)
+    vref = float(vp.mean())
+    p = ads.AcousticPropagatorParams(NX=NX, NY=NY, NSTEP=T, DELTAX=h, DELTAY=h, DELTAT=dt,
+                                     NPOINTS_PML=npml, vp_ref=vref, PropagatorKernel=1)
+    wav = ads.Ricker(p, ads.ricker_width_samples(10.0, dt), 1.5 / 10.0 / dt, 1e6)
+    src = ads.AcousticSource(np.array([NX // 2 + 1]), np.array([npml + 21]), wav[:, None])
+    rcv = ads.AcousticReceiver(np.arange(npml + 2, npml + 202), np.full(200, npml + 6))
+    s, t = orc.acoustic_pml(NX, NY, h, h, npml, vref)
+    args = (NX, NY, T, dt, h, h, s, t)
+    obs = orc.acoustic_forward(*args, (vp * 1.01).reshape(-1), src.srci, src.srcj, src.srcv,
+                               rcv.rcvi, rcv.rcvj)
+    ref_loss, ref_grad = orc.acoustic_gradient(*args, vp.reshape(-1), src.srci, src.srcj,
+                                               src.srcv, rcv.rcvi, rcv.rcvj, obs)
+    loss, grad = ads.dropin_loss_and_grad(p, src, rcv, obs, vp)
+    torch.cuda.synchronize()
+    assert abs(float(loss) - ref_loss) <= TOL64 * ref_loss
+    assert rel(grad.cpu().numpy().reshape(-1), ref_grad) <= TOL64
+
+
 @pytest.mark.parametrize("precision,tol", [("f64", TOL64), ("f32", 1e-4)])
 @pytest.mark.parametrize("resident", [-1, 0])
 def test_source_time_gradient_vs_oracle(ads, orc, cuda, precision, tol, resident):
