@@ -5,6 +5,9 @@
  * Conventions (all entry points):
  *  - Arrays are flat, row-major (NX+2) x (NY+2) grids, idx = i*(NY+2) + j,
  *    j (depth) contiguous -- the layout of the reference's custom operators.
+ *    A column-major caller (Julia, Fortran) passes the transpose of its
+ *    (NX+2, NY+2) array (Julia: permutedims(A, (2, 1))) and reads an (n, m)
+ *    row-major result v as permutedims(reshape(v, m, n), (2, 1)).
  *  - Source / receiver indices are 1-based into the padded grid, as in
  *    ADSeismic (the cell of (srci, srcj) is (srci-1)*(NY+2) + srcj-1).
  *  - Device pointers unless a parameter says "host".  Outputs are owned by the
@@ -162,29 +165,51 @@ int ads_elastic_step_fwd_f64(const double* state_in, double* state_out,
                              const int64_t* srci, const int64_t* srcj,
                              const int64_t* srctype, const double* srcv, int64_t nsrc,
                              ads_stream_t stream);
+/* FP32 form of ads_elastic_step_fwd_f64: one_step of src/Core.jl:215-228
+ * with FP32 arrays, profiles and source values.  The reference computes this
+ * step in FP64; results agree with it to FP32 rounding. */
+int ads_elastic_step_fwd_f32(const float* state_in, float* state_out, const float* lambda,
+                             const float* mu, const float* rho, const float* ax,
+                             const float* bx, const float* kx, const float* ay,
+                             const float* by, const float* ky, double dt, double dx,
+                             double dy, int64_t NX, int64_t NY, const int64_t* srci,
+                             const int64_t* srcj, const int64_t* srctype, const float* srcv,
+                             int64_t nsrc, ads_stream_t stream);
 /* Transpose of one elastic step about state_in: grad_in (13*N, overwritten) is
  * the gradient w.r.t. state_in given grad_out w.r.t. the step's output;
- * grad_lambda, grad_mu, grad_rho are ACCUMULATED (+=). */
+ * grad_lambda, grad_mu, grad_rho are ACCUMULATED (+=).  The TF gradient of
+ * src/Core.jl:215-228 (fw4 .. fw1 and AddSource reversed). */
 int ads_elastic_step_bwd_f64(const double* state_in, const double* grad_out,
                              double* grad_in, double* grad_lambda, double* grad_mu,
                              double* grad_rho, const double* lambda, const double* mu,
                              const double* rho, const double* ax, const double* bx,
                              const double* ay, const double* by, double dt, double dx,
                              double dy, int64_t NX, int64_t NY, ads_stream_t stream);
+/* FP32 form of ads_elastic_step_bwd_f64 (FP32 arrays; the parameter gradients
+ * are summed in FP64 inside the call and added to the FP32 outputs). */
+int ads_elastic_step_bwd_f32(const float* state_in, const float* grad_out, float* grad_in,
+                             float* grad_lambda, float* grad_mu, float* grad_rho,
+                             const float* lambda, const float* mu, const float* rho,
+                             const float* ax, const float* bx, const float* ay,
+                             const float* by, double dt, double dx, double dy, int64_t NX,
+                             int64_t NY, ads_stream_t stream);
 
 /* Allocation-free form of ads_elastic_step_bwd_f64 (same arguments, same
  * results).  No counterpart in the reference: it exists for callers that cannot
- * allocate device memory when they run the step, such as code inside another
- * framework's stream capture or custom-call hook (where cudaMalloc or
- * cudaMallocAsync would break the capture or bypass that framework's memory
- * accounting) or loops that must never enter the CUDA allocator.  Its scratch is
- * one fixed array of 34 x 65536 doubles (about 17.8 MB) compiled into the
- * library and resident on every GPU that loads it until the process exits;
- * grids with (NX+2)*(NY+2) > 65536 are rejected with ADS_ERR_INVALID.  The
- * first call on each device looks up the array's device address (make that
- * first call before any stream capture).  All calls share the one array: calls
- * whose executions overlap on the GPU (different streams without ordering, or
- * threads racing on one device) corrupt each other's scratch. */
+ * allocate device memory when they run the step, such as an operator called
+ * from another framework's custom-call hook (that framework owns the device
+ * memory, and a cudaMalloc from an extension bypasses its accounting or fails
+ * once it has reserved the device) or time-critical loops that must never enter
+ * the CUDA allocator.  Its scratch is one fixed array of 34 x 65536 doubles
+ * (about 17.8 MB) compiled into the library and resident on every GPU that
+ * loads it until the process exits; grids with (NX+2)*(NY+2) > 65536 are
+ * rejected with ADS_ERR_INVALID.  The first call on each device looks up the
+ * array's device address and caches it (make that first call before any stream
+ * capture); the cache assumes the device's primary context lives until the
+ * process exits, so do not call it after cudaDeviceReset.  All calls share the
+ * one array, which keeps the last call's contents (each call clears what it
+ * uses): calls whose executions overlap on the GPU (different streams without
+ * ordering, or threads racing on one device) corrupt each other's scratch. */
 int ads_elastic_step_bwd_f64_noalloc(const double* state_in, const double* grad_out,
                                      double* grad_in, double* grad_lambda, double* grad_mu,
                                      double* grad_rho, const double* lambda, const double* mu,

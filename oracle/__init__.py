@@ -11,8 +11,9 @@ Two libraries sit behind it:
   the elastic composition (src/Core.jl:96-228) and its hand-derived adjoint.
   Builds anywhere (``make -C oracle``).
 * ``_ref/libadsref.so`` -- the reference's OWN CPU operators compiled from the
-  reference checkout (``make -C oracle ref``); only where that checkout exists.
-  Used to pin the restatement.
+  reference checkout named by the environment variable ``ADS_REFERENCE_SRC``
+  (``make -C oracle ref``); only where that variable names a checkout.  Used
+  to pin the restatement.
 
 All arrays are float64 numpy, flat row-major (NX+2)x(NY+2) with j contiguous;
 source/receiver indices are 1-based into the padded grid (reference convention).
@@ -28,19 +29,24 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 REF_PATH = os.path.join(HERE, "_ref", "libadsref.so")
-DEFAULT_REF_SRC = "/root/reference"
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int64)
 
 
+def reference_checkout():
+    """The reference checkout named by ADS_REFERENCE_SRC, or None."""
+    src = os.environ.get("ADS_REFERENCE_SRC", "")
+    return src if src and os.path.isdir(src) else None
+
+
 def build(ref: bool = True) -> None:
-    """Compile the restatement and, when the reference checkout exists, _ref."""
+    """Compile the restatement and, when ADS_REFERENCE_SRC names a reference
+    checkout, _ref."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
-    if ref and os.path.isdir(os.environ.get("ADS_REFERENCE_SRC", DEFAULT_REF_SRC)):
-        subprocess.run(["make", "-s", "-C", HERE, "ref",
-                        "REF=" + os.environ.get("ADS_REFERENCE_SRC", DEFAULT_REF_SRC)],
-                       check=True)
+    src = reference_checkout()
+    if ref and src:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + src], check=True)
 
 
 _lib = None

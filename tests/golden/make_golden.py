@@ -4,9 +4,10 @@ Acoustic step / loop / gradient and the AddSource, GetReceive, ScatterAdd,
 Gather fixtures come from the reference's OWN CPU operators compiled from the
 reference checkout (oracle/_ref, `make -C oracle ref`).  The elastic fixtures
 come from the oracle's restatement of src/Core.jl (the reference has no
-compiled elastic stencil).  Run from the repository root:
+compiled elastic stencil).  Run from the repository root, with
+ADS_REFERENCE_SRC naming the reference checkout:
 
-    python tests/golden/make_golden.py
+    ADS_REFERENCE_SRC=<checkout> python tests/golden/make_golden.py
 """
 import os
 import sys

@@ -137,3 +137,58 @@ def test_ctypes_structs_match_the_header_layout(ads, tmp_path):
         assert int(got[cname]) == ctypes.sizeof(cls), cname
         for fname, _ in cls._fields_:
             assert int(got[f"{cname}.{fname}"]) == getattr(cls, fname).offset, (cname, fname)
+
+
+# ------------------------------------------------- column-major (Julia) callers
+# A Julia Array holds element (i, j) of an (n, m) matrix at i + j n.  The Julia
+# shims pass permutedims(A, (2, 1)) into the ABI and read an (n, m) row-major
+# result v back as permutedims(reshape(v, m, n), (2, 1)).  These helpers emulate
+# that memory on numpy arrays.
+
+def julia_memory(A):
+    """The memory of a Julia array with A's elements (column-major)."""
+    return np.asfortranarray(A).ravel(order="K")
+
+
+def to_abi(A):
+    """Memory of permutedims(A, (2, 1)): A in the ABI's row-major order."""
+    return julia_memory(np.ascontiguousarray(np.asarray(A).T))
+
+
+def from_abi(v, n, m):
+    """permutedims(reshape(v, m, n), (2, 1)): Julia reshape fills columns first."""
+    return np.reshape(np.asarray(v), (m, n), order="F").T
+
+
+def test_julia_layout_conversion_matches_the_abi_order(ads, orc):
+    """A non-square model held column-major, converted as the shims do, gives the
+    oracle's traces and gradient on the row-major model; passed unconverted it
+    would not."""
+    NX, NY, T, h, dt = 17, 9, 60, 10.0, 1e-3
+    rng = np.random.default_rng(4)
+    vp = 2000.0 + 500.0 * rng.random((NX + 2, NY + 2))     # the Julia (NX+2, NY+2) model
+    vp_julia = np.asfortranarray(vp)
+    abi = to_abi(vp_julia)
+    assert np.array_equal(abi, vp.reshape(-1))               # i*(NY+2) + j order
+    assert not np.array_equal(julia_memory(vp_julia), vp.reshape(-1))
+    # the reference's own sigma_ij = constant(param.Σx'[:]) is the same conversion
+    Sx, Sy = ads.compute_acoustic_PML_Params(
+        ads.AcousticPropagatorParams(NX=NX, NY=NY, DELTAX=h, DELTAY=h, NPOINTS_PML=3))
+    assert np.array_equal(julia_memory(Sx.T), to_abi(Sx))
+    sx, ty = orc.acoustic_pml(NX, NY, h, h, 3, 1000.0)
+    srcv = rng.standard_normal((T, 1))
+    srci, srcj, rcvi, rcvj = [9], [5], np.arange(2, NX + 2), np.full(NX, 3)
+    ref = orc.acoustic_forward(NX, NY, T, dt, h, h, sx, ty, vp.reshape(-1), srci, srcj, srcv,
+                               rcvi, rcvj)
+    got = orc.acoustic_forward(NX, NY, T, dt, h, h, sx, ty, abi, srci, srcj, srcv, rcvi, rcvj)
+    # the (T+1, nrcv) row-major buffer read back as the Julia matrix rcv.rcvv
+    assert np.array_equal(from_abi(got.reshape(-1), T + 1, NX), ref)
+    bad = orc.acoustic_forward(NX, NY, T, dt, h, h, sx, ty, julia_memory(vp_julia), srci, srcj,
+                               srcv, rcvi, rcvj)
+    assert not np.allclose(bad, ref)
+    obs = ref * 1.01
+    _, gref = orc.acoustic_gradient(NX, NY, T, dt, h, h, sx, ty, vp.reshape(-1), srci, srcj,
+                                    srcv, rcvi, rcvj, obs)
+    _, g = orc.acoustic_gradient(NX, NY, T, dt, h, h, sx, ty, abi, srci, srcj, srcv, rcvi,
+                                 rcvj, to_abi(obs))
+    assert np.array_equal(from_abi(g, NX + 2, NY + 2), gref.reshape(NX + 2, NY + 2))

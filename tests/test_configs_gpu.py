@@ -1,0 +1,247 @@
+"""Accuracy at the benchmark configurations' full sizes, on the GPU.
+
+The FP32 paths the benchmark times are compared with the FP64 plans on the
+same seeded inputs (adseismic_gb300.configs), per receiver trace and per
+gradient field, at the configurations' full record lengths: C3 (1000 x 500,
+3000 steps), C4 (600 x 300 elastic CPML, 4000 steps) and the longest C5 shot
+(6000 steps).  The FP64 plans are pinned to the oracle at the same
+geometries: C3 traces over all 3000 steps and the C3 gradient over 300 steps;
+C4 traces over 1000 steps and its gradient over 150 steps.  C2's check is
+central finite differences of the FP64 plan's loss on 16 random cells.
+
+Tolerances (rel-L2 = ||x - x_ref|| / ||x_ref||):
+  FP64 plan vs oracle                        1e-12
+  FP32 vs FP64, gradient (each field)        1e-4
+  FP32 vs FP64, all traces of a shot         1e-5
+  C2 central differences (eps = 1e-4 vp)     1e-6 per cell
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32_GRAD = 1e-4
+TOL32_TRACE = 1e-5
+TOL_FD = 1e-6
+
+
+def rel(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def dev(a, dtype=torch.float64):
+    return torch.as_tensor(np.asarray(a), dtype=dtype, device="cuda")
+
+
+def report(name, **kv):
+    print(f"\n[{name}] " + ", ".join(f"{k}={v:.3e}" if isinstance(v, float) else f"{k}={v}"
+                                    for k, v in kv.items()))
+
+
+@pytest.fixture(scope="module")
+def cfgs(ads):
+    from adseismic_gb300 import configs
+
+    return configs
+
+
+# ------------------------------------------------------------------ C3
+
+@pytest.fixture(scope="module")
+def c3(cfgs):
+    cfg, shots, vt, v0 = cfgs.c3_batched(nshots=64)
+    return cfg, shots, vt, v0
+
+
+def test_c3_fp64_plan_traces_match_oracle_3000_steps(ads, orc, cuda, cfgs, c3):
+    cfg, shots, vt, v0 = c3
+    s = shots[20]
+    plan = cfgs.acoustic_plan(ads, cfg, [s], "f64")
+    tr = plan.forward(dev(vt)).cpu().numpy()
+    plan.close()
+    MX, MY = cfg["MX"], cfg["MY"]
+    sx, ty = orc.acoustic_pml(MX, MY, cfg["h"], cfg["h"], cfg["npml"], cfg["vp_ref"])
+    ref = orc.acoustic_forward(MX, MY, cfg["nstep"], cfg["dt"], cfg["h"], cfg["h"], sx, ty,
+                               vt.reshape(-1), s["srci"], s["srcj"], s["srcv"], s["rcvi"],
+                               s["rcvj"])
+    r = rel(tr, ref.reshape(-1))
+    report("C3 FP64 plan traces vs oracle, 3000 steps", rel=r)
+    assert r <= TOL64
+
+
+def test_c3_fp64_plan_gradient_matches_oracle_300_steps(ads, orc, cuda, cfgs):
+    cfg, shots, vt, v0 = cfgs.c3_batched(nshots=64, nstep=300)
+    s = shots[20]
+    plan = cfgs.acoustic_plan(ads, cfg, [s], "f64", ckpt_every=100)
+    obs = plan.forward(dev(vt)).clone()
+    loss, g = plan.gradient(dev(v0), obs)
+    torch.cuda.synchronize()
+    plan.close()
+    MX, MY = cfg["MX"], cfg["MY"]
+    sx, ty = orc.acoustic_pml(MX, MY, cfg["h"], cfg["h"], cfg["npml"], cfg["vp_ref"])
+    lref, gref = orc.acoustic_gradient(MX, MY, 300, cfg["dt"], cfg["h"], cfg["h"], sx, ty,
+                                       v0.reshape(-1), s["srci"], s["srcj"], s["srcv"],
+                                       s["rcvi"], s["rcvj"], obs.cpu().numpy())
+    r = rel(g.cpu().numpy().reshape(-1), gref)
+    report("C3 FP64 plan gradient vs oracle, 300 steps", rel=r,
+           loss_rel=abs(float(loss) - lref) / lref)
+    assert abs(float(loss) - lref) <= TOL64 * lref
+    assert r <= TOL64
+
+
+def test_c3_fp32_vs_fp64_full_length(ads, cuda, cfgs, c3):
+    """Two of the 64 shots, 3000 steps, the benchmark's plan settings."""
+    cfg, shots, vt, v0 = c3
+    pick = [shots[0], shots[32]]
+    p64 = cfgs.acoustic_plan(ads, cfg, pick, "f64", ckpt_every=100)
+    obs64 = p64.forward(dev(vt)).clone()
+    l64, g64, tr64 = p64.gradient(dev(v0), obs64, want_traces=True)
+    torch.cuda.synchronize()
+    p64.close()
+    p32 = cfgs.acoustic_plan(ads, cfg, pick, "f32", ckpt_every=100, autotune=True,
+                             resident_mem_pct=50)
+    l32, g32, tr32 = p32.gradient(dev(v0), obs64.float(), want_traces=True)
+    torch.cuda.synchronize()
+    p32.close()
+    tr64, tr32 = tr64.cpu().numpy(), tr32.double().cpu().numpy()
+    rg = rel(g32.cpu().numpy(), g64.cpu().numpy())
+    n = (cfg["nstep"] + 1) * 500
+    per = np.concatenate([cfgs.per_trace_rel(tr32[k * n:(k + 1) * n], tr64[k * n:(k + 1) * n],
+                                             500) for k in range(2)])
+    rt = max(rel(tr32[k * n:(k + 1) * n], tr64[k * n:(k + 1) * n]) for k in range(2))
+    report("C3 FP32 vs FP64, 2 shots x 3000 steps", grad=rg, traces=rt,
+           trace_max=float(per.max()), trace_median=float(np.median(per)),
+           loss_rel=abs(float(l32) - float(l64)) / float(l64))
+    assert rg <= TOL32_GRAD
+    assert rt <= TOL32_TRACE
+
+
+# ------------------------------------------------------------------ C5
+
+def test_c5_longest_shot_fp32_vs_fp64(ads, cuda, cfgs):
+    cfg, shots, vt, v0 = cfgs.c5_uneven()
+    s = max(shots, key=lambda d: d["nstep"])
+    assert s["nstep"] >= 5900
+    p64 = cfgs.acoustic_plan(ads, cfg, [s], "f64", ckpt_every=100)
+    obs = p64.forward(dev(vt)).clone()
+    l64, g64, tr64 = p64.gradient(dev(v0), obs, want_traces=True)
+    torch.cuda.synchronize()
+    p64.close()
+    p32 = cfgs.acoustic_plan(ads, cfg, [s], "f32", ckpt_every=100)
+    l32, g32, tr32 = p32.gradient(dev(v0), obs.float(), want_traces=True)
+    torch.cuda.synchronize()
+    p32.close()
+    tr64, tr32 = tr64.cpu().numpy(), tr32.double().cpu().numpy()
+    rg = rel(g32.cpu().numpy(), g64.cpu().numpy())
+    rt = rel(tr32, tr64)
+    per = cfgs.per_trace_rel(tr32, tr64, len(s["rcvi"]))
+    report(f"C5 longest shot FP32 vs FP64 ({s['nx']} x {cfg['MY']}, {s['nstep']} steps)",
+           grad=rg, traces=rt, trace_max=float(per.max()), trace_median=float(np.median(per)))
+    assert rg <= TOL32_GRAD
+    assert rt <= TOL32_TRACE
+
+
+# ------------------------------------------------------------------ C2
+
+def test_c2_fp64_gradient_central_differences(ads, cuda, cfgs):
+    """16 random interior cells (outside the PML) among those whose gradient is
+    at least 1% of the largest; eps = 1e-4 vp."""
+    cfg, shots, vt, v0 = cfgs.c2_fwi()
+    plan = cfgs.acoustic_plan(ads, cfg, shots, "f64", ckpt_every=100)
+    obs = plan.forward(dev(vt)).clone()
+    vd = dev(v0)
+    _, g = plan.gradient(vd, obs)
+    g = g.cpu().numpy()
+    npml, MX, MY = cfg["npml"], cfg["MX"], cfg["MY"]
+    inner = np.zeros_like(g, dtype=bool)
+    inner[npml + 1:MX - npml + 1, npml + 1:MY - npml + 1] = True
+    cand = np.argwhere(inner & (np.abs(g) >= 1e-2 * np.abs(g[inner]).max()))
+    rng = np.random.default_rng(2)
+    cells = cand[rng.choice(len(cand), 16, replace=False)]
+
+    def loss(v):
+        d = plan.forward(v) - obs
+        return float(torch.sum(d * d))
+
+    errs = []
+    for i, j in cells:
+        eps = 1e-4 * v0[i, j]
+        vp_, vm_ = vd.clone(), vd.clone()
+        vp_[i, j] += eps
+        vm_[i, j] -= eps
+        fd = (loss(vp_) - loss(vm_)) / (2 * eps)
+        errs.append(abs(fd - g[i, j]) / abs(g[i, j]))
+    plan.close()
+    report("C2 FD on 16 cells, 400^2 x 2000 steps x 8 shots", max_rel=max(errs),
+           median_rel=float(np.median(errs)))
+    assert max(errs) <= TOL_FD
+
+
+# ------------------------------------------------------------------ C4
+
+@pytest.fixture(scope="module")
+def c4(cfgs):
+    return cfgs.c4_elastic(nshots=32)
+
+
+def test_c4_fp32_vs_fp64_full_length(ads, cuda, cfgs, c4):
+    p, shots, lam, mu, rho = c4
+    pick = [shots[3], shots[20]]
+    t = lambda a: dev(a.reshape(-1))
+    l0, m0, r0 = (t(a) for a in cfgs.c4_start_model(lam, mu, rho))
+    p64 = ads.ElasticPlan(p, pick, precision="f64", ckpt_every=100)
+    obs = p64.forward(t(lam), t(mu), t(rho)).clone()
+    out64 = p64.gradient(l0, m0, r0, obs, want_traces=True)
+    torch.cuda.synchronize()
+    p64.close()
+    p32 = ads.ElasticPlan(p, pick, precision="f32", ckpt_every=100)
+    out32 = p32.gradient(l0, m0, r0, obs.float(), want_traces=True)
+    torch.cuda.synchronize()
+    p32.close()
+    rg = {k: rel(a.cpu().numpy(), b.cpu().numpy())
+          for k, a, b in zip(("lambda", "mu", "rho"), out32[1:4], out64[1:4])}
+    tr32, tr64 = out32[4].double().cpu().numpy(), out64[4].cpu().numpy()
+    n = 600 * (p.NSTEP + 1)
+    rt = max(rel(tr32[k * n:(k + 1) * n], tr64[k * n:(k + 1) * n]) for k in range(2))
+    # elastic traces are (nrcv, NSTEP+1) rows
+    per = np.concatenate([cfgs.per_trace_rel(tr32[k * n:(k + 1) * n].reshape(600, -1).T,
+                                             tr64[k * n:(k + 1) * n].reshape(600, -1).T, 600)
+                          for k in range(2)])
+    report("C4 FP32 vs FP64, 2 shots x 4000 steps", grad_lambda=rg["lambda"],
+           grad_mu=rg["mu"], grad_rho=rg["rho"], traces=rt, trace_max=float(per.max()),
+           trace_median=float(np.median(per)))
+    assert max(rg.values()) <= TOL32_GRAD
+    assert rt <= TOL32_TRACE
+
+
+def test_c4_fp64_plan_matches_oracle(ads, orc, cuda, cfgs):
+    """Traces over 1000 steps and the gradient over 150 steps of one C4 shot."""
+    for T, what in ((1000, "traces"), (150, "gradient")):
+        p, shots, lam, mu, rho = cfgs.c4_elastic(nshots=32, T=T)
+        s = shots[20]
+        ax, bx, kx, ay, by, ky = (a.reshape(-1) for a in ads.compute_elastic_PML_Params(p))
+        plan = ads.ElasticPlan(p, [s], precision="f64", ckpt_every=50)
+        t = lambda a: dev(a.reshape(-1))
+        args = (p.NX, p.NY, T, p.DELTAT, p.DELTAX, p.DELTAY, ax, bx, ay, by)
+        if what == "traces":
+            tr = plan.forward(t(lam), t(mu), t(rho)).cpu().numpy()
+            ref = orc.elastic_forward(*args, lam.reshape(-1), mu.reshape(-1), rho.reshape(-1),
+                                      s["srci"], s["srcj"], s["srctype"], s["srcv"],
+                                      s["rcvi"], s["rcvj"], s["rcvtype"])
+            r = rel(tr, ref.reshape(-1))
+        else:
+            obs = plan.forward(t(lam), t(mu), t(rho)).clone()
+            st = cfgs.c4_start_model(lam, mu, rho)
+            loss, gl, gm, gr = plan.gradient(*(t(a) for a in st), obs)
+            torch.cuda.synchronize()
+            ref = orc.elastic_gradient(*args, *(a.reshape(-1) for a in st), s["srci"],
+                                       s["srcj"], s["srctype"], s["srcv"], s["rcvi"], s["rcvj"],
+                                       s["rcvtype"], obs.cpu().numpy())
+            r = max(rel(a.cpu().numpy(), b) for a, b in zip((gl, gm, gr), ref[1:]))
+            assert abs(float(loss) - ref[0]) <= TOL64 * ref[0]
+        plan.close()
+        report(f"C4 FP64 plan {what} vs oracle, {T} steps", rel=r)
+        assert r <= TOL64

@@ -82,11 +82,13 @@ def test_mat_v73_and_lfs_pointers_rejected(ads, tmp_path):
         ads.load_acoustic_model(str(f))
 
 
-BP = os.path.join("/root/reference", "examples", "invert_velocity_model", "models",
+REF_SRC = os.environ.get("ADS_REFERENCE_SRC", "")
+BP = os.path.join(REF_SRC, "examples", "invert_velocity_model", "models",
                   "BP-model-smooth.mat")
 
 
-@pytest.mark.skipif(not os.path.exists(BP), reason="reference checkout not present")
+@pytest.mark.skipif(not REF_SRC or not os.path.exists(BP),
+                    reason="ADS_REFERENCE_SRC does not name a reference checkout")
 def test_reference_bp_model_loads(ads):
     m = ads.load_acoustic_model(BP)
     srcs, rcvs = ads.load_acoustic_source(BP), ads.load_acoustic_receiver(BP)

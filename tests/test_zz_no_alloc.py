@@ -1,7 +1,8 @@
 """The allocation-free elastic step transpose (ads_elastic_step_bwd_f64_noalloc).
 
 It serves callers that cannot allocate device memory while the step runs (for
-example code inside another framework's stream capture).  Its scratch is a fixed
+example an operator inside another framework's custom-call hook, where that
+framework owns the device memory).  Its scratch is a fixed
 array inside the library, shared by every call, so this test checks it against
 the allocating entry point ads_elastic_step_bwd_f64 on two calls in a row with
 different inputs: the second call must not see the first call's scratch.  The
