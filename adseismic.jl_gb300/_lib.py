@@ -92,7 +92,9 @@ _SIGS = {
     "ads_get_receive_f64": [P] * 6 + [I64, P, P, P, I64, I64, I64, P],
     "ads_get_receive_bwd_f64": [P] * 6 + [I64, P, P, P, I64, I64, I64, P],
     "ads_elastic_step_fwd_f64": [P] * 11 + [D, D, D, I64, I64, P, P, P, P, I64, P],
+    "ads_elastic_step_fwd_f32": [P] * 11 + [D, D, D, I64, I64, P, P, P, P, I64, P],
     "ads_elastic_step_bwd_f64": [P] * 13 + [D, D, D, I64, I64, P],
+    "ads_elastic_step_bwd_f32": [P] * 13 + [D, D, D, I64, I64, P],
     "ads_elastic_step_bwd_f64_noalloc": [P] * 13 + [D, D, D, I64, I64, P],
     "ads_acoustic_pml_profiles": [I64, I64, D, D, I64, D, D, I32, P, P],
     "ads_elastic_cpml_profiles": [I64, I64, D, D, D, I64, D, D, D, D, D, I32] + [P] * 6,

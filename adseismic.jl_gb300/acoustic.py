@@ -162,17 +162,21 @@ class AcousticPlan:
     resident_segments / resident_mem_pct: how many of the last checkpoint
     segments keep their forward wavefields on the device instead of being
     recomputed in the reverse sweep (-1 none, 0 as many as fit in
-    resident_mem_pct percent, default 50, of the free device memory)."""
+    resident_mem_pct percent, default 50, of the free device memory).
+    variant: ADS_VARIANT_W (the custom operators' form, phi / psi from the old
+    field; PropagatorKernel 1 and 2) or ADS_VARIANT_U (one_step, phi / psi
+    from the new field; PropagatorKernel 0, the reference's default)."""
 
     def __init__(self, MX, MY, dx, dy, dt, shots, npml=12, Rcoef=0.001, vp_ref=1000.0,
                  use_pml=15, precision="f64", use_graph=True, ckpt_every=0,
                  rows_per_thread=0, steps_per_block=0, block_rows=0, autotune=False,
-                 resident_segments=0, resident_mem_pct=0, stream=None):
+                 resident_segments=0, resident_mem_pct=0, stream=None,
+                 variant=ADS_VARIANT_W):
         cfg = _lib.AcousticConfig()
         cfg.MX, cfg.MY, cfg.dx, cfg.dy, cfg.dt = MX, MY, dx, dy, dt
         cfg.npml, cfg.Rcoef, cfg.vp_ref, cfg.use_pml = npml, Rcoef, vp_ref, use_pml
         cfg.precision = ADS_F64 if precision == "f64" else ADS_F32
-        cfg.variant = ADS_VARIANT_W
+        cfg.variant = int(variant)
         cfg.use_graph = int(bool(use_graph))
         cfg.ckpt_every = ckpt_every
         cfg.rows_per_thread = rows_per_thread
@@ -307,10 +311,10 @@ class AcousticPlan:
 class AcousticPropagator:
     """Result handle of AcousticPropagatorSolver (src/Struct.jl:140-147).
     Receiver traces come from SimulatedObservation without any history (the
-    plans keep O(1) steps per shot).  The reference's u, phi and psi fields,
-    the (NSTEP+1, NX+2, NY+2) histories, are formed on first access by the
-    FP64 single-step operator chain in the form PropagatorKernel selects,
-    and kept on the device."""
+    plans keep O(1) steps per shot, in the form PropagatorKernel selects).
+    The reference's u, phi and psi fields, the (NSTEP+1, NX+2, NY+2)
+    histories, are formed on first access by the FP64 single-step operator
+    chain in that form, and kept on the device."""
 
     def __init__(self, param, src, vp, precision):
         self.param, self.src, self.vp, self.precision = param, src, vp, precision
@@ -351,10 +355,9 @@ def step_variant(param: AcousticPropagatorParams) -> int:
 
 def AcousticPropagatorSolver(param: AcousticPropagatorParams, src: AcousticSource, vp,
                              precision="f64"):
-    """src/Core.jl:562-620 (c = vp^2, PML from param, zero initial slots).
-    PropagatorKernel 1 and 2 (the custom operator's form) run on the batched
-    plans; 0 (one_step, phi / psi from the new u, which the plans do not
-    implement) runs the single-step operator chain in FP64."""
+    """src/Core.jl:562-620 (c = vp^2, PML from param, zero initial slots), in
+    the form param.PropagatorKernel selects; traces and gradients run on the
+    batched plans."""
     step_variant(param)
     return AcousticPropagator(param, src, vp, precision)
 
@@ -367,13 +370,10 @@ def _shot_dict(param, src, rcv):
 def SimulatedObservation(ap: AcousticPropagator, rcv: AcousticReceiver):
     """src/Core.jl:726-730: fills rcv.rcvv with the (NSTEP+1, nrcv) traces."""
     p = ap.param
-    if step_variant(p) == ADS_VARIANT_U:
-        rcv.rcvv = _chain_forward(p, ap.src, rcv, ap.vp)[0].view(p.NSTEP + 1, len(rcv.rcvi))
-        torch.cuda.current_stream().synchronize()
-        return rcv.rcvv
     plan = AcousticPlan(p.NX, p.NY, p.DELTAX, p.DELTAY, p.DELTAT, [_shot_dict(p, ap.src, rcv)],
                         npml=p.NPOINTS_PML, Rcoef=p.Rcoef, vp_ref=p.vp_ref,
-                        use_pml=p.use_pml, precision=ap.precision, use_graph=False)
+                        use_pml=p.use_pml, precision=ap.precision, use_graph=False,
+                        variant=step_variant(p))
     vp = torch.as_tensor(ap.vp, dtype=torch.float64, device="cuda").reshape(p.NX + 2, p.NY + 2)
     tr = plan.forward(vp)
     torch.cuda.current_stream().synchronize()
@@ -390,15 +390,11 @@ def compute_forward_GPU(param: AcousticPropagatorParams, srcs, rcvs, vp, precisi
         from .elastic import compute_forward_GPU as elastic_forward
 
         return elastic_forward(param, srcs, rcvs, vp, precision)
-    if step_variant(param) == ADS_VARIANT_U:
-        out = [_chain_forward(param, s, r, vp)[0].view(param.NSTEP + 1, len(r.rcvi))
-               for s, r in zip(srcs, rcvs)]
-        torch.cuda.current_stream().synchronize()
-        return out
     shots = [_shot_dict(param, s, r) for s, r in zip(srcs, rcvs)]
     plan = AcousticPlan(param.NX, param.NY, param.DELTAX, param.DELTAY, param.DELTAT, shots,
                         npml=param.NPOINTS_PML, Rcoef=param.Rcoef, vp_ref=param.vp_ref,
-                        use_pml=param.use_pml, precision=precision, use_graph=False)
+                        use_pml=param.use_pml, precision=precision, use_graph=False,
+                        variant=step_variant(param))
     vp = torch.as_tensor(vp, dtype=torch.float64, device="cuda").reshape(param.NX + 2,
                                                                          param.NY + 2)
     out = [t.clone() for t in plan.split_traces(plan.forward(vp))]
@@ -408,33 +404,43 @@ def compute_forward_GPU(param: AcousticPropagatorParams, srcs, rcvs, vp, precisi
 
 
 def compute_loss_and_grads_GPU(param: AcousticPropagatorParams, srcs, rcvs, Rs, vp,
-                               precision="f64", ckpt_every=0):
+                               precision="f64", ckpt_every=0, aux_loss=None, as_lists=False):
     """src/Utils.jl:300-332 for one GPU: loss = sum over shots of sum((rcvv - Rs)^2)
-    and its gradient w.r.t. vp, all shots in one batched plan.  With
-    ElasticPropagatorParams the model is (rho, lambda, mu) and the result
-    (loss, grad_lambda, grad_mu, grad_rho)."""
+    and its gradient w.r.t. vp, all shots in one batched plan, in the form
+    param.PropagatorKernel selects.
+
+    aux_loss: an extra term added to the loss before differentiating (the
+    reference's aux_loss, src/Utils.jl:309-311): a float, or a callable
+    vp -> (value, d value / d vp) when the term depends on the model.
+    as_lists: return ([loss], [grad]), the per-GPU lists the reference returns
+    (src/Utils.jl:321-331), here for its one GPU.  With ElasticPropagatorParams
+    the model is (rho, lambda, mu) and the result (loss, grad_lambda, grad_mu,
+    grad_rho)."""
     if not isinstance(param, AcousticPropagatorParams):
         from .elastic import compute_loss_and_grads_GPU as elastic_grads
 
-        return elastic_grads(param, srcs, rcvs, Rs, vp, precision, ckpt_every)
-    if step_variant(param) == ADS_VARIANT_U:
-        loss, grad = 0.0, 0.0
-        for s, r, o in zip(srcs, rcvs, Rs):
-            l, g = dropin_loss_and_grad(param, s, r, o, vp)
-            loss, grad = loss + l, grad + g
-        torch.cuda.current_stream().synchronize()
-        return loss, grad
+        return elastic_grads(param, srcs, rcvs, Rs, vp, precision, ckpt_every, aux_loss,
+                             as_lists)
     shots = [_shot_dict(param, s, r) for s, r in zip(srcs, rcvs)]
     plan = AcousticPlan(param.NX, param.NY, param.DELTAX, param.DELTAY, param.DELTAT, shots,
                         npml=param.NPOINTS_PML, Rcoef=param.Rcoef, vp_ref=param.vp_ref,
                         use_pml=param.use_pml, precision=precision, use_graph=False,
-                        ckpt_every=ckpt_every)
+                        ckpt_every=ckpt_every, variant=step_variant(param))
     vp = torch.as_tensor(vp, dtype=torch.float64, device="cuda").reshape(param.NX + 2,
                                                                          param.NY + 2)
     obs = plan.pack([torch.as_tensor(r, device="cuda") for r in Rs])
     loss, grad = plan.gradient(vp, obs)
-    torch.cuda.current_stream().synchronize()
     plan.close()
+    if aux_loss is not None:
+        if callable(aux_loss):
+            v, g = aux_loss(vp)
+            loss = loss + v
+            grad = grad + torch.as_tensor(g, dtype=torch.float64, device=grad.device)
+        else:
+            loss = loss + float(aux_loss)
+    torch.cuda.current_stream().synchronize()
+    if as_lists:
+        return [loss], [grad]
     return loss, grad
 
 

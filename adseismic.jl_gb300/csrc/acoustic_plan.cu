@@ -282,7 +282,12 @@ __device__ __forceinline__ void record_traces(const AcItem& it, const AcShot<T>&
 // (sigma = tau = 0 on every row and column it reads, classified on the host)
 // and only the plain wave update is compiled, so the kernel needs few
 // registers and keeps many warps resident; INT = false: the general PML form.
-template <typename T, int MODE, bool INT>
+//
+// VU = true (variant U, PML items only): phi_{t-1} and psi_{t-1} were formed
+// from u_{t-1} by k_ac_phi_u at the start of this step, so this kernel only
+// reads them (as the custom-operator form reads its phi_{t-1}, psi_{t-1}) and
+// writes neither; its checkpoints store the phi / psi it read.
+template <typename T, int MODE, bool INT, bool VU = false>
 __global__ void __launch_bounds__(Tile<T>::TPB, INT ? Tile<T>::MINB_FI : Tile<T>::MINB_F)
 k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
          const CellRef* __restrict__ srcs, const CellRef* __restrict__ rcvs, AcConst<T> K,
@@ -454,11 +459,13 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
           if (r.cell == row + c) v += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
         }
         vo.v[c] = v;
-        po.v[c] = (T(1) - K.dt * sg) * p0.v[c] + K.ex * cv * (tj[c] - sg) * (wp.v[c] - wm.v[c]);
-        qo.v[c] = (T(1) - K.dt * tj[c]) * q0.v[c] + K.ey * cv * (sg - tj[c]) * (wN - wS);
+        if constexpr (!VU) {
+          po.v[c] = (T(1) - K.dt * sg) * p0.v[c] + K.ex * cv * (tj[c] - sg) * (wp.v[c] - wm.v[c]);
+          qo.v[c] = (T(1) - K.dt * tj[c]) * q0.v[c] + K.ey * cv * (sg - tj[c]) * (wN - wS);
+        }
       }
       stv<T, C>(out, row, vo, j, ny);
-      if (n0) {
+      if (!VU && n0) {
         stv<T, C>(pout, row, po, j, ny);
         stv<T, C>(qout, row, qo, j, ny);
       }
@@ -467,8 +474,8 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
         stv<T, C>(ck, row, vo, j, ny);
         stv<T, C>(ck + fs, row, w0, j, ny);
         if (n0) {
-          stv<T, C>(ck + 2 * fs, row, po, j, ny);
-          stv<T, C>(ck + 3 * fs, row, qo, j, ny);
+          stv<T, C>(ck + 2 * fs, row, VU ? p0 : po, j, ny);
+          stv<T, C>(ck + 3 * fs, row, VU ? q0 : qo, j, ny);
         }
       }
     }
@@ -586,17 +593,52 @@ __device__ __forceinline__ void add_grad(const AcShot<T>& sh, int64_t row, const
 // cell (t >= 2), so d loss / d srcv[t-1] = dt^2 lambdaU_t there.  After the
 // adjoint step k (and the residuals of slot k-1) lambdaU_{k-1} is final: the
 // warp that wrote a source cell records it.
-template <typename T, int C>
+//
+// Variant U: the source value also left phi_{k-1} and psi_{k-1} (the pre-pass
+// formed them from u_{k-1} less its source value), so d loss / d srcv is
+// lambdaU_{k-1} less the part of it that came back through phi_{k-1},
+// psi_{k-1}: Q = sum over the four neighbours of what their lambdaPhi_{k-1},
+// lambdaPsi_{k-1} (lp, lq, written by the pre-pass) sent to the cell.
+//
+// An item's source list may hold sources of neighbouring cells (variant U
+// lists also carry those within one cell of the item); only the warp owning a
+// source's cell (its rows and the strip's columns) records it.
+template <typename T, int C, bool VU>
 __device__ __forceinline__ void record_src_grad(const AcItem& it, const AcShot<T>& sh,
                                                 const CellRef* __restrict__ srcs, const T* lun,
+                                                const T* lp, const T* lq, const AcConst<T>& K,
                                                 int k, int lane, int i0, int i_end, double dt2) {
   if (k - 1 < 2 || it.src_e <= it.src_b) return;
   __syncwarp();
   for (int e = it.src_b + lane; e < it.src_e; e += 32) {
     const CellRef r = srcs[e];
-    if (r.row >= i0 && r.row < i_end)
-      sh.gsrc[(int64_t)(k - 2) * sh.nsrc + r.idx] = dt2 * (double)lun[r.cell];
+    const int jc = (int)(r.cell - (int64_t)r.row * sh.pitch) - JOFF;
+    if (r.row < i0 || r.row >= i_end || jc < it.j0 || jc >= it.j0 + 32 * C) continue;
+    double g = (double)lun[r.cell];
+    if constexpr (VU) {
+      const int64_t P = sh.pitch, x = r.cell;
+      const T* cc = sh.c;
+      const T sm = sh.sx[r.row - 1], s0 = sh.sx[r.row], sp = sh.sx[r.row + 1];
+      const T tm = sh.ty[jc - 1], t0 = sh.ty[jc], tp = sh.ty[jc + 1];
+      const T q = K.ex * cc[x - P] * (t0 - sm) * lp[x - P] - K.ex * cc[x + P] * (t0 - sp) * lp[x + P] +
+                  K.ey * cc[x - 1] * (s0 - tm) * lq[x - 1] - K.ey * cc[x + 1] * (s0 - tp) * lq[x + 1];
+      g -= (double)q;
+    }
+    sh.gsrc[(int64_t)(k - 2) * sh.nsrc + r.idx] = dt2 * g;
   }
+}
+
+// The source value added to u_t at pitched cell `cell` (0 where none; t >= 2):
+// the sum over the item's listed sources there, as the forward injects them.
+template <typename T>
+__device__ __forceinline__ T src_at(const AcItem& it, const AcShot<T>& sh,
+                                    const CellRef* __restrict__ srcs, int64_t cell, int t) {
+  T v = T(0);
+  for (int e = it.src_b; e < it.src_e; e++) {
+    const CellRef r = srcs[e];
+    if (r.cell == cell) v += sh.srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
+  }
+  return v;
 }
 
 // Residuals of step k-1 go to receiver cells this warp's lanes wrote in the
@@ -625,7 +667,14 @@ __device__ __forceinline__ void inject_residuals(const AcItem& it, const AcShot<
 // (flushed into the FP64 accumulator at the end of each segment); FP64 plans
 // accumulate in FP64.
 // Items, warps and INT as in k_ac_fwd.
-template <typename T, bool INT>
+//
+// VU = true (variant U, PML items only): k_ac_adjphi_u has already formed
+// lambdaPhi_{k-1}, lambdaPsi_{k-1} (the adjoints of the phi_{k-1}, psi_{k-1}
+// that step k reads); lambdaU_{k-1} takes its phi / psi terms from those
+// instead of from lambdaPhi_k, lambdaPsi_k, the grad_c terms of phi_{k-1},
+// psi_{k-1} use them too (with u_{k-1} less its source value, as the forward
+// pre-pass formed them), and the kernel writes no lambdaPhi / lambdaPsi.
+template <typename T, bool INT, bool VU = false>
 __global__ void __launch_bounds__(Tile<T>::TPB, INT ? Tile<T>::MINB_AI : Tile<T>::MINB_A)
 k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
          const CellRef* __restrict__ srcs, const CellRef* __restrict__ rcvs, AcConst<T> K,
@@ -641,9 +690,11 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   const T* w = sh.seg + (int64_t)(k - 1 - base) * fs;   // u_{k-1}
   T* lun = sh.lu + (int64_t)((k + 1) & 1) * fs;         // in: lambdaU_{k+1}; out: _{k-1}
   const T* luc = sh.lu + (int64_t)(k & 1) * fs;         // lambdaU_k
-  const T* lpc = sh.lp + (int64_t)(k & 1) * fs;
+  // lambdaPhi / lambdaPsi read by this step: those of step k (variant W), or
+  // those of phi_{k-1}, psi_{k-1} from the pre-pass (variant U)
+  const T* lpc = sh.lp + (int64_t)((VU ? k - 1 : k) & 1) * fs;
   T* lpo = sh.lp + (int64_t)((k - 1) & 1) * fs;
-  const T* lqc = sh.lq + (int64_t)(k & 1) * fs;
+  const T* lqc = sh.lq + (int64_t)((VU ? k - 1 : k) & 1) * fs;
   T* lqo = sh.lq + (int64_t)((k - 1) & 1) * fs;
   const T* __restrict__ cc = sh.c;
   const T* __restrict__ sx = sh.sx;
@@ -770,7 +821,7 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     }
     if constexpr (!INT) {
       inject_residuals<T, C>(it, sh, rcvs, lun, k, lane, i0, i_end);
-      record_src_grad<T, C>(it, sh, srcs, lun, k, lane, i0, i_end, dt2);
+      record_src_grad<T, C, VU>(it, sh, srcs, lun, lpc, lqc, K, k, lane, i0, i_end, dt2);
     }
   } else {
   // rows i-1 (m), i (0), i+1 (p): lambdaU_k, lambdaPhi_k, c and 1/den per cell
@@ -855,14 +906,27 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
         const T cv = c0.v[c], s = sg0 + tj[c];
         nu.v[c] = -(T(1) - s * K.hdt) * inv0.v[c] * ln.v[c] +
                   (T(2) - sg0 * tj[c] * K.dt2 - K.kxy * cv) * gui[c] + XPm + XMp + ypl + ymr;
-        np.v[c] = (T(1) - K.dt * sg0) * gp0.v[c] + K.fx * guim - K.fx * guip;
-        nq.v[c] = (T(1) - K.dt * tj[c]) * gq.v[c] + yrl - yrr;
+        if constexpr (!VU) {
+          np.v[c] = (T(1) - K.dt * sg0) * gp0.v[c] + K.fx * guim - K.fx * guip;
+          nq.v[c] = (T(1) - K.dt * tj[c]) * gq.v[c] + yrl - yrr;
+        }
+        T dx_ = wp.v[c] - wm.v[c], dy_ = wN - wS;
+        if constexpr (VU) {
+          // u_{k-1} without its source value, as the forward pre-pass used it
+          if (k - 1 >= 2 && it.src_e > it.src_b) {
+            const T sp = src_at(it, sh, srcs, row + P + c, k - 1),
+                    sm = src_at(it, sh, srcs, row - P + c, k - 1);
+            const T sn = src_at(it, sh, srcs, row + c + 1, k - 1),
+                    ss = src_at(it, sh, srcs, row + c - 1, k - 1);
+            dx_ = (wp.v[c] - sp) - (wm.v[c] - sm);
+            dy_ = (wN - sn) - (wS - ss);
+          }
+        }
         g[c] = (-K.kxy * w0.v[c] + K.cx * (wp.v[c] + wm.v[c]) + K.cy * (wN + wS)) * gui[c] +
-               K.ex * (tj[c] - sg0) * (wp.v[c] - wm.v[c]) * gp0.v[c] +
-               K.ey * (sg0 - tj[c]) * (wN - wS) * gq.v[c];
+               K.ex * (tj[c] - sg0) * dx_ * gp0.v[c] + K.ey * (sg0 - tj[c]) * dy_ * gq.v[c];
       }
       stv<T, C>(lun, row, nu, j, ny);
-      if (n0) {
+      if (!VU && n0) {
         stv<T, C>(lpo, row, np, j, ny);
         stv<T, C>(lqo, row, nq, j, ny);
       }
@@ -877,7 +941,196 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     n0 = n1;
   }
   inject_residuals<T, C>(it, sh, rcvs, lun, k, lane, i0, i_end);
-  record_src_grad<T, C>(it, sh, srcs, lun, k, lane, i0, i_end, dt2);
+  record_src_grad<T, C, VU>(it, sh, srcs, lun, lpc, lqc, K, k, lane, i0, i_end, dt2);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Variant U (one_step, src/Core.jl:528-549, the reference's default
+// PropagatorKernel = 0): phi and psi are updated from the NEW field,
+//   u_t = F(u_{t-1}, u_{t-2}, phi_{t-1}, psi_{t-1}) (+ source),
+//   phi_t = (1 - dt sigma) phi_{t-1} + dt c (tau - sigma) / (2 hx) (u_t(i+1) - u_t(i-1)),
+// with u_t taken before its source value is added (the loop adds the source
+// after one_step).  A step kernel cannot form phi_t from u_t at its tile's
+// edges (the neighbouring tiles write u_t in the same launch), so the update
+// of phi_{t-1}, psi_{t-1} moves to the start of step t, where u_{t-1} is in
+// memory: k_ac_phi_u forms them (PML items only; elsewhere they stay 0), then
+// the step kernel (k_ac_fwd<..., VU = true>) computes u_t from them exactly as
+// the custom-operator form does.  The reverse sweep mirrors it: k_ac_adjphi_u
+// forms lambdaPhi_{k-1}, lambdaPsi_{k-1} from lambdaU_k, then
+// k_ac_adj<..., VU = true> uses them.  phi_NSTEP is never formed: no trace
+// depends on it.
+// ---------------------------------------------------------------------------
+
+// phi_{t-1}, psi_{t-1} from phi_{t-2}, psi_{t-2} and u_{t-1} less its source
+// value (PML items, forward step t; MODE as k_ac_fwd).  Ring parity: step t
+// reads phi from set (t-1) & 1, so phi_{t-2} is in set t & 1.
+template <typename T, int MODE>
+__global__ void __launch_bounds__(Tile<T>::TPB, Tile<T>::MINB_F)
+k_ac_phi_u(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
+           const CellRef* __restrict__ srcs, AcConst<T> K, int t, int base, int ri) {
+  constexpr bool SEG = MODE != 0;
+  constexpr int C = Tile<T>::CF;
+  using V = Vec<T, C>;
+  const AcItem it = items[blockIdx.x];
+  const AcShot<T>& sh = shots[it.shot];
+  const int lane = threadIdx.x & 31;
+  const int j = it.j0 + lane * C;
+  const int nx = sh.nx, ny = sh.ny;
+  const int64_t P = sh.pitch, fs = sh.fs;
+  const T* w = SEG ? sh.seg + (int64_t)(t - 1 - base) * fs : sh.u + (int64_t)((t - 1) & 1) * fs;
+  const T* pin = sh.p + (int64_t)(t & 1) * fs;
+  T* pout = sh.p + (int64_t)((t - 1) & 1) * fs;
+  const T* qin = sh.q + (int64_t)(t & 1) * fs;
+  T* qout = sh.q + (int64_t)((t - 1) & 1) * fs;
+  const T* __restrict__ cc = sh.c;
+  const T* __restrict__ sx = sh.sx;
+  const T* __restrict__ ty = sh.ty;
+  const bool jld = j <= ny + 1;
+  const bool hr = j + C <= ny + 1;
+  const int64_t col = j + JOFF;
+  T tj[C];
+#pragma unroll
+  for (int c = 0; c < C; c++) tj[c] = (j + c <= ny + 1) ? ty[j + c] : T(0);
+  const bool tfree = warp_tau_free<T, C>(ty, j, ny);
+  auto nz = [&](int r) { return !(tfree && sx[r] == T(0)); };
+  const int i0 = it.i0 + (threadIdx.x >> 5) * ri, i_end = min(i0 + ri, nx + 1);
+  if (i0 > nx) return;
+  auto off = [&](int r) { return (int64_t)r * P + col; };
+  const bool srcd = t - 1 >= 2 && it.src_e > it.src_b;  // u_{t-1} received source values
+  const int64_t hoff = lane == 0 ? -1 : C;
+  const bool hon = (lane == 0 && jld) || (lane == 31 && hr);
+  V wm = ldvp<T, C>(w, off(i0 - 1), jld), w0 = ldvp<T, C>(w, off(i0), jld),
+    wp = ldvp<T, C>(w, off(i0 + 1), jld);
+  bool n0 = nz(i0);
+  V p0 = ldvp<T, C>(pin, off(i0), jld && n0), q0 = ldvp<T, C>(qin, off(i0), jld && n0),
+    c0 = ldvp<T, C>(cc, off(i0), jld && n0);
+  T hw = ld1p(w + off(i0) + hoff, hon && n0);
+  for (int i = i0; i < i_end; i++) {
+    const int64_t row = off(i);
+    const bool more = i + 1 < i_end;
+    const bool n1 = more && nz(i + 1);
+    V wn = ldvp<T, C>(w, off(i + 2), jld && more);
+    V pn = ldvp<T, C>(pin, off(i + 1), jld && n1), qn = ldvp<T, C>(qin, off(i + 1), jld && n1),
+      cn = ldvp<T, C>(cc, off(i + 1), jld && n1);
+    const T hwn = ld1p(w + row + P + hoff, more && hon && n1);
+    T wL = __shfl_up_sync(FULL, w0.v[C - 1], 1), wR = __shfl_down_sync(FULL, w0.v[0], 1);
+    if (lane == 0) wL = hw;
+    else if (lane == 31) wR = hw;
+    if (jld && n0) {
+      const T sg = sx[i];
+      V po, qo;
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        const T wS = c == 0 ? wL : w0.v[c - 1];
+        const T wN = c == C - 1 ? wR : w0.v[c + 1];
+        T dx_ = wp.v[c] - wm.v[c], dy_ = wN - wS;
+        if (srcd) {
+          const T sp = src_at(it, sh, srcs, row + P + c, t - 1),
+                  sm = src_at(it, sh, srcs, row - P + c, t - 1);
+          const T sn = src_at(it, sh, srcs, row + c + 1, t - 1),
+                  ss = src_at(it, sh, srcs, row + c - 1, t - 1);
+          dx_ = (wp.v[c] - sp) - (wm.v[c] - sm);
+          dy_ = (wN - sn) - (wS - ss);
+        }
+        po.v[c] = (T(1) - K.dt * sg) * p0.v[c] + K.ex * c0.v[c] * (tj[c] - sg) * dx_;
+        qo.v[c] = (T(1) - K.dt * tj[c]) * q0.v[c] + K.ey * c0.v[c] * (sg - tj[c]) * dy_;
+      }
+      stv<T, C>(pout, row, po, j, ny);
+      stv<T, C>(qout, row, qo, j, ny);
+    }
+    wm = w0;
+    w0 = wp;
+    wp = wn;
+    p0 = pn;
+    q0 = qn;
+    c0 = cn;
+    hw = hwn;
+    n0 = n1;
+  }
+}
+
+// lambdaPhi_{k-1}, lambdaPsi_{k-1} (the adjoints of the phi_{k-1}, psi_{k-1}
+// that forward step k read) from lambdaPhi_k, lambdaPsi_k and lambdaU_k: the
+// transpose of phi_{k-1}'s appearance in u_k and in phi_k (PML items of the
+// adjoint tiling).  The same expressions as the variant-W kernel's
+// lambdaPhi / lambdaPsi.
+template <typename T>
+__global__ void __launch_bounds__(Tile<T>::TPB, Tile<T>::MINB_F)
+k_ac_adjphi_u(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
+              AcConst<T> K, int k, int ri) {
+  constexpr int C = Tile<T>::CA;
+  using V = Vec<T, C>;
+  const AcItem it = items[blockIdx.x];
+  const AcShot<T>& sh = shots[it.shot];
+  const int lane = threadIdx.x & 31;
+  const int j = it.j0 + lane * C;
+  const int nx = sh.nx, ny = sh.ny;
+  const int64_t P = sh.pitch, fs = sh.fs;
+  const T* luc = sh.lu + (int64_t)(k & 1) * fs;
+  const T* lpc = sh.lp + (int64_t)(k & 1) * fs;
+  T* lpo = sh.lp + (int64_t)((k - 1) & 1) * fs;
+  const T* lqc = sh.lq + (int64_t)(k & 1) * fs;
+  T* lqo = sh.lq + (int64_t)((k - 1) & 1) * fs;
+  const T* __restrict__ sx = sh.sx;
+  const T* __restrict__ ty = sh.ty;
+  const bool jld = j <= ny + 1;
+  const bool hr = j + C <= ny + 1;
+  const int64_t col = j + JOFF;
+  T tj[C];
+#pragma unroll
+  for (int c = 0; c < C; c++) tj[c] = (j + c <= ny + 1) ? ty[j + c] : T(0);
+  const bool tfree = warp_tau_free<T, C>(ty, j, ny);
+  auto nz = [&](int r) { return !(tfree && sx[r] == T(0)); };
+  const int i0 = it.i0 + (threadIdx.x >> 5) * ri, i_end = min(i0 + ri, nx + 1);
+  if (i0 > nx) return;
+  auto off = [&](int r) { return (int64_t)r * P + col; };
+  const int64_t hoff = lane == 0 ? -1 : C;
+  const bool hon = (lane == 0 && jld) || (lane == 31 && hr);
+  const T th = hon ? ty[j + (int)hoff] : T(0);
+  V gum = ldvp<T, C>(luc, off(i0 - 1), jld), gu0 = ldvp<T, C>(luc, off(i0), jld),
+    gup = ldvp<T, C>(luc, off(i0 + 1), jld);
+  bool n0 = nz(i0);
+  V gp0 = ldvp<T, C>(lpc, off(i0), jld && n0), gq0 = ldvp<T, C>(lqc, off(i0), jld && n0);
+  T hgu = ld1p(luc + off(i0) + hoff, hon && n0);
+  for (int i = i0; i < i_end; i++) {
+    const int64_t row = off(i);
+    const bool more = i + 1 < i_end;
+    const bool n1 = more && nz(i + 1);
+    V gun = ldvp<T, C>(luc, off(i + 2), jld && more);
+    V gpn = ldvp<T, C>(lpc, off(i + 1), jld && n1), gqn = ldvp<T, C>(lqc, off(i + 1), jld && n1);
+    const T hgun = ld1p(luc + row + P + hoff, more && hon && n1);
+    const T sgm = sx[i - 1], sg0 = sx[i], sgp = sx[i + 1];
+    // lambdaU / den of this thread's cells (row i), sent to the j-neighbours' psi
+    T YR[C];
+#pragma unroll
+    for (int c = 0; c < C; c++) YR[c] = K.fy * (gu0.v[c] * inv_den<T>(sg0 + tj[c], K));
+    T yrl = __shfl_up_sync(FULL, YR[C - 1], 1), yrr = __shfl_down_sync(FULL, YR[0], 1);
+    if (lane == 0 || lane == 31) {
+      const T h = hon ? K.fy * (hgu * inv_den<T>(sg0 + th, K)) : T(0);
+      if (lane == 0) yrl = h;
+      else yrr = h;
+    }
+    if (jld && n0) {
+      V np, nq;
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        const T guim = gum.v[c] * inv_den<T>(sgm + tj[c], K);
+        const T guip = gup.v[c] * inv_den<T>(sgp + tj[c], K);
+        const T l = c == 0 ? yrl : YR[c - 1], r = c == C - 1 ? yrr : YR[c + 1];
+        np.v[c] = (T(1) - K.dt * sg0) * gp0.v[c] + K.fx * guim - K.fx * guip;
+        nq.v[c] = (T(1) - K.dt * tj[c]) * gq0.v[c] + l - r;
+      }
+      stv<T, C>(lpo, row, np, j, ny);
+      stv<T, C>(lqo, row, nq, j, ny);
+    }
+    gum = gu0;
+    gu0 = gup;
+    gup = gun;
+    gp0 = gpn;
+    gq0 = gqn;
+    hgu = hgun;
+    n0 = n1;
   }
 }
 
@@ -1215,6 +1468,7 @@ template <typename T>
 struct AcPlan final : AcPlanBase {
   ads_acoustic_config cfg{};
   int nshots = 0;
+  bool vu = false;    // variant U: phi / psi from the new field (pre-pass kernels)
   int K = 0;          // checkpoint spacing
   // Resident segments: segments res_seg .. nseg_max-1 keep the forward
   // wavefields of their steps in the shots' stores (slot t - res_base), so
@@ -1246,10 +1500,11 @@ struct AcPlan final : AcPlanBase {
     AcItem* items = nullptr;  // interior items, then the PML items at pm_off
     CellRef *srcs = nullptr, *rcvs = nullptr;
     int pm_off = 0;
+    int vu = 0;  // variant U: the PML items get a pre-pass launch too
     std::vector<int> in_end, pm_end;
     int in_upto(int n) const { return n <= 0 ? 0 : in_end[n - 1]; }
     int pm_upto(int n) const { return n <= 0 ? 0 : pm_end[n - 1]; }
-    int launches(int n) const { return (in_upto(n) > 0) + (pm_upto(n) > 0); }
+    int launches(int n) const { return (in_upto(n) > 0) + (pm_upto(n) > 0) * (1 + vu); }
   };
   DevTiles tf, ta;  // forward / adjoint items
   // pm_rows > 0: PML items are cut into items of pm_rows-row tiles (more warps
@@ -1354,9 +1609,9 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
               "model size out of range");
   ADS_REQUIRE(c.dx > 0 && c.dy > 0 && c.dt > 0, "dx, dy, dt must be positive");
   ADS_REQUIRE(c.npml >= 1 && c.Rcoef > 0 && c.Rcoef < 1, "invalid PML parameters");
-  ADS_REQUIRE(c.variant == ADS_VARIANT_W,
-              "whole-path plans implement variant W (the custom-operator form); use the "
-              "single-step operators for variant U");
+  ADS_REQUIRE(c.variant == ADS_VARIANT_W || c.variant == ADS_VARIANT_U,
+              "variant must be ADS_VARIANT_W or ADS_VARIANT_U");
+  vu = c.variant == ADS_VARIANT_U;
   ADS_REQUIRE(c.ckpt_every >= 0 && c.rows_per_thread >= 0, "negative tuning parameter");
   for (int s = 0; s < ns; s++) {
     const ads_acoustic_shot& h = shots[s];
@@ -1432,6 +1687,8 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
               "steps_per_block must be 0 (automatic), 1, 2, 4 or 8");
   ADS_REQUIRE(sizeof(T) == 4 || c.steps_per_block <= 1,
               "time blocking is implemented for FP32 plans (steps_per_block 0 or 1 for FP64)");
+  ADS_REQUIRE(!vu || KB == 1,
+              "time blocking is implemented for variant W (steps_per_block 0 or 1 for U)");
   if (c.block_rows > 0) {
     RB = c.block_rows;
   } else {
@@ -1871,7 +2128,21 @@ void AcPlan<T>::build_tiles(int rows, int width, int64_t pitch, TileList& L,
     std::vector<std::vector<int>> bs((size_t)nti * ntj), br((size_t)nti * ntj);
     for (size_t k = 0; k < hsrc[s].size(); k++) {
       const int3 q = hsrc[s][k];
-      bs[(size_t)((q.x - 1) / gh) * ntj + (q.y - 1) / width].push_back((int)k);
+      if (!vu) {
+        bs[(size_t)((q.x - 1) / gh) * ntj + (q.y - 1) / width].push_back((int)k);
+        continue;
+      }
+      // variant U: the pre-pass and the adjoint read u less its source value
+      // one cell beyond the item, so every item whose rows i0-1 .. i_end and
+      // columns j0-1 .. j0+width hold the source lists it
+      for (int ti = std::max(0, (q.x - 2) / gh); ti <= std::min(nti - 1, q.x / gh); ti++)
+        for (int tj = std::max(0, (q.y - 2) / width); tj <= std::min(ntj - 1, q.y / width);
+             tj++) {
+          const int i0 = 1 + ti * gh, i_end = std::min(i0 + gh, nx + 1);
+          const int j0 = 1 + tj * width;
+          if (q.x >= i0 - 1 && q.x <= i_end && q.y >= j0 - 1 && q.y <= j0 + width)
+            bs[(size_t)ti * ntj + tj].push_back((int)k);
+        }
     }
     for (size_t k = 0; k < hrcv[s].size(); k++) {
       const int3 q = hrcv[s][k];
@@ -1948,6 +2219,7 @@ int AcPlan<T>::upload_tiles(const TileList& L, DevTiles& D, cudaStream_t st) {
     ADS_CUDA(cudaMemcpyAsync(D.rcvs, L.rcvs.data(), sizeof(CellRef) * L.rcvs.size(),
                              cudaMemcpyHostToDevice, st));
   D.pm_off = (int)L.in.size();
+  D.vu = vu ? 1 : 0;
   D.in_end = L.in_end;
   D.pm_end = L.pm_end;
   return ADS_OK;
@@ -1967,21 +2239,32 @@ int AcPlan<T>::launch_fwd(cudaStream_t st, int mode, int na, int t, int base, in
     ADS_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
     sp = side;
   }
-#define ADS_FWD(M, IN, items_, n_, s_, rows_)                                            \
-  k_ac_fwd<T, M, IN><<<n_, TPB, 0, s_>>>(items_, d_shots, tf.srcs, tf.rcvs, kc, t, base, ck, \
-                                         rows_)
-#define ADS_FWD_MODE(IN, items_, n_, s_, rows_) \
-  do {                                          \
-    if (mode == 1) ADS_FWD(1, IN, items_, n_, s_, rows_);      \
-    else if (mode == 2) ADS_FWD(2, IN, items_, n_, s_, rows_); \
-    else ADS_FWD(0, IN, items_, n_, s_, rows_);                \
+#define ADS_FWD(M, IN, VUF, items_, n_, s_, rows_)                                       \
+  k_ac_fwd<T, M, IN, VUF><<<n_, TPB, 0, s_>>>(items_, d_shots, tf.srcs, tf.rcvs, kc, t, base, \
+                                              ck, rows_)
+#define ADS_FWD_MODE(IN, VUF, items_, n_, s_, rows_)                 \
+  do {                                                               \
+    if (mode == 1) ADS_FWD(1, IN, VUF, items_, n_, s_, rows_);      \
+    else if (mode == 2) ADS_FWD(2, IN, VUF, items_, n_, s_, rows_); \
+    else ADS_FWD(0, IN, VUF, items_, n_, s_, rows_);                \
   } while (0)
   if (ni > 0) {
-    ADS_FWD_MODE(true, tf.items, ni, st, ri_f);
+    ADS_FWD_MODE(true, false, tf.items, ni, st, ri_f);
     ADS_LAUNCHED(1);
   }
   if (np > 0) {
-    ADS_FWD_MODE(false, pm, np, sp, ri_pf > 0 ? ri_pf : ri_f);
+    const int rows = ri_pf > 0 ? ri_pf : ri_f;
+    if (vu) {
+      // phi_{t-1}, psi_{t-1} from u_{t-1}, then the step reads them
+      if (mode == 0)
+        k_ac_phi_u<T, 0><<<np, TPB, 0, sp>>>(pm, d_shots, tf.srcs, kc, t, base, rows);
+      else
+        k_ac_phi_u<T, 1><<<np, TPB, 0, sp>>>(pm, d_shots, tf.srcs, kc, t, base, rows);
+      ADS_LAUNCHED(1);
+      ADS_FWD_MODE(false, true, pm, np, sp, rows);
+    } else {
+      ADS_FWD_MODE(false, false, pm, np, sp, rows);
+    }
     ADS_LAUNCHED(1);
   }
 #undef ADS_FWD_MODE
@@ -2010,8 +2293,17 @@ int AcPlan<T>::launch_adj(cudaStream_t st, int na, int k, int base) {
     ADS_LAUNCHED(1);
   }
   if (np > 0) {
-    k_ac_adj<T, false><<<np, TPB, 0, sp>>>(ta.items + ta.pm_off, d_shots, ta.srcs, ta.rcvs, kc,
-                                           k, base, ri_pa > 0 ? ri_pa : ri, dt2d);
+    const int rows = ri_pa > 0 ? ri_pa : ri;
+    if (vu) {
+      // lambdaPhi_{k-1}, lambdaPsi_{k-1} first, then the step's transpose
+      k_ac_adjphi_u<T><<<np, TPB, 0, sp>>>(ta.items + ta.pm_off, d_shots, kc, k, rows);
+      ADS_LAUNCHED(1);
+      k_ac_adj<T, false, true><<<np, TPB, 0, sp>>>(ta.items + ta.pm_off, d_shots, ta.srcs,
+                                                   ta.rcvs, kc, k, base, rows, dt2d);
+    } else {
+      k_ac_adj<T, false><<<np, TPB, 0, sp>>>(ta.items + ta.pm_off, d_shots, ta.srcs, ta.rcvs,
+                                             kc, k, base, rows, dt2d);
+    }
     ADS_LAUNCHED(1);
   }
   if (fork) {
@@ -2242,7 +2534,10 @@ int AcPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     const int base = res ? res_base : a - 2;
     if (!res) {
       if (!count) {
-        k_ac_restore<T><<<dim3(kRowBlocks, na), 256, 0, st>>>(d_shots, s, a, KB > 1 ? 0 : -1);
+        // phi / psi set the recompute's first step reads: variant W's step a
+        // reads set (a-1) & 1; variant U's pre-pass of step a reads set a & 1
+        k_ac_restore<T><<<dim3(kRowBlocks, na), 256, 0, st>>>(d_shots, s, a,
+                                                             KB > 1 ? 0 : (vu ? (a & 1) : -1));
         ADS_LAUNCHED(1);
       }
       n++;

@@ -18,8 +18,9 @@
 #include <algorithm>
 #include <cmath>
 #include <memory>
-#include <numeric>
 #include <mutex>
+#include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "ads_internal.h"
@@ -1422,13 +1423,15 @@ __global__ void k_el_gather_grads(const ElShot<T>* __restrict__ shots, int nshot
 }
 
 // Single-step operator sources: 1-based device indices, CPU AddSource order.
+template <typename T>
 struct Fields5 {
-  double* p[5];
+  T* p[5];
 };
 
-__global__ void k_el_step_src(Fields5 f5, const int64_t* __restrict__ si,
+template <typename T>
+__global__ void k_el_step_src(Fields5<T> f5, const int64_t* __restrict__ si,
                               const int64_t* __restrict__ sj, const int64_t* __restrict__ st,
-                              const double* __restrict__ sv, int64_t nsrc, int NX, int NY) {
+                              const T* __restrict__ sv, int64_t nsrc, int NX, int NY) {
   if (threadIdx.x != 0) return;
   for (int64_t k = 0; k < nsrc; k++) {
     const int64_t t = st[k], a = si[k] - 1, b = sj[k] - 1;
@@ -2464,6 +2467,151 @@ int ElPlan<T>::profile(const double* l, const double* m, const double* r, double
   return ADS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Single-step operators (one_step of src/Core.jl:215-228 and its transpose) in
+// the caller's precision: T = double for the f64 entry points, float for f32.
+// ---------------------------------------------------------------------------
+
+// Profile rows ax, bx, ay, by (2*NX / 2*NY, row 0 integer grid, row 1 half
+// grid) copied into the packed layout the kernels index.
+template <typename T>
+int el_copy_profiles(T* prof, const T* ax, const T* bx, const T* ay, const T* by, int64_t NX,
+                     int64_t NY, cudaStream_t st) {
+  ADS_CUDA(cudaMemcpyAsync(prof, ax, sizeof(T) * 2 * NX, cudaMemcpyDeviceToDevice, st));
+  ADS_CUDA(cudaMemcpyAsync(prof + 2 * NX, bx, sizeof(T) * 2 * NX, cudaMemcpyDeviceToDevice, st));
+  ADS_CUDA(cudaMemcpyAsync(prof + 4 * NX, ay, sizeof(T) * 2 * NY, cudaMemcpyDeviceToDevice, st));
+  ADS_CUDA(cudaMemcpyAsync(prof + 4 * NX + 2 * NY, by, sizeof(T) * 2 * NY,
+                           cudaMemcpyDeviceToDevice, st));
+  return ADS_OK;
+}
+
+template <typename T>
+int el_step_fwd(const T* state_in, T* state_out, const T* lambda, const T* mu, const T* rho,
+                const T* ax, const T* bx, const T* ay, const T* by, double dt, double dx,
+                double dy, int64_t NX, int64_t NY, const int64_t* srci, const int64_t* srcj,
+                const int64_t* srctype, const T* srcv, int64_t nsrc, ads_stream_t stream) {
+  if (int e = require_device()) return e;
+  ADS_REQUIRE(NX >= 4 && NY >= 4 && NX < (1 << 24) && NY < (1 << 24), "NX, NY out of range");
+  ADS_REQUIRE(state_in && state_out && lambda && mu && rho && ax && bx && ay && by,
+              "null pointer argument");
+  ADS_REQUIRE(state_in != state_out, "state_out must not alias state_in");
+  ADS_REQUIRE(nsrc >= 0 && (nsrc == 0 || (srci && srcj && srctype && srcv)),
+              "invalid source arrays");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t N = (NX + 2) * (NY + 2);
+  // profiles, repacked on the device-side scratch
+  T* prof = nullptr;
+  const size_t prof_n = 4 * NX + 4 * NY;
+  ADS_CUDA(cudaMallocAsync((void**)&prof, sizeof(T) * prof_n, st));
+  if (int e = el_copy_profiles<T>(prof, ax, bx, ay, by, NX, NY, st)) {
+    cudaFreeAsync(prof, st);
+    return e;
+  }
+  ElModel<T> M = make_model<T>((int)NX, (int)NY, NY + 2, 0, dt, dx, dy, lambda, mu, rho, prof);
+  ElShot<T> one{};
+  for (int f = 0; f < NF; f++) {
+    one.fin[f] = state_in + f * N;
+    one.f[f] = state_out + f * N;
+  }
+  one.fs = N;
+  dim3 grd((unsigned)div_up(NY + 2, BX), (unsigned)div_up(NX + 2, BY), 1);
+  k_el_stress<T, false><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
+  ADS_LAUNCHED(1);
+  k_el_velocity<T, false><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
+  ADS_LAUNCHED(1);
+  if (nsrc > 0) {
+    Fields5<T> f5{{state_out, state_out + N, state_out + 2 * N, state_out + 3 * N,
+                   state_out + 4 * N}};
+    k_el_step_src<T><<<1, 32, 0, st>>>(f5, srci, srcj, srctype, srcv, nsrc, (int)NX, (int)NY);
+    ADS_LAUNCHED(1);
+  }
+  ADS_CUDA(cudaFreeAsync(prof, st));
+  return ADS_OK;
+}
+
+// out[e] += (G) acc[e]: the f32 transpose accumulates its parameter gradients in
+// FP64 scratch (as the kernels do) and adds them to the caller's FP32 arrays.
+template <typename G>
+__global__ void k_el_add_grad(G* __restrict__ out, const double* __restrict__ acc, int64_t n) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    out[e] += (G)acc[e];
+}
+
+template <typename T, typename G>
+int el_step_bwd(const T* state_in, const T* grad_out, T* grad_in, G* grad_lambda, G* grad_mu,
+                G* grad_rho, const T* lambda, const T* mu, const T* rho, const T* ax,
+                const T* bx, const T* ay, const T* by, double dt, double dx, double dy,
+                int64_t NX, int64_t NY, ads_stream_t stream) {
+  constexpr bool kDirect = std::is_same<G, double>::value;  // accumulate into the caller's
+  if (int e = require_device()) return e;
+  ADS_REQUIRE(NX >= 4 && NY >= 4 && NX < (1 << 24) && NY < (1 << 24), "NX, NY out of range");
+  ADS_REQUIRE(state_in && grad_out && grad_in && grad_lambda && grad_mu && grad_rho &&
+                  lambda && mu && rho && ax && bx && ay && by,
+              "null pointer argument");
+  ADS_REQUIRE(grad_in != grad_out, "grad_in must not alias grad_out");
+  cudaStream_t st = (cudaStream_t)stream;
+  const int64_t N = (NX + 2) * (NY + 2);
+  const size_t prof_n = 4 * NX + 4 * NY;
+  // scratch: profiles, forward output state, per-step store, adjoint temps
+  // (and, for FP32 outputs, three FP64 accumulators)
+  const size_t n_scr = prof_n + (size_t)(NF + NSTORE + NTMP) * N;
+  const size_t n_acc = kDirect ? 0 : (size_t)3 * N;
+  char* scratch = nullptr;
+  const size_t b_scr = sizeof(T) * ((n_scr + 1) & ~size_t(1));
+  ADS_CUDA(cudaMallocAsync((void**)&scratch, b_scr + sizeof(double) * n_acc, st));
+  ADS_CUDA(cudaMemsetAsync(scratch, 0, b_scr + sizeof(double) * n_acc, st));
+  T* prof = (T*)scratch;
+  if (int e = el_copy_profiles<T>(prof, ax, bx, ay, by, NX, NY, st)) {
+    cudaFreeAsync(scratch, st);
+    return e;
+  }
+  T* fout = prof + prof_n;
+  T* store = fout + NF * N;
+  T* tmp = store + NSTORE * N;
+  double* acc = (double*)(scratch + b_scr);
+  ElModel<T> M = make_model<T>((int)NX, (int)NY, NY + 2, 0, dt, dx, dy, lambda, mu, rho, prof);
+  ElShot<T> one{};
+  for (int f = 0; f < NF; f++) {
+    one.fin[f] = state_in + f * N;
+    one.f[f] = fout + f * N;
+    one.g[f] = grad_in + f * N;
+  }
+  for (int k = 0; k < NTMP; k++) one.tmp[k] = tmp + k * N;
+  one.store = store;
+  one.fs = N;
+  if constexpr (kDirect) {
+    one.glam = grad_lambda;
+    one.gmu = grad_mu;
+    one.grho = grad_rho;
+  } else {
+    one.glam = acc;
+    one.gmu = acc + N;
+    one.grho = acc + 2 * N;
+  }
+  dim3 grd((unsigned)div_up(NY + 2, BX), (unsigned)div_up(NX + 2, BY), 1);
+  k_el_stress<T, true><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
+  ADS_LAUNCHED(1);
+  k_el_velocity<T, true><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
+  ADS_LAUNCHED(1);
+  ADS_CUDA(cudaMemcpyAsync(grad_in, grad_out, sizeof(T) * NF * N, cudaMemcpyDeviceToDevice, st));
+  k_el_adj1<T><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
+  ADS_LAUNCHED(1);
+  k_el_adj2<T><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
+  ADS_LAUNCHED(1);
+  k_el_adj3<T><<<grd, dim3(BX, BY), 0, st>>>(M, one);
+  ADS_LAUNCHED(1);
+  if constexpr (!kDirect) {
+    const unsigned nb = (unsigned)std::min<int64_t>(div_up(N, 256), 4096);
+    k_el_add_grad<G><<<nb, 256, 0, st>>>(grad_lambda, acc, N);
+    k_el_add_grad<G><<<nb, 256, 0, st>>>(grad_mu, acc + N, N);
+    k_el_add_grad<G><<<nb, 256, 0, st>>>(grad_rho, acc + 2 * N, N);
+    ADS_LAUNCHED(3);
+  }
+  ADS_CUDA(cudaFreeAsync(scratch, st));
+  return ADS_OK;
+}
+
 }  // namespace
 }  // namespace ads
 
@@ -2484,49 +2632,21 @@ int ads_elastic_step_fwd_f64(const double* state_in, double* state_out, const do
                              int64_t nsrc, ads_stream_t stream) {
   (void)kx;
   (void)ky;
-  if (int e = require_device()) return e;
-  ADS_REQUIRE(NX >= 4 && NY >= 4 && NX < (1 << 24) && NY < (1 << 24), "NX, NY out of range");
-  ADS_REQUIRE(state_in && state_out && lambda && mu && rho && ax && bx && ay && by,
-              "null pointer argument");
-  ADS_REQUIRE(state_in != state_out, "state_out must not alias state_in");
-  ADS_REQUIRE(nsrc >= 0 && (nsrc == 0 || (srci && srcj && srctype && srcv)),
-              "invalid source arrays");
-  cudaStream_t st = (cudaStream_t)stream;
-  const int64_t N = (NX + 2) * (NY + 2);
-  // profiles, repacked on the device-side scratch
-  double* scratch = nullptr;
-  const size_t prof_n = 4 * NX + 4 * NY;
-  ADS_CUDA(cudaMallocAsync((void**)&scratch, sizeof(double) * prof_n, st));
-  // rows are already in the right order on the device: copy them into place
-  double* prof = scratch;
-  ADS_CUDA(cudaMemcpyAsync(prof, ax, sizeof(double) * 2 * NX, cudaMemcpyDeviceToDevice, st));
-  ADS_CUDA(cudaMemcpyAsync(prof + 2 * NX, bx, sizeof(double) * 2 * NX, cudaMemcpyDeviceToDevice,
-                           st));
-  ADS_CUDA(cudaMemcpyAsync(prof + 4 * NX, ay, sizeof(double) * 2 * NY, cudaMemcpyDeviceToDevice,
-                           st));
-  ADS_CUDA(cudaMemcpyAsync(prof + 4 * NX + 2 * NY, by, sizeof(double) * 2 * NY,
-                           cudaMemcpyDeviceToDevice, st));
-  ElModel<double> M =
-      make_model<double>((int)NX, (int)NY, NY + 2, 0, dt, dx, dy, lambda, mu, rho, prof);
-  ElShot<double> one{};
-  for (int f = 0; f < NF; f++) {
-    one.fin[f] = state_in + f * N;
-    one.f[f] = state_out + f * N;
-  }
-  one.fs = N;
-  dim3 grd((unsigned)div_up(NY + 2, BX), (unsigned)div_up(NX + 2, BY), 1);
-  k_el_stress<double, false><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
-  ADS_LAUNCHED(1);
-  k_el_velocity<double, false><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
-  ADS_LAUNCHED(1);
-  if (nsrc > 0) {
-    Fields5 f5{{state_out, state_out + N, state_out + 2 * N, state_out + 3 * N,
-                state_out + 4 * N}};
-    k_el_step_src<<<1, 32, 0, st>>>(f5, srci, srcj, srctype, srcv, nsrc, (int)NX, (int)NY);
-    ADS_LAUNCHED(1);
-  }
-  ADS_CUDA(cudaFreeAsync(scratch, st));
-  return ADS_OK;
+  return el_step_fwd<double>(state_in, state_out, lambda, mu, rho, ax, bx, ay, by, dt, dx, dy,
+                             NX, NY, srci, srcj, srctype, srcv, nsrc, stream);
+}
+
+int ads_elastic_step_fwd_f32(const float* state_in, float* state_out, const float* lambda,
+                             const float* mu, const float* rho, const float* ax,
+                             const float* bx, const float* kx, const float* ay,
+                             const float* by, const float* ky, double dt, double dx,
+                             double dy, int64_t NX, int64_t NY, const int64_t* srci,
+                             const int64_t* srcj, const int64_t* srctype, const float* srcv,
+                             int64_t nsrc, ads_stream_t stream) {
+  (void)kx;
+  (void)ky;
+  return el_step_fwd<float>(state_in, state_out, lambda, mu, rho, ax, bx, ay, by, dt, dx, dy,
+                            NX, NY, srci, srcj, srctype, srcv, nsrc, stream);
 }
 
 int ads_elastic_step_bwd_f64(const double* state_in, const double* grad_out, double* grad_in,
@@ -2535,60 +2655,20 @@ int ads_elastic_step_bwd_f64(const double* state_in, const double* grad_out, dou
                              const double* ax, const double* bx, const double* ay,
                              const double* by, double dt, double dx, double dy, int64_t NX,
                              int64_t NY, ads_stream_t stream) {
-  if (int e = require_device()) return e;
-  ADS_REQUIRE(NX >= 4 && NY >= 4 && NX < (1 << 24) && NY < (1 << 24), "NX, NY out of range");
-  ADS_REQUIRE(state_in && grad_out && grad_in && grad_lambda && grad_mu && grad_rho &&
-                  lambda && mu && rho && ax && bx && ay && by,
-              "null pointer argument");
-  ADS_REQUIRE(grad_in != grad_out, "grad_in must not alias grad_out");
-  cudaStream_t st = (cudaStream_t)stream;
-  const int64_t N = (NX + 2) * (NY + 2);
-  const size_t prof_n = 4 * NX + 4 * NY;
-  // scratch: profiles, forward output state, per-step store, adjoint temps
-  const size_t n_scr = prof_n + (size_t)(NF + NSTORE + NTMP) * N;
-  double* scratch = nullptr;
-  ADS_CUDA(cudaMallocAsync((void**)&scratch, sizeof(double) * n_scr, st));
-  ADS_CUDA(cudaMemsetAsync(scratch, 0, sizeof(double) * n_scr, st));
-  double* prof = scratch;
-  ADS_CUDA(cudaMemcpyAsync(prof, ax, sizeof(double) * 2 * NX, cudaMemcpyDeviceToDevice, st));
-  ADS_CUDA(cudaMemcpyAsync(prof + 2 * NX, bx, sizeof(double) * 2 * NX, cudaMemcpyDeviceToDevice,
-                           st));
-  ADS_CUDA(cudaMemcpyAsync(prof + 4 * NX, ay, sizeof(double) * 2 * NY, cudaMemcpyDeviceToDevice,
-                           st));
-  ADS_CUDA(cudaMemcpyAsync(prof + 4 * NX + 2 * NY, by, sizeof(double) * 2 * NY,
-                           cudaMemcpyDeviceToDevice, st));
-  double* fout = scratch + prof_n;
-  double* store = fout + NF * N;
-  double* tmp = store + NSTORE * N;
-  ElModel<double> M =
-      make_model<double>((int)NX, (int)NY, NY + 2, 0, dt, dx, dy, lambda, mu, rho, prof);
-  ElShot<double> one{};
-  for (int f = 0; f < NF; f++) {
-    one.fin[f] = state_in + f * N;
-    one.f[f] = fout + f * N;
-    one.g[f] = grad_in + f * N;
-  }
-  for (int k = 0; k < NTMP; k++) one.tmp[k] = tmp + k * N;
-  one.store = store;
-  one.fs = N;
-  one.glam = grad_lambda;
-  one.gmu = grad_mu;
-  one.grho = grad_rho;
-  dim3 grd((unsigned)div_up(NY + 2, BX), (unsigned)div_up(NX + 2, BY), 1);
-  k_el_stress<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
-  ADS_LAUNCHED(1);
-  k_el_velocity<double, true><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
-  ADS_LAUNCHED(1);
-  ADS_CUDA(cudaMemcpyAsync(grad_in, grad_out, sizeof(double) * NF * N,
-                           cudaMemcpyDeviceToDevice, st));
-  k_el_adj1<double><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
-  ADS_LAUNCHED(1);
-  k_el_adj2<double><<<grd, dim3(BX, BY), 0, st>>>(M, one, 0);
-  ADS_LAUNCHED(1);
-  k_el_adj3<double><<<grd, dim3(BX, BY), 0, st>>>(M, one);
-  ADS_LAUNCHED(1);
-  ADS_CUDA(cudaFreeAsync(scratch, st));
-  return ADS_OK;
+  return el_step_bwd<double, double>(state_in, grad_out, grad_in, grad_lambda, grad_mu,
+                                     grad_rho, lambda, mu, rho, ax, bx, ay, by, dt, dx, dy, NX,
+                                     NY, stream);
+}
+
+int ads_elastic_step_bwd_f32(const float* state_in, const float* grad_out, float* grad_in,
+                             float* grad_lambda, float* grad_mu, float* grad_rho,
+                             const float* lambda, const float* mu, const float* rho,
+                             const float* ax, const float* bx, const float* ay,
+                             const float* by, double dt, double dx, double dy, int64_t NX,
+                             int64_t NY, ads_stream_t stream) {
+  return el_step_bwd<float, float>(state_in, grad_out, grad_in, grad_lambda, grad_mu, grad_rho,
+                                   lambda, mu, rho, ax, bx, ay, by, dt, dx, dy, NX, NY,
+                                   stream);
 }
 
 }  // extern "C"
@@ -2597,14 +2677,16 @@ int ads_elastic_step_bwd_f64(const double* state_in, const double* grad_out, dou
 // Allocation-free variant of the elastic step transpose.
 //
 // Some callers cannot allocate device memory at the time they run this step:
-// code executing inside another framework's stream capture or custom-call
-// hook, where cudaMalloc/cudaMallocAsync would break the capture or the
-// framework's memory accounting, and callers that must not touch the CUDA
-// allocator at all (pre-planned real-time loops).  For them the scratch this
-// step needs (forward output state, per-step strains, adjoint temporaries and
-// the packed CPML rows) lives in one fixed array in device global memory,
-// compiled into the library.  Every GPU that loads the library holds the array
-// (34 x 65536 doubles, about 17.8 MB) until the process exits.
+// an operator called from another framework's custom-call or kernel hook,
+// where that framework owns all device memory and an extension that calls
+// cudaMalloc bypasses its memory accounting (and can fail once the framework
+// has reserved the device), and time-critical loops that must never enter the
+// CUDA allocator, whose calls can synchronise the device and take unbounded
+// time.  For them the scratch this step needs (forward output state, per-step
+// strains, adjoint temporaries and the packed CPML rows) lives in one fixed
+// array in device global memory, compiled into the library.  Every GPU that
+// loads the library holds the array (34 x 65536 doubles, about 17.8 MB) until
+// the process exits.
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -2617,6 +2699,9 @@ double* g_noalloc_ptr[128] = {};  // device address of g_el_bwd_scratch, per dev
 
 // Device address of the scratch array for the current device, looked up once
 // per device (the host-side symbol is only a stand-in, never a device address).
+// The cached address belongs to the device's primary context: it assumes that
+// context lives for the whole process, so a caller that resets the device
+// (cudaDeviceReset) must not call the allocation-free entry point afterwards.
 int noalloc_scratch(double** out) {
   int dev = 0;
   ADS_CUDA(cudaGetDevice(&dev));

@@ -78,50 +78,54 @@ def compute_PML_Params(param: ElasticPropagatorParams):
 
 def elastic_one_step(param: ElasticPropagatorParams, rho, lam, mu, state, profiles,
                      srci=None, srcj=None, srcv=None, srctype=None):
-    """one_step of src/Core.jl:215-228 on CUDA float64 tensors.  state: (13, N)
-    (vx, vy, sxx, syy, sxy, mem[1..8]); profiles: (ax, bx, kx, ay, by, ky) tensors;
+    """one_step of src/Core.jl:215-228 on CUDA tensors, float64 (the reference's
+    precision) or float32 (the dtype of `state` decides).  state: (13, N)
+    (vx, vy, sxx, syy, sxy, mem[1..8]); profiles: (ax, bx, kx, ay, by, ky);
     srcv: this step's (nsrc,) values.  Returns the new (13, N) state."""
     NX, NY = param.NX, param.NY
     ts = [rho, lam, mu, state]
     _require_cuda(*ts)
-    state = state.contiguous().to(torch.float64)
+    dt_ = torch.float32 if state.dtype == torch.float32 else torch.float64
+    state = state.contiguous().to(dt_)
     out = torch.empty_like(state)
-    ax, bx, kx, ay, by, ky = [torch.as_tensor(p, dtype=torch.float64, device=state.device)
-                              .contiguous() for p in profiles]
+    ax, bx, kx, ay, by, ky = [torch.as_tensor(p, device=state.device).to(dt_).contiguous()
+                              for p in profiles]
     if srci is not None and len(srci):
         dev = state.device
         si = torch.as_tensor(np.asarray(srci), dtype=torch.int64, device=dev)
         sj = torch.as_tensor(np.asarray(srcj), dtype=torch.int64, device=dev)
         stp = torch.as_tensor(np.asarray(srctype), dtype=torch.int64, device=dev)
-        sv = torch.as_tensor(srcv, dtype=torch.float64, device=dev).contiguous()
+        sv = torch.as_tensor(srcv, device=dev).to(dt_).contiguous()
         nsrc = len(srci)
     else:
         si = sj = stp = sv = None
         nsrc = 0
-    lam, mu, rho = (t.contiguous().to(torch.float64) for t in (lam, mu, rho))
-    call("ads_elastic_step_fwd_f64", _ptr(state), _ptr(out), _ptr(lam), _ptr(mu), _ptr(rho),
-         _ptr(ax), _ptr(bx), _ptr(kx), _ptr(ay), _ptr(by), _ptr(ky), param.DELTAT,
-         param.DELTAX, param.DELTAY, NX, NY, _ptr(si), _ptr(sj), _ptr(stp), _ptr(sv), nsrc,
-         _stream())
+    lam, mu, rho = (t.contiguous().to(dt_) for t in (lam, mu, rho))
+    name = "ads_elastic_step_fwd_f64" if dt_ == torch.float64 else "ads_elastic_step_fwd_f32"
+    call(name, _ptr(state), _ptr(out), _ptr(lam), _ptr(mu), _ptr(rho), _ptr(ax), _ptr(bx),
+         _ptr(kx), _ptr(ay), _ptr(by), _ptr(ky), param.DELTAT, param.DELTAX, param.DELTAY, NX,
+         NY, _ptr(si), _ptr(sj), _ptr(stp), _ptr(sv), nsrc, _stream())
     return out
 
 
 def elastic_one_step_grad(param: ElasticPropagatorParams, rho, lam, mu, state, grad_out,
                           profiles):
-    """Transpose of elastic_one_step about `state`: returns (grad_state, grad_lambda,
-    grad_mu, grad_rho)."""
+    """Transpose of elastic_one_step about `state` (float64 or float32, as
+    `state`): returns (grad_state, grad_lambda, grad_mu, grad_rho)."""
     dev = state.device
-    state = state.contiguous().to(torch.float64)
-    gout = grad_out.contiguous().to(torch.float64)
+    dt_ = torch.float32 if state.dtype == torch.float32 else torch.float64
+    state = state.contiguous().to(dt_)
+    gout = grad_out.contiguous().to(dt_)
     gin = torch.empty_like(state)
     N = state.shape[-1]
-    gl, gm, gr = (torch.zeros(N, dtype=torch.float64, device=dev) for _ in range(3))
-    ax, bx, kx, ay, by, ky = [torch.as_tensor(p, dtype=torch.float64, device=dev).contiguous()
+    gl, gm, gr = (torch.zeros(N, dtype=dt_, device=dev) for _ in range(3))
+    ax, bx, kx, ay, by, ky = [torch.as_tensor(p, device=dev).to(dt_).contiguous()
                               for p in profiles]
-    lam, mu, rho = (t.contiguous().to(torch.float64) for t in (lam, mu, rho))
-    call("ads_elastic_step_bwd_f64", _ptr(state), _ptr(gout), _ptr(gin), _ptr(gl), _ptr(gm),
-         _ptr(gr), _ptr(lam), _ptr(mu), _ptr(rho), _ptr(ax), _ptr(bx), _ptr(ay), _ptr(by),
-         param.DELTAT, param.DELTAX, param.DELTAY, param.NX, param.NY, _stream())
+    lam, mu, rho = (t.contiguous().to(dt_) for t in (lam, mu, rho))
+    name = "ads_elastic_step_bwd_f64" if dt_ == torch.float64 else "ads_elastic_step_bwd_f32"
+    call(name, _ptr(state), _ptr(gout), _ptr(gin), _ptr(gl), _ptr(gm), _ptr(gr), _ptr(lam),
+         _ptr(mu), _ptr(rho), _ptr(ax), _ptr(bx), _ptr(ay), _ptr(by), param.DELTAT,
+         param.DELTAX, param.DELTAY, param.NX, param.NY, _stream())
     return gin, gl, gm, gr
 
 
@@ -386,17 +390,32 @@ def compute_forward_GPU(param: ElasticPropagatorParams, srcs, rcvs, model, preci
 
 
 def compute_loss_and_grads_GPU(param: ElasticPropagatorParams, srcs, rcvs, Rs, model,
-                               precision="f64", ckpt_every=0):
+                               precision="f64", ckpt_every=0, aux_loss=None, as_lists=False):
     """src/Utils.jl:300-332 with elastic sources, one GPU: loss = sum over
     shots of sum((rcvv - Rs)^2) and its gradients with respect to lambda, mu
     and rho, all shots in one batched plan; model = (rho, lambda, mu), Rs per
     shot (nrcv, NSTEP+1).  Returns (loss, grad_lambda, grad_mu, grad_rho), the
     gradients shaped like lambda; compute_properties_grad turns them into
-    vp / vs / rho gradients."""
+    vp / vs / rho gradients.  aux_loss: an extra term added to the loss (a
+    float, or a callable model -> (value, (d/d lambda, d/d mu, d/d rho))), as
+    the reference's aux_loss (src/Utils.jl:309-311).  as_lists: the loss and
+    the gradient tuple as the one-GPU lists the reference returns."""
     plan = _batched_plan(param, srcs, rcvs, precision, ckpt_every)
     obs = plan.pack([torch.as_tensor(r, device="cuda") for r in Rs])
     loss, *grads = plan.gradient(*_materials(model), obs)
-    torch.cuda.current_stream().synchronize()
     plan.close()
     shape = tuple(np.shape(model[1]))
-    return (loss, *(g.view(shape) for g in grads))
+    grads = [g.view(shape) for g in grads]
+    if aux_loss is not None:
+        if callable(aux_loss):
+            v, ga = aux_loss(model)
+            loss = loss + v
+            grads = [g + torch.as_tensor(np.asarray(x), dtype=torch.float64,
+                                         device=g.device).view(shape)
+                     for g, x in zip(grads, ga)]
+        else:
+            loss = loss + float(aux_loss)
+    torch.cuda.current_stream().synchronize()
+    if as_lists:
+        return [loss], [tuple(grads)]
+    return (loss, *grads)

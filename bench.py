@@ -50,27 +50,15 @@ BYTES = {
 TRAFFIC_16SHOT = {"k_ac_fwd": 139.4e6, "k_ac_adj": 246.2e6}
 
 
-def workload(MX=1000, MY=500, npml=40, nstep=3000, nshots=64, nrcv=500, fpeak=15.0,
-             dt=0.8e-3, h=10.0, seed=1234):
+def workload(nstep=3000, nshots=64, seed=1234):
+    """The C3 workload (adseismic_gb300.configs.c3_batched)."""
     import __graft_entry__ as g
 
     ads = g.load_package()
-    rng = np.random.default_rng(seed)
-    vp_true = ads.folded_layer_model(MX + 2, MY + 2, 1500.0, 4500.0, seed=seed)
-    vp0 = ads.gaussian_smooth(vp_true, sigma=0.05 * MX)
-    a = ads.ricker_width_samples(fpeak, dt)
-    shift = 1.5 / fpeak / dt
-    p = ads.AcousticPropagatorParams(NX=MX, NY=MY, NSTEP=nstep, DELTAT=dt)
-    wav = ads.Ricker(p, a, shift, 1e6)
-    lo, hi = npml + 2, MX - npml
-    shots = []
-    for s in range(nshots):
-        si = int(round(lo + (s + 0.5) * (hi - lo) / nshots))
-        rcvi = np.round(np.linspace(npml + 2, MX - npml, nrcv)).astype(np.int64)
-        shots.append(dict(x0=0, nx=MX, nstep=nstep, srci=[si], srcj=[npml + 11],
-                          srcv=wav[:, None], rcvi=rcvi, rcvj=np.full(nrcv, npml + 6)))
-    cfg = dict(MX=MX, MY=MY, h=h, dt=dt, npml=npml, vp_ref=float(vp_true.mean()))
-    return ads, cfg, shots, vp_true, vp0, rng
+    from adseismic_gb300 import configs
+
+    cfg, shots, vp_true, vp0 = configs.c3_batched(nshots=nshots, nstep=nstep, seed=seed)
+    return ads, cfg, shots, vp_true, vp0, np.random.default_rng(seed)
 
 
 class ClockSampler:
@@ -246,13 +234,11 @@ def run_acoustic_fwd_f64(args):
     import oracle
 
     ads = g.load_package()
-    NX = NY = 240
-    npml, T, h, dt = 20, 1000, 10.0, 1e-3
-    vp = ads.layered_gaussian_model(NX + 2, NY + 2, 2000.0, 3500.0, seed=7)
-    p = ads.AcousticPropagatorParams(NX=NX, NY=NY, NSTEP=T, DELTAT=dt)
-    wav = ads.Ricker(p, ads.ricker_width_samples(10.0, dt), 1.5 / 10.0 / dt, 1e6)
-    shot = dict(x0=0, nx=NX, nstep=T, srci=[NX // 2 + 1], srcj=[npml + 21], srcv=wav[:, None],
-                rcvi=np.arange(npml + 2, npml + 202), rcvj=np.full(200, npml + 6))
+    from adseismic_gb300 import configs
+
+    cfg, shot, vp = configs.c1_forward()
+    NX, NY, npml, T, h, dt = cfg["MX"], cfg["MY"], cfg["npml"], cfg["nstep"], cfg["h"], cfg["dt"]
+    wav = shot["srcv"]
     plan = ads.AcousticPlan(NX, NY, h, h, dt, [shot], npml=npml, vp_ref=float(vp.mean()),
                             precision="f64")
     vdev = torch.tensor(vp, device="cuda")
@@ -270,7 +256,7 @@ def run_acoustic_fwd_f64(args):
     sx, ty = oracle.acoustic_pml(NX, NY, h, h, npml, float(vp.mean()))
     t0 = time.perf_counter()
     oracle.acoustic_forward(NX, NY, T, dt, h, h, sx, ty, vp.reshape(-1), shot["srci"],
-                            shot["srcj"], wav[:, None], shot["rcvi"], shot["rcvj"],
+                            shot["srcj"], wav, shot["rcvi"], shot["rcvj"],
                             use_ref=oracle.ref_available())
     t_cpu = time.perf_counter() - t0
     _line("acoustic forward Gcell-updates/s, plain FP64 drop-in", cells / (ms / 1e3) / 1e9,
@@ -294,17 +280,10 @@ def run_fwi_f64(args):
     import __graft_entry__ as g
 
     ads = g.load_package()
-    NX = NY = 400
-    npml, T, h, dt = 30, 2000, 10.0, 1e-3
-    vt = ads.layered_gaussian_model(NX + 2, NY + 2, 2000.0, 3500.0, seed=11)
-    v0 = ads.gaussian_smooth(vt, 20.0)
-    p = ads.AcousticPropagatorParams(NX=NX, NY=NY, NSTEP=T, DELTAT=dt)
-    wav = ads.Ricker(p, ads.ricker_width_samples(10.0, dt), 1.5 / 10.0 / dt, 1e6)
-    seg = (NX - 2 * npml) / 8
-    shots = [dict(x0=0, nx=NX, nstep=T, srci=[int(npml + 1 + (k + 0.5) * seg) + 1],
-                  srcj=[npml + 21], srcv=wav[:, None],
-                  rcvi=np.arange(npml + 2, NX - npml + 2), rcvj=np.full(NX - 2 * npml, npml + 6))
-             for k in range(8)]
+    from adseismic_gb300 import configs
+
+    cfg, shots, vt, v0 = configs.c2_fwi()
+    NX, NY, npml, T, h, dt = cfg["MX"], cfg["MY"], cfg["npml"], cfg["nstep"], cfg["h"], cfg["dt"]
     plan = ads.AcousticPlan(NX, NY, h, h, dt, shots, npml=npml, vp_ref=float(vt.mean()),
                             precision="f64")
     obs = plan.forward(torch.tensor(vt, device="cuda")).clone()
@@ -318,47 +297,31 @@ def run_fwi_f64(args):
     plan.close()
 
 
-def elastic_workload(ads, nshots=32, NX=600, NY=300, npml=30, T=4000, h=10.0, dt=0.8e-3,
-                     fpeak=10.0, seed=5):
-    rng = np.random.default_rng(seed)
-    j = np.arange(NY + 2, dtype=np.float64)
-    vp1 = 2500.0 + 2500.0 * np.floor(j / (NY + 2) * 5) / 4
-    vp = np.repeat(vp1[None, :], NX + 2, axis=0)
-    vs = vp / np.sqrt(3) * (1 + 0.05 * (2 * rng.random(vp.shape) - 1))
-    rho = 310.0 * vp ** 0.25
-    lam, mu, rho = ads.compute_properties(vp, vs, rho)
-    p = ads.ElasticPropagatorParams(NX=NX, NY=NY, NSTEP=T, DELTAX=h, DELTAY=h, DELTAT=dt,
-                                    NPOINTS_PML=npml, vp_ref=float(vp.mean()), f0=fpeak)
-    wav = ads.Ricker(p, ads.ricker_width_samples(fpeak, dt), 1.5 / fpeak / dt, 1e6)
-    xr = np.round(np.linspace(npml + 2, NX - npml, 300)).astype(np.int64)
-    shots = []
-    for s in range(nshots):
-        si = int(round(npml + 2 + (s + 0.5) * (NX - 2 * npml - 2) / nshots))
-        shots.append(dict(srci=[si, si], srcj=[npml + 11] * 2, srctype=[2, 3],
-                          srcv=np.repeat(wav[:, None], 2, axis=1),
-                          rcvi=np.concatenate([xr, xr]), rcvj=np.full(600, npml + 6),
-                          rcvtype=np.array([0] * 300 + [1] * 300)))
-    return p, shots, lam, mu, rho
+def elastic_workload(ads, nshots=32, T=4000):
+    from adseismic_gb300 import configs
+
+    return configs.c4_elastic(nshots=nshots, T=T)
 
 
-def run_elastic_fwi(args):
-    """Elastic CPML FWI gradient w.r.t. lambda, mu, rho: 600x300 incl. CPML 30,
-    4000 steps, FP32 stencils with FP64 accumulation, 32 explosive shots (sigma_xx
-    and sigma_yy, 10 Hz Ricker), 300 two-component receivers."""
+def elastic_measure(steps, warmup, nshots=32, T=4000, with_rel_err=True):
+    """Elastic CPML FWI gradient w.r.t. lambda, mu, rho (C4): 600x300 incl. CPML
+    30, T steps, FP32 stencils with FP64 accumulation, explosive shots (sigma_xx
+    and sigma_yy, 10 Hz Ricker), 300 two-component receivers.  Returns the
+    measured figures as a dict (value in shot-gradients/s)."""
     import torch
     import __graft_entry__ as g
 
     ads = g.load_package()
-    p, shots, lam, mu, rho = elastic_workload(ads, nshots=args.shots if args.shots != 64 else 32,
-                                              T=args.nstep if args.nstep != 3000 else 4000)
+    from adseismic_gb300 import configs
+
+    p, shots, lam, mu, rho = elastic_workload(ads, nshots=nshots, T=T)
     t = lambda a: torch.tensor(a.reshape(-1), device="cuda")
     # the last checkpoint segments' adjoint inputs stay resident in HBM (up to
     # 92% of the memory free after the plan's other buffers)
     plan = ads.ElasticPlan(p, shots, precision="f32", ckpt_every=100, resident_mem_pct=92)
     obs = plan.forward(t(lam), t(mu), t(rho)).clone()
-    sm = lambda a: t(ads.gaussian_smooth(a, 10.0))
-    l0, m0, r0 = sm(lam), sm(mu), sm(rho)
-    ms = _timed(lambda: plan.gradient(l0, m0, r0, obs), args.steps, args.warmup)
+    l0, m0, r0 = (t(a) for a in configs.c4_start_model(lam, mu, rho))
+    ms = _timed(lambda: plan.gradient(l0, m0, r0, obs), steps, warmup)
     n = len(shots)
     cells = 2 * n * p.NX * p.NY * p.NSTEP
     # roofline: algorithmic bytes per cell-update, forward (13 + 16 f_pml) x 4 B
@@ -376,24 +339,107 @@ def run_elastic_fwi(args):
         "k_el_step_rows": (fwd_ms, b_fwd * c1),
         "k_el_adj1_rows+k_el_adj2_rows+k_el_adj3_rows": (adj_ms, b_adj * c1),
     }
-    kern = {k: {"ms_per_step": round(t, 4), "achieved_gbs": round(b / (t / 1e3) / 1e9, 1),
-                "frac": round(b / (t / 1e3) / 1e9 / peak, 4)} for k, (t, b) in groups.items()}
+    kern = {k: {"ms_per_step": round(tt, 4), "achieved_gbs": round(b / (tt / 1e3) / 1e9, 1),
+                "frac": round(b / (tt / 1e3) / 1e9 / peak, 4)} for k, (tt, b) in groups.items()}
     kern.update({k: {"ms_per_launch": round(v[0], 4)} for k, v in prof.items()})
     dom = "k_el_adj1_rows+k_el_adj2_rows+k_el_adj3_rows"
-    t, b = groups[dom]
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(b / (t / 1e3) / 1e9, 1),
-                "peak": peak, "unit": "GB/s", "frac": round(b / (t / 1e3) / 1e9 / peak, 4),
+    tt, b = groups[dom]
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(b / (tt / 1e3) / 1e9, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(b / (tt / 1e3) / 1e9 / peak, 4),
                 "peak_source": peak_kind, "traffic": None, "bytes_per_launch": b,
                 "bytes_per_cell": {"forward": b_fwd, "adjoint": b_adj, "f_pml": round(f_pml, 4)},
                 "kernels": kern}
-    _line("elastic FWI shot-gradients/s (FP32 stencils, FP64 accumulation)", n / (ms / 1e3),
-          "shot-gradients/s", args, ms, "f32",
-          f"elastic CPML gradient {p.NX}x{p.NY} (CPML {p.NPOINTS_PML}), {p.NSTEP} steps, "
-          f"{n} explosive shots x 300 two-component receivers, checkpoints every 100, "
-          f"the last {plan.resident_segments} of {-(-p.NSTEP // 100)} segments resident in HBM",
-          {"gcell_updates_per_s": cells / (ms / 1e3) / 1e9, "roofline": roofline,
-           "device_bytes": plan.device_bytes, "gpu_launches": int(plan.launches_gradient)})
+    out = {"value": n / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": steps,
+           "warmup": warmup, "dtype": "f32",
+           "workload": f"elastic CPML gradient {p.NX}x{p.NY} (CPML {p.NPOINTS_PML}), "
+                       f"{p.NSTEP} steps, {n} explosive shots x 300 two-component receivers, "
+                       f"checkpoints every 100, the last {plan.resident_segments} of "
+                       f"{-(-p.NSTEP // 100)} segments resident in HBM",
+           "gcell_updates_per_s": cells / (ms / 1e3) / 1e9, "roofline": roofline,
+           "device_bytes": plan.device_bytes, "gpu_launches": int(plan.launches_gradient)}
     plan.close()
+    if with_rel_err:
+        out["rel_err"] = elastic_rel_err(ads, p, [shots[3], shots[n // 2 + 4]], lam, mu, rho,
+                                         (l0, m0, r0))
+    return out
+
+
+def elastic_rel_err(ads, p, pick, lam, mu, rho, start):
+    """FP32 plan against the FP64 plan (pinned to the oracle at 1e-12) on `pick`:
+    rel-L2 of each gradient field and of every receiver trace."""
+    import torch
+    from adseismic_gb300 import configs
+
+    t = lambda a: torch.tensor(a.reshape(-1), device="cuda")
+    p64 = ads.ElasticPlan(p, pick, precision="f64", ckpt_every=100)
+    obs = p64.forward(t(lam), t(mu), t(rho)).clone()
+    o64 = p64.gradient(*start, obs, want_traces=True)
+    torch.cuda.synchronize()
+    p64.close()
+    p32 = ads.ElasticPlan(p, pick, precision="f32", ckpt_every=100)
+    o32 = p32.gradient(*start, obs.float(), want_traces=True)
+    torch.cuda.synchronize()
+    p32.close()
+    rel = lambda a, b: float(torch.linalg.vector_norm(a.double() - b) / torch.linalg.vector_norm(b))
+    nt = p.NSTEP + 1
+    tr32, tr64 = o32[4].double().cpu().numpy(), o64[4].cpu().numpy()
+    per, n0 = [], 0
+    for s in pick:
+        n = len(s["rcvi"])
+        a = tr32[n0:n0 + n * nt].reshape(n, nt).T
+        b = tr64[n0:n0 + n * nt].reshape(n, nt).T
+        per.append(configs.per_trace_rel(a, b, n))
+        n0 += n * nt
+    per = np.concatenate(per)
+    return {"grad_lambda": rel(o32[1], o64[1]), "grad_mu": rel(o32[2], o64[2]),
+            "grad_rho": rel(o32[3], o64[3]), "traces": rel(o32[4], o64[4]),
+            "trace_max": float(per.max()), "trace_median": float(np.median(per)),
+            "traces_compared": int(per.size), "shots": len(pick),
+            "reference": "FP64 plan, pinned to the oracle at rel-L2 1e-12"}
+
+
+def acoustic_rel_err(ads, cfg, pick, vp_true, vp0):
+    """The FP32 plan (the benchmark's settings) against the FP64 plan (pinned to
+    the oracle at 1e-12) on the shots `pick`: rel-L2 of the gradient, of all
+    traces and of every receiver trace (traces with signal, see per_trace_rel)."""
+    import torch
+    from adseismic_gb300 import configs
+
+    vt = torch.tensor(vp_true, device="cuda")
+    v0 = torch.tensor(vp0, device="cuda")
+    p64 = configs.acoustic_plan(ads, cfg, pick, "f64", ckpt_every=100)
+    obs = p64.forward(vt).clone()
+    l64, g64, tr64 = p64.gradient(v0, obs, want_traces=True)
+    torch.cuda.synchronize()
+    p64.close()
+    p32 = configs.acoustic_plan(ads, cfg, pick, "f32", ckpt_every=100, autotune=True)
+    l32, g32, tr32 = p32.gradient(v0, obs.float(), want_traces=True)
+    torch.cuda.synchronize()
+    offs = p32.trace_offsets
+    p32.close()
+    rel = lambda a, b: float(torch.linalg.vector_norm(a.double() - b) / torch.linalg.vector_norm(b))
+    a, b = tr32.double().cpu().numpy(), tr64.cpu().numpy()
+    per = []
+    for k, s in enumerate(pick):
+        n = (s["nstep"] + 1) * len(s["rcvi"])
+        per.append(configs.per_trace_rel(a[offs[k]:offs[k] + n], b[offs[k]:offs[k] + n],
+                                         len(s["rcvi"])))
+    per = np.concatenate(per)
+    return {"grad": rel(g32, g64), "traces": rel(tr32, tr64), "trace_max": float(per.max()),
+            "trace_median": float(np.median(per)), "traces_compared": int(per.size),
+            "loss": abs(float(l32) - float(l64)) / float(l64), "shots": len(pick),
+            "reference": "FP64 plan, pinned to the oracle at rel-L2 1e-12"}
+
+
+def run_elastic_fwi(args):
+    """The elastic C4 gradient as its own bench line."""
+    nshots = args.shots if args.shots != 64 else 32
+    T = args.nstep if args.nstep != 3000 else 4000
+    r = elastic_measure(args.steps, args.warmup, nshots=nshots, T=T)
+    _line("elastic FWI shot-gradients/s (FP32 stencils, FP64 accumulation)", r["value"],
+          "shot-gradients/s", args, r["ms_per_step"], "f32", r["workload"],
+          {k: r[k] for k in ("gcell_updates_per_s", "roofline", "device_bytes", "gpu_launches",
+                             "rel_err")})
 
 
 def run_fwi_uneven(args):
@@ -404,27 +450,11 @@ def run_fwi_uneven(args):
     import __graft_entry__ as g
 
     ads = g.load_package()
-    MX, MY, npml, h, dt = 4000, 2000, 40, 10.0, 0.8e-3
-    rng = np.random.default_rng(2025)
-    vt = ads.folded_layer_model(MX + 2, MY + 2, 1500.0, 4500.0, seed=2025)
-    ii, jj = np.meshgrid(np.arange(MX + 2), np.arange(MY + 2), indexing="ij")
-    for _ in range(6):
-        ci, cj = rng.uniform(0, MX), rng.uniform(0.2 * MY, MY)
-        vt *= 1 + rng.uniform(-0.1, 0.1) * np.exp(-((ii - ci) ** 2 + (jj - cj) ** 2) / (2 * 60.0 ** 2))
-    v0 = ads.gaussian_smooth(vt, 40.0)
-    nshots = args.shots if args.shots != 64 else 128
-    shots = []
-    for s in range(nshots):
-        W = int(rng.integers(400, 1201))
-        x0 = int(rng.integers(0, MX - W + 1))
-        T = int(rng.integers(2000, 6001))
-        R = min(int(rng.integers(200, 1201)), W - 2 * npml)
-        p = ads.AcousticPropagatorParams(NX=W, NY=MY, NSTEP=T, DELTAT=dt)
-        wav = ads.Ricker(p, ads.ricker_width_samples(15.0, dt), 1.5 / 15.0 / dt, 1e6)
-        shots.append(dict(x0=x0, nx=W, nstep=T, srci=[int(rng.integers(npml + 2, W - npml))],
-                          srcj=[npml + 11], srcv=wav[:, None],
-                          rcvi=np.round(np.linspace(npml + 2, W - npml, R)).astype(np.int64),
-                          rcvj=np.full(R, npml + 6)))
+    from adseismic_gb300 import configs
+
+    cfg, shots, vt, v0 = configs.c5_uneven(nshots=args.shots if args.shots != 64 else 128)
+    MX, MY, npml, h, dt = cfg["MX"], cfg["MY"], cfg["npml"], cfg["h"], cfg["dt"]
+    nshots = len(shots)
     plan = ads.AcousticPlan(MX, MY, h, h, dt, shots, npml=npml, vp_ref=float(vt.mean()),
                             precision="f32", ckpt_every=100)
     obs = plan.forward(torch.tensor(vt, device="cuda")).clone()
@@ -453,6 +483,7 @@ def main():
     ap.add_argument("--nstep", type=int, default=3000)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-elastic", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -589,6 +620,12 @@ def main():
     resident = plan.resident_segments
     plan.close()  # its resident wavefields free the memory the FP64 paths need
 
+    # accuracy of the timed FP32 path: two of the shots against the FP64 plan
+    rel_err = None
+    if not args.no_fp64:
+        rel_err = acoustic_rel_err(ads, cfg, [shots[0], shots[len(shots) // 2]], vp_true, vp0)
+        rel_err["shot_indices"] = [0, len(shots) // 2]
+
     # plain FP64 on the same per-shot geometry, one shot per call
     fp64 = None
     if not args.no_fp64:
@@ -636,6 +673,12 @@ def main():
                 "fp64_plan_one_shot": plan64}
         torch.cuda.empty_cache()
 
+    # the elastic C4 gradient (32 shots, 4000 steps), measured in the same run
+    elastic = None
+    if not args.no_elastic and rank == 0:
+        elastic = elastic_measure(min(args.steps, 3), min(max(args.warmup, 1), 3))
+        torch.cuda.empty_cache()
+
     cpu = None
     if not args.no_cpu and rank == 0:
         v, t = cpu_baseline(cfg, shots, vp0, nstep, cores=1, steps=100)
@@ -661,7 +704,9 @@ def main():
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "rel_err": rel_err,
             "fp64_plain": fp64,
+            "elastic": elastic,
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
             "loss": float(loss),

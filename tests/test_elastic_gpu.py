@@ -50,6 +50,39 @@ def test_step_forward_and_transpose_vs_oracle(ads, orc, cuda):
         assert rel(a.cpu().numpy(), b) <= 1e-13
 
 
+def test_step_fp32_forward_and_transpose_vs_fp64_oracle(ads, orc, cuda):
+    """ads_elastic_step_fwd_f32 / _bwd_f32 against the FP64 oracle on the same
+    FP32-rounded inputs: rel-L2 <= 1e-5 for the state, its transpose and the
+    lambda / mu / rho gradients."""
+    g = golden("elastic_small.npz")
+    p = params(ads, g)
+    NX, NY = p.NX, p.NY
+    N = (NX + 2) * (NY + 2)
+    r32 = lambda a: np.asarray(a, dtype=np.float32).astype(np.float64)
+    prof = [r32(a) for a in ads.compute_elastic_PML_Params(p)]
+    ax, bx, kx, ay, by, ky = [a.reshape(-1) for a in prof]
+    rng = np.random.default_rng(21)
+    st = r32(rng.standard_normal(13 * N))
+    lam, mu, rho = r32(g["lam"]), r32(g["mu"]), r32(g["rho"])
+    srci, srcj, srct, srcv = [15, 3, 15], [10, 4, 10], [2, 0, 2], r32([1.5, -2.0, 0.25])
+    ref = orc.elastic_step_fwd(st, lam, mu, rho, ax, bx, ay, by, p.DELTAT, p.DELTAX, p.DELTAY,
+                               NX, NY, srci, srcj, srct, srcv)
+    t = lambda a: torch.as_tensor(np.asarray(a), dtype=torch.float32, device=cuda)
+    got = ads.elastic_one_step(p, t(rho), t(lam), t(mu), t(st).view(13, N),
+                               [t(a) for a in prof], srci, srcj, srcv, srct)
+    assert got.dtype == torch.float32
+    assert rel(got.double().cpu().numpy().reshape(-1), ref) <= 1e-5
+    w = r32(rng.standard_normal(13 * N))
+    gin, gl, gm, gr = orc.elastic_step_bwd(st, w, lam, mu, rho, ax, bx, ay, by, p.DELTAT,
+                                           p.DELTAX, p.DELTAY, NX, NY)
+    Gin, Gl, Gm, Gr = ads.elastic_one_step_grad(p, t(rho), t(lam), t(mu), t(st).view(13, N),
+                                                t(w).view(13, N), [t(a) for a in prof])
+    assert Gin.dtype == Gl.dtype == torch.float32
+    assert rel(Gin.double().cpu().numpy().reshape(-1), gin) <= 1e-5
+    for a, b in ((Gl, gl), (Gm, gm), (Gr, gr)):
+        assert rel(a.double().cpu().numpy(), b) <= 1e-5
+
+
 def shots_from(g):
     return [dict(srci=g["srci"], srcj=g["srcj"], srctype=g["srctype"], srcv=g["srcv"],
                  rcvi=g["rcvi"], rcvj=g["rcvj"], rcvtype=g["rcvtype"])]
