@@ -105,6 +105,7 @@ _SIGS = {
     "ads_acoustic_plan_device_bytes": [P],
     "ads_acoustic_plan_launches": [P, I32],
     "ads_acoustic_plan_resident_segments": [P],
+    "ads_acoustic_plan_steps_per_block": [P],
     "ads_acoustic_plan_profile": [P, P, P, P, P],
     "ads_acoustic_plan_forward": [P, P, P, P],
     "ads_acoustic_plan_gradient": [P, P, P, P, P, P, P],
@@ -143,6 +144,7 @@ _RESTYPE = {
     "ads_acoustic_plan_device_bytes": C.c_int64,
     "ads_acoustic_plan_launches": C.c_int64,
     "ads_acoustic_plan_resident_segments": C.c_int64,
+    "ads_acoustic_plan_steps_per_block": C.c_int64,
     "ads_elastic_plan_trace_offset": C.c_int64,
     "ads_elastic_plan_trace_count": C.c_int64,
     "ads_elastic_plan_device_bytes": C.c_int64,

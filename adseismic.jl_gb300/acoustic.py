@@ -219,6 +219,7 @@ class AcousticPlan:
         self.launches_forward = L.ads_acoustic_plan_launches(h, 0)
         self.launches_gradient = L.ads_acoustic_plan_launches(h, 1)
         self.resident_segments = L.ads_acoustic_plan_resident_segments(h)
+        self.steps_per_block = L.ads_acoustic_plan_steps_per_block(h)
 
     def close(self):
         if getattr(self, "_h", None):

@@ -1460,6 +1460,7 @@ struct AcPlanBase {
   int64_t bytes = 0;
   int64_t launches_fwd = 0, launches_grad = 0;
   int64_t resident = 0;  // checkpoint segments kept resident (no recompute)
+  int64_t steps_per_block = 1;  // forward steps per launch (configured or tuned)
 };
 
 namespace {
@@ -1548,6 +1549,21 @@ struct AcPlan final : AcPlanBase {
   double tcount[6] = {};  // launches, cell-steps for fwd / recompute / adjoint
   // time-blocked forward (FP32): steps per block, tile rows, tile lists
   int KB = 1, RB = 32;
+  // time-blocked tiles: items, their sources (halo KB), receiver rows and maps
+  struct TbLists {
+    std::vector<TbItem> items;
+    std::vector<TbSrc> srcs;
+    std::vector<TbRcvRow> rows;
+    std::vector<int> map, shot_end;
+  };
+  void build_tb(int kb, int rb, const ads_acoustic_shot* shots, TbLists& L) const;
+  int upload_tb(const TbLists& L, cudaStream_t st);
+  int tb_rows_for(int kb) const;  // rows of a time-blocked tile for kb steps per launch
+  // autotune may pick steps_per_block in {1, 2, 4} (FP32, variant W, no
+  // resident segments): the candidate lists and the device capacity they need
+  bool tb_auto = false;
+  std::vector<std::pair<int, TbLists>> tb_cand;
+  int64_t tb_cells = 0;  // interior cells of all shots (tile sizing)
   std::vector<int> tb_shot_end;  // per sorted shot: TB items of shots [0..s]
   TbItem* d_tb_items = nullptr;
   TbSrc* d_tb_srcs = nullptr;
@@ -1689,13 +1705,9 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
               "time blocking is implemented for FP32 plans (steps_per_block 0 or 1 for FP64)");
   ADS_REQUIRE(!vu || KB == 1,
               "time blocking is implemented for variant W (steps_per_block 0 or 1 for U)");
-  if (c.block_rows > 0) {
-    RB = c.block_rows;
-  } else {
-    RB = 32;
-    const int64_t colw = TB_THREADS - 2 * KB;
-    while (RB > 4 && cells / ((int64_t)RB * colw) < 152 * 4) RB /= 2;
-  }
+  tb_cells = cells;
+  RB = tb_rows_for(KB);
+  tb_auto = sizeof(T) == 4 && c.autotune && c.steps_per_block == 0 && !vu;
   // ---- trace layout (packed in the caller's shot order)
   trace_off.resize(ns);
   trace_total = 0;
@@ -1725,7 +1737,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   for (int s = 0; s < ns; s++) {
     const int64_t fs = (shots[order[s]].nx + 2) * pitch * (int64_t)sizeof(T);
     offs[s].u = L.take(2 * fs);
-    offs[s].u2 = L.take(KB > 1 ? 2 * fs : 0);
+    offs[s].u2 = L.take(KB > 1 || tb_auto ? 2 * fs : 0);
     offs[s].p = L.take(2 * fs);
     offs[s].q = L.take(2 * fs);
   }
@@ -1810,71 +1822,44 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
             (size_t)div_up(MY, std::min(Tile<T>::WF, Tile<T>::WA));
     cap_items = std::max(cap_items, n2);
   }
-  // time-blocked tiles: output columns [jo, jo + W), rows [i0, i0 + RB); sources
-  // of the loaded region (halo KB); receiver maps of the output region
-  std::vector<TbItem> tb_items;
-  std::vector<TbSrc> tb_srcs;
-  std::vector<TbRcvRow> tb_rows;
-  std::vector<int> tb_map, rcv_next_all;
+  // time-blocked tiles (build_tb) for the configured steps per launch and, when
+  // the autotuner may choose them, for 2 and 4; the device lists get the
+  // capacity of the largest
+  TbLists tbl;
+  std::vector<int> rcv_next_all;
   std::vector<int> rcv_next_off(ns, 0);
   tb_shot_end.assign(ns, 0);
-  if (KB > 1) {
-    const int W = TB_THREADS - 2 * KB;
-    for (int s = 0; s < ns; s++) {
+  if (KB > 1) build_tb(KB, RB, shots, tbl);
+  if (tb_auto)
+    for (int kb : {2, 4}) {
+      tb_cand.emplace_back(kb, TbLists{});
+      build_tb(kb, tb_rows_for(kb), shots, tb_cand.back().second);
+    }
+  if (KB > 1 || tb_auto)
+    for (int s = 0; s < ns; s++) {  // chain receivers sharing a cell
       const ads_acoustic_shot& h = shots[order[s]];
-      const int nx = (int)h.nx, ny = (int)MY;
       rcv_next_off[s] = (int)rcv_next_all.size();
       std::vector<int> next(h.nrcv, -1);
-      for (int64_t r = 0; r < h.nrcv; r++)  // chain receivers sharing a cell
+      for (int64_t r = 0; r < h.nrcv; r++)
         for (int64_t q = r + 1; q < h.nrcv; q++)
           if (h.rcvi[q] == h.rcvi[r] && h.rcvj[q] == h.rcvj[r]) {
             next[r] = (int)q;
             break;
           }
       rcv_next_all.insert(rcv_next_all.end(), next.begin(), next.end());
-      for (int i0 = 1; i0 <= nx; i0 += RB) {
-        const int i1 = std::min(i0 + RB, nx + 1);
-        for (int jo = 1; jo <= ny; jo += W) {
-          TbItem it{};
-          it.shot = s;
-          it.i0 = i0;
-          it.jo = jo;
-          it.src_b = (int)tb_srcs.size();
-          for (int64_t k = 0; k < h.nsrc; k++) {
-            const int i = (int)h.srci[k] - 1, j = (int)h.srcj[k] - 1;
-            if (i >= i0 - KB && i < i1 + KB && j >= jo - KB && j < jo - KB + TB_THREADS)
-              tb_srcs.push_back({i, j, (int)k, 0});
-          }
-          it.src_e = (int)tb_srcs.size();
-          it.rr_b = (int)tb_rows.size();
-          for (int i = i0; i < i1; i++) {
-            int off = -1;
-            for (int64_t r = 0; r < h.nrcv; r++) {
-              const int ri_ = (int)h.rcvi[r] - 1, rj = (int)h.rcvj[r] - 1;
-              if (ri_ != i || rj < jo || rj >= jo + W || rj < 1 || rj > ny) continue;
-              bool first = true;  // only the first receiver of a cell enters the map
-              for (int64_t q = 0; q < r; q++)
-                if (h.rcvi[q] == h.rcvi[r] && h.rcvj[q] == h.rcvj[r]) first = false;
-              if (!first) continue;
-              if (off < 0) {
-                off = (int)tb_map.size();
-                tb_map.insert(tb_map.end(), TB_THREADS, -1);
-                tb_rows.push_back({i, off});
-              }
-              tb_map[off + (rj - jo + KB)] = (int)r;
-            }
-          }
-          it.rr_e = (int)tb_rows.size();
-          tb_items.push_back(it);
-        }
-      }
-      tb_shot_end[s] = (int)tb_items.size();
     }
+  size_t cap_tbi = tbl.items.size(), cap_tbs = tbl.srcs.size(), cap_tbr = tbl.rows.size(),
+         cap_tbm = tbl.map.size();
+  for (const auto& cl : tb_cand) {
+    cap_tbi = std::max(cap_tbi, cl.second.items.size());
+    cap_tbs = std::max(cap_tbs, cl.second.srcs.size());
+    cap_tbr = std::max(cap_tbr, cl.second.rows.size());
+    cap_tbm = std::max(cap_tbm, cl.second.map.size());
   }
-  const size_t tbi_off = L.take(sizeof(TbItem) * std::max<size_t>(tb_items.size(), 1));
-  const size_t tbs_off = L.take(sizeof(TbSrc) * std::max<size_t>(tb_srcs.size(), 1));
-  const size_t tbr_off = L.take(sizeof(TbRcvRow) * std::max<size_t>(tb_rows.size(), 1));
-  const size_t tbm_off = L.take(sizeof(int) * std::max<size_t>(tb_map.size(), 1));
+  const size_t tbi_off = L.take(sizeof(TbItem) * std::max<size_t>(cap_tbi, 1));
+  const size_t tbs_off = L.take(sizeof(TbSrc) * std::max<size_t>(cap_tbs, 1));
+  const size_t tbr_off = L.take(sizeof(TbRcvRow) * std::max<size_t>(cap_tbr, 1));
+  const size_t tbm_off = L.take(sizeof(int) * std::max<size_t>(cap_tbm, 1));
   const size_t rnx_off = L.take(sizeof(int) * std::max<size_t>(rcv_next_all.size(), 1));
   const size_t shots_off = L.take(sizeof(AcShot<T>) * ns);
   // (sources / receivers: each is bucketed into exactly one item of a list)
@@ -1927,6 +1912,13 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   pool_bytes = L.used;
   bytes = (int64_t)pool_bytes;
   resident = nseg_max - res_seg;
+  // resident segments skip the recompute, which saves more than time blocking
+  // gains; the time-blocked kernel has no resident-store mode, so the
+  // autotuner considers it only for plans without them
+  if (resident > 0) {
+    tb_auto = false;
+    tb_cand.clear();
+  }
   {
     cudaError_t e = cudaMalloc(&pool, pool_bytes);
     if (e != cudaSuccess) {
@@ -2046,10 +2038,8 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     if (n) ADS_CUDA(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, st));
     return ADS_OK;
   };
-  if (int e = up(d_tb_items, tb_items.data(), sizeof(TbItem) * tb_items.size())) return e;
-  if (int e = up(d_tb_srcs, tb_srcs.data(), sizeof(TbSrc) * tb_srcs.size())) return e;
-  if (int e = up(d_tb_rows, tb_rows.data(), sizeof(TbRcvRow) * tb_rows.size())) return e;
-  if (int e = up(d_tb_map, tb_map.data(), sizeof(int) * tb_map.size())) return e;
+  if (KB > 1)
+    if (int e = upload_tb(tbl, st)) return e;
   if (int e = up(pool + rnx_off, rcv_next_all.data(), sizeof(int) * rcv_next_all.size()))
     return e;
   ADS_CUDA(cudaStreamSynchronize(st));  // host staging buffers go out of scope
@@ -2076,6 +2066,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     issue_reverse(nullptr, &n);
     nR = n;
   }
+  steps_per_block = KB;
   launches_fwd = 1 + nF;            // prep + loop
   launches_grad = 1 + nF + 2 + nR + 1;  // prep, loop, misfit+reduce, reverse, assemble
   // ---- graphs
@@ -2104,6 +2095,85 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
       }
     }
   }
+  return ADS_OK;
+}
+
+// Rows of a time-blocked tile: the configured block_rows, else 32 halved
+// until the tiles of kb steps per launch fill the SMs about four times over.
+template <typename T>
+int AcPlan<T>::tb_rows_for(int kb) const {
+  if (cfg.block_rows > 0) return (int)cfg.block_rows;
+  int rb = 32;
+  const int64_t colw = TB_THREADS - 2 * kb;
+  while (rb > 4 && tb_cells / ((int64_t)rb * colw) < 152 * 4) rb /= 2;
+  return rb;
+}
+
+// Time-blocked tiles for kb steps per launch: output columns [jo, jo + W),
+// W = TB_THREADS - 2 kb, rows [i0, i0 + rb); the sources of the loaded region
+// (halo kb); receiver maps of the output region.
+template <typename T>
+void AcPlan<T>::build_tb(int kb, int rb, const ads_acoustic_shot* shots, TbLists& L) const {
+  L = TbLists{};
+  L.shot_end.assign(nshots, 0);
+  const int W = TB_THREADS - 2 * kb;
+  const int ny = (int)cfg.MY;
+  for (int s = 0; s < nshots; s++) {
+    const ads_acoustic_shot& h = shots[order[s]];
+    const int nx = (int)h.nx;
+    for (int i0 = 1; i0 <= nx; i0 += rb) {
+      const int i1 = std::min(i0 + rb, nx + 1);
+      for (int jo = 1; jo <= ny; jo += W) {
+        TbItem it{};
+        it.shot = s;
+        it.i0 = i0;
+        it.jo = jo;
+        it.src_b = (int)L.srcs.size();
+        for (int64_t k = 0; k < h.nsrc; k++) {
+          const int i = (int)h.srci[k] - 1, j = (int)h.srcj[k] - 1;
+          if (i >= i0 - kb && i < i1 + kb && j >= jo - kb && j < jo - kb + TB_THREADS)
+            L.srcs.push_back({i, j, (int)k, 0});
+        }
+        it.src_e = (int)L.srcs.size();
+        it.rr_b = (int)L.rows.size();
+        for (int i = i0; i < i1; i++) {
+          int off = -1;
+          for (int64_t r = 0; r < h.nrcv; r++) {
+            const int ri_ = (int)h.rcvi[r] - 1, rj = (int)h.rcvj[r] - 1;
+            if (ri_ != i || rj < jo || rj >= jo + W || rj < 1 || rj > ny) continue;
+            bool first = true;  // only the first receiver of a cell enters the map
+            for (int64_t q = 0; q < r; q++)
+              if (h.rcvi[q] == h.rcvi[r] && h.rcvj[q] == h.rcvj[r]) first = false;
+            if (!first) continue;
+            if (off < 0) {
+              off = (int)L.map.size();
+              L.map.insert(L.map.end(), TB_THREADS, -1);
+              L.rows.push_back({i, off});
+            }
+            L.map[off + (rj - jo + kb)] = (int)r;
+          }
+        }
+        it.rr_e = (int)L.rows.size();
+        L.items.push_back(it);
+      }
+    }
+    L.shot_end[s] = (int)L.items.size();
+  }
+}
+
+template <typename T>
+int AcPlan<T>::upload_tb(const TbLists& L, cudaStream_t st) {
+  auto up = [&](void* dst, const void* src, size_t n) -> int {
+    if (n) ADS_CUDA(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, st));
+    return ADS_OK;
+  };
+  if (int e = up(d_tb_items, L.items.data(), sizeof(TbItem) * L.items.size())) return e;
+  if (int e = up(d_tb_srcs, L.srcs.data(), sizeof(TbSrc) * L.srcs.size())) return e;
+  if (int e = up(d_tb_rows, L.rows.data(), sizeof(TbRcvRow) * L.rows.size())) return e;
+  if (int e = up(d_tb_map, L.map.data(), sizeof(int) * L.map.size())) return e;
+  tb_shot_end = L.shot_end;
+  // the host lists of a candidate stay alive until the copies are done
+  ADS_CUDA(cudaStreamSynchronize(st));
   return ADS_OK;
 }
 
@@ -2434,6 +2504,51 @@ int AcPlan<T>::autotune(cudaStream_t st, int64_t pitch, size_t cap) {
     build_tiles(rows, width, pitch, L, pm);
     if (int e = upload_tiles(L, D, st)) return e;
   }
+  // third phase (tb_auto): steps per forward launch, 1 (the tiles chosen
+  // above) against the time-blocked kernel at 2 and 4, over the same steps
+  if (tb_auto && !tb_cand.empty()) {
+    const int t_end = std::min(9, nstep[0]);
+    auto time_tb = [&](int kb, float& ms) -> int {
+      for (int pass = 0; pass < 2; pass++) {
+        ADS_CUDA(cudaEventRecord(e0, st));
+        for (int t0 = 2, blk = 0; t0 <= t_end; blk++) {
+          const int NS = std::min(kb, t_end - t0 + 1);
+          const int na = shots_with_nstep_ge(t0);
+          if (kb == 1) {
+            if (int e = launch_fwd(st, 0, na, t0, 0, 0)) return e;
+          } else if (int e = launch_tb(st, false, tb_items_upto(na), t0, NS, 0, blk & 1, 0)) {
+            return e;
+          }
+          t0 += NS;
+        }
+        ADS_CUDA(cudaEventRecord(e1, st));
+        ADS_CUDA(cudaEventSynchronize(e1));
+        ADS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      }
+      return ADS_OK;
+    };
+    float best = 0.f;
+    KB = 1;
+    if (int e = time_tb(1, best)) return e;
+    int best_kb = 1;
+    for (const auto& cand : tb_cand) {
+      if (int e = upload_tb(cand.second, st)) return e;
+      KB = cand.first;
+      RB = tb_rows_for(KB);
+      float ms = 0.f;
+      if (int e = time_tb(KB, ms)) return e;
+      if (ms < best) {
+        best = ms;
+        best_kb = KB;
+      }
+    }
+    KB = best_kb;
+    RB = tb_rows_for(KB);
+    for (const auto& cand : tb_cand)
+      if (cand.first == KB)
+        if (int e = upload_tb(cand.second, st)) return e;
+    tb_cand.clear();
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   ADS_CUDA(cudaStreamSynchronize(st));
@@ -2736,6 +2851,10 @@ int64_t ads_acoustic_plan_launches(const ads_acoustic_plan* plan, int gradient) 
 
 int64_t ads_acoustic_plan_resident_segments(const ads_acoustic_plan* plan) {
   return plan ? plan->impl->resident : -1;
+}
+
+int64_t ads_acoustic_plan_steps_per_block(const ads_acoustic_plan* plan) {
+  return plan && plan->impl ? plan->impl->steps_per_block : -1;
 }
 
 int ads_acoustic_plan_profile(ads_acoustic_plan* plan, const double* vp, const void* observed,

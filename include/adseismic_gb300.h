@@ -266,7 +266,10 @@ typedef struct ads_acoustic_config {
                               FP64: 1); 0 = automatic (1) */
   int32_t block_rows;      /* tile height of the time-blocked forward; 0 = automatic */
   int32_t autotune;        /* 1: time candidate tile heights of the forward and adjoint
-                              kernels at plan creation and keep the fastest */
+                              kernels at plan creation and keep the fastest; FP32
+                              variant-W plans without resident segments and with
+                              steps_per_block 0 also time 1, 2 and 4 forward steps
+                              per launch and keep the fastest */
   int32_t resident_segments; /* checkpoint segments (the last ones) whose forward
                                 wavefields stay in device memory for the reverse sweep,
                                 which then neither restores nor recomputes them:
@@ -315,6 +318,9 @@ int64_t ads_acoustic_plan_device_bytes(const ads_acoustic_plan* plan);
 int64_t ads_acoustic_plan_launches(const ads_acoustic_plan* plan, int gradient);
 /* Checkpoint segments kept resident (see resident_segments); -1 for a null plan. */
 int64_t ads_acoustic_plan_resident_segments(const ads_acoustic_plan* plan);
+/* Forward steps per launch the plan runs (steps_per_block as configured, or as
+ * the autotuner chose it); -1 for a null plan.  No reference counterpart. */
+int64_t ads_acoustic_plan_steps_per_block(const ads_acoustic_plan* plan);
 /* Kernel timing: runs one gradient with direct launches (no graphs) and CUDA
  * events recorded around (0) the forward loop (k_ac_fwd launches only), (1)
  * one full checkpoint segment's recompute launches and (2) the same segment's

@@ -235,14 +235,18 @@ def test_plan_fp32_time_blocked_vs_oracle(ads, orc, cuda, kb, rows):
 
 
 @pytest.mark.parametrize("precision", ["f64", "f32"])
-def test_autotuned_plan_vs_oracle(ads, orc, cuda, precision):
+@pytest.mark.parametrize("resident", [0, -1])
+def test_autotuned_plan_vs_oracle(ads, orc, cuda, precision, resident):
+    """Tuned row heights; FP32 plans without resident segments also tune the
+    forward steps per launch (1, 2 or 4)."""
     MX, MY, shots, vp = uneven_case(31, nshots=5)
     h, dt, npml, vref = 10.0, 1e-3, 5, 1500.0
     ref_tr = oracle_multishot(orc, MX, MY, shots, vp, h, dt, npml, vref)
     obs = [t * 0.97 for t in ref_tr]
     ref_loss, ref_grad = oracle_multishot(orc, MX, MY, shots, vp, h, dt, npml, vref, obs)
     plan = ads.AcousticPlan(MX, MY, h, h, dt, shots, npml=npml, vp_ref=vref, precision=precision,
-                            ckpt_every=11, autotune=True)
+                            ckpt_every=11, autotune=True, resident_segments=resident)
+    assert plan.steps_per_block in ((1, 2, 4) if precision == "f32" and resident < 0 else (1,))
     dtype = plan.dtype
     loss, grad = plan.gradient(T(vp, cuda), plan.pack([T(o, cuda, dtype) for o in obs]))
     torch.cuda.synchronize()
