@@ -11,7 +11,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libadseismic_gb300.so")
 
-ADS_OK, ADS_ERR_INVALID, ADS_ERR_CUDA, ADS_ERR_NOMEM, ADS_ERR_UNSUPPORTED, ADS_ERR_TIMEOUT = range(6)
+ADS_OK, ADS_ERR_INVALID, ADS_ERR_CUDA, ADS_ERR_NOMEM, ADS_ERR_UNSUPPORTED = range(5)
 ADS_F64, ADS_F32 = 0, 1
 ADS_VARIANT_W, ADS_VARIANT_U = 0, 1
 
@@ -20,7 +20,6 @@ _STATUS = {
     ADS_ERR_CUDA: "CUDA error",
     ADS_ERR_NOMEM: "out of device memory",
     ADS_ERR_UNSUPPORTED: "unsupported",
-    ADS_ERR_TIMEOUT: "device wait timed out",
 }
 
 

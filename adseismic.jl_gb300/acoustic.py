@@ -182,7 +182,7 @@ class AcousticPlan:
         cfg.rows_per_thread = rows_per_thread
         cfg.steps_per_block = steps_per_block
         cfg.block_rows = block_rows
-        cfg.autotune = int(bool(autotune))
+        cfg.autotune = int(autotune)
         cfg.resident_segments = int(resident_segments)
         cfg.resident_mem_pct = int(resident_mem_pct)
         self.MX, self.MY = MX, MY

@@ -102,6 +102,7 @@ struct AcShot {
   int64_t pitch, fs;  // row pitch and elements per field
   int nsrc, nrcv, nseg, pad_;
   T *u, *p, *q;       // forward rings (2 fields each)
+  T* d;               // FP32 increment form: d_t = u_t - u_{t-1}, updated in place
   T* u2;              // time-blocked forward: U_{t-1} of the two state sets
   const int* rcv_next; // next receiver on the same cell, or -1 (time-blocked forward)
   T *seg, *ckpt;      // segment store (k+1 fields), checkpoints (nseg x 4 fields)
@@ -287,7 +288,22 @@ __device__ __forceinline__ void record_traces(const AcItem& it, const AcShot<T>&
 // from u_{t-1} by k_ac_phi_u at the start of this step, so this kernel only
 // reads them (as the custom-operator form reads its phi_{t-1}, psi_{t-1}) and
 // writes neither; its checkpoints store the phi / psi it read.
-template <typename T, int MODE, bool INT, bool VU = false>
+//
+// CK = true: the kernel may write checkpoint ckpt_slot (MODE 0).  The PML
+// kernel takes that code only at checkpoint times, which keeps its other
+// steps free of spills; the interior kernel keeps it in every MODE 0 step
+// (measured: the form without it spills more at its 32 registers).
+//
+// INC = true (FP32 plans): the increment form.  The state is u_t and
+// d_t = u_t - u_{t-1} (one field, updated in place) instead of u_t and
+// u_{t-1}; the step forms d_{t+1} from d_t and the Laplacian written as
+// differences of u, then u_{t+1} = u_t + d_{t+1}.  In exact arithmetic this is
+// the same update; in FP32 the three-level form's rounding of u_{t+1} (about
+// eps |u|) perturbs the difference u_{t+1} - u_t, which the oscillation
+// amplifies by 1 / (w dt), while here the rounding of d is relative to |d|.
+// Traces and gradients then stay near 1e-6 of the FP64 ones over thousands of
+// steps instead of drifting to 1e-4.  The checkpoints hold (u_t, d_t, phi, psi).
+template <typename T, int MODE, bool INT, bool VU = false, bool CK = false, bool INC = false>
 __global__ void __launch_bounds__(Tile<T>::TPB, INT ? Tile<T>::MINB_FI : Tile<T>::MINB_F)
 k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
          const CellRef* __restrict__ srcs, const CellRef* __restrict__ rcvs, AcConst<T> K,
@@ -313,6 +329,8 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     out = sh.u + (int64_t)(t & 1) * fs;
     wo = out;  // u_t overwrites u_{t-2}: row r is read one iteration before it is written
   }
+  T* dd = sh.d;  // increment form: d_{t-1} in, d_t out (row r read before it is written)
+  if (INC) wo = dd;
   const T* pin = sh.p + (int64_t)((t - 1) & 1) * fs;
   T* pout = sh.p + (int64_t)(t & 1) * fs;
   const T* qin = sh.q + (int64_t)((t - 1) & 1) * fs;
@@ -332,7 +350,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   const int i0 = it.i0 + (threadIdx.x >> 5) * ri, i_end = min(i0 + ri, nx + 1);
   if (i0 > nx) return;  // whole warps only: every later barrier is warp-level
   auto off = [&](int r) { return (int64_t)r * P + col; };
-  const bool ck_on = !SEG && ckpt_slot > 0 && ckpt_slot < sh.nseg;
+  const bool ck_on = CK && !SEG && ckpt_slot > 0 && ckpt_slot < sh.nseg;
   if (INT || interior_rows<T>(tfree, sx, i0, i_end, lane)) {
     // Interior item: sigma = tau = 0 on every row and column the warp reads,
     // so phi = psi = 0 there and the step reduces to the plain wave update
@@ -371,14 +389,22 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       if (lane == 0) wL = hq[0];
       else if (lane == 31) wR = hq[0];
       if (jld) {
-        V vo;
+        V vo, dv;
 #pragma unroll
         for (int c = 0; c < C; c++) {
           const T wS = c == 0 ? wL : w0.v[c - 1];
           const T wN = c == C - 1 ? wR : w0.v[c + 1];
           const T cv = cq[0].v[c];
-          T v = (T(2) - K.kxy * cv) * w0.v[c] + cv * K.cx * (wp.v[c] + wm.v[c]) +
+          T v;
+          if constexpr (INC) {
+            const T u0 = w0.v[c];
+            dv.v[c] = oq[0].v[c] + cv * (K.cx * ((wp.v[c] - u0) + (wm.v[c] - u0)) +
+                                         K.cy * ((wN - u0) + (wS - u0)));
+            v = u0 + dv.v[c];
+          } else {
+            v = (T(2) - K.kxy * cv) * w0.v[c] + cv * K.cx * (wp.v[c] + wm.v[c]) +
                 cv * K.cy * (wN + wS) - oq[0].v[c];
+          }
           if constexpr (!INT) {
             for (int e = it.src_b; e < it.src_e; e++) {
               const CellRef r = srcs[e];
@@ -388,10 +414,11 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
           vo.v[c] = v;
         }
         stv<T, C>(out, row, vo, j, ny);
+        if constexpr (INC) stv<T, C>(dd, row, dv, j, ny);
         if (ck_on) {
           T* ck = sh.ckpt + (int64_t)ckpt_slot * 4 * fs;
           stv<T, C>(ck, row, vo, j, ny);
-          stv<T, C>(ck + fs, row, w0, j, ny);
+          stv<T, C>(ck + fs, row, INC ? dv : w0, j, ny);
         }
       }
 #pragma unroll
@@ -442,7 +469,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     }
     if (jld) {
       const T sg = sx[i];
-      V vo, po, qo;
+      V vo, po, qo, dv;
 #pragma unroll
       for (int c = 0; c < C; c++) {
         const T wS = c == 0 ? wL : w0.v[c - 1];
@@ -450,13 +477,31 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
         const T qS = c == 0 ? qL : q0.v[c - 1];
         const T qN = c == C - 1 ? qR : q0.v[c + 1];
         const T cv = c0.v[c], s = sg + tj[c];
-        T v = (T(2) - sg * tj[c] * K.dt2 - K.kxy * cv) * w0.v[c] + cv * K.cx * (wp.v[c] + wm.v[c]) +
-              cv * K.cy * (wN + wS) + K.fx * (pp.v[c] - pm.v[c]) + K.fy * (qN - qS) -
-              (T(1) - s * K.hdt) * wo0.v[c];
-        v = pml_damp<T>(v, s, K);
-        for (int e = it.src_b; e < it.src_e; e++) {
-          const CellRef r = srcs[e];
-          if (r.cell == row + c) v += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
+        T v;
+        if constexpr (INC) {
+          // d_{t} = [(1 - s dt/2) d_{t-1} + c (cx (u_{i+1} - u) + ...) - sigma tau dt^2 u
+          //          + phi / psi terms] / (1 + s dt/2), the three-level update less u_{t-1}
+          const T u0 = w0.v[c];
+          T dn = (T(1) - s * K.hdt) * wo0.v[c] +
+                 cv * (K.cx * ((wp.v[c] - u0) + (wm.v[c] - u0)) +
+                       K.cy * ((wN - u0) + (wS - u0))) -
+                 sg * tj[c] * K.dt2 * u0 + K.fx * (pp.v[c] - pm.v[c]) + K.fy * (qN - qS);
+          dn = pml_damp<T>(dn, s, K);
+          for (int e = it.src_b; e < it.src_e; e++) {
+            const CellRef r = srcs[e];
+            if (r.cell == row + c) dn += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
+          }
+          dv.v[c] = dn;
+          v = u0 + dn;
+        } else {
+          v = (T(2) - sg * tj[c] * K.dt2 - K.kxy * cv) * w0.v[c] +
+              cv * K.cx * (wp.v[c] + wm.v[c]) + cv * K.cy * (wN + wS) +
+              K.fx * (pp.v[c] - pm.v[c]) + K.fy * (qN - qS) - (T(1) - s * K.hdt) * wo0.v[c];
+          v = pml_damp<T>(v, s, K);
+          for (int e = it.src_b; e < it.src_e; e++) {
+            const CellRef r = srcs[e];
+            if (r.cell == row + c) v += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
+          }
         }
         vo.v[c] = v;
         if constexpr (!VU) {
@@ -465,6 +510,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
         }
       }
       stv<T, C>(out, row, vo, j, ny);
+      if constexpr (INC) stv<T, C>(dd, row, dv, j, ny);
       if (!VU && n0) {
         stv<T, C>(pout, row, po, j, ny);
         stv<T, C>(qout, row, qo, j, ny);
@@ -472,7 +518,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       if (ck_on) {
         T* ck = sh.ckpt + (int64_t)ckpt_slot * 4 * fs;
         stv<T, C>(ck, row, vo, j, ny);
-        stv<T, C>(ck + fs, row, w0, j, ny);
+        stv<T, C>(ck + fs, row, INC ? dv : w0, j, ny);
         if (n0) {
           stv<T, C>(ck + 2 * fs, row, VU ? p0 : po, j, ny);
           stv<T, C>(ck + 3 * fs, row, VU ? q0 : qo, j, ny);
@@ -496,21 +542,24 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   }
 }
 
-// Restore checkpoint `slot` of every active shot into the segment store
-// (slot 0 <- u_{a-2}, slot 1 <- u_{a-1}) and the phi/psi rings at a-1.
+// Restore checkpoint `slot` of every active shot: u_{a-1} into segment-store
+// slot 1 and, in the three-level form, u_{a-2} into slot 0 (increment form,
+// inc = 1: d_{a-1} into the increment field), and phi / psi into set `pset`
+// (-1: set (a-1) & 1).
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_ac_restore(const AcShot<T>* __restrict__ shots, int slot, int a, int pset) {
+k_ac_restore(const AcShot<T>* __restrict__ shots, int slot, int a, int pset, int inc) {
   const AcShot<T>& sh = shots[blockIdx.y];
   const int64_t P = sh.pitch, fs = sh.fs;
   const T* ck = sh.ckpt + (int64_t)slot * 4 * fs;
   const int ps = pset >= 0 ? pset : ((a - 1) & 1);  // phi/psi set the recompute reads
   T* pr = sh.p + (int64_t)ps * fs;
   T* qr = sh.q + (int64_t)ps * fs;
+  T* second = inc ? sh.d : sh.seg;
   for (int i = 1 + blockIdx.x; i <= sh.nx; i += gridDim.x)
     for (int j = 1 + threadIdx.x; j <= sh.ny; j += blockDim.x) {
       const int64_t row = (int64_t)i * P + j + JOFF;
-      sh.seg[row] = ck[fs + row];
+      second[row] = ck[fs + row];
       sh.seg[fs + row] = ck[row];
       pr[row] = ck[2 * fs + row];
       qr[row] = ck[3 * fs + row];
@@ -1470,6 +1519,7 @@ struct AcPlan final : AcPlanBase {
   ads_acoustic_config cfg{};
   int nshots = 0;
   bool vu = false;    // variant U: phi / psi from the new field (pre-pass kernels)
+  bool inc = false;   // FP32 increment form (k_ac_fwd INC); off for time blocking
   int K = 0;          // checkpoint spacing
   // Resident segments: segments res_seg .. nseg_max-1 keep the forward
   // wavefields of their steps in the shots' stores (slot t - res_base), so
@@ -1623,7 +1673,9 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   ADS_REQUIRE(ns >= 1 && ns < (1 << 20), "nshots must be in [1, 2^20)");
   ADS_REQUIRE(c.MX >= 1 && c.MY >= 1 && c.MY < (1 << 24) && c.MX < (1 << 24),
               "model size out of range");
-  ADS_REQUIRE(c.dx > 0 && c.dy > 0 && c.dt > 0, "dx, dy, dt must be positive");
+  ADS_REQUIRE(c.dx > 0 && c.dy > 0 && c.dt > 0 && std::isfinite(c.dx) && std::isfinite(c.dy) &&
+                  std::isfinite(c.dt) && std::isfinite(c.vp_ref),
+              "dx, dy, dt must be positive and finite (and vp_ref finite)");
   ADS_REQUIRE(c.npml >= 1 && c.Rcoef > 0 && c.Rcoef < 1, "invalid PML parameters");
   ADS_REQUIRE(c.variant == ADS_VARIANT_W || c.variant == ADS_VARIANT_U,
               "variant must be ADS_VARIANT_W or ADS_VARIANT_U");
@@ -1707,7 +1759,10 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
               "time blocking is implemented for variant W (steps_per_block 0 or 1 for U)");
   tb_cells = cells;
   RB = tb_rows_for(KB);
-  tb_auto = sizeof(T) == 4 && c.autotune && c.steps_per_block == 0 && !vu;
+  // steps per launch are tuned only on request (autotune 2): the time-blocked
+  // kernel keeps the three-level form, whose FP32 rounding error is larger
+  tb_auto = sizeof(T) == 4 && c.autotune >= 2 && c.steps_per_block == 0 && !vu;
+  inc = sizeof(T) == 4 && KB == 1;
   // ---- trace layout (packed in the caller's shot order)
   trace_off.resize(ns);
   trace_total = 0;
@@ -1724,7 +1779,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   size_t off_fwd_begin, off_fwd_end, off_adj_begin, off_adj_end;
   DevPool L;
   struct Offs {
-    size_t u, u2, p, q, seg, ckpt, lu, lp, lq, c, sx, ty, gc, gc32, gsrc, srcv, slist;
+    size_t u, u2, d, p, q, seg, ckpt, lu, lp, lq, c, sx, ty, gc, gc32, gsrc, srcv, slist;
   };
   std::vector<Offs> offs(ns);
   std::vector<int> nseg(ns);
@@ -1738,6 +1793,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     const int64_t fs = (shots[order[s]].nx + 2) * pitch * (int64_t)sizeof(T);
     offs[s].u = L.take(2 * fs);
     offs[s].u2 = L.take(KB > 1 || tb_auto ? 2 * fs : 0);
+    offs[s].d = L.take(sizeof(T) == 4 ? fs : 0);
     offs[s].p = L.take(2 * fs);
     offs[s].q = L.take(2 * fs);
   }
@@ -1971,6 +2027,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     d.nseg = nseg[s];
     d.u = (T*)(pool + offs[s].u);
     d.u2 = (T*)(pool + offs[s].u2);
+    d.d = sizeof(T) == 4 ? (T*)(pool + offs[s].d) : nullptr;
     d.rcv_next = (const int*)(pool + rnx_off) + rcv_next_off[s];
     d.p = (T*)(pool + offs[s].p);
     d.q = (T*)(pool + offs[s].q);
@@ -2049,6 +2106,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   // ---- autotuner: time candidate tilings on the plan's own buffers
   if (c.autotune)
     if (int e = autotune(st, pitch, cap_items)) return e;
+  inc = sizeof(T) == 4 && KB == 1;
   // ---- timing ranges: the first full-length segment the reverse sweep meets
   cells_prefix.resize(ns);
   for (int s = 0; s < ns; s++)
@@ -2309,14 +2367,24 @@ int AcPlan<T>::launch_fwd(cudaStream_t st, int mode, int na, int t, int base, in
     ADS_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
     sp = side;
   }
-#define ADS_FWD(M, IN, VUF, items_, n_, s_, rows_)                                       \
-  k_ac_fwd<T, M, IN, VUF><<<n_, TPB, 0, s_>>>(items_, d_shots, tf.srcs, tf.rcvs, kc, t, base, \
-                                              ck, rows_)
-#define ADS_FWD_MODE(IN, VUF, items_, n_, s_, rows_)                 \
-  do {                                                               \
-    if (mode == 1) ADS_FWD(1, IN, VUF, items_, n_, s_, rows_);      \
-    else if (mode == 2) ADS_FWD(2, IN, VUF, items_, n_, s_, rows_); \
-    else ADS_FWD(0, IN, VUF, items_, n_, s_, rows_);                \
+#define ADS_FWD_(M, IN, VUF, CKF, INCF, items_, n_, s_, rows_)                              \
+  k_ac_fwd<T, M, IN, VUF, CKF, INCF><<<n_, TPB, 0, s_>>>(items_, d_shots, tf.srcs, tf.rcvs, kc, \
+                                                         t, base, ck, rows_)
+#define ADS_FWD(M, IN, VUF, CKF, items_, n_, s_, rows_)                 \
+  do {                                                                  \
+    if constexpr (sizeof(T) == 4) {                                     \
+      if (inc) ADS_FWD_(M, IN, VUF, CKF, true, items_, n_, s_, rows_);  \
+      else ADS_FWD_(M, IN, VUF, CKF, false, items_, n_, s_, rows_);     \
+    } else {                                                            \
+      ADS_FWD_(M, IN, VUF, CKF, false, items_, n_, s_, rows_);          \
+    }                                                                   \
+  } while (0)
+#define ADS_FWD_MODE(IN, VUF, items_, n_, s_, rows_)                        \
+  do {                                                                      \
+    if (mode == 1) ADS_FWD(1, IN, VUF, false, items_, n_, s_, rows_);      \
+    else if (mode == 2) ADS_FWD(2, IN, VUF, false, items_, n_, s_, rows_); \
+    else if (IN || ck > 0) ADS_FWD(0, IN, VUF, true, items_, n_, s_, rows_); \
+    else ADS_FWD(0, IN, VUF, false, items_, n_, s_, rows_);                \
   } while (0)
   if (ni > 0) {
     ADS_FWD_MODE(true, false, tf.items, ni, st, ri_f);
@@ -2339,6 +2407,7 @@ int AcPlan<T>::launch_fwd(cudaStream_t st, int mode, int na, int t, int base, in
   }
 #undef ADS_FWD_MODE
 #undef ADS_FWD
+#undef ADS_FWD_
   if (fork) {
     ADS_CUDA(cudaEventRecord(ev_join, side));
     ADS_CUDA(cudaStreamWaitEvent(st, ev_join, 0));
@@ -2651,8 +2720,8 @@ int AcPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
       if (!count) {
         // phi / psi set the recompute's first step reads: variant W's step a
         // reads set (a-1) & 1; variant U's pre-pass of step a reads set a & 1
-        k_ac_restore<T><<<dim3(kRowBlocks, na), 256, 0, st>>>(d_shots, s, a,
-                                                             KB > 1 ? 0 : (vu ? (a & 1) : -1));
+        k_ac_restore<T><<<dim3(kRowBlocks, na), 256, 0, st>>>(
+            d_shots, s, a, KB > 1 ? 0 : (vu ? (a & 1) : -1), inc ? 1 : 0);
         ADS_LAUNCHED(1);
       }
       n++;

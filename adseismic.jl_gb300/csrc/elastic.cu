@@ -1747,7 +1747,9 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   ADS_REQUIRE(c.NX >= 4 && c.NY >= 4 && c.NX < (1 << 20) && c.NY < (1 << 20),
               "NX, NY must be in [4, 2^20)");
   ADS_REQUIRE(c.NSTEP >= 1 && c.NSTEP < (1 << 24), "NSTEP must be >= 1");
-  ADS_REQUIRE(c.dx > 0 && c.dy > 0 && c.dt > 0, "dx, dy, dt must be positive");
+  ADS_REQUIRE(c.dx > 0 && c.dy > 0 && c.dt > 0 && std::isfinite(c.dx) && std::isfinite(c.dy) &&
+                  std::isfinite(c.dt) && std::isfinite(c.vp_ref),
+              "dx, dy, dt must be positive and finite (and vp_ref finite)");
   ADS_REQUIRE(c.npml >= 1 && c.Rcoef > 0 && c.Rcoef < 1, "invalid CPML parameters");
   ADS_REQUIRE(c.ckpt_every >= 0, "negative ckpt_every");
   nshots = (int)ns;

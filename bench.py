@@ -38,8 +38,9 @@ UNIT = "shot-gradients/s"
 
 # algorithmic bytes per interior cell-step (each array counted once per step)
 BYTES = {
-    ("fwd", "f32"): 32,   # read w, w_old, phi, psi, c; write u, phi', psi'
-    ("fwd", "f64"): 64,
+    ("fwd", "f32"): 36,   # increment form: read u, d, phi, psi, c; write u', d', phi', psi'
+    ("fwd", "f64"): 64,   # read w, w_old, phi, psi, c; write u, phi', psi'
+
     ("adj", "f32"): 52,   # adjoint state 32 + forward w 4 + FP64 grad_c RMW 16
     ("adj", "f64"): 88,   # 64 + 8 + 16
 }

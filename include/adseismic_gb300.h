@@ -37,8 +37,9 @@ enum {
   ADS_ERR_INVALID = 1,     /* bad argument, shape or index */
   ADS_ERR_CUDA = 2,        /* CUDA runtime error (launch, device, copy) */
   ADS_ERR_NOMEM = 3,       /* device allocation failed */
-  ADS_ERR_UNSUPPORTED = 4, /* valid request outside what this build implements */
-  ADS_ERR_TIMEOUT = 5      /* a bounded device-side wait gave up */
+  ADS_ERR_UNSUPPORTED = 4  /* valid request outside what this build implements */
+  /* 5 is reserved: no kernel of this library waits on another block, flag or
+     device, so no call can time out on the device. */
 };
 
 enum { ADS_F64 = 0, ADS_F32 = 1 };          /* arithmetic / storage type */
@@ -257,7 +258,11 @@ typedef struct ads_acoustic_config {
   double vp_ref;      /* PML reference velocity (Struct.jl default 1000) */
   int32_t use_pml;    /* bitmask as ads_acoustic_pml_profiles; 15 = all sides */
   int32_t precision;  /* ADS_F64: plain FP64 drop-in; ADS_F32: FP32 stencils and
-                         storage, FP64 misfit and gradient accumulation */
+                         storage, FP64 misfit and gradient accumulation.  FP32 plans
+                         step in the increment form (state u_t and d_t = u_t - u_{t-1},
+                         the same update in exact arithmetic, whose FP32 rounding
+                         does not build up over thousands of steps); with
+                         steps_per_block > 1 they keep the three-level form */
   int32_t variant;    /* ADS_VARIANT_W (only form with a whole-path adjoint) */
   int32_t use_graph;  /* 1: capture the time loops in CUDA graphs (default) */
   int64_t ckpt_every; /* forward checkpoint spacing k in steps; 0 = automatic */
@@ -266,10 +271,11 @@ typedef struct ads_acoustic_config {
                               FP64: 1); 0 = automatic (1) */
   int32_t block_rows;      /* tile height of the time-blocked forward; 0 = automatic */
   int32_t autotune;        /* 1: time candidate tile heights of the forward and adjoint
-                              kernels at plan creation and keep the fastest; FP32
-                              variant-W plans without resident segments and with
-                              steps_per_block 0 also time 1, 2 and 4 forward steps
-                              per launch and keep the fastest */
+                              kernels at plan creation and keep the fastest; 2: also,
+                              for FP32 variant-W plans without resident segments and
+                              with steps_per_block 0, time 1, 2 and 4 forward steps
+                              per launch and keep the fastest (more than 1 selects
+                              the time-blocked three-level form) */
   int32_t resident_segments; /* checkpoint segments (the last ones) whose forward
                                 wavefields stay in device memory for the reverse sweep,
                                 which then neither restores nor recomputes them:

@@ -245,7 +245,7 @@ def test_autotuned_plan_vs_oracle(ads, orc, cuda, precision, resident):
     obs = [t * 0.97 for t in ref_tr]
     ref_loss, ref_grad = oracle_multishot(orc, MX, MY, shots, vp, h, dt, npml, vref, obs)
     plan = ads.AcousticPlan(MX, MY, h, h, dt, shots, npml=npml, vp_ref=vref, precision=precision,
-                            ckpt_every=11, autotune=True, resident_segments=resident)
+                            ckpt_every=11, autotune=2, resident_segments=resident)
     assert plan.steps_per_block in ((1, 2, 4) if precision == "f32" and resident < 0 else (1,))
     dtype = plan.dtype
     loss, grad = plan.gradient(T(vp, cuda), plan.pack([T(o, cuda, dtype) for o in obs]))

@@ -12,20 +12,17 @@ central finite differences of the FP64 plan's loss on 16 random cells.
 Tolerances (rel-L2 = ||x - x_ref|| / ||x_ref||):
   FP64 plan vs oracle                              1e-12
   FP32 vs FP64, gradient (each field)              1e-4   (the benchmark spec's bound)
-  FP32 vs FP64, elastic traces (4000 steps)        1e-5
-  FP32 vs FP64, acoustic traces, 3000 steps        1e-4
-  FP32 vs FP64, acoustic traces, 6000 steps        3e-4
+  FP32 vs FP64, all traces of a shot               1e-5
   C2 central differences (eps = 1e-4 vp)           1e-6 per cell
 
-The acoustic step stores u_{t+1} = 2 u_t - u_{t-1} + ... in FP32 (the
-custom operator's three-level form).  Each rounding of u, about eps |u|, acts
-on the oscillation as a velocity kick of that size, which the oscillation
-turns into a displacement 1 / (w dt) times larger; the kicks add up as a
-random walk.  The trace error is therefore about eps sqrt(NSTEP) / (w dt):
-4e-5 at 3000 steps of 0.8 ms for 15 Hz (w dt = 0.075), rising with the record
-length, which the trace tolerances above follow.  The velocity-stress elastic
-scheme has no such cancellation and stays near 1e-6.  The gradient's bound
-holds either way.
+FP32 acoustic plans run the increment form (state u_t, d_t = u_t - u_{t-1}).
+In the custom operator's three-level form, u_{t+1} = 2 u_t - u_{t-1} + ...,
+each FP32 rounding of u (about eps |u|) perturbs the difference u_{t+1} - u_t,
+which the oscillation amplifies by 1 / (w dt); the trace error then grows as
+eps sqrt(NSTEP) / (w dt), measured 3.6e-5 at C3's 3000 steps and 1.6e-4 at
+C5's 6000, and a small misfit amplifies it further in the gradient (2.9e-4
+at C5's longest shot).  The increment form rounds d relative to |d|, like the
+velocity-stress elastic scheme, which stays near 1e-6.
 """
 import numpy as np
 import pytest
@@ -35,9 +32,7 @@ pytestmark = pytest.mark.gpu
 
 TOL64 = 1e-12
 TOL32_GRAD = 1e-4
-TOL32_TRACE_EL = 1e-5
-TOL32_TRACE_3000 = 1e-4
-TOL32_TRACE_6000 = 3e-4
+TOL32_TRACE = 1e-5
 TOL_FD = 1e-6
 
 
@@ -130,7 +125,7 @@ def test_c3_fp32_vs_fp64_full_length(ads, cuda, cfgs, c3):
            trace_max=float(per.max()), trace_median=float(np.median(per)),
            loss_rel=abs(float(l32) - float(l64)) / float(l64))
     assert rg <= TOL32_GRAD
-    assert rt <= TOL32_TRACE_3000
+    assert rt <= TOL32_TRACE
 
 
 # ------------------------------------------------------------------ C5
@@ -160,7 +155,7 @@ def test_c5_longest_shot_fp32_vs_fp64(ads, cuda, cfgs):
            grad=rg, traces=rt, trace_max=float(per.max()), trace_median=float(np.median(per)),
            loss_rel=abs(float(l32) - float(l64)) / float(l64))
     assert rg <= TOL32_GRAD
-    assert rt <= TOL32_TRACE_6000
+    assert rt <= TOL32_TRACE
 
 
 # ------------------------------------------------------------------ C2
@@ -233,7 +228,7 @@ def test_c4_fp32_vs_fp64_full_length(ads, cuda, cfgs, c4):
            grad_mu=rg["mu"], grad_rho=rg["rho"], traces=rt, trace_max=float(per.max()),
            trace_median=float(np.median(per)))
     assert max(rg.values()) <= TOL32_GRAD
-    assert rt <= TOL32_TRACE_EL
+    assert rt <= TOL32_TRACE
 
 
 def test_c4_fp64_plan_matches_oracle(ads, orc, cuda, cfgs):
