@@ -63,7 +63,7 @@ class ElasticConfig(C.Structure):
         ("use_pml", C.c_int32), ("precision", C.c_int32), ("use_graph", C.c_int32),
         ("rows_per_warp", C.c_int32), ("ckpt_every", C.c_int64),
         ("resident_segments", C.c_int32), ("resident_mem_pct", C.c_int32),
-        ("source_gradient", C.c_int32), ("reserved", C.c_int32 * 5),
+        ("source_gradient", C.c_int32), ("autotune", C.c_int32), ("reserved", C.c_int32 * 4),
     ]
 
 
@@ -120,6 +120,7 @@ _SIGS = {
     "ads_elastic_plan_device_bytes": [P],
     "ads_elastic_plan_launches": [P, I32],
     "ads_elastic_plan_resident_segments": [P],
+    "ads_elastic_plan_rows": [P, I32],
     "ads_elastic_plan_gradient_ex": [P, P, P, P, P, P, P, P, P, P, P, P],
     "ads_elastic_plan_source_offset": [P, I64],
     "ads_elastic_plan_set_source_values": [P, I64, P, P],
@@ -149,6 +150,7 @@ _RESTYPE = {
     "ads_elastic_plan_device_bytes": C.c_int64,
     "ads_elastic_plan_launches": C.c_int64,
     "ads_elastic_plan_resident_segments": C.c_int64,
+    "ads_elastic_plan_rows": C.c_int64,
     "ads_elastic_plan_source_offset": C.c_int64,
 }
 EXPORTED = sorted(_SIGS)

@@ -362,6 +362,8 @@ k_el_adj3(ElModel<T> M, ElShot<T> one) {
 constexpr int EC = 2;             // columns per lane
 constexpr int ESTRIP = 30 * EC;   // columns an adjoint strip updates
 constexpr int EW = 4;             // warps per CTA (independent strips)
+constexpr int kTuneMinRows = 6;   // smallest adjoint strip height the autotuner tries
+constexpr int kTuneMinRowsF = 12; // smallest fused-step tile height it tries
 // Which adjoint passes launch as two concurrent halves (measured: the first
 // gains occupancy from it; the gather-heavy second and third do better whole).
 constexpr bool kSplitAdj1 = true, kSplitAdj23 = false;
@@ -1628,6 +1630,7 @@ struct ElPlanBase {
   int64_t src_total = 0;
   int64_t trace_total = 0, bytes = 0, launches_fwd = 0, launches_grad = 0;
   int64_t resident = 0;  // checkpoint segments kept resident (no recompute)
+  int64_t tiling[2] = {0, 0};  // rows per adjoint strip, rows per fused-step tile
 };
 
 namespace {
@@ -1660,6 +1663,12 @@ struct ElPlan final : ElPlanBase {
   int ncolf = 0, rows_f = 0, nwtf = 0, jsh = 0, ish = 0;
   int nwk[4] = {}, owk[4] = {};  // items of each kind (k_el_step_rows KIND) and their offsets
   int* d_wlf = nullptr;
+  // host copies: the packed CPML rows and the item lists of the current tiling
+  std::vector<T> hprof;
+  std::vector<int> wl_host, wlf_host;
+  void build_lists(int rw, int rf);  // items for rows_w = rw, rows_f = rf
+  int upload_lists(cudaStream_t st);
+  int autotune(cudaStream_t st, int rw_min, int rf_min);
   static int par(int n) { return n & 1; }
   cudaStream_t side[3] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[3] = {};
@@ -1822,10 +1831,15 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
                                                      8, div_up(workf, (int64_t)sms * 20))));
   }
   nwt = ncolw * (int)div_up(NX, rows_w);
+  // the autotuner tries rows down to kTuneMinRows (adjoint) and
+  // kTuneMinRowsF (fused step): the lists get room for those
+  const int rw_min = c.autotune ? std::min(rows_w, kTuneMinRows) : rows_w;
+  const int rf_min = c.autotune ? std::min(rows_f, kTuneMinRowsF) : rows_f;
+  const int nwt_max = ncolw * (int)div_up(NX, rw_min);
   // upper bound of the fused items for any shift (the shifts are chosen once
   // the CPML profiles are known)
   const int nwtf_max =
-      (int)(div_up(NY + FSTRIP - 2, FSTRIP) * div_up(NX + rows_f - 1, rows_f));
+      (int)(div_up(NY + FSTRIP - 2, FSTRIP) * div_up(NX + rf_min - 1, rf_min));
   trace_off.resize(ns);
   trace_total = 0;
   for (int s = 0; s < ns; s++) {
@@ -1879,7 +1893,7 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   const size_t part_o = take(sizeof(double) * kBlocks);
   const size_t gsrc_o = take(sizeof(double) * (src_grad ? std::max<int64_t>(src_total, 1) : 1));
   const size_t shots_o = take(sizeof(ElShot<T>) * ns);
-  const size_t wl_o = take(sizeof(int) * std::max(nwt, 1));
+  const size_t wl_o = take(sizeof(int) * std::max(nwt_max, 1));
   const size_t wlf_o = take(sizeof(int) * std::max(nwtf_max, 1));
   // ---- the shots' stores: K slots for a segment's recompute, then one slot
   // per step of the resident segments (the last ones that fit in the allowed
@@ -1931,99 +1945,12 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   elastic_cpml(NX, NY, c.dx, c.dy, c.dt, c.npml, c.npower, c.k_max, c.alpha_max, c.vp_ref,
                c.Rcoef, c.use_pml, ax.data(), bx.data(), kx.data(), ay.data(), by.data(),
                ky.data());
-  std::vector<T> prof = pack_profiles<T>(NX, NY, ax.data(), bx.data(), ay.data(), by.data());
-  // warp items: a (strip, row tile) is interior when every cell it updates lies
-  // inside all four update boxes (2 <= i <= NX-1, 2 <= j <= NY-1) with no
-  // active CPML profile on its rows and columns (as the kernels see them)
-  std::vector<int> wl_host, wlf_host;
-  {
-    const T *axi = prof.data(), *axh = axi + NX, *bxi = axi + 2 * NX, *bxh = axi + 3 * NX;
-    const T *ayi = axi + 4 * NX, *ayh = ayi + NY, *byi = ayi + 2 * NY, *byh = ayi + 3 * NY;
-    std::vector<char> row_ok(NX + 2, 0), col_ok(NY + 2, 0);
-    for (int i = 2; i <= NX - 1; i++)
-      row_ok[i] = axh[i - 1] == T(0) && bxh[i - 1] == T(1) && axi[i - 1] == T(0) &&
-                  bxi[i - 1] == T(1);
-    for (int jc = 2; jc <= NY - 1; jc++)
-      col_ok[jc] = ayi[jc - 1] == T(0) && byi[jc - 1] == T(1) && ayh[jc - 1] == T(0) &&
-                   byh[jc - 1] == T(1);
-    std::vector<int> wpm;
-    for (int wi = 0; wi < nwt; wi++) {
-      const int strip = wi % ncolw, rt = wi / ncolw;
-      const int i0 = 1 + rt * rows_w, i1 = std::min(i0 + rows_w, NX + 1);
-      bool ok = true;
-      for (int i = i0; i < i1 && ok; i++) ok = row_ok[i];
-      for (int jc = strip * ESTRIP + 1; jc <= strip * ESTRIP + ESTRIP && ok; jc++)
-        ok = jc <= NY - 1 && col_ok[jc];
-      (ok ? wl_host : wpm).push_back(wi);
-    }
-    nw_in = (int)wl_host.size();
-    nw_pm = (int)wpm.size();
-    wl_host.insert(wl_host.end(), wpm.begin(), wpm.end());
-    // fused-step items by kind: bit 0 when a row whose stresses the warp
-    // computes (i0-2 .. i_end+1) lies on a box edge or in the x-CPML, bit 1
-    // when a column of lanes 1..30 (a-2 .. a+FSTRIP+1 for a strip owning
-    // columns from a) lies on a box edge or in the y-CPML
-    auto tile_ok = [&](int rt, int sh_) {
-      const int i0r = 1 + sh_ + rt * rows_f;
-      const int i0 = std::max(i0r, 1), i1 = std::min(i0r + rows_f, NX + 1);
-      for (int i = i0 - 2; i <= i1 + 1; i++)
-        if (i < 0 || i > NX + 1 || !row_ok[i]) return false;
-      return true;
-    };
-    auto strip_ok = [&](int strip, int sh_) {
-      const int a = 1 + sh_ + strip * FSTRIP;
-      for (int jc = a - 2; jc <= a + FSTRIP + 1; jc++)
-        if (jc < 0 || jc > NY + 1 || !col_ok[jc]) return false;
-      return true;
-    };
-    // shifts of the strip and tile origins with the most CPML-free strips
-    // and tiles (then the fewest strips and tiles)
-    {
-      int best = -1, bestn = 0;
-      for (int sh_ = 0; sh_ > -FSTRIP; sh_ -= 2) {
-        const int n = (int)div_up(NY - sh_, FSTRIP);
-        int ok = 0;
-        for (int k = 0; k < n; k++) ok += strip_ok(k, sh_);
-        if (ok > best || (ok == best && n < bestn)) {
-          best = ok;
-          bestn = n;
-          jsh = sh_;
-        }
-      }
-      ncolf = bestn;
-      best = -1;
-      int bestt = 0;
-      for (int sh_ = 0; sh_ > -rows_f; sh_--) {
-        const int n = (int)div_up(NX - sh_, rows_f);
-        int ok = 0;
-        for (int k = 0; k < n; k++) ok += tile_ok(k, sh_);
-        if (ok > best || (ok == best && n < bestt)) {
-          best = ok;
-          bestt = n;
-          ish = sh_;
-        }
-      }
-      nwtf = ncolf * bestt;
-    }
-    std::vector<int> wk[4];
-    for (int wi = 0; wi < nwtf; wi++) {
-      const int strip = wi % ncolf, rt = wi / ncolf;
-      wk[(tile_ok(rt, ish) ? 0 : 1) | (strip_ok(strip, jsh) ? 0 : 2)].push_back(wi);
-    }
-    wlf_host.clear();
-    for (int k = 0; k < 4; k++) {
-      owk[k] = (int)wlf_host.size();
-      nwk[k] = (int)wk[k].size();
-      wlf_host.insert(wlf_host.end(), wk[k].begin(), wk[k].end());
-    }
-  }
+  hprof = pack_profiles<T>(NX, NY, ax.data(), bx.data(), ay.data(), by.data());
+  const std::vector<T>& prof = hprof;
+  build_lists(rows_w, rows_f);
   d_wl = (int*)(pool + wl_o);
-  ADS_CUDA(cudaMemcpyAsync(d_wl, wl_host.data(), sizeof(int) * wl_host.size(),
-                           cudaMemcpyHostToDevice, st));
   d_wlf = (int*)(pool + wlf_o);
-  if (!wlf_host.empty())
-    ADS_CUDA(cudaMemcpyAsync(d_wlf, wlf_host.data(), sizeof(int) * wlf_host.size(),
-                             cudaMemcpyHostToDevice, st));
+  if (int e = upload_lists(st)) return e;
   for (auto& q : side) ADS_CUDA(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
   ADS_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
   for (auto& e : ev_join) ADS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -2144,6 +2071,10 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   ADS_CUDA(cudaMemcpyAsync(d_shots, hs.data(), sizeof(ElShot<T>) * ns, cudaMemcpyHostToDevice,
                            st));
   ADS_CUDA(cudaStreamSynchronize(st));
+  if (c.autotune && c.rows_per_warp <= 0)
+    if (int e = autotune(st, rw_min, rf_min)) return e;
+  tiling[0] = rows_w;
+  tiling[1] = rows_f;
   {
     int64_t n = 0;
     issue_forward(nullptr, &n);
@@ -2174,6 +2105,159 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
     }
   }
   return ADS_OK;
+}
+
+// Warp items of the tiling rows_w = rw (adjoint passes) and rows_f = rf (the
+// fused step), from the packed CPML rows hprof.
+template <typename T>
+void ElPlan<T>::build_lists(int rw, int rf) {
+  rows_w = rw;
+  rows_f = rf;
+  nwt = ncolw * (int)div_up(NX, rows_w);
+  wl_host.clear();
+  wlf_host.clear();
+  // warp items: a (strip, row tile) is interior when every cell it updates lies
+  // inside all four update boxes (2 <= i <= NX-1, 2 <= j <= NY-1) with no
+  // active CPML profile on its rows and columns (as the kernels see them)
+  const T *axi = hprof.data(), *axh = axi + NX, *bxi = axi + 2 * NX, *bxh = axi + 3 * NX;
+  const T *ayi = axi + 4 * NX, *ayh = ayi + NY, *byi = ayi + 2 * NY, *byh = ayi + 3 * NY;
+  std::vector<char> row_ok(NX + 2, 0), col_ok(NY + 2, 0);
+  for (int i = 2; i <= NX - 1; i++)
+    row_ok[i] = axh[i - 1] == T(0) && bxh[i - 1] == T(1) && axi[i - 1] == T(0) &&
+                bxi[i - 1] == T(1);
+  for (int jc = 2; jc <= NY - 1; jc++)
+    col_ok[jc] = ayi[jc - 1] == T(0) && byi[jc - 1] == T(1) && ayh[jc - 1] == T(0) &&
+                 byh[jc - 1] == T(1);
+  std::vector<int> wpm;
+  for (int wi = 0; wi < nwt; wi++) {
+    const int strip = wi % ncolw, rt = wi / ncolw;
+    const int i0 = 1 + rt * rows_w, i1 = std::min(i0 + rows_w, NX + 1);
+    bool ok = true;
+    for (int i = i0; i < i1 && ok; i++) ok = row_ok[i];
+    for (int jc = strip * ESTRIP + 1; jc <= strip * ESTRIP + ESTRIP && ok; jc++)
+      ok = jc <= NY - 1 && col_ok[jc];
+    (ok ? wl_host : wpm).push_back(wi);
+  }
+  nw_in = (int)wl_host.size();
+  nw_pm = (int)wpm.size();
+  wl_host.insert(wl_host.end(), wpm.begin(), wpm.end());
+  // fused-step items by kind: bit 0 when a row whose stresses the warp
+  // computes (i0-2 .. i_end+1) lies on a box edge or in the x-CPML, bit 1
+  // when a column of lanes 1..30 (a-2 .. a+FSTRIP+1 for a strip owning
+  // columns from a) lies on a box edge or in the y-CPML
+  auto tile_ok = [&](int rt, int sh_) {
+    const int i0r = 1 + sh_ + rt * rows_f;
+    const int i0 = std::max(i0r, 1), i1 = std::min(i0r + rows_f, NX + 1);
+    for (int i = i0 - 2; i <= i1 + 1; i++)
+      if (i < 0 || i > NX + 1 || !row_ok[i]) return false;
+    return true;
+  };
+  auto strip_ok = [&](int strip, int sh_) {
+    const int a = 1 + sh_ + strip * FSTRIP;
+    for (int jc = a - 2; jc <= a + FSTRIP + 1; jc++)
+      if (jc < 0 || jc > NY + 1 || !col_ok[jc]) return false;
+    return true;
+  };
+  // shifts of the strip and tile origins with the most CPML-free strips and
+  // tiles (then the fewest strips and tiles)
+  int best = -1, bestn = 0;
+  for (int sh_ = 0; sh_ > -FSTRIP; sh_ -= 2) {
+    const int n = (int)div_up(NY - sh_, FSTRIP);
+    int ok = 0;
+    for (int k = 0; k < n; k++) ok += strip_ok(k, sh_);
+    if (ok > best || (ok == best && n < bestn)) {
+      best = ok;
+      bestn = n;
+      jsh = sh_;
+    }
+  }
+  ncolf = bestn;
+  best = -1;
+  int bestt = 0;
+  for (int sh_ = 0; sh_ > -rows_f; sh_--) {
+    const int n = (int)div_up(NX - sh_, rows_f);
+    int ok = 0;
+    for (int k = 0; k < n; k++) ok += tile_ok(k, sh_);
+    if (ok > best || (ok == best && n < bestt)) {
+      best = ok;
+      bestt = n;
+      ish = sh_;
+    }
+  }
+  nwtf = ncolf * bestt;
+  std::vector<int> wk[4];
+  for (int wi = 0; wi < nwtf; wi++) {
+    const int strip = wi % ncolf, rt = wi / ncolf;
+    wk[(tile_ok(rt, ish) ? 0 : 1) | (strip_ok(strip, jsh) ? 0 : 2)].push_back(wi);
+  }
+  for (int k = 0; k < 4; k++) {
+    owk[k] = (int)wlf_host.size();
+    nwk[k] = (int)wk[k].size();
+    wlf_host.insert(wlf_host.end(), wk[k].begin(), wk[k].end());
+  }
+}
+
+template <typename T>
+int ElPlan<T>::upload_lists(cudaStream_t st) {
+  ADS_CUDA(cudaMemcpyAsync(d_wl, wl_host.data(), sizeof(int) * wl_host.size(),
+                           cudaMemcpyHostToDevice, st));
+  if (!wlf_host.empty())
+    ADS_CUDA(cudaMemcpyAsync(d_wlf, wlf_host.data(), sizeof(int) * wlf_host.size(),
+                             cudaMemcpyHostToDevice, st));
+  ADS_CUDA(cudaStreamSynchronize(st));  // the host lists change between trials
+  return ADS_OK;
+}
+
+// Autotuner: time the fused step for candidate tile heights rows_f, then the
+// three adjoint passes for candidate strip heights rows_w, on the plan's own
+// buffers (CUDA events on `st`), and keep the fastest of each.  The state the
+// trials touch is reset by every forward / gradient call.
+template <typename T>
+int ElPlan<T>::autotune(cudaStream_t st, int rw_min, int rf_min) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  ADS_CUDA(cudaEventCreate(&e0));
+  ADS_CUDA(cudaEventCreate(&e1));
+  auto timed = [&](bool adj, float& ms) -> int {
+    for (int pass = 0; pass < 2; pass++) {  // pass 0 warms up
+      ADS_CUDA(cudaEventRecord(e0, st));
+      for (int n = 1; n <= 6; n++)
+        if (int e = adj ? adjoint_step(st, 0) : step(st, n, false, 0, false)) return e;
+      ADS_CUDA(cudaEventRecord(e1, st));
+      ADS_CUDA(cudaEventSynchronize(e1));
+      ADS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    }
+    return ADS_OK;
+  };
+  int rc = ADS_OK;
+  int best_f = rows_f, best_w = rows_w;
+  float best = 1e30f;
+  for (int rf : {12, 16, 20, 24, 32}) {
+    if (rf < rf_min || rf > NX) continue;
+    build_lists(best_w, rf);
+    float ms = 0.f;
+    if ((rc = upload_lists(st)) || (rc = timed(false, ms))) break;
+    if (ms < best) {
+      best = ms;
+      best_f = rf;
+    }
+  }
+  best = 1e30f;
+  for (int rw : {6, 8, 12, 16, 24, 32}) {
+    if (rc != ADS_OK) break;
+    if (rw < rw_min || rw > NX) continue;
+    build_lists(rw, best_f);
+    float ms = 0.f;
+    if ((rc = upload_lists(st)) || (rc = timed(true, ms))) break;
+    if (ms < best) {
+      best = ms;
+      best_w = rw;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != ADS_OK) return rc;
+  build_lists(best_w, best_f);
+  return upload_lists(st);
 }
 
 // One forward step n (slot n-1 -> slot n) for every shot.
@@ -2838,6 +2922,11 @@ int64_t ads_elastic_plan_device_bytes(const ads_elastic_plan* plan) {
 
 int64_t ads_elastic_plan_resident_segments(const ads_elastic_plan* plan) {
   return plan ? plan->impl->resident : -1;
+}
+
+int64_t ads_elastic_plan_rows(const ads_elastic_plan* plan, int which) {
+  if (!plan || which < 0 || which > 1) return -1;
+  return plan->impl->tiling[which];
 }
 
 int64_t ads_elastic_plan_launches(const ads_elastic_plan* plan, int gradient) {

@@ -143,7 +143,8 @@ class ElasticPlan:
 
     def __init__(self, param: ElasticPropagatorParams, shots, precision="f64",
                  use_graph=True, ckpt_every=0, stream=None, rows_per_warp=0,
-                 resident_segments=0, resident_mem_pct=0, source_gradient=False):
+                 resident_segments=0, resident_mem_pct=0, source_gradient=False,
+                 autotune=False):
         cfg = _lib.ElasticConfig()
         cfg.NX, cfg.NY, cfg.NSTEP = param.NX, param.NY, param.NSTEP
         cfg.dx, cfg.dy, cfg.dt = param.DELTAX, param.DELTAY, param.DELTAT
@@ -157,6 +158,7 @@ class ElasticPlan:
         cfg.resident_segments = int(resident_segments)
         cfg.resident_mem_pct = int(resident_mem_pct)
         cfg.source_gradient = int(bool(source_gradient))
+        cfg.autotune = int(bool(autotune))
         self.param = param
         self.dtype = torch.float64 if precision == "f64" else torch.float32
         self._keep = []
@@ -187,6 +189,8 @@ class ElasticPlan:
         self.launches_forward = L.ads_elastic_plan_launches(h, 0)
         self.launches_gradient = L.ads_elastic_plan_launches(h, 1)
         self.resident_segments = L.ads_elastic_plan_resident_segments(h)
+        self.rows_per_warp = L.ads_elastic_plan_rows(h, 0)
+        self.rows_per_tile = L.ads_elastic_plan_rows(h, 1)
 
     def close(self):
         if getattr(self, "_h", None):

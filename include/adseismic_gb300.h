@@ -408,7 +408,10 @@ typedef struct ads_elastic_config {
                                 vx rows/columns 3..NX+1 / 3..NY+1 1-based, vy
                                 2..NX / 2..NY, sxx and syy 2..NX / 3..NY+1, sxy
                                 3..NX+1 / 2..NY are updated); 0: not */
-  int32_t reserved[5];
+  int32_t autotune;          /* 1: time candidate row heights of the fused step and of the
+                                adjoint passes at plan creation and keep the fastest
+                                (ignored when rows_per_warp is set) */
+  int32_t reserved[4];
 } ads_elastic_config;
 
 typedef struct ads_elastic_shot {
@@ -438,6 +441,10 @@ int64_t ads_elastic_plan_device_bytes(const ads_elastic_plan* plan);
 int64_t ads_elastic_plan_launches(const ads_elastic_plan* plan, int gradient);
 /* Checkpoint segments kept resident (see resident_segments); -1 for a null plan. */
 int64_t ads_elastic_plan_resident_segments(const ads_elastic_plan* plan);
+/* The plan's tiling (as configured or as the autotuner chose it): which = 0,
+ * rows per adjoint strip; 1, rows per fused-step tile; -1 for a null plan or
+ * another `which`.  No reference counterpart. */
+int64_t ads_elastic_plan_rows(const ads_elastic_plan* plan, int which);
 /* ads_elastic_plan_gradient plus the source-time gradient grad_srcv = d loss /
  * d srcv, the gradient AddSource's backward (AddSource.cpp:91-155) gathers:
  * device doubles, per shot an (NSTEP, nsrc) row-major block at

@@ -114,6 +114,24 @@ def test_plan_fp64_vs_oracle(ads, cuda, use_graph, ckpt, resident):
     plan.close()
 
 
+@pytest.mark.parametrize("precision,tol", [("f64", 1e-12), ("f32", 1e-4)])
+def test_autotuned_plan_vs_oracle(ads, cuda, precision, tol):
+    """The autotuner picks the fused-step tile and adjoint strip heights; the
+    results stay the oracle's."""
+    g = golden("elastic_small.npz")
+    p = params(ads, g)
+    plan = ads.ElasticPlan(p, shots_from(g), precision=precision, ckpt_every=17, autotune=True)
+    assert plan.rows_per_warp in (6, 8, 12, 16, 24) and plan.rows_per_tile in (12, 16, 20, 24)
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=cuda)
+    loss, gl, gm, gr = plan.gradient(t(g["lam"]), t(g["mu"]), t(g["rho"]),
+                                     t(g["obs"].reshape(-1)))
+    torch.cuda.synchronize()
+    assert abs(float(loss) - float(g["loss"])) <= tol * float(g["loss"])
+    for a, k in ((gl, "grad_lambda"), (gm, "grad_mu"), (gr, "grad_rho")):
+        assert rel(a.cpu().numpy(), g[k]) <= tol, k
+    plan.close()
+
+
 def test_plan_fp32_vs_fp64_oracle(ads, cuda):
     g = golden("elastic_small.npz")
     p = params(ads, g)
