@@ -366,7 +366,10 @@ constexpr int kTuneMinRows = 6;   // smallest adjoint strip height the autotuner
 constexpr int kTuneMinRowsF = 12; // smallest fused-step tile height it tries
 // Which adjoint passes launch as two concurrent halves (measured: the first
 // gains occupancy from it; the gather-heavy second and third do better whole).
-constexpr bool kSplitAdj1 = true, kSplitAdj23 = false;
+#ifndef ADS_EL_SPLIT_ADJ23
+#define ADS_EL_SPLIT_ADJ23 0
+#endif
+constexpr bool kSplitAdj1 = true, kSplitAdj23 = ADS_EL_SPLIT_ADJ23 != 0;
 #ifndef ADS_EL_MINB
 #define ADS_EL_MINB 6                 // resident CTAs per SM, first adjoint pass (CPML items)
 #endif

@@ -226,24 +226,23 @@ def _line(metric, value, unit, args, ms, dtype, workload, extra):
     print(json.dumps(out))
 
 
-def run_acoustic_fwd_f64(args):
-    """Plain FP64 acoustic forward: 200x200 interior plus a 20-cell PML, h = 10 m,
+def measure_c1(steps, warmup, with_cpu=True):
+    """Plain FP64 acoustic forward (C1): 200x200 interior plus a 20-cell PML, h = 10 m,
     dt = 1 ms, 1000 steps, one 10 Hz Ricker source 20 cells below the PML, 200
-    receivers 5 cells below it (the reference CPU operators' own configuration)."""
+    receivers 5 cells below it (the reference CPU operators' own configuration).
+    Returns the measured figures (value in Gcell-updates/s)."""
     import torch
     import __graft_entry__ as g
-    import oracle
 
     ads = g.load_package()
     from adseismic_gb300 import configs
 
     cfg, shot, vp = configs.c1_forward()
     NX, NY, npml, T, h, dt = cfg["MX"], cfg["MY"], cfg["npml"], cfg["nstep"], cfg["h"], cfg["dt"]
-    wav = shot["srcv"]
-    plan = ads.AcousticPlan(NX, NY, h, h, dt, [shot], npml=npml, vp_ref=float(vp.mean()),
+    plan = ads.AcousticPlan(NX, NY, h, h, dt, [shot], npml=npml, vp_ref=cfg["vp_ref"],
                             precision="f64")
     vdev = torch.tensor(vp, device="cuda")
-    ms = _timed(lambda: plan.forward(vdev), args.steps, args.warmup)
+    ms = _timed(lambda: plan.forward(vdev), steps, warmup)
     cells = NX * NY * (T - 1)
     vh = torch.tensor(vp).pin_memory()
     th = torch.empty(plan.trace_count, dtype=torch.float64).pin_memory()
@@ -252,28 +251,42 @@ def run_acoustic_fwd_f64(args):
         vdev.copy_(vh, non_blocking=True)
         th.copy_(plan.forward(vdev), non_blocking=True)
 
-    ms_e2e = _timed(e2e, args.steps, 1)
-    oracle.build(ref=False)
-    sx, ty = oracle.acoustic_pml(NX, NY, h, h, npml, float(vp.mean()))
-    t0 = time.perf_counter()
-    oracle.acoustic_forward(NX, NY, T, dt, h, h, sx, ty, vp.reshape(-1), shot["srci"],
-                            shot["srcj"], wav, shot["rcvi"], shot["rcvj"],
-                            use_ref=oracle.ref_available())
-    t_cpu = time.perf_counter() - t0
-    _line("acoustic forward Gcell-updates/s, plain FP64 drop-in", cells / (ms / 1e3) / 1e9,
-          "Gcell-updates/s", args, ms, "f64",
-          "acoustic forward 240x240 (200x200 + PML 20), 1000 steps, 1 shot, 200 receivers",
-          {"e2e": {"value": cells / (ms_e2e / 1e3) / 1e9, "unit": "Gcell-updates/s",
-                   "h2d_bytes_per_step": vp.size * 8, "d2h_bytes_per_step": plan.trace_count * 8},
-           "cpu_baseline": {"value": cells / t_cpu / 1e9, "unit": "Gcell-updates/s", "cores": 1,
-                            "kind": "reference" if oracle.ref_available() else "port",
-                            "sample": "the full forward, one core"},
-           "gpu_launches": int(plan.launches_forward)})
+    ms_e2e = _timed(e2e, steps, 1)
+    out = {"value": cells / (ms / 1e3) / 1e9, "unit": "Gcell-updates/s", "ms_per_step": ms,
+           "dtype": "f64",
+           "workload": "acoustic forward 240x240 (200x200 + PML 20), 1000 steps, 1 shot, "
+                       "200 receivers",
+           "e2e": {"value": cells / (ms_e2e / 1e3) / 1e9, "unit": "Gcell-updates/s",
+                   "h2d_bytes_per_step": vp.size * 8,
+                   "d2h_bytes_per_step": plan.trace_count * 8},
+           "gpu_launches": int(plan.launches_forward)}
     plan.close()
+    if with_cpu:
+        import oracle
+
+        oracle.build(ref=False)
+        sx, ty = oracle.acoustic_pml(NX, NY, h, h, npml, cfg["vp_ref"])
+        t0 = time.perf_counter()
+        oracle.acoustic_forward(NX, NY, T, dt, h, h, sx, ty, vp.reshape(-1), shot["srci"],
+                                shot["srcj"], shot["srcv"], shot["rcvi"], shot["rcvj"],
+                                use_ref=oracle.ref_available())
+        t_cpu = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": cells / t_cpu / 1e9, "unit": "Gcell-updates/s",
+                               "cores": 1,
+                               "kind": "reference" if oracle.ref_available() else "port",
+                               "sample": "the full forward, one core"}
+    return out
 
 
-def run_fwi_f64(args):
-    """Plain FP64 acoustic FWI gradient: 400x400 incl. PML 30, 2000 steps, 8 shots
+def run_acoustic_fwd_f64(args):
+    r = measure_c1(args.steps, args.warmup)
+    _line("acoustic forward Gcell-updates/s, plain FP64 drop-in", r["value"], r["unit"], args,
+          r["ms_per_step"], "f64", r["workload"],
+          {k: r[k] for k in ("e2e", "cpu_baseline", "gpu_launches")})
+
+
+def measure_c2(steps, warmup):
+    """Plain FP64 acoustic FWI gradient (C2): 400x400 incl. PML 30, 2000 steps, 8 shots
     20 cells below the PML at the centres of 8 equal segments, one receiver per
     interior column 5 cells below the PML, observed data from the true model,
     gradient at a Gaussian-smoothed (20 cells) start model."""
@@ -284,18 +297,25 @@ def run_fwi_f64(args):
     from adseismic_gb300 import configs
 
     cfg, shots, vt, v0 = configs.c2_fwi()
-    NX, NY, npml, T, h, dt = cfg["MX"], cfg["MY"], cfg["npml"], cfg["nstep"], cfg["h"], cfg["dt"]
-    plan = ads.AcousticPlan(NX, NY, h, h, dt, shots, npml=npml, vp_ref=float(vt.mean()),
-                            precision="f64")
+    NX, NY, T = cfg["MX"], cfg["MY"], cfg["nstep"]
+    plan = configs.acoustic_plan(ads, cfg, shots, "f64")
     obs = plan.forward(torch.tensor(vt, device="cuda")).clone()
     vdev = torch.tensor(v0, device="cuda")
-    ms = _timed(lambda: plan.gradient(vdev, obs), args.steps, args.warmup)
-    cells = 2 * 8 * NX * NY * (T - 1)
-    _line("FWI shot-gradients/s, plain FP64 drop-in", 8 / (ms / 1e3), "shot-gradients/s", args,
-          ms, "f64", "acoustic FWI gradient 400x400 (PML 30), 2000 steps, 8 shots",
-          {"gcell_updates_per_s": cells / (ms / 1e3) / 1e9,
-           "gpu_launches": int(plan.launches_gradient)})
+    ms = _timed(lambda: plan.gradient(vdev, obs), steps, warmup)
+    cells = 2 * len(shots) * NX * NY * (T - 1)
+    out = {"value": len(shots) / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "dtype": "f64",
+           "workload": "acoustic FWI gradient 400x400 (PML 30), 2000 steps, 8 shots",
+           "gcell_updates_per_s": cells / (ms / 1e3) / 1e9,
+           "gpu_launches": int(plan.launches_gradient)}
     plan.close()
+    return out
+
+
+def run_fwi_f64(args):
+    r = measure_c2(args.steps, args.warmup)
+    _line("FWI shot-gradients/s, plain FP64 drop-in", r["value"], r["unit"], args,
+          r["ms_per_step"], "f64", r["workload"],
+          {k: r[k] for k in ("gcell_updates_per_s", "gpu_launches")})
 
 
 def elastic_workload(ads, nshots=32, T=4000):
@@ -304,7 +324,7 @@ def elastic_workload(ads, nshots=32, T=4000):
     return configs.c4_elastic(nshots=nshots, T=T)
 
 
-def elastic_measure(steps, warmup, nshots=32, T=4000, with_rel_err=True):
+def elastic_measure(steps, warmup, nshots=32, T=4000, with_rel_err=True, autotune=True):
     """Elastic CPML FWI gradient w.r.t. lambda, mu, rho (C4): 600x300 incl. CPML
     30, T steps, FP32 stencils with FP64 accumulation, explosive shots (sigma_xx
     and sigma_yy, 10 Hz Ricker), 300 two-component receivers.  Returns the
@@ -319,7 +339,8 @@ def elastic_measure(steps, warmup, nshots=32, T=4000, with_rel_err=True):
     t = lambda a: torch.tensor(a.reshape(-1), device="cuda")
     # the last checkpoint segments' adjoint inputs stay resident in HBM (up to
     # 92% of the memory free after the plan's other buffers)
-    plan = ads.ElasticPlan(p, shots, precision="f32", ckpt_every=100, resident_mem_pct=92)
+    plan = ads.ElasticPlan(p, shots, precision="f32", ckpt_every=100, resident_mem_pct=92,
+                           autotune=autotune)
     obs = plan.forward(t(lam), t(mu), t(rho)).clone()
     l0, m0, r0 = (t(a) for a in configs.c4_start_model(lam, mu, rho))
     ms = _timed(lambda: plan.gradient(l0, m0, r0, obs), steps, warmup)
@@ -357,7 +378,9 @@ def elastic_measure(steps, warmup, nshots=32, T=4000, with_rel_err=True):
                        f"checkpoints every 100, the last {plan.resident_segments} of "
                        f"{-(-p.NSTEP // 100)} segments resident in HBM",
            "gcell_updates_per_s": cells / (ms / 1e3) / 1e9, "roofline": roofline,
-           "device_bytes": plan.device_bytes, "gpu_launches": int(plan.launches_gradient)}
+           "device_bytes": plan.device_bytes, "gpu_launches": int(plan.launches_gradient),
+           "tiling": {"rows_per_adjoint_strip": plan.rows_per_warp,
+                      "rows_per_fused_tile": plan.rows_per_tile, "autotuned": bool(autotune)}}
     plan.close()
     if with_rel_err:
         out["rel_err"] = elastic_rel_err(ads, p, [shots[3], shots[n // 2 + 4]], lam, mu, rho,
@@ -436,39 +459,46 @@ def run_elastic_fwi(args):
     """The elastic C4 gradient as its own bench line."""
     nshots = args.shots if args.shots != 64 else 32
     T = args.nstep if args.nstep != 3000 else 4000
-    r = elastic_measure(args.steps, args.warmup, nshots=nshots, T=T)
+    r = elastic_measure(args.steps, args.warmup, nshots=nshots, T=T,
+                        autotune=not args.no_elastic_autotune)
     _line("elastic FWI shot-gradients/s (FP32 stencils, FP64 accumulation)", r["value"],
           "shot-gradients/s", args, r["ms_per_step"], "f32", r["workload"],
           {k: r[k] for k in ("gcell_updates_per_s", "roofline", "device_bytes", "gpu_launches",
-                             "rel_err")})
+                             "rel_err", "tiling")})
 
 
-def run_fwi_uneven(args):
-    """Uneven batched acoustic FWI gradient: 4000 x 2000 model, 128 shots, each with
-    its own window of 400-1200 columns (PML 40 inside), 200-1200 receivers and
-    2000-6000 steps drawn from the seed; FP32 stencils, FP64 accumulation."""
+def measure_c5(steps, warmup, nshots=128):
+    """Uneven batched acoustic FWI gradient (C5): 4000 x 2000 model, 128 shots, each
+    with its own window of 400-1200 columns (PML 40 inside), 200-1200 receivers
+    and 2000-6000 steps drawn from the seed; FP32 stencils, FP64 accumulation."""
     import torch
     import __graft_entry__ as g
 
     ads = g.load_package()
     from adseismic_gb300 import configs
 
-    cfg, shots, vt, v0 = configs.c5_uneven(nshots=args.shots if args.shots != 64 else 128)
-    MX, MY, npml, h, dt = cfg["MX"], cfg["MY"], cfg["npml"], cfg["h"], cfg["dt"]
-    nshots = len(shots)
-    plan = ads.AcousticPlan(MX, MY, h, h, dt, shots, npml=npml, vp_ref=float(vt.mean()),
-                            precision="f32", ckpt_every=100)
+    cfg, shots, vt, v0 = configs.c5_uneven(nshots=nshots)
+    MY = cfg["MY"]
+    plan = configs.acoustic_plan(ads, cfg, shots, "f32", ckpt_every=100)
     obs = plan.forward(torch.tensor(vt, device="cuda")).clone()
     vdev = torch.tensor(v0, device="cuda")
-    ms = _timed(lambda: plan.gradient(vdev, obs), args.steps, args.warmup)
+    ms = _timed(lambda: plan.gradient(vdev, obs), steps, warmup)
     cells = 2 * sum(s["nx"] * MY * (s["nstep"] - 1) for s in shots)
-    _line("FWI shot-gradients/s & Gcell-updates/s, FP32-batched uneven shots",
-          nshots / (ms / 1e3), "shot-gradients/s", args, ms, "f32",
-          "uneven acoustic FWI gradient on a 4000x2000 model, 128 shots, windows 400-1200, "
-          "200-1200 receivers, 2000-6000 steps, PML 40 per window",
-          {"gcell_updates_per_s": cells / (ms / 1e3) / 1e9, "device_bytes": plan.device_bytes,
-           "gpu_launches": int(plan.launches_gradient)})
+    out = {"value": len(shots) / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "dtype": "f32",
+           "workload": f"uneven acoustic FWI gradient on a 4000x2000 model, {len(shots)} shots, "
+                       "windows 400-1200, 200-1200 receivers, 2000-6000 steps, PML 40 per window",
+           "gcell_updates_per_s": cells / (ms / 1e3) / 1e9, "device_bytes": plan.device_bytes,
+           "resident_segments": plan.resident_segments,
+           "gpu_launches": int(plan.launches_gradient)}
     plan.close()
+    return out
+
+
+def run_fwi_uneven(args):
+    r = measure_c5(args.steps, args.warmup, nshots=args.shots if args.shots != 64 else 128)
+    _line("FWI shot-gradients/s & Gcell-updates/s, FP32-batched uneven shots", r["value"],
+          r["unit"], args, r["ms_per_step"], "f32", r["workload"],
+          {k: r[k] for k in ("gcell_updates_per_s", "device_bytes", "gpu_launches")})
 
 
 def main():
@@ -485,6 +515,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-elastic", action="store_true")
+    ap.add_argument("--no-elastic-autotune", action="store_true")
+    ap.add_argument("--no-configs", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -680,6 +712,16 @@ def main():
         elastic = elastic_measure(min(args.steps, 3), min(max(args.warmup, 1), 3))
         torch.cuda.empty_cache()
 
+    # the other configurations, briefly, in the same run
+    other = None
+    if not args.no_configs and rank == 0:
+        other = {"C1": measure_c1(min(args.steps, 5), min(max(args.warmup, 1), 3),
+                                  with_cpu=not args.no_cpu),
+                 "C2": measure_c2(min(args.steps, 3), min(max(args.warmup, 1), 2))}
+        torch.cuda.empty_cache()
+        other["C5"] = measure_c5(min(args.steps, 2), 1)
+        torch.cuda.empty_cache()
+
     cpu = None
     if not args.no_cpu and rank == 0:
         v, t = cpu_baseline(cfg, shots, vp0, nstep, cores=1, steps=100)
@@ -708,6 +750,7 @@ def main():
             "rel_err": rel_err,
             "fp64_plain": fp64,
             "elastic": elastic,
+            "configs": other,
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
             "loss": float(loss),
