@@ -63,7 +63,8 @@ class ElasticConfig(C.Structure):
         ("use_pml", C.c_int32), ("precision", C.c_int32), ("use_graph", C.c_int32),
         ("rows_per_warp", C.c_int32), ("ckpt_every", C.c_int64),
         ("resident_segments", C.c_int32), ("resident_mem_pct", C.c_int32),
-        ("source_gradient", C.c_int32), ("autotune", C.c_int32), ("reserved", C.c_int32 * 4),
+        ("source_gradient", C.c_int32), ("autotune", C.c_int32),
+        ("adjoint_passes", C.c_int32), ("reserved", C.c_int32 * 3),
     ]
 
 

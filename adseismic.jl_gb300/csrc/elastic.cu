@@ -1312,6 +1312,393 @@ k_el_adj3_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
   }
 }
 
+// ---------------------------------------------------------------------------
+// Fused adjoint step for the plans: the three gather passes above in one
+// row-streaming pass over the fused forward step's strips and row tiles.
+//
+// The adjoint state alternates between two buffers like the forward state:
+// the adjoint step of step n reads the adjoint of slot n from buffer pin and
+// writes that of slot n-1 into buffer 1-pin.  So a warp can recompute the
+// halo values its gathers need from the old adjoint state while the
+// neighbouring strips and row tiles write their own cells.
+//
+// Per iteration a warp runs
+//   phase A on row a (lanes 0..31): the transposes of fw3 and fw4 at the
+//     velocity cells (D5..D8, R4 of the three-pass form, and the first rho
+//     term), and the memory adjoints g5..g8;
+//   phase B on row a-2 (needed on lanes 1..30): the stress adjoints, gathered
+//     from D5..D8 of rows a-4..a, and the transposes of fw1 and fw2 (D1..D4,
+//     the lambda / mu terms, g1..g4);
+//   phase C on row a-4 (lanes 2..29 own): the velocity adjoints, gathered from
+//     D1..D4 of rows a-6..a-2.
+// D1..D8 live in register windows instead of device memory.  A tile owns R
+// rows: phase A runs on R + 8 rows, phase B on R + 4, phase C on R.  The rho
+// accumulator is updated in phase A (its fw4 term needs R4 of rows a-1, a)
+// and the lambda / mu accumulators in phase B (their terms need rows b-1, b),
+// on the cells the warp owns, in the order the three-pass form adds them;
+// values, masks and arithmetic are those of k_el_adj1_rows .. k_el_adj3_rows.
+// ---------------------------------------------------------------------------
+#ifndef ADS_EL_MINB_AI
+#define ADS_EL_MINB_AI 3              // resident CTAs per SM, fused adjoint of CPML-free items
+#endif
+#ifndef ADS_EL_MINB_AC
+#define ADS_EL_MINB_AC 3              // the same for items with CPML or box-edge logic
+#endif
+template <typename T, int KIND>
+constexpr int el_minb_fadj() {
+  return sizeof(T) != 4 ? 1 : KIND == 0 ? ADS_EL_MINB_AI : ADS_EL_MINB_AC;
+}
+
+template <typename T, int KIND>
+__global__ void __launch_bounds__(EW * 32, el_minb_fadj<T, KIND>())
+k_el_adj_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __restrict__ wlist,
+              int ncolw, int R, int nwt, int store_slot, int pin, int jsh, int ish) {
+  // KIND bit 0: rows need the box edge and x-profile logic; bit 1: columns
+  // need the box edge and y-profile logic (0: neither)
+  constexpr bool GR = (KIND & 1) != 0, GC = (KIND & 2) != 0;
+  const int wl = blockIdx.x * EW + (threadIdx.x >> 5);
+  if (wl >= nwt) return;
+  const int wi = wlist[wl];  // the warp's (strip, row tile)
+  const ElShot<T>& sh = shots[blockIdx.y];
+  const int lane = threadIdx.x & 31, NX = M.NX, NY = M.NY;
+  const int strip = wi % ncolw, rt = wi / ncolw;
+  const int j = strip * FSTRIP - 3 + lane * EC + jsh;  // odd: 8/16-byte aligned pairs
+  const bool own = lane >= 2 && lane <= 29;
+  const bool colok = j >= -1 && j <= NY + 1;
+  const int i0r = 1 + ish + rt * R;
+  const int i0 = max(i0r, 1), i_end = min(i0r + R, NX + 1);
+  const int64_t fs = sh.fs, P = M.P;
+  const int64_t bin = (int64_t)pin * NF * fs, bout = (int64_t)(1 - pin) * NF * fs;
+  const T* __restrict__ gvx = sh.g[VX] + bin;
+  const T* __restrict__ gvy = sh.g[VY] + bin;
+  const T* __restrict__ gxx = sh.g[SXX] + bin;
+  const T* __restrict__ gyy = sh.g[SYY] + bin;
+  const T* __restrict__ gxy = sh.g[SXY] + bin;
+  T* __restrict__ ovxp = sh.g[VX] + bout;
+  T* __restrict__ ovyp = sh.g[VY] + bout;
+  T* __restrict__ oxxp = sh.g[SXX] + bout;
+  T* __restrict__ oyyp = sh.g[SYY] + bout;
+  T* __restrict__ oxyp = sh.g[SXY] + bout;
+  const T* __restrict__ st = sh.store + (int64_t)store_slot * NSTORE * fs;
+  const T* __restrict__ e1p = st + E1 * fs;
+  const T* __restrict__ e2p = st + E2 * fs;
+  const T* __restrict__ e12p = st + E12 * fs;
+  const T* __restrict__ a3p = st + A3 * fs;
+  const T* __restrict__ a4p = st + A4 * fs;
+  using A = typename ElAcc<T>::type;
+  static_assert(std::is_same<A, T>::value, "the step's partials have the stencil type");
+  A* __restrict__ accl = ElAcc<T>::lam(sh);
+  A* __restrict__ accm = ElAcc<T>::mu(sh);
+  A* __restrict__ accr = ElAcc<T>::rho(sh);
+  // memory adjoints 1..8, input / output buffer
+  const T* __restrict__ g1i = sh.g[M1 + 0] + bin;
+  const T* __restrict__ g2i = sh.g[M1 + 1] + bin;
+  const T* __restrict__ g3i = sh.g[M1 + 2] + bin;
+  const T* __restrict__ g4i = sh.g[M1 + 3] + bin;
+  const T* __restrict__ g5i = sh.g[M1 + 4] + bin;
+  const T* __restrict__ g6i = sh.g[M1 + 5] + bin;
+  const T* __restrict__ g7i = sh.g[M1 + 6] + bin;
+  const T* __restrict__ g8i = sh.g[M1 + 7] + bin;
+  T* __restrict__ g1o = sh.g[M1 + 0] + bout;
+  T* __restrict__ g2o = sh.g[M1 + 1] + bout;
+  T* __restrict__ g3o = sh.g[M1 + 2] + bout;
+  T* __restrict__ g4o = sh.g[M1 + 3] + bout;
+  T* __restrict__ g5o = sh.g[M1 + 4] + bout;
+  T* __restrict__ g6o = sh.g[M1 + 5] + bout;
+  T* __restrict__ g7o = sh.g[M1 + 6] + bout;
+  T* __restrict__ g8o = sh.g[M1 + 7] + bout;
+  auto stw = [&](T* p, int64_t o, const T (&x)[2], bool k0, bool k1) {
+    if constexpr (GC) {
+      st2s<T>(p, o, x, k0, k1);
+    } else {
+      st2p(p, o, x, k0, k1);
+    }
+  };
+  auto off = [&](int r) { return (int64_t)r * P + j + JOFF; };
+  auto ld = [&](const T* p, int r) {
+    return ld2p(p, off(r), colok && r >= 0 && r <= NX + 1);
+  };
+  const ColProf<T> Y(M, j);
+  // columns of the vx / sxx / syy boxes (2..NY), the vy / sxy boxes (1..NY-1)
+  // and of the accumulators (1..NY)
+  bool c3[2], c4[2], cp[2];
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    const int jc = j + c;
+    c3[c] = !GC || (jc >= 2 && jc <= NY);
+    c4[c] = !GC || (jc >= 1 && jc <= NY - 1);
+    cp[c] = !GC || (jc >= 1 && jc <= NY);
+  }
+  const bool lc3 = c3[0] || c3[1], lc4 = c4[0] || c4[1];
+  const bool ly3 = GC && ((c3[0] && Y.acti[0]) || (c3[1] && Y.acti[1]));
+  const bool ly4 = GC && ((c4[0] && Y.acth[0]) || (c4[1] && Y.acth[1]));
+  // rows of the vx / sxy boxes (2..NX) and of the vy / sxx / syy boxes (1..NX-1)
+  auto rb3 = [&](int r) { return !GR || (r >= 2 && r <= NX); };
+  auto rb4 = [&](int r) { return !GR || (r >= 1 && r <= NX - 1); };
+  auto xp = [&](const T* p, int r, T dflt) { return GR ? p[min(max(r, 1), NX) - 1] : dflt; };
+  // windows: D5 rows a-3..a-1, D7 rows a-4..a-1, D6 / D8 rows a-2, a-1, R4 row
+  // a-1; D1 rows b-4..b-1, D3 rows b-3..b-1, D2 / D4 rows b-2, b-1, GL1 / GM1
+  // row b-1 (b = a - 2); rho rows a, a+1; lam / mu row b
+  V2<T> W5_0{}, W5_1{}, W5_2{}, W7_0{}, W7_1{}, W7_2{}, W7_3{}, W6_0{}, W6_1{}, W8_0{},
+      W8_1{}, R4p{};
+  V2<T> W1_0{}, W1_1{}, W1_2{}, W1_3{}, W3_0{}, W3_1{}, W3_2{}, W2_0{}, W2_1{}, W4_0{},
+      W4_1{}, GL1p{}, GM1p{};
+  V2<T> R0 = ld(M.rho, i0 - 4), R1 = ld(M.rho, i0 - 3);
+  V2<T> L0 = ld(M.lam, i0 - 6), U0 = ld(M.mu, i0 - 6);
+  for (int a = i0 - 4; a <= i_end + 3; a++) {
+    const int b = a - 2, t = a - 4;
+    const bool doB = b >= i0 - 2, doC = t >= i0;
+    const bool ownA = a >= i0 && a < i_end, ownB = b >= i0 && b < i_end;  // warp-uniform
+    // ---- every load of the iteration first (predicated), so that its three
+    // phases wait for memory once
+    const int64_t oa = off(a), ob = off(b), ot = off(t);
+    const bool okA = colok && a >= 0 && a <= NX + 1;
+    const bool okB = doB && colok && b >= 0 && b <= NX + 1;
+    const V2<T> GX = ld2p(gvx, oa, okA), GY = ld2p(gvy, oa, okA);
+    const V2<T> EA3 = ld2p(a3p, oa, okA), EA4 = ld2p(a4p, oa, okA);
+    const V2<T> R2 = ld(M.rho, a + 2);
+    const V2<A> AR = ld2p(accr, oa, ownA && own && colok);
+    const V2<T> GA = ld2p(gxx, ob, okB), GB = ld2p(gyy, ob, okB), GCv = ld2p(gxy, ob, okB);
+    const V2<T> EA = ld2p(e1p, ob, okB), EB = ld2p(e2p, ob, okB), EC12 = ld2p(e12p, ob, okB);
+    const V2<T> L1 = ld(M.lam, b + 1), U1 = ld(M.mu, b + 1);
+    const V2<A> AL = ld2p(accl, ob, doB && ownB && own && colok);
+    const V2<A> AM = ld2p(accm, ob, doB && ownB && own && colok);
+    const V2<T> VX0 = ld2p(gvx, ot, doC && colok), VY0 = ld2p(gvy, ot, doC && colok);
+    const T axi = xp(M.axi, a, T(0)), bxi = xp(M.bxi, a, T(1));
+    const T axh = xp(M.axh, a, T(0)), bxh = xp(M.bxh, a, T(1));
+    const T baxh = xp(M.axh, b, T(0)), bbxh = xp(M.bxh, b, T(1));
+    const T baxi = xp(M.axi, b, T(0)), bbxi = xp(M.bxi, b, T(1));
+    const bool r3 = rb3(a), r4 = rb4(a);
+    const bool rx5 = GR && r3 && (axi != T(0) || bxi != T(1));
+    const bool rx7 = GR && r4 && (axh != T(0) || bxh != T(1));
+    const bool r1b = doB && rb4(b), r2b = doB && rb3(b);
+    const bool rx1 = GR && r1b && (baxh != T(0) || bbxh != T(1));
+    const bool rx3 = GR && r2b && (baxi != T(0) || bbxi != T(1));
+    V2<T> m5{}, m6{}, m7{}, m8{}, m1{}, m2{}, m3{}, m4{};
+    if constexpr (GR) {
+      m5 = ld2p(g5i, oa, rx5 && lc3);
+      m7 = ld2p(g7i, oa, rx7 && lc4);
+      m1 = ld2p(g1i, ob, rx1 && lc3);
+      m3 = ld2p(g3i, ob, rx3 && lc4);
+    }
+    if constexpr (GC) {
+      m6 = ld2p(g6i, oa, r3 && ly3);
+      m8 = ld2p(g8i, oa, r4 && ly4);
+      m2 = ld2p(g2i, ob, r1b && ly3);
+      m4 = ld2p(g4i, ob, r2b && ly4);
+    }
+    // ================= phase A: row a
+    T r0[3], r1[3];
+    r0[0] = R0.v[0];
+    r0[1] = R0.v[1];
+    r0[2] = shdn(R0.v[0]);
+    r1[0] = R1.v[0];
+    r1[1] = R1.v[1];
+    r1[2] = shdn(R1.v[0]);
+    V2<T> D5n, D6n, D7n, D8n, R4n;
+    T sg5[2], sg6[2], sg7[2], sg8[2], grt[2];
+    bool k3[2], w5[2], w6[2], w7[2], w8[2];
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      k3[c] = r3 && c3[c];
+      const bool k4 = r4 && c4[c];
+      // fw3 transpose
+      const T gv = GX.v[c], r = r0[c];
+      const T q = divr<T>(gv * M.dt, r);
+      const bool u5 = k3[c] && rx5, u6 = GC && k3[c] && Y.acti[c];
+      const T gm5 = u5 ? q + m5.v[c] : q;
+      const T gm6 = u6 ? q + m6.v[c] : q;
+      sg5[c] = bxi * gm5;
+      sg6[c] = Y.bi[c] * gm6;
+      w5[c] = u5;
+      w6[c] = u6;
+      D5n.v[c] = k3[c] ? hdiv<T>(q + axi * gm5, M.hx24, M.rhx24) : T(0);
+      D6n.v[c] = k3[c] ? hdiv<T>(q + (GC ? Y.ai[c] : T(0)) * gm6, M.hy24, M.rhy24) : T(0);
+      grt[c] = divr<T>(-gv * EA3.v[c] * M.dt, r * r);
+      // fw4 transpose
+      const T gw = GY.v[c];
+      const T rho_ = T(0.25) * (r0[c] + r1[c] + r1[c + 1] + r0[c + 1]);
+      const T q4 = divr<T>(gw * M.dt, rho_);
+      const bool u7 = k4 && rx7, u8 = GC && k4 && Y.acth[c];
+      const T gm7 = u7 ? q4 + m7.v[c] : q4;
+      const T gm8 = u8 ? q4 + m8.v[c] : q4;
+      sg7[c] = bxh * gm7;
+      sg8[c] = Y.bh[c] * gm8;
+      w7[c] = u7;
+      w8[c] = u8;
+      D7n.v[c] = k4 ? hdiv<T>(q4 + axh * gm7, M.hx24, M.rhx24) : T(0);
+      D8n.v[c] = k4 ? hdiv<T>(q4 + (GC ? Y.ah[c] : T(0)) * gm8, M.hy24, M.rhy24) : T(0);
+      R4n.v[c] = k4 ? divr<T>(-gw * EA4.v[c] * M.dt, rho_ * rho_) * T(0.25) : T(0);
+    }
+    {
+      // R4 of rows a and a-1 at columns jc-1, jc
+      T rs[3], rp[3];
+      rs[0] = shup(R4n.v[1]);
+      rs[1] = R4n.v[0];
+      rs[2] = R4n.v[1];
+      rp[0] = shup(R4p.v[1]);
+      rp[1] = R4p.v[0];
+      rp[2] = R4p.v[1];
+      if (ownA) {
+        A orr[2];
+#pragma unroll
+        for (int c = 0; c < 2; c++)
+          orr[c] = (k3[c] ? AR.v[c] + grt[c] : AR.v[c]) + (rs[1 + c] + rp[1 + c] + rp[c] + rs[c]);
+        if (own) {
+          stw(accr, oa, orr, cp[0], cp[1]);
+          if constexpr (GR) {
+            stw(g5o, oa, sg5, w5[0], w5[1]);
+            stw(g7o, oa, sg7, w7[0], w7[1]);
+          }
+          if constexpr (GC) {
+            stw(g6o, oa, sg6, w6[0], w6[1]);
+            stw(g8o, oa, sg8, w8[0], w8[1]);
+          }
+        }
+      }
+    }
+    // ================= phase B: row b
+    V2<T> D1n{}, D2n{}, D3n{}, D4n{}, GL1n{}, GM1n{};
+    if (doB) {
+      // row b across columns: D6 at jc-1..jc+2, D8 at jc-2..jc+1, mu at jc..jc+1
+      T f6[5], f8[5], ur[3];
+      f6[0] = shup(W6_0.v[1]);
+      f6[1] = W6_0.v[0];
+      f6[2] = W6_0.v[1];
+      f6[3] = shdn(W6_0.v[0]);
+      f6[4] = shdn(W6_0.v[1]);
+      f8[0] = shup(W8_0.v[0]);
+      f8[1] = shup(W8_0.v[1]);
+      f8[2] = W8_0.v[0];
+      f8[3] = W8_0.v[1];
+      f8[4] = shdn(W8_0.v[0]);
+      ur[0] = U0.v[0];
+      ur[1] = U0.v[1];
+      ur[2] = shdn(U0.v[0]);
+      T oxx[2], oyy[2], oxy[2], sg1[2], sg2[2], sg3[2], sg4[2], gm2v[2];
+      bool k12[2], w1[2], w2[2], w3[2], w4[2];
+#pragma unroll
+      for (int c = 0; c < 2; c++) {
+        const bool b1 = r1b && c3[c], b2 = r2b && c4[c];
+        k12[c] = b1 || b2;
+        // gathers: D5 rows b-1..b+2, D7 rows b-2..b+1
+        const T gsxx = GA.v[c] + T(27) * W5_1.v[c] - T(27) * W5_2.v[c] - W5_0.v[c] + D5n.v[c];
+        const T gsyy = GB.v[c] + T(27) * f8[1 + c] - T(27) * f8[2 + c] - f8[c] + f8[3 + c];
+        const T gsxy = GCv.v[c] + T(27) * f6[1 + c] - T(27) * f6[2 + c] - f6[c] + f6[3 + c] +
+                       T(27) * W7_1.v[c] - T(27) * W7_2.v[c] - W7_0.v[c] + W7_3.v[c];
+        oxx[c] = gsxx;
+        oyy[c] = gsyy;
+        oxy[c] = gsxy;
+        // fw1 transpose
+        const T lam_ = T(0.5) * (L1.v[c] + L0.v[c]);
+        const T mu1 = T(0.5) * (U1.v[c] + U0.v[c]);
+        const T lm = lam_ + T(2) * mu1;
+        const T e1 = EA.v[c], e2 = EB.v[c];
+        const T gE1 = M.dt * (lm * gsxx + lam_ * gsyy);
+        const T gE2 = M.dt * (lam_ * gsxx + lm * gsyy);
+        const T glm = M.dt * (e1 * gsxx + e2 * gsyy);
+        const T glam = M.dt * (e2 * gsxx + e1 * gsyy) + glm;
+        const bool u1 = b1 && rx1, u2 = GC && b1 && Y.acti[c];
+        const T gm1 = u1 ? gE1 + m1.v[c] : gE1;
+        const T gm2 = u2 ? gE2 + m2.v[c] : gE2;
+        sg1[c] = bbxh * gm1;
+        sg2[c] = Y.bi[c] * gm2;
+        w1[c] = u1;
+        w2[c] = u2;
+        GL1n.v[c] = b1 ? T(0.5) * glam : T(0);
+        GM1n.v[c] = b1 ? glm : T(0);
+        D1n.v[c] = b1 ? hdiv<T>(gE1 + baxh * gm1, M.hx24, M.rhx24) : T(0);
+        D2n.v[c] = b1 ? hdiv<T>(gE2 + (GC ? Y.ai[c] : T(0)) * gm2, M.hy24, M.rhy24) : T(0);
+        // fw2 transpose
+        const T mu2 = T(0.5) * (ur[c] + ur[c + 1]);
+        const T q = gsxy * mu2 * M.dt;
+        const bool u3 = b2 && rx3, u4 = GC && b2 && Y.acth[c];
+        const T gm3 = u3 ? q + m3.v[c] : q;
+        const T gm4 = u4 ? q + m4.v[c] : q;
+        sg3[c] = bbxi * gm3;
+        sg4[c] = Y.bh[c] * gm4;
+        w3[c] = u3;
+        w4[c] = u4;
+        D3n.v[c] = b2 ? hdiv<T>(q + baxi * gm3, M.hx24, M.rhx24) : T(0);
+        D4n.v[c] = b2 ? hdiv<T>(q + (GC ? Y.ah[c] : T(0)) * gm4, M.hy24, M.rhy24) : T(0);
+        gm2v[c] = b2 ? gsxy * EC12.v[c] * M.dt * T(0.5) : T(0);  // GM2, the sxy term of mu
+      }
+      // GM2 of row b at columns jc-1, jc
+      T g12[3];
+      g12[1] = gm2v[0];
+      g12[2] = gm2v[1];
+      g12[0] = shup(g12[2]);
+      if (ownB) {
+        A ol[2], om[2];
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+          ol[c] = AL.v[c] + (GL1n.v[c] + GL1p.v[c]);
+          om[c] = AM.v[c] + (GM1n.v[c] + GM1p.v[c] + g12[1 + c] + g12[c]);
+        }
+        if (own) {
+          stw(oxxp, ob, oxx, k12[0], k12[1]);
+          stw(oyyp, ob, oyy, k12[0], k12[1]);
+          stw(oxyp, ob, oxy, k12[0], k12[1]);
+          stw(accl, ob, ol, cp[0], cp[1]);
+          stw(accm, ob, om, cp[0], cp[1]);
+          if constexpr (GR) {
+            stw(g1o, ob, sg1, w1[0], w1[1]);
+            stw(g3o, ob, sg3, w3[0], w3[1]);
+          }
+          if constexpr (GC) {
+            stw(g2o, ob, sg2, w2[0], w2[1]);
+            stw(g4o, ob, sg4, w4[0], w4[1]);
+          }
+        }
+      }
+    }
+    // ================= phase C: row t
+    if (doC) {
+      // row t across columns: D4 at jc-2..jc+1, D2 at jc-1..jc+2
+      T f4[5], f2[5];
+      f4[0] = shup(W4_0.v[0]);
+      f4[1] = shup(W4_0.v[1]);
+      f4[2] = W4_0.v[0];
+      f4[3] = W4_0.v[1];
+      f4[4] = shdn(W4_0.v[0]);
+      f2[0] = shup(W2_0.v[1]);
+      f2[1] = W2_0.v[0];
+      f2[2] = W2_0.v[1];
+      f2[3] = shdn(W2_0.v[0]);
+      f2[4] = shdn(W2_0.v[1]);
+      const bool r3t = rb3(t), r4t = rb4(t);
+      T ovx[2], ovy[2];
+      bool k3t[2], k4t[2];
+#pragma unroll
+      for (int c = 0; c < 2; c++) {
+        k3t[c] = r3t && c3[c];
+        k4t[c] = r4t && c4[c];
+        // D1 rows t-2..t+1, D3 rows t-1..t+2
+        ovx[c] = VX0.v[c] + (T(27) * W1_1.v[c] - T(27) * W1_2.v[c] - W1_0.v[c] + W1_3.v[c] +
+                             T(27) * f4[1 + c] - T(27) * f4[2 + c] - f4[c] + f4[3 + c]);
+        ovy[c] = VY0.v[c] + (T(27) * f2[1 + c] - T(27) * f2[2 + c] - f2[c] + f2[3 + c] +
+                             T(27) * W3_1.v[c] - T(27) * W3_2.v[c] - W3_0.v[c] + D3n.v[c]);
+      }
+      if (own) {
+        stw(ovxp, ot, ovx, k3t[0], k3t[1]);
+        stw(ovyp, ot, ovy, k4t[0], k4t[1]);
+      }
+    }
+    W5_0 = W5_1; W5_1 = W5_2; W5_2 = D5n;
+    W7_0 = W7_1; W7_1 = W7_2; W7_2 = W7_3; W7_3 = D7n;
+    W6_0 = W6_1; W6_1 = D6n;
+    W8_0 = W8_1; W8_1 = D8n;
+    R4p = R4n;
+    W1_0 = W1_1; W1_1 = W1_2; W1_2 = W1_3; W1_3 = D1n;
+    W3_0 = W3_1; W3_1 = W3_2; W3_2 = D3n;
+    W2_0 = W2_1; W2_1 = D2n;
+    W4_0 = W4_1; W4_1 = D4n;
+    GL1p = GL1n; GM1p = GM1n;
+    R0 = R1; R1 = R2;
+    L0 = L1; U0 = U1;
+  }
+}
+
 // End of a checkpoint segment (FP32 plans): accumulators += partials, partials = 0.
 __global__ void k_el_flush_acc(const ElShot<float>* __restrict__ shots, int64_t n) {
   const ElShot<float>& sh = shots[blockIdx.y];
@@ -1352,25 +1739,27 @@ __global__ void k_el_src_rcv(const ElShot<T>* __restrict__ shots, int n, int nt,
 }
 
 // Adjoint state += residual of slot n at the receivers (one thread each).
+// par: the adjoint buffer that holds slot n (0 for the in-place form).
 template <typename T>
-__global__ void k_el_resid(const ElShot<T>* __restrict__ shots, int n, int nt) {
+__global__ void k_el_resid(const ElShot<T>* __restrict__ shots, int n, int nt, int par) {
   const ElShot<T>& sh = shots[blockIdx.y];
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= sh.nrcv) return;
   T* p = sh.rcv_gptr[r];
-  if (p) atomicAdd(p, sh.resid[(int64_t)r * nt + n]);
+  if (p) atomicAdd(p + (par ? (int64_t)NF * sh.fs : 0), sh.resid[(int64_t)r * nt + n]);
 }
 
 // d loss / d srcv row n-1: srcv row n-1 is added to state n, so its gradient
 // is the adjoint of state n (residual of slot n included) at the source cell
 // (AddSource.cpp:91-155 gathers grad_srcv the same way).  One thread a source.
 template <typename T>
-__global__ void k_el_src_grad(const ElShot<T>* __restrict__ shots, int n) {
+__global__ void k_el_src_grad(const ElShot<T>* __restrict__ shots, int n, int par) {
   const ElShot<T>& sh = shots[blockIdx.y];
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= sh.nsrc) return;
   const T* p = sh.src_gptr[k];
-  sh.gsrc[(int64_t)(n - 1) * sh.nsrc + k] = p ? (double)*p : 0.0;
+  sh.gsrc[(int64_t)(n - 1) * sh.nsrc + k] =
+      p ? (double)p[par ? (int64_t)NF * sh.fs : 0] : 0.0;
 }
 
 // State <-> checkpoint copies (13 contiguous fields per shot).  Saving reads
@@ -1599,6 +1988,20 @@ void el_step(bool store, int kind, dim3 g, cudaStream_t s, const ElModel<T>& M,
 #undef ADS_K
 }
 
+template <typename T>
+void el_fadj(int kind, dim3 g, cudaStream_t s, const ElModel<T>& M, const ElShot<T>* sh,
+             const int* wl, int ncolw, int R, int nw, int slot, int pin, int jsh, int ish) {
+#define ADS_K(KD) \
+  k_el_adj_rows<T, KD><<<g, EW * 32, 0, s>>>(M, sh, wl, ncolw, R, nw, slot, pin, jsh, ish)
+  switch (kind) {
+    case 0: ADS_K(0); break;
+    case 1: ADS_K(1); break;
+    case 2: ADS_K(2); break;
+    default: ADS_K(3); break;
+  }
+#undef ADS_K
+}
+
 // ======================================================================
 // whole-path elastic plan
 // ======================================================================
@@ -1633,7 +2036,8 @@ struct ElPlanBase {
   int64_t src_total = 0;
   int64_t trace_total = 0, bytes = 0, launches_fwd = 0, launches_grad = 0;
   int64_t resident = 0;  // checkpoint segments kept resident (no recompute)
-  int64_t tiling[2] = {0, 0};  // rows per adjoint strip, rows per fused-step tile
+  int64_t tiling[2] = {0, 0};  // rows per adjoint tile or strip, rows per fused-step tile
+  int64_t adj_items[4] = {0, 0, 0, 0};  // fused adjoint items of each kind
 };
 
 namespace {
@@ -1666,13 +2070,28 @@ struct ElPlan final : ElPlanBase {
   int ncolf = 0, rows_f = 0, nwtf = 0, jsh = 0, ish = 0;
   int nwk[4] = {}, owk[4] = {};  // items of each kind (k_el_step_rows KIND) and their offsets
   int* d_wlf = nullptr;
+  // the fused adjoint step (k_el_adj_rows): its own row tiles and item lists
+  // (its halo is four rows and two lanes deep), and the adjoint buffer that
+  // holds slot n.  fused == false: the three gather passes, in place.
+  bool fused = true;
+  int ncola = 0, rows_a = 0, nwta = 0, jsha = 0, isha = 0;
+  int nwka[4] = {}, owka[4] = {};
+  int* d_wla = nullptr;
   // host copies: the packed CPML rows and the item lists of the current tiling
   std::vector<T> hprof;
-  std::vector<int> wl_host, wlf_host;
-  void build_lists(int rw, int rf);  // items for rows_w = rw, rows_f = rf
+  std::vector<int> wl_host, wlf_host, wla_host;
+  // items for rows_w = rw (three-pass adjoint), rows_f = rf (fused step) and
+  // rows_a = ra (fused adjoint)
+  void build_lists(int rw, int rf, int ra);
   int upload_lists(cudaStream_t st);
   int autotune(cudaStream_t st, int rw_min, int rf_min);
   static int par(int n) { return n & 1; }
+  int apar(int n) const { return fused ? n & 1 : 0; }  // adjoint buffer of slot n
+  int adj_launches() const {
+    if (fused) return (nwka[0] > 0) + (nwka[1] > 0) + (nwka[2] > 0) + (nwka[3] > 0);
+    return group_launches(kSplitAdj1, nw_in, nw_pm) +
+           2 * group_launches(kSplitAdj23, nw_in, nw_pm);
+  }
   cudaStream_t side[3] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[3] = {};
   // launches of one row-kernel step over the interior and CPML lists, whole
@@ -1683,9 +2102,9 @@ struct ElPlan final : ElPlanBase {
   int fwd_launches() const {
     return (nwk[0] > 0) + (nwk[1] > 0) + (nwk[2] > 0) + (nwk[3] > 0);
   }
-  // fn(stream, kind) for each kind of fused-step items, concurrently
+  // fn(stream, kind) for each kind with items (nk[kind] > 0), concurrently
   template <typename F>
-  int kinds(cudaStream_t st, F&& fn);
+  int kinds(cudaStream_t st, const int* nk, F&& fn);
   // fn(stream, interior, part) for each non-empty list (n_in interior items,
   // n_pm CPML items) and part, launched concurrently on the main stream and
   // the side streams (disjoint outputs)
@@ -1736,7 +2155,7 @@ struct ElPlan final : ElPlanBase {
   int create(const ads_elastic_config& c, const ads_elastic_shot* shots, int64_t ns,
              cudaStream_t st);
   int step(cudaStream_t st, int n, bool store, int slot, bool record);
-  int adjoint_step(cudaStream_t st, int slot);
+  int adjoint_step(cudaStream_t st, int slot, int n);
   int issue_forward(cudaStream_t st, int64_t* count);
   int issue_reverse(cudaStream_t st, int64_t* count);
   int prep(const double* l, const double* m, const double* r, cudaStream_t st);
@@ -1764,6 +2183,9 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
               "dx, dy, dt must be positive and finite (and vp_ref finite)");
   ADS_REQUIRE(c.npml >= 1 && c.Rcoef > 0 && c.Rcoef < 1, "invalid CPML parameters");
   ADS_REQUIRE(c.ckpt_every >= 0, "negative ckpt_every");
+  ADS_REQUIRE(c.adjoint_passes == 0 || c.adjoint_passes == 1 || c.adjoint_passes == 3,
+              "adjoint_passes must be 0, 1 or 3");
+  fused = c.adjoint_passes != 3;
   nshots = (int)ns;
   max_rcv = 0;
   for (int64_t s = 0; s < ns; s++) max_rcv = std::max<int>(max_rcv, (int)shots[s].nrcv);
@@ -1832,6 +2254,13 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
                  : (int)std::min<int64_t>(
                        NX, std::min<int64_t>(24, std::max<int64_t>(
                                                      8, div_up(workf, (int64_t)sms * 20))));
+    // the fused adjoint recomputes four rows on each side of a row tile: 24-row
+    // tiles, shorter when that leaves less than about one wave of ~16 warps per SM
+    rows_a = c.rows_per_warp > 0
+                 ? (int)c.rows_per_warp
+                 : (int)std::min<int64_t>(
+                       NX, std::min<int64_t>(24, std::max<int64_t>(
+                                                     8, div_up(workf, (int64_t)sms * 16))));
   }
   nwt = ncolw * (int)div_up(NX, rows_w);
   // the autotuner tries rows down to kTuneMinRows (adjoint) and
@@ -1843,6 +2272,9 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   // the CPML profiles are known)
   const int nwtf_max =
       (int)(div_up(NY + FSTRIP - 2, FSTRIP) * div_up(NX + rf_min - 1, rf_min));
+  const int ra_min = c.autotune ? std::min(rows_a, kTuneMinRowsF) : rows_a;
+  const int nwta_max =
+      (int)(div_up(NY + FSTRIP - 2, FSTRIP) * div_up(NX + ra_min - 1, ra_min));
   trace_off.resize(ns);
   trace_total = 0;
   for (int s = 0; s < ns; s++) {
@@ -1869,7 +2301,7 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   zero_fwd_len = used - fwd0;
   const size_t adj0 = used;
   for (int s = 0; s < ns; s++) {
-    o[s].g = take(NF * F);
+    o[s].g = take((fused ? 2 : 1) * NF * F);  // the fused adjoint alternates two buffers
     o[s].acc = take(3 * sizeof(double) * fs);
     o[s].acc32 = sizeof(T) == 4 ? take(3 * sizeof(float) * fs) : 0;
   }
@@ -1877,7 +2309,7 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   zero_adj_len = used - adj0;
   for (int s = 0; s < ns; s++) {
     const ads_elastic_shot& h = shots[s];
-    o[s].tmp = take(NTMP * F);
+    o[s].tmp = fused ? 0 : take(NTMP * F);  // D1..D8, R4, GL1, GM1, GM2 of the three passes
     o[s].ckpt = take((size_t)nseg * NF * F);
     o[s].srcv = take(sizeof(T) * std::max<int64_t>(NSTEP * h.nsrc, 1));
     o[s].scell = take(sizeof(int64_t) * std::max<int64_t>(h.nsrc, 1));
@@ -1898,6 +2330,7 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   const size_t shots_o = take(sizeof(ElShot<T>) * ns);
   const size_t wl_o = take(sizeof(int) * std::max(nwt_max, 1));
   const size_t wlf_o = take(sizeof(int) * std::max(nwtf_max, 1));
+  const size_t wla_o = take(sizeof(int) * std::max(fused ? nwta_max : 1, 1));
   // ---- the shots' stores: K slots for a segment's recompute, then one slot
   // per step of the resident segments (the last ones that fit in the allowed
   // share of the free device memory)
@@ -1950,9 +2383,10 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
                ky.data());
   hprof = pack_profiles<T>(NX, NY, ax.data(), bx.data(), ay.data(), by.data());
   const std::vector<T>& prof = hprof;
-  build_lists(rows_w, rows_f);
+  build_lists(rows_w, rows_f, rows_a);
   d_wl = (int*)(pool + wl_o);
   d_wlf = (int*)(pool + wlf_o);
+  d_wla = (int*)(pool + wla_o);
   if (int e = upload_lists(st)) return e;
   for (auto& q : side) ADS_CUDA(cudaStreamCreateWithFlags(&q, cudaStreamNonBlocking));
   ADS_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
@@ -1974,7 +2408,7 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
       d.fin[f] = d.f[f];
       d.g[f] = (T*)(pool + o[s].g) + f * fs;
     }
-    for (int k = 0; k < NTMP; k++) d.tmp[k] = (T*)(pool + o[s].tmp) + k * fs;
+    for (int k = 0; k < NTMP; k++) d.tmp[k] = fused ? nullptr : (T*)(pool + o[s].tmp) + k * fs;
     d.store = (T*)(pool + o[s].store);
     d.ckpt = (T*)(pool + o[s].ckpt);
     d.glam = (double*)(pool + o[s].acc);
@@ -2076,8 +2510,9 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   ADS_CUDA(cudaStreamSynchronize(st));
   if (c.autotune && c.rows_per_warp <= 0)
     if (int e = autotune(st, rw_min, rf_min)) return e;
-  tiling[0] = rows_w;
+  tiling[0] = fused ? rows_a : rows_w;
   tiling[1] = rows_f;
+  for (int k = 0; k < 4; k++) adj_items[k] = fused ? nwka[k] : 0;
   {
     int64_t n = 0;
     issue_forward(nullptr, &n);
@@ -2113,12 +2548,14 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
 // Warp items of the tiling rows_w = rw (adjoint passes) and rows_f = rf (the
 // fused step), from the packed CPML rows hprof.
 template <typename T>
-void ElPlan<T>::build_lists(int rw, int rf) {
+void ElPlan<T>::build_lists(int rw, int rf, int ra) {
   rows_w = rw;
   rows_f = rf;
+  rows_a = ra;
   nwt = ncolw * (int)div_up(NX, rows_w);
   wl_host.clear();
   wlf_host.clear();
+  wla_host.clear();
   // warp items: a (strip, row tile) is interior when every cell it updates lies
   // inside all four update boxes (2 <= i <= NX-1, 2 <= j <= NY-1) with no
   // active CPML profile on its rows and columns (as the kernels see them)
@@ -2144,60 +2581,68 @@ void ElPlan<T>::build_lists(int rw, int rf) {
   nw_in = (int)wl_host.size();
   nw_pm = (int)wpm.size();
   wl_host.insert(wl_host.end(), wpm.begin(), wpm.end());
-  // fused-step items by kind: bit 0 when a row whose stresses the warp
-  // computes (i0-2 .. i_end+1) lies on a box edge or in the x-CPML, bit 1
-  // when a column of lanes 1..30 (a-2 .. a+FSTRIP+1 for a strip owning
-  // columns from a) lies on a box edge or in the y-CPML
-  auto tile_ok = [&](int rt, int sh_) {
-    const int i0r = 1 + sh_ + rt * rows_f;
-    const int i0 = std::max(i0r, 1), i1 = std::min(i0r + rows_f, NX + 1);
-    for (int i = i0 - 2; i <= i1 + 1; i++)
-      if (i < 0 || i > NX + 1 || !row_ok[i]) return false;
-    return true;
-  };
-  auto strip_ok = [&](int strip, int sh_) {
-    const int a = 1 + sh_ + strip * FSTRIP;
-    for (int jc = a - 2; jc <= a + FSTRIP + 1; jc++)
-      if (jc < 0 || jc > NY + 1 || !col_ok[jc]) return false;
-    return true;
-  };
-  // shifts of the strip and tile origins with the most CPML-free strips and
-  // tiles (then the fewest strips and tiles)
-  int best = -1, bestn = 0;
-  for (int sh_ = 0; sh_ > -FSTRIP; sh_ -= 2) {
-    const int n = (int)div_up(NY - sh_, FSTRIP);
-    int ok = 0;
-    for (int k = 0; k < n; k++) ok += strip_ok(k, sh_);
-    if (ok > best || (ok == best && n < bestn)) {
-      best = ok;
-      bestn = n;
-      jsh = sh_;
+  // Items of a fused kernel (FSTRIP-column strips, R-row tiles) by kind: bit 0
+  // when a row it computes (hr rows beyond its own on each side) lies on a box
+  // edge or in the x-CPML, bit 1 when a column of its computing lanes (hc
+  // columns beyond its own on each side) lies on a box edge or in the y-CPML.
+  // The strip and tile origins are shifted (js, is <= 0) to make the most
+  // strips and tiles CPML-free (then the fewest).
+  auto fused_items = [&](int R, int hr, int hc, int& js, int& is, int& ncol, int& nwtot,
+                         int (&nk)[4], int (&ok)[4], std::vector<int>& out) {
+    auto tile_ok = [&](int rt, int sh_) {
+      const int i0r = 1 + sh_ + rt * R;
+      const int i0 = std::max(i0r, 1), i1 = std::min(i0r + R, NX + 1);
+      for (int i = i0 - hr; i <= i1 - 1 + hr; i++)
+        if (i < 0 || i > NX + 1 || !row_ok[i]) return false;
+      return true;
+    };
+    auto strip_ok = [&](int strip, int sh_) {
+      const int a = 1 + sh_ + strip * FSTRIP;
+      for (int jc = a - hc; jc <= a + FSTRIP - 1 + hc; jc++)
+        if (jc < 0 || jc > NY + 1 || !col_ok[jc]) return false;
+      return true;
+    };
+    int best = -1, bestn = 0;
+    for (int sh_ = 0; sh_ > -FSTRIP; sh_ -= 2) {
+      const int n = (int)div_up(NY - sh_, FSTRIP);
+      int k = 0;
+      for (int s = 0; s < n; s++) k += strip_ok(s, sh_);
+      if (k > best || (k == best && n < bestn)) {
+        best = k;
+        bestn = n;
+        js = sh_;
+      }
     }
-  }
-  ncolf = bestn;
-  best = -1;
-  int bestt = 0;
-  for (int sh_ = 0; sh_ > -rows_f; sh_--) {
-    const int n = (int)div_up(NX - sh_, rows_f);
-    int ok = 0;
-    for (int k = 0; k < n; k++) ok += tile_ok(k, sh_);
-    if (ok > best || (ok == best && n < bestt)) {
-      best = ok;
-      bestt = n;
-      ish = sh_;
+    ncol = bestn;
+    best = -1;
+    int bestt = 0;
+    for (int sh_ = 0; sh_ > -R; sh_--) {
+      const int n = (int)div_up(NX - sh_, R);
+      int k = 0;
+      for (int s = 0; s < n; s++) k += tile_ok(s, sh_);
+      if (k > best || (k == best && n < bestt)) {
+        best = k;
+        bestt = n;
+        is = sh_;
+      }
     }
-  }
-  nwtf = ncolf * bestt;
-  std::vector<int> wk[4];
-  for (int wi = 0; wi < nwtf; wi++) {
-    const int strip = wi % ncolf, rt = wi / ncolf;
-    wk[(tile_ok(rt, ish) ? 0 : 1) | (strip_ok(strip, jsh) ? 0 : 2)].push_back(wi);
-  }
-  for (int k = 0; k < 4; k++) {
-    owk[k] = (int)wlf_host.size();
-    nwk[k] = (int)wk[k].size();
-    wlf_host.insert(wlf_host.end(), wk[k].begin(), wk[k].end());
-  }
+    nwtot = ncol * bestt;
+    std::vector<int> wk[4];
+    for (int wi = 0; wi < nwtot; wi++) {
+      const int strip = wi % ncol, rt = wi / ncol;
+      wk[(tile_ok(rt, is) ? 0 : 1) | (strip_ok(strip, js) ? 0 : 2)].push_back(wi);
+    }
+    for (int k = 0; k < 4; k++) {
+      ok[k] = (int)out.size();
+      nk[k] = (int)wk[k].size();
+      out.insert(out.end(), wk[k].begin(), wk[k].end());
+    }
+  };
+  // the fused step computes stresses two rows and one lane (two columns)
+  // beyond what it owns; the fused adjoint runs phase A four rows and two
+  // lanes beyond
+  fused_items(rows_f, 2, 2, jsh, ish, ncolf, nwtf, nwk, owk, wlf_host);
+  if (fused) fused_items(rows_a, 4, 4, jsha, isha, ncola, nwta, nwka, owka, wla_host);
 }
 
 template <typename T>
@@ -2206,6 +2651,9 @@ int ElPlan<T>::upload_lists(cudaStream_t st) {
                            cudaMemcpyHostToDevice, st));
   if (!wlf_host.empty())
     ADS_CUDA(cudaMemcpyAsync(d_wlf, wlf_host.data(), sizeof(int) * wlf_host.size(),
+                             cudaMemcpyHostToDevice, st));
+  if (!wla_host.empty())
+    ADS_CUDA(cudaMemcpyAsync(d_wla, wla_host.data(), sizeof(int) * wla_host.size(),
                              cudaMemcpyHostToDevice, st));
   ADS_CUDA(cudaStreamSynchronize(st));  // the host lists change between trials
   return ADS_OK;
@@ -2224,7 +2672,7 @@ int ElPlan<T>::autotune(cudaStream_t st, int rw_min, int rf_min) {
     for (int pass = 0; pass < 2; pass++) {  // pass 0 warms up
       ADS_CUDA(cudaEventRecord(e0, st));
       for (int n = 1; n <= 6; n++)
-        if (int e = adj ? adjoint_step(st, 0) : step(st, n, false, 0, false)) return e;
+        if (int e = adj ? adjoint_step(st, 0, n) : step(st, n, false, 0, false)) return e;
       ADS_CUDA(cudaEventRecord(e1, st));
       ADS_CUDA(cudaEventSynchronize(e1));
       ADS_CUDA(cudaEventElapsedTime(&ms, e0, e1));
@@ -2236,7 +2684,7 @@ int ElPlan<T>::autotune(cudaStream_t st, int rw_min, int rf_min) {
   float best = 1e30f;
   for (int rf : {12, 16, 20, 24, 32}) {
     if (rf < rf_min || rf > NX) continue;
-    build_lists(best_w, rf);
+    build_lists(best_w, rf, rows_a);
     float ms = 0.f;
     if ((rc = upload_lists(st)) || (rc = timed(false, ms))) break;
     if (ms < best) {
@@ -2245,21 +2693,30 @@ int ElPlan<T>::autotune(cudaStream_t st, int rw_min, int rf_min) {
     }
   }
   best = 1e30f;
-  for (int rw : {6, 8, 12, 16, 24, 32}) {
+  int best_a = rows_a;
+  // the fused adjoint: tile heights as the fused step's; the three passes:
+  // strip heights
+  const std::vector<int> cand =
+      fused ? std::vector<int>{12, 16, 20, 24, 32} : std::vector<int>{6, 8, 12, 16, 24, 32};
+  for (int rw : cand) {
     if (rc != ADS_OK) break;
-    if (rw < rw_min || rw > NX) continue;
-    build_lists(rw, best_f);
+    if ((!fused && rw < rw_min) || rw > NX) continue;  // (the lists hold >= 12-row tiles)
+    if (fused) {
+      build_lists(best_w, best_f, rw);
+    } else {
+      build_lists(rw, best_f, rows_a);
+    }
     float ms = 0.f;
     if ((rc = upload_lists(st)) || (rc = timed(true, ms))) break;
     if (ms < best) {
       best = ms;
-      best_w = rw;
+      (fused ? best_a : best_w) = rw;
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (rc != ADS_OK) return rc;
-  build_lists(best_w, best_f);
+  build_lists(best_w, best_f, best_a);
   return upload_lists(st);
 }
 
@@ -2294,10 +2751,10 @@ int ElPlan<T>::group(cudaStream_t st, bool split, int n_in, int n_pm, F&& fn) {
 
 template <typename T>
 template <typename F>
-int ElPlan<T>::kinds(cudaStream_t st, F&& fn) {
+int ElPlan<T>::kinds(cudaStream_t st, const int* nk, F&& fn) {
   int kd[4], n = 0;
   for (int k = 0; k < 4; k++)
-    if (nwk[k] > 0) kd[n++] = k;
+    if (nk[k] > 0) kd[n++] = k;
   if (n > 1) {
     ADS_CUDA(cudaEventRecord(ev_fork, st));
     for (int k = 1; k < n; k++) ADS_CUDA(cudaStreamWaitEvent(side[k - 1], ev_fork, 0));
@@ -2313,9 +2770,16 @@ int ElPlan<T>::kinds(cudaStream_t st, F&& fn) {
   return ADS_OK;
 }
 
-// The three adjoint passes of step n (store slot `slot`).
+// The adjoint of step n (store slot `slot`): the fused kernel's launches over
+// the item kinds (adjoint of slot n in buffer apar(n) -> slot n-1 in the
+// other), or the three passes in place.
 template <typename T>
-int ElPlan<T>::adjoint_step(cudaStream_t st, int slot) {
+int ElPlan<T>::adjoint_step(cudaStream_t st, int slot, int n) {
+  if (fused)
+    return kinds(st, nwka, [&](cudaStream_t s, int k) {
+      el_fadj<T>(k, grid_rows(nwka[k]), s, M, d_shots, d_wla + owka[k], ncola, rows_a, nwka[k],
+                 slot, apar(n), jsha, isha);
+    });
   auto wl = [&](bool in) { return in ? d_wl : d_wl + nw_in; };
   auto nw = [&](bool in) { return in ? nw_in : nw_pm; };
   if (int e = group(st, kSplitAdj1, nw_in, nw_pm, [&](cudaStream_t s, bool in, int part) {
@@ -2338,7 +2802,7 @@ int ElPlan<T>::adjoint_step(cudaStream_t st, int slot) {
 template <typename T>
 int ElPlan<T>::step(cudaStream_t st, int n, bool store, int slot, bool record) {
   const int sl = store ? slot : 0;
-  if (int e = kinds(st, [&](cudaStream_t s, int k) {
+  if (int e = kinds(st, nwk, [&](cudaStream_t s, int k) {
         el_step<T>(store, k, grid_rows(nwk[k]), s, M, d_shots, d_wlf + owk[k], ncolf, rows_f,
                    nwk[k], sl, par(n - 1), jsh, ish);
       }))
@@ -2379,8 +2843,7 @@ int ElPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     for (int s = nseg - 1; s >= 0; s--) {
       const int a = 1 + s * K, b = std::min(a + K - 1, NSTEP);
       if (s < res_seg) c += 1 + (fwd_launches() + 1) * (b - a + 1);
-      c += (group_launches(kSplitAdj1, nw_in, nw_pm) +
-            2 * group_launches(kSplitAdj23, nw_in, nw_pm)) * (b - a + 1) +
+      c += adj_launches() * (b - a + 1) +
            (b - std::max(a, 2) + 1) + (src_grad ? b - a + 1 : 0) +
            (sizeof(T) == 4 ? 1 : 0);
     }
@@ -2388,7 +2851,7 @@ int ElPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     return ADS_OK;
   }
   ADS_CUDA(cudaMemsetAsync(pool + zero_adj_off, 0, zero_adj_len, st));
-  k_el_resid<T><<<grid_resid(), 256, 0, st>>>(d_shots, NSTEP, NSTEP + 1);
+  k_el_resid<T><<<grid_resid(), 256, 0, st>>>(d_shots, NSTEP, NSTEP + 1, apar(NSTEP));
   ADS_LAUNCHED(1);
   for (int s = nseg - 1; s >= 0; s--) {
     const int a = 1 + s * K, b = std::min(a + K - 1, NSTEP);
@@ -2403,14 +2866,14 @@ int ElPlan<T>::issue_reverse(cudaStream_t st, int64_t* count) {
     for (int n = b; n >= a; n--) {
       if (src_grad) {  // the adjoint state refers to slot n, its residual included
         k_el_src_grad<T><<<dim3((unsigned)div_up(std::max(max_src, 1), 128), nshots), 128, 0,
-                            st>>>(d_shots, n);
+                            st>>>(d_shots, n, apar(n));
         ADS_LAUNCHED(1);
       }
-      if (int e = adjoint_step(st, slot0 + n - a)) return e;
+      if (int e = adjoint_step(st, slot0 + n - a, n)) return e;
       // the adjoint state now refers to slot n-1: add its residual (slot 0 is
       // the constant zero state and takes none)
       if (n - 1 >= 1) {
-        k_el_resid<T><<<grid_resid(), 256, 0, st>>>(d_shots, n - 1, NSTEP + 1);
+        k_el_resid<T><<<grid_resid(), 256, 0, st>>>(d_shots, n - 1, NSTEP + 1, apar(n - 1));
         ADS_LAUNCHED(1);
       }
     }
@@ -2521,22 +2984,27 @@ int ElPlan<T>::profile(const double* l, const double* m, const double* r, double
   auto nw = [&](bool in) { return in ? nw_in : nw_pm; };
   for (int k = 0; k < 2; k++)
     run(k, [&] {
-      kinds(st, [&](cudaStream_t s, int kd) {
+      kinds(st, nwk, [&](cudaStream_t s, int kd) {
         el_step<T>(k == 1, kd, grid_rows(nwk[kd]), s, M, d_shots, d_wlf + owk[kd], ncolf,
                    rows_f, nwk[kd], 0, 0, jsh, ish);
       });
     });
-  run(2, [&] {
+  if (fused) {  // the fused adjoint in slot 2; slots 3 and 4 stay empty
+    run(2, [&] { adjoint_step(st, 0, 1); });
+    out[6] = out[8] = 0.0;
+    out[7] = out[9] = cells;
+  }
+  if (!fused) run(2, [&] {
     group(st, kSplitAdj1, nw_in, nw_pm, [&](cudaStream_t s, bool in, int part) {
       el_adj1<T>(in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w, nw(in), 0);
     });
   });
-  run(3, [&] {
+  if (!fused) run(3, [&] {
     group(st, kSplitAdj23, nw_in, nw_pm, [&](cudaStream_t s, bool in, int part) {
       el_adj2<T>(in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w, nw(in), 0);
     });
   });
-  run(4, [&] {
+  if (!fused) run(4, [&] {
     group(st, kSplitAdj23, nw_in, nw_pm, [&](cudaStream_t s, bool in, int part) {
       el_adj3<T>(in, part, grid_rows(nw(in)), s, M, d_shots, wl(in), ncolw, rows_w, nw(in));
     });
@@ -2544,7 +3012,7 @@ int ElPlan<T>::profile(const double* l, const double* m, const double* r, double
   run(5, [&] {
     k_el_src_rcv<T><<<nshots, rcv_threads(), 0, st>>>(d_shots, 1, NSTEP + 1, 1, 0, 0);
   });
-  run(6, [&] { k_el_resid<T><<<grid_resid(), 256, 0, st>>>(d_shots, 1, NSTEP + 1); });
+  run(6, [&] { k_el_resid<T><<<grid_resid(), 256, 0, st>>>(d_shots, 1, NSTEP + 1, 0); });
   note_launches(2 * (kProfileReps + 1));  // the pairs count their own launches
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -2928,8 +3396,8 @@ int64_t ads_elastic_plan_resident_segments(const ads_elastic_plan* plan) {
 }
 
 int64_t ads_elastic_plan_rows(const ads_elastic_plan* plan, int which) {
-  if (!plan || which < 0 || which > 1) return -1;
-  return plan->impl->tiling[which];
+  if (!plan || which < 0 || which > 5) return -1;
+  return which < 2 ? plan->impl->tiling[which] : plan->impl->adj_items[which - 2];
 }
 
 int64_t ads_elastic_plan_launches(const ads_elastic_plan* plan, int gradient) {

@@ -139,12 +139,13 @@ class ElasticPlan:
     free device memory).  source_gradient: the reverse sweep also records
     d loss / d srcv (gradient(..., want_source_grad=True)); the plan then
     rejects (AdsError) sources on the padded frame, the cells the stencil of
-    their field does not update."""
+    their field does not update.  adjoint_passes: 1 (default) runs each
+    adjoint step as one fused pass, 3 as the three gather passes."""
 
     def __init__(self, param: ElasticPropagatorParams, shots, precision="f64",
                  use_graph=True, ckpt_every=0, stream=None, rows_per_warp=0,
                  resident_segments=0, resident_mem_pct=0, source_gradient=False,
-                 autotune=False):
+                 autotune=False, adjoint_passes=1):
         cfg = _lib.ElasticConfig()
         cfg.NX, cfg.NY, cfg.NSTEP = param.NX, param.NY, param.NSTEP
         cfg.dx, cfg.dy, cfg.dt = param.DELTAX, param.DELTAY, param.DELTAT
@@ -159,6 +160,7 @@ class ElasticPlan:
         cfg.resident_mem_pct = int(resident_mem_pct)
         cfg.source_gradient = int(bool(source_gradient))
         cfg.autotune = int(bool(autotune))
+        cfg.adjoint_passes = int(adjoint_passes)
         self.param = param
         self.dtype = torch.float64 if precision == "f64" else torch.float32
         self._keep = []
@@ -191,6 +193,8 @@ class ElasticPlan:
         self.resident_segments = L.ads_elastic_plan_resident_segments(h)
         self.rows_per_warp = L.ads_elastic_plan_rows(h, 0)
         self.rows_per_tile = L.ads_elastic_plan_rows(h, 1)
+        # fused adjoint warp items per shot: CPML-free, rows, columns, both
+        self.adjoint_items = [L.ads_elastic_plan_rows(h, k) for k in range(2, 6)]
 
     def close(self):
         if getattr(self, "_h", None):

@@ -324,7 +324,8 @@ def elastic_workload(ads, nshots=32, T=4000):
     return configs.c4_elastic(nshots=nshots, T=T)
 
 
-def elastic_measure(steps, warmup, nshots=32, T=4000, with_rel_err=True, autotune=True):
+def elastic_measure(steps, warmup, nshots=32, T=4000, with_rel_err=True, autotune=True,
+                    adjoint_passes=1):
     """Elastic CPML FWI gradient w.r.t. lambda, mu, rho (C4): 600x300 incl. CPML
     30, T steps, FP32 stencils with FP64 accumulation, explosive shots (sigma_xx
     and sigma_yy, 10 Hz Ricker), 300 two-component receivers.  Returns the
@@ -340,7 +341,7 @@ def elastic_measure(steps, warmup, nshots=32, T=4000, with_rel_err=True, autotun
     # the last checkpoint segments' adjoint inputs stay resident in HBM (up to
     # 92% of the memory free after the plan's other buffers)
     plan = ads.ElasticPlan(p, shots, precision="f32", ckpt_every=100, resident_mem_pct=92,
-                           autotune=autotune)
+                           autotune=autotune, adjoint_passes=adjoint_passes)
     obs = plan.forward(t(lam), t(mu), t(rho)).clone()
     l0, m0, r0 = (t(a) for a in configs.c4_start_model(lam, mu, rho))
     ms = _timed(lambda: plan.gradient(l0, m0, r0, obs), steps, warmup)
@@ -460,7 +461,8 @@ def run_elastic_fwi(args):
     nshots = args.shots if args.shots != 64 else 32
     T = args.nstep if args.nstep != 3000 else 4000
     r = elastic_measure(args.steps, args.warmup, nshots=nshots, T=T,
-                        autotune=not args.no_elastic_autotune)
+                        autotune=not args.no_elastic_autotune,
+                        adjoint_passes=args.elastic_adjoint_passes)
     _line("elastic FWI shot-gradients/s (FP32 stencils, FP64 accumulation)", r["value"],
           "shot-gradients/s", args, r["ms_per_step"], "f32", r["workload"],
           {k: r[k] for k in ("gcell_updates_per_s", "roofline", "device_bytes", "gpu_launches",
@@ -517,6 +519,7 @@ def main():
     ap.add_argument("--no-elastic", action="store_true")
     ap.add_argument("--no-elastic-autotune", action="store_true")
     ap.add_argument("--no-configs", action="store_true")
+    ap.add_argument("--elastic-adjoint-passes", type=int, default=1, choices=(1, 3))
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

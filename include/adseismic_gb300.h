@@ -409,9 +409,13 @@ typedef struct ads_elastic_config {
                                 2..NX / 2..NY, sxx and syy 2..NX / 3..NY+1, sxy
                                 3..NX+1 / 2..NY are updated); 0: not */
   int32_t autotune;          /* 1: time candidate row heights of the fused step and of the
-                                adjoint passes at plan creation and keep the fastest
+                                adjoint at plan creation and keep the fastest
                                 (ignored when rows_per_warp is set) */
-  int32_t reserved[4];
+  int32_t adjoint_passes;    /* the reverse sweep's adjoint step: 0 or 1 = one fused
+                                row-streaming pass (two adjoint state buffers, no
+                                intermediate fields in device memory); 3 = three gather
+                                passes over intermediate fields, in place */
+  int32_t reserved[3];
 } ads_elastic_config;
 
 typedef struct ads_elastic_shot {
@@ -442,8 +446,11 @@ int64_t ads_elastic_plan_launches(const ads_elastic_plan* plan, int gradient);
 /* Checkpoint segments kept resident (see resident_segments); -1 for a null plan. */
 int64_t ads_elastic_plan_resident_segments(const ads_elastic_plan* plan);
 /* The plan's tiling (as configured or as the autotuner chose it): which = 0,
- * rows per adjoint strip; 1, rows per fused-step tile; -1 for a null plan or
- * another `which`.  No reference counterpart. */
+ * rows per adjoint tile (fused adjoint) or strip (three passes); 1, rows per
+ * fused-step tile; 2..5, warp items of the fused adjoint per shot whose logic
+ * is CPML-free (2), x-CPML / box-edge rows (3), y-CPML / box-edge columns
+ * (4) or both (5), 0 for the three passes; -1 for a null plan or another
+ * `which`.  No reference counterpart. */
 int64_t ads_elastic_plan_rows(const ads_elastic_plan* plan, int which);
 /* ads_elastic_plan_gradient plus the source-time gradient grad_srcv = d loss /
  * d srcv, the gradient AddSource's backward (AddSource.cpp:91-155) gathers:
@@ -484,7 +491,8 @@ int ads_elastic_gradient(const ads_elastic_config* cfg, const ads_elastic_shot* 
  * launched 20 times on the plan's buffers between CUDA events.  out: 14
  * doubles, pairs (ms per launch, interior cell-updates per launch) for the
  * forward step, the forward step storing the adjoint's strains, adjoint
- * 1..3, the source / receiver and the residual kernels.  Leaves the plan's
+ * 1..3 (the fused adjoint step in the first of them, zero time in the other
+ * two), the source / receiver and the residual kernels.  Leaves the plan's
  * state zeroed; synchronises the stream. */
 int ads_elastic_plan_profile(ads_elastic_plan* plan, const double* lambda,
                              const double* mu, const double* rho, double* out,

@@ -121,7 +121,7 @@ def test_autotuned_plan_vs_oracle(ads, cuda, precision, tol):
     g = golden("elastic_small.npz")
     p = params(ads, g)
     plan = ads.ElasticPlan(p, shots_from(g), precision=precision, ckpt_every=17, autotune=True)
-    assert plan.rows_per_warp in (6, 8, 12, 16, 24) and plan.rows_per_tile in (12, 16, 20, 24)
+    assert plan.rows_per_warp in (12, 16, 20, 24, 32) and plan.rows_per_tile in (12, 16, 20, 24)
     t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=cuda)
     loss, gl, gm, gr = plan.gradient(t(g["lam"]), t(g["mu"]), t(g["rho"]),
                                      t(g["obs"].reshape(-1)))
@@ -382,3 +382,66 @@ def test_one_shot_entry_points_match_the_plan(ads, cuda):
         ads._lib.check(L.ads_elastic_forward(ctypes.byref(plan._cfg), None, lam.data_ptr(),
                                              mu.data_ptr(), rho.data_ptr(), tr1.data_ptr(), st))
     plan.close()
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+def test_fused_adjoint_all_item_kinds_vs_oracle_and_three_passes(ads, orc, cuda, precision):
+    """The fused adjoint step (the default) on a grid with warp items of all
+    four kinds (CPML-free, x-CPML rows, y-CPML columns, both), two shots, an
+    odd checkpoint interval and two resident segments: against the oracle
+    (FP64 1e-12, FP32 1e-4) and against the three gather passes on the same
+    plan geometry (FP64 1e-13, FP32 1e-6: the same arithmetic in the same
+    order)."""
+    NX, NY, T = 150, 190, 33
+    p = ads.ElasticPropagatorParams(NX=NX, NY=NY, NSTEP=T, DELTAX=10.0, DELTAY=12.0,
+                                    DELTAT=0.8e-3, NPOINTS_PML=10, vp_ref=3000.0, f0=15.0)
+    prof = ads.compute_elastic_PML_Params(p)
+    ax, bx, kx, ay, by, ky = [a.reshape(-1) for a in prof]
+    rng = np.random.default_rng(31)
+    vp = 3000 + 400 * rng.random((NX + 2, NY + 2))
+    lam, mu, rho = ads.compute_properties(vp, vp / 1.7,
+                                          2000 + 300 * rng.random((NX + 2, NY + 2)))
+    lam, mu, rho = (a.reshape(-1) for a in (lam, mu, rho))
+    shots, refs = [], []
+    for k in range(2):
+        srci = np.array([40 + 60 * k, 40 + 60 * k, 8, 75])
+        srcj = np.array([95, 95, 120 - 50 * k, 6])
+        srct = np.array([2, 3, 0, 4])
+        srcv = rng.standard_normal((T, 4)) * 1e3
+        nr = 60
+        rcvi = rng.integers(2, NX, nr)
+        rcvj = rng.integers(2, NY, nr)
+        rcvt = rng.integers(0, 5, nr)
+        obs = rng.standard_normal((nr, T + 1)) * 1e-3
+        shots.append(dict(srci=srci, srcj=srcj, srctype=srct, srcv=srcv, rcvi=rcvi, rcvj=rcvj,
+                          rcvtype=rcvt, obs=obs))
+        if precision == "f64":
+            refs.append(orc.elastic_gradient(NX, NY, T, p.DELTAT, p.DELTAX, p.DELTAY, ax, bx,
+                                             ay, by, lam, mu, rho, srci, srcj, srct, srcv,
+                                             rcvi, rcvj, rcvt, obs))
+    obs = np.concatenate([s["obs"].reshape(-1) for s in shots])
+    dt = torch.float64 if precision == "f64" else torch.float32
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=cuda)
+    out = {}
+    for passes in (1, 3):
+        plan = ads.ElasticPlan(p, shots, precision=precision, ckpt_every=7, rows_per_warp=16,
+                               resident_segments=2, adjoint_passes=passes)
+        if passes == 1:
+            assert all(n > 0 for n in plan.adjoint_items), plan.adjoint_items
+        else:
+            assert plan.adjoint_items == [0, 0, 0, 0]
+        loss, gl, gm, gr = plan.gradient(t(lam), t(mu), t(rho),
+                                         torch.as_tensor(obs, dtype=dt, device=cuda))
+        torch.cuda.synchronize()
+        out[passes] = [float(loss)] + [a.cpu().numpy() for a in (gl, gm, gr)]
+        plan.close()
+    f, s3 = out[1], out[3]
+    tol3 = 1e-13 if precision == "f64" else 1e-6
+    assert abs(f[0] - s3[0]) <= tol3 * abs(s3[0])
+    for a, b in zip(f[1:], s3[1:]):
+        assert rel(a, b) <= tol3
+    if precision == "f64":
+        lref = sum(r[0] for r in refs)
+        assert abs(f[0] - lref) <= 1e-12 * lref
+        for k in range(3):
+            assert rel(f[1 + k], sum(r[1 + k] for r in refs)) <= 1e-12
