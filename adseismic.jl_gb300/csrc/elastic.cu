@@ -406,6 +406,28 @@ __device__ __forceinline__ V2<float> ld2p(const float* p, int64_t o, bool on) {
   x.v[1] = b;
   return x;
 }
+// 32-bit offsets (within one field of one shot) let the address be formed in
+// one wide multiply-add
+__device__ __forceinline__ V2<float> ld2p(const float* p, int o, bool on) {
+  float a = 0.f, b = 0.f;
+  asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %3, 0;\n\t@q ld.global.v2.f32 {%0, %1}, [%2];\n\t}"
+      : "+f"(a), "+f"(b)
+      : "l"(p + o), "r"((unsigned)on));
+  V2<float> x;
+  x.v[0] = a;
+  x.v[1] = b;
+  return x;
+}
+__device__ __forceinline__ V2<double> ld2p(const double* p, int o, bool on) {
+  double a = 0.0, b = 0.0;
+  asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %3, 0;\n\t@q ld.global.v2.f64 {%0, %1}, [%2];\n\t}"
+      : "+d"(a), "+d"(b)
+      : "l"(p + o), "r"((unsigned)on));
+  V2<double> x;
+  x.v[0] = a;
+  x.v[1] = b;
+  return x;
+}
 __device__ __forceinline__ V2<double> ld2p(const double* p, int64_t o, bool on) {
   double a = 0.0, b = 0.0;
   asm("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %3, 0;\n\t@q ld.global.v2.f64 {%0, %1}, [%2];\n\t}"
@@ -420,8 +442,8 @@ __device__ __forceinline__ V2<double> ld2p(const double* p, int64_t o, bool on) 
 // Store the two cells of a lane, each only where its flag is set, as three
 // independent guarded stores (a vector store when both cells are written,
 // else the single cell).
-template <typename T>
-__device__ __forceinline__ void st2p(T* p, int64_t o, const T (&x)[2], bool k0, bool k1) {
+template <typename T, typename I = int64_t>
+__device__ __forceinline__ void st2p(T* p, I o, const T (&x)[2], bool k0, bool k1) {
   if (k0 && k1) {
     V2<T> y;
     y.v[0] = x[0];
@@ -434,8 +456,8 @@ __device__ __forceinline__ void st2p(T* p, int64_t o, const T (&x)[2], bool k0, 
 
 // Two guarded scalar stores: for store masks that differ between the lanes
 // of a warp (columns at a box edge), where the vector form diverges.
-template <typename T>
-__device__ __forceinline__ void st2s(T* p, int64_t o, const T (&x)[2], bool k0, bool k1) {
+template <typename T, typename I = int64_t>
+__device__ __forceinline__ void st2s(T* p, I o, const T (&x)[2], bool k0, bool k1) {
   if (k0) p[o] = x[0];
   if (k1) p[o + 1] = x[1];
 }
@@ -1326,20 +1348,23 @@ k_el_adj3_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
 //   phase A on row a (lanes 0..31): the transposes of fw3 and fw4 at the
 //     velocity cells (D5..D8, R4 of the three-pass form, and the first rho
 //     term), and the memory adjoints g5..g8;
-//   phase B on row a-2 (needed on lanes 1..30): the stress adjoints, gathered
-//     from D5..D8 of rows a-4..a, and the transposes of fw1 and fw2 (D1..D4,
-//     the lambda / mu terms, g1..g4);
-//   phase C on row a-4 (lanes 2..29 own): the velocity adjoints, gathered from
-//     D1..D4 of rows a-6..a-2.
-// D1..D8 live in register windows instead of device memory.  A tile owns R
-// rows: phase A runs on R + 8 rows, phase B on R + 4, phase C on R.  The rho
-// accumulator is updated in phase A (its fw4 term needs R4 of rows a-1, a)
-// and the lambda / mu accumulators in phase B (their terms need rows b-1, b),
-// on the cells the warp owns, in the order the three-pass form adds them;
-// values, masks and arithmetic are those of k_el_adj1_rows .. k_el_adj3_rows.
+//   phase B on row b = a-3 (needed on lanes 1..30): the stress adjoints,
+//     gathered from D5..D8 of rows b-2..b+2, and the transposes of fw1 and
+//     fw2 (D1..D4, the lambda / mu terms, g1..g4);
+//   phase C on row t = b-3 (lanes 2..29 own): the velocity adjoints, gathered
+//     from D1..D4 of rows t-2..t+2.
+// D1..D8 go through per-warp rings of rows in shared memory instead of device
+// memory.  Every ring row a phase reads was written in an earlier iteration,
+// so the three phases of an iteration are independent of one another (one
+// __syncwarp per iteration orders the ring).  A tile owns R rows: phase A runs
+// on R + 8 rows, phase B on R + 4, phase C on R.  The rho accumulator is
+// updated in phase A (its fw4 term needs R4 of rows a-1, a) and the lambda /
+// mu accumulators in phase B (their terms need rows b-1, b), on the cells the
+// warp owns, in the order the three-pass form adds them; values, masks and
+// arithmetic are those of k_el_adj1_rows .. k_el_adj3_rows.
 // ---------------------------------------------------------------------------
 #ifndef ADS_EL_MINB_AI
-#define ADS_EL_MINB_AI 3              // resident CTAs per SM, fused adjoint of CPML-free items
+#define ADS_EL_MINB_AI 4              // resident CTAs per SM, fused adjoint of CPML-free items
 #endif
 #ifndef ADS_EL_MINB_AC
 #define ADS_EL_MINB_AC 3              // the same for items with CPML or box-edge logic
@@ -1347,6 +1372,27 @@ k_el_adj3_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
 template <typename T, int KIND>
 constexpr int el_minb_fadj() {
   return sizeof(T) != 4 ? 1 : KIND == 0 ? ADS_EL_MINB_AI : ADS_EL_MINB_AC;
+}
+// Rings of D1..D8 without their 1 / (24 h) factor (the gathers apply it once
+// to each 4-term sum): RD rows each (a phase reads up to five rows behind the
+// one written), RW elements a row (the warp's 64 columns and two on each
+// side).  On CPML-free items D5 = D6, D7 = D8 and D3 = D4 before scaling
+// (the memory-variable terms vanish), so those items keep five rings.
+template <int KIND>
+struct FRing {
+  static constexpr bool Q = KIND == 0;
+  static constexpr int d5 = 0, d6 = Q ? 0 : 1, d7 = Q ? 1 : 2, d8 = Q ? 1 : 3;
+  static constexpr int d1 = Q ? 2 : 4, d2 = Q ? 3 : 5, d3 = Q ? 4 : 6, d4 = Q ? 4 : 7;
+  static constexpr int n = Q ? 5 : 8;
+};
+#ifndef ADS_EL_FADJ_PREFETCH
+#define ADS_EL_FADJ_PREFETCH 1        // issue the next iteration's loads before the arithmetic
+#endif
+constexpr bool kFadjPrefetch = ADS_EL_FADJ_PREFETCH != 0;
+constexpr int RD = 6, RW = 68;
+template <typename T, int KIND>
+constexpr size_t el_fadj_smem() {
+  return (size_t)EW * FRing<KIND>::n * RD * RW * sizeof(T);
 }
 
 template <typename T, int KIND>
@@ -1356,6 +1402,7 @@ k_el_adj_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __re
   // KIND bit 0: rows need the box edge and x-profile logic; bit 1: columns
   // need the box edge and y-profile logic (0: neither)
   constexpr bool GR = (KIND & 1) != 0, GC = (KIND & 2) != 0;
+  extern __shared__ __align__(16) unsigned char el_smem[];
   const int wl = blockIdx.x * EW + (threadIdx.x >> 5);
   if (wl >= nwt) return;
   const int wi = wlist[wl];  // the warp's (strip, row tile)
@@ -1407,14 +1454,53 @@ k_el_adj_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __re
   T* __restrict__ g6o = sh.g[M1 + 5] + bout;
   T* __restrict__ g7o = sh.g[M1 + 6] + bout;
   T* __restrict__ g8o = sh.g[M1 + 7] + bout;
-  auto stw = [&](T* p, int64_t o, const T (&x)[2], bool k0, bool k1) {
+  // this warp's rings; ring row of row r: (r - rbase) % RD (rbase <= every row read)
+  using RG = FRing<KIND>;
+  T* const ring = reinterpret_cast<T*>(el_smem) + (threadIdx.x >> 5) * (RG::n * RD * RW) + 2;
+  // so[k]: offset of the ring row of row a - k (k < RD; row a - k - RD shares
+  // it), rotated at the end of each iteration
+  int so[RD];
+#pragma unroll
+  for (int k = 0; k < RD; k++) so[k] = ((RD + 4 - k) % RD) * RW;
+  auto rrow = [&](int g, int k) { return ring + g * (RD * RW) + so[k % RD]; };
+  // the pad columns (-2, -1, 64, 65) are read only for lanes whose results
+  // are discarded; zero them once so those stay finite
+  for (int e = lane; e < RG::n * RD * 4; e += 32) {
+    const int row = e >> 2, k = e & 3;
+    ring[row * RW + (k < 2 ? k - 2 : 62 + k)] = T(0);
+  }
+  // a lane's pair, and the pairs around it: columns jc-1..jc+2 (x[0..4] =
+  // columns j-1..j+3) and jc-2..jc+1 (x[0..4] = j-2..j+2)
+  const int le = lane * EC;
+  auto rget = [&](const T* rw) { return *reinterpret_cast<const V2<T>*>(rw + le); };
+  auto rput = [&](T* rw, const V2<T>& v) { *reinterpret_cast<V2<T>*>(rw + le) = v; };
+  auto rspan_m1 = [&](const T* rw, T (&x)[5]) {
+    x[0] = rw[le - 1];
+    const V2<T> p = *reinterpret_cast<const V2<T>*>(rw + le);
+    const V2<T> q = *reinterpret_cast<const V2<T>*>(rw + le + 2);
+    x[1] = p.v[0];
+    x[2] = p.v[1];
+    x[3] = q.v[0];
+    x[4] = q.v[1];
+  };
+  auto rspan_m2 = [&](const T* rw, T (&x)[5]) {
+    const V2<T> p = *reinterpret_cast<const V2<T>*>(rw + le - 2);
+    const V2<T> q = *reinterpret_cast<const V2<T>*>(rw + le);
+    x[0] = p.v[0];
+    x[1] = p.v[1];
+    x[2] = q.v[0];
+    x[3] = q.v[1];
+    x[4] = rw[le + 2];
+  };
+  auto stw = [&](T* p, int o, const T (&x)[2], bool k0, bool k1) {
     if constexpr (GC) {
       st2s<T>(p, o, x, k0, k1);
     } else {
       st2p(p, o, x, k0, k1);
     }
   };
-  auto off = [&](int r) { return (int64_t)r * P + j + JOFF; };
+  // offsets within a field fit 32 bits (the plan checks (NX + 2) * P < 2^31)
+  auto off = [&](int r) { return r * (int)P + j + JOFF; };
   auto ld = [&](const T* p, int r) {
     return ld2p(p, off(r), colok && r >= 0 && r <= NX + 1);
   };
@@ -1436,156 +1522,210 @@ k_el_adj_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __re
   auto rb3 = [&](int r) { return !GR || (r >= 2 && r <= NX); };
   auto rb4 = [&](int r) { return !GR || (r >= 1 && r <= NX - 1); };
   auto xp = [&](const T* p, int r, T dflt) { return GR ? p[min(max(r, 1), NX) - 1] : dflt; };
-  // windows: D5 rows a-3..a-1, D7 rows a-4..a-1, D6 / D8 rows a-2, a-1, R4 row
-  // a-1; D1 rows b-4..b-1, D3 rows b-3..b-1, D2 / D4 rows b-2, b-1, GL1 / GM1
-  // row b-1 (b = a - 2); rho rows a, a+1; lam / mu row b
-  V2<T> W5_0{}, W5_1{}, W5_2{}, W7_0{}, W7_1{}, W7_2{}, W7_3{}, W6_0{}, W6_1{}, W8_0{},
-      W8_1{}, R4p{};
-  V2<T> W1_0{}, W1_1{}, W1_2{}, W1_3{}, W3_0{}, W3_1{}, W3_2{}, W2_0{}, W2_1{}, W4_0{},
-      W4_1{}, GL1p{}, GM1p{};
+  // carried: rho rows a, a+1; lam / mu row b; R4 row a-1; GL1 / GM1 row b-1
   V2<T> R0 = ld(M.rho, i0 - 4), R1 = ld(M.rho, i0 - 3);
-  V2<T> L0 = ld(M.lam, i0 - 6), U0 = ld(M.mu, i0 - 6);
-  for (int a = i0 - 4; a <= i_end + 3; a++) {
-    const int b = a - 2, t = a - 4;
-    const bool doB = b >= i0 - 2, doC = t >= i0;
-    const bool ownA = a >= i0 && a < i_end, ownB = b >= i0 && b < i_end;  // warp-uniform
-    // ---- every load of the iteration first (predicated), so that its three
-    // phases wait for memory once
-    const int64_t oa = off(a), ob = off(b), ot = off(t);
-    const bool okA = colok && a >= 0 && a <= NX + 1;
+  V2<T> L0 = ld(M.lam, i0 - 7), U0 = ld(M.mu, i0 - 7);
+  V2<T> R4p{}, GL1p{}, GM1p{};
+  // the loads of iteration a: phase A row a, phase B row a-3, phase C row a-6
+  struct Loads {
+    V2<T> GX, GY, EA3, EA4, R2, AR, GA, GB, GCv, EA, EB, EC12, L1, U1, AL, AM, VX0, VY0;
+    V2<T> m5, m6, m7, m8, m1, m2, m3, m4;
+    T axi, bxi, axh, bxh, baxh, bbxh, baxi, bbxi;
+  };
+  auto load = [&](int a, Loads& L) {
+    const int b = a - 3, t = a - 6;
+    const bool doA = a <= i_end + 3, doB = b >= i0 - 2 && b <= i_end + 1, doC = t >= i0;
+    const bool ownA = a >= i0 && a < i_end, ownB = b >= i0 && b < i_end;
+    const int oa = off(a), ob = off(b), ot = off(t);
+    const bool okA = doA && colok && a >= 0 && a <= NX + 1;
     const bool okB = doB && colok && b >= 0 && b <= NX + 1;
-    const V2<T> GX = ld2p(gvx, oa, okA), GY = ld2p(gvy, oa, okA);
-    const V2<T> EA3 = ld2p(a3p, oa, okA), EA4 = ld2p(a4p, oa, okA);
-    const V2<T> R2 = ld(M.rho, a + 2);
-    const V2<A> AR = ld2p(accr, oa, ownA && own && colok);
-    const V2<T> GA = ld2p(gxx, ob, okB), GB = ld2p(gyy, ob, okB), GCv = ld2p(gxy, ob, okB);
-    const V2<T> EA = ld2p(e1p, ob, okB), EB = ld2p(e2p, ob, okB), EC12 = ld2p(e12p, ob, okB);
-    const V2<T> L1 = ld(M.lam, b + 1), U1 = ld(M.mu, b + 1);
-    const V2<A> AL = ld2p(accl, ob, doB && ownB && own && colok);
-    const V2<A> AM = ld2p(accm, ob, doB && ownB && own && colok);
-    const V2<T> VX0 = ld2p(gvx, ot, doC && colok), VY0 = ld2p(gvy, ot, doC && colok);
-    const T axi = xp(M.axi, a, T(0)), bxi = xp(M.bxi, a, T(1));
-    const T axh = xp(M.axh, a, T(0)), bxh = xp(M.bxh, a, T(1));
-    const T baxh = xp(M.axh, b, T(0)), bbxh = xp(M.bxh, b, T(1));
-    const T baxi = xp(M.axi, b, T(0)), bbxi = xp(M.bxi, b, T(1));
-    const bool r3 = rb3(a), r4 = rb4(a);
+    L.GX = ld2p(gvx, oa, okA);
+    L.GY = ld2p(gvy, oa, okA);
+    L.EA3 = ld2p(a3p, oa, okA);
+    L.EA4 = ld2p(a4p, oa, okA);
+    L.R2 = ld(M.rho, a + 2);
+    L.AR = ld2p(accr, oa, ownA && own && colok);
+    L.GA = ld2p(gxx, ob, okB);
+    L.GB = ld2p(gyy, ob, okB);
+    L.GCv = ld2p(gxy, ob, okB);
+    L.EA = ld2p(e1p, ob, okB);
+    L.EB = ld2p(e2p, ob, okB);
+    L.EC12 = ld2p(e12p, ob, okB);
+    L.L1 = ld(M.lam, b + 1);
+    L.U1 = ld(M.mu, b + 1);
+    L.AL = ld2p(accl, ob, ownB && own && colok);
+    L.AM = ld2p(accm, ob, ownB && own && colok);
+    L.VX0 = ld2p(gvx, ot, doC && colok);
+    L.VY0 = ld2p(gvy, ot, doC && colok);
+    L.axi = xp(M.axi, a, T(0));
+    L.bxi = xp(M.bxi, a, T(1));
+    L.axh = xp(M.axh, a, T(0));
+    L.bxh = xp(M.bxh, a, T(1));
+    L.baxh = xp(M.axh, b, T(0));
+    L.bbxh = xp(M.bxh, b, T(1));
+    L.baxi = xp(M.axi, b, T(0));
+    L.bbxi = xp(M.bxi, b, T(1));
+    const bool r3 = doA && rb3(a), r4 = doA && rb4(a);
+    const bool r1b = doB && rb4(b), r2b = doB && rb3(b);
+    const bool rx5 = GR && r3 && (L.axi != T(0) || L.bxi != T(1));
+    const bool rx7 = GR && r4 && (L.axh != T(0) || L.bxh != T(1));
+    const bool rx1 = GR && r1b && (L.baxh != T(0) || L.bbxh != T(1));
+    const bool rx3 = GR && r2b && (L.baxi != T(0) || L.bbxi != T(1));
+    L.m5 = L.m6 = L.m7 = L.m8 = L.m1 = L.m2 = L.m3 = L.m4 = V2<T>{};
+    if constexpr (GR) {
+      L.m5 = ld2p(g5i, oa, rx5 && lc3);
+      L.m7 = ld2p(g7i, oa, rx7 && lc4);
+      L.m1 = ld2p(g1i, ob, rx1 && lc3);
+      L.m3 = ld2p(g3i, ob, rx3 && lc4);
+    }
+    if constexpr (GC) {
+      L.m6 = ld2p(g6i, oa, r3 && ly3);
+      L.m8 = ld2p(g8i, oa, r4 && ly4);
+      L.m2 = ld2p(g2i, ob, r1b && ly3);
+      L.m4 = ld2p(g4i, ob, r2b && ly4);
+    }
+  };
+  // (corner items, with both row and column logic, have no registers to spare)
+  constexpr bool PF = kFadjPrefetch && KIND != 3;
+  Loads cur;
+  if (PF) load(i0 - 4, cur);
+  __syncwarp();
+  for (int a = i0 - 4; a <= i_end + 5; a++) {
+    const int b = a - 3, t = a - 6;
+    const bool doA = a <= i_end + 3, doB = b >= i0 - 2 && b <= i_end + 1, doC = t >= i0;
+    const bool ownA = a >= i0 && a < i_end, ownB = b >= i0 && b < i_end;  // warp-uniform
+    const int oa = off(a), ob = off(b), ot = off(t);
+    // this iteration's loads were issued one iteration ahead (kFadjPrefetch)
+    // or are issued now; the next iteration's go out before the arithmetic
+    Loads nxt;
+    if (PF) {
+      if (a < i_end + 5) load(a + 1, nxt);
+    } else {
+      load(a, cur);
+    }
+    const V2<T> GX = cur.GX, GY = cur.GY, EA3 = cur.EA3, EA4 = cur.EA4, R2 = cur.R2, AR = cur.AR;
+    const V2<T> GA = cur.GA, GB = cur.GB, GCv = cur.GCv, EA = cur.EA, EB = cur.EB,
+                EC12 = cur.EC12, L1 = cur.L1, U1 = cur.U1, AL = cur.AL, AM = cur.AM;
+    const V2<T> VX0 = cur.VX0, VY0 = cur.VY0;
+    const V2<T> m5 = cur.m5, m6 = cur.m6, m7 = cur.m7, m8 = cur.m8, m1 = cur.m1, m2 = cur.m2,
+                m3 = cur.m3, m4 = cur.m4;
+    const T axi = cur.axi, bxi = cur.bxi, axh = cur.axh, bxh = cur.bxh;
+    const T baxh = cur.baxh, bbxh = cur.bbxh, baxi = cur.baxi, bbxi = cur.bbxi;
+    const bool r3 = doA && rb3(a), r4 = doA && rb4(a);
     const bool rx5 = GR && r3 && (axi != T(0) || bxi != T(1));
     const bool rx7 = GR && r4 && (axh != T(0) || bxh != T(1));
     const bool r1b = doB && rb4(b), r2b = doB && rb3(b);
     const bool rx1 = GR && r1b && (baxh != T(0) || bbxh != T(1));
     const bool rx3 = GR && r2b && (baxi != T(0) || bbxi != T(1));
-    V2<T> m5{}, m6{}, m7{}, m8{}, m1{}, m2{}, m3{}, m4{};
-    if constexpr (GR) {
-      m5 = ld2p(g5i, oa, rx5 && lc3);
-      m7 = ld2p(g7i, oa, rx7 && lc4);
-      m1 = ld2p(g1i, ob, rx1 && lc3);
-      m3 = ld2p(g3i, ob, rx3 && lc4);
-    }
-    if constexpr (GC) {
-      m6 = ld2p(g6i, oa, r3 && ly3);
-      m8 = ld2p(g8i, oa, r4 && ly4);
-      m2 = ld2p(g2i, ob, r1b && ly3);
-      m4 = ld2p(g4i, ob, r2b && ly4);
-    }
     // ================= phase A: row a
-    T r0[3], r1[3];
-    r0[0] = R0.v[0];
-    r0[1] = R0.v[1];
-    r0[2] = shdn(R0.v[0]);
-    r1[0] = R1.v[0];
-    r1[1] = R1.v[1];
-    r1[2] = shdn(R1.v[0]);
-    V2<T> D5n, D6n, D7n, D8n, R4n;
-    T sg5[2], sg6[2], sg7[2], sg8[2], grt[2];
-    bool k3[2], w5[2], w6[2], w7[2], w8[2];
-#pragma unroll
-    for (int c = 0; c < 2; c++) {
-      k3[c] = r3 && c3[c];
-      const bool k4 = r4 && c4[c];
-      // fw3 transpose
-      const T gv = GX.v[c], r = r0[c];
-      const T q = divr<T>(gv * M.dt, r);
-      const bool u5 = k3[c] && rx5, u6 = GC && k3[c] && Y.acti[c];
-      const T gm5 = u5 ? q + m5.v[c] : q;
-      const T gm6 = u6 ? q + m6.v[c] : q;
-      sg5[c] = bxi * gm5;
-      sg6[c] = Y.bi[c] * gm6;
-      w5[c] = u5;
-      w6[c] = u6;
-      D5n.v[c] = k3[c] ? hdiv<T>(q + axi * gm5, M.hx24, M.rhx24) : T(0);
-      D6n.v[c] = k3[c] ? hdiv<T>(q + (GC ? Y.ai[c] : T(0)) * gm6, M.hy24, M.rhy24) : T(0);
-      grt[c] = divr<T>(-gv * EA3.v[c] * M.dt, r * r);
-      // fw4 transpose
-      const T gw = GY.v[c];
-      const T rho_ = T(0.25) * (r0[c] + r1[c] + r1[c + 1] + r0[c + 1]);
-      const T q4 = divr<T>(gw * M.dt, rho_);
-      const bool u7 = k4 && rx7, u8 = GC && k4 && Y.acth[c];
-      const T gm7 = u7 ? q4 + m7.v[c] : q4;
-      const T gm8 = u8 ? q4 + m8.v[c] : q4;
-      sg7[c] = bxh * gm7;
-      sg8[c] = Y.bh[c] * gm8;
-      w7[c] = u7;
-      w8[c] = u8;
-      D7n.v[c] = k4 ? hdiv<T>(q4 + axh * gm7, M.hx24, M.rhx24) : T(0);
-      D8n.v[c] = k4 ? hdiv<T>(q4 + (GC ? Y.ah[c] : T(0)) * gm8, M.hy24, M.rhy24) : T(0);
-      R4n.v[c] = k4 ? divr<T>(-gw * EA4.v[c] * M.dt, rho_ * rho_) * T(0.25) : T(0);
-    }
     {
+      T r0[3], r1[3];
+      r0[0] = R0.v[0];
+      r0[1] = R0.v[1];
+      r0[2] = shdn(R0.v[0]);
+      r1[0] = R1.v[0];
+      r1[1] = R1.v[1];
+      r1[2] = shdn(R1.v[0]);
+      V2<T> D5n, D6n, D7n, D8n, R4n;
+      T sg5[2], sg6[2], sg7[2], sg8[2], grt[2];
+      bool k3[2], w5[2], w6[2], w7[2], w8[2];
+#pragma unroll
+      for (int c = 0; c < 2; c++) {
+        k3[c] = r3 && c3[c];
+        const bool k4 = r4 && c4[c];
+        // fw3 transpose
+        const T gv = GX.v[c], r = r0[c];
+        const T q = divr<T>(gv * M.dt, r);
+        const bool u5 = k3[c] && rx5, u6 = GC && k3[c] && Y.acti[c];
+        const T gm5 = u5 ? q + m5.v[c] : q;
+        const T gm6 = u6 ? q + m6.v[c] : q;
+        sg5[c] = bxi * gm5;
+        sg6[c] = Y.bi[c] * gm6;
+        w5[c] = u5;
+        w6[c] = u6;
+        D5n.v[c] = k3[c] ? (GR ? q + axi * gm5 : q) : T(0);
+        D6n.v[c] = k3[c] ? (GC ? q + Y.ai[c] * gm6 : q) : T(0);
+        grt[c] = divr<T>(-gv * EA3.v[c] * M.dt, r * r);
+        // fw4 transpose
+        const T gw = GY.v[c];
+        const T rho_ = T(0.25) * (r0[c] + r1[c] + r1[c + 1] + r0[c + 1]);
+        const T q4 = divr<T>(gw * M.dt, rho_);
+        const bool u7 = k4 && rx7, u8 = GC && k4 && Y.acth[c];
+        const T gm7 = u7 ? q4 + m7.v[c] : q4;
+        const T gm8 = u8 ? q4 + m8.v[c] : q4;
+        sg7[c] = bxh * gm7;
+        sg8[c] = Y.bh[c] * gm8;
+        w7[c] = u7;
+        w8[c] = u8;
+        D7n.v[c] = k4 ? (GR ? q4 + axh * gm7 : q4) : T(0);
+        D8n.v[c] = k4 ? (GC ? q4 + Y.ah[c] * gm8 : q4) : T(0);
+        R4n.v[c] = k4 ? divr<T>(-gw * EA4.v[c] * M.dt, rho_ * rho_) * T(0.25) : T(0);
+      }
+      if (doA) {
+        rput(rrow(RG::d5, 0), D5n);
+        rput(rrow(RG::d7, 0), D7n);
+        if constexpr (!RG::Q) {
+          rput(rrow(RG::d6, 0), D6n);
+          rput(rrow(RG::d8, 0), D8n);
+        }
+      }
       // R4 of rows a and a-1 at columns jc-1, jc
-      T rs[3], rp[3];
+      T rs[3], rq[3];
       rs[0] = shup(R4n.v[1]);
       rs[1] = R4n.v[0];
       rs[2] = R4n.v[1];
-      rp[0] = shup(R4p.v[1]);
-      rp[1] = R4p.v[0];
-      rp[2] = R4p.v[1];
-      if (ownA) {
+      rq[0] = shup(R4p.v[1]);
+      rq[1] = R4p.v[0];
+      rq[2] = R4p.v[1];
+      if (ownA && own) {
         A orr[2];
 #pragma unroll
         for (int c = 0; c < 2; c++)
-          orr[c] = (k3[c] ? AR.v[c] + grt[c] : AR.v[c]) + (rs[1 + c] + rp[1 + c] + rp[c] + rs[c]);
-        if (own) {
-          stw(accr, oa, orr, cp[0], cp[1]);
-          if constexpr (GR) {
-            stw(g5o, oa, sg5, w5[0], w5[1]);
-            stw(g7o, oa, sg7, w7[0], w7[1]);
-          }
-          if constexpr (GC) {
-            stw(g6o, oa, sg6, w6[0], w6[1]);
-            stw(g8o, oa, sg8, w8[0], w8[1]);
-          }
+          orr[c] = (k3[c] ? AR.v[c] + grt[c] : AR.v[c]) + (rs[1 + c] + rq[1 + c] + rq[c] + rs[c]);
+        stw(accr, oa, orr, cp[0], cp[1]);
+        if constexpr (GR) {
+          stw(g5o, oa, sg5, w5[0], w5[1]);
+          stw(g7o, oa, sg7, w7[0], w7[1]);
+        }
+        if constexpr (GC) {
+          stw(g6o, oa, sg6, w6[0], w6[1]);
+          stw(g8o, oa, sg8, w8[0], w8[1]);
         }
       }
+      R4p = R4n;
     }
     // ================= phase B: row b
-    V2<T> D1n{}, D2n{}, D3n{}, D4n{}, GL1n{}, GM1n{};
     if (doB) {
-      // row b across columns: D6 at jc-1..jc+2, D8 at jc-2..jc+1, mu at jc..jc+1
+      // D5 rows b-1..b+2, D7 rows b-2..b+1 (this column); row b across
+      // columns: D6 at jc-1..jc+2, D8 at jc-2..jc+1, mu at jc..jc+1
+      const V2<T> P0 = rget(rrow(RG::d5, 4)), P1 = rget(rrow(RG::d5, 3)),
+                  P2 = rget(rrow(RG::d5, 2)), P3 = rget(rrow(RG::d5, 1));
+      const V2<T> Q0 = rget(rrow(RG::d7, 5)), Q1 = rget(rrow(RG::d7, 4)),
+                  Q2 = rget(rrow(RG::d7, 3)), Q3 = rget(rrow(RG::d7, 2));
       T f6[5], f8[5], ur[3];
-      f6[0] = shup(W6_0.v[1]);
-      f6[1] = W6_0.v[0];
-      f6[2] = W6_0.v[1];
-      f6[3] = shdn(W6_0.v[0]);
-      f6[4] = shdn(W6_0.v[1]);
-      f8[0] = shup(W8_0.v[0]);
-      f8[1] = shup(W8_0.v[1]);
-      f8[2] = W8_0.v[0];
-      f8[3] = W8_0.v[1];
-      f8[4] = shdn(W8_0.v[0]);
+      rspan_m1(rrow(RG::d6, 3), f6);
+      rspan_m2(rrow(RG::d8, 3), f8);
       ur[0] = U0.v[0];
       ur[1] = U0.v[1];
       ur[2] = shdn(U0.v[0]);
+      V2<T> D1n, D2n, D3n, D4n, GL1n, GM1n;
       T oxx[2], oyy[2], oxy[2], sg1[2], sg2[2], sg3[2], sg4[2], gm2v[2];
       bool k12[2], w1[2], w2[2], w3[2], w4[2];
 #pragma unroll
       for (int c = 0; c < 2; c++) {
         const bool b1 = r1b && c3[c], b2 = r2b && c4[c];
         k12[c] = b1 || b2;
-        // gathers: D5 rows b-1..b+2, D7 rows b-2..b+1
-        const T gsxx = GA.v[c] + T(27) * W5_1.v[c] - T(27) * W5_2.v[c] - W5_0.v[c] + D5n.v[c];
-        const T gsyy = GB.v[c] + T(27) * f8[1 + c] - T(27) * f8[2 + c] - f8[c] + f8[3 + c];
-        const T gsxy = GCv.v[c] + T(27) * f6[1 + c] - T(27) * f6[2 + c] - f6[c] + f6[3 + c] +
-                       T(27) * W7_1.v[c] - T(27) * W7_2.v[c] - W7_0.v[c] + W7_3.v[c];
+        const T gsxx =
+            GA.v[c] + hdiv<T>(T(27) * P1.v[c] - T(27) * P2.v[c] - P0.v[c] + P3.v[c], M.hx24,
+                              M.rhx24);
+        const T gsyy =
+            GB.v[c] + hdiv<T>(T(27) * f8[1 + c] - T(27) * f8[2 + c] - f8[c] + f8[3 + c], M.hy24,
+                              M.rhy24);
+        const T gsxy =
+            GCv.v[c] +
+            hdiv<T>(T(27) * f6[1 + c] - T(27) * f6[2 + c] - f6[c] + f6[3 + c], M.hy24,
+                    M.rhy24) +
+            hdiv<T>(T(27) * Q1.v[c] - T(27) * Q2.v[c] - Q0.v[c] + Q3.v[c], M.hx24, M.rhx24);
         oxx[c] = gsxx;
         oyy[c] = gsyy;
         oxy[c] = gsxy;
@@ -1607,8 +1747,8 @@ k_el_adj_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __re
         w2[c] = u2;
         GL1n.v[c] = b1 ? T(0.5) * glam : T(0);
         GM1n.v[c] = b1 ? glm : T(0);
-        D1n.v[c] = b1 ? hdiv<T>(gE1 + baxh * gm1, M.hx24, M.rhx24) : T(0);
-        D2n.v[c] = b1 ? hdiv<T>(gE2 + (GC ? Y.ai[c] : T(0)) * gm2, M.hy24, M.rhy24) : T(0);
+        D1n.v[c] = b1 ? (GR ? gE1 + baxh * gm1 : gE1) : T(0);
+        D2n.v[c] = b1 ? (GC ? gE2 + Y.ai[c] * gm2 : gE2) : T(0);
         // fw2 transpose
         const T mu2 = T(0.5) * (ur[c] + ur[c + 1]);
         const T q = gsxy * mu2 * M.dt;
@@ -1619,53 +1759,54 @@ k_el_adj_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __re
         sg4[c] = Y.bh[c] * gm4;
         w3[c] = u3;
         w4[c] = u4;
-        D3n.v[c] = b2 ? hdiv<T>(q + baxi * gm3, M.hx24, M.rhx24) : T(0);
-        D4n.v[c] = b2 ? hdiv<T>(q + (GC ? Y.ah[c] : T(0)) * gm4, M.hy24, M.rhy24) : T(0);
+        D3n.v[c] = b2 ? (GR ? q + baxi * gm3 : q) : T(0);
+        D4n.v[c] = b2 ? (GC ? q + Y.ah[c] * gm4 : q) : T(0);
         gm2v[c] = b2 ? gsxy * EC12.v[c] * M.dt * T(0.5) : T(0);  // GM2, the sxy term of mu
       }
+      rput(rrow(RG::d1, 3), D1n);
+      rput(rrow(RG::d2, 3), D2n);
+      rput(rrow(RG::d3, 3), D3n);
+      if constexpr (!RG::Q) rput(rrow(RG::d4, 3), D4n);
       // GM2 of row b at columns jc-1, jc
       T g12[3];
       g12[1] = gm2v[0];
       g12[2] = gm2v[1];
       g12[0] = shup(g12[2]);
-      if (ownB) {
+      if (ownB && own) {
         A ol[2], om[2];
 #pragma unroll
         for (int c = 0; c < 2; c++) {
           ol[c] = AL.v[c] + (GL1n.v[c] + GL1p.v[c]);
           om[c] = AM.v[c] + (GM1n.v[c] + GM1p.v[c] + g12[1 + c] + g12[c]);
         }
-        if (own) {
-          stw(oxxp, ob, oxx, k12[0], k12[1]);
-          stw(oyyp, ob, oyy, k12[0], k12[1]);
-          stw(oxyp, ob, oxy, k12[0], k12[1]);
-          stw(accl, ob, ol, cp[0], cp[1]);
-          stw(accm, ob, om, cp[0], cp[1]);
-          if constexpr (GR) {
-            stw(g1o, ob, sg1, w1[0], w1[1]);
-            stw(g3o, ob, sg3, w3[0], w3[1]);
-          }
-          if constexpr (GC) {
-            stw(g2o, ob, sg2, w2[0], w2[1]);
-            stw(g4o, ob, sg4, w4[0], w4[1]);
-          }
+        stw(oxxp, ob, oxx, k12[0], k12[1]);
+        stw(oyyp, ob, oyy, k12[0], k12[1]);
+        stw(oxyp, ob, oxy, k12[0], k12[1]);
+        stw(accl, ob, ol, cp[0], cp[1]);
+        stw(accm, ob, om, cp[0], cp[1]);
+        if constexpr (GR) {
+          stw(g1o, ob, sg1, w1[0], w1[1]);
+          stw(g3o, ob, sg3, w3[0], w3[1]);
+        }
+        if constexpr (GC) {
+          stw(g2o, ob, sg2, w2[0], w2[1]);
+          stw(g4o, ob, sg4, w4[0], w4[1]);
         }
       }
+      GL1p = GL1n;
+      GM1p = GM1n;
     }
     // ================= phase C: row t
     if (doC) {
-      // row t across columns: D4 at jc-2..jc+1, D2 at jc-1..jc+2
+      // D1 rows t-2..t+1, D3 rows t-1..t+2 (this column); row t across
+      // columns: D4 at jc-2..jc+1, D2 at jc-1..jc+2
+      const V2<T> P0 = rget(rrow(RG::d1, 8)), P1 = rget(rrow(RG::d1, 7)),
+                  P2 = rget(rrow(RG::d1, 6)), P3 = rget(rrow(RG::d1, 5));
+      const V2<T> Q0 = rget(rrow(RG::d3, 7)), Q1 = rget(rrow(RG::d3, 6)),
+                  Q2 = rget(rrow(RG::d3, 5)), Q3 = rget(rrow(RG::d3, 4));
       T f4[5], f2[5];
-      f4[0] = shup(W4_0.v[0]);
-      f4[1] = shup(W4_0.v[1]);
-      f4[2] = W4_0.v[0];
-      f4[3] = W4_0.v[1];
-      f4[4] = shdn(W4_0.v[0]);
-      f2[0] = shup(W2_0.v[1]);
-      f2[1] = W2_0.v[0];
-      f2[2] = W2_0.v[1];
-      f2[3] = shdn(W2_0.v[0]);
-      f2[4] = shdn(W2_0.v[1]);
+      rspan_m2(rrow(RG::d4, 6), f4);
+      rspan_m1(rrow(RG::d2, 6), f2);
       const bool r3t = rb3(t), r4t = rb4(t);
       T ovx[2], ovy[2];
       bool k3t[2], k4t[2];
@@ -1673,29 +1814,34 @@ k_el_adj_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __re
       for (int c = 0; c < 2; c++) {
         k3t[c] = r3t && c3[c];
         k4t[c] = r4t && c4[c];
-        // D1 rows t-2..t+1, D3 rows t-1..t+2
-        ovx[c] = VX0.v[c] + (T(27) * W1_1.v[c] - T(27) * W1_2.v[c] - W1_0.v[c] + W1_3.v[c] +
-                             T(27) * f4[1 + c] - T(27) * f4[2 + c] - f4[c] + f4[3 + c]);
-        ovy[c] = VY0.v[c] + (T(27) * f2[1 + c] - T(27) * f2[2 + c] - f2[c] + f2[3 + c] +
-                             T(27) * W3_1.v[c] - T(27) * W3_2.v[c] - W3_0.v[c] + D3n.v[c]);
+        ovx[c] = VX0.v[c] +
+                 (hdiv<T>(T(27) * P1.v[c] - T(27) * P2.v[c] - P0.v[c] + P3.v[c], M.hx24,
+                          M.rhx24) +
+                  hdiv<T>(T(27) * f4[1 + c] - T(27) * f4[2 + c] - f4[c] + f4[3 + c], M.hy24,
+                          M.rhy24));
+        ovy[c] = VY0.v[c] +
+                 (hdiv<T>(T(27) * f2[1 + c] - T(27) * f2[2 + c] - f2[c] + f2[3 + c], M.hy24,
+                          M.rhy24) +
+                  hdiv<T>(T(27) * Q1.v[c] - T(27) * Q2.v[c] - Q0.v[c] + Q3.v[c], M.hx24,
+                          M.rhx24));
       }
       if (own) {
         stw(ovxp, ot, ovx, k3t[0], k3t[1]);
         stw(ovyp, ot, ovy, k4t[0], k4t[1]);
       }
     }
-    W5_0 = W5_1; W5_1 = W5_2; W5_2 = D5n;
-    W7_0 = W7_1; W7_1 = W7_2; W7_2 = W7_3; W7_3 = D7n;
-    W6_0 = W6_1; W6_1 = D6n;
-    W8_0 = W8_1; W8_1 = D8n;
-    R4p = R4n;
-    W1_0 = W1_1; W1_1 = W1_2; W1_2 = W1_3; W1_3 = D1n;
-    W3_0 = W3_1; W3_1 = W3_2; W3_2 = D3n;
-    W2_0 = W2_1; W2_1 = D2n;
-    W4_0 = W4_1; W4_1 = D4n;
-    GL1p = GL1n; GM1p = GM1n;
-    R0 = R1; R1 = R2;
-    L0 = L1; U0 = U1;
+    __syncwarp();  // this iteration's ring rows before the next one reads them
+    {
+      const int s5 = so[RD - 1];
+#pragma unroll
+      for (int k = RD - 1; k > 0; k--) so[k] = so[k - 1];
+      so[0] = s5;
+    }
+    R0 = R1;
+    R1 = R2;
+    L0 = L1;
+    U0 = U1;
+    if (PF) cur = nxt;
   }
 }
 
@@ -1991,8 +2137,9 @@ void el_step(bool store, int kind, dim3 g, cudaStream_t s, const ElModel<T>& M,
 template <typename T>
 void el_fadj(int kind, dim3 g, cudaStream_t s, const ElModel<T>& M, const ElShot<T>* sh,
              const int* wl, int ncolw, int R, int nw, int slot, int pin, int jsh, int ish) {
-#define ADS_K(KD) \
-  k_el_adj_rows<T, KD><<<g, EW * 32, 0, s>>>(M, sh, wl, ncolw, R, nw, slot, pin, jsh, ish)
+#define ADS_K(KD)                                                                      \
+  k_el_adj_rows<T, KD><<<g, EW * 32, el_fadj_smem<T, KD>(), s>>>(M, sh, wl, ncolw, R, nw, slot, \
+                                                            pin, jsh, ish)
   switch (kind) {
     case 0: ADS_K(0); break;
     case 1: ADS_K(1); break;
@@ -2000,6 +2147,21 @@ void el_fadj(int kind, dim3 g, cudaStream_t s, const ElModel<T>& M, const ElShot
     default: ADS_K(3); break;
   }
 #undef ADS_K
+}
+
+// The fused adjoint's rings take more than the default 48 KB of dynamic
+// shared memory a CTA.
+template <typename T>
+int el_fadj_prepare() {
+  ADS_CUDA(cudaFuncSetAttribute(k_el_adj_rows<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)el_fadj_smem<T, 0>()));
+  ADS_CUDA(cudaFuncSetAttribute(k_el_adj_rows<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)el_fadj_smem<T, 1>()));
+  ADS_CUDA(cudaFuncSetAttribute(k_el_adj_rows<T, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)el_fadj_smem<T, 2>()));
+  ADS_CUDA(cudaFuncSetAttribute(k_el_adj_rows<T, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)el_fadj_smem<T, 3>()));
+  return ADS_OK;
 }
 
 // ======================================================================
@@ -2185,7 +2347,13 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   ADS_REQUIRE(c.ckpt_every >= 0, "negative ckpt_every");
   ADS_REQUIRE(c.adjoint_passes == 0 || c.adjoint_passes == 1 || c.adjoint_passes == 3,
               "adjoint_passes must be 0, 1 or 3");
-  fused = c.adjoint_passes != 3;
+  // automatic (0): the fused adjoint for FP32 plans, the three passes for FP64
+  // plans (their fused kernel runs out of registers: measured 1.5x slower);
+  // the fused adjoint indexes a field with 32-bit offsets
+  fused = (c.adjoint_passes == 1 || (c.adjoint_passes == 0 && sizeof(T) == 4)) &&
+          (int64_t)(c.NX + 2) * grid_pitch(c.NY) < (int64_t(1) << 31);
+  if (fused)
+    if (int e = el_fadj_prepare<T>()) return e;
   nshots = (int)ns;
   max_rcv = 0;
   for (int64_t s = 0; s < ns; s++) max_rcv = std::max<int>(max_rcv, (int)shots[s].nrcv);

@@ -139,13 +139,14 @@ class ElasticPlan:
     free device memory).  source_gradient: the reverse sweep also records
     d loss / d srcv (gradient(..., want_source_grad=True)); the plan then
     rejects (AdsError) sources on the padded frame, the cells the stencil of
-    their field does not update.  adjoint_passes: 1 (default) runs each
-    adjoint step as one fused pass, 3 as the three gather passes."""
+    their field does not update.  adjoint_passes: 1 runs each adjoint step
+    as one fused pass, 3 as the three gather passes, 0 (default) the fused
+    pass for FP32 plans and the three passes for FP64 plans."""
 
     def __init__(self, param: ElasticPropagatorParams, shots, precision="f64",
                  use_graph=True, ckpt_every=0, stream=None, rows_per_warp=0,
                  resident_segments=0, resident_mem_pct=0, source_gradient=False,
-                 autotune=False, adjoint_passes=1):
+                 autotune=False, adjoint_passes=0):
         cfg = _lib.ElasticConfig()
         cfg.NX, cfg.NY, cfg.NSTEP = param.NX, param.NY, param.NSTEP
         cfg.dx, cfg.dy, cfg.dt = param.DELTAX, param.DELTAY, param.DELTAT

@@ -325,7 +325,7 @@ def elastic_workload(ads, nshots=32, T=4000):
 
 
 def elastic_measure(steps, warmup, nshots=32, T=4000, with_rel_err=True, autotune=True,
-                    adjoint_passes=1):
+                    adjoint_passes=0):
     """Elastic CPML FWI gradient w.r.t. lambda, mu, rho (C4): 600x300 incl. CPML
     30, T steps, FP32 stencils with FP64 accumulation, explosive shots (sigma_xx
     and sigma_yy, 10 Hz Ricker), 300 two-component receivers.  Returns the
@@ -349,28 +349,35 @@ def elastic_measure(steps, warmup, nshots=32, T=4000, with_rel_err=True, autotun
     cells = 2 * n * p.NX * p.NY * p.NSTEP
     # roofline: algorithmic bytes per cell-update, forward (13 + 16 f_pml) x 4 B
     # (5 fields read + written, lambda / mu / rho, 8 memory variables in CPML
-    # cells), adjoint step = forward + 68 B
+    # cells); the forward step that stores the adjoint's inputs writes 5 more
+    # fields (+20 B); adjoint step = forward + 20 B (the stored strains and
+    # accelerations) + 24 B (the FP32 lambda / mu / rho partials, read and
+    # written)
     f_pml = 1 - (p.NX - 2 * p.NPOINTS_PML) * (p.NY - 2 * p.NPOINTS_PML) / (p.NX * p.NY)
     b_fwd = (13 + 16 * f_pml) * 4
-    b_adj = b_fwd + 68
+    b_adj = b_fwd + 20 + 24
     prof = plan.profile(l0, m0, r0)
     peak, peak_kind = measured_peak()
-    fwd_ms = prof["step"][0]
+    fwd_ms, st_ms = prof["step"][0], prof["step_store"][0]
     adj_ms = prof["adj1"][0] + prof["adj2"][0] + prof["adj3"][0]
     c1 = prof["step"][1]
+    adj_name = ("k_el_adj_rows" if prof["adj2"][0] == 0 else
+                "k_el_adj1_rows+k_el_adj2_rows+k_el_adj3_rows")
     groups = {
         "k_el_step_rows": (fwd_ms, b_fwd * c1),
-        "k_el_adj1_rows+k_el_adj2_rows+k_el_adj3_rows": (adj_ms, b_adj * c1),
+        "k_el_step_rows (storing)": (st_ms, (b_fwd + 20) * c1),
+        adj_name: (adj_ms, b_adj * c1),
     }
     kern = {k: {"ms_per_step": round(tt, 4), "achieved_gbs": round(b / (tt / 1e3) / 1e9, 1),
                 "frac": round(b / (tt / 1e3) / 1e9 / peak, 4)} for k, (tt, b) in groups.items()}
     kern.update({k: {"ms_per_launch": round(v[0], 4)} for k, v in prof.items()})
-    dom = "k_el_adj1_rows+k_el_adj2_rows+k_el_adj3_rows"
+    dom = adj_name
     tt, b = groups[dom]
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(b / (tt / 1e3) / 1e9, 1),
                 "peak": peak, "unit": "GB/s", "frac": round(b / (tt / 1e3) / 1e9 / peak, 4),
                 "peak_source": peak_kind, "traffic": None, "bytes_per_launch": b,
-                "bytes_per_cell": {"forward": b_fwd, "adjoint": b_adj, "f_pml": round(f_pml, 4)},
+                "bytes_per_cell": {"forward": round(b_fwd, 2), "forward_storing": round(b_fwd + 20, 2),
+                                   "adjoint": round(b_adj, 2), "f_pml": round(f_pml, 4)},
                 "kernels": kern}
     out = {"value": n / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": steps,
            "warmup": warmup, "dtype": "f32",
@@ -519,7 +526,7 @@ def main():
     ap.add_argument("--no-elastic", action="store_true")
     ap.add_argument("--no-elastic-autotune", action="store_true")
     ap.add_argument("--no-configs", action="store_true")
-    ap.add_argument("--elastic-adjoint-passes", type=int, default=1, choices=(1, 3))
+    ap.add_argument("--elastic-adjoint-passes", type=int, default=0, choices=(0, 1, 3))
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -411,10 +411,12 @@ typedef struct ads_elastic_config {
   int32_t autotune;          /* 1: time candidate row heights of the fused step and of the
                                 adjoint at plan creation and keep the fastest
                                 (ignored when rows_per_warp is set) */
-  int32_t adjoint_passes;    /* the reverse sweep's adjoint step: 0 or 1 = one fused
+  int32_t adjoint_passes;    /* the reverse sweep's adjoint step: 1 = one fused
                                 row-streaming pass (two adjoint state buffers, no
-                                intermediate fields in device memory); 3 = three gather
-                                passes over intermediate fields, in place */
+                                intermediate fields in device memory; fields of fewer
+                                than 2^31 elements, else 3); 3 = three gather passes
+                                over intermediate fields, in place; 0 = 1 for FP32
+                                plans, 3 for FP64 plans */
   int32_t reserved[3];
 } ads_elastic_config;
 

@@ -121,7 +121,9 @@ def test_autotuned_plan_vs_oracle(ads, cuda, precision, tol):
     g = golden("elastic_small.npz")
     p = params(ads, g)
     plan = ads.ElasticPlan(p, shots_from(g), precision=precision, ckpt_every=17, autotune=True)
-    assert plan.rows_per_warp in (12, 16, 20, 24, 32) and plan.rows_per_tile in (12, 16, 20, 24)
+    # adjoint tile heights (fused, FP32) or strip heights (three passes, FP64)
+    assert plan.rows_per_warp in (6, 8, 12, 16, 20, 24, 32)
+    assert plan.rows_per_tile in (12, 16, 20, 24)
     t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=cuda)
     loss, gl, gm, gr = plan.gradient(t(g["lam"]), t(g["mu"]), t(g["rho"]),
                                      t(g["obs"].reshape(-1)))
@@ -390,8 +392,8 @@ def test_fused_adjoint_all_item_kinds_vs_oracle_and_three_passes(ads, orc, cuda,
     four kinds (CPML-free, x-CPML rows, y-CPML columns, both), two shots, an
     odd checkpoint interval and two resident segments: against the oracle
     (FP64 1e-12, FP32 1e-4) and against the three gather passes on the same
-    plan geometry (FP64 1e-13, FP32 1e-6: the same arithmetic in the same
-    order)."""
+    plan geometry (FP64 1e-13, FP32 1e-5: the same terms, with the 1 / (24 h)
+    factor of each gather applied to its 4-term sum instead of to each term)."""
     NX, NY, T = 150, 190, 33
     p = ads.ElasticPropagatorParams(NX=NX, NY=NY, NSTEP=T, DELTAX=10.0, DELTAY=12.0,
                                     DELTAT=0.8e-3, NPOINTS_PML=10, vp_ref=3000.0, f0=15.0)
@@ -436,7 +438,7 @@ def test_fused_adjoint_all_item_kinds_vs_oracle_and_three_passes(ads, orc, cuda,
         out[passes] = [float(loss)] + [a.cpu().numpy() for a in (gl, gm, gr)]
         plan.close()
     f, s3 = out[1], out[3]
-    tol3 = 1e-13 if precision == "f64" else 1e-6
+    tol3 = 1e-13 if precision == "f64" else 1e-5
     assert abs(f[0] - s3[0]) <= tol3 * abs(s3[0])
     for a, b in zip(f[1:], s3[1:]):
         assert rel(a, b) <= tol3
