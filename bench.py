@@ -325,7 +325,7 @@ def elastic_workload(ads, nshots=32, T=4000):
 
 
 def elastic_measure(steps, warmup, nshots=32, T=4000, with_rel_err=True, autotune=True,
-                    adjoint_passes=0):
+                    adjoint_passes=0, ckpt_every=100, resident_pct=92):
     """Elastic CPML FWI gradient w.r.t. lambda, mu, rho (C4): 600x300 incl. CPML
     30, T steps, FP32 stencils with FP64 accumulation, explosive shots (sigma_xx
     and sigma_yy, 10 Hz Ricker), 300 two-component receivers.  Returns the
@@ -340,8 +340,10 @@ def elastic_measure(steps, warmup, nshots=32, T=4000, with_rel_err=True, autotun
     t = lambda a: torch.tensor(a.reshape(-1), device="cuda")
     # the last checkpoint segments' adjoint inputs stay resident in HBM (up to
     # 92% of the memory free after the plan's other buffers)
-    plan = ads.ElasticPlan(p, shots, precision="f32", ckpt_every=100, resident_mem_pct=92,
-                           autotune=autotune, adjoint_passes=adjoint_passes)
+    plan = ads.ElasticPlan(p, shots, precision="f32", ckpt_every=ckpt_every,
+                           resident_segments=-1 if resident_pct < 0 else 0,
+                           resident_mem_pct=max(resident_pct, 0), autotune=autotune,
+                           adjoint_passes=adjoint_passes)
     obs = plan.forward(t(lam), t(mu), t(rho)).clone()
     l0, m0, r0 = (t(a) for a in configs.c4_start_model(lam, mu, rho))
     ms = _timed(lambda: plan.gradient(l0, m0, r0, obs), steps, warmup)
@@ -383,8 +385,8 @@ def elastic_measure(steps, warmup, nshots=32, T=4000, with_rel_err=True, autotun
            "warmup": warmup, "dtype": "f32",
            "workload": f"elastic CPML gradient {p.NX}x{p.NY} (CPML {p.NPOINTS_PML}), "
                        f"{p.NSTEP} steps, {n} explosive shots x 300 two-component receivers, "
-                       f"checkpoints every 100, the last {plan.resident_segments} of "
-                       f"{-(-p.NSTEP // 100)} segments resident in HBM",
+                       f"checkpoints every {ckpt_every}, the last {plan.resident_segments} of "
+                       f"{-(-p.NSTEP // ckpt_every)} segments resident in HBM",
            "gcell_updates_per_s": cells / (ms / 1e3) / 1e9, "roofline": roofline,
            "device_bytes": plan.device_bytes, "gpu_launches": int(plan.launches_gradient),
            "tiling": {"rows_per_adjoint_strip": plan.rows_per_warp,
@@ -468,12 +470,13 @@ def run_elastic_fwi(args):
     nshots = args.shots if args.shots != 64 else 32
     T = args.nstep if args.nstep != 3000 else 4000
     r = elastic_measure(args.steps, args.warmup, nshots=nshots, T=T,
-                        autotune=not args.no_elastic_autotune,
-                        adjoint_passes=args.elastic_adjoint_passes)
+                        with_rel_err=not args.no_fp64, autotune=not args.no_elastic_autotune,
+                        adjoint_passes=args.elastic_adjoint_passes,
+                        ckpt_every=args.ckpt_every, resident_pct=args.resident_pct)
     _line("elastic FWI shot-gradients/s (FP32 stencils, FP64 accumulation)", r["value"],
           "shot-gradients/s", args, r["ms_per_step"], "f32", r["workload"],
           {k: r[k] for k in ("gcell_updates_per_s", "roofline", "device_bytes", "gpu_launches",
-                             "rel_err", "tiling")})
+                             "rel_err", "tiling") if k in r})
 
 
 def measure_c5(steps, warmup, nshots=128):
@@ -527,6 +530,11 @@ def main():
     ap.add_argument("--no-elastic-autotune", action="store_true")
     ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--elastic-adjoint-passes", type=int, default=0, choices=(0, 1, 3))
+    # elastic-fwi workload only: checkpoint interval and the resident share of
+    # the free device memory in percent (-1: no resident segments), for small
+    # profiler captures
+    ap.add_argument("--ckpt-every", type=int, default=100)
+    ap.add_argument("--resident-pct", type=int, default=92)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
