@@ -27,6 +27,7 @@
 #include <cstring>
 #include <memory>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "ads_internal.h"
@@ -161,8 +162,8 @@ __device__ __forceinline__ double ld1p(const double* p, bool on) {
 // all C cells are interior; otherwise per cell (the frame must stay zero).
 // ldv is a guarded load (the interior loops, whose masks agree across a
 // warp); ldvp the predicated form for the PML loops.
-template <typename T, int C>
-__device__ __forceinline__ Vec<T, C> ldv(const T* base, int64_t off, bool on) {
+template <typename T, int C, typename I = int64_t>
+__device__ __forceinline__ Vec<T, C> ldv(const T* base, I off, bool on) {
   Vec<T, C> x;
   if (on) {
     x = *reinterpret_cast<const Vec<T, C>*>(base + off);
@@ -198,8 +199,8 @@ __device__ __forceinline__ Vec<T, C> ldvp(const T* base, int64_t off, bool on) {
   return x;
 }
 
-template <typename T, int C>
-__device__ __forceinline__ void stv(T* base, int64_t off, const Vec<T, C>& x, int j, int ny) {
+template <typename T, int C, typename I = int64_t>
+__device__ __forceinline__ void stv(T* base, I off, const Vec<T, C>& x, int j, int ny) {
   if constexpr (C == 2) {
     // two guarded stores, predicated rather than branched
     if (j + 1 <= ny) *reinterpret_cast<Vec<T, C>*>(base + off) = x;
@@ -358,6 +359,12 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     // Register queues PF rows deep: w rows i-1 .. i+PF, wo / c / halo rows
     // i .. i+PF-1; each iteration issues the loads of the farthest rows.
     constexpr int PF = Tile<T>::PF;
+    // offsets within a field fit 32 bits (the plan checks fs < 2^31), which
+    // frees the registers of 64-bit row offsets in the increment form (the
+    // three-level form keeps 64-bit offsets: measured fewer spills that way)
+    using OffT = std::conditional_t<INC, int, int64_t>;
+    const OffT P32 = (OffT)P, col32 = j + JOFF;
+    auto off = [&](int r) { return (OffT)r * P32 + col32; };
     V wq[PF + 2], oq[PF], cq[PF];
     T hq[PF];
     auto halo = [&](int r) -> T {
@@ -376,7 +383,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       hq[q] = halo(i0 + q);
     }
     for (int i = i0; i < i_end; i++) {
-      const int64_t row = off(i);
+      const OffT row = off(i);
       const int rn = i + PF;  // farthest row of the wo / c / halo queues
       V wn = ldv<T, C>(w, off(rn + 1), jld && rn + 1 <= i_end);
       V on = ldv<T, C>(wo, off(rn), jld && rn < i_end);
@@ -1687,6 +1694,9 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
                 "shot %d: window [x0=%lld, x0+nx+2=%lld) outside the model (MX+2=%lld)", s,
                 (long long)h.x0, (long long)(h.x0 + h.nx + 2), (long long)(c.MX + 2));
     ADS_REQUIRE(h.nstep >= 2 && h.nstep < (1 << 24), "shot %d: nstep must be >= 2", s);
+    // the interior kernels index a field with 32-bit offsets
+    ADS_REQUIRE((h.nx + 2) * grid_pitch(c.MY) < (int64_t(1) << 31),
+                "shot %d: a field of (nx + 2) x pitch elements must stay below 2^31", s);
     ADS_REQUIRE(h.nsrc >= 0 && h.nrcv >= 0, "shot %d: negative counts", s);
     ADS_REQUIRE(h.nsrc == 0 || (h.srci && h.srcj && h.srcv), "shot %d: null source arrays",
                 s);

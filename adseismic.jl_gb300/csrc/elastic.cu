@@ -556,6 +556,11 @@ struct ColProf {
 // value, as when the step updates the fields in place.
 // ---------------------------------------------------------------------------
 constexpr int FSTRIP = 28 * EC;
+#ifndef ADS_EL_STEP_LAG
+#define ADS_EL_STEP_LAG 2             // rows the velocity half of the fused step runs behind
+#endif
+constexpr int kStepLag = ADS_EL_STEP_LAG;
+static_assert(kStepLag == 2 || kStepLag == 3, "the fused step lags its velocities 2 or 3 rows");
 #ifndef ADS_EL_MINB_F
 #define ADS_EL_MINB_F 3               // resident CTAs per SM, fused kernel of corner items
 #endif
@@ -647,77 +652,92 @@ k_el_step_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
   const bool lA = cA[0] || cA[1], lB = cB[0] || cB[1];
   const bool lAi = GC && lA, lBh = GC && lB;
   // row parts of the boxes: stress rows (fw1: 1..NX-1, fw2: 2..NX) and
-  // velocity rows r = s - 2 (fw3: 2..NX, fw4: 1..NX-1)
+  // velocity rows r = s - VL (fw3: 2..NX, fw4: 1..NX-1)
+  constexpr int VL = kStepLag;
   auto rs1 = [&](int s) { return !GR || (s >= 1 && s <= NX - 1); };
   auto rs2 = [&](int s) { return !GR || (s >= 2 && s <= NX); };
-  auto rv3 = [&](int s) { return !GR || s - 2 >= 2; };
-  auto rv4 = [&](int s) { return !GR || s - 2 <= NX - 1; };
-  // memory variables m1..m4 of stress row s and m5..m8 of velocity row s - 2
-  // (where they can be nonzero), loaded one iteration ahead
-  auto mload = [&](int s, bool on, V2<T> (&m)[8]) {
-    const int64_t o = (int64_t)s * P + j + JOFF, q = o - 2 * P;
-    const bool vr = on && own && s >= i0 + 2;
+  auto rv3 = [&](int s) { return !GR || s - VL >= 2; };
+  auto rv4 = [&](int s) { return !GR || s - VL <= NX - 1; };
+  // memory variables m1..m4 of stress row s (onS) and m5..m8 of velocity row
+  // s - VL (onV, where they can be nonzero), loaded one iteration ahead
+  auto mload = [&](int s, bool onS, bool onV, V2<T> (&m)[8]) {
+    const int64_t o = (int64_t)s * P + j + JOFF, q = o - VL * P;
+    const bool vr = onV && own && s >= i0 + VL;
     if constexpr (GR) {
-      m[0] = ld2p(m1i, o, on && rs1(s) && lA);
-      m[2] = ld2p(m3i, o, on && rs2(s) && lB);
+      m[0] = ld2p(m1i, o, onS && rs1(s) && lA);
+      m[2] = ld2p(m3i, o, onS && rs2(s) && lB);
       m[4] = ld2p(m5i, q, vr && rv3(s) && lA);
       m[6] = ld2p(m7i, q, vr && rv4(s) && lB);
     }
     if constexpr (GC) {
-      m[1] = ld2p(m2i, o, on && rs1(s) && lAi);
-      m[3] = ld2p(m4i, o, on && rs2(s) && lBh);
+      m[1] = ld2p(m2i, o, onS && rs1(s) && lAi);
+      m[3] = ld2p(m4i, o, onS && rs2(s) && lBh);
       m[5] = ld2p(m6i, q, vr && rv3(s) && lAi);
       m[7] = ld2p(m8i, q, vr && rv4(s) && lBh);
     }
   };
   const int s0 = i0 - 2;
-  // windows at stress row s: old vx rows s-2..s+2, old vy rows s-2..s+1,
-  // lam / mu rows s, s+1, old stresses row s, rho rows s-2, s-1; new sxx rows
-  // s-4..s-1, new sxy rows s-3..s-1, new syy rows s-2, s-1
-  V2<T> X0 = ld(vx, s0 - 2), X1 = ld(vx, s0 - 1), X2 = ld(vx, s0), X3 = ld(vx, s0 + 1),
-        X4 = ld(vx, s0 + 2);
-  V2<T> Y0 = ld(vy, s0 - 2), Y1 = ld(vy, s0 - 1), Y2 = ld(vy, s0), Y3 = ld(vy, s0 + 1);
+  // windows at stress row s: old vx rows s-VL..s+2 (X[k] = row s-VL+k), old
+  // vy rows s-VL..s+1, lam / mu rows s, s+1, old stresses row s, rho rows
+  // s-VL, s-VL+1; new sxx rows s-VL-2..s-1 (NA[k] = row s-VL-2+k), new sxy
+  // rows s-VL-1..s-1, new syy rows s-VL..s-1.  With VL = 3 the velocities of
+  // row s-3 need no stress of row s, so the two halves of an iteration are
+  // independent of each other.
+  V2<T> X[VL + 3], Yv[VL + 2], NA[VL + 2], NC[VL + 1], NB[VL];
+#pragma unroll
+  for (int k = 0; k < VL + 3; k++) X[k] = ld(vx, s0 - VL + k);
+#pragma unroll
+  for (int k = 0; k < VL + 2; k++) Yv[k] = ld(vy, s0 - VL + k);
+#pragma unroll
+  for (int k = 0; k < VL + 2; k++) NA[k] = V2<T>{};
+#pragma unroll
+  for (int k = 0; k < VL + 1; k++) NC[k] = V2<T>{};
+#pragma unroll
+  for (int k = 0; k < VL; k++) NB[k] = V2<T>{};
   V2<T> L0 = ld(M.lam, s0), L1 = ld(M.lam, s0 + 1), U0 = ld(M.mu, s0), U1 = ld(M.mu, s0 + 1);
   V2<T> A0 = ld(sxx, s0), B0 = ld(syy, s0), C0 = ld(sxy, s0);
-  V2<T> R0 = ld(M.rho, s0 - 2), R1 = ld(M.rho, s0 - 1);
-  V2<T> NA0{}, NA1{}, NA2{}, NA3{}, NC0{}, NC1{}, NC2{}, NB0{}, NB1{};
+  V2<T> R0 = ld(M.rho, s0 - VL), R1 = ld(M.rho, s0 - VL + 1);
   V2<T> mm[8] = {};
-  mload(s0, true, mm);
-  for (int s = s0; s <= i_end + 1; s++) {
-    const bool more = s <= i_end;
+  mload(s0, true, true, mm);
+  for (int s = s0; s <= i_end + VL - 1; s++) {
+    const bool doS = s <= i_end + 1;  // stresses of row s this iteration
+    const bool more = s <= i_end;     // stresses of row s + 1 next iteration
+    const bool vmore = s + 1 - VL <= i_end - 1;  // velocities of row s + 1 - VL next
     const V2<T> X5 = ld(vx, more ? s + 3 : -1), Y4 = ld(vy, more ? s + 2 : -1),
                 L2 = ld(M.lam, more ? s + 2 : -1), U2 = ld(M.mu, more ? s + 2 : -1),
-                R2 = ld(M.rho, more ? s : -1);
+                R2 = ld(M.rho, vmore ? s + 2 - VL : -1);
     const V2<T> An = ld(sxx, more ? s + 1 : -1), Bn = ld(syy, more ? s + 1 : -1),
                 Cn = ld(sxy, more ? s + 1 : -1);
     V2<T> mn[8] = {};
-    mload(s + 1, more, mn);
-    const int64_t o = (int64_t)s * P + j + JOFF, q = o - 2 * P;
-    // x profiles of stress row s and velocity row s - 2
-    const int sx = min(max(s, 1), NX) - 1, vx_ = min(max(s - 2, 1), NX) - 1;
+    mload(s + 1, more, vmore, mn);
+    const int64_t o = (int64_t)s * P + j + JOFF, q = o - VL * P;
+    // x profiles of stress row s and velocity row s - VL
+    const int sx = min(max(s, 1), NX) - 1, vx_ = min(max(s - VL, 1), NX) - 1;
     const T axh = GR ? M.axh[sx] : T(0), bxh = GR ? M.bxh[sx] : T(1);
     const T axi = GR ? M.axi[sx] : T(0), bxi = GR ? M.bxi[sx] : T(1);
     const T vaxi = GR ? M.axi[vx_] : T(0), vbxi = GR ? M.bxi[vx_] : T(1);
     const T vaxh = GR ? M.axh[vx_] : T(0), vbxh = GR ? M.bxh[vx_] : T(1);
-    const bool r1 = rs1(s), r2 = rs2(s);
+    const bool r1 = doS && rs1(s), r2 = doS && rs2(s);
     const bool rx1 = GR && r1 && (axh != T(0) || bxh != T(1));
     const bool rx3 = GR && r2 && (axi != T(0) || bxi != T(1));
-    const bool vrow = s >= i0 + 2;  // velocities of row s - 2 this iteration
+    const bool vrow = s >= i0 + VL;  // velocities of row s - VL this iteration
     const bool r3 = rv3(s), r4 = rv4(s);
     const bool rx5 = GR && vrow && r3 && (vaxi != T(0) || vbxi != T(1));
     const bool rx7 = GR && vrow && r4 && (vaxh != T(0) || vbxh != T(1));
     // ---- new stresses of row s
+    const V2<T>& Xs = X[VL];  // old vx row s
+    const V2<T>& Ys = Yv[VL];  // old vy row s
     T xr[5], yr[5], ur[3];
-    xr[0] = shup(X2.v[1]);
-    xr[1] = X2.v[0];
-    xr[2] = X2.v[1];
-    xr[3] = shdn(X2.v[0]);
-    xr[4] = shdn(X2.v[1]);
-    yr[0] = shup(Y2.v[0]);
-    yr[1] = shup(Y2.v[1]);
-    yr[2] = Y2.v[0];
-    yr[3] = Y2.v[1];
-    yr[4] = shdn(Y2.v[0]);
+    xr[0] = shup(Xs.v[1]);
+    xr[1] = Xs.v[0];
+    xr[2] = Xs.v[1];
+    xr[3] = shdn(Xs.v[0]);
+    xr[4] = shdn(Xs.v[1]);
+    yr[0] = shup(Ys.v[0]);
+    yr[1] = shup(Ys.v[1]);
+    yr[2] = Ys.v[0];
+    yr[3] = Ys.v[1];
+    yr[4] = shdn(Ys.v[0]);
     ur[0] = U0.v[0];
     ur[1] = U0.v[1];
     ur[2] = shdn(U0.v[0]);
@@ -733,7 +753,8 @@ k_el_step_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
       const T lam_ = T(0.5) * (L1.v[c] + L0.v[c]);
       const T mu1 = T(0.5) * (U1.v[c] + U0.v[c]);
       const T lm = lam_ + T(2) * mu1;
-      const T dvx = d4r<T>(X3.v[c], X2.v[c], X4.v[c], X1.v[c], M.hx24, M.rhx24);
+      const T dvx = d4r<T>(X[VL + 1].v[c], X[VL].v[c], X[VL + 2].v[c], X[VL - 1].v[c], M.hx24,
+                           M.rhx24);
       const T dvy = d4r<T>(yr[2 + c], yr[1 + c], yr[3 + c], yr[c], M.hy24, M.rhy24);
       u1[c] = k1[c] && rx1;
       u2[c] = GC && k1[c];
@@ -746,7 +767,8 @@ k_el_step_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
       e2s[c] = e2;
       // fw2
       const T mu2 = T(0.5) * (ur[c] + ur[c + 1]);
-      const T dvydx = d4r<T>(Y2.v[c], Y1.v[c], Y3.v[c], Y0.v[c], M.hx24, M.rhx24);
+      const T dvydx = d4r<T>(Yv[VL].v[c], Yv[VL - 1].v[c], Yv[VL + 1].v[c], Yv[VL - 2].v[c],
+                             M.hx24, M.rhx24);
       const T dvxdy = d4r<T>(xr[2 + c], xr[1 + c], xr[3 + c], xr[c], M.hy24, M.rhy24);
       u3[c] = k2[c] && rx3;
       u4[c] = GC && k2[c];
@@ -774,19 +796,23 @@ k_el_step_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
         stw(m4o, o, m4v, u4[0], u4[1]);
       }
     }
-    // ---- new velocities of row s - 2
+    // ---- new velocities of row r = s - VL: new sxx rows r-2..r+1, sxy rows
+    // r-1..r+2 (the last of them row s itself when VL = 2), syy row r
     if (vrow) {
+      const V2<T>& NC1 = NC[1];
+      const V2<T>& NCt = VL == 2 ? NCs : NC[VL];  // new sxy row r + 2
+      const V2<T>& NBr = NB[0];
       T qr[5], wr[5], r0[3], r1v[3];
       qr[0] = shup(NC1.v[0]);
       qr[1] = shup(NC1.v[1]);
       qr[2] = NC1.v[0];
       qr[3] = NC1.v[1];
       qr[4] = shdn(NC1.v[0]);
-      wr[0] = shup(NB0.v[1]);
-      wr[1] = NB0.v[0];
-      wr[2] = NB0.v[1];
-      wr[3] = shdn(NB0.v[0]);
-      wr[4] = shdn(NB0.v[1]);
+      wr[0] = shup(NBr.v[1]);
+      wr[1] = NBr.v[0];
+      wr[2] = NBr.v[1];
+      wr[3] = shdn(NBr.v[0]);
+      wr[4] = shdn(NBr.v[1]);
       r0[0] = R0.v[0];
       r0[1] = R0.v[1];
       r0[2] = shdn(R0.v[0]);
@@ -800,25 +826,25 @@ k_el_step_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
         k3[c] = own && r3 && cA[c];
         k4[c] = own && r4 && cB[c];
         // fw3
-        const T a = d4r<T>(NA2.v[c], NA1.v[c], NA3.v[c], NA0.v[c], M.hx24, M.rhx24);
+        const T a = d4r<T>(NA[2].v[c], NA[1].v[c], NA[3].v[c], NA[0].v[c], M.hx24, M.rhx24);
         const T b = d4r<T>(qr[2 + c], qr[1 + c], qr[3 + c], qr[c], M.hy24, M.rhy24);
         u5[c] = k3[c] && rx5;
         u6[c] = GC && k3[c];
         m5v[c] = u5[c] ? vbxi * mm[4].v[c] + vaxi * a : T(0);
         m6v[c] = u6[c] ? Y.bi[c] * mm[5].v[c] + Y.ai[c] * b : T(0);
         const T e3 = (a + m5v[c]) + (b + m6v[c]);
-        nvx[c] = X0.v[c] + divr<T>(e3 * M.dt, r0[c]);
+        nvx[c] = X[0].v[c] + divr<T>(e3 * M.dt, r0[c]);
         a3s[c] = e3;
         // fw4
         const T rho_ = T(0.25) * (r0[c] + r1v[c] + r1v[c + 1] + r0[c + 1]);
-        const T a4 = d4r<T>(NC2.v[c], NC1.v[c], NCs.v[c], NC0.v[c], M.hx24, M.rhx24);
+        const T a4 = d4r<T>(NC[2].v[c], NC[1].v[c], NCt.v[c], NC[0].v[c], M.hx24, M.rhx24);
         const T b4 = d4r<T>(wr[2 + c], wr[1 + c], wr[3 + c], wr[c], M.hy24, M.rhy24);
         u7[c] = k4[c] && rx7;
         u8[c] = GC && k4[c];
         m7v[c] = u7[c] ? vbxh * mm[6].v[c] + vaxh * a4 : T(0);
         m8v[c] = u8[c] ? Y.bh[c] * mm[7].v[c] + Y.ah[c] * b4 : T(0);
         const T e4 = (a4 + m7v[c]) + (b4 + m8v[c]);
-        nvy[c] = Y0.v[c] + divr<T>(e4 * M.dt, rho_);
+        nvy[c] = Yv[0].v[c] + divr<T>(e4 * M.dt, rho_);
         a4s[c] = e4;
       }
       stw(vxo, q, nvx, k3[0], k3[1]);
@@ -836,14 +862,24 @@ k_el_step_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
         stw(m8o, q, m8v, u8[0], u8[1]);
       }
     }
-    X0 = X1; X1 = X2; X2 = X3; X3 = X4; X4 = X5;
-    Y0 = Y1; Y1 = Y2; Y2 = Y3; Y3 = Y4;
+#pragma unroll
+    for (int k = 0; k < VL + 2; k++) X[k] = X[k + 1];
+    X[VL + 2] = X5;
+#pragma unroll
+    for (int k = 0; k < VL + 1; k++) Yv[k] = Yv[k + 1];
+    Yv[VL + 1] = Y4;
     L0 = L1; L1 = L2; U0 = U1; U1 = U2;
     A0 = An; B0 = Bn; C0 = Cn;
     R0 = R1; R1 = R2;
-    NA0 = NA1; NA1 = NA2; NA2 = NA3; NA3 = NAs;
-    NC0 = NC1; NC1 = NC2; NC2 = NCs;
-    NB0 = NB1; NB1 = NBs;
+#pragma unroll
+    for (int k = 0; k < VL + 1; k++) NA[k] = NA[k + 1];
+    NA[VL + 1] = NAs;
+#pragma unroll
+    for (int k = 0; k < VL; k++) NC[k] = NC[k + 1];
+    NC[VL] = NCs;
+#pragma unroll
+    for (int k = 0; k < VL - 1; k++) NB[k] = NB[k + 1];
+    NB[VL - 1] = NBs;
 #pragma unroll
     for (int k = 0; k < 8; k++) mm[k] = mn[k];
   }
