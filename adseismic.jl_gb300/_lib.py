@@ -11,7 +11,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libadseismic_gb300.so")
 
-ADS_OK, ADS_ERR_INVALID, ADS_ERR_CUDA, ADS_ERR_NOMEM, ADS_ERR_UNSUPPORTED = range(5)
+ADS_OK, ADS_ERR_INVALID, ADS_ERR_CUDA, ADS_ERR_NOMEM, ADS_ERR_UNSUPPORTED, ADS_ERR_TIMEOUT = range(6)
 ADS_F64, ADS_F32 = 0, 1
 ADS_VARIANT_W, ADS_VARIANT_U = 0, 1
 
@@ -20,6 +20,7 @@ _STATUS = {
     ADS_ERR_CUDA: "CUDA error",
     ADS_ERR_NOMEM: "out of device memory",
     ADS_ERR_UNSUPPORTED: "unsupported",
+    ADS_ERR_TIMEOUT: "a bounded device wait ran out",
 }
 
 
@@ -41,7 +42,7 @@ class AcousticConfig(C.Structure):
         ("rows_per_thread", C.c_int32), ("steps_per_block", C.c_int32),
         ("block_rows", C.c_int32), ("autotune", C.c_int32),
         ("resident_segments", C.c_int32), ("resident_mem_pct", C.c_int32),
-        ("reserved", C.c_int32 * 2),
+        ("tma", C.c_int32), ("reserved", C.c_int32 * 1),
     ]
 
 
@@ -122,6 +123,8 @@ _SIGS = {
     "ads_elastic_plan_launches": [P, I32],
     "ads_elastic_plan_resident_segments": [P],
     "ads_elastic_plan_rows": [P, I32],
+    "ads_acoustic_plan_tma": [P],
+    "ads_acoustic_plan_device_status": [P, P],
     "ads_elastic_plan_gradient_ex": [P, P, P, P, P, P, P, P, P, P, P, P],
     "ads_elastic_plan_source_offset": [P, I64],
     "ads_elastic_plan_set_source_values": [P, I64, P, P],
@@ -152,6 +155,7 @@ _RESTYPE = {
     "ads_elastic_plan_launches": C.c_int64,
     "ads_elastic_plan_resident_segments": C.c_int64,
     "ads_elastic_plan_rows": C.c_int64,
+    "ads_acoustic_plan_tma": C.c_int64,
     "ads_elastic_plan_source_offset": C.c_int64,
 }
 EXPORTED = sorted(_SIGS)

@@ -165,13 +165,16 @@ class AcousticPlan:
     resident_mem_pct percent, default 50, of the free device memory).
     variant: ADS_VARIANT_W (the custom operators' form, phi / psi from the old
     field; PropagatorKernel 1 and 2) or ADS_VARIANT_U (one_step, phi / psi
-    from the new field; PropagatorKernel 0, the reference's default)."""
+    from the new field; PropagatorKernel 0, the reference's default).
+    tma (FP32): 1 runs the interior forward steps through tensor-map tile
+    copies where the driver supports them, 0 (default) through the
+    register-queue kernel; the results are identical."""
 
     def __init__(self, MX, MY, dx, dy, dt, shots, npml=12, Rcoef=0.001, vp_ref=1000.0,
                  use_pml=15, precision="f64", use_graph=True, ckpt_every=0,
                  rows_per_thread=0, steps_per_block=0, block_rows=0, autotune=False,
                  resident_segments=0, resident_mem_pct=0, stream=None,
-                 variant=ADS_VARIANT_W):
+                 variant=ADS_VARIANT_W, tma=0):
         cfg = _lib.AcousticConfig()
         cfg.MX, cfg.MY, cfg.dx, cfg.dy, cfg.dt = MX, MY, dx, dy, dt
         cfg.npml, cfg.Rcoef, cfg.vp_ref, cfg.use_pml = npml, Rcoef, vp_ref, use_pml
@@ -185,6 +188,7 @@ class AcousticPlan:
         cfg.autotune = int(autotune)
         cfg.resident_segments = int(resident_segments)
         cfg.resident_mem_pct = int(resident_mem_pct)
+        cfg.tma = int(tma)
         self.MX, self.MY = MX, MY
         self.precision = precision
         self.dtype = torch.float64 if precision == "f64" else torch.float32
@@ -220,6 +224,12 @@ class AcousticPlan:
         self.launches_gradient = L.ads_acoustic_plan_launches(h, 1)
         self.resident_segments = L.ads_acoustic_plan_resident_segments(h)
         self.steps_per_block = L.ads_acoustic_plan_steps_per_block(h)
+        self.uses_tma = bool(L.ads_acoustic_plan_tma(h) == 1)
+
+    def device_status(self):
+        """Raise AdsError (ADS_ERR_TIMEOUT) if a bounded wait of the plan's
+        kernels has run out since its creation; synchronises the stream."""
+        call("ads_acoustic_plan_device_status", self._h, _stream())
 
     def close(self):
         if getattr(self, "_h", None):

@@ -21,11 +21,14 @@
 //    backwards, accumulating grad_c in FP64.
 //  * The forward and the reverse time loops are captured once as CUDA graphs
 //    and replayed each call.
+#include <cuda.h>  // CUtensorMap (the encoder comes through the runtime's driver entry point)
+
 #include <algorithm>
 #include <climits>
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <numeric>
 #include <type_traits>
 #include <vector>
@@ -588,6 +591,204 @@ k_ac_seed(const AcShot<T>* __restrict__ shots, int a, int base) {
        e += (int64_t)gridDim.x * blockDim.x) {
     d2[e] = u2[e];
     d1[e] = u1[e];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Interior forward step fed by TMA (FP32 increment form; ads_acoustic_config
+// tma = 1).  The register queues of k_ac_fwd keep about three 256-byte rows
+// in flight per warp, too few to cover the DRAM latency at full bandwidth;
+// here one thread of a CTA
+// issues tensor-map tile copies (cp.async.bulk.tensor) of TMA_RB-row chunks
+// of u (with a one-column and one-row halo), d and c into shared memory,
+// TMA_ST chunks ahead, each chunk completing on its own mbarrier, and the four
+// warps compute from shared memory.  The CTA takes a whole interior item (one
+// 64-column strip of one shot, rows [i0, i0 + gh)); the arithmetic is that of
+// k_ac_fwd's interior loop.  Launched alone it is faster than the register
+// kernel (21.3 against 25.9 us on 16 shots of 1000 x 500), but beside the
+// concurrent PML-item launch the whole step is not (47.4 against 47.8
+// shot-gradients/s at two chunks in flight, 45.1 at four), so it is opt-in.
+//
+// Every wait is bounded by the SM clock: if a chunk has not arrived after
+// about a second the CTA records ADS_ERR_TIMEOUT's flag in *err, waits (again
+// bounded) for the copies it has in flight and returns; the plan reports the
+// flag on its next call.  The tile origins are multiples of 4 columns by
+// construction (strips start at column 1 + 64k of the pitched layout with
+// JOFF = 31); the kernel checks that before issuing any copy.
+// ---------------------------------------------------------------------------
+#ifndef ADS_TMA_RB
+#define ADS_TMA_RB 8
+#endif
+constexpr int TMA_RB = ADS_TMA_RB;                           // rows of a chunk
+#ifndef ADS_TMA_ST
+#define ADS_TMA_ST 2
+#endif
+constexpr int TMA_ST = ADS_TMA_ST;                           // chunks in flight
+constexpr int TMA_UW = 72;                                   // u box: columns j0-4 .. j0+67
+constexpr int TMA_W = 64;                                    // d, c boxes: columns j0 .. j0+63
+constexpr int TMA_UBYTES = TMA_UW * (TMA_RB + 2) * 4;        // 2880
+constexpr int TMA_DBYTES = TMA_W * TMA_RB * 4;               // 2048
+constexpr int TMA_UOFF = 0;
+constexpr int TMA_DOFF = (TMA_UBYTES + 127) / 128 * 128;     // 2944
+constexpr int TMA_COFF = TMA_DOFF + TMA_DBYTES;
+constexpr int TMA_STAGE = TMA_COFF + TMA_DBYTES;             // 7040 bytes a chunk
+constexpr int TMA_SMEM = TMA_ST * TMA_STAGE + TMA_ST * 8;    // + the mbarriers
+constexpr long long kTmaWaitCycles = 2000000000LL;           // about 1 s at 2 GHz
+#ifndef ADS_MINB_FT32
+#define ADS_MINB_FT32 12  // resident CTAs per SM of the TMA-fed interior forward (40 registers)
+#endif
+
+// Per shot: the tensor maps of u's two-slot ring, the segment store, d and c
+// (written once at plan creation; CUtensorMap carries its own alignment).
+struct AcTmaMaps {
+  CUtensorMap ring, seg, d, c;
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint32_t a, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(a), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t a, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// wait for phase `parity` of the mbarrier at a, at most kTmaWaitCycles
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t a, unsigned parity) {
+  if (mbar_try_wait(a, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(a, parity))
+    if (clock64() - t0 > kTmaWaitCycles) return false;
+  return true;
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(map), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                            int z, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
+template <int MODE, bool CK>
+__global__ void __launch_bounds__(Tile<float>::TPB, ADS_MINB_FT32)
+k_ac_fwd_tma(const AcItem* __restrict__ items, const AcShot<float>* __restrict__ shots,
+             const AcTmaMaps* __restrict__ maps, AcConst<float> K, int t, int base,
+             int ckpt_slot, int gh, int* __restrict__ err) {
+  constexpr bool SEG = MODE != 0;
+  extern __shared__ __align__(128) unsigned char tsm[];
+  const AcItem it = items[blockIdx.x];
+  const AcShot<float>& sh = shots[it.shot];
+  const AcTmaMaps* mp = maps + it.shot;
+  const int nx = sh.nx, ny = sh.ny;
+  const int i0 = it.i0, i_end = min(i0 + gh, nx + 1);
+  if (i0 > nx) return;  // (whole CTA)
+  const int nch = (i_end - i0 + TMA_RB - 1) / TMA_RB;
+  const int xu = it.j0 + JOFF - 4, xd = it.j0 + JOFF;
+  if ((xu & 3) != 0 || (xd & 3) != 0) {  // a tile origin off the 16-byte grid: copy nothing
+    if (threadIdx.x == 0) atomicOr(err, 2);
+    return;
+  }
+  const int64_t P = sh.pitch, fs = sh.fs;
+  float* out = SEG ? sh.seg + (int64_t)(t - base) * fs : sh.u + (int64_t)(t & 1) * fs;
+  float* dd = sh.d;
+  const int zu = SEG ? t - 1 - base : (t - 1) & 1;
+  const CUtensorMap* mu = SEG ? &mp->seg : &mp->ring;
+  const uint32_t sbase = smem_addr(tsm), bar0 = sbase + TMA_ST * TMA_STAGE;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TMA_ST; s++) mbar_init(bar0 + 8 * s, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  auto issue = [&](int ch) {  // thread 0
+    const int s = ch % TMA_ST;
+    const uint32_t st = sbase + s * TMA_STAGE, bar = bar0 + 8 * s;
+    const int r0 = i0 + ch * TMA_RB;
+    mbar_expect_tx(bar, TMA_UBYTES + 2 * TMA_DBYTES);
+    tma_load_3d(st + TMA_UOFF, mu, xu, r0 - 1, zu, bar);
+    tma_load_2d(st + TMA_DOFF, &mp->d, xd, r0, bar);
+    tma_load_2d(st + TMA_COFF, &mp->c, xd, r0, bar);
+  };
+  if (threadIdx.x == 0)
+    for (int ch = 0; ch < min(TMA_ST, nch); ch++) issue(ch);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = it.j0 + 2 * lane;
+  const bool ck_on = CK && !SEG && ckpt_slot > 0 && ckpt_slot < sh.nseg;
+  float* ck = ck_on ? sh.ckpt + (int64_t)ckpt_slot * 4 * fs : nullptr;
+  for (int ch = 0; ch < nch; ch++) {
+    const int s = ch % TMA_ST;
+    const bool ok = mbar_wait_bounded(bar0 + 8 * s, (ch / TMA_ST) & 1);
+    if (__syncthreads_or(!ok)) {
+      // record, let the copies in flight (chunks ch .. ch + TMA_ST - 1) land, stop
+      if (threadIdx.x == 0) {
+        atomicOr(err, 1);
+        for (int c2 = ch; c2 < min(ch + TMA_ST, nch); c2++)
+          mbar_wait_bounded(bar0 + 8 * (c2 % TMA_ST), (c2 / TMA_ST) & 1);
+      }
+      __syncthreads();
+      return;
+    }
+    const float* U = reinterpret_cast<const float*>(tsm + s * TMA_STAGE + TMA_UOFF);
+    const float* D = reinterpret_cast<const float*>(tsm + s * TMA_STAGE + TMA_DOFF);
+    const float* Cc = reinterpret_cast<const float*>(tsm + s * TMA_STAGE + TMA_COFF);
+#pragma unroll
+    for (int k = 0; k < TMA_RB / Tile<float>::G; k++) {
+      const int q = warp * (TMA_RB / Tile<float>::G) + k;  // row of the chunk
+      const int i = i0 + ch * TMA_RB + q;
+      if (i >= i_end) break;
+      // u rows i-1, i, i+1 are box rows q, q+1, q+2; column j + c is box column 4 + 2 lane + c
+      const float* u1 = U + (q + 1) * TMA_UW + 4 + 2 * lane;
+      const Vec<float, 2> u0 = *reinterpret_cast<const Vec<float, 2>*>(u1);
+      const Vec<float, 2> um = *reinterpret_cast<const Vec<float, 2>*>(u1 - TMA_UW);
+      const Vec<float, 2> up = *reinterpret_cast<const Vec<float, 2>*>(u1 + TMA_UW);
+      const float uS = u1[-1], uN = u1[2];
+      const Vec<float, 2> dv0 = *reinterpret_cast<const Vec<float, 2>*>(D + q * TMA_W + 2 * lane);
+      const Vec<float, 2> cv = *reinterpret_cast<const Vec<float, 2>*>(Cc + q * TMA_W + 2 * lane);
+      Vec<float, 2> vo, dv;
+#pragma unroll
+      for (int c = 0; c < 2; c++) {
+        const float wS = c == 0 ? uS : u0.v[0];
+        const float wN = c == 1 ? uN : u0.v[1];
+        const float x0 = u0.v[c];
+        dv.v[c] = dv0.v[c] + cv.v[c] * (K.cx * ((up.v[c] - x0) + (um.v[c] - x0)) +
+                                        K.cy * ((wN - x0) + (wS - x0)));
+        vo.v[c] = x0 + dv.v[c];
+      }
+      if (j <= ny) {
+        const int64_t row = (int64_t)i * P + j + JOFF;
+        stv<float, 2>(out, row, vo, j, ny);
+        stv<float, 2>(dd, row, dv, j, ny);
+        if (ck_on) {
+          stv<float, 2>(ck, row, vo, j, ny);
+          stv<float, 2>(ck + fs, row, dv, j, ny);
+        }
+      }
+    }
+    __syncthreads();  // every warp is done with chunk ch's stage
+    if (threadIdx.x == 0 && ch + TMA_ST < nch) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      issue(ch + TMA_ST);
+    }
   }
 }
 
@@ -1517,6 +1718,8 @@ struct AcPlanBase {
   int64_t launches_fwd = 0, launches_grad = 0;
   int64_t resident = 0;  // checkpoint segments kept resident (no recompute)
   int64_t steps_per_block = 1;  // forward steps per launch (configured or tuned)
+  int64_t uses_tma = 0;         // interior forward steps through tensor-map copies
+  virtual int device_status(cudaStream_t st) = 0;
 };
 
 namespace {
@@ -1527,6 +1730,24 @@ struct AcPlan final : AcPlanBase {
   int nshots = 0;
   bool vu = false;    // variant U: phi / psi from the new field (pre-pass kernels)
   bool inc = false;   // FP32 increment form (k_ac_fwd INC); off for time blocking
+  // FP32: interior forward steps through k_ac_fwd_tma (tensor maps per shot);
+  // d_err collects its status flags (1: a bounded wait ran out, 2: a tile
+  // origin off the 16-byte grid, never expected)
+  bool tma_ok = false;
+  AcTmaMaps* d_maps = nullptr;
+  int* d_err = nullptr;
+  std::vector<size_t> seg_slots;  // per sorted shot: store slots
+  int build_maps(cudaStream_t st);
+  int device_status(cudaStream_t st) override {
+    int h = 0;
+    if (d_err) {
+      ADS_CUDA(cudaMemcpyAsync(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+      ADS_CUDA(cudaStreamSynchronize(st));
+    }
+    if (h & 1) return fail(ADS_ERR_TIMEOUT, "a bounded wait of the tensor-map pipeline ran out");
+    if (h & 2) return fail(ADS_ERR_INVALID, "internal: a tile origin off the 16-byte grid");
+    return ADS_OK;
+  }
   int K = 0;          // checkpoint spacing
   // Resident segments: segments res_seg .. nseg_max-1 keep the forward
   // wavefields of their steps in the shots' stores (slot t - res_base), so
@@ -1973,8 +2194,11 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
       const size_t slots =
           (size_t)(K + 2) + (res_seg < nseg_max && nstep[q] >= a ? nstep[q] - (a - 2) + 1 : 0);
       offs[q].seg = L.take(slots * fsb[q]);
+      seg_slots.push_back(slots);
     }
   }
+  const size_t maps_off = L.take(sizeof(AcTmaMaps) * ns);
+  const size_t err_off = L.take(sizeof(int));
   pool_bytes = L.used;
   bytes = (int64_t)pool_bytes;
   resident = nseg_max - res_seg;
@@ -2016,6 +2240,8 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   d_tb_srcs = (TbSrc*)(pool + tbs_off);
   d_tb_rows = (TbRcvRow*)(pool + tbr_off);
   d_tb_map = (int*)(pool + tbm_off);
+  d_maps = (AcTmaMaps*)(pool + maps_off);
+  d_err = (int*)(pool + err_off);
   // per-shot structs and host-side data (profiles, scaled wavelets)
   hshots.resize(ns);
   srcv_dev.assign(ns, nullptr);
@@ -2110,6 +2336,8 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   if (int e = up(pool + rnx_off, rcv_next_all.data(), sizeof(int) * rcv_next_all.size()))
     return e;
   ADS_CUDA(cudaStreamSynchronize(st));  // host staging buffers go out of scope
+  if (sizeof(T) == 4 && c.tma > 0)
+    if (int e = build_maps(st)) return e;
   ADS_CUDA(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
   ADS_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
   ADS_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
@@ -2363,6 +2591,73 @@ int AcPlan<T>::upload_tiles(const TileList& L, DevTiles& D, cudaStream_t st) {
   return ADS_OK;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (the library
+// does not link the driver API); null when the driver has none.
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    else
+      cudaGetLastError();
+  });
+  return fn;
+}
+
+// The tensor maps of every shot (FP32 plans): u's ring and segment store as
+// 3D (pitch x rows x slot) with a 72 x 10 x 1 box, d and c as 2D with a
+// 64 x 8 box; zero fill outside the field.  Leaves tma_ok false when the
+// driver has no encoder.
+template <typename T>
+int AcPlan<T>::build_maps(cudaStream_t st) {
+  tma_ok = false;
+  EncodeTiledFn enc = encode_tiled_fn();
+  if (!enc) return ADS_OK;
+  std::vector<AcTmaMaps> hm(nshots);
+  const cuuint32_t es[3] = {1, 1, 1};
+  for (int s = 0; s < nshots; s++) {
+    const AcShot<T>& h = hshots[s];
+    const cuuint64_t rows = (cuuint64_t)h.nx + 2, P = (cuuint64_t)h.pitch;
+    const cuuint64_t rs = P * sizeof(T), ss = (cuuint64_t)h.fs * sizeof(T);
+    ADS_REQUIRE(rs % 16 == 0 && ss % 16 == 0 && P >= (cuuint64_t)TMA_UW,
+                "internal: field layout unfit for tensor maps");
+    auto map3 = [&](CUtensorMap* m, void* base, cuuint64_t slots) {
+      const cuuint64_t dim[3] = {P, rows, slots}, str[2] = {rs, ss};
+      const cuuint32_t box[3] = {(cuuint32_t)TMA_UW, (cuuint32_t)TMA_RB + 2, 1};
+      return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dim, str, box, es,
+                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    };
+    auto map2 = [&](CUtensorMap* m, void* base) {
+      const cuuint64_t dim[2] = {P, rows}, str[1] = {rs};
+      const cuuint32_t box[2] = {(cuuint32_t)TMA_W, (cuuint32_t)TMA_RB};
+      return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dim, str, box, es,
+                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    };
+    if (map3(&hm[s].ring, (void*)h.u, 2) != CUDA_SUCCESS ||
+        map3(&hm[s].seg, (void*)h.seg, (cuuint64_t)seg_slots[s]) != CUDA_SUCCESS ||
+        map2(&hm[s].d, (void*)h.d) != CUDA_SUCCESS || map2(&hm[s].c, (void*)h.c) != CUDA_SUCCESS)
+      return fail(ADS_ERR_CUDA, "cuTensorMapEncodeTiled rejected a field of shot %d", s);
+  }
+  ADS_CUDA(cudaMemcpyAsync(d_maps, hm.data(), sizeof(AcTmaMaps) * nshots,
+                           cudaMemcpyHostToDevice, st));
+  ADS_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), st));
+  ADS_CUDA(cudaStreamSynchronize(st));
+  tma_ok = true;
+  uses_tma = 1;
+  return ADS_OK;
+}
+
 // One forward step of the first na sorted shots: the interior-item kernel and
 // the PML-item kernel (each launched only when it has items).
 template <typename T>
@@ -2397,7 +2692,27 @@ int AcPlan<T>::launch_fwd(cudaStream_t st, int mode, int na, int t, int base, in
     else ADS_FWD(0, IN, VUF, false, items_, n_, s_, rows_);                \
   } while (0)
   if (ni > 0) {
-    ADS_FWD_MODE(true, false, tf.items, ni, st, ri_f);
+    if constexpr (sizeof(T) == 4) {
+      if (tma_ok && inc) {
+        const int gh = Tile<T>::G * ri_f;
+        if (mode == 1)
+          k_ac_fwd_tma<1, false><<<ni, TPB, TMA_SMEM, st>>>(tf.items, d_shots, d_maps, kc, t,
+                                                            base, ck, gh, d_err);
+        else if (mode == 2)
+          k_ac_fwd_tma<2, false><<<ni, TPB, TMA_SMEM, st>>>(tf.items, d_shots, d_maps, kc, t,
+                                                            base, ck, gh, d_err);
+        else if (ck > 0)
+          k_ac_fwd_tma<0, true><<<ni, TPB, TMA_SMEM, st>>>(tf.items, d_shots, d_maps, kc, t,
+                                                           base, ck, gh, d_err);
+        else
+          k_ac_fwd_tma<0, false><<<ni, TPB, TMA_SMEM, st>>>(tf.items, d_shots, d_maps, kc, t,
+                                                            base, ck, gh, d_err);
+      } else {
+        ADS_FWD_MODE(true, false, tf.items, ni, st, ri_f);
+      }
+    } else {
+      ADS_FWD_MODE(true, false, tf.items, ni, st, ri_f);
+    }
     ADS_LAUNCHED(1);
   }
   if (np > 0) {
@@ -2934,6 +3249,16 @@ int64_t ads_acoustic_plan_resident_segments(const ads_acoustic_plan* plan) {
 
 int64_t ads_acoustic_plan_steps_per_block(const ads_acoustic_plan* plan) {
   return plan && plan->impl ? plan->impl->steps_per_block : -1;
+}
+
+int64_t ads_acoustic_plan_tma(const ads_acoustic_plan* plan) {
+  // the interior forward runs through the tensor maps only in the increment form
+  return plan && plan->impl ? (plan->impl->uses_tma && plan->impl->steps_per_block == 1) : -1;
+}
+
+int ads_acoustic_plan_device_status(ads_acoustic_plan* plan, ads_stream_t stream) {
+  ADS_REQUIRE(plan, "null plan");
+  return plan->impl->device_status((cudaStream_t)stream);
 }
 
 int ads_acoustic_plan_profile(ads_acoustic_plan* plan, const double* vp, const void* observed,

@@ -37,9 +37,11 @@ enum {
   ADS_ERR_INVALID = 1,     /* bad argument, shape or index */
   ADS_ERR_CUDA = 2,        /* CUDA runtime error (launch, device, copy) */
   ADS_ERR_NOMEM = 3,       /* device allocation failed */
-  ADS_ERR_UNSUPPORTED = 4  /* valid request outside what this build implements */
-  /* 5 is reserved: no kernel of this library waits on another block, flag or
-     device, so no call can time out on the device. */
+  ADS_ERR_UNSUPPORTED = 4, /* valid request outside what this build implements */
+  ADS_ERR_TIMEOUT = 5      /* a bounded wait on the device ran out (the tensor-map copies
+                              of the FP32 acoustic interior forward); reported by
+                              ads_acoustic_plan_device_status, the results of the calls
+                              since then are not valid */
 };
 
 enum { ADS_F64 = 0, ADS_F32 = 1 };          /* arithmetic / storage type */
@@ -284,7 +286,13 @@ typedef struct ads_acoustic_config {
   int32_t resident_mem_pct;  /* share of the device memory free at plan creation (after
                                 the plan's other buffers) those wavefields may use, in
                                 percent (1..95); 0 = 50 */
-  int32_t reserved[2];
+  int32_t tma;               /* FP32 plans: 1 = the interior forward steps read u, d and
+                                c through tensor-map tile copies (TMA) into shared
+                                memory, row chunks ahead (where the driver has the
+                                tensor-map encoder); 0 = the register-queue kernel
+                                (measured faster beside the concurrent PML launch).
+                                Results are identical either way. */
+  int32_t reserved[1];
 } ads_acoustic_config;
 
 typedef struct ads_acoustic_shot {
@@ -327,6 +335,14 @@ int64_t ads_acoustic_plan_resident_segments(const ads_acoustic_plan* plan);
 /* Forward steps per launch the plan runs (steps_per_block as configured, or as
  * the autotuner chose it); -1 for a null plan.  No reference counterpart. */
 int64_t ads_acoustic_plan_steps_per_block(const ads_acoustic_plan* plan);
+/* 1 when the plan's interior forward steps run through tensor-map copies (see
+ * ads_acoustic_config.tma), 0 when not, -1 for a null plan.  No reference
+ * counterpart. */
+int64_t ads_acoustic_plan_tma(const ads_acoustic_plan* plan);
+/* The plan's device-side status since its creation: ADS_OK, or ADS_ERR_TIMEOUT
+ * when a bounded wait of its kernels ran out (the results of the calls since
+ * then are not valid).  Synchronises the stream.  No reference counterpart. */
+int ads_acoustic_plan_device_status(ads_acoustic_plan* plan, ads_stream_t stream);
 /* Kernel timing: runs one gradient with direct launches (no graphs) and CUDA
  * events recorded around (0) the forward loop (k_ac_fwd launches only), (1)
  * one full checkpoint segment's recompute launches and (2) the same segment's

@@ -559,3 +559,38 @@ def test_fwi_lbfgs_reduces_misfit(ads, cuda):
     assert losses[-1] < 0.5 * l0, (l0, losses)
     assert np.all(vp >= 1500.0 - 1e-9) and np.all(vp <= 3500.0 + 1e-9)
     plan.close()
+
+
+@pytest.mark.parametrize("resident", [-1, 2])
+def test_tma_interior_forward_is_bitwise_the_register_kernel(ads, cuda, resident):
+    """FP32 plans with tma = 1 step their interior items through tensor-map
+    tile copies (k_ac_fwd_tma); the arithmetic is the register-queue kernel's,
+    so traces, loss and gradient are bitwise those of the default plan.
+    Uneven shots, odd checkpoint spacing and resident segments exercise the
+    ring (MODE 0, with checkpoints), the recompute (MODE 1) and the resident
+    store (MODE 2)."""
+    rng = np.random.default_rng(17)
+    MX, MY, npml = 360, 300, 20
+    shots = []
+    for k, (x0, nx, T) in enumerate([(0, 360, 70), (40, 250, 55), (100, 197, 64)]):
+        nr = 40
+        shots.append(dict(x0=x0, nx=nx, nstep=T, srci=[nx // 2 + k], srcj=[npml + 8],
+                          srcv=rng.standard_normal((T, 1)),
+                          rcvi=np.linspace(2, nx - 1, nr).astype(int), rcvj=np.full(nr, npml + 3)))
+    vp = torch.as_tensor(2000 + 800 * rng.random((MX + 2, MY + 2)), device="cuda")
+    out = {}
+    for tma in (1, 0):
+        plan = ads.AcousticPlan(MX, MY, 10.0, 10.0, 1e-3, shots, npml=npml, vp_ref=2400.0,
+                                precision="f32", ckpt_every=9, resident_segments=resident,
+                                rows_per_thread=4, tma=tma)
+        assert plan.uses_tma == (tma == 1)
+        obs = plan.forward(vp * 1.02).clone()
+        tr = plan.forward(vp).clone()
+        loss, grad = plan.gradient(vp, obs)
+        torch.cuda.synchronize()
+        plan.device_status()
+        out[tma] = (tr.cpu(), float(loss), grad.cpu())
+        plan.close()
+    assert torch.equal(out[1][0], out[0][0])
+    assert out[1][1] == out[0][1]
+    assert torch.equal(out[1][2], out[0][2])
