@@ -597,6 +597,8 @@ k_el_step_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
   const int i0 = max(i0r, 1), i_end = min(i0r + R, NX + 1);
   const int64_t fs = sh.fs, P = M.P;
   const int64_t bin = (int64_t)pin * NF * fs, bout = (int64_t)(1 - pin) * NF * fs;
+  // offsets within a field fit 32 bits (the plan checks (NX + 2) * P < 2^31)
+  const int P32 = (int)P, col = j + JOFF;
   const T* __restrict__ vx = sh.f[VX] + bin;
   const T* __restrict__ vy = sh.f[VY] + bin;
   const T* __restrict__ sxx = sh.f[SXX] + bin;
@@ -610,16 +612,14 @@ k_el_step_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
   T* __restrict__ st = STORE ? sh.store + (int64_t)store_slot * NSTORE * fs : nullptr;
   // stores of a lane's two cells: lane-dependent masks (column logic) use
   // scalar stores
-  auto stw = [&](T* p, int64_t o, const T (&x)[2], bool k0, bool k1) {
+  auto stw = [&](T* p, int o, const T (&x)[2], bool k0, bool k1) {
     if constexpr (GC) {
       st2s<T>(p, o, x, k0, k1);
     } else {
       st2p(p, o, x, k0, k1);
     }
   };
-  auto ld = [&](const T* p, int r) {
-    return ld2p(p, (int64_t)r * P + j + JOFF, colok && r >= 0 && r <= NX + 1);
-  };
+  auto ld = [&](const T* p, int r) { return ld2p(p, r * P32 + col, colok && r >= 0 && r <= NX + 1); };
   // memory variables 1..8 of the input / output buffer
   const T* __restrict__ m1i = sh.f[M1 + 0] + bin;
   const T* __restrict__ m2i = sh.f[M1 + 1] + bin;
@@ -661,7 +661,7 @@ k_el_step_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
   // memory variables m1..m4 of stress row s (onS) and m5..m8 of velocity row
   // s - VL (onV, where they can be nonzero), loaded one iteration ahead
   auto mload = [&](int s, bool onS, bool onV, V2<T> (&m)[8]) {
-    const int64_t o = (int64_t)s * P + j + JOFF, q = o - VL * P;
+    const int o = s * P32 + col, q = o - VL * P32;
     const bool vr = onV && own && s >= i0 + VL;
     if constexpr (GR) {
       m[0] = ld2p(m1i, o, onS && rs1(s) && lA);
@@ -710,7 +710,7 @@ k_el_step_rows(ElModel<T> M, const ElShot<T>* __restrict__ shots, const int* __r
                 Cn = ld(sxy, more ? s + 1 : -1);
     V2<T> mn[8] = {};
     mload(s + 1, more, vmore, mn);
-    const int64_t o = (int64_t)s * P + j + JOFF, q = o - VL * P;
+    const int o = s * P32 + col, q = o - VL * P32;
     // x profiles of stress row s and velocity row s - VL
     const int sx = min(max(s, 1), NX) - 1, vx_ = min(max(s - VL, 1), NX) - 1;
     const T axh = GR ? M.axh[sx] : T(0), bxh = GR ? M.bxh[sx] : T(1);
@@ -2383,11 +2383,13 @@ int ElPlan<T>::create(const ads_elastic_config& c, const ads_elastic_shot* shots
   ADS_REQUIRE(c.ckpt_every >= 0, "negative ckpt_every");
   ADS_REQUIRE(c.adjoint_passes == 0 || c.adjoint_passes == 1 || c.adjoint_passes == 3,
               "adjoint_passes must be 0, 1 or 3");
+  // the fused kernels index a field with 32-bit offsets (a field this size
+  // would not leave room for a plan on the device anyway)
+  ADS_REQUIRE((int64_t)(c.NX + 2) * grid_pitch(c.NY) < (int64_t(1) << 31),
+              "(NX + 2) x pitch must stay below 2^31 elements");
   // automatic (0): the fused adjoint for FP32 plans, the three passes for FP64
-  // plans (their fused kernel runs out of registers: measured 1.5x slower);
-  // the fused adjoint indexes a field with 32-bit offsets
-  fused = (c.adjoint_passes == 1 || (c.adjoint_passes == 0 && sizeof(T) == 4)) &&
-          (int64_t)(c.NX + 2) * grid_pitch(c.NY) < (int64_t(1) << 31);
+  // plans (their fused kernel runs out of registers: measured 1.5x slower)
+  fused = c.adjoint_passes == 1 || (c.adjoint_passes == 0 && sizeof(T) == 4);
   if (fused)
     if (int e = el_fadj_prepare<T>()) return e;
   nshots = (int)ns;

@@ -429,8 +429,7 @@ typedef struct ads_elastic_config {
                                 (ignored when rows_per_warp is set) */
   int32_t adjoint_passes;    /* the reverse sweep's adjoint step: 1 = one fused
                                 row-streaming pass (two adjoint state buffers, no
-                                intermediate fields in device memory; fields of fewer
-                                than 2^31 elements, else 3); 3 = three gather passes
+                                intermediate fields in device memory); 3 = three gather passes
                                 over intermediate fields, in place; 0 = 1 for FP32
                                 plans, 3 for FP64 plans */
   int32_t reserved[3];
