@@ -177,8 +177,8 @@ __device__ __forceinline__ Vec<T, C> ldv(const T* base, I off, bool on) {
   return x;
 }
 
-template <typename T, int C>
-__device__ __forceinline__ Vec<T, C> ldvp(const T* base, int64_t off, bool on) {
+template <typename T, int C, typename I = int64_t>
+__device__ __forceinline__ Vec<T, C> ldvp(const T* base, I off, bool on) {
   Vec<T, C> x;
   const T* p = base + off;
   if constexpr (C == 2 && sizeof(T) == 4) {
@@ -824,8 +824,8 @@ __device__ __forceinline__ double* grad_base(const AcShot<double>& sh) { return 
 // grad_c += g for a thread's C cells: the FP32 per-segment partial in FP32
 // plans, the FP64 accumulator in FP64 plans; one vector access when all C
 // cells are interior.
-template <typename T, int C>
-__device__ __forceinline__ void add_grad(const AcShot<T>& sh, int64_t row, const T (&g)[C], int j,
+template <typename T, int C, typename I = int64_t>
+__device__ __forceinline__ void add_grad(const AcShot<T>& sh, I row, const T (&g)[C], int j,
                                          int ny) {
   if (sizeof(T) == 4) {
     float* gp = sh.gc32 + row;
@@ -958,17 +958,18 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   const T* __restrict__ ty = sh.ty;
   const bool jld = j <= ny + 1;
   const bool hr = j + C <= ny + 1;
-  const int64_t col = j + JOFF;
+  // offsets within a field fit 32 bits (the plan checks fs < 2^31)
+  const int col = j + JOFF, P32 = (int)P;
   T tj[C];
 #pragma unroll
   for (int c = 0; c < C; c++) tj[c] = (j + c <= ny + 1) ? ty[j + c] : T(0);
   const bool tfree = warp_tau_free<T, C>(ty, j, ny);
   auto nz = [&](int r) { return !(tfree && sx[r] == T(0)); };
   // halo column of a warp-edge lane and its tau
-  const int64_t hoff = lane == 0 ? -1 : C;
+  const int hoff = lane == 0 ? -1 : C;
   const bool hon = (lane == 0 && jld) || (lane == 31 && hr);
   const T th = hon ? ty[j + (int)hoff] : T(0);
-  auto off = [&](int r) { return (int64_t)r * P + col; };
+  auto off = [&](int r) { return r * P32 + col; };
   const int i0 = it.i0 + (threadIdx.x >> 5) * ri, i_end = min(i0 + ri, nx + 1);
   if (i0 > nx) return;  // whole warps only: every later barrier is warp-level
   if (INT || interior_rows<T>(tfree, sx, i0, i_end, lane)) {
@@ -987,7 +988,7 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     auto load_halo = [&](int r, T& a, T& b, T& d) {
       a = b = d = T(0);
       if (hon && r < i_end) {
-        const int64_t o = off(r) + hoff;
+        const int o = off(r) + hoff;
         a = luc[o];
         b = cc[o];
         d = w[o];
@@ -1008,7 +1009,7 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       load_halo(i0 + q, hu[q], hcq[q], hwq[q]);
     }
     for (int i = i0; i < i_end; i++) {
-      const int64_t row = off(i);
+      const int row = off(i);
       const int rn = i + PF;
       const bool on1 = jld && rn + 1 <= i_end, on0 = jld && rn < i_end;
       V un = ldv<T, C>(luc, off(rn + 1), on1);
@@ -1100,7 +1101,7 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   V gq = ldvp<T, C>(lqc, off(i0), jld && n0), ln = ldvp<T, C>(lun, off(i0), jld);
   T hgu, hgq, hc, hw;
   {
-    const int64_t r = off(i0) + hoff;
+    const int r = off(i0) + hoff;
     hgu = ld1p(luc + r, hon);
     hgq = ld1p(lqc + r, hon && n0);
     hc = ld1p(cc + r, hon);
@@ -1108,7 +1109,7 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   }
   T sgm = sx[i0 - 1], sg0 = sx[i0];
   for (int i = i0; i < i_end; i++) {
-    const int64_t row = off(i);
+    const int row = off(i);
     const T sgp = sx[i + 1];
     V invp;
 #pragma unroll
@@ -1123,7 +1124,7 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     V w2 = ldvp<T, C>(w, off(i + 2), jld && more);
     V gqn = ldvp<T, C>(lqc, off(i + 1), jld && n1);
     V lnn = ldvp<T, C>(lun, off(i + 1), jld && more);
-    const int64_t rh = row + P + hoff;
+    const int rh = row + P32 + hoff;
     const T hgun = ld1p(luc + rh, more && hon), hgqn = ld1p(lqc + rh, more && hon && n1),
             hcn = ld1p(cc + rh, more && hon), hwn = ld1p(w + rh, more && hon);
     // j-direction terms of this thread's cells and of the neighbouring columns
