@@ -11,7 +11,7 @@ central finite differences of the FP64 plan's loss on 16 random cells.
 
 Tolerances (rel-L2 = ||x - x_ref|| / ||x_ref||):
   FP64 plan vs oracle                              1e-12
-  FP32 vs FP64, gradient (each field)              1e-4   (the benchmark spec's bound)
+  FP32 vs FP64, gradient (each field)              1e-4   (the FP32 accuracy target)
   FP32 vs FP64, all traces of a shot               1e-5
   C2 central differences (eps = 1e-4 vp)           1e-6 per cell
 
