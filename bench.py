@@ -48,7 +48,7 @@ BYTES = {
 
 # DRAM bytes (read + write) of one step of each kernel on the bench geometry
 # at 16 shots, from ncu --set full captures of both launches of a step
-TRAFFIC_16SHOT = {"k_ac_fwd": 148.9e6, "k_ac_adj": 246.2e6}
+TRAFFIC_16SHOT = {"k_ac_fwd": 148.9e6, "k_ac_adj": 245.3e6}
 
 
 def workload(nstep=3000, nshots=64, seed=1234):
