@@ -6,8 +6,10 @@
 // (fw1..fw4 + add_source).  Here the single-step operators are two kernels
 // (stresses: fw1+fw2; velocities: fw3+fw4, one thread per cell) and their
 // transpose three; the plans step with one fused row-streaming kernel plus a
-// tiny source/receiver launch, and run the adjoint as three gather-form
-// row-streaming kernels.  In the plans, per-cell work on the eight memory
+// tiny source/receiver launch, and run each adjoint step as one fused
+// row-streaming kernel (FP32 plans; FP64 plans by default, and any plan on
+// request, as three gather-form row-streaming kernels).  In the plans, per-cell
+// work on the eight memory
 // variables only runs where the 1D CPML profile is active (a != 0 or b != 1);
 // elsewhere the forward memory stays exactly zero and its adjoint never
 // reaches a gradient (it is multiplied by a = 0), so skipping it changes no
