@@ -447,3 +447,25 @@ def test_fused_adjoint_all_item_kinds_vs_oracle_and_three_passes(ads, orc, cuda,
         assert abs(f[0] - lref) <= 1e-12 * lref
         for k in range(3):
             assert rel(f[1 + k], sum(r[1 + k] for r in refs)) <= 1e-12
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+@pytest.mark.parametrize("resident", [-1, 2])
+def test_fused_adjoint_fp64_golden_loop(ads, cuda, use_graph, resident):
+    """The fused adjoint (adjoint_passes = 1) in an FP64 plan against the
+    golden loop (rel-L2 <= 1e-12), with and without graphs, with every segment
+    recomputed or the last two resident (the adjoint state alternates between
+    two buffers, so odd and even segment lengths both occur)."""
+    g = golden("elastic_small.npz")
+    p = params(ads, g)
+    plan = ads.ElasticPlan(p, shots_from(g), precision="f64", use_graph=use_graph,
+                           ckpt_every=7, resident_segments=resident, adjoint_passes=1)
+    assert all(n >= 0 for n in plan.adjoint_items) and sum(plan.adjoint_items) > 0
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=cuda)
+    loss, gl, gm, gr = plan.gradient(t(g["lam"]), t(g["mu"]), t(g["rho"]),
+                                     t(g["obs"].reshape(-1)))
+    torch.cuda.synchronize()
+    assert abs(float(loss) - float(g["loss"])) <= 1e-12 * float(g["loss"])
+    for a, k in ((gl, "grad_lambda"), (gm, "grad_mu"), (gr, "grad_rho")):
+        assert rel(a.cpu().numpy(), g[k]) <= 1e-12, k
+    plan.close()
