@@ -124,6 +124,7 @@ _SIGS = {
     "ads_elastic_plan_resident_segments": [P],
     "ads_elastic_plan_rows": [P, I32],
     "ads_acoustic_plan_tma": [P],
+    "ads_acoustic_plan_rows": [P, I32],
     "ads_acoustic_plan_device_status": [P, P],
     "ads_elastic_plan_gradient_ex": [P, P, P, P, P, P, P, P, P, P, P, P],
     "ads_elastic_plan_source_offset": [P, I64],
@@ -156,6 +157,7 @@ _RESTYPE = {
     "ads_elastic_plan_resident_segments": C.c_int64,
     "ads_elastic_plan_rows": C.c_int64,
     "ads_acoustic_plan_tma": C.c_int64,
+    "ads_acoustic_plan_rows": C.c_int64,
     "ads_elastic_plan_source_offset": C.c_int64,
 }
 EXPORTED = sorted(_SIGS)

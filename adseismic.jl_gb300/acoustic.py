@@ -225,6 +225,8 @@ class AcousticPlan:
         self.resident_segments = L.ads_acoustic_plan_resident_segments(h)
         self.steps_per_block = L.ads_acoustic_plan_steps_per_block(h)
         self.uses_tma = bool(L.ads_acoustic_plan_tma(h) == 1)
+        # rows per warp of the step items: forward / adjoint interior, forward / adjoint PML
+        self.rows = tuple(int(L.ads_acoustic_plan_rows(h, w)) for w in range(4))
 
     def device_status(self):
         """Raise AdsError (ADS_ERR_TIMEOUT) if a bounded wait of the plan's

@@ -78,7 +78,7 @@ struct Tile {
   static constexpr int WA = 32 * CA;  // columns of an adjoint strip
   // resident CTAs of TPB threads per SM the register allocation must allow
   // (general / interior-only kernels; 65536 / (TPB x MINB) registers a thread)
-  static constexpr int MINB_F = sizeof(T) == 4 ? ADS_MINB_F32 : 4;
+  static constexpr int MINB_F = sizeof(T) == 4 ? ADS_MINB_F32 : 3;
   static constexpr int MINB_A = sizeof(T) == 4 ? ADS_MINB_A32 : 4;
   static constexpr int MINB_FI = sizeof(T) == 4 ? ADS_MINB_FI32 : 6;
   static constexpr int MINB_AI = sizeof(T) == 4 ? ADS_MINB_AI32 : 5;
@@ -112,6 +112,9 @@ struct AcShot {
   T *seg, *ckpt;      // segment store (k+1 fields), checkpoints (nseg x 4 fields)
   T *lu, *lp, *lq;    // adjoint rings (2 fields each)
   T *c, *sx, *ty;     // c = vp^2 (pitched), PML profiles along i and j
+  // damping tables of the PML profiles (KT_N arrays each): along i, nx + 2
+  // entries per array, after sx; along j, ny + 2 entries, after ty
+  T *sxk, *tyk;
   double* gc;         // FP64 gradient accumulator (pitched)
   float* gc32;        // FP32 per-segment partial of grad_c (FP32 plans)
   const T* srcv;      // (nstep, nsrc), already multiplied by dt^2
@@ -119,6 +122,29 @@ struct AcShot {
   double* gsrc;       // d loss / d srcv, (nstep, nsrc) FP64
   const CellRef* src_list;  // the shot's sources (pitched cell, index, row)
 };
+
+// Damping tables of a PML profile s (sigma along i, tau along j), one array
+// each, computed in FP64 on the host and rounded once:
+//   r = 1 / (1 + s dt/2), ar = (1 - s dt/2) r, e = 1 - s dt,
+//   ex = s dt / (2 hx), ey = s dt / (2 hy).
+enum { KT_R, KT_AR, KT_E, KT_EX, KT_EY, KT_N };
+
+// The profile s followed by its KT_N tables.
+template <typename T>
+std::vector<T> with_tables(const std::vector<double>& s, double dt, double hx, double hy) {
+  const size_t n = s.size();
+  std::vector<T> o((1 + KT_N) * n);
+  for (size_t k = 0; k < n; k++) {
+    const double r = 1.0 / std::fma(s[k], 0.5 * dt, 1.0);
+    o[k] = (T)s[k];
+    o[(1 + KT_R) * n + k] = (T)r;
+    o[(1 + KT_AR) * n + k] = (T)(std::fma(-s[k], 0.5 * dt, 1.0) * r);
+    o[(1 + KT_E) * n + k] = (T)std::fma(-s[k], dt, 1.0);
+    o[(1 + KT_EX) * n + k] = (T)(s[k] * (dt / 2.0 / hx));
+    o[(1 + KT_EY) * n + k] = (T)(s[k] * (dt / 2.0 / hy));
+  }
+  return o;
+}
 
 template <typename T>
 struct AcConst {
@@ -342,6 +368,8 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   const T* __restrict__ cc = sh.c;
   const T* __restrict__ sx = sh.sx;
   const T* __restrict__ ty = sh.ty;
+  const T* __restrict__ sxk = sh.sxk;
+  const T* __restrict__ tyk = sh.tyk;
   const T* __restrict__ srcv = sh.srcv;
   const bool jld = j <= ny + 1;
   const bool hr = j + C <= ny + 1;  // right halo column exists (last lane of a warp)
@@ -446,108 +474,173 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     }
     if constexpr (!INT) record_traces<T, C, NOREC>(it, sh, rcvs, out, t, lane, i0, i_end);
   } else {
-  bool n0 = nz(i0);
-  V wm = ldvp<T, C>(w, off(i0 - 1), jld), w0 = ldvp<T, C>(w, off(i0), jld),
-    wp = ldvp<T, C>(w, off(i0 + 1), jld);
-  V pm = ldvp<T, C>(pin, off(i0 - 1), jld && nz(i0 - 1)), p0 = ldvp<T, C>(pin, off(i0), jld && n0),
-    pp = ldvp<T, C>(pin, off(i0 + 1), jld && nz(i0 + 1));
-  V q0 = ldvp<T, C>(qin, off(i0), jld && n0), wo0 = ldvp<T, C>(wo, off(i0), jld),
-    c0 = ldvp<T, C>(cc, off(i0), jld);
-  // lane 0: column j-1; lane 31: column j+C
-  const int64_t hoff = lane == 0 ? -1 : C;
-  const bool hon = (lane == 0 && jld) || (lane == 31 && hr);
-  T hw = ld1p(w + off(i0) + hoff, hon), hq = ld1p(qin + off(i0) + hoff, hon && n0);
-  for (int i = i0; i < i_end; i++) {
-    const int64_t row = off(i);
-    const bool more = i + 1 < i_end;
-    const bool n1 = more && nz(i + 1);
-    V wn = ldvp<T, C>(w, off(i + 2), jld && more);
-    V pn_ = ldvp<T, C>(pin, off(i + 2), jld && more && nz(i + 2));
-    V qn = ldvp<T, C>(qin, off(i + 1), jld && n1);
-    V won = ldvp<T, C>(wo, off(i + 1), jld && more);
-    V cn = ldvp<T, C>(cc, off(i + 1), jld && more);
-    const T hwn = ld1p(w + row + P + hoff, more && hon),
-            hqn = ld1p(qin + row + P + hoff, more && hon && n1);
-    T wL = __shfl_up_sync(FULL, w0.v[C - 1], 1), wR = __shfl_down_sync(FULL, w0.v[0], 1);
-    T qL = __shfl_up_sync(FULL, q0.v[C - 1], 1), qR = __shfl_down_sync(FULL, q0.v[0], 1);
-    if (lane == 0) {
-      wL = hw;
-      qL = hq;
-    } else if (lane == 31) {
-      wR = hw;
-      qR = hq;
-    }
-    if (jld) {
-      const T sg = sx[i];
-      V vo, po, qo, dv;
+  // The general (PML) form.  FP64 plans of variant W specialise it by the
+  // warp's kind (uniform over the warp): PK = 1 where tau = 0 at every column
+  // the warp reads (sigma rows only; the damping 1 / (1 + sigma dt/2) comes per
+  // row from the shot's reciprocal table), PK = 2 where sigma = 0 on every row
+  // it updates (tau columns only; the damping and the tau terms are per-thread
+  // constants), PK = 0 elsewhere (the corners, and every FP32 or variant-U
+  // warp).  The specialised forms drop terms that are exact zeros there and
+  // multiply by the tabulated reciprocal instead of dividing (within an ulp of
+  // the divide).  FP64 plans are bound by the FP64 issue rate, so the count of
+  // FP64 instructions is their cost.
+  auto pml_rows = [&](auto kd) {
+    constexpr int PK = decltype(kd)::value;
+    T rc[C], arc[C], bq[C], ext[C], eyt[C];  // PK 2: per-column constants
 #pragma unroll
-      for (int c = 0; c < C; c++) {
-        const T wS = c == 0 ? wL : w0.v[c - 1];
-        const T wN = c == C - 1 ? wR : w0.v[c + 1];
-        const T qS = c == 0 ? qL : q0.v[c - 1];
-        const T qN = c == C - 1 ? qR : q0.v[c + 1];
-        const T cv = c0.v[c], s = sg + tj[c];
-        T v;
-        if constexpr (INC) {
-          // d_{t} = [(1 - s dt/2) d_{t-1} + c (cx (u_{i+1} - u) + ...) - sigma tau dt^2 u
-          //          + phi / psi terms] / (1 + s dt/2), the three-level update less u_{t-1}
-          const T u0 = w0.v[c];
-          T dn = (T(1) - s * K.hdt) * wo0.v[c] +
-                 cv * (K.cx * ((wp.v[c] - u0) + (wm.v[c] - u0)) +
-                       K.cy * ((wN - u0) + (wS - u0))) -
-                 sg * tj[c] * K.dt2 * u0 + K.fx * (pp.v[c] - pm.v[c]) + K.fy * (qN - qS);
-          dn = pml_damp<T>(dn, s, K);
-          for (int e = it.src_b; e < it.src_e; e++) {
-            const CellRef r = srcs[e];
-            if (r.cell == row + c) dn += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
-          }
-          dv.v[c] = dn;
-          v = u0 + dn;
-        } else {
-          v = (T(2) - sg * tj[c] * K.dt2 - K.kxy * cv) * w0.v[c] +
-              cv * K.cx * (wp.v[c] + wm.v[c]) + cv * K.cy * (wN + wS) +
-              K.fx * (pp.v[c] - pm.v[c]) + K.fy * (qN - qS) - (T(1) - s * K.hdt) * wo0.v[c];
-          v = pml_damp<T>(v, s, K);
-          for (int e = it.src_b; e < it.src_e; e++) {
-            const CellRef r = srcs[e];
-            if (r.cell == row + c) v += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
-          }
-        }
-        vo.v[c] = v;
-        if constexpr (!VU) {
-          po.v[c] = (T(1) - K.dt * sg) * p0.v[c] + K.ex * cv * (tj[c] - sg) * (wp.v[c] - wm.v[c]);
-          qo.v[c] = (T(1) - K.dt * tj[c]) * q0.v[c] + K.ey * cv * (sg - tj[c]) * (wN - wS);
-        }
-      }
-      stv<T, C>(out, row, vo, j, ny);
-      if constexpr (INC) stv<T, C>(dd, row, dv, j, ny);
-      if (!VU && n0) {
-        stv<T, C>(pout, row, po, j, ny);
-        stv<T, C>(qout, row, qo, j, ny);
-      }
-      if (ck_on) {
-        T* ck = sh.ckpt + (int64_t)ckpt_slot * 4 * fs;
-        stv<T, C>(ck, row, vo, j, ny);
-        stv<T, C>(ck + fs, row, INC ? dv : w0, j, ny);
-        if (n0) {
-          stv<T, C>(ck + 2 * fs, row, VU ? p0 : po, j, ny);
-          stv<T, C>(ck + 3 * fs, row, VU ? q0 : qo, j, ny);
+    for (int c = 0; c < C; c++) {
+      rc[c] = arc[c] = bq[c] = T(1);
+      ext[c] = eyt[c] = T(0);
+      if constexpr (PK == 2) {
+        if (j + c <= ny + 1) {
+          const int n = ny + 2, q = j + c;
+          rc[c] = tyk[KT_R * n + q];
+          arc[c] = tyk[KT_AR * n + q];
+          bq[c] = tyk[KT_E * n + q];
+          ext[c] = tyk[KT_EX * n + q];
+          eyt[c] = tyk[KT_EY * n + q];
         }
       }
     }
-    wm = w0;
-    w0 = wp;
-    wp = wn;
-    pm = p0;
-    p0 = pp;
-    pp = pn_;
-    q0 = qn;
-    wo0 = won;
-    c0 = cn;
-    hw = hwn;
-    hq = hqn;
-    n0 = n1;
+    bool n0 = nz(i0);
+    V wm = ldvp<T, C>(w, off(i0 - 1), jld), w0 = ldvp<T, C>(w, off(i0), jld),
+      wp = ldvp<T, C>(w, off(i0 + 1), jld);
+    V pm = ldvp<T, C>(pin, off(i0 - 1), jld && nz(i0 - 1)), p0 = ldvp<T, C>(pin, off(i0), jld && n0),
+      pp = ldvp<T, C>(pin, off(i0 + 1), jld && nz(i0 + 1));
+    V q0 = ldvp<T, C>(qin, off(i0), jld && n0), wo0 = ldvp<T, C>(wo, off(i0), jld),
+      c0 = ldvp<T, C>(cc, off(i0), jld);
+    // lane 0: column j-1; lane 31: column j+C
+    const int64_t hoff = lane == 0 ? -1 : C;
+    const bool hon = (lane == 0 && jld) || (lane == 31 && hr);
+    T hw = ld1p(w + off(i0) + hoff, hon), hq = ld1p(qin + off(i0) + hoff, hon && n0);
+    for (int i = i0; i < i_end; i++) {
+      const int64_t row = off(i);
+      const bool more = i + 1 < i_end;
+      const bool n1 = more && nz(i + 1);
+      V wn = ldvp<T, C>(w, off(i + 2), jld && more);
+      V pn_ = ldvp<T, C>(pin, off(i + 2), jld && more && nz(i + 2));
+      V qn = ldvp<T, C>(qin, off(i + 1), jld && n1);
+      V won = ldvp<T, C>(wo, off(i + 1), jld && more);
+      V cn = ldvp<T, C>(cc, off(i + 1), jld && more);
+      const T hwn = ld1p(w + row + P + hoff, more && hon),
+              hqn = ld1p(qin + row + P + hoff, more && hon && n1);
+      T wL = __shfl_up_sync(FULL, w0.v[C - 1], 1), wR = __shfl_down_sync(FULL, w0.v[0], 1);
+      T qL = __shfl_up_sync(FULL, q0.v[C - 1], 1), qR = __shfl_down_sync(FULL, q0.v[0], 1);
+      if (lane == 0) {
+        wL = hw;
+        qL = hq;
+      } else if (lane == 31) {
+        wR = hw;
+        qR = hq;
+      }
+      if (jld) {
+        const T sg = PK == 2 ? T(0) : sx[i];
+        T ar_r = T(1), r_r = T(1), e_r = T(1), exs = T(0), eys = T(0);  // PK 1: row constants
+        if constexpr (PK == 1) {
+          const int n = nx + 2;
+          r_r = sxk[KT_R * n + i];
+          ar_r = sxk[KT_AR * n + i];
+          e_r = sxk[KT_E * n + i];
+          exs = sxk[KT_EX * n + i];
+          eys = sxk[KT_EY * n + i];
+        }
+        V vo, po, qo, dv;
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+          const T wS = c == 0 ? wL : w0.v[c - 1];
+          const T wN = c == C - 1 ? wR : w0.v[c + 1];
+          const T qS = c == 0 ? qL : q0.v[c - 1];
+          const T qN = c == C - 1 ? qR : q0.v[c + 1];
+          const T cv = c0.v[c], s = sg + tj[c];
+          T v;
+          if constexpr (PK != 0) {
+            // three-level form, sigma tau = 0: s = sigma (PK 1) or tau (PK 2)
+            v = ((T(2) - K.kxy * cv) * w0.v[c] + cv * K.cx * (wp.v[c] + wm.v[c]) +
+                 cv * K.cy * (wN + wS) + K.fx * (pp.v[c] - pm.v[c]) + K.fy * (qN - qS)) *
+                    (PK == 1 ? r_r : rc[c]) -
+                (PK == 1 ? ar_r : arc[c]) * wo0.v[c];
+            for (int e = it.src_b; e < it.src_e; e++) {
+              const CellRef r = srcs[e];
+              if (r.cell == row + c) v += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
+            }
+            if constexpr (PK == 1) {
+              po.v[c] = e_r * p0.v[c] - exs * cv * (wp.v[c] - wm.v[c]);
+              qo.v[c] = q0.v[c] + eys * cv * (wN - wS);
+            } else {
+              po.v[c] = p0.v[c] + ext[c] * cv * (wp.v[c] - wm.v[c]);
+              qo.v[c] = bq[c] * q0.v[c] - eyt[c] * cv * (wN - wS);
+            }
+          } else if constexpr (INC) {
+            // d_{t} = [(1 - s dt/2) d_{t-1} + c (cx (u_{i+1} - u) + ...) - sigma tau dt^2 u
+            //          + phi / psi terms] / (1 + s dt/2), the three-level update less u_{t-1}
+            const T u0 = w0.v[c];
+            T dn = (T(1) - s * K.hdt) * wo0.v[c] +
+                   cv * (K.cx * ((wp.v[c] - u0) + (wm.v[c] - u0)) +
+                         K.cy * ((wN - u0) + (wS - u0))) -
+                   sg * tj[c] * K.dt2 * u0 + K.fx * (pp.v[c] - pm.v[c]) + K.fy * (qN - qS);
+            dn = pml_damp<T>(dn, s, K);
+            for (int e = it.src_b; e < it.src_e; e++) {
+              const CellRef r = srcs[e];
+              if (r.cell == row + c) dn += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
+            }
+            dv.v[c] = dn;
+            v = u0 + dn;
+          } else {
+            v = (T(2) - sg * tj[c] * K.dt2 - K.kxy * cv) * w0.v[c] +
+                cv * K.cx * (wp.v[c] + wm.v[c]) + cv * K.cy * (wN + wS) +
+                K.fx * (pp.v[c] - pm.v[c]) + K.fy * (qN - qS) - (T(1) - s * K.hdt) * wo0.v[c];
+            v = pml_damp<T>(v, s, K);
+            for (int e = it.src_b; e < it.src_e; e++) {
+              const CellRef r = srcs[e];
+              if (r.cell == row + c) v += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
+            }
+          }
+          vo.v[c] = v;
+          if constexpr (!VU && PK == 0) {
+            po.v[c] = (T(1) - K.dt * sg) * p0.v[c] + K.ex * cv * (tj[c] - sg) * (wp.v[c] - wm.v[c]);
+            qo.v[c] = (T(1) - K.dt * tj[c]) * q0.v[c] + K.ey * cv * (sg - tj[c]) * (wN - wS);
+          }
+        }
+        stv<T, C>(out, row, vo, j, ny);
+        if constexpr (INC) stv<T, C>(dd, row, dv, j, ny);
+        if (!VU && n0) {
+          stv<T, C>(pout, row, po, j, ny);
+          stv<T, C>(qout, row, qo, j, ny);
+        }
+        if (ck_on) {
+          T* ck = sh.ckpt + (int64_t)ckpt_slot * 4 * fs;
+          stv<T, C>(ck, row, vo, j, ny);
+          stv<T, C>(ck + fs, row, INC ? dv : w0, j, ny);
+          if (n0) {
+            stv<T, C>(ck + 2 * fs, row, VU ? p0 : po, j, ny);
+            stv<T, C>(ck + 3 * fs, row, VU ? q0 : qo, j, ny);
+          }
+        }
+      }
+      wm = w0;
+      w0 = wp;
+      wp = wn;
+      pm = p0;
+      p0 = pp;
+      pp = pn_;
+      q0 = qn;
+      wo0 = won;
+      c0 = cn;
+      hw = hwn;
+      hq = hqn;
+      n0 = n1;
+    }
+  };
+  constexpr bool SPEC = sizeof(T) == 8 && !VU && !INC;
+  bool sfree = false;
+  if constexpr (SPEC) {
+    bool z = true;
+    for (int r = i0 + lane; r < i_end; r += 32) z = z && sx[r] == T(0);
+    sfree = __all_sync(FULL, z);
   }
+  if (SPEC && tfree) pml_rows(std::integral_constant<int, SPEC ? 1 : 0>{});
+  else if (SPEC && sfree) pml_rows(std::integral_constant<int, SPEC ? 2 : 0>{});
+  else pml_rows(std::integral_constant<int, 0>{});
   record_traces<T, C, NOREC>(it, sh, rcvs, out, t, lane, i0, i_end);
   }
 }
@@ -956,6 +1049,8 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   const T* __restrict__ cc = sh.c;
   const T* __restrict__ sx = sh.sx;
   const T* __restrict__ ty = sh.ty;
+  const T* __restrict__ sxk = sh.sxk;
+  const T* __restrict__ tyk = sh.tyk;
   const bool jld = j <= ny + 1;
   const bool hr = j + C <= ny + 1;
   // offsets within a field fit 32 bits (the plan checks fs < 2^31)
@@ -1082,122 +1177,224 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       record_src_grad<T, C, VU>(it, sh, srcs, lun, lpc, lqc, K, k, lane, i0, i_end, dt2);
     }
   } else {
-  // rows i-1 (m), i (0), i+1 (p): lambdaU_k, lambdaPhi_k, c and 1/den per cell
-  V gum = ldvp<T, C>(luc, off(i0 - 1), jld), gpm = ldvp<T, C>(lpc, off(i0 - 1), jld && nz(i0 - 1)),
-    cm = ldvp<T, C>(cc, off(i0 - 1), jld);
-  V gu0 = ldvp<T, C>(luc, off(i0), jld), gp0 = ldvp<T, C>(lpc, off(i0), jld && nz(i0)),
-    c0 = ldvp<T, C>(cc, off(i0), jld);
-  V gu1 = ldvp<T, C>(luc, off(i0 + 1), jld), gp1 = ldvp<T, C>(lpc, off(i0 + 1), jld && nz(i0 + 1)),
-    c1 = ldvp<T, C>(cc, off(i0 + 1), jld);
-  V invm, inv0;
-#pragma unroll
-  for (int c = 0; c < C; c++) {
-    invm.v[c] = inv_den<T>(sx[i0 - 1] + tj[c], K);
-    inv0.v[c] = inv_den<T>(sx[i0] + tj[c], K);
-  }
-  V wm = ldvp<T, C>(w, off(i0 - 1), jld), w0 = ldvp<T, C>(w, off(i0), jld),
-    wp = ldvp<T, C>(w, off(i0 + 1), jld);
-  bool n0 = nz(i0);
-  V gq = ldvp<T, C>(lqc, off(i0), jld && n0), ln = ldvp<T, C>(lun, off(i0), jld);
-  T hgu, hgq, hc, hw;
-  {
-    const int r = off(i0) + hoff;
-    hgu = ld1p(luc + r, hon);
-    hgq = ld1p(lqc + r, hon && n0);
-    hc = ld1p(cc + r, hon);
-    hw = ld1p(w + r, hon);
-  }
-  T sgm = sx[i0 - 1], sg0 = sx[i0];
-  for (int i = i0; i < i_end; i++) {
-    const int row = off(i);
-    const T sgp = sx[i + 1];
-    V invp;
-#pragma unroll
-    for (int c = 0; c < C; c++) invp.v[c] = inv_den<T>(sgp + tj[c], K);
-    // prefetch: row i+2 (lambdaU_k, lambdaPhi_k, c, u_{k-1}), row i+1 (lambdaPsi_k,
-    // lambdaU_{k+1}) and the halo cell of row i+1
-    const bool more = i + 1 < i_end;
-    const bool n1 = more && nz(i + 1);
-    V gu2 = ldvp<T, C>(luc, off(i + 2), jld && more);
-    V gp2 = ldvp<T, C>(lpc, off(i + 2), jld && more && nz(i + 2));
-    V c2 = ldvp<T, C>(cc, off(i + 2), jld && more);
-    V w2 = ldvp<T, C>(w, off(i + 2), jld && more);
-    V gqn = ldvp<T, C>(lqc, off(i + 1), jld && n1);
-    V lnn = ldvp<T, C>(lun, off(i + 1), jld && more);
-    const int rh = row + P32 + hoff;
-    const T hgun = ld1p(luc + rh, more && hon), hgqn = ld1p(lqc + rh, more && hon && n1),
-            hcn = ld1p(cc + rh, more && hon), hwn = ld1p(w + rh, more && hon);
-    // j-direction terms of this thread's cells and of the neighbouring columns
-    T YP[C], YM[C], YR[C], gui[C];
+  // The general (PML) form.  FP64 plans of variant W specialise it by the
+  // warp's kind, as k_ac_fwd does: PK = 1 where tau = 0 at every column the
+  // warp reads (1/den and the sigma terms per row from the damping tables),
+  // PK = 2 where sigma = 0 on rows i0-1 .. i_end (1/den and the tau terms
+  // per-thread constants), PK = 0 elsewhere.
+  auto pml_rows = [&](auto kd) {
+    constexpr int PK = decltype(kd)::value;
+    const int nr = nx + 2, ncol = ny + 2;
+    // PK 2: the tables at this thread's columns and at its halo column
+    T rc[C], arc[C], bq[C], ext[C], eyt[C], hrc = T(1), heyt = T(0);
 #pragma unroll
     for (int c = 0; c < C; c++) {
-      gui[c] = gu0.v[c] * inv0.v[c];
-      col_terms<T>(gui[c], gq.v[c], c0.v[c], sg0, tj[c], K, YP[c], YM[c], YR[c]);
-    }
-    T YPl = __shfl_up_sync(FULL, YP[C - 1], 1), YRl = __shfl_up_sync(FULL, YR[C - 1], 1);
-    T YMr = __shfl_down_sync(FULL, YM[0], 1), YRr = __shfl_down_sync(FULL, YR[0], 1);
-    T wL = __shfl_up_sync(FULL, w0.v[C - 1], 1), wR = __shfl_down_sync(FULL, w0.v[0], 1);
-    if (lane == 0 || lane == 31) {
-      T a = 0, b = 0, r = 0;
-      if (hon) col_terms<T>(hgu * inv_den<T>(sg0 + th, K), hgq, hc, sg0, th, K, a, b, r);
-      if (lane == 0) {
-        YPl = a;
-        YRl = r;
-        wL = hw;
-      } else {
-        YMr = b;
-        YRr = r;
-        wR = hw;
+      rc[c] = arc[c] = bq[c] = T(1);
+      ext[c] = eyt[c] = T(0);
+      if constexpr (PK == 2) {
+        if (j + c <= ny + 1) {
+          const int q = j + c;
+          rc[c] = tyk[KT_R * ncol + q];
+          arc[c] = tyk[KT_AR * ncol + q];
+          bq[c] = tyk[KT_E * ncol + q];
+          ext[c] = tyk[KT_EX * ncol + q];
+          eyt[c] = tyk[KT_EY * ncol + q];
+        }
       }
     }
-    if (jld) {
-      V nu, np, nq;
-      T g[C];
+    if constexpr (PK == 2) {
+      if (hon) {
+        hrc = tyk[KT_R * ncol + j + hoff];
+        heyt = tyk[KT_EY * ncol + j + hoff];
+      }
+    }
+    // phi / psi may be non-zero in row r (always, where tau != 0)
+    auto nzk = [&](int r) { return PK == 2 || nz(r); };
+    // 1/den of the cell in row r, column j + c
+    auto invd = [&](int r, int c) -> T {
+      if constexpr (PK == 1) return sxk[KT_R * nr + r];
+      else if constexpr (PK == 2) return rc[c];
+      else return inv_den<T>(sx[r] + tj[c], K);
+    };
+    // rows i-1 (m), i (0), i+1 (p): lambdaU_k, lambdaPhi_k, c and 1/den per cell
+    V gum = ldvp<T, C>(luc, off(i0 - 1), jld), gpm = ldvp<T, C>(lpc, off(i0 - 1), jld && nzk(i0 - 1)),
+      cm = ldvp<T, C>(cc, off(i0 - 1), jld);
+    V gu0 = ldvp<T, C>(luc, off(i0), jld), gp0 = ldvp<T, C>(lpc, off(i0), jld && nzk(i0)),
+      c0 = ldvp<T, C>(cc, off(i0), jld);
+    V gu1 = ldvp<T, C>(luc, off(i0 + 1), jld), gp1 = ldvp<T, C>(lpc, off(i0 + 1), jld && nzk(i0 + 1)),
+      c1 = ldvp<T, C>(cc, off(i0 + 1), jld);
+    V invm, inv0;
+    V gim, gi0;  // lambdaU_k / den of rows i-1, i (carried down the rows)
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      invm.v[c] = invd(i0 - 1, c);
+      inv0.v[c] = invd(i0, c);
+      gim.v[c] = gum.v[c] * invm.v[c];
+      gi0.v[c] = gu0.v[c] * inv0.v[c];
+    }
+    V wm = ldvp<T, C>(w, off(i0 - 1), jld), w0 = ldvp<T, C>(w, off(i0), jld),
+      wp = ldvp<T, C>(w, off(i0 + 1), jld);
+    bool n0 = nzk(i0);
+    V gq = ldvp<T, C>(lqc, off(i0), jld && n0), ln = ldvp<T, C>(lun, off(i0), jld);
+    T hgu, hgq, hc, hw;
+    {
+      const int r = off(i0) + hoff;
+      hgu = ld1p(luc + r, hon);
+      hgq = ld1p(lqc + r, hon && n0);
+      hc = ld1p(cc + r, hon);
+      hw = ld1p(w + r, hon);
+    }
+    T sgm = PK == 2 ? T(0) : sx[i0 - 1], sg0 = PK == 2 ? T(0) : sx[i0];
+    for (int i = i0; i < i_end; i++) {
+      const int row = off(i);
+      const T sgp = PK == 2 ? T(0) : sx[i + 1];
+      V invp, gip;
 #pragma unroll
       for (int c = 0; c < C; c++) {
-        const T ypl = c == 0 ? YPl : YP[c - 1], yrl = c == 0 ? YRl : YR[c - 1];
-        const T ymr = c == C - 1 ? YMr : YM[c + 1], yrr = c == C - 1 ? YRr : YR[c + 1];
-        const T wS = c == 0 ? wL : w0.v[c - 1], wN = c == C - 1 ? wR : w0.v[c + 1];
-        const T guim = gum.v[c] * invm.v[c], guip = gu1.v[c] * invp.v[c];
-        const T XPm = cm.v[c] * K.cx * guim + K.ex * cm.v[c] * (tj[c] - sgm) * gpm.v[c];
-        const T XMp = c1.v[c] * K.cx * guip - K.ex * c1.v[c] * (tj[c] - sgp) * gp1.v[c];
-        const T cv = c0.v[c], s = sg0 + tj[c];
-        nu.v[c] = -(T(1) - s * K.hdt) * inv0.v[c] * ln.v[c] +
-                  (T(2) - sg0 * tj[c] * K.dt2 - K.kxy * cv) * gui[c] + XPm + XMp + ypl + ymr;
-        if constexpr (!VU) {
-          np.v[c] = (T(1) - K.dt * sg0) * gp0.v[c] + K.fx * guim - K.fx * guip;
-          nq.v[c] = (T(1) - K.dt * tj[c]) * gq.v[c] + yrl - yrr;
+        invp.v[c] = invd(i + 1, c);
+        gip.v[c] = gu1.v[c] * invp.v[c];
+      }
+      // PK 1: the sigma terms of rows i-1, i, i+1 from the damping tables
+      T exm = T(0), ex0 = T(0), exp_ = T(0), eys0 = T(0), ar0 = T(1), e0 = T(1);
+      if constexpr (PK == 1) {
+        exm = sxk[KT_EX * nr + i - 1];
+        ex0 = sxk[KT_EX * nr + i];
+        exp_ = sxk[KT_EX * nr + i + 1];
+        eys0 = sxk[KT_EY * nr + i];
+        ar0 = sxk[KT_AR * nr + i];
+        e0 = sxk[KT_E * nr + i];
+      }
+      // prefetch: row i+2 (lambdaU_k, lambdaPhi_k, c, u_{k-1}), row i+1 (lambdaPsi_k,
+      // lambdaU_{k+1}) and the halo cell of row i+1
+      const bool more = i + 1 < i_end;
+      const bool n1 = more && nzk(i + 1);
+      V gu2 = ldvp<T, C>(luc, off(i + 2), jld && more);
+      V gp2 = ldvp<T, C>(lpc, off(i + 2), jld && more && nzk(i + 2));
+      V c2 = ldvp<T, C>(cc, off(i + 2), jld && more);
+      V w2 = ldvp<T, C>(w, off(i + 2), jld && more);
+      V gqn = ldvp<T, C>(lqc, off(i + 1), jld && n1);
+      V lnn = ldvp<T, C>(lun, off(i + 1), jld && more);
+      const int rh = row + P32 + hoff;
+      const T hgun = ld1p(luc + rh, more && hon), hgqn = ld1p(lqc + rh, more && hon && n1),
+              hcn = ld1p(cc + rh, more && hon), hwn = ld1p(w + rh, more && hon);
+      // j-direction terms of this thread's cells and of the neighbouring columns
+      T YP[C], YM[C], YR[C], gui[C];
+#pragma unroll
+      for (int c = 0; c < C; c++) {
+        gui[c] = gi0.v[c];
+        if constexpr (PK == 0) {
+          col_terms<T>(gui[c], gq.v[c], c0.v[c], sg0, tj[c], K, YP[c], YM[c], YR[c]);
+        } else {
+          const T by = c0.v[c] * K.cy * gui[c];
+          const T eyg = (PK == 1 ? eys0 : -eyt[c]) * c0.v[c] * gq.v[c];
+          YP[c] = by + eyg;
+          YM[c] = by - eyg;
+          YR[c] = K.fy * gui[c];
         }
-        T dx_ = wp.v[c] - wm.v[c], dy_ = wN - wS;
-        if constexpr (VU) {
-          // u_{k-1} without its source value, as the forward pre-pass used it
-          if (k - 1 >= 2 && it.src_e > it.src_b) {
-            const T sp = src_at(it, sh, srcs, row + P + c, k - 1),
-                    sm = src_at(it, sh, srcs, row - P + c, k - 1);
-            const T sn = src_at(it, sh, srcs, row + c + 1, k - 1),
-                    ss = src_at(it, sh, srcs, row + c - 1, k - 1);
-            dx_ = (wp.v[c] - sp) - (wm.v[c] - sm);
-            dy_ = (wN - sn) - (wS - ss);
+      }
+      T YPl = __shfl_up_sync(FULL, YP[C - 1], 1), YRl = __shfl_up_sync(FULL, YR[C - 1], 1);
+      T YMr = __shfl_down_sync(FULL, YM[0], 1), YRr = __shfl_down_sync(FULL, YR[0], 1);
+      T wL = __shfl_up_sync(FULL, w0.v[C - 1], 1), wR = __shfl_down_sync(FULL, w0.v[0], 1);
+      if (lane == 0 || lane == 31) {
+        T a = 0, b = 0, r = 0;
+        if (hon) {
+          if constexpr (PK == 0) {
+            col_terms<T>(hgu * inv_den<T>(sg0 + th, K), hgq, hc, sg0, th, K, a, b, r);
+          } else {
+            // PK 1: tau = 0 at the halo column too, so its 1/den is the row's
+            const T hg = hgu * (PK == 1 ? inv0.v[0] : hrc);
+            const T by = hc * K.cy * hg, eyg = (PK == 1 ? eys0 : -heyt) * hc * hgq;
+            a = by + eyg;
+            b = by - eyg;
+            r = K.fy * hg;
           }
         }
-        g[c] = (-K.kxy * w0.v[c] + K.cx * (wp.v[c] + wm.v[c]) + K.cy * (wN + wS)) * gui[c] +
-               K.ex * (tj[c] - sg0) * dx_ * gp0.v[c] + K.ey * (sg0 - tj[c]) * dy_ * gq.v[c];
+        if (lane == 0) {
+          YPl = a;
+          YRl = r;
+          wL = hw;
+        } else {
+          YMr = b;
+          YRr = r;
+          wR = hw;
+        }
       }
-      stv<T, C>(lun, row, nu, j, ny);
-      if (!VU && n0) {
-        stv<T, C>(lpo, row, np, j, ny);
-        stv<T, C>(lqo, row, nq, j, ny);
+      if (jld) {
+        V nu, np, nq;
+        T g[C];
+#pragma unroll
+        for (int c = 0; c < C; c++) {
+          const T ypl = c == 0 ? YPl : YP[c - 1], yrl = c == 0 ? YRl : YR[c - 1];
+          const T ymr = c == C - 1 ? YMr : YM[c + 1], yrr = c == C - 1 ? YRr : YR[c + 1];
+          const T wS = c == 0 ? wL : w0.v[c - 1], wN = c == C - 1 ? wR : w0.v[c + 1];
+          const T guim = gim.v[c], guip = gip.v[c];
+          const T cv = c0.v[c];
+          if constexpr (PK == 0) {
+            const T XPm = cm.v[c] * K.cx * guim + K.ex * cm.v[c] * (tj[c] - sgm) * gpm.v[c];
+            const T XMp = c1.v[c] * K.cx * guip - K.ex * c1.v[c] * (tj[c] - sgp) * gp1.v[c];
+            const T s = sg0 + tj[c];
+            nu.v[c] = -(T(1) - s * K.hdt) * inv0.v[c] * ln.v[c] +
+                      (T(2) - sg0 * tj[c] * K.dt2 - K.kxy * cv) * gui[c] + XPm + XMp + ypl + ymr;
+            if constexpr (!VU) {
+              np.v[c] = (T(1) - K.dt * sg0) * gp0.v[c] + K.fx * guim - K.fx * guip;
+              nq.v[c] = (T(1) - K.dt * tj[c]) * gq.v[c] + yrl - yrr;
+            }
+          } else {
+            // sigma tau = 0; PK 1: tau = 0, PK 2: sigma = 0 (tables / constants)
+            const T XPm = cm.v[c] * (K.cx * guim + (PK == 1 ? -exm : ext[c]) * gpm.v[c]);
+            const T XMp = c1.v[c] * (K.cx * guip + (PK == 1 ? exp_ : -ext[c]) * gp1.v[c]);
+            nu.v[c] = -(PK == 1 ? ar0 : arc[c]) * ln.v[c] + (T(2) - K.kxy * cv) * gui[c] + XPm +
+                      XMp + ypl + ymr;
+            np.v[c] = (PK == 1 ? e0 * gp0.v[c] : gp0.v[c]) + K.fx * (guim - guip);
+            nq.v[c] = (PK == 1 ? gq.v[c] : bq[c] * gq.v[c]) + yrl - yrr;
+          }
+          T dx_ = wp.v[c] - wm.v[c], dy_ = wN - wS;
+          if constexpr (VU) {
+            // u_{k-1} without its source value, as the forward pre-pass used it
+            if (k - 1 >= 2 && it.src_e > it.src_b) {
+              const T sp = src_at(it, sh, srcs, row + P + c, k - 1),
+                      sm = src_at(it, sh, srcs, row - P + c, k - 1);
+              const T sn = src_at(it, sh, srcs, row + c + 1, k - 1),
+                      ss = src_at(it, sh, srcs, row + c - 1, k - 1);
+              dx_ = (wp.v[c] - sp) - (wm.v[c] - sm);
+              dy_ = (wN - sn) - (wS - ss);
+            }
+          }
+          if constexpr (PK == 0)
+            g[c] = (-K.kxy * w0.v[c] + K.cx * (wp.v[c] + wm.v[c]) + K.cy * (wN + wS)) * gui[c] +
+                   K.ex * (tj[c] - sg0) * dx_ * gp0.v[c] + K.ey * (sg0 - tj[c]) * dy_ * gq.v[c];
+          else
+            g[c] = (-K.kxy * w0.v[c] + K.cx * (wp.v[c] + wm.v[c]) + K.cy * (wN + wS)) * gui[c] +
+                   (PK == 1 ? -ex0 : ext[c]) * dx_ * gp0.v[c] +
+                   (PK == 1 ? eys0 : -eyt[c]) * dy_ * gq.v[c];
+        }
+        stv<T, C>(lun, row, nu, j, ny);
+        if (!VU && n0) {
+          stv<T, C>(lpo, row, np, j, ny);
+          stv<T, C>(lqo, row, nq, j, ny);
+        }
+        add_grad<T, C>(sh, row, g, j, ny);
       }
-      add_grad<T, C>(sh, row, g, j, ny);
+      gim = gi0; gpm = gp0; cm = c0; sgm = sg0;
+      gi0 = gip;
+      gu0 = gu1; gp0 = gp1; c0 = c1; inv0 = invp; sg0 = sgp;
+      gu1 = gu2; gp1 = gp2; c1 = c2;
+      wm = w0; w0 = wp; wp = w2;
+      gq = gqn; ln = lnn;
+      hgu = hgun; hgq = hgqn; hc = hcn; hw = hwn;
+      n0 = n1;
     }
-    gum = gu0; gpm = gp0; cm = c0; invm = inv0; sgm = sg0;
-    gu0 = gu1; gp0 = gp1; c0 = c1; inv0 = invp; sg0 = sgp;
-    gu1 = gu2; gp1 = gp2; c1 = c2;
-    wm = w0; w0 = wp; wp = w2;
-    gq = gqn; ln = lnn;
-    hgu = hgun; hgq = hgqn; hc = hcn; hw = hwn;
-    n0 = n1;
+  };
+  constexpr bool SPEC = sizeof(T) == 8 && !VU;
+  bool sfree = false;
+  if constexpr (SPEC) {
+    bool z = true;
+    for (int r = i0 - 1 + lane; r <= i_end; r += 32) z = z && sx[r] == T(0);
+    sfree = __all_sync(FULL, z);
   }
+  if (SPEC && tfree) pml_rows(std::integral_constant<int, SPEC ? 1 : 0>{});
+  else if (SPEC && sfree) pml_rows(std::integral_constant<int, SPEC ? 2 : 0>{});
+  else pml_rows(std::integral_constant<int, 0>{});
   inject_residuals<T, C>(it, sh, rcvs, lun, k, lane, i0, i_end);
   record_src_grad<T, C, VU>(it, sh, srcs, lun, lpc, lqc, K, k, lane, i0, i_end, dt2);
   }
@@ -1720,6 +1917,7 @@ struct AcPlanBase {
   int64_t resident = 0;  // checkpoint segments kept resident (no recompute)
   int64_t steps_per_block = 1;  // forward steps per launch (configured or tuned)
   int64_t uses_tma = 0;         // interior forward steps through tensor-map copies
+  int64_t rows[4] = {0, 0, 0, 0};  // rows per warp: fwd / adj interior, fwd / adj PML
   virtual int device_status(cudaStream_t st) = 0;
 };
 
@@ -2048,8 +2246,8 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     const int64_t fs = (h.nx + 2) * pitch * (int64_t)sizeof(T);
     offs[s].ckpt = L.take((size_t)nseg[s] * 4 * fs);
     offs[s].c = L.take(fs);
-    offs[s].sx = L.take(sizeof(T) * (h.nx + 2));
-    offs[s].ty = L.take(sizeof(T) * (MY + 2));
+    offs[s].sx = L.take((1 + KT_N) * sizeof(T) * (h.nx + 2));  // sigma, its tables
+    offs[s].ty = L.take((1 + KT_N) * sizeof(T) * (MY + 2));    // tau, its tables
     offs[s].srcv = L.take(sizeof(T) * std::max<int64_t>(h.nstep * h.nsrc, 1));
     offs[s].slist = L.take(sizeof(CellRef) * std::max<int64_t>(h.nsrc, 1));
   }
@@ -2276,6 +2474,8 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     d.c = (T*)(pool + offs[s].c);
     d.sx = (T*)(pool + offs[s].sx);
     d.ty = (T*)(pool + offs[s].ty);
+    d.sxk = d.sx + (h.nx + 2);
+    d.tyk = d.ty + (MY + 2);
     d.gc = (double*)(pool + offs[s].gc);
     d.gc32 = sizeof(T) == 4 ? (float*)(pool + offs[s].gc32) : nullptr;
     d.gsrc = (double*)(pool + offs[s].gsrc);
@@ -2299,11 +2499,11 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     d.resid = d_resid + trace_off[order[s]];
     sx = hsx[s];
     ty = hty;
-    host_bufs.emplace_back(sx.begin(), sx.end());
-    ADS_CUDA(cudaMemcpyAsync(d.sx, host_bufs.back().data(), sizeof(T) * sx.size(),
+    host_bufs.emplace_back(with_tables<T>(sx, c.dt, c.dx, c.dy));
+    ADS_CUDA(cudaMemcpyAsync(d.sx, host_bufs.back().data(), sizeof(T) * (1 + KT_N) * sx.size(),
                              cudaMemcpyHostToDevice, st));
-    host_bufs.emplace_back(ty.begin(), ty.end());
-    ADS_CUDA(cudaMemcpyAsync(d.ty, host_bufs.back().data(), sizeof(T) * ty.size(),
+    host_bufs.emplace_back(with_tables<T>(ty, c.dt, c.dx, c.dy));
+    ADS_CUDA(cudaMemcpyAsync(d.ty, host_bufs.back().data(), sizeof(T) * (1 + KT_N) * ty.size(),
                              cudaMemcpyHostToDevice, st));
     if (h.nsrc > 0) {
       std::vector<T> sv((size_t)(h.nstep * h.nsrc));
@@ -2364,6 +2564,10 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     nR = n;
   }
   steps_per_block = KB;
+  rows[0] = ri_f;
+  rows[1] = ri;
+  rows[2] = ri_pf > 0 ? ri_pf : ri_f;
+  rows[3] = ri_pa > 0 ? ri_pa : ri;
   launches_fwd = 1 + nF;            // prep + loop
   launches_grad = 1 + nF + 2 + nR + 1;  // prep, loop, misfit+reduce, reverse, assemble
   // ---- graphs
@@ -2487,6 +2691,7 @@ void AcPlan<T>::build_tiles(int rows, int width, int64_t pitch, TileList& L,
   L.rcvs.clear();
   L.in_end.assign(nshots, 0);
   L.pm_end.assign(nshots, 0);
+  std::vector<int> pm_cost;  // per PML item, for the ordering below
   const int ny = (int)cfg.MY;
   const int gh = Tile<T>::G * rows;  // rows of one item (its G warps' row tiles)
   for (int s = 0; s < nshots; s++) {
@@ -2517,6 +2722,19 @@ void AcPlan<T>::build_tiles(int rows, int width, int64_t pitch, TileList& L,
     }
     // tau-free column strips: tau = 0 at columns j0-1 .. j0+width (inside the frame)
     std::vector<char> col_free(ntj), row_free(nti);
+    // relative cost of a PML item: per warp 1 where it is free of both
+    // profiles, 3 where it meets one, 6 where it meets both (a corner)
+    auto item_cost = [&](const AcItem& it, int r, bool cfree) {
+      int c = 0;
+      for (int w = 0; w < Tile<T>::G; w++) {
+        const int a = it.i0 + w * r, e = std::min(a + r, nx + 1);
+        if (a > nx) break;
+        bool z = true;
+        for (int i = a - 1; i <= e; i++) z = z && hsx[s][i] == 0.0;
+        c += z && cfree ? 1 : (z || cfree ? 3 : 6);
+      }
+      return c;
+    };
     for (int tj = 0; tj < ntj; tj++) {
       const int j0 = 1 + tj * width;
       bool z = true;
@@ -2561,13 +2779,36 @@ void AcPlan<T>::build_tiles(int rows, int width, int64_t pitch, TileList& L,
             AcItem sub = it;
             sub.i0 = i0;
             L.pm.push_back(sub);
+            pm_cost.push_back(item_cost(sub, pm_rows, col_free[tj]));
           }
         } else {
           L.pm.push_back(it);
+          pm_cost.push_back(item_cost(it, rows, col_free[tj]));
         }
       }
     L.in_end[s] = (int)L.in.size();
     L.pm_end[s] = (int)L.pm.size();
+  }
+  // Heaviest PML items first.  Their cost varies several-fold (corner warps
+  // take the general form, edge warps a cheaper specialised one, warps past the
+  // profile the interior update), and the blocks start roughly in index order,
+  // so this order lets the launch end on light items.  Items move only within
+  // a group of shots of equal record length: a launch always covers whole
+  // groups (the shots with nstep >= t), so the prefix counts at group ends stay
+  // valid.
+  std::vector<int> idx;
+  for (int sa = 0; sa < nshots;) {
+    int sb = sa + 1;
+    while (sb < nshots && nstep[sb] == nstep[sa]) sb++;
+    const int b = sa > 0 ? L.pm_end[sa - 1] : 0, e = L.pm_end[sb - 1];
+    idx.resize(e - b);
+    std::iota(idx.begin(), idx.end(), b);
+    std::stable_sort(idx.begin(), idx.end(),
+                     [&](int x, int y) { return pm_cost[x] > pm_cost[y]; });
+    std::vector<AcItem> sorted(e - b);
+    for (int k = 0; k < e - b; k++) sorted[k] = L.pm[idx[k]];
+    std::copy(sorted.begin(), sorted.end(), L.pm.begin() + b);
+    sa = sb;
   }
 }
 
@@ -3250,6 +3491,11 @@ int64_t ads_acoustic_plan_resident_segments(const ads_acoustic_plan* plan) {
 
 int64_t ads_acoustic_plan_steps_per_block(const ads_acoustic_plan* plan) {
   return plan && plan->impl ? plan->impl->steps_per_block : -1;
+}
+
+int64_t ads_acoustic_plan_rows(const ads_acoustic_plan* plan, int which) {
+  if (!plan || !plan->impl || which < 0 || which > 3) return -1;
+  return plan->impl->rows[which];
 }
 
 int64_t ads_acoustic_plan_tma(const ads_acoustic_plan* plan) {

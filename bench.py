@@ -285,8 +285,8 @@ def run_acoustic_fwd_f64(args):
           {k: r[k] for k in ("e2e", "cpu_baseline", "gpu_launches")})
 
 
-def measure_c2(steps, warmup):
-    """Plain FP64 acoustic FWI gradient (C2): 400x400 incl. PML 30, 2000 steps, 8 shots
+def measure_c2(steps, warmup, nstep=2000, rows=0):
+    """Plain FP64 acoustic FWI gradient (C2): 400x400 incl. PML 30, nstep steps, 8 shots
     20 cells below the PML at the centres of 8 equal segments, one receiver per
     interior column 5 cells below the PML, observed data from the true model,
     gradient at a Gaussian-smoothed (20 cells) start model."""
@@ -296,26 +296,30 @@ def measure_c2(steps, warmup):
     ads = g.load_package()
     from adseismic_gb300 import configs
 
-    cfg, shots, vt, v0 = configs.c2_fwi()
+    cfg, shots, vt, v0 = configs.c2_fwi(nstep=nstep)
     NX, NY, T = cfg["MX"], cfg["MY"], cfg["nstep"]
-    plan = configs.acoustic_plan(ads, cfg, shots, "f64")
+    # rows > 0 fixes the item tiling (the autotuner's timings mean nothing under a profiler)
+    plan = configs.acoustic_plan(ads, cfg, shots, "f64", autotune=rows <= 0,
+                                 rows_per_thread=max(rows, 0))
     obs = plan.forward(torch.tensor(vt, device="cuda")).clone()
     vdev = torch.tensor(v0, device="cuda")
     ms = _timed(lambda: plan.gradient(vdev, obs), steps, warmup)
     cells = 2 * len(shots) * NX * NY * (T - 1)
     out = {"value": len(shots) / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "dtype": "f64",
-           "workload": "acoustic FWI gradient 400x400 (PML 30), 2000 steps, 8 shots",
+           "workload": f"acoustic FWI gradient 400x400 (PML 30), {T} steps, 8 shots",
            "gcell_updates_per_s": cells / (ms / 1e3) / 1e9,
-           "gpu_launches": int(plan.launches_gradient)}
+           "gpu_launches": int(plan.launches_gradient),
+           "rows_per_warp": dict(zip(("fwd", "adj", "fwd_pml", "adj_pml"), plan.rows))}
     plan.close()
     return out
 
 
 def run_fwi_f64(args):
-    r = measure_c2(args.steps, args.warmup)
-    _line("FWI shot-gradients/s, plain FP64 drop-in", r["value"], r["unit"], args,
+    r = measure_c2(args.steps, args.warmup, nstep=args.nstep if args.nstep != 3000 else 2000,
+                   rows=args.rows)
+    _line("FWI shot-gradients/s, FP64 plan", r["value"], r["unit"], args,
           r["ms_per_step"], "f64", r["workload"],
-          {k: r[k] for k in ("gcell_updates_per_s", "gpu_launches")})
+          {k: r[k] for k in ("gcell_updates_per_s", "gpu_launches", "rows_per_warp")})
 
 
 def elastic_workload(ads, nshots=32, T=4000):
@@ -529,6 +533,8 @@ def main():
     ap.add_argument("--no-elastic", action="store_true")
     ap.add_argument("--no-elastic-autotune", action="store_true")
     ap.add_argument("--no-configs", action="store_true")
+    ap.add_argument("--rows", type=int, default=0,
+                    help="fwi-f64: rows per warp of the step items instead of the autotuner")
     ap.add_argument("--elastic-adjoint-passes", type=int, default=0, choices=(0, 1, 3))
     # elastic-fwi workload only: checkpoint interval and the resident share of
     # the free device memory in percent (-1: no resident segments), for small
@@ -680,7 +686,7 @@ def main():
     # plain FP64 on the same per-shot geometry, one shot per call
     fp64 = None
     if not args.no_fp64:
-        p64 = mk("f64", shots[:1])
+        p64 = mk("f64", shots[:1], autotune=True)
         o64 = p64.forward(vt).clone()
         p64.gradient(v0, o64)
         torch.cuda.synchronize()

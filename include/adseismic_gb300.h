@@ -335,6 +335,11 @@ int64_t ads_acoustic_plan_resident_segments(const ads_acoustic_plan* plan);
 /* Forward steps per launch the plan runs (steps_per_block as configured, or as
  * the autotuner chose it); -1 for a null plan.  No reference counterpart. */
 int64_t ads_acoustic_plan_steps_per_block(const ads_acoustic_plan* plan);
+/* Rows per warp of the plan's step items, as created or as the autotuner chose
+ * them: forward interior (which = 0), adjoint interior (1), forward PML (2),
+ * adjoint PML (3); -1 for a null plan or another `which`.  No reference
+ * counterpart. */
+int64_t ads_acoustic_plan_rows(const ads_acoustic_plan* plan, int which);
 /* 1 when the plan's interior forward steps run through tensor-map copies (see
  * ads_acoustic_config.tma), 0 when not, -1 for a null plan.  No reference
  * counterpart. */
