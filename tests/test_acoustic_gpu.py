@@ -256,6 +256,37 @@ def test_autotuned_plan_vs_oracle(ads, orc, cuda, precision, resident):
     plan.close()
 
 
+@pytest.mark.parametrize("rows", [2, 4])
+@pytest.mark.parametrize("resident", [-1, 2])
+def test_fp64_pml_warp_kinds_vs_oracle(ads, orc, cuda, rows, resident):
+    """FP64 plans specialise the PML kernels by warp kind (sigma rows only, tau
+    columns only, corners). A 150 x 190 grid with a 12-cell PML holds warps of
+    every kind and interior warps inside PML items (64-column forward and
+    32-column adjoint strips); the uneven shot windows move the sigma rows
+    against the row tiles."""
+    MX, MY, npml, h, dt, vref = 150, 190, 12, 10.0, 1e-3, 1500.0
+    rng = np.random.default_rng(17)
+    shots = []
+    for x0, nx, nstep in ((0, 150, 120), (13, 101, 120), (40, 97, 95)):
+        shots.append(dict(x0=x0, nx=nx, nstep=nstep, srci=[nx // 2], srcj=[MY // 3],
+                          srcv=rng.standard_normal((nstep, 1)) * 1e3,
+                          rcvi=np.arange(2, nx + 2, 3), rcvj=np.full(len(range(2, nx + 2, 3)), 20)))
+    vp = 1800 + 900 * rng.random((MX + 2, MY + 2))
+    ref_tr = oracle_multishot(orc, MX, MY, shots, vp, h, dt, npml, vref)
+    obs = [t * 0.95 for t in ref_tr]
+    ref_loss, ref_grad = oracle_multishot(orc, MX, MY, shots, vp, h, dt, npml, vref, obs)
+    plan = ads.AcousticPlan(MX, MY, h, h, dt, shots, npml=npml, vp_ref=vref, precision="f64",
+                            ckpt_every=17, rows_per_thread=rows, resident_segments=resident)
+    assert plan.rows == (rows, rows, rows, rows)
+    for a, b in zip(plan.split_traces(plan.forward(T(vp, cuda))), ref_tr):
+        assert rel(a.cpu().numpy(), b) <= TOL64
+    loss, grad = plan.gradient(T(vp, cuda), plan.pack([T(o, cuda) for o in obs]))
+    torch.cuda.synchronize()
+    assert abs(float(loss) - ref_loss) <= TOL64 * ref_loss
+    assert rel(grad.cpu().numpy(), ref_grad) <= TOL64
+    plan.close()
+
+
 def test_repeated_calls_are_deterministic(ads, cuda):
     MX, MY, shots, vp = uneven_case(5, nshots=3)
     plan = ads.AcousticPlan(MX, MY, 10.0, 10.0, 1e-3, shots, npml=5, precision="f32")
