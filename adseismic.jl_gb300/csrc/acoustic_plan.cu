@@ -79,7 +79,7 @@ struct Tile {
   // resident CTAs of TPB threads per SM the register allocation must allow
   // (general / interior-only kernels; 65536 / (TPB x MINB) registers a thread)
   static constexpr int MINB_F = sizeof(T) == 4 ? ADS_MINB_F32 : 3;
-  static constexpr int MINB_A = sizeof(T) == 4 ? ADS_MINB_A32 : 4;
+  static constexpr int MINB_A = sizeof(T) == 4 ? ADS_MINB_A32 : 3;
   static constexpr int MINB_FI = sizeof(T) == 4 ? ADS_MINB_FI32 : 6;
   static constexpr int MINB_AI = sizeof(T) == 4 ? ADS_MINB_AI32 : 5;
 };
@@ -115,6 +115,7 @@ struct AcShot {
   // damping tables of the PML profiles (KT_N arrays each): along i, nx + 2
   // entries per array, after sx; along j, ny + 2 entries, after ty
   T *sxk, *tyk;
+  T* rdt;  // FP64 plans: 1 / (1 + (sigma + tau) dt/2) per cell (pitched), else null
   double* gc;         // FP64 gradient accumulator (pitched)
   float* gc32;        // FP32 per-segment partial of grad_c (FP32 plans)
   const T* srcv;      // (nstep, nsrc), already multiplied by dt^2
@@ -370,6 +371,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   const T* __restrict__ ty = sh.ty;
   const T* __restrict__ sxk = sh.sxk;
   const T* __restrict__ tyk = sh.tyk;
+  const T* __restrict__ rdt = sh.rdt;
   const T* __restrict__ srcv = sh.srcv;
   const bool jld = j <= ny + 1;
   const bool hr = j + C <= ny + 1;  // right halo column exists (last lane of a warp)
@@ -439,6 +441,10 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
             dv.v[c] = oq[0].v[c] + cv * (K.cx * ((wp.v[c] - u0) + (wm.v[c] - u0)) +
                                          K.cy * ((wN - u0) + (wS - u0)));
             v = u0 + dv.v[c];
+          } else if constexpr (sizeof(T) == 8) {
+            // FP64 plans (issue-bound): seven operations instead of nine
+            v = (T(2) * w0.v[c] - oq[0].v[c]) +
+                cv * (K.cx * (wp.v[c] + wm.v[c]) + K.cy * (wN + wS) - K.kxy * w0.v[c]);
           } else {
             v = (T(2) - K.kxy * cv) * w0.v[c] + cv * K.cx * (wp.v[c] + wm.v[c]) +
                 cv * K.cy * (wN + wS) - oq[0].v[c];
@@ -476,14 +482,16 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   } else {
   // The general (PML) form.  FP64 plans of variant W specialise it by the
   // warp's kind (uniform over the warp): PK = 1 where tau = 0 at every column
-  // the warp reads (sigma rows only; the damping 1 / (1 + sigma dt/2) comes per
-  // row from the shot's reciprocal table), PK = 2 where sigma = 0 on every row
-  // it updates (tau columns only; the damping and the tau terms are per-thread
-  // constants), PK = 0 elsewhere (the corners, and every FP32 or variant-U
-  // warp).  The specialised forms drop terms that are exact zeros there and
-  // multiply by the tabulated reciprocal instead of dividing (within an ulp of
-  // the divide).  FP64 plans are bound by the FP64 issue rate, so the count of
-  // FP64 instructions is their cost.
+  // the warp reads (sigma rows only: the damping factors come per row from the
+  // shot's tables), PK = 2 where sigma = 0 on every row it updates (tau columns
+  // only: the factors are per-thread constants), PK = 3 elsewhere (the
+  // corners: the sigma factors per row, the tau products per cell and
+  // 1 / (1 + s dt/2) from the shot's per-cell table).  PK = 0, the general form
+  // with its divide, serves FP32 and variant-U plans.  The specialised forms
+  // drop terms that are exact zeros there and multiply by the tabulated
+  // reciprocal instead of dividing (within an ulp of the divide; with
+  // r = 1 / (1 + s dt/2), (1 - s dt/2) r = 2 r - 1).  FP64 plans are bound by
+  // the FP64 issue rate, so the count of FP64 instructions is their cost.
   auto pml_rows = [&](auto kd) {
     constexpr int PK = decltype(kd)::value;
     T rc[C], arc[C], bq[C], ext[C], eyt[C];  // PK 2: per-column constants
@@ -513,6 +521,8 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     const int64_t hoff = lane == 0 ? -1 : C;
     const bool hon = (lane == 0 && jld) || (lane == 31 && hr);
     T hw = ld1p(w + off(i0) + hoff, hon), hq = ld1p(qin + off(i0) + hoff, hon && n0);
+    V rd0{};  // PK 3: 1 / (1 + s dt/2) of the row's cells, one row ahead
+    if constexpr (PK == 3) rd0 = ldvp<T, C>(rdt, off(i0), jld);
     for (int i = i0; i < i_end; i++) {
       const int64_t row = off(i);
       const bool more = i + 1 < i_end;
@@ -524,6 +534,8 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       V cn = ldvp<T, C>(cc, off(i + 1), jld && more);
       const T hwn = ld1p(w + row + P + hoff, more && hon),
               hqn = ld1p(qin + row + P + hoff, more && hon && n1);
+      V rdn{};
+      if constexpr (PK == 3) rdn = ldvp<T, C>(rdt, off(i + 1), jld && more);
       T wL = __shfl_up_sync(FULL, w0.v[C - 1], 1), wR = __shfl_down_sync(FULL, w0.v[0], 1);
       T qL = __shfl_up_sync(FULL, q0.v[C - 1], 1), qR = __shfl_down_sync(FULL, q0.v[0], 1);
       if (lane == 0) {
@@ -535,11 +547,14 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       }
       if (jld) {
         const T sg = PK == 2 ? T(0) : sx[i];
-        T ar_r = T(1), r_r = T(1), e_r = T(1), exs = T(0), eys = T(0);  // PK 1: row constants
-        if constexpr (PK == 1) {
+        // PK 1, 3: the row's factors
+        T ar_r = T(1), r_r = T(1), e_r = T(1), exs = T(0), eys = T(0);
+        if constexpr (PK == 1 || PK == 3) {
           const int n = nx + 2;
-          r_r = sxk[KT_R * n + i];
-          ar_r = sxk[KT_AR * n + i];
+          if constexpr (PK == 1) {
+            r_r = sxk[KT_R * n + i];
+            ar_r = sxk[KT_AR * n + i];
+          }
           e_r = sxk[KT_E * n + i];
           exs = sxk[KT_EX * n + i];
           eys = sxk[KT_EY * n + i];
@@ -553,7 +568,20 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
           const T qN = c == C - 1 ? qR : q0.v[c + 1];
           const T cv = c0.v[c], s = sg + tj[c];
           T v;
-          if constexpr (PK != 0) {
+          if constexpr (PK == 3) {
+            // three-level form, both profiles
+            const T rd = rd0.v[c];
+            v = ((T(2) - sg * tj[c] * K.dt2 - K.kxy * cv) * w0.v[c] +
+                 cv * K.cx * (wp.v[c] + wm.v[c]) + cv * K.cy * (wN + wS) +
+                 K.fx * (pp.v[c] - pm.v[c]) + K.fy * (qN - qS)) * rd -
+                (T(2) * rd - T(1)) * wo0.v[c];
+            for (int e = it.src_b; e < it.src_e; e++) {
+              const CellRef r = srcs[e];
+              if (r.cell == row + c) v += srcv[(int64_t)(t - 1) * sh.nsrc + r.idx];
+            }
+            po.v[c] = e_r * p0.v[c] + cv * (K.ex * tj[c] - exs) * (wp.v[c] - wm.v[c]);
+            qo.v[c] = (T(1) - K.dt * tj[c]) * q0.v[c] + cv * (eys - K.ey * tj[c]) * (wN - wS);
+          } else if constexpr (PK != 0) {
             // three-level form, sigma tau = 0: s = sigma (PK 1) or tau (PK 2)
             v = ((T(2) - K.kxy * cv) * w0.v[c] + cv * K.cx * (wp.v[c] + wm.v[c]) +
                  cv * K.cy * (wN + wS) + K.fx * (pp.v[c] - pm.v[c]) + K.fy * (qN - qS)) *
@@ -629,6 +657,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       hw = hwn;
       hq = hqn;
       n0 = n1;
+      if constexpr (PK == 3) rd0 = rdn;
     }
   };
   constexpr bool SPEC = sizeof(T) == 8 && !VU && !INC;
@@ -640,7 +669,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   }
   if (SPEC && tfree) pml_rows(std::integral_constant<int, SPEC ? 1 : 0>{});
   else if (SPEC && sfree) pml_rows(std::integral_constant<int, SPEC ? 2 : 0>{});
-  else pml_rows(std::integral_constant<int, 0>{});
+  else pml_rows(std::integral_constant<int, SPEC ? 3 : 0>{});
   record_traces<T, C, NOREC>(it, sh, rcvs, out, t, lane, i0, i_end);
   }
 }
@@ -1051,6 +1080,7 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   const T* __restrict__ ty = sh.ty;
   const T* __restrict__ sxk = sh.sxk;
   const T* __restrict__ tyk = sh.tyk;
+  const T* __restrict__ rdt = sh.rdt;
   const bool jld = j <= ny + 1;
   const bool hr = j + C <= ny + 1;
   // offsets within a field fit 32 bits (the plan checks fs < 2^31)
@@ -1103,6 +1133,15 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       gq[q] = ldv<G, C>(gb, off(i0 + q), on);
       load_halo(i0 + q, hu[q], hcq[q], hwq[q]);
     }
+    // FP64 plans (issue-bound) carry z = c lambdaU_k of rows i-1, i down the rows:
+    // one product per cell instead of three
+    constexpr bool ZF = sizeof(T) == 8;
+    V zm, z0;
+#pragma unroll
+    for (int c = 0; c < C; c++) {
+      zm.v[c] = ZF ? cq[0].v[c] * uq[0].v[c] : T(0);
+      z0.v[c] = ZF ? cq[1].v[c] * uq[1].v[c] : T(0);
+    }
     for (int i = i0; i < i_end; i++) {
       const int row = off(i);
       const int rn = i + PF;
@@ -1117,14 +1156,23 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       const V &gum = uq[0], &gu0 = uq[1], &gu1 = uq[2];
       const V &cm = cq[0], &c0 = cq[1], &c1 = cq[2];
       const V &wm = wq[0], &w0 = wq[1], &wp = wq[2];
-      // what each cell sends to its j-neighbours: c cy lambdaU
+      // what each cell sends to its j-neighbours: c cy lambdaU (ZF: c lambdaU,
+      // the cy applied once to the sum of both neighbours)
       T Y[C];
+      V z1;
 #pragma unroll
-      for (int c = 0; c < C; c++) Y[c] = c0.v[c] * K.cy * gu0.v[c];
+      for (int c = 0; c < C; c++) {
+        if constexpr (ZF) {
+          z1.v[c] = c1.v[c] * gu1.v[c];
+          Y[c] = z0.v[c];
+        } else {
+          Y[c] = c0.v[c] * K.cy * gu0.v[c];
+        }
+      }
       T Yl = __shfl_up_sync(FULL, Y[C - 1], 1), Yr = __shfl_down_sync(FULL, Y[0], 1);
       T wL = __shfl_up_sync(FULL, w0.v[C - 1], 1), wR = __shfl_down_sync(FULL, w0.v[0], 1);
       if (lane == 0 || lane == 31) {
-        const T h = hon ? hcq[0] * K.cy * hu[0] : T(0);
+        const T h = hon ? (ZF ? hcq[0] * hu[0] : hcq[0] * K.cy * hu[0]) : T(0);
         if (lane == 0) {
           Yl = h;
           wL = hwq[0];
@@ -1141,13 +1189,21 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
           const T yl = c == 0 ? Yl : Y[c - 1], yr = c == C - 1 ? Yr : Y[c + 1];
           const T wS = c == 0 ? wL : w0.v[c - 1], wN = c == C - 1 ? wR : w0.v[c + 1];
           const T cv = c0.v[c];
-          nu.v[c] = -lq[0].v[c] + (T(2) - K.kxy * cv) * gu0.v[c] + cm.v[c] * K.cx * gum.v[c] +
-                    c1.v[c] * K.cx * gu1.v[c] + yl + yr;
+          if constexpr (ZF)
+            nu.v[c] = (T(2) * gu0.v[c] - lq[0].v[c]) + K.cx * (zm.v[c] + z1.v[c]) +
+                      K.cy * (yl + yr) - K.kxy * z0.v[c];
+          else
+            nu.v[c] = -lq[0].v[c] + (T(2) - K.kxy * cv) * gu0.v[c] +
+                      cm.v[c] * K.cx * gum.v[c] + c1.v[c] * K.cx * gu1.v[c] + yl + yr;
           ga.v[c] += (G)((-K.kxy * w0.v[c] + K.cx * (wp.v[c] + wm.v[c]) + K.cy * (wN + wS)) *
                          gu0.v[c]);
         }
         stv<T, C>(lun, row, nu, j, ny);
         stv<G, C>(gb, row, ga, j, ny);
+      }
+      if constexpr (ZF) {
+        zm = z0;
+        z0 = z1;
       }
 #pragma unroll
       for (int q = 0; q < PF + 1; q++) {
@@ -1181,7 +1237,9 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   // warp's kind, as k_ac_fwd does: PK = 1 where tau = 0 at every column the
   // warp reads (1/den and the sigma terms per row from the damping tables),
   // PK = 2 where sigma = 0 on rows i0-1 .. i_end (1/den and the tau terms
-  // per-thread constants), PK = 0 elsewhere.
+  // per-thread constants), PK = 3 elsewhere (1/den from the per-cell table,
+  // the sigma terms per row); PK = 0 (general, with divides) for FP32 and
+  // variant-U plans.
   auto pml_rows = [&](auto kd) {
     constexpr int PK = decltype(kd)::value;
     const int nr = nx + 2, ncol = ny + 2;
@@ -1223,12 +1281,19 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       c0 = ldvp<T, C>(cc, off(i0), jld);
     V gu1 = ldvp<T, C>(luc, off(i0 + 1), jld), gp1 = ldvp<T, C>(lpc, off(i0 + 1), jld && nzk(i0 + 1)),
       c1 = ldvp<T, C>(cc, off(i0 + 1), jld);
-    V invm, inv0;
+    V invm, inv0, rd1{};  // PK 3: 1/den of rows i-1, i, i+1 from the table
+    if constexpr (PK == 3) {
+      invm = ldvp<T, C>(rdt, off(i0 - 1), jld);
+      inv0 = ldvp<T, C>(rdt, off(i0), jld);
+      rd1 = ldvp<T, C>(rdt, off(i0 + 1), jld);
+    }
     V gim, gi0;  // lambdaU_k / den of rows i-1, i (carried down the rows)
 #pragma unroll
     for (int c = 0; c < C; c++) {
-      invm.v[c] = invd(i0 - 1, c);
-      inv0.v[c] = invd(i0, c);
+      if constexpr (PK != 3) {
+        invm.v[c] = invd(i0 - 1, c);
+        inv0.v[c] = invd(i0, c);
+      }
       gim.v[c] = gum.v[c] * invm.v[c];
       gi0.v[c] = gu0.v[c] * inv0.v[c];
     }
@@ -1244,24 +1309,30 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       hc = ld1p(cc + r, hon);
       hw = ld1p(w + r, hon);
     }
+    T hrd = T(1);  // PK 3: 1/den of the halo cell
+    if constexpr (PK == 3) hrd = ld1p(rdt + off(i0) + hoff, hon);
     T sgm = PK == 2 ? T(0) : sx[i0 - 1], sg0 = PK == 2 ? T(0) : sx[i0];
     for (int i = i0; i < i_end; i++) {
       const int row = off(i);
       const T sgp = PK == 2 ? T(0) : sx[i + 1];
-      V invp, gip;
+      V invp, gip, rd2{};
+      if constexpr (PK == 3) {
+        invp = rd1;
+        rd2 = ldvp<T, C>(rdt, off(i + 2), jld && i + 1 < i_end);
+      }
 #pragma unroll
       for (int c = 0; c < C; c++) {
-        invp.v[c] = invd(i + 1, c);
+        if constexpr (PK != 3) invp.v[c] = invd(i + 1, c);
         gip.v[c] = gu1.v[c] * invp.v[c];
       }
-      // PK 1: the sigma terms of rows i-1, i, i+1 from the damping tables
+      // PK 1, 3: the sigma terms of rows i-1, i, i+1 from the damping tables
       T exm = T(0), ex0 = T(0), exp_ = T(0), eys0 = T(0), ar0 = T(1), e0 = T(1);
-      if constexpr (PK == 1) {
+      if constexpr (PK == 1 || PK == 3) {
         exm = sxk[KT_EX * nr + i - 1];
         ex0 = sxk[KT_EX * nr + i];
         exp_ = sxk[KT_EX * nr + i + 1];
         eys0 = sxk[KT_EY * nr + i];
-        ar0 = sxk[KT_AR * nr + i];
+        if constexpr (PK == 1) ar0 = sxk[KT_AR * nr + i];
         e0 = sxk[KT_E * nr + i];
       }
       // prefetch: row i+2 (lambdaU_k, lambdaPhi_k, c, u_{k-1}), row i+1 (lambdaPsi_k,
@@ -1277,6 +1348,8 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       const int rh = row + P32 + hoff;
       const T hgun = ld1p(luc + rh, more && hon), hgqn = ld1p(lqc + rh, more && hon && n1),
               hcn = ld1p(cc + rh, more && hon), hwn = ld1p(w + rh, more && hon);
+      T hrdn = T(1);
+      if constexpr (PK == 3) hrdn = ld1p(rdt + rh, more && hon);
       // j-direction terms of this thread's cells and of the neighbouring columns
       T YP[C], YM[C], YR[C], gui[C];
 #pragma unroll
@@ -1286,7 +1359,8 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
           col_terms<T>(gui[c], gq.v[c], c0.v[c], sg0, tj[c], K, YP[c], YM[c], YR[c]);
         } else {
           const T by = c0.v[c] * K.cy * gui[c];
-          const T eyg = (PK == 1 ? eys0 : -eyt[c]) * c0.v[c] * gq.v[c];
+          const T ey = PK == 1 ? eys0 : (PK == 2 ? -eyt[c] : eys0 - K.ey * tj[c]);
+          const T eyg = ey * c0.v[c] * gq.v[c];
           YP[c] = by + eyg;
           YM[c] = by - eyg;
           YR[c] = K.fy * gui[c];
@@ -1302,8 +1376,9 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
             col_terms<T>(hgu * inv_den<T>(sg0 + th, K), hgq, hc, sg0, th, K, a, b, r);
           } else {
             // PK 1: tau = 0 at the halo column too, so its 1/den is the row's
-            const T hg = hgu * (PK == 1 ? inv0.v[0] : hrc);
-            const T by = hc * K.cy * hg, eyg = (PK == 1 ? eys0 : -heyt) * hc * hgq;
+            const T hg = hgu * (PK == 1 ? inv0.v[0] : (PK == 2 ? hrc : hrd));
+            const T hey = PK == 1 ? eys0 : (PK == 2 ? -heyt : eys0 - K.ey * th);
+            const T by = hc * K.cy * hg, eyg = hey * hc * hgq;
             a = by + eyg;
             b = by - eyg;
             r = K.fy * hg;
@@ -1339,6 +1414,15 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
               np.v[c] = (T(1) - K.dt * sg0) * gp0.v[c] + K.fx * guim - K.fx * guip;
               nq.v[c] = (T(1) - K.dt * tj[c]) * gq.v[c] + yrl - yrr;
             }
+          } else if constexpr (PK == 3) {
+            // both profiles: the sigma terms per row, 1/den per cell
+            const T ext3 = K.ex * tj[c];
+            const T XPm = cm.v[c] * (K.cx * guim + (ext3 - exm) * gpm.v[c]);
+            const T XMp = c1.v[c] * (K.cx * guip - (ext3 - exp_) * gp1.v[c]);
+            nu.v[c] = -(T(2) * inv0.v[c] - T(1)) * ln.v[c] +
+                      (T(2) - sg0 * tj[c] * K.dt2 - K.kxy * cv) * gui[c] + XPm + XMp + ypl + ymr;
+            np.v[c] = e0 * gp0.v[c] + K.fx * (guim - guip);
+            nq.v[c] = (T(1) - K.dt * tj[c]) * gq.v[c] + yrl - yrr;
           } else {
             // sigma tau = 0; PK 1: tau = 0, PK 2: sigma = 0 (tables / constants)
             const T XPm = cm.v[c] * (K.cx * guim + (PK == 1 ? -exm : ext[c]) * gpm.v[c]);
@@ -1363,6 +1447,9 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
           if constexpr (PK == 0)
             g[c] = (-K.kxy * w0.v[c] + K.cx * (wp.v[c] + wm.v[c]) + K.cy * (wN + wS)) * gui[c] +
                    K.ex * (tj[c] - sg0) * dx_ * gp0.v[c] + K.ey * (sg0 - tj[c]) * dy_ * gq.v[c];
+          else if constexpr (PK == 3)
+            g[c] = (-K.kxy * w0.v[c] + K.cx * (wp.v[c] + wm.v[c]) + K.cy * (wN + wS)) * gui[c] +
+                   (K.ex * tj[c] - ex0) * dx_ * gp0.v[c] + (eys0 - K.ey * tj[c]) * dy_ * gq.v[c];
           else
             g[c] = (-K.kxy * w0.v[c] + K.cx * (wp.v[c] + wm.v[c]) + K.cy * (wN + wS)) * gui[c] +
                    (PK == 1 ? -ex0 : ext[c]) * dx_ * gp0.v[c] +
@@ -1383,6 +1470,10 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       gq = gqn; ln = lnn;
       hgu = hgun; hgq = hgqn; hc = hcn; hw = hwn;
       n0 = n1;
+      if constexpr (PK == 3) {
+        rd1 = rd2;
+        hrd = hrdn;
+      }
     }
   };
   constexpr bool SPEC = sizeof(T) == 8 && !VU;
@@ -1394,7 +1485,7 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
   }
   if (SPEC && tfree) pml_rows(std::integral_constant<int, SPEC ? 1 : 0>{});
   else if (SPEC && sfree) pml_rows(std::integral_constant<int, SPEC ? 2 : 0>{});
-  else pml_rows(std::integral_constant<int, 0>{});
+  else pml_rows(std::integral_constant<int, SPEC ? 3 : 0>{});
   inject_residuals<T, C>(it, sh, rcvs, lun, k, lane, i0, i_end);
   record_src_grad<T, C, VU>(it, sh, srcs, lun, lpc, lqc, K, k, lane, i0, i_end, dt2);
   }
@@ -1809,6 +1900,20 @@ __global__ void k_ac_prep(const AcShot<T>* __restrict__ shots, const double* __r
   }
 }
 
+// 1 / (1 + (sigma_i + tau_j) dt/2) over each shot's padded window: the damping
+// of the FP64 PML kernels' corner warps, where both profiles meet.
+template <typename T>
+__global__ void k_ac_rden(const AcShot<T>* __restrict__ shots, double hdt) {
+  const AcShot<T>& sh = shots[blockIdx.y];
+  const int64_t n = (int64_t)(sh.nx + 2) * (sh.ny + 2);
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = e / (sh.ny + 2), j = e % (sh.ny + 2);
+    sh.rdt[i * sh.pitch + j + JOFF] =
+        (T)(1.0 / fma((double)sh.sx[i] + (double)sh.ty[j], hdt, 1.0));
+  }
+}
+
 // residual = 2 (trace - observed) in T; per-block FP64 partial sums of
 // (trace - observed)^2 (deterministic two-pass reduction).
 template <typename T>
@@ -2209,7 +2314,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   size_t off_fwd_begin, off_fwd_end, off_adj_begin, off_adj_end;
   DevPool L;
   struct Offs {
-    size_t u, u2, d, p, q, seg, ckpt, lu, lp, lq, c, sx, ty, gc, gc32, gsrc, srcv, slist;
+    size_t u, u2, d, p, q, seg, ckpt, lu, lp, lq, c, rdt, sx, ty, gc, gc32, gsrc, srcv, slist;
   };
   std::vector<Offs> offs(ns);
   std::vector<int> nseg(ns);
@@ -2246,6 +2351,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     const int64_t fs = (h.nx + 2) * pitch * (int64_t)sizeof(T);
     offs[s].ckpt = L.take((size_t)nseg[s] * 4 * fs);
     offs[s].c = L.take(fs);
+    offs[s].rdt = L.take(sizeof(T) == 8 ? fs : 0);  // FP64 corner warps' 1/den
     offs[s].sx = L.take((1 + KT_N) * sizeof(T) * (h.nx + 2));  // sigma, its tables
     offs[s].ty = L.take((1 + KT_N) * sizeof(T) * (MY + 2));    // tau, its tables
     offs[s].srcv = L.take(sizeof(T) * std::max<int64_t>(h.nstep * h.nsrc, 1));
@@ -2472,6 +2578,7 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
     d.lp = (T*)(pool + offs[s].lp);
     d.lq = (T*)(pool + offs[s].lq);
     d.c = (T*)(pool + offs[s].c);
+    d.rdt = sizeof(T) == 8 ? (T*)(pool + offs[s].rdt) : nullptr;
     d.sx = (T*)(pool + offs[s].sx);
     d.ty = (T*)(pool + offs[s].ty);
     d.sxk = d.sx + (h.nx + 2);
@@ -2519,6 +2626,10 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   }
   ADS_CUDA(cudaMemcpyAsync(d_shots, hshots.data(), sizeof(AcShot<T>) * ns,
                            cudaMemcpyHostToDevice, st));
+  if constexpr (sizeof(T) == 8) {
+    k_ac_rden<T><<<dim3(kRowBlocks, ns), 256, 0, st>>>(d_shots, c.dt / 2);
+    ADS_LAUNCHED(1);
+  }
   if (int e = upload_tiles(tiles_a, ta, st)) return e;
   if (int e = upload_tiles(tiles_f, tf, st)) return e;
   if (!shot_rcvs.empty())
