@@ -2393,9 +2393,12 @@ int AcPlan<T>::create(const ads_acoustic_config& c, const ads_acoustic_shot* sho
   // for several resident waves
   if (c.rows_per_thread <= 0) {
     ri_f = 8;
-    while (ri_f > 2 && cells / ((int64_t)ri_f * Tile<T>::WF) < 152 * 64) ri_f /= 2;
+    // FP64 items go down to one row per warp: on small grids a warp's serial
+    // chain of FP64 operations, not the item count, sets a step's duration
+    const int rmin = sizeof(T) == 8 ? 1 : 2;
+    while (ri_f > rmin && cells / ((int64_t)ri_f * Tile<T>::WF) < 152 * 64) ri_f /= 2;
     ri = 16;
-    while (ri > 2 && cells / ((int64_t)ri * Tile<T>::WA) < 152 * 32) ri /= 2;
+    while (ri > rmin && cells / ((int64_t)ri * Tile<T>::WA) < 152 * 32) ri /= 2;
   } else {
     ri_f = ri;
   }
@@ -3136,7 +3139,7 @@ int AcPlan<T>::launch_adj(cudaStream_t st, int na, int k, int base) {
 // touch are reset by every forward / gradient call.
 template <typename T>
 int AcPlan<T>::autotune(cudaStream_t st, int64_t pitch, size_t cap) {
-  const int cand[] = {2, 4, 8, 16, 32, 64};
+  const int cand[] = {1, 2, 4, 8, 16, 32, 64};
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   ADS_CUDA(cudaEventCreate(&e0));
   ADS_CUDA(cudaEventCreate(&e1));
