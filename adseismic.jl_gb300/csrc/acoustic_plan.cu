@@ -64,7 +64,7 @@ constexpr unsigned FULL = 0xffffffffu;
 template <typename T>
 struct Tile {
   static constexpr int J = sizeof(T) == 4 ? 512 : 256;
-  static constexpr int CF = sizeof(T) == 4 ? 2 : 2;
+  static constexpr int CF = sizeof(T) == 4 ? 2 : 1;
   static constexpr int CA = sizeof(T) == 4 ? 2 : 1;
   // rows of register prefetch in the interior loops (bytes in flight per warp)
   static constexpr int PF = sizeof(T) == 4 ? ADS_PF32 : 1;
