@@ -3047,45 +3047,56 @@ int AcPlan<T>::launch_fwd(cudaStream_t st, int mode, int na, int t, int base, in
     else if (IN || ck > 0) ADS_FWD(0, IN, VUF, true, items_, n_, s_, rows_); \
     else ADS_FWD(0, IN, VUF, false, items_, n_, s_, rows_);                \
   } while (0)
-  if (ni > 0) {
-    if constexpr (sizeof(T) == 4) {
-      if (tma_ok && inc) {
-        const int gh = Tile<T>::G * ri_f;
-        if (mode == 1)
-          k_ac_fwd_tma<1, false><<<ni, TPB, TMA_SMEM, st>>>(tf.items, d_shots, d_maps, kc, t,
-                                                            base, ck, gh, d_err);
-        else if (mode == 2)
-          k_ac_fwd_tma<2, false><<<ni, TPB, TMA_SMEM, st>>>(tf.items, d_shots, d_maps, kc, t,
-                                                            base, ck, gh, d_err);
-        else if (ck > 0)
-          k_ac_fwd_tma<0, true><<<ni, TPB, TMA_SMEM, st>>>(tf.items, d_shots, d_maps, kc, t,
-                                                           base, ck, gh, d_err);
-        else
-          k_ac_fwd_tma<0, false><<<ni, TPB, TMA_SMEM, st>>>(tf.items, d_shots, d_maps, kc, t,
-                                                            base, ck, gh, d_err);
+  auto run_in = [&]() -> int {
+    if (ni > 0) {
+      if constexpr (sizeof(T) == 4) {
+        if (tma_ok && inc) {
+          const int gh = Tile<T>::G * ri_f;
+          if (mode == 1)
+            k_ac_fwd_tma<1, false><<<ni, TPB, TMA_SMEM, st>>>(tf.items, d_shots, d_maps, kc, t,
+                                                              base, ck, gh, d_err);
+          else if (mode == 2)
+            k_ac_fwd_tma<2, false><<<ni, TPB, TMA_SMEM, st>>>(tf.items, d_shots, d_maps, kc, t,
+                                                              base, ck, gh, d_err);
+          else if (ck > 0)
+            k_ac_fwd_tma<0, true><<<ni, TPB, TMA_SMEM, st>>>(tf.items, d_shots, d_maps, kc, t,
+                                                             base, ck, gh, d_err);
+          else
+            k_ac_fwd_tma<0, false><<<ni, TPB, TMA_SMEM, st>>>(tf.items, d_shots, d_maps, kc, t,
+                                                              base, ck, gh, d_err);
+        } else {
+          ADS_FWD_MODE(true, false, tf.items, ni, st, ri_f);
+        }
       } else {
         ADS_FWD_MODE(true, false, tf.items, ni, st, ri_f);
       }
-    } else {
-      ADS_FWD_MODE(true, false, tf.items, ni, st, ri_f);
-    }
-    ADS_LAUNCHED(1);
-  }
-  if (np > 0) {
-    const int rows = ri_pf > 0 ? ri_pf : ri_f;
-    if (vu) {
-      // phi_{t-1}, psi_{t-1} from u_{t-1}, then the step reads them
-      if (mode == 0)
-        k_ac_phi_u<T, 0><<<np, TPB, 0, sp>>>(pm, d_shots, tf.srcs, kc, t, base, rows);
-      else
-        k_ac_phi_u<T, 1><<<np, TPB, 0, sp>>>(pm, d_shots, tf.srcs, kc, t, base, rows);
       ADS_LAUNCHED(1);
-      ADS_FWD_MODE(false, true, pm, np, sp, rows);
-    } else {
-      ADS_FWD_MODE(false, false, pm, np, sp, rows);
     }
-    ADS_LAUNCHED(1);
-  }
+    return ADS_OK;
+  };
+  auto run_pm = [&]() -> int {
+    if (np > 0) {
+      const int rows = ri_pf > 0 ? ri_pf : ri_f;
+      if (vu) {
+        // phi_{t-1}, psi_{t-1} from u_{t-1}, then the step reads them
+        if (mode == 0)
+          k_ac_phi_u<T, 0><<<np, TPB, 0, sp>>>(pm, d_shots, tf.srcs, kc, t, base, rows);
+        else
+          k_ac_phi_u<T, 1><<<np, TPB, 0, sp>>>(pm, d_shots, tf.srcs, kc, t, base, rows);
+        ADS_LAUNCHED(1);
+        ADS_FWD_MODE(false, true, pm, np, sp, rows);
+      } else {
+        ADS_FWD_MODE(false, false, pm, np, sp, rows);
+      }
+      ADS_LAUNCHED(1);
+    }
+    return ADS_OK;
+  };
+  // the PML launch first: the launches of a fork start roughly in the order
+  // they are issued, and its items are the heavier (FP64 C2: 36.7 against
+  // 35.7 shot-gradients/s; FP32 C3 unchanged)
+  if (int e = run_pm()) return e;
+  if (int e = run_in()) return e;
 #undef ADS_FWD_MODE
 #undef ADS_FWD
 #undef ADS_FWD_
@@ -3107,25 +3118,33 @@ int AcPlan<T>::launch_adj(cudaStream_t st, int na, int k, int base) {
     ADS_CUDA(cudaStreamWaitEvent(side, ev_fork, 0));
     sp = side;
   }
-  if (ni > 0) {
-    k_ac_adj<T, true><<<ni, TPB, 0, st>>>(ta.items, d_shots, ta.srcs, ta.rcvs, kc, k, base, ri,
-                                          dt2d);
-    ADS_LAUNCHED(1);
-  }
-  if (np > 0) {
-    const int rows = ri_pa > 0 ? ri_pa : ri;
-    if (vu) {
-      // lambdaPhi_{k-1}, lambdaPsi_{k-1} first, then the step's transpose
-      k_ac_adjphi_u<T><<<np, TPB, 0, sp>>>(ta.items + ta.pm_off, d_shots, kc, k, rows);
+  auto run_in = [&]() -> int {
+    if (ni > 0) {
+      k_ac_adj<T, true><<<ni, TPB, 0, st>>>(ta.items, d_shots, ta.srcs, ta.rcvs, kc, k, base, ri,
+                                            dt2d);
       ADS_LAUNCHED(1);
-      k_ac_adj<T, false, true><<<np, TPB, 0, sp>>>(ta.items + ta.pm_off, d_shots, ta.srcs,
-                                                   ta.rcvs, kc, k, base, rows, dt2d);
-    } else {
-      k_ac_adj<T, false><<<np, TPB, 0, sp>>>(ta.items + ta.pm_off, d_shots, ta.srcs, ta.rcvs,
-                                             kc, k, base, rows, dt2d);
     }
-    ADS_LAUNCHED(1);
-  }
+    return ADS_OK;
+  };
+  auto run_pm = [&]() -> int {
+    if (np > 0) {
+      const int rows = ri_pa > 0 ? ri_pa : ri;
+      if (vu) {
+        // lambdaPhi_{k-1}, lambdaPsi_{k-1} first, then the step's transpose
+        k_ac_adjphi_u<T><<<np, TPB, 0, sp>>>(ta.items + ta.pm_off, d_shots, kc, k, rows);
+        ADS_LAUNCHED(1);
+        k_ac_adj<T, false, true><<<np, TPB, 0, sp>>>(ta.items + ta.pm_off, d_shots, ta.srcs,
+                                                     ta.rcvs, kc, k, base, rows, dt2d);
+      } else {
+        k_ac_adj<T, false><<<np, TPB, 0, sp>>>(ta.items + ta.pm_off, d_shots, ta.srcs, ta.rcvs,
+                                               kc, k, base, rows, dt2d);
+      }
+      ADS_LAUNCHED(1);
+    }
+    return ADS_OK;
+  };
+  if (int e = run_pm()) return e;  // the PML launch first, as in launch_fwd
+  if (int e = run_in()) return e;
   if (fork) {
     ADS_CUDA(cudaEventRecord(ev_join, side));
     ADS_CUDA(cudaStreamWaitEvent(st, ev_join, 0));

@@ -2960,8 +2960,11 @@ int ElPlan<T>::group(cudaStream_t st, bool split, int n_in, int n_pm, F&& fn) {
 template <typename T>
 template <typename F>
 int ElPlan<T>::kinds(cudaStream_t st, const int* nk, F&& fn) {
+  // The CPML kinds first: their few items carry the longest chains, and the
+  // launches of a fork start roughly in the order they are issued (measured
+  // on the C4 gradient: 20.1 shot-gradients/s against 17.4 with kind 0 first)
   int kd[4], n = 0;
-  for (int k = 0; k < 4; k++)
+  for (int k = 3; k >= 0; k--)
     if (nk[k] > 0) kd[n++] = k;
   if (n > 1) {
     ADS_CUDA(cudaEventRecord(ev_fork, st));
