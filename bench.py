@@ -379,12 +379,22 @@ def elastic_measure(steps, warmup, nshots=32, T=4000, with_rel_err=True, autotun
     kern.update({k: {"ms_per_launch": round(v[0], 4)} for k, v in prof.items()})
     dom = adj_name
     tt, b = groups[dom]
+    # the whole gradient: algorithmic bytes of all its steps over its measured
+    # time (forward steps without / with stores, the recompute, the adjoint)
+    K, res = ckpt_every, plan.resident_segments
+    nseg = -(-p.NSTEP // K)
+    cps = n * p.NX * p.NY
+    n_store = min(res * K, p.NSTEP) + max(nseg - res, 0) * K
+    job_b = cps * (b_fwd * max(p.NSTEP - res * K, 0) + (b_fwd + 20) * n_store + b_adj * p.NSTEP)
+    job = {"bytes": job_b, "achieved_gbs": round(job_b / (ms / 1e3) / 1e9, 1),
+           "frac": round(job_b / (ms / 1e3) / 1e9 / peak, 4),
+           "steps": {"forward": p.NSTEP, "storing": n_store, "adjoint": p.NSTEP}}
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(b / (tt / 1e3) / 1e9, 1),
                 "peak": peak, "unit": "GB/s", "frac": round(b / (tt / 1e3) / 1e9 / peak, 4),
                 "peak_source": peak_kind, "traffic": None, "bytes_per_launch": b,
                 "bytes_per_cell": {"forward": round(b_fwd, 2), "forward_storing": round(b_fwd + 20, 2),
                                    "adjoint": round(b_adj, 2), "f_pml": round(f_pml, 4)},
-                "kernels": kern}
+                "kernels": kern, "gradient": job}
     out = {"value": n / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": steps,
            "warmup": warmup, "dtype": "f32",
            "workload": f"elastic CPML gradient {p.NX}x{p.NY} (CPML {p.NPOINTS_PML}), "
@@ -651,6 +661,15 @@ def main():
                                 "launches_per_step": round(v["launches_per_step"], 2),
                                 "share_of_step": round(v["total_ms"] / ms, 3)}
                             for k, v in kern.items()}}
+    # the whole gradient: algorithmic bytes of its forward, recompute and
+    # adjoint cell-updates over its measured time
+    rc_cu = rc_cells * max(nseg - plan.resident_segments, 0)
+    job_b = (BYTES[("fwd", "f32")] * (cell_steps / world + rc_cu) +
+             BYTES[("adj", "f32")] * cell_steps / world)
+    roofline["gradient"] = {"bytes": job_b, "achieved_gbs": round(job_b / (ms / 1e3) / 1e9, 1),
+                            "frac": round(job_b / (ms / 1e3) / 1e9 / peak, 4),
+                            "cell_updates": {"forward": cell_steps // world, "recompute": rc_cu,
+                                             "adjoint": cell_steps // world}}
 
     # e2e through the C ABI with host buffers (pinned), copies inside the timed region
     vp_host = torch.tensor(vp0).pin_memory()
