@@ -480,14 +480,14 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
     }
     if constexpr (!INT) record_traces<T, C, NOREC>(it, sh, rcvs, out, t, lane, i0, i_end);
   } else {
-  // The general (PML) form.  FP64 plans of variant W specialise it by the
-  // warp's kind (uniform over the warp): PK = 1 where tau = 0 at every column
+  // The general (PML) form.  FP64 plans specialise it by the warp's kind
+  // (uniform over the warp): PK = 1 where tau = 0 at every column
   // the warp reads (sigma rows only: the damping factors come per row from the
   // shot's tables), PK = 2 where sigma = 0 on every row it updates (tau columns
   // only: the factors are per-thread constants), PK = 3 elsewhere (the
   // corners: the sigma factors per row, the tau products per cell and
   // 1 / (1 + s dt/2) from the shot's per-cell table).  PK = 0, the general form
-  // with its divide, serves FP32 and variant-U plans.  The specialised forms
+  // with its divide, serves FP32 plans.  The specialised forms
   // drop terms that are exact zeros there and multiply by the tabulated
   // reciprocal instead of dividing (within an ulp of the divide; with
   // r = 1 / (1 + s dt/2), (1 - s dt/2) r = 2 r - 1).  FP64 plans are bound by
@@ -660,7 +660,7 @@ k_ac_fwd(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       if constexpr (PK == 3) rd0 = rdn;
     }
   };
-  constexpr bool SPEC = sizeof(T) == 8 && !VU && !INC;
+  constexpr bool SPEC = sizeof(T) == 8 && !INC;
   bool sfree = false;
   if constexpr (SPEC) {
     bool z = true;
@@ -1233,13 +1233,14 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       record_src_grad<T, C, VU>(it, sh, srcs, lun, lpc, lqc, K, k, lane, i0, i_end, dt2);
     }
   } else {
-  // The general (PML) form.  FP64 plans of variant W specialise it by the
-  // warp's kind, as k_ac_fwd does: PK = 1 where tau = 0 at every column the
+  // The general (PML) form.  FP64 plans specialise it by the warp's kind, as
+  // k_ac_fwd does: PK = 1 where tau = 0 at every column the
   // warp reads (1/den and the sigma terms per row from the damping tables),
   // PK = 2 where sigma = 0 on rows i0-1 .. i_end (1/den and the tau terms
   // per-thread constants), PK = 3 elsewhere (1/den from the per-cell table,
-  // the sigma terms per row); PK = 0 (general, with divides) for FP32 and
-  // variant-U plans.
+  // the sigma terms per row); PK = 0 (general, with divides) for FP32 plans.
+  // Variant U uses the same forms (its phi / psi terms read the pre-pass's
+  // values; it writes no lambdaPhi / lambdaPsi).
   auto pml_rows = [&](auto kd) {
     constexpr int PK = decltype(kd)::value;
     const int nr = nx + 2, ncol = ny + 2;
@@ -1476,7 +1477,7 @@ k_ac_adj(const AcItem* __restrict__ items, const AcShot<T>* __restrict__ shots,
       }
     }
   };
-  constexpr bool SPEC = sizeof(T) == 8 && !VU;
+  constexpr bool SPEC = sizeof(T) == 8;
   bool sfree = false;
   if constexpr (SPEC) {
     bool z = true;
