@@ -265,7 +265,10 @@ typedef struct ads_acoustic_config {
                          the same update in exact arithmetic, whose FP32 rounding
                          does not build up over thousands of steps); with
                          steps_per_block > 1 they keep the three-level form */
-  int32_t variant;    /* ADS_VARIANT_W (only form with a whole-path adjoint) */
+  int32_t variant;    /* ADS_VARIANT_W (phi/psi from the old field, the custom
+                         operators' form) or ADS_VARIANT_U (from the new field,
+                         one_step, the reference's default PropagatorKernel = 0);
+                         both with the whole-path adjoint */
   int32_t use_graph;  /* 1: capture the time loops in CUDA graphs (default) */
   int64_t ckpt_every; /* forward checkpoint spacing k in steps; 0 = automatic */
   int32_t rows_per_thread; /* stencil tile height (autotuner); 0 = automatic */
