@@ -92,6 +92,10 @@ def test_null_arguments_are_rejected_before_any_device_call(ads):
     assert L.ads_acoustic_plan_source_offset(None, 0) == -1
     assert L.ads_elastic_plan_source_offset(None, 0) == -1
     assert L.ads_elastic_plan_resident_segments(None) == -1
+    assert all(L.ads_acoustic_plan_rows(None, w) == -1 for w in range(4))
+    assert all(L.ads_elastic_plan_rows(None, w) == -1 for w in range(2, 6))
+    assert L.ads_acoustic_plan_tma(None) == -1
+    assert L.ads_acoustic_plan_steps_per_block(None) == -1
 
 
 def test_compute_calls_fail_loudly_without_gpu(ads):
